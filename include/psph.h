@@ -1,0 +1,194 @@
+/*
+ * persiansph-gb300 C ABI: the drop-in boundary for PersianSPH's per-step hot
+ * path on one GB300 (sm_103a).
+ *
+ * The reference runs its hot path as methods of SPH::Domain called from
+ * Domain::Solve (Source/Domain.cpp:1735-1797). This ABI replaces the body of
+ * that loop (Source/Domain.cpp:1764-1792) and the set-up it relies on
+ * (Source/Domain.cpp:1746-1751): a host wrapper keeps the Domain / Particle
+ * API, packs the particles once into the structures below, and drives the
+ * device through these calls. Plain C types only; no CUDA or torch types cross
+ * the boundary (streams travel as void*).
+ *
+ * Conventions
+ *  - Every call returns psph_status (0 = success). psph_last_error() gives the
+ *    message; the C++ wrapper turns a non-zero status into the reference's
+ *    `throw new Fatal(...)` (External/fatal.h:65).
+ *  - Per-particle arrays are host arrays indexed by the particle's position in
+ *    Domain::Particles at upload time ("original index"). Vectors are
+ *    interleaved [3*i+d]; 3x3 tensors row-major [9*i+3*r+c].
+ *  - One context = one Domain = one CUDA stream; calls on a context must come
+ *    from one host thread at a time (the reference's Domain is not re-entrant
+ *    either, Source/Domain.h:125).
+ */
+#ifndef PSPH_H
+#define PSPH_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PSPH_ABI_VERSION 1
+
+typedef enum psph_status {
+  PSPH_OK = 0,
+  PSPH_ERR_INVALID_ARGUMENT = 1, /* bad enum/size/pointer; reference aborts or throws Fatal */
+  PSPH_ERR_UNSUPPORTED = 2,      /* valid reference option outside this build (FSI, seepage, in/out-flow) */
+  PSPH_ERR_CUDA = 3,             /* a CUDA runtime call failed */
+  PSPH_ERR_OUT_OF_MEMORY = 4,
+  PSPH_ERR_NONFINITE = 5,        /* NaN/Inf found in an acceleration or density rate */
+  PSPH_ERR_DT_COLLAPSE = 6,      /* "Too small time step" (Source/Domain.cpp:150-151) */
+  PSPH_ERR_CFL = 7,              /* user dt above the CFL limit (Source/Domain.cpp:1731-1732) */
+  PSPH_ERR_CELL_OVERFLOW = 8,    /* a cell holds more particles than the kernels stage */
+  PSPH_ERR_NO_DEVICE = 9,        /* no CUDA device or not an sm_103 part */
+  PSPH_ERR_STATE = 10,           /* call out of order (e.g. step before upload) */
+  PSPH_ERR_NOT_FOUND = 11        /* DelParticles found no particle with the tag (Source/Domain.cpp:511) */
+} psph_status;
+
+/* Kernel_Set / Viscosity_Eq_Set / Gradient_Approach_Set (Source/Domain.h:38-40). */
+enum { PSPH_QUBIC_SPLINE = 0, PSPH_QUINTIC = 1, PSPH_QUINTIC_SPLINE = 2 };
+enum { PSPH_MORRIS = 0, PSPH_SHAO = 1, PSPH_INCOMPRESSIBLE_FULL = 2, PSPH_TAKEDA = 3 };
+enum { PSPH_SQUARED_DENSITY = 0, PSPH_MULTIPLIED_DENSITY = 1 };
+/* Domain::Scheme (Source/Domain.h:136). */
+enum { PSPH_MVERLET = 0, PSPH_LEAPFROG = 1 };
+/* Arithmetic form of the pair kernels. */
+enum { PSPH_FP64 = 0, PSPH_FP32C = 1 };
+/* Wall-pressure orientation (Source/Domain.cpp:1034-1053). REFERENCE reproduces
+ * the reference's sign of the g.x_ij term, which depends on which particle its
+ * neighbour search lists first; PHYSICAL always uses x_wall - x_fluid. */
+enum { PSPH_WALLP_REFERENCE = 0, PSPH_WALLP_PHYSICAL = 1 };
+
+/* Domain-level settings (public fields of SPH::Domain, Source/Domain.h:93-145). */
+typedef struct psph_config {
+  int32_t dimension;          /* Domain::Dimension: 2 or 3 */
+  int32_t kernel_type;        /* PSPH_QUBIC_SPLINE ... */
+  int32_t vis_eq;             /* PSPH_MORRIS ... */
+  int32_t gradient_type;      /* PSPH_SQUARED_DENSITY ... */
+  int32_t scheme;             /* PSPH_MVERLET or PSPH_LEAPFROG */
+  int32_t periodic[3];        /* Domain::BC.Periodic */
+  int32_t swi_type;           /* Domain::SWIType; only 0 (no seepage) is in this build */
+  int32_t shepard_step;       /* Particle::ShepardStep, uniform over particles (default 40) */
+  int32_t precision;          /* PSPH_FP64 or PSPH_FP32C */
+  int32_t wall_pressure_mode; /* PSPH_WALLP_REFERENCE or PSPH_WALLP_PHYSICAL */
+  double gravity[3];          /* Domain::Gravity */
+  double body_force[3];       /* constant acceleration added to free particles where the
+                                 GeneralBefore hook runs (the 1-Poiseuille.cpp UserAcc pattern) */
+  double xsph;                /* Domain::XSPH */
+  double sqrt_h_a;            /* Domain::sqrt_h_a (default 0.0025) */
+  double R;                   /* Domain::R: lattice half-spacing, pads periodic domains */
+  double dom_max[3];          /* Domain::DomMax (default -1e11: no override) */
+  double dom_min[3];          /* Domain::DomMin (default +1e11: no override) */
+  double dt;                  /* Solve's dt argument: initial and maximum time step */
+  double time;                /* Domain::Time at upload */
+  int32_t reserved[8];        /* must be zero */
+} psph_config;
+
+/* Cell grid made by CellInitiate (Source/Domain.cpp:549-660). */
+typedef struct psph_grid {
+  double blpf[3];      /* Domain::BLPF, bottom-left-front corner after padding */
+  double trpr[3];      /* Domain::TRPR */
+  double cell_size[3]; /* Domain::CellSize */
+  double dom_size[3];  /* Domain::DomSize (non-zero on periodic axes) */
+  double hmax;         /* Domain::hmax */
+  double rhomax;       /* Domain::rhomax */
+  double cellfac;      /* Domain::Cellfac: 3 for the quintic spline, else 2 */
+  int32_t cell_no[3];  /* Domain::CellNo, including the 2 ghost columns of a periodic axis */
+  int32_t pad;
+} psph_grid;
+
+/* Time-integration state. The reference keeps FirstStep/ct/ShepardCounter per
+ * particle, but every free particle advances them identically each step
+ * (Source/Particle.cpp:189-274, :561-596), so they are held once per domain. */
+typedef struct psph_integrator {
+  double time;              /* Domain::Time */
+  double deltat;            /* Domain::deltat */
+  double deltatint;         /* Domain::deltatint (user dt) */
+  double deltatmin;         /* Domain::deltatmin of the last step */
+  int64_t steps;            /* steps taken since upload */
+  int32_t first_step;       /* Particle::FirstStep */
+  int32_t ct;               /* Particle::ct (Modified Verlet restart counter) */
+  int32_t shepard_counter;  /* Particle::ShepardCounter */
+  int32_t pad;
+} psph_integrator;
+
+/* Host view of the particles (SPH::Particle fields, Source/Particle.h:29-149).
+ * Any pointer may be NULL: on upload the Particle-constructor default is used
+ * (Source/Particle.cpp:25-117); on download the field is skipped. */
+typedef struct psph_particles {
+  int64_t n;
+  /* int32 per particle */
+  int32_t *id, *material, *is_free, *no_slip, *pres_eq, *shepard, *les, *vis_m, *fail;
+  /* 3-vectors */
+  double *x, *v, *va, *vb, *a, *nsv, *vxsph;
+  /* scalars */
+  double *density, *densitya, *densityb, *ddensity, *pressure, *mass, *h, *cs, *p0, *ref_density,
+      *fpmassc, *alpha, *beta, *mu, *mu_ref, *t0, *bingham_m, *csmag, *ti, *tin, *ti_init_dist, *g_mod,
+      *k_mod, *sigmay, *cohesion, *phi, *psi, *zwab, *sumden, *sumkernel, *shear_rate, *sbar;
+  /* 3x3 tensors */
+  double *sigma, *sigmaa, *sigmab, *shear_stress, *shear_stressa, *shear_stressb, *strain, *straina,
+      *strainb, *strain_rate, *rotation_rate, *tir;
+} psph_particles;
+
+typedef struct psph_ctx psph_ctx;
+
+/* Library / device probe. Returns PSPH_OK when an sm_103 device is usable. */
+int psph_abi_version(void);
+psph_status psph_device_check(int* device_count);
+
+/* Domain construction: validates cfg (Domain ctor + selectors, Source/Domain.cpp:54-131). */
+psph_status psph_create(const psph_config* cfg, psph_ctx** out);
+void psph_destroy(psph_ctx* ctx);
+const char* psph_last_error(const psph_ctx* ctx);
+/* cudaStream_t to run on (NULL = the context's own stream). */
+psph_status psph_set_stream(psph_ctx* ctx, void* cuda_stream);
+
+/* Optional, before upload: continue with a saved grid / integrator state
+ * instead of Solve's set-up. */
+psph_status psph_set_grid(psph_ctx* ctx, const psph_grid* grid);
+psph_status psph_set_integrator(psph_ctx* ctx, const psph_integrator* integ);
+
+/* Copies particles to the device. With initial != 0 it also performs Solve's
+ * set-up: InitialChecks (initial EOS pressure, Source/Domain.cpp:1662-1719),
+ * CellInitiate (unless psph_set_grid was called) and TimestepCheck
+ * (Source/Domain.cpp:1721-1733; returns PSPH_ERR_CFL like the reference throws). */
+psph_status psph_upload(psph_ctx* ctx, const psph_particles* p, int initial);
+
+/* Runs up to nsteps steps of Solve's loop body (Source/Domain.cpp:1764-1792),
+ * stopping before a step when Domain::Time >= t_stop (Solve's `Time<tf` test).
+ * *steps_done (may be NULL) receives the number of steps taken. */
+psph_status psph_step(psph_ctx* ctx, int64_t nsteps, double t_stop, int64_t* steps_done);
+
+/* Particles currently alive (CheckParticleLeave removes those leaving the grid). */
+int64_t psph_num_particles(const psph_ctx* ctx);
+
+/* Copies the current state into every non-NULL array of out (out->n must be at
+ * least psph_num_particles). Particles come back in their original order with
+ * deleted ones removed, as Array::DelItems leaves them (External/array.h:726). */
+psph_status psph_download(psph_ctx* ctx, psph_particles* out);
+
+psph_status psph_get_grid(const psph_ctx* ctx, psph_grid* grid);
+psph_status psph_get_integrator(const psph_ctx* ctx, psph_integrator* integ);
+
+/* Neighbour pairs of the current positions, as original indices, written as
+ * (first, second) int64 couples in the orientation MainNeighbourSearch would
+ * list them (Source/Domain.cpp:808-945). which = 0: every candidate pair
+ * (SMPairs + FSMPairs + NSMPairs); which = 1: only pairs inside the kernel
+ * support (r/h_ij <= Cellfac), the set CalcForce* works on. At most cap pairs
+ * are written; *n_total receives the full count. */
+psph_status psph_pairs_export(psph_ctx* ctx, int which, int64_t* pairs, int64_t cap, int64_t* n_total);
+
+/* Device time of each phase of the last psph_step call, in ms: [0] cell sort +
+ * reorder, [1] wall interpolation, [2] pair forces, [3] dt reduction, [4]
+ * update; n_phases receives 5. Timing is recorded only when enabled. */
+psph_status psph_enable_timing(psph_ctx* ctx, int enable);
+psph_status psph_phase_times(const psph_ctx* ctx, double* ms, int cap, int* n_phases);
+/* Number of kernel launches the last psph_step issued. */
+int64_t psph_last_launch_count(const psph_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PSPH_H */

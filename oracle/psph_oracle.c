@@ -1,0 +1,1591 @@
+/*
+ * CPU restatement of PersianSPH's per-step hot path: the parity ORACLE.
+ * TEST INFRASTRUCTURE ONLY (see psph_oracle.h): never linked into the product.
+ *
+ * Each function restates one reference routine and cites it. Arithmetic is
+ * written in the reference's own expression order (the blitz / matvec.h
+ * element-wise operators evaluate per element in source order), so with
+ * -ffp-contract=off the restatement reproduces the reference build bit for bit
+ * on the same libm; the committed golden fixtures pin it.
+ *
+ * Differences from the reference, all outside its defined behaviour:
+ *  - The acceleration dt minimum uses a proper reduction. The reference
+ *    tests outside its lock (Source/Domain.cpp:1289-1294), which with Nproc>1
+ *    can keep a larger value; with Nproc=1 both are the plain minimum.
+ *  - A particle more than hmax outside the grid makes ListGenerate index out of
+ *    bounds in the reference (Source/Domain.cpp:669-691); here it is an error.
+ *  - Interactions outside this build (NSMPairs: fluid-soil seepage, FSI) are
+ *    reported as PSPH_ERR_UNSUPPORTED instead of being computed.
+ */
+#include "psph_oracle.h"
+
+#include <math.h>
+#include <omp.h>
+#include <stdarg.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#include "state_io.h"
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+typedef struct {
+  int64_t* v; /* (first, second) couples */
+  int64_t n, cap;
+} pairvec;
+
+struct psph_oracle {
+  psph_config cfg;
+  psph_grid g;
+  psph_integrator it;
+  double I[9]; /* Domain::I: identity, I(2,2)=0 in 2D (Source/Domain.cpp:1665) */
+  int64_t n;
+#define DECL_I(NAME) int32_t* NAME;
+#define DECL_D(NAME) double* NAME;
+  PSPH_INT_FIELDS(DECL_I)
+  PSPH_F64_FIELDS(DECL_D)
+  PSPH_VEC_FIELDS(DECL_D)
+  PSPH_TEN_FIELDS(DECL_D)
+  int64_t* orig;
+  int32_t* LL; /* Particle::LL */
+  int32_t* CC; /* Particle::CC[3] */
+  int32_t* HOC;
+  int64_t ncells;
+  int nthr;
+  pairvec *sm, *fsm, *nsm;
+  int64_t* fixed;
+  int64_t nfixed;
+  omp_lock_t* locks;
+  double *a_scale, *dr_scale;
+  double mu_max, cs_max; /* Domain::MuMax / CsMax from CellInitiate */
+  double phase_s[5];
+  int status;
+  char err[512];
+};
+
+static int fail(psph_oracle* o, int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(o->err, sizeof o->err, fmt, ap);
+  va_end(ap);
+  o->status = code;
+  return code;
+}
+
+static double now_s(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
+static void pv_push(pairvec* p, int64_t a, int64_t b) {
+  if (p->n + 1 > p->cap) {
+    p->cap = p->cap ? 2 * p->cap : 1024;
+    p->v = (int64_t*)realloc(p->v, (size_t)p->cap * 2 * sizeof(int64_t));
+  }
+  p->v[2 * p->n] = a;
+  p->v[2 * p->n + 1] = b;
+  p->n++;
+}
+
+/* ---------------------------------------------------------------------------
+ * SPH functions (Source/Functions.cpp)
+ * ------------------------------------------------------------------------- */
+
+/* Kernel (Functions.cpp:25-63) */
+static double Kernel(int Dim, int KT, double q, double h) {
+  double C;
+  switch (KT) {
+    case 0:
+      C = (Dim == 2) ? 10.0 / (7.0 * h * h * M_PI) : 1.0 / (h * h * h * M_PI);
+      if (q < 1.0) return C * (1.0 - (3.0 / 2.0) * q * q + (3.0 / 4.0) * q * q * q);
+      else if (q < 2.0) return C * ((1.0 / 4.0) * (2.0 - q) * (2.0 - q) * (2.0 - q));
+      else return 0.0;
+    case 1:
+      C = (Dim == 2) ? 7.0 / (4.0 * h * h * M_PI) : 7.0 / (8.0 * h * h * h * M_PI);
+      if (q < 2.0) return C * pow((1.0 - q / 2.0), 4.0) * (2.0 * q + 1.0);
+      else return 0.0;
+    default:
+      C = (Dim == 2) ? 7.0 / (478.0 * h * h * M_PI) : 1.0 / (120.0 * h * h * h * M_PI);
+      if (q < 1.0) return C * (pow((3.0 - q), 5.0) - 6.0 * pow((2.0 - q), 5.0) + 15.0 * pow((1.0 - q), 5.0));
+      else if (q < 2.0) return C * (pow((3.0 - q), 5.0) - 6.0 * pow((2.0 - q), 5.0));
+      else if (q < 3.0) return C * (pow((3.0 - q), 5.0));
+      else return 0.0;
+  }
+}
+
+/* GradKernel (Functions.cpp:65-106): (1/r) dW/dr */
+static double GradKernel(int Dim, int KT, double q, double h) {
+  double C;
+  switch (KT) {
+    case 0:
+      C = (Dim == 2) ? 10.0 / (7.0 * h * h * h * M_PI) : 1.0 / (h * h * h * h * M_PI);
+      if (q == 0.0) return C / h * (-3.0 + (9.0 / 2.0) * q);
+      else if (q < 1.0) return C / (q * h) * (-3.0 * q + (9.0 / 4.0) * q * q);
+      else if (q < 2.0) return C / (q * h) * ((-3.0 / 4.0) * (2.0 - q) * (2.0 - q));
+      else return 0.0;
+    case 1:
+      C = (Dim == 2) ? 7.0 / (4.0 * h * h * h * M_PI) : 7.0 / (8.0 * h * h * h * h * M_PI);
+      if (q == 0.0) return C * -5.0 / h * (pow((1.0 - q / 2.0), 3.0) - 3.0 * q / 2.0 * pow((1.0 - q / 2.0), 2.0));
+      else if (q < 2.0) return C / (q * h) * -5.0 * q * pow((1.0 - q / 2.0), 3.0);
+      else return 0.0;
+    default:
+      C = (Dim == 2) ? 7.0 / (478.0 * h * h * h * M_PI) : 1.0 / (120.0 * h * h * h * h * M_PI);
+      if (q == 0.0)
+        return C / h * (20.0 * pow((3.0 - q), 3.0) - 120.0 * pow((2.0 - q), 3.0) + 300.0 * pow((1.0 - q), 3.0));
+      else if (q < 1.0)
+        return C / (q * h) * (-5.0 * pow((3.0 - q), 4.0) + 30.0 * pow((2.0 - q), 4.0) - 75.0 * pow((1.0 - q), 4.0));
+      else if (q < 2.0) return C / (q * h) * (-5.0 * pow((3.0 - q), 4.0) + 30.0 * pow((2.0 - q), 4.0));
+      else if (q < 3.0) return C / (q * h) * (-5.0 * pow((3.0 - q), 4.0));
+      else return 0.0;
+  }
+}
+
+/* LaplaceKernel (Functions.cpp:108-146) */
+static double LaplaceKernel(int Dim, int KT, double q, double h) {
+  double C;
+  switch (KT) {
+    case 0:
+      C = (Dim == 2) ? 10.0 / (7.0 * h * h * h * h * M_PI) : 1.0 / (h * h * h * h * h * M_PI);
+      if (q < 1.0) return C * (-3.0 + (9.0 / 2.0) * q) + C * (Dim - 1.0) / q * (-3.0 * q + (9.0 / 4.0) * q * q);
+      else if (q < 2.0)
+        return C * ((3.0 / 2.0) * (2.0 - q)) + C * (Dim - 1.0) / q * ((-3.0 / 4.0) * (2.0 - q) * (2.0 - q));
+      else return 0.0;
+    case 1:
+      C = (Dim == 2) ? 7.0 / (4.0 * h * h * h * h * M_PI) : 7.0 / (8.0 * h * h * h * h * h * M_PI);
+      if (q < 2.0)
+        return C * pow((1.0 - q / 2.0), 2.0) * (10.0 * q - 5.0) +
+               C * (Dim - 1.0) / q * -5.0 * q * pow((1.0 - q / 2.0), 3.0);
+      else return 0.0;
+    default:
+      C = (Dim == 2) ? 7.0 / (478.0 * h * h * h * h * M_PI) : 1.0 / (120.0 * h * h * h * h * h * M_PI);
+      if (q < 1.0)
+        return C * (20.0 * pow((3.0 - q), 3.0) - 120.0 * pow((2 - q), 3.0) + 300.0 * pow((1 - q), 3.0)) +
+               C * (Dim - 1.0) / q *
+                   (-5.0 * pow((3.0 - q), 4.0) + 30.0 * pow((2.0 - q), 4.0) - 75.0 * pow((1.0 - q), 4.0));
+      else if (q < 2.0)
+        return C * (20.0 * pow((3.0 - q), 3.0) - 120.0 * pow((2 - q), 3.0)) +
+               C * (Dim - 1.0) / q * (-5.0 * pow((3.0 - q), 4.0) + 30.0 * pow((2.0 - q), 4.0));
+      else if (q < 3.0)
+        return C * (20.0 * pow((3.0 - q), 3.0)) + C * (Dim - 1.0) / q * (-5.0 * pow((3.0 - q), 4.0));
+      else return 0.0;
+  }
+}
+
+/* SecDerivativeKernel (Functions.cpp:148-186) */
+static double SecDerivativeKernel(int Dim, int KT, double q, double h) {
+  double C;
+  switch (KT) {
+    case 0:
+      C = (Dim == 2) ? 10.0 / (7.0 * h * h * h * h * M_PI) : 1.0 / (h * h * h * h * h * M_PI);
+      if (q < 1.0) return C * (-3.0 + (9.0 / 2.0) * q);
+      else if (q < 2.0) return C * ((3.0 / 2.0) * (2.0 - q));
+      else return 0.0;
+    case 1:
+      C = (Dim == 2) ? 7.0 / (4.0 * h * h * h * h * M_PI) : 7.0 / (8.0 * h * h * h * h * h * M_PI);
+      if (q < 2.0) return C * pow((1.0 - q / 2.0), 2.0) * (10.0 * q - 5.0);
+      else return 0.0;
+    default:
+      C = (Dim == 2) ? 7.0 / (478.0 * h * h * h * h * M_PI) : 1.0 / (120.0 * h * h * h * h * h * M_PI);
+      if (q < 1.0) return C * (20.0 * pow((3.0 - q), 3.0) - 120.0 * pow((2.0 - q), 3.0) + 300.0 * pow((1.0 - q), 3.0));
+      else if (q < 2.0) return C * (20.0 * pow((3.0 - q), 3.0) - 120.0 * pow((2.0 - q), 3.0));
+      else if (q < 3.0) return C * (20.0 * pow((3.0 - q), 3.0));
+      else return 0.0;
+  }
+}
+
+/* EOS (Functions.cpp:188-212) */
+static double EOS(int EQ, double Cs0, double P00, double Density, double Density0) {
+  switch (EQ) {
+    case 0: return P00 + (Cs0 * Cs0) * (Density - Density0);
+    case 1: return P00 + (Density0 * Cs0 * Cs0 / 7.0) * (pow(Density / Density0, 7.0) - 1);
+    default: return (Cs0 * Cs0) * Density;
+  }
+}
+
+/* SoundSpeed (Functions.cpp:214-238) */
+static double SoundSpeed(int EQ, double Cs0, double Density, double Density0) {
+  switch (EQ) {
+    case 1: return sqrt((Cs0 * Cs0) * pow(Density / Density0, 6.0));
+    default: return Cs0;
+  }
+}
+
+/* DensitySolid (Functions.cpp:240-264): inverse EOS */
+static double DensitySolid(int EQ, double Cs0, double P00, double Pressure, double Density0) {
+  switch (EQ) {
+    case 0: return (Pressure - P00) / (Cs0 * Cs0) + Density0;
+    case 1: return pow(((Pressure - P00) * (7.0 / (Density0 * Cs0 * Cs0)) + 1), 1.0 / 7.0) * Density0;
+    default: return Pressure / (Cs0 * Cs0);
+  }
+}
+
+static double dot3(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+/* Viscous_Force (Functions.cpp:300-332) */
+static void Viscous_Force(int VisEq, double* VI, double Mu, double di, double dj, double GK, const double* vab,
+                          int Dim, int KT, double rij, double h, const double* xij, const double* vij) {
+  switch (VisEq) {
+    case 0: {
+      double s = 2.0 * Mu / (di * dj) * GK;
+      for (int d = 0; d < 3; ++d) VI[d] = s * vab[d];
+    } break;
+    case 1: {
+      double s = 8.0 * Mu / ((di + dj) * (di + dj)) * GK;
+      for (int d = 0; d < 3; ++d) VI[d] = s * vab[d];
+    } break;
+    case 2: {
+      double s = -Mu / (di * dj) * LaplaceKernel(Dim, KT, rij / h, h);
+      for (int d = 0; d < 3; ++d) VI[d] = s * vab[d];
+    } break;
+    default: {
+      double L = LaplaceKernel(Dim, KT, rij / h, h);
+      double S2 = SecDerivativeKernel(Dim, KT, rij / h, h);
+      double dv = dot3(vij, xij);
+      double s = -Mu / (di * dj);
+      for (int d = 0; d < 3; ++d)
+        VI[d] = s * (L * vab[d] + 1.0 / 3.0 * (GK * vij[d] + dv * xij[d] / (rij * rij) * (-GK + S2)));
+    } break;
+  }
+}
+
+/* ---------------------------------------------------------------------------
+ * 3x3 helpers (External/matvec.h)
+ * ------------------------------------------------------------------------- */
+/* Mult(A,B,M) (matvec.h:814-820), the reference's own term order */
+static void mat_mult(const double* A, const double* B, double* M) {
+#define a(i, j) A[3 * (i) + (j)]
+#define b(i, j) B[3 * (i) + (j)]
+  M[0] = a(0, 2) * b(2, 0) + a(0, 1) * b(1, 0) + a(0, 0) * b(0, 0);
+  M[1] = a(0, 2) * b(2, 1) + a(0, 1) * b(1, 1) + a(0, 0) * b(0, 1);
+  M[2] = a(0, 2) * b(2, 2) + a(0, 1) * b(1, 2) + a(0, 0) * b(0, 2);
+  M[3] = a(1, 2) * b(2, 0) + b(1, 0) * a(1, 1) + b(0, 0) * a(1, 0);
+  M[4] = a(1, 2) * b(2, 1) + a(1, 1) * b(1, 1) + b(0, 1) * a(1, 0);
+  M[5] = a(1, 2) * b(2, 2) + a(1, 1) * b(1, 2) + b(0, 2) * a(1, 0);
+  M[6] = a(2, 2) * b(2, 0) + b(1, 0) * a(2, 1) + b(0, 0) * a(2, 0);
+  M[7] = b(2, 1) * a(2, 2) + b(1, 1) * a(2, 1) + b(0, 1) * a(2, 0);
+  M[8] = a(2, 2) * b(2, 2) + b(1, 2) * a(2, 1) + b(0, 2) * a(2, 0);
+#undef a
+#undef b
+}
+static void mat_trans(const double* M, double* T) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) T[3 * i + j] = M[3 * j + i];
+}
+static const double OI[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1}; /* OrthoSys::I */
+
+/* J2 of a deviatoric tensor, as Particle.cpp writes it (e.g. :363-365) */
+static double J2of(const double* S) {
+  return 0.5 * (S[0] * S[0] + 2.0 * S[1] * S[3] + 2.0 * S[2] * S[6] + S[4] * S[4] + 2.0 * S[5] * S[7] +
+                S[8] * S[8]);
+}
+
+/* Cyclic Jacobi eigen-decomposition of a symmetric 3x3 (columns of Q are
+ * eigenvectors), ascending eigenvalues: the Rotation() contract
+ * (Functions.cpp:334-348 -> matvec.h:753-782 with SortAsc). */
+static void sym_eig3(const double* Ain, double* val, double* Q) {
+  double a[9];
+  memcpy(a, Ain, sizeof a);
+  for (int i = 0; i < 9; ++i) Q[i] = (i % 4 == 0) ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = a[1] * a[1] + a[2] * a[2] + a[5] * a[5];
+    if (off == 0.0) break;
+    for (int p = 0; p < 3; ++p)
+      for (int r = p + 1; r < 3; ++r) {
+        double apr = a[3 * p + r];
+        if (apr == 0.0) continue;
+        double theta = (a[3 * r + r] - a[3 * p + p]) / (2.0 * apr);
+        double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+        double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < 3; ++k) {
+          double akp = a[3 * k + p], akr = a[3 * k + r];
+          a[3 * k + p] = c * akp - s * akr;
+          a[3 * k + r] = s * akp + c * akr;
+        }
+        for (int k = 0; k < 3; ++k) {
+          double apk = a[3 * p + k], ark = a[3 * r + k];
+          a[3 * p + k] = c * apk - s * ark;
+          a[3 * r + k] = s * apk + c * ark;
+        }
+        for (int k = 0; k < 3; ++k) {
+          double qkp = Q[3 * k + p], qkr = Q[3 * k + r];
+          Q[3 * k + p] = c * qkp - s * qkr;
+          Q[3 * k + r] = s * qkp + c * qkr;
+        }
+      }
+  }
+  for (int i = 0; i < 3; ++i) val[i] = a[4 * i];
+  for (int i = 0; i < 2; ++i) { /* ascending selection sort */
+    int b = i;
+    for (int j = i + 1; j < 3; ++j)
+      if (val[j] < val[b]) b = j;
+    if (b != i) {
+      double t = val[i];
+      val[i] = val[b];
+      val[b] = t;
+      for (int k = 0; k < 3; ++k) {
+        double u = Q[3 * k + i];
+        Q[3 * k + i] = Q[3 * k + b];
+        Q[3 * k + b] = u;
+      }
+    }
+  }
+}
+
+/* Tensile-instability tensor TIR from Sigma (Source/Domain.cpp:955-987, repeated
+ * for fixed particles at :1174-1204). */
+static void tensile_tir(int dim, const double* S, double TI, double rho, double* TIR) {
+  if (dim == 2) {
+    double teta, Sxx, Syy, C, Sn;
+    if ((S[0] - S[4]) != 0.0) teta = 0.5 * atan(2.0 * S[1] / (S[0] - S[4]));
+    else teta = M_PI / 4.0;
+    C = cos(teta);
+    Sn = sin(teta);
+    Sxx = C * C * S[0] + 2.0 * C * Sn * S[1] + Sn * Sn * S[4];
+    Syy = Sn * Sn * S[0] - 2.0 * C * Sn * S[1] + C * C * S[4];
+    if (Sxx > 0) Sxx = -TI * Sxx / (rho * rho); else Sxx = 0.0;
+    if (Syy > 0) Syy = -TI * Syy / (rho * rho); else Syy = 0.0;
+    TIR[0] = C * C * Sxx + Sn * Sn * Syy;
+    TIR[4] = Sn * Sn * Sxx + C * C * Syy;
+    TIR[1] = TIR[3] = Sn * C * (Sxx - Syy);
+  } else {
+    double val[3], Vec[9], VecT[9], Val[9] = {0}, tmp[9];
+    sym_eig3(S, val, Vec);
+    mat_trans(Vec, VecT);
+    for (int k = 0; k < 3; ++k) Val[4 * k] = (val[k] > 0) ? -TI * val[k] / (rho * rho) : 0.0;
+    mat_mult(Vec, Val, tmp);
+    mat_mult(tmp, VecT, TIR);
+  }
+}
+
+/* ---------------------------------------------------------------------------
+ * Domain routines
+ * ------------------------------------------------------------------------- */
+
+#define FREE(p) (o->is_free[p] != 0)
+
+/* Periodic_X_Correction (Source/Domain.cpp:110-115) */
+static void periodic_correction(const psph_oracle* o, double* x, double h, int64_t p1, int64_t p2) {
+  const double cf = o->g.cellfac;
+  for (int d = 0; d < 3; ++d)
+    if (o->g.dom_size[d] > 0.0)
+      if (x[d] > 2 * cf * h || x[d] < -2 * cf * h) {
+        if (o->CC[3 * p1 + d] > o->CC[3 * p2 + d]) x[d] -= o->g.dom_size[d];
+        else x[d] += o->g.dom_size[d];
+      }
+}
+
+/* CellInitiate (Source/Domain.cpp:549-660) */
+static int cell_initiate(psph_oracle* o) {
+  double TRPR[3] = {0, 0, 0}, BLPF[3] = {0, 0, 0};
+  double hmax = 0, rhomax = 0;
+  const double cf = o->g.cellfac;
+  const int64_t n = o->n;
+  if (n < 1) return fail(o, PSPH_ERR_INVALID_ARGUMENT, "no particles");
+  for (int d = 0; d < 3; ++d) BLPF[d] = TRPR[d] = o->x[d];
+  hmax = o->h[0];
+  rhomax = o->density[0];
+  for (int64_t i = 0; i < n; ++i) {
+    for (int d = 0; d < 3; ++d) {
+      if (o->x[3 * i + d] > TRPR[d]) TRPR[d] = o->x[3 * i + d];
+      if (o->x[3 * i + d] < BLPF[d]) BLPF[d] = o->x[3 * i + d];
+    }
+    if (o->h[i] > hmax) hmax = o->h[i];
+    if (o->density[i] > rhomax) rhomax = o->density[i];
+    if (o->mu[i] > o->mu_max) o->mu_max = o->mu[i];
+    if (o->cs[i] > o->cs_max) o->cs_max = o->cs[i];
+  }
+  for (int d = 0; d < 3; ++d) {
+    if (o->cfg.dom_max[d] > TRPR[d]) TRPR[d] = o->cfg.dom_max[d];
+    if (o->cfg.dom_min[d] < BLPF[d]) BLPF[d] = o->cfg.dom_min[d];
+  }
+  for (int d = 0; d < 3; ++d) {
+    if (!o->cfg.periodic[d]) {
+      TRPR[d] += hmax / 2;
+      BLPF[d] -= hmax / 2;
+    } else {
+      TRPR[d] += o->cfg.R;
+      BLPF[d] -= o->cfg.R;
+    }
+  }
+  int ndim = o->cfg.dimension;
+  for (int d = 0; d < 3; ++d) {
+    if (d < ndim) {
+      double r = (TRPR[d] - BLPF[d]) / (cf * hmax);
+      if ((double)(ceil(((TRPR[d] - BLPF[d]) / (cf * hmax))) - r) < (hmax / 10.0)) o->g.cell_no[d] = (int)ceil(r);
+      else o->g.cell_no[d] = (int)floor(r);
+      if (o->g.cell_no[d] < 1) return fail(o, PSPH_ERR_INVALID_ARGUMENT, "domain thinner than one cell on axis %d", d);
+      o->g.cell_size[d] = (TRPR[d] - BLPF[d]) / o->g.cell_no[d];
+    } else {
+      o->g.cell_no[d] = 1;
+      o->g.cell_size[d] = 0.0;
+    }
+  }
+  for (int d = 0; d < 3; ++d) {
+    if (o->cfg.periodic[d]) o->g.cell_no[d] += 2;
+    o->g.dom_size[d] = o->cfg.periodic[d] ? (TRPR[d] - BLPF[d]) : 0.0;
+    o->g.blpf[d] = BLPF[d];
+    o->g.trpr[d] = TRPR[d];
+  }
+  o->g.hmax = hmax;
+  o->g.rhomax = rhomax;
+  return PSPH_OK;
+}
+
+static int alloc_cells(psph_oracle* o) {
+  o->ncells = (int64_t)o->g.cell_no[0] * o->g.cell_no[1] * o->g.cell_no[2];
+  free(o->HOC);
+  o->HOC = (int32_t*)malloc((size_t)o->ncells * sizeof(int32_t));
+  if (!o->HOC) return fail(o, PSPH_ERR_OUT_OF_MEMORY, "HOC");
+  for (int64_t c = 0; c < o->ncells; ++c) o->HOC[c] = -1;
+  return PSPH_OK;
+}
+
+#define HOCI(o, i, j, k) ((o)->HOC[((int64_t)(i) * (o)->g.cell_no[1] + (j)) * (o)->g.cell_no[2] + (k)])
+
+/* ListGenerate (Source/Domain.cpp:662-784) */
+static int list_generate(psph_oracle* o) {
+  const int dim = o->cfg.dimension;
+  o->nfixed = 0;
+  for (int64_t a = 0; a < o->n; ++a) {
+    int c[3] = {0, 0, 0};
+    for (int d = 0; d < dim; ++d) {
+      const double xd = o->x[3 * a + d];
+      c[d] = (int)(floor((xd - o->g.blpf[d]) / o->g.cell_size[d]));
+      if (c[d] < 0) {
+        if ((o->g.blpf[d] - xd) <= o->g.hmax) c[d] = 0;
+        else return fail(o, PSPH_ERR_INVALID_ARGUMENT, "particle %lld left the grid (axis %d, low side)", (long long)o->orig[a], d);
+      }
+      if (c[d] >= o->g.cell_no[d]) {
+        if ((xd - o->g.trpr[d]) <= o->g.hmax) c[d] = o->g.cell_no[d] - 1;
+        else return fail(o, PSPH_ERR_INVALID_ARGUMENT, "particle %lld left the grid (axis %d, high side)", (long long)o->orig[a], d);
+      }
+    }
+    int32_t temp = HOCI(o, c[0], c[1], c[2]);
+    HOCI(o, c[0], c[1], c[2]) = (int32_t)a;
+    o->LL[a] = temp;
+    for (int d = 0; d < 3; ++d) o->CC[3 * a + d] = c[d];
+    if (!FREE(a)) o->fixed[o->nfixed++] = a;
+  }
+  const int *N = o->g.cell_no;
+  if (o->cfg.periodic[0])
+    for (int j = 0; j < N[1]; j++)
+      for (int k = 0; k < N[2]; k++) {
+        HOCI(o, N[0] - 1, j, k) = HOCI(o, 1, j, k);
+        HOCI(o, N[0] - 2, j, k) = HOCI(o, 0, j, k);
+      }
+  if (o->cfg.periodic[1])
+    for (int i = 0; i < N[0]; i++)
+      for (int k = 0; k < N[2]; k++) {
+        HOCI(o, i, N[1] - 1, k) = HOCI(o, i, 1, k);
+        HOCI(o, i, N[1] - 2, k) = HOCI(o, i, 0, k);
+      }
+  if (o->cfg.periodic[2])
+    for (int i = 0; i < N[0]; i++)
+      for (int j = 0; j < N[1]; j++) {
+        HOCI(o, i, j, N[2] - 1) = HOCI(o, i, j, 1);
+        HOCI(o, i, j, N[2] - 2) = HOCI(o, i, j, 0);
+      }
+  return PSPH_OK;
+}
+
+/* CellReset (Source/Domain.cpp:786-806) */
+static void cell_reset(psph_oracle* o) {
+  for (int64_t c = 0; c < o->ncells; ++c) o->HOC[c] = -1;
+  for (int64_t a = 0; a < o->n; ++a) o->LL[a] = -1;
+  o->nfixed = 0;
+}
+
+/* One candidate pair's classification (Source/Domain.cpp:844-856). */
+static inline void classify(psph_oracle* o, int T, int64_t t1, int64_t t2) {
+  if (FREE(t1) || FREE(t2)) {
+    if (o->material[t1] == o->material[t2]) {
+      if (FREE(t1) * FREE(t2)) pv_push(&o->sm[T], t1, t2);
+      else pv_push(&o->fsm[T], t1, t2);
+    } else
+      pv_push(&o->nsm[T], t1, t2);
+  }
+}
+
+/* YZPlaneCellsNeighbourSearch (Source/Domain.cpp:824-945) */
+static void yz_plane_search(psph_oracle* o, int q1, int T) {
+  const int *N = o->g.cell_no;
+  const int *P = o->cfg.periodic;
+  for (int q3 = P[2] ? 1 : 0; P[2] ? (q3 < (N[2] - 1)) : (q3 < N[2]); q3++)
+    for (int q2 = P[1] ? 1 : 0; P[1] ? (q2 < (N[1] - 1)) : (q2 < N[1]); q2++) {
+      if (HOCI(o, q1, q2, q3) == -1) continue;
+      int32_t temp1 = HOCI(o, q1, q2, q3);
+      while (temp1 != -1) {
+        int32_t temp2 = o->LL[temp1];
+        while (temp2 != -1) {
+          classify(o, T, temp1, temp2);
+          temp2 = o->LL[temp2];
+        }
+        if (q1 + 1 < N[0]) {
+          temp2 = HOCI(o, q1 + 1, q2, q3);
+          while (temp2 != -1) {
+            classify(o, T, temp1, temp2);
+            temp2 = o->LL[temp2];
+          }
+        }
+        if (q2 + 1 < N[1]) {
+          for (int i = q1 - 1; i <= q1 + 1; i++)
+            if (i < N[0] && i >= 0) {
+              temp2 = HOCI(o, i, q2 + 1, q3);
+              while (temp2 != -1) {
+                classify(o, T, temp1, temp2);
+                temp2 = o->LL[temp2];
+              }
+            }
+        }
+        if (q3 + 1 < N[2]) {
+          for (int j = q2 - 1; j <= q2 + 1; j++)
+            for (int i = q1 - 1; i <= q1 + 1; i++)
+              if (i < N[0] && i >= 0 && j < N[1] && j >= 0) {
+                temp2 = HOCI(o, i, j, q3 + 1);
+                while (temp2 != -1) {
+                  classify(o, T, temp1, temp2);
+                  temp2 = o->LL[temp2];
+                }
+              }
+        }
+        temp1 = o->LL[temp1];
+      }
+    }
+}
+
+/* MainNeighbourSearch (Source/Domain.cpp:808-822) */
+static void main_search(psph_oracle* o, int nthr) {
+  for (int t = 0; t < o->nthr; ++t) o->sm[t].n = o->fsm[t].n = o->nsm[t].n = 0;
+  const int lo = o->cfg.periodic[0] ? 1 : 0;
+  const int hi = o->cfg.periodic[0] ? o->g.cell_no[0] - 1 : o->g.cell_no[0];
+#pragma omp parallel for schedule(dynamic) num_threads(nthr)
+  for (int q1 = lo; q1 < hi; q1++) yz_plane_search(o, q1, omp_get_thread_num());
+}
+
+/* StartAcceleration (Source/Domain.cpp:947-1018) + the constant body force of
+ * the GeneralBefore hook. */
+static void start_acceleration(psph_oracle* o, int nthr) {
+  const int dim = o->cfg.dimension;
+  const double g0 = o->cfg.gravity[0], g1 = o->cfg.gravity[1], g2 = o->cfg.gravity[2];
+  const double gn = sqrt(g0 * g0 + g1 * g1 + g2 * g2);
+  const double* bf = o->cfg.body_force;
+  const double bn = sqrt(bf[0] * bf[0] + bf[1] * bf[1] + bf[2] * bf[2]);
+#pragma omp parallel for schedule(static) num_threads(nthr)
+  for (int64_t i = 0; i < o->n; i++) {
+    if (FREE(i)) {
+      if (o->material[i] > 1 && o->ti[i] > 0.0) tensile_tir(dim, o->sigma + 9 * i, o->ti[i], o->density[i], o->tir + 9 * i);
+    } else {
+      for (int d = 0; d < 3; ++d) o->nsv[3 * i + d] = 0.0;
+      o->pressure[i] = 0.0;
+      memset(o->sigma + 9 * i, 0, 9 * sizeof(double));
+      memset(o->shear_stress + 9 * i, 0, 9 * sizeof(double));
+    }
+    o->a[3 * i] = g0;
+    o->a[3 * i + 1] = g1;
+    o->a[3 * i + 2] = g2;
+    o->ddensity[i] = 0.0;
+    for (int d = 0; d < 3; ++d) o->vxsph[3 * i + d] = 0.0;
+    o->zwab[i] = 0.0;
+    o->sumden[i] = 0.0;
+    o->sumkernel[i] = 0.0;
+    if (dim == 2) o->v[3 * i + 2] = 0.0;
+    memset(o->strain_rate + 9 * i, 0, 9 * sizeof(double));
+    memset(o->rotation_rate + 9 * i, 0, 9 * sizeof(double));
+    o->a_scale[i] = gn + (FREE(i) ? bn : 0.0);
+    o->dr_scale[i] = 0.0;
+    /* GeneralBefore: constant body force on free particles */
+    if (FREE(i) && (bf[0] != 0.0 || bf[1] != 0.0 || bf[2] != 0.0))
+      for (int d = 0; d < 3; ++d) o->a[3 * i + d] += bf[d];
+  }
+}
+
+/* PrimaryComputeAcceleration, wall branch (Source/Domain.cpp:1020-1059,
+ * normalisation and fixed-particle TIR :1164-1206). */
+static void primary_compute(psph_oracle* o, int nthr) {
+  const int dim = o->cfg.dimension, kt = o->cfg.kernel_type;
+  const double* G = o->cfg.gravity;
+  const int physical = o->cfg.wall_pressure_mode == PSPH_WALLP_PHYSICAL;
+#pragma omp parallel for schedule(static) num_threads(nthr)
+  for (int k = 0; k < o->nthr; k++) {
+    for (int64_t a = 0; a < o->fsm[k].n; a++) {
+      int64_t P1 = o->fsm[k].v[2 * a], P2 = o->fsm[k].v[2 * a + 1];
+      double xij[3];
+      for (int d = 0; d < 3; ++d) xij[d] = o->x[3 * P1 + d] - o->x[3 * P2 + d];
+      double h = (o->h[P1] + o->h[P2]) / 2.0;
+      periodic_correction(o, xij, h, P1, P2);
+      double K = Kernel(dim, kt, sqrt(dot3(xij, xij)) / h, h);
+      int64_t W = FREE(P1) ? P2 : P1, F = FREE(P1) ? P1 : P2;
+      double gx = dot3(G, xij);
+      if (physical && W == P2) gx = -gx; /* x_wall - x_fluid */
+      omp_set_lock(&o->locks[W]);
+      o->sumkernel[W] += K;
+      if (o->material[W] < 3) o->pressure[W] += o->pressure[F] * K + gx * o->density[F] * K;
+      if (o->material[W] > 1)
+        for (int e = 0; e < 9; ++e) o->sigma[9 * W + e] = o->sigma[9 * W + e] + o->sigma[9 * F + e] * K;
+      if (o->no_slip[W])
+        for (int d = 0; d < 3; ++d) o->nsv[3 * W + d] += o->v[3 * F + d] * K;
+      omp_unset_lock(&o->locks[W]);
+    }
+  }
+#pragma omp parallel for schedule(static) num_threads(nthr)
+  for (int64_t i = 0; i < o->nfixed; i++) {
+    int64_t a = o->fixed[i];
+    if (o->sumkernel[a] != 0.0) {
+      if (o->material[a] < 3) o->pressure[a] = o->pressure[a] / o->sumkernel[a];
+      if (o->material[a] > 1) {
+        double s = 1.0 / o->sumkernel[a];
+        for (int e = 0; e < 9; ++e) o->sigma[9 * a + e] = o->sigma[9 * a + e] * s;
+      }
+      if (o->no_slip[a])
+        for (int d = 0; d < 3; ++d) o->nsv[3 * a + d] = o->nsv[3 * a + d] / o->sumkernel[a];
+      if (o->material[a] > 1 && o->ti[a] > 0.0) tensile_tir(dim, o->sigma + 9 * a, o->ti[a], o->density[a], o->tir + 9 * a);
+    }
+  }
+}
+
+static inline double shepard_counter_of(const psph_oracle* o, int64_t p) {
+  return FREE(p) ? o->it.shepard_counter : 0; /* fixed particles never move */
+}
+
+/* CalcForce11 (Source/Interaction.cpp:25-184) */
+static void calc_force11(psph_oracle* o, int64_t p1, int64_t p2) {
+  const int dim = o->cfg.dimension, kt = o->cfg.kernel_type;
+  double h = (o->h[p1] + o->h[p2]) / 2;
+  double xij[3];
+  for (int d = 0; d < 3; ++d) xij[d] = o->x[3 * p1 + d] - o->x[3 * p2 + d];
+  periodic_correction(o, xij, h, p1, p2);
+  double rij = sqrt(dot3(xij, xij));
+  if ((rij / h) > o->g.cellfac) return;
+  const int f1 = FREE(p1), f2 = FREE(p2);
+  double di = 0.0, dj = 0.0, mi = 0.0, mj = 0.0;
+  double Alpha = (o->alpha[p1] + o->alpha[p2]) / 2.0;
+  double Beta = (o->beta[p1] + o->beta[p2]) / 2.0;
+  double vij[3];
+  for (int d = 0; d < 3; ++d) vij[d] = o->v[3 * p1 + d] - o->v[3 * p2 + d];
+  if (!f1) {
+    di = DensitySolid(o->pres_eq[p2], o->cs[p2], o->p0[p2], o->pressure[p1], o->ref_density[p2]);
+    mi = o->fpmassc[p1] * o->mass[p2];
+  } else {
+    di = o->density[p1];
+    mi = o->mass[p1];
+  }
+  if (!f2) {
+    dj = DensitySolid(o->pres_eq[p1], o->cs[p1], o->p0[p1], o->pressure[p2], o->ref_density[p1]);
+    mj = o->fpmassc[p2] * o->mass[p1];
+  } else {
+    dj = o->density[p2];
+    mj = o->mass[p2];
+  }
+  double GK = GradKernel(dim, kt, rij / h, h);
+  double K = Kernel(dim, kt, rij / h, h);
+
+  double PIij = 0.0;
+  if (Alpha != 0.0 || Beta != 0.0) {
+    double Ci, Cj;
+    if (!f1) Ci = SoundSpeed(o->pres_eq[p2], o->cs[p2], di, o->ref_density[p2]);
+    else Ci = SoundSpeed(o->pres_eq[p1], o->cs[p1], di, o->ref_density[p1]);
+    if (!f2) Cj = SoundSpeed(o->pres_eq[p1], o->cs[p1], dj, o->ref_density[p1]);
+    else Cj = SoundSpeed(o->pres_eq[p2], o->cs[p2], dj, o->ref_density[p2]);
+    double MUij = h * dot3(vij, xij) / (rij * rij + 0.01 * h * h);
+    if (dot3(vij, xij) < 0) PIij = (-Alpha * 0.5 * (Ci + Cj) * MUij + Beta * MUij * MUij) / (0.5 * (di + dj));
+  }
+
+  double TIij = 0.0;
+  if (o->ti[p1] > 0.0 || o->ti[p2] > 0.0) {
+    double Ri = 0.0, Rj = 0.0;
+    if ((o->pressure[p1] + o->pressure[p2]) < 0.0) {
+      if (o->pressure[p1] < 0.0) Ri = -o->pressure[p1] / (di * di);
+      if (o->pressure[p2] < 0.0) Rj = -o->pressure[p2] / (dj * dj);
+    }
+    TIij = (o->ti[p1] * Ri + o->ti[p2] * Rj) *
+           pow((K / Kernel(dim, kt, (o->ti_init_dist[p1] + o->ti_init_dist[p2]) / (2.0 * h), h)),
+               (o->tin[p1] + o->tin[p2]) / 2.0);
+  }
+
+  double SR[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  double VI[3] = {0, 0, 0}, vab[3] = {0, 0, 0};
+  const int want_sr = (o->t0[p1] > 0.0 || o->t0[p2] > 0.0 || (o->les[p1] * o->les[p2]));
+  if ((o->no_slip[p1] || o->no_slip[p2]) || (f1 * f2)) {
+    double Mu = 0.0;
+    if (f1 * f2) {
+      for (int d = 0; d < 3; ++d) vab[d] = vij[d];
+      Mu = 2.0 * o->mu[p1] * o->mu[p2] / (o->mu[p1] + o->mu[p2]);
+    } else {
+      if (f1)
+        for (int d = 0; d < 3; ++d) vab[d] = o->v[3 * p1 + d] - (2.0 * o->v[3 * p2 + d] - o->nsv[3 * p2 + d]);
+      else
+        for (int d = 0; d < 3; ++d) vab[d] = (2.0 * o->v[3 * p1 + d] - o->nsv[3 * p1 + d]) - o->v[3 * p2 + d];
+      if (!f1) Mu = o->mu[p2];
+      if (!f2) Mu = o->mu[p1];
+    }
+    if (want_sr) {
+      SR[0] = 2.0 * vab[0] * xij[0];
+      SR[1] = vab[0] * xij[1] + vab[1] * xij[0];
+      SR[2] = vab[0] * xij[2] + vab[2] * xij[0];
+      SR[3] = vab[0] * xij[1] + vab[1] * xij[0];
+      SR[4] = 2.0 * vab[1] * xij[1];
+      SR[5] = vab[1] * xij[2] + vab[2] * xij[1];
+      SR[6] = vab[0] * xij[2] + vab[2] * xij[0];
+      SR[7] = vab[1] * xij[2] + vab[2] * xij[1];
+      SR[8] = 2.0 * vab[2] * xij[2];
+      for (int e = 0; e < 9; ++e) SR[e] = SR[e] * -GK;
+    }
+    Viscous_Force(o->cfg.vis_eq, VI, Mu, di, dj, GK, vab, dim, kt, rij, h, xij, vij);
+  }
+
+  double X1[3] = {0, 0, 0}, X2[3] = {0, 0, 0};
+  const int do_xsph = (o->cfg.xsph != 0.0 && (f1 * f2));
+  if (do_xsph) {
+    double s1 = o->cfg.xsph * mj / (0.5 * (di + dj)) * K, s2 = o->cfg.xsph * mi / (0.5 * (di + dj)) * K;
+    for (int d = 0; d < 3; ++d) {
+      X1[d] = s1 * -vij[d];
+      X2[d] = s2 * vij[d];
+    }
+  }
+
+  double temp[3], s;
+  if (o->cfg.gradient_type == 0)
+    s = -1.0 * (o->pressure[p1] / (di * di) + o->pressure[p2] / (dj * dj) + PIij + TIij) * GK;
+  else
+    s = -1.0 * ((o->pressure[p1] + o->pressure[p2]) / (di * dj) + PIij + TIij) * GK;
+  for (int d = 0; d < 3; ++d) temp[d] = s * xij[d] + VI[d];
+  if (dim == 2) temp[2] = 0.0;
+  double gx[3] = {GK * xij[0], GK * xij[1], GK * xij[2]};
+  double temp1 = dot3(vij, gx);
+  const double tn = sqrt(dot3(temp, temp));
+
+  omp_set_lock(&o->locks[p1]);
+  for (int d = 0; d < 3; ++d) o->a[3 * p1 + d] += mj * temp[d];
+  o->ddensity[p1] += mj * (di / dj) * temp1;
+  if (do_xsph)
+    for (int d = 0; d < 3; ++d) o->vxsph[3 * p1 + d] += X1[d];
+  if (f1) {
+    if (o->t0[p1] > 0.0 || o->les[p1]) {
+      double c = mj / dj;
+      for (int e = 0; e < 9; ++e) o->strain_rate[9 * p1 + e] = o->strain_rate[9 * p1 + e] + SR[e] * c;
+    }
+    o->zwab[p1] += mj / dj * K;
+  } else
+    o->zwab[p1] = 1.0;
+  if (o->shepard[p1])
+    if (shepard_counter_of(o, p1) == o->cfg.shepard_step) o->sumden[p1] += mj * K;
+  o->a_scale[p1] += fabs(mj) * tn;
+  o->dr_scale[p1] += fabs(mj * (di / dj) * temp1);
+  omp_unset_lock(&o->locks[p1]);
+
+  omp_set_lock(&o->locks[p2]);
+  for (int d = 0; d < 3; ++d) o->a[3 * p2 + d] -= mi * temp[d];
+  o->ddensity[p2] += mi * (dj / di) * temp1;
+  if (do_xsph)
+    for (int d = 0; d < 3; ++d) o->vxsph[3 * p2 + d] += X2[d];
+  if (f2) {
+    if (o->t0[p2] > 0.0 || o->les[p2]) {
+      double c = mi / di;
+      for (int e = 0; e < 9; ++e) o->strain_rate[9 * p2 + e] = o->strain_rate[9 * p2 + e] + SR[e] * c;
+    }
+    o->zwab[p2] += mi / di * K;
+  } else
+    o->zwab[p2] = 1.0;
+  if (o->shepard[p2])
+    if (shepard_counter_of(o, p2) == o->cfg.shepard_step) o->sumden[p2] += mi * K;
+  o->a_scale[p2] += fabs(mi) * tn;
+  o->dr_scale[p2] += fabs(mi * (dj / di) * temp1);
+  omp_unset_lock(&o->locks[p2]);
+}
+
+/* CalcForce2233 (Source/Interaction.cpp:186-377) */
+static void calc_force2233(psph_oracle* o, int64_t p1, int64_t p2) {
+  const int dim = o->cfg.dimension, kt = o->cfg.kernel_type;
+  double h = (o->h[p1] + o->h[p2]) / 2;
+  double xij[3];
+  for (int d = 0; d < 3; ++d) xij[d] = o->x[3 * p1 + d] - o->x[3 * p2 + d];
+  periodic_correction(o, xij, h, p1, p2);
+  double rij = sqrt(dot3(xij, xij));
+  if ((rij / h) > o->g.cellfac) return;
+  const int f1 = FREE(p1), f2 = FREE(p2);
+  double di = 0.0, dj = 0.0, mi = 0.0, mj = 0.0;
+  double Alpha = (o->alpha[p1] + o->alpha[p2]) / 2.0;
+  double Beta = (o->beta[p1] + o->beta[p2]) / 2.0;
+  const int soil = (o->material[p1] * o->material[p2] == 9);
+  if (soil) {
+    if (!f1) { di = o->density[p2]; mi = o->fpmassc[p1] * o->mass[p2]; } else { di = o->density[p1]; mi = o->mass[p1]; }
+    if (!f2) { dj = o->density[p1]; mj = o->fpmassc[p2] * o->mass[p1]; } else { dj = o->density[p2]; mj = o->mass[p2]; }
+  } else {
+    if (!f1) {
+      di = DensitySolid(o->pres_eq[p2], o->cs[p2], o->p0[p2], o->pressure[p1], o->ref_density[p2]);
+      mi = o->fpmassc[p1] * o->mass[p2];
+    } else {
+      di = o->density[p1];
+      mi = o->mass[p1];
+    }
+    if (!f2) {
+      dj = DensitySolid(o->pres_eq[p1], o->cs[p1], o->p0[p1], o->pressure[p2], o->ref_density[p1]);
+      mj = o->fpmassc[p2] * o->mass[p1];
+    } else {
+      dj = o->density[p2];
+      mj = o->mass[p2];
+    }
+  }
+  double vij[3];
+  for (int d = 0; d < 3; ++d) vij[d] = o->v[3 * p1 + d] - o->v[3 * p2 + d];
+  double GK = GradKernel(dim, kt, rij / h, h);
+  double K = Kernel(dim, kt, rij / h, h);
+
+  double PIij[9] = {0};
+  if (Alpha != 0.0 || Beta != 0.0) {
+    double MUij = h * dot3(vij, xij) / (rij * rij + 0.01 * h * h);
+    double Cij;
+    if (soil) Cij = 0.5 * (o->cs[p1] + o->cs[p2]);
+    else {
+      double Ci, Cj;
+      if (!f1) Ci = SoundSpeed(o->pres_eq[p2], o->cs[p2], di, o->ref_density[p2]);
+      else Ci = SoundSpeed(o->pres_eq[p1], o->cs[p1], di, o->ref_density[p1]);
+      if (!f2) Cj = SoundSpeed(o->pres_eq[p1], o->cs[p1], dj, o->ref_density[p1]);
+      else Cj = SoundSpeed(o->pres_eq[p2], o->cs[p2], dj, o->ref_density[p2]);
+      Cij = 0.5 * (Ci + Cj);
+    }
+    if (dot3(vij, xij) < 0) {
+      double s = (Alpha * Cij * MUij + Beta * MUij * MUij) / (0.5 * (di + dj));
+      for (int e = 0; e < 9; ++e) PIij[e] = o->I[e] * s;
+    }
+  }
+  const double* Sigmai = o->sigma + 9 * p1;
+  const double* Sigmaj = o->sigma + 9 * p2;
+  double TIij[9] = {0};
+  if (o->ti[p1] > 0.0 || o->ti[p2] > 0.0) {
+    double s = pow((K / Kernel(dim, kt, (o->ti_init_dist[p1] + o->ti_init_dist[p2]) / (2.0 * h), h)),
+                   (o->tin[p1] + o->tin[p2]) / 2.0);
+    for (int e = 0; e < 9; ++e) TIij[e] = (o->tir[9 * p1 + e] + o->tir[9 * p2 + e]) * s;
+  }
+  double vab[3] = {0, 0, 0};
+  if (f1 * f2) {
+    for (int d = 0; d < 3; ++d) vab[d] = vij[d];
+  } else {
+    const int ns = o->no_slip[p1] || o->no_slip[p2];
+    if (ns) {
+      if (f1)
+        for (int d = 0; d < 3; ++d) vab[d] = o->v[3 * p1 + d] - (2.0 * o->v[3 * p2 + d] - o->nsv[3 * p2 + d]);
+      else
+        for (int d = 0; d < 3; ++d) vab[d] = (2.0 * o->v[3 * p1 + d] - o->nsv[3 * p1 + d]) - o->v[3 * p2 + d];
+    }
+    if (!ns) {
+      if (f1)
+        for (int d = 0; d < 3; ++d) vab[d] = o->v[3 * p1 + d] - o->vb[3 * p2 + d];
+      else
+        for (int d = 0; d < 3; ++d) vab[d] = o->vb[3 * p1 + d] - o->v[3 * p2 + d];
+    }
+  }
+  double SR[9], RR[9] = {0};
+  SR[0] = 2.0 * vab[0] * xij[0];
+  SR[1] = vab[0] * xij[1] + vab[1] * xij[0];
+  SR[2] = vab[0] * xij[2] + vab[2] * xij[0];
+  SR[3] = SR[1];
+  SR[4] = 2.0 * vab[1] * xij[1];
+  SR[5] = vab[1] * xij[2] + vab[2] * xij[1];
+  SR[6] = SR[2];
+  SR[7] = SR[5];
+  SR[8] = 2.0 * vab[2] * xij[2];
+  double sc = -0.5 * GK;
+  for (int e = 0; e < 9; ++e) SR[e] = SR[e] * sc;
+  RR[1] = vab[0] * xij[1] - vab[1] * xij[0];
+  RR[2] = vab[0] * xij[2] - vab[2] * xij[0];
+  RR[5] = vab[1] * xij[2] - vab[2] * xij[1];
+  RR[3] = -RR[1];
+  RR[6] = -RR[2];
+  RR[7] = -RR[5];
+  for (int e = 0; e < 9; ++e) RR[e] = RR[e] * sc;
+
+  double X1[3] = {0, 0, 0}, X2[3] = {0, 0, 0};
+  const int do_xsph = (o->cfg.xsph != 0.0 && (f1 * f2));
+  if (do_xsph) {
+    double s1 = o->cfg.xsph * mj / (0.5 * (di + dj)) * K, s2 = o->cfg.xsph * mi / (0.5 * (di + dj)) * K;
+    for (int d = 0; d < 3; ++d) {
+      X1[d] = s1 * -vij[d];
+      X2[d] = s2 * vij[d];
+    }
+  }
+
+  double M[9], temp[3];
+  if (o->cfg.gradient_type == 0) {
+    double ci = 1.0 / (di * di), cj = 1.0 / (dj * dj);
+    for (int e = 0; e < 9; ++e) M[e] = ((Sigmai[e] * ci + Sigmaj[e] * cj) + PIij[e]) + TIij[e];
+  } else {
+    double c = 1.0 / (di * dj);
+    for (int e = 0; e < 9; ++e) M[e] = ((Sigmai[e] + Sigmaj[e]) * c + PIij[e]) + TIij[e];
+  }
+  double gx[3] = {GK * xij[0], GK * xij[1], GK * xij[2]};
+  for (int c = 0; c < 3; ++c) temp[c] = gx[0] * M[c] + gx[1] * M[3 + c] + gx[2] * M[6 + c]; /* Mult(Vec,Mat) */
+  if (dim == 2) temp[2] = 0.0;
+  double temp1 = dot3(vij, gx);
+  const double tn = sqrt(dot3(temp, temp));
+
+  omp_set_lock(&o->locks[p1]);
+  for (int d = 0; d < 3; ++d) o->a[3 * p1 + d] += mj * temp[d];
+  o->ddensity[p1] += mj * (di / dj) * temp1;
+  if (do_xsph)
+    for (int d = 0; d < 3; ++d) o->vxsph[3 * p1 + d] += X1[d];
+  if (f1) {
+    o->zwab[p1] += mj / dj * K;
+    double c = mj / dj;
+    for (int e = 0; e < 9; ++e) {
+      o->strain_rate[9 * p1 + e] = o->strain_rate[9 * p1 + e] + SR[e] * c;
+      o->rotation_rate[9 * p1 + e] = o->rotation_rate[9 * p1 + e] + RR[e] * c;
+    }
+  } else
+    o->zwab[p1] = 1.0;
+  if (o->shepard[p1])
+    if (shepard_counter_of(o, p1) == o->cfg.shepard_step) o->sumden[p1] += mj * K;
+  o->a_scale[p1] += fabs(mj) * tn;
+  o->dr_scale[p1] += fabs(mj * (di / dj) * temp1);
+  omp_unset_lock(&o->locks[p1]);
+
+  omp_set_lock(&o->locks[p2]);
+  for (int d = 0; d < 3; ++d) o->a[3 * p2 + d] -= mi * temp[d];
+  o->ddensity[p2] += mi * (dj / di) * temp1;
+  if (do_xsph)
+    for (int d = 0; d < 3; ++d) o->vxsph[3 * p2 + d] += X2[d];
+  if (f2) {
+    o->zwab[p2] += mi / di * K;
+    double c = mi / di;
+    for (int e = 0; e < 9; ++e) {
+      o->strain_rate[9 * p2 + e] = o->strain_rate[9 * p2 + e] + SR[e] * c;
+      o->rotation_rate[9 * p2 + e] = o->rotation_rate[9 * p2 + e] + RR[e] * c;
+    }
+  } else
+    o->zwab[p2] = 1.0;
+  if (o->shepard[p2])
+    if (shepard_counter_of(o, p2) == o->cfg.shepard_step) o->sumden[p2] += mi * K;
+  o->a_scale[p2] += fabs(mi) * tn;
+  o->dr_scale[p2] += fabs(mi * (dj / di) * temp1);
+  omp_unset_lock(&o->locks[p2]);
+}
+
+/* LastComputeAcceleration (Source/Domain.cpp:1238-1297) */
+static int last_compute(psph_oracle* o, int nthr) {
+  for (int k = 0; k < o->nthr; ++k)
+    if (o->nsm[k].n) return fail(o, PSPH_ERR_UNSUPPORTED, "interaction between different materials (NSMPairs) is outside this build");
+#pragma omp parallel for schedule(static) num_threads(nthr)
+  for (int k = 0; k < o->nthr; k++) {
+    for (int64_t i = 0; i < o->sm[k].n; i++) {
+      int64_t p1 = o->sm[k].v[2 * i], p2 = o->sm[k].v[2 * i + 1];
+      if (o->material[p1] == 1) calc_force11(o, p1, p2); else calc_force2233(o, p1, p2);
+    }
+    for (int64_t i = 0; i < o->fsm[k].n; i++) {
+      int64_t p1 = o->fsm[k].v[2 * i], p2 = o->fsm[k].v[2 * i + 1];
+      if (o->material[p1] == 1) calc_force11(o, p1, p2); else calc_force2233(o, p1, p2);
+    }
+  }
+  double dtmin = o->it.deltatint;
+  const double sha = o->cfg.sqrt_h_a;
+#pragma omp parallel for schedule(static) num_threads(nthr) reduction(min : dtmin)
+  for (int64_t i = 0; i < o->n; i++)
+    if (FREE(i)) {
+      const double* a = o->a + 3 * i;
+      double test = sqrt(o->h[i] / sqrt(dot3(a, a)));
+      if (dtmin > (sha * test)) dtmin = sha * test;
+    }
+  o->it.deltatmin = dtmin;
+  return PSPH_OK;
+}
+
+/* AdaptiveTimeStep (Source/Domain.cpp:133-152) */
+static int adaptive_time_step(psph_oracle* o) {
+  psph_integrator* t = &o->it;
+  if (t->deltatint > t->deltatmin) {
+    if (t->deltat < t->deltatmin) t->deltat = 2.0 * t->deltat * t->deltatmin / (t->deltat + t->deltatmin);
+    else t->deltat = t->deltatmin;
+  } else {
+    if (t->deltatint != t->deltat) t->deltat = 2.0 * t->deltat * t->deltatint / (t->deltat + t->deltatint);
+    else t->deltat = t->deltatint;
+  }
+  if (t->deltat < (t->deltatint / 1.0e5))
+    return fail(o, PSPH_ERR_DT_COLLAPSE, "Too small time step, please choose a smaller time step initially to make the simulation more stable");
+  return PSPH_OK;
+}
+
+/* Mat1 (Source/Particle.cpp:146-186) */
+static void mat1(psph_oracle* o, int64_t i) {
+  o->pressure[i] = EOS(o->pres_eq[i], o->cs[i], o->p0[i], o->density[i], o->ref_density[i]);
+  const double* S = o->strain_rate + 9 * i;
+  double temp = (S[0] * S[0] + 2.0 * S[1] * S[3] + 2.0 * S[2] * S[6] + S[4] * S[4] + 2.0 * S[5] * S[7] + S[8] * S[8]);
+  o->shear_rate[i] = sqrt(0.5 * temp);
+  o->sbar[i] = sqrt(2.0 * temp);
+  if (o->les[i]) o->mu[i] = o->mu_ref[i] + o->ref_density[i] * pow((o->csmag[i] * o->h[i]), 2.0) * o->sbar[i];
+  if (o->t0[i] > 0.0) {
+    const double sr = o->shear_rate[i], T0 = o->t0[i], MuRef = o->mu_ref[i], m = o->bingham_m[i];
+    if (o->vis_m[i] == 0) {
+      if (sr != 0.0) o->mu[i] = MuRef + T0 * (1 - exp(-m * sr)) / sr;
+      else o->mu[i] = MuRef + T0 * m;
+    } else
+      o->mu[i] = (1000.0 * MuRef + MuRef * MuRef * 1000.0 / T0 * sr) / (1 + 1000.0 * MuRef / T0 * sr);
+  }
+}
+
+/* Deviatoric elastic rate 2G(D - tr(D)/3 I) + S W^T + W S, the bracket of
+ * Particle.cpp:286-289 / :614-617 (solid, around ShearStress). */
+static void mat2_rate(const double* SR, const double* RR, const double* SS, double G, double* X) {
+  double RRT[9], SRT[9], RS[9];
+  mat_trans(RR, RRT);
+  mat_mult(SS, RRT, SRT);
+  mat_mult(RR, SS, RS);
+  double s_tr = 1.0 / 3.0 * (SR[0] + SR[4] + SR[8]);
+  double g2 = 2.0 * G;
+  for (int e = 0; e < 9; ++e) X[e] = (((SR[e] - OI[e] * s_tr) * g2) + SRT[e]) + RS[e];
+}
+
+/* Elastic stress rate K tr(D) I + 2G(D - tr(D)/3 I) + Sigma W^T + W Sigma
+ * (Particle.cpp:337-339 / :659-661, soil, around Sigma). */
+static void mat3_rate(const double* SR, const double* RR, const double* Sig, double K, double G, double* X) {
+  double RRT[9], SRT[9], RS[9];
+  mat_trans(RR, RRT);
+  mat_mult(Sig, RRT, SRT);
+  mat_mult(RR, Sig, RS);
+  double I1s = SR[0] + SR[4] + SR[8];
+  double sK = I1s * K, s3 = 1.0 / 3.0 * I1s, g2 = 2.0 * G;
+  for (int e = 0; e < 9; ++e) X[e] = ((OI[e] * sK + ((SR[e] - OI[e] * s3) * g2)) + SRT[e]) + RS[e];
+}
+
+/* Mat2Leapfrog (Particle.cpp:598-639) */
+static int mat2_leapfrog(psph_oracle* o, int64_t i, double dt) {
+  o->pressure[i] = EOS(o->pres_eq[i], o->cs[i], o->p0[i], o->density[i], o->ref_density[i]);
+  double *SS = o->shear_stress + 9 * i, *Sa = o->shear_stressa + 9 * i, *Sb = o->shear_stressb + 9 * i;
+  const double *SR = o->strain_rate + 9 * i, *RR = o->rotation_rate + 9 * i;
+  double X[9];
+  mat2_rate(SR, RR, SS, o->g_mod[i], X);
+  if (o->it.first_step)
+    for (int e = 0; e < 9; ++e) Sa[e] = X[e] * (-dt / 2.0) + SS[e];
+  for (int e = 0; e < 9; ++e) Sb[e] = Sa[e];
+  for (int e = 0; e < 9; ++e) Sa[e] = X[e] * dt + Sa[e];
+  if (o->fail[i] == 1) {
+    double J2 = J2of(Sa);
+    double r = o->sigmay[i] / sqrt(3.0 * J2);
+    double s = (1.0 < r) ? 1.0 : r; /* std::min(r, 1.0) */
+    for (int e = 0; e < 9; ++e) Sa[e] = Sa[e] * s;
+  }
+  for (int e = 0; e < 9; ++e) SS[e] = (Sa[e] + Sb[e]) * (1.0 / 2.0);
+  double* Sig = o->sigma + 9 * i;
+  for (int e = 0; e < 9; ++e) Sig[e] = OI[e] * -o->pressure[i] + SS[e];
+  double *E = o->strain + 9 * i, *Ea = o->straina + 9 * i, *Eb = o->strainb + 9 * i;
+  if (o->it.first_step)
+    for (int e = 0; e < 9; ++e) Ea[e] = SR[e] * (-dt / 2.0) + E[e];
+  for (int e = 0; e < 9; ++e) Eb[e] = Ea[e];
+  for (int e = 0; e < 9; ++e) Ea[e] = SR[e] * dt + Ea[e];
+  for (int e = 0; e < 9; ++e) E[e] = (Ea[e] + Eb[e]) * (1.0 / 2.0);
+  if (o->fail[i] > 1) return fail(o, PSPH_ERR_INVALID_ARGUMENT, "Undefined failure criteria for solids");
+  return PSPH_OK;
+}
+
+/* Mat2MVerlet (Particle.cpp:276-318) */
+static int mat2_mverlet(psph_oracle* o, int64_t i, double dt, int ct) {
+  o->pressure[i] = EOS(o->pres_eq[i], o->cs[i], o->p0[i], o->density[i], o->ref_density[i]);
+  double *SS = o->shear_stress + 9 * i, *Sb = o->shear_stressb + 9 * i;
+  const double *SR = o->strain_rate + 9 * i, *RR = o->rotation_rate + 9 * i;
+  double X[9], Stress[9];
+  mat2_rate(SR, RR, SS, o->g_mod[i], X);
+  memcpy(Stress, SS, sizeof Stress);
+  if (ct == 30)
+    for (int e = 0; e < 9; ++e) SS[e] = X[e] * dt + SS[e];
+  else
+    for (int e = 0; e < 9; ++e) SS[e] = X[e] * (2.0 * dt) + Sb[e];
+  memcpy(Sb, Stress, sizeof Stress);
+  if (o->fail[i] == 1) {
+    double J2 = J2of(SS);
+    double r = o->sigmay[i] / sqrt(3.0 * J2);
+    double s = (1.0 < r) ? 1.0 : r; /* std::min(r, 1.0) */
+    for (int e = 0; e < 9; ++e) SS[e] = SS[e] * s;
+  }
+  double* Sig = o->sigma + 9 * i;
+  for (int e = 0; e < 9; ++e) Sig[e] = OI[e] * -o->pressure[i] + SS[e];
+  double *E = o->strain + 9 * i, *Eb = o->strainb + 9 * i;
+  memcpy(Stress, E, sizeof Stress);
+  if (ct == 30)
+    for (int e = 0; e < 9; ++e) E[e] = SR[e] * dt + E[e];
+  else
+    for (int e = 0; e < 9; ++e) E[e] = SR[e] * (2.0 * dt) + Eb[e];
+  memcpy(Eb, Stress, sizeof Stress);
+  if (o->fail[i] > 1) return fail(o, PSPH_ERR_INVALID_ARGUMENT, "Undefined failure criteria for solids");
+  return PSPH_OK;
+}
+
+/* Drucker-Prager constants (Particle.cpp:344-356 / :665-675). */
+static void dp_constants(const psph_oracle* o, int64_t i, double* alpha, double* kf) {
+  const double phi = o->phi[i], c = o->cohesion[i];
+  if (o->I[8] == 0.0) {
+    *alpha = tan(phi) / sqrt(9.0 + 12.0 * tan(phi) * tan(phi));
+    *kf = 3.0 * c / sqrt(9.0 + 12.0 * tan(phi) * tan(phi));
+  } else {
+    *alpha = (2.0 * sin(phi)) / (sqrt(3.0) * (3.0 - sin(phi)));
+    *kf = (6.0 * c * cos(phi)) / (sqrt(3.0) * (3.0 - sin(phi)));
+  }
+}
+
+/* Bring a stress back to the apex of the yield cone (Particle.cpp:359-368). */
+static double dp_apex(double* S, double alpha, double kf) {
+  double I1 = S[0] + S[4] + S[8];
+  if ((kf - alpha * I1) < 0.0) {
+    double Ratio = (alpha == 0.0) ? 0.0 : kf / alpha;
+    S[0] -= 1.0 / 3.0 * (I1 - Ratio);
+    S[4] -= 1.0 / 3.0 * (I1 - Ratio);
+    S[8] -= 1.0 / 3.0 * (I1 - Ratio);
+    I1 = Ratio;
+  }
+  return I1;
+}
+
+static void deviator(const double* S, double I1, double* D) {
+  double s = 1.0 / 3.0 * I1;
+  for (int e = 0; e < 9; ++e) D[e] = S[e] - OI[e] * s;
+}
+
+/* Drucker-Prager plastic corrector + final scale-back, shared by Mat3Leapfrog
+ * (Particle.cpp:677-746) and Mat3MVerlet (:357-425). Sig is the elastic
+ * predictor (modified in place), Sn the stress at the start of the step,
+ * fac the step multiplier of the corrector (dt or 2dt). */
+static int dp_return(psph_oracle* o, int64_t i, double* Sig, const double* Sn, const double* SR, double I1strain,
+                     double fac) {
+  double alpha, kf, SS[9];
+  dp_constants(o, i, &alpha, &kf);
+  const double K = o->k_mod[i], G = o->g_mod[i];
+  double I1 = dp_apex(Sig, alpha, kf);
+  deviator(Sig, I1, SS);
+  double J2 = J2of(SS);
+  if ((sqrt(J2) + alpha * I1 - kf) > 0.0) {
+    deviator(Sn, Sn[0] + Sn[4] + Sn[8], SS);
+    J2 = J2of(SS);
+    if (sqrt(J2) > 0.0) {
+      double sum = 0.0, dLanda, Plastic[9];
+      for (int e = 0; e < 9; ++e) sum = (e == 0) ? SS[0] * SR[0] : sum + SS[e] * SR[e]; /* abab + sum */
+      const double gj = G / sqrt(J2);
+      if (o->fail[i] == 2) {
+        dLanda = 1.0 / (9.0 * alpha * alpha * K + G) * ((3.0 * alpha * K * I1strain) + (G / sqrt(J2)) * sum);
+        double s = 3.0 * alpha * K;
+        for (int e = 0; e < 9; ++e) Plastic[e] = o->I[e] * s + SS[e] * gj;
+      } else if (o->fail[i] == 3) {
+        dLanda = 1.0 / (9.0 * alpha * K * 3.0 * sin(o->psi[i]) + G) * ((3.0 * alpha * K * I1strain) + (G / sqrt(J2)) * sum);
+        double s = 3.0 * 3.0 * sin(o->psi[i]) * K;
+        for (int e = 0; e < 9; ++e) Plastic[e] = o->I[e] * s + SS[e] * gj;
+      } else
+        return fail(o, PSPH_ERR_INVALID_ARGUMENT, "Failure Type No is out of range");
+      for (int e = 0; e < 9; ++e) Sig[e] = Sig[e] - (Plastic[e] * dLanda) * fac;
+    }
+    I1 = dp_apex(Sig, alpha, kf);
+    deviator(Sig, I1, SS);
+    J2 = J2of(SS);
+    if ((sqrt(J2) + alpha * I1 - kf) > 0.0 && sqrt(J2) > 0.0) {
+      double s1 = I1 / 3.0, s2 = (kf - alpha * I1) / sqrt(J2);
+      for (int e = 0; e < 9; ++e) Sig[e] = OI[e] * s1 + SS[e] * s2;
+    }
+  }
+  memcpy(o->shear_stress + 9 * i, SS, sizeof SS); /* Particle::ShearStress keeps the last deviator */
+  return PSPH_OK;
+}
+
+/* Mat3Leapfrog (Particle.cpp:641-795; porosity update out of scope) */
+static int mat3_leapfrog(psph_oracle* o, int64_t i, double dt) {
+  double *Sig = o->sigma + 9 * i, *Sa = o->sigmaa + 9 * i, *Sb = o->sigmab + 9 * i;
+  const double *SR = o->strain_rate + 9 * i, *RR = o->rotation_rate + 9 * i;
+  double X[9];
+  mat3_rate(SR, RR, Sig, o->k_mod[i], o->g_mod[i], X);
+  const double I1strain = SR[0] + SR[4] + SR[8];
+  if (o->it.first_step)
+    for (int e = 0; e < 9; ++e) Sa[e] = X[e] * (-dt / 2.0) + Sig[e];
+  for (int e = 0; e < 9; ++e) Sb[e] = Sa[e];
+  for (int e = 0; e < 9; ++e) Sa[e] = X[e] * dt + Sa[e];
+  if (o->fail[i] > 1) {
+    int st = dp_return(o, i, Sa, Sig, SR, I1strain, dt);
+    if (st) return st;
+  }
+  for (int e = 0; e < 9; ++e) Sig[e] = (Sa[e] + Sb[e]) * (1.0 / 2.0);
+  double *E = o->strain + 9 * i, *Ea = o->straina + 9 * i, *Eb = o->strainb + 9 * i;
+  if (o->it.first_step)
+    for (int e = 0; e < 9; ++e) Ea[e] = SR[e] * (-dt / 2.0) + E[e];
+  for (int e = 0; e < 9; ++e) Eb[e] = Ea[e];
+  for (int e = 0; e < 9; ++e) Ea[e] = SR[e] * dt + Ea[e];
+  for (int e = 0; e < 9; ++e) E[e] = (Ea[e] + Eb[e]) * (1.0 / 2.0);
+  return PSPH_OK;
+}
+
+/* Mat3MVerlet (Particle.cpp:320-482; porosity update out of scope) */
+static int mat3_mverlet(psph_oracle* o, int64_t i, double dt, int ct) {
+  double *Sig = o->sigma + 9 * i, *Sb = o->sigmab + 9 * i;
+  const double *SR = o->strain_rate + 9 * i, *RR = o->rotation_rate + 9 * i;
+  double X[9], Stress[9];
+  mat3_rate(SR, RR, Sig, o->k_mod[i], o->g_mod[i], X);
+  const double I1strain = SR[0] + SR[4] + SR[8];
+  memcpy(Stress, Sig, sizeof Stress);
+  if (ct == 30)
+    for (int e = 0; e < 9; ++e) Sig[e] = X[e] * dt + Sig[e];
+  else
+    for (int e = 0; e < 9; ++e) Sig[e] = X[e] * (2.0 * dt) + Sb[e];
+  memcpy(Sb, Stress, sizeof Stress);
+  if (o->fail[i] > 1) {
+    int st = dp_return(o, i, Sig, Stress, SR, I1strain, (ct == 30) ? dt : 2.0 * dt);
+    if (st) return st;
+  }
+  double *E = o->strain + 9 * i, *Eb = o->strainb + 9 * i;
+  memcpy(Stress, E, sizeof Stress);
+  if (ct == 30)
+    for (int e = 0; e < 9; ++e) E[e] = SR[e] * dt + E[e];
+  else
+    for (int e = 0; e < 9; ++e) E[e] = SR[e] * (2.0 * dt) + Eb[e];
+  memcpy(Eb, Stress, sizeof Stress);
+  return PSPH_OK;
+}
+
+/* Domain::Move (Source/Domain.cpp:1299-1325) -> Particle::Move (Particle.cpp:119-144)
+ * -> Move_MVerlet (:189-274) | Move_Leapfrog (:561-596). The per-particle
+ * counters are advanced once for the domain afterwards. */
+static int move(psph_oracle* o, int nthr) {
+  const double dt = o->it.deltat;
+  const int ct = o->it.ct;
+  const int shep_now = (o->it.shepard_counter == o->cfg.shepard_step);
+  int status = PSPH_OK;
+#pragma omp parallel for schedule(static) num_threads(nthr)
+  for (int64_t i = 0; i < o->n; i++) {
+    if (!FREE(i)) continue;
+    double* x = o->x + 3 * i;
+    double* v = o->v + 3 * i;
+    const double* a = o->a + 3 * i;
+    if (o->cfg.scheme == PSPH_MVERLET) {
+      const double* vx = o->vxsph + 3 * i;
+      for (int d = 0; d < 3; ++d) x[d] += dt * (v[d] + vx[d]) + 0.5 * dt * dt * a[d];
+      const int shep = o->shepard[i] && shep_now;
+      if (ct == 30) {
+        if (shep && o->zwab[i] > 0.6) {
+          o->densityb[i] = o->sumden[i] / o->zwab[i];
+          o->density[i] = o->sumden[i] / o->zwab[i];
+        } else {
+          o->densityb[i] = o->density[i];
+          o->density[i] += dt * o->ddensity[i];
+        }
+        double* vb = o->vb + 3 * i;
+        for (int d = 0; d < 3; ++d) {
+          vb[d] = v[d];
+          v[d] += dt * a[d];
+        }
+      } else {
+        if (shep && o->zwab[i] > 0.6) {
+          o->densityb[i] = o->sumden[i] / o->zwab[i];
+          o->density[i] = o->sumden[i] / o->zwab[i];
+        } else {
+          double dens = o->density[i];
+          o->density[i] = o->densityb[i] + 2.0 * dt * o->ddensity[i];
+          o->densityb[i] = dens;
+        }
+        double* vb = o->vb + 3 * i;
+        for (int d = 0; d < 3; ++d) {
+          double t = v[d];
+          v[d] = vb[d] + 2 * dt * a[d];
+          vb[d] = t;
+        }
+      }
+      int st = PSPH_OK;
+      switch (o->material[i]) {
+        case 1: mat1(o, i); break;
+        case 2: st = mat2_mverlet(o, i, dt, ct); break;
+        default: st = mat3_mverlet(o, i, dt, ct); break;
+      }
+      if (st) status = st;
+    } else {
+      double* va = o->va + 3 * i;
+      double* vb = o->vb + 3 * i;
+      if (o->it.first_step) {
+        o->densitya[i] = o->density[i] - dt / 2.0 * o->ddensity[i];
+        for (int d = 0; d < 3; ++d) va[d] = v[d] - dt / 2.0 * a[d];
+      }
+      o->densityb[i] = o->densitya[i];
+      o->densitya[i] += dt * o->ddensity[i];
+      o->density[i] = (o->densitya[i] + o->densityb[i]) / 2.0;
+      for (int d = 0; d < 3; ++d) {
+        vb[d] = va[d];
+        va[d] += dt * a[d];
+        v[d] = (va[d] + vb[d]) / 2.0;
+        x[d] += dt * va[d];
+      }
+      int st = PSPH_OK;
+      switch (o->material[i]) {
+        case 1: mat1(o, i); break;
+        case 2: st = mat2_leapfrog(o, i, dt); break;
+        default: st = mat3_leapfrog(o, i, dt); break;
+      }
+      if (st) status = st;
+    }
+    /* periodic wrap (Particle.cpp:128-142) */
+    for (int d = 0; d < 3; ++d)
+      if (o->g.dom_size[d] > 0.0) {
+        if (x[d] > o->g.trpr[d]) x[d] -= o->g.dom_size[d];
+        if (x[d] < o->g.blpf[d]) x[d] += o->g.dom_size[d];
+      }
+  }
+  if (status) return status;
+  if (o->cfg.scheme == PSPH_MVERLET) {
+    o->it.ct = (o->it.ct == 30) ? 0 : o->it.ct + 1;
+    o->it.shepard_counter = (o->it.shepard_counter == o->cfg.shepard_step) ? 0 : o->it.shepard_counter + 1;
+  }
+  o->it.first_step = 0;
+  return PSPH_OK;
+}
+
+/* CheckParticleLeave (Source/Domain.cpp:517-547): order-preserving removal. */
+static void check_particle_leave(psph_oracle* o) {
+  int64_t k = 0;
+  for (int64_t i = 0; i < o->n; ++i) {
+    const double* x = o->x + 3 * i;
+    int out = 0;
+    for (int d = 0; d < 3; ++d) out |= (x[d] > o->g.trpr[d]) || (x[d] < o->g.blpf[d]);
+    if (out) continue;
+    if (k != i) {
+#define MOVE_I(NAME) o->NAME[k] = o->NAME[i];
+#define MOVE_D(NAME) o->NAME[k] = o->NAME[i];
+#define MOVE_V(NAME) memmove(o->NAME + 3 * k, o->NAME + 3 * i, 3 * sizeof(double));
+#define MOVE_T(NAME) memmove(o->NAME + 9 * k, o->NAME + 9 * i, 9 * sizeof(double));
+      PSPH_INT_FIELDS(MOVE_I)
+      PSPH_F64_FIELDS(MOVE_D)
+      PSPH_VEC_FIELDS(MOVE_V)
+      PSPH_TEN_FIELDS(MOVE_T)
+      o->orig[k] = o->orig[i];
+    }
+    k++;
+  }
+  o->n = k;
+}
+
+static int one_step(psph_oracle* o, int nthr) {
+  double t0 = now_s();
+  start_acceleration(o, nthr);
+  /* FirstStep of Move_MVerlet forces ct=30 (Particle.cpp:191-195) */
+  if (o->cfg.scheme == PSPH_MVERLET && o->it.first_step) o->it.ct = 30;
+  main_search(o, nthr);
+  double t1 = now_s();
+  primary_compute(o, nthr);
+  double t2 = now_s();
+  int st = last_compute(o, nthr);
+  if (st) return st;
+  double t3 = now_s();
+  st = adaptive_time_step(o);
+  if (st) return st;
+  st = move(o, nthr);
+  if (st) return st;
+  o->it.time += o->it.deltat;
+  o->it.steps += 1;
+  double t4 = now_s();
+  check_particle_leave(o);
+  cell_reset(o);
+  st = list_generate(o);
+  double t5 = now_s();
+  o->phase_s[0] += t1 - t0;
+  o->phase_s[1] += t2 - t1;
+  o->phase_s[2] += t3 - t2;
+  o->phase_s[3] += t4 - t3;
+  o->phase_s[4] += t5 - t4;
+  return st;
+}
+
+/* ---------------------------------------------------------------------------
+ * Public entry points
+ * ------------------------------------------------------------------------- */
+
+static int validate(psph_oracle* o) {
+  const psph_config* c = &o->cfg;
+  if (c->dimension != 2 && c->dimension != 3) return fail(o, PSPH_ERR_INVALID_ARGUMENT, "Please correct the dimension (2=>2D or 3=>3D)");
+  if (c->kernel_type < 0 || c->kernel_type > 2) return fail(o, PSPH_ERR_INVALID_ARGUMENT, "Kernel Type No is out of range");
+  if (c->vis_eq < 0 || c->vis_eq > 3) return fail(o, PSPH_ERR_INVALID_ARGUMENT, "Viscosity Equation No is out of range");
+  if (c->swi_type != 0) return fail(o, PSPH_ERR_UNSUPPORTED, "soil-water interaction is outside this build");
+  for (int64_t i = 0; i < o->n; ++i) {
+    if (o->material[i] < 1 || o->material[i] > 3) return fail(o, PSPH_ERR_INVALID_ARGUMENT, "Material Type No is out of range");
+    if (o->pres_eq[i] < 0 || o->pres_eq[i] > 2) return fail(o, PSPH_ERR_INVALID_ARGUMENT, "Please correct Pressure Equation No");
+  }
+  return PSPH_OK;
+}
+
+psph_oracle* psph_oracle_create(const psph_config* cfg, const psph_particles* p, int initial, const psph_grid* grid,
+                                const psph_integrator* integ) {
+  psph_oracle* o = (psph_oracle*)calloc(1, sizeof(psph_oracle));
+  o->cfg = *cfg;
+  const int64_t n = p->n;
+  o->n = n;
+#define ALLOC_I(NAME) o->NAME = (int32_t*)calloc((size_t)(n ? n : 1), sizeof(int32_t));
+#define ALLOC_D(NAME) o->NAME = (double*)calloc((size_t)(n ? n : 1), sizeof(double));
+#define ALLOC_V(NAME) o->NAME = (double*)calloc((size_t)(n ? n : 1) * 3, sizeof(double));
+#define ALLOC_T(NAME) o->NAME = (double*)calloc((size_t)(n ? n : 1) * 9, sizeof(double));
+  PSPH_INT_FIELDS(ALLOC_I)
+  PSPH_F64_FIELDS(ALLOC_D)
+  PSPH_VEC_FIELDS(ALLOC_V)
+  PSPH_TEN_FIELDS(ALLOC_T)
+  /* Particle constructor defaults (Source/Particle.cpp:25-117) */
+  for (int64_t i = 0; i < n; ++i) {
+    o->is_free[i] = 1;
+    o->fpmassc[i] = 1.0;
+    o->bingham_m[i] = 300.0;
+    o->csmag[i] = 0.17;
+    o->tin[i] = 4.0;
+  }
+#define COPY_I(NAME) if (p->NAME) memcpy(o->NAME, p->NAME, (size_t)n * sizeof(int32_t));
+#define COPY_D(NAME) if (p->NAME) memcpy(o->NAME, p->NAME, (size_t)n * sizeof(double));
+#define COPY_V(NAME) if (p->NAME) memcpy(o->NAME, p->NAME, (size_t)n * 3 * sizeof(double));
+#define COPY_T(NAME) if (p->NAME) memcpy(o->NAME, p->NAME, (size_t)n * 9 * sizeof(double));
+  PSPH_INT_FIELDS(COPY_I)
+  PSPH_F64_FIELDS(COPY_D)
+  PSPH_VEC_FIELDS(COPY_V)
+  PSPH_TEN_FIELDS(COPY_T)
+  if (!p->ref_density && p->density) memcpy(o->ref_density, p->density, (size_t)n * sizeof(double));
+  o->orig = (int64_t*)malloc((size_t)(n ? n : 1) * sizeof(int64_t));
+  for (int64_t i = 0; i < n; ++i) o->orig[i] = i;
+  o->LL = (int32_t*)malloc((size_t)(n ? n : 1) * sizeof(int32_t));
+  o->CC = (int32_t*)calloc((size_t)(n ? n : 1) * 3, sizeof(int32_t));
+  o->fixed = (int64_t*)malloc((size_t)(n ? n : 1) * sizeof(int64_t));
+  o->a_scale = (double*)calloc((size_t)(n ? n : 1), sizeof(double));
+  o->dr_scale = (double*)calloc((size_t)(n ? n : 1), sizeof(double));
+  o->locks = (omp_lock_t*)malloc((size_t)(n ? n : 1) * sizeof(omp_lock_t));
+  for (int64_t i = 0; i < n; ++i) omp_init_lock(&o->locks[i]);
+  o->nthr = omp_get_max_threads() > 0 ? omp_get_max_threads() : 1;
+  if (o->nthr < 256) o->nthr = 256;
+  o->sm = (pairvec*)calloc(o->nthr, sizeof(pairvec));
+  o->fsm = (pairvec*)calloc(o->nthr, sizeof(pairvec));
+  o->nsm = (pairvec*)calloc(o->nthr, sizeof(pairvec));
+  for (int e = 0; e < 9; ++e) o->I[e] = OI[e];
+  if (cfg->dimension == 2) o->I[8] = 0.0;
+  o->g.cellfac = (cfg->kernel_type == 2) ? 3.0 : 2.0; /* Kernel_Set (Source/Domain.cpp:117-121) */
+  o->it.time = cfg->time;
+  o->it.deltat = o->it.deltatint = o->it.deltatmin = cfg->dt;
+  o->it.first_step = 1;
+  if (validate(o)) return o;
+  if (integ) o->it = *integ;
+  if (initial) {
+    /* InitialChecks (Source/Domain.cpp:1662-1678): initial EOS pressure */
+    for (int64_t i = 0; i < n; i++)
+      if (o->material[i] < 3) o->pressure[i] = EOS(o->pres_eq[i], o->cs[i], o->p0[i], o->density[i], o->ref_density[i]);
+  }
+  if (grid) {
+    o->g = *grid;
+  } else if (cell_initiate(o)) {
+    return o;
+  }
+  if (alloc_cells(o)) return o;
+  if (list_generate(o)) return o;
+  if (initial && !grid) {
+    /* TimestepCheck (Source/Domain.cpp:1721-1733) */
+    double t1 = 0.25 * o->g.hmax / (o->cs_max), t2;
+    if (o->mu_max > 0.0) t2 = 0.125 * o->g.hmax * o->g.hmax * o->g.rhomax / o->mu_max; else t2 = 1000000.0;
+    if (o->it.deltatint > (t1 < t2 ? t1 : t2)) fail(o, PSPH_ERR_CFL, "Please decrease the time step to the allowable range");
+  }
+  return o;
+}
+
+void psph_oracle_destroy(psph_oracle* o) {
+  if (!o) return;
+#define FREE_F(NAME) free(o->NAME);
+  PSPH_INT_FIELDS(FREE_F)
+  PSPH_F64_FIELDS(FREE_F)
+  PSPH_VEC_FIELDS(FREE_F)
+  PSPH_TEN_FIELDS(FREE_F)
+  for (int64_t i = 0; i < o->n; ++i) omp_destroy_lock(&o->locks[i]);
+  for (int t = 0; t < o->nthr; ++t) {
+    free(o->sm[t].v);
+    free(o->fsm[t].v);
+    free(o->nsm[t].v);
+  }
+  free(o->sm);
+  free(o->fsm);
+  free(o->nsm);
+  free(o->orig);
+  free(o->LL);
+  free(o->CC);
+  free(o->HOC);
+  free(o->fixed);
+  free(o->a_scale);
+  free(o->dr_scale);
+  free(o->locks);
+  free(o);
+}
+
+const char* psph_oracle_error(const psph_oracle* o) { return o->status ? o->err : ""; }
+
+int psph_oracle_step(psph_oracle* o, int64_t nsteps, int nthreads) {
+  if (o->status) return o->status;
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > o->nthr) nthreads = o->nthr;
+  for (int e = 0; e < 5; ++e) o->phase_s[e] = 0.0;
+  for (int64_t s = 0; s < nsteps; ++s) {
+    int st = one_step(o, nthreads);
+    if (st) return fail(o, st, "%s", o->err[0] ? o->err : "step failed");
+  }
+  return PSPH_OK;
+}
+
+int64_t psph_oracle_num_particles(const psph_oracle* o) { return o->n; }
+
+int psph_oracle_download(const psph_oracle* o, psph_particles* out) {
+  const int64_t n = o->n;
+  if (out->n < n) return PSPH_ERR_INVALID_ARGUMENT;
+#define OUT_I(NAME) if (out->NAME) memcpy(out->NAME, o->NAME, (size_t)n * sizeof(int32_t));
+#define OUT_D(NAME) if (out->NAME) memcpy(out->NAME, o->NAME, (size_t)n * sizeof(double));
+#define OUT_V(NAME) if (out->NAME) memcpy(out->NAME, o->NAME, (size_t)n * 3 * sizeof(double));
+#define OUT_T(NAME) if (out->NAME) memcpy(out->NAME, o->NAME, (size_t)n * 9 * sizeof(double));
+  PSPH_INT_FIELDS(OUT_I)
+  PSPH_F64_FIELDS(OUT_D)
+  PSPH_VEC_FIELDS(OUT_V)
+  PSPH_TEN_FIELDS(OUT_T)
+  return PSPH_OK;
+}
+
+int psph_oracle_original_index(const psph_oracle* o, int64_t* out) {
+  memcpy(out, o->orig, (size_t)o->n * sizeof(int64_t));
+  return PSPH_OK;
+}
+
+int psph_oracle_get_grid(const psph_oracle* o, psph_grid* g) {
+  *g = o->g;
+  return PSPH_OK;
+}
+
+int psph_oracle_get_integrator(const psph_oracle* o, psph_integrator* it) {
+  *it = o->it;
+  return PSPH_OK;
+}
+
+int64_t psph_oracle_pairs(psph_oracle* o, int which, int64_t* buf, int64_t cap) {
+  if (o->status) return -1;
+  main_search(o, 1);
+  int64_t cnt = 0;
+  for (int k = 0; k < o->nthr; ++k) {
+    pairvec* lists[3] = {&o->sm[k], &o->fsm[k], &o->nsm[k]};
+    for (int l = 0; l < 3; ++l) {
+      if (which < 3 && l != which) continue;
+      for (int64_t i = 0; i < lists[l]->n; ++i) {
+        int64_t p1 = lists[l]->v[2 * i], p2 = lists[l]->v[2 * i + 1];
+        if (which == 3) {
+          double xij[3];
+          for (int d = 0; d < 3; ++d) xij[d] = o->x[3 * p1 + d] - o->x[3 * p2 + d];
+          double h = (o->h[p1] + o->h[p2]) / 2;
+          periodic_correction(o, xij, h, p1, p2);
+          if (sqrt(dot3(xij, xij)) / h > o->g.cellfac) continue;
+        }
+        if (cnt < cap) {
+          buf[2 * cnt] = o->orig[p1];
+          buf[2 * cnt + 1] = o->orig[p2];
+        }
+        cnt++;
+      }
+    }
+  }
+  for (int t = 0; t < o->nthr; ++t) o->sm[t].n = o->fsm[t].n = o->nsm[t].n = 0;
+  return cnt;
+}
+
+int psph_oracle_scales(const psph_oracle* o, double* a_scale, double* drho_scale) {
+  memcpy(a_scale, o->a_scale, (size_t)o->n * sizeof(double));
+  memcpy(drho_scale, o->dr_scale, (size_t)o->n * sizeof(double));
+  return PSPH_OK;
+}
+
+int psph_oracle_phase_times(const psph_oracle* o, double* s, int cap) {
+  for (int e = 0; e < 5 && e < cap; ++e) s[e] = o->phase_s[e];
+  return 5;
+}

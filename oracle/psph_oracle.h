@@ -1,0 +1,61 @@
+/*
+ * CPU restatement of PersianSPH's per-step hot path: the parity ORACLE.
+ *
+ * TEST INFRASTRUCTURE ONLY. Only tests/, __graft_entry__.smoke() and bench.py's
+ * CPU-baseline / reference legs may load it, and only as the checker or as the
+ * timed CPU implementation of the reference algorithm; the GPU product never
+ * calls it. It shares the boundary's plain-C structures (include/psph.h) so a
+ * test can feed the same particles to both sides.
+ *
+ * Pinning: the restatement is checked against the unmodified reference built
+ * here (oracle/build_ref.sh -> oracle/_ref/ref_driver) through the committed
+ * fixtures in tests/golden/ (generated by tests/golden/make_golden.py).
+ */
+#ifndef PSPH_ORACLE_H
+#define PSPH_ORACLE_H
+
+#include "psph.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct psph_oracle psph_oracle;
+
+/* initial != 0: Solve's set-up (InitialChecks, CellInitiate, ListGenerate).
+ * grid / integ (may be NULL) continue from a saved state instead. */
+psph_oracle* psph_oracle_create(const psph_config* cfg, const psph_particles* p, int initial,
+                                const psph_grid* grid, const psph_integrator* integ);
+void psph_oracle_destroy(psph_oracle* o);
+const char* psph_oracle_error(const psph_oracle* o);
+
+/* nsteps of Solve's loop body with nthreads OpenMP threads (1 = the reference's
+ * deterministic Nproc=1 order). Returns a psph_status. */
+int psph_oracle_step(psph_oracle* o, int64_t nsteps, int nthreads);
+
+int64_t psph_oracle_num_particles(const psph_oracle* o);
+int psph_oracle_download(const psph_oracle* o, psph_particles* out);
+/* original index of each surviving particle */
+int psph_oracle_original_index(const psph_oracle* o, int64_t* out);
+int psph_oracle_get_grid(const psph_oracle* o, psph_grid* g);
+int psph_oracle_get_integrator(const psph_oracle* o, psph_integrator* it);
+
+/* Pair lists of the NEXT step's neighbour search from the current state, as
+ * original indices (first, second): which 0 = SM, 1 = FSM, 2 = NSM, 3 = the
+ * in-support subset of all three. Returns the count (<0 on error). */
+int64_t psph_oracle_pairs(psph_oracle* o, int which, int64_t* buf, int64_t cap);
+
+/* Per-particle magnitude of the sums behind the last step's acceleration and
+ * density rate: |g| + |body force| + sum_j |m_j F_ij|, and sum_j |m_j (di/dj) v.gradW|.
+ * Tests scale their per-particle tolerance by these. */
+int psph_oracle_scales(const psph_oracle* o, double* a_scale, double* drho_scale);
+
+/* Wall time (s) of the phases of the last psph_oracle_step call: search,
+ * wall interpolation, pair forces, update, relist; returns the count. */
+int psph_oracle_phase_times(const psph_oracle* o, double* s, int cap);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,172 @@
+"""ctypes mirror of the C ABI in include/psph.h.
+
+The structures here must match include/psph.h field for field; the ABI tests
+check the sizes against the compiled library. `load_library()` loads the CUDA
+library built in-tree by `persiansph_gb300.build` and fails loudly when it is
+missing: there is no CPU fallback behind this API.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+# Field lists in include/psph.h order.
+INT_FIELDS = ("id", "material", "is_free", "no_slip", "pres_eq", "shepard", "les", "vis_m", "fail")
+VEC_FIELDS = ("x", "v", "va", "vb", "a", "nsv", "vxsph")
+F64_FIELDS = (
+    "density", "densitya", "densityb", "ddensity", "pressure", "mass", "h", "cs", "p0", "ref_density",
+    "fpmassc", "alpha", "beta", "mu", "mu_ref", "t0", "bingham_m", "csmag", "ti", "tin", "ti_init_dist",
+    "g_mod", "k_mod", "sigmay", "cohesion", "phi", "psi", "zwab", "sumden", "sumkernel", "shear_rate", "sbar",
+)
+TEN_FIELDS = (
+    "sigma", "sigmaa", "sigmab", "shear_stress", "shear_stressa", "shear_stressb", "strain", "straina",
+    "strainb", "strain_rate", "rotation_rate", "tir",
+)
+ALL_FIELDS = INT_FIELDS + VEC_FIELDS + F64_FIELDS + TEN_FIELDS
+
+# status codes (psph_status)
+PSPH_OK = 0
+STATUS_NAMES = {
+    0: "PSPH_OK", 1: "PSPH_ERR_INVALID_ARGUMENT", 2: "PSPH_ERR_UNSUPPORTED", 3: "PSPH_ERR_CUDA",
+    4: "PSPH_ERR_OUT_OF_MEMORY", 5: "PSPH_ERR_NONFINITE", 6: "PSPH_ERR_DT_COLLAPSE", 7: "PSPH_ERR_CFL",
+    8: "PSPH_ERR_CELL_OVERFLOW", 9: "PSPH_ERR_NO_DEVICE", 10: "PSPH_ERR_STATE", 11: "PSPH_ERR_NOT_FOUND",
+}
+
+
+class PsphConfig(C.Structure):
+    _fields_ = [
+        ("dimension", C.c_int32), ("kernel_type", C.c_int32), ("vis_eq", C.c_int32),
+        ("gradient_type", C.c_int32), ("scheme", C.c_int32), ("periodic", C.c_int32 * 3),
+        ("swi_type", C.c_int32), ("shepard_step", C.c_int32), ("precision", C.c_int32),
+        ("wall_pressure_mode", C.c_int32), ("gravity", C.c_double * 3), ("body_force", C.c_double * 3),
+        ("xsph", C.c_double), ("sqrt_h_a", C.c_double), ("R", C.c_double), ("dom_max", C.c_double * 3),
+        ("dom_min", C.c_double * 3), ("dt", C.c_double), ("time", C.c_double), ("reserved", C.c_int32 * 8),
+    ]
+
+
+class PsphGrid(C.Structure):
+    _fields_ = [
+        ("blpf", C.c_double * 3), ("trpr", C.c_double * 3), ("cell_size", C.c_double * 3),
+        ("dom_size", C.c_double * 3), ("hmax", C.c_double), ("rhomax", C.c_double), ("cellfac", C.c_double),
+        ("cell_no", C.c_int32 * 3), ("pad", C.c_int32),
+    ]
+
+
+class PsphIntegrator(C.Structure):
+    _fields_ = [
+        ("time", C.c_double), ("deltat", C.c_double), ("deltatint", C.c_double), ("deltatmin", C.c_double),
+        ("steps", C.c_int64), ("first_step", C.c_int32), ("ct", C.c_int32), ("shepard_counter", C.c_int32),
+        ("pad", C.c_int32),
+    ]
+
+
+class PsphParticles(C.Structure):
+    _fields_ = (
+        [("n", C.c_int64)]
+        + [(f, C.POINTER(C.c_int32)) for f in INT_FIELDS]
+        + [(f, C.POINTER(C.c_double)) for f in VEC_FIELDS]
+        + [(f, C.POINTER(C.c_double)) for f in F64_FIELDS]
+        + [(f, C.POINTER(C.c_double)) for f in TEN_FIELDS]
+    )
+
+
+def field_shape(name: str, n: int):
+    if name in VEC_FIELDS:
+        return (n, 3)
+    if name in TEN_FIELDS:
+        return (n, 3, 3)
+    return (n,)
+
+
+def field_dtype(name: str):
+    return np.int32 if name in INT_FIELDS else np.float64
+
+
+def particles_struct(arrays: dict, n: int, fields=None) -> PsphParticles:
+    """Builds a PsphParticles pointing into numpy arrays (kept alive by the caller).
+
+    Arrays must be C-contiguous with the dtype/shape of `field_shape`; a field
+    missing from `arrays` (or not in `fields`) is passed as NULL.
+    """
+    s = PsphParticles()
+    s.n = n
+    for f in ALL_FIELDS:
+        if fields is not None and f not in fields:
+            continue
+        arr = arrays.get(f)
+        if arr is None:
+            continue
+        if not arr.flags["C_CONTIGUOUS"] or arr.dtype != field_dtype(f) or arr.shape[0] < n:
+            raise ValueError(f"field {f}: need a C-contiguous {field_dtype(f).__name__} array of {n} rows")
+        ptype = C.POINTER(C.c_int32) if f in INT_FIELDS else C.POINTER(C.c_double)
+        setattr(s, f, arr.ctypes.data_as(ptype))
+    return s
+
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_NAME = "libpsph_gb300.so"
+
+
+def library_path() -> str:
+    return os.path.join(_HERE, "_build", LIB_NAME)
+
+
+_lib = None
+
+
+def load_library():
+    """Loads the in-tree CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"{path} is missing: build the CUDA library first "
+            "(python -c 'import __graft_entry__ as g; g.build()')")
+    lib = C.CDLL(path)
+    _declare(lib)
+    _lib = lib
+    return lib
+
+
+def _declare(lib):
+    P = C.POINTER
+    ctx = C.c_void_p
+    lib.psph_abi_version.restype = C.c_int
+    lib.psph_device_check.argtypes = [P(C.c_int)]
+    lib.psph_create.argtypes = [P(PsphConfig), P(ctx)]
+    lib.psph_destroy.argtypes = [ctx]
+    lib.psph_destroy.restype = None
+    lib.psph_last_error.argtypes = [ctx]
+    lib.psph_last_error.restype = C.c_char_p
+    lib.psph_set_stream.argtypes = [ctx, C.c_void_p]
+    lib.psph_set_grid.argtypes = [ctx, P(PsphGrid)]
+    lib.psph_set_integrator.argtypes = [ctx, P(PsphIntegrator)]
+    lib.psph_upload.argtypes = [ctx, P(PsphParticles), C.c_int]
+    lib.psph_step.argtypes = [ctx, C.c_int64, C.c_double, P(C.c_int64)]
+    lib.psph_num_particles.argtypes = [ctx]
+    lib.psph_num_particles.restype = C.c_int64
+    lib.psph_download.argtypes = [ctx, P(PsphParticles)]
+    lib.psph_get_grid.argtypes = [ctx, P(PsphGrid)]
+    lib.psph_get_integrator.argtypes = [ctx, P(PsphIntegrator)]
+    lib.psph_pairs_export.argtypes = [ctx, C.c_int, P(C.c_int64), C.c_int64, P(C.c_int64)]
+    lib.psph_enable_timing.argtypes = [ctx, C.c_int]
+    lib.psph_phase_times.argtypes = [ctx, P(C.c_double), C.c_int, P(C.c_int)]
+    lib.psph_last_launch_count.argtypes = [ctx]
+    lib.psph_last_launch_count.restype = C.c_int64
+    for name in ("psph_device_check", "psph_create", "psph_set_stream", "psph_set_grid", "psph_set_integrator",
+                 "psph_upload", "psph_step", "psph_download", "psph_get_grid", "psph_get_integrator",
+                 "psph_pairs_export", "psph_enable_timing", "psph_phase_times"):
+        getattr(lib, name).restype = C.c_int
+
+
+class PsphError(RuntimeError):
+    """A non-zero psph_status, carrying the library's message (the reference
+    throws `Fatal` at these points)."""
+
+    def __init__(self, code: int, message: str):
+        self.code = code
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {message}")

@@ -1,0 +1,265 @@
+"""Workload builders with the shapes of the benchmarked configurations.
+
+Each builder fills a `Domain` through the reference's own API
+(AddBoxLength + per-particle fields + DelParticles), the way the reference's
+example drivers do, with sizes parameterised so tests can run them small:
+
+  poiseuille      2D periodic channel (1-Poiseuille.cpp shape)
+  dam_break_2d    2D water column in a tank (3-DamBreak.cpp shape)
+  dam_break_3d    3D water column in a tank (4-DamBreak3D.cpp shape)
+  granular_column 2D Drucker-Prager soil column (Old_Tests/ReposeAngle2.cpp shape)
+
+All inputs are synthetic and seeded; the reference ships no datasets.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .domain import Domain, Morris, Qubic_Spline, Quintic, Quintic_Spline, Squared_density
+
+
+def poiseuille(dx=2.5e-5, H=1.0e-3, W=0.5e-3, wall_layers=3, rho=1000.0, nu=1.0e-6, gx=1.0e-4,
+               scheme=1, kernel=Quintic_Spline, hfac=1.3):
+    """2D Poiseuille flow between no-slip walls, periodic in x.
+
+    Umax = gx H^2 / (8 nu); c0 = 10 Umax; dt = min(0.25 h/c0, 0.125 h^2/nu)
+    (the second bound is TimestepCheck's viscous limit, Source/Domain.cpp:1724-1732).
+    Returns (domain, dt, info).
+    """
+    dom = Domain()
+    dom.Dimension = 2
+    dom.BC.Periodic[0] = True
+    dom.Scheme = scheme
+    dom.Kernel_Set(kernel)
+    dom.Viscosity_Eq_Set(Morris)
+    dom.Gradient_Approach_Set(Squared_density)
+    h = hfac * dx
+    mu = nu * rho
+    umax = gx * H * H / (8.0 * nu)
+    cs = 10.0 * umax
+    nrow = int(round(H / dx))
+    ncol = int(round(W / dx))
+    half = nrow // 2
+    dom.InitialDist = dx
+    dom.AddBoxLength(1, (0.0, -(half + wall_layers) * dx, 0.0), ncol * dx + dx / 10.0,
+                     (nrow + 2 * wall_layers) * dx + dx / 10.0, 0, dx / 2.0, rho, h, 1, 0, False, False)
+    p = dom.particles
+    y = p.get("x")[:, 1]
+    wall = (y >= half * dx) | (y <= -half * dx)
+    p.set("cs", cs)
+    p.set("pres_eq", 0)
+    p.set("mu", mu)
+    p.set("mu_ref", mu)
+    p.set("material", 1)
+    p.get("id")[wall] = 2
+    p.get("is_free")[wall] = 0
+    p.get("no_slip")[wall] = 1
+    dom.BodyForce = [gx, 0.0, 0.0]
+    dt = min(0.25 * h / cs, 0.125 * h * h / nu)
+    return dom, dt, {"umax": umax, "cs": cs, "H": H, "nu": nu, "gx": gx, "h": h}
+
+
+def _tank(dom, dx, TL, TH, TW, wall_layers):
+    """Lattice box covering the tank plus its wall layers (cubic packing)."""
+    w = wall_layers
+    if dom.Dimension == 2:
+        dom.AddBoxLength(1, (-w * dx, -w * dx, 0.0), 2 * w * dx + TL + dx / 10.0, w * dx + TH + dx / 10.0, 0,
+                         dx / 2.0, 1.0, 1.0, 1, 0, False, False)
+    else:
+        dom.AddBoxLength(1, (-w * dx, -w * dx, -w * dx), 2 * w * dx + TL + dx / 10.0, w * dx + TH + dx / 10.0,
+                         2 * w * dx + TW + dx / 10.0, dx / 2.0, 1.0, 1.0, 1, 0, False, False)
+
+
+def dam_break_2d(dx=5e-3, L=1.0, H=2.0, TL=4.0, TH=3.0, wall_layers=3, rho=1000.0, g=9.81, alpha=0.1,
+                 mu=1.002e-3, scheme=0, shepard=True, kernel=Qubic_Spline, hfac=1.2, c0=None):
+    """2D dam break: an L x H water column at the left of a TL x TH tank.
+
+    Tait EOS (gamma 7) with c0 = 10 sqrt(2 g H) unless given, hydrostatic initial
+    density as 3-DamBreak.cpp:95-99. Returns (domain, dt, info).
+    """
+    dom = Domain()
+    dom.Dimension = 2
+    dom.Scheme = scheme
+    dom.Kernel_Set(kernel)
+    dom.Viscosity_Eq_Set(Morris)
+    dom.Gradient_Approach_Set(Squared_density)
+    h = hfac * dx
+    cs = 10.0 * math.sqrt(2.0 * g * H) if c0 is None else c0
+    dom.InitialDist = dx
+    dom.Gravity = [0.0, -g, 0.0]
+    _tank(dom, dx, TL, TH, 0.0, wall_layers)
+    p = dom.particles
+    x = p.get("x")
+    xb, yb = x[:, 0], x[:, 1]
+    wall = (xb < 0.0) | (yb < 0.0) | (xb > TL)
+    drop = (~wall) & ((yb > H) | (xb > L))
+    keep = ~drop
+    p.keep(keep)
+    x = p.get("x")
+    xb, yb = x[:, 0], x[:, 1]
+    wall = (xb < 0.0) | (yb < 0.0) | (xb > TL)
+    _fluid_fields(p, wall, rho, cs, mu, alpha, shepard, h)
+    fl = ~wall
+    dens = rho * np.power((1 + 7.0 * g * (H - yb[fl]) / (cs * cs)), (1.0 / 7.0))
+    p.get("density")[fl] = dens
+    p.get("densityb")[fl] = dens
+    p.set("mass", 2.0 * (dx / 2.0) * 2.0 * (dx / 2.0) * rho)
+    dt = 0.25 * h / cs
+    return dom, dt, {"cs": cs, "H": H, "L": L, "g": g, "h": h, "n_fluid": int(fl.sum()), "n_wall": int(wall.sum())}
+
+
+def _fluid_fields(p, wall, rho, cs, mu, alpha, shepard, h):
+    n = p.n
+    p.set("h", h)
+    p.set("density", rho)
+    p.set("ref_density", rho)
+    p.set("cs", cs)
+    p.set("pres_eq", 1)
+    p.set("mu", mu)
+    p.set("mu_ref", mu)
+    p.set("material", 1)
+    p.set("alpha", alpha)
+    p.set("shepard", 1 if shepard else 0)
+    ids = np.ones(n, np.int32)
+    ids[wall] = 2
+    p.set("id", ids)
+    p.set("is_free", (~wall).astype(np.int32))
+    p.set("no_slip", wall.astype(np.int32))
+
+
+def dam_break_3d(dx=5e-3, L=1.2, H=0.55, W=1.0, TL=3.22, TH=1.0, TW=1.0, wall_layers=3, rho=1000.0, g=9.81,
+                 alpha=0.05, mu=1.002e-3, c0=40.0, scheme=0, shepard=True, kernel=Quintic, hfac=1.3):
+    """3D dam break: L (x) x H (y, up) x W (z) column in a TL x TH x TW tank.
+
+    Built directly on the cubic lattice AddBoxLength would produce for the
+    whole tank (4-DamBreak3D.cpp shape) without materialising the dropped
+    particles; particle mass is that box's dx^3 rho rule (Source/Domain.cpp:399-415).
+    Returns (domain, dt, info).
+    """
+    dom = Domain()
+    dom.Dimension = 3
+    dom.Scheme = scheme
+    dom.Kernel_Set(kernel)
+    dom.Viscosity_Eq_Set(Morris)
+    dom.Gradient_Approach_Set(Squared_density)
+    h = hfac * dx
+    r = dx / 2.0
+    w = wall_layers
+    V = (-w * dx, -w * dx, -w * dx)
+    Ls = (2 * w * dx + TL + dx / 10.0, w * dx + TH + dx / 10.0, 2 * w * dx + TW + dx / 10.0)
+    axes = []
+    for d in range(3):
+        n = Domain._count(V[d], V[d] + Ls[d] - r, lambda i, d=d: V[d] + (2.0 * i + 1) * r)
+        axes.append(V[d] + (2.0 * np.arange(n) + 1) * r)
+    xs, ys, zs = axes
+    xwall = (xs < 0.0) | (xs > TL)
+    xfl = (~xwall) & (xs <= L)
+    zwall = (zs < 0.0) | (zs > TW)
+    zfl = (~zwall) & (zs <= W)
+    chunks = []
+    wall_flags = []
+    for yk, y in enumerate(ys):
+        ywall = y < 0.0
+        for zk, z in enumerate(zs):
+            if ywall or zwall[zk]:
+                sel = np.ones(len(xs), bool)  # whole row is wall
+                is_wall = np.ones(len(xs), bool)
+            else:
+                is_wall = xwall
+                sel = xwall | (xfl if (zfl[zk] and y <= H) else np.zeros(len(xs), bool))
+            nsel = int(sel.sum())
+            if nsel == 0:
+                continue
+            pts = np.empty((nsel, 3))
+            pts[:, 0] = xs[sel]
+            pts[:, 1] = y
+            pts[:, 2] = z
+            chunks.append(pts)
+            wall_flags.append(is_wall[sel])
+    X = np.concatenate(chunks)
+    wall = np.concatenate(wall_flags)
+    # AddBoxLength orders k (z) outer, j (y) middle, i (x) inner; reorder to match
+    order = np.lexsort((X[:, 0], X[:, 1], X[:, 2]))
+    X = np.ascontiguousarray(X[order])
+    wall = wall[order]
+    n = X.shape[0]
+    ext = [(axes[d][-1] + r) - V[d] for d in range(3)]
+    mass = ext[0] * ext[1] * ext[2] * rho / (len(xs) * len(ys) * len(zs))
+    dom.particles.append(n, {"x": X, "mass": np.full(n, mass)})
+    dom.R = r
+    p = dom.particles
+    cs = c0
+    _fluid_fields(p, wall, rho, cs, mu, alpha, shepard, h)
+    fl = ~wall
+    yb = X[:, 1]
+    dens = rho * np.power((1 + 7.0 * g * (H - yb[fl]) / (cs * cs)), (1.0 / 7.0))
+    p.get("density")[fl] = dens
+    p.get("densityb")[fl] = dens
+    dom.InitialDist = dx
+    dom.Gravity = [0.0, -g, 0.0]
+    dt = 0.25 * h / cs
+    return dom, dt, {"cs": cs, "H": H, "L": L, "g": g, "h": h, "n_fluid": int(fl.sum()), "n_wall": int(wall.sum())}
+
+
+def granular_column(dx=1e-3, W=0.2, aspect=1.0, TL_factor=4.0, wall_layers=3, rho=1850.0, E=0.84e6, nu=0.3,
+                    phi_deg=30.0, psi_deg=0.0, cohesion=0.0, fail=2, ti=0.5, tin=2.55, alpha=0.1, beta=0.1,
+                    cs=None, scheme=0, g=9.81, hfac=1.2):
+    """2D granular column collapse (Drucker-Prager soil, Material 3), as
+    Old_Tests/ReposeAngle2.cpp: a W x (aspect W) column against a left wall on
+    a floor, geostatic initial stress, Monaghan tensile-instability correction.
+    Returns (domain, dt, info).
+    """
+    dom = Domain()
+    dom.Dimension = 2
+    dom.Scheme = scheme
+    dom.Kernel_Set(Qubic_Spline)
+    dom.Viscosity_Eq_Set(Morris)
+    dom.Gradient_Approach_Set(Squared_density)
+    dom.Gravity = [0.0, -g, 0.0]
+    H = aspect * W
+    K = E / (3.0 * (1.0 - 2.0 * nu))
+    G = E / (2.0 * (1.0 + nu))
+    h = hfac * dx
+    if cs is None:
+        cs = math.sqrt(E / rho)
+    w = wall_layers
+    TL = TL_factor * W + (1.0 + aspect) * W
+    dom.InitialDist = dx
+    dom.AddBoxLength(1, (-w * dx, 0.0, 0.0), W + w * dx + dx / 10.0, H + dx / 10.0, 0, dx / 2.0, rho, h, 1, 0,
+                     False, False)
+    dom.AddBoxLength(1, (-w * dx, -w * dx, 0.0), TL + w * dx, w * dx + dx / 10.0, 0, dx / 2.0, rho, h, 1, 0,
+                     False, False)
+    p = dom.particles
+    x = p.get("x")
+    xb, yb = x[:, 0], x[:, 1]
+    wall = (yb < 0.0) | ((xb < 0.0) & (yb > 0.0))
+    n = p.n
+    p.set("g_mod", G)
+    p.set("cs", cs)
+    p.set("k_mod", K)
+    p.set("material", 3)
+    p.set("fail", fail)
+    p.set("cohesion", cohesion)
+    p.set("phi", phi_deg / 180.0 * math.pi)
+    p.set("psi", psi_deg / 180.0 * math.pi)
+    p.set("alpha", alpha)
+    p.set("beta", beta)
+    p.set("ti", ti)
+    p.set("tin", tin)
+    p.set("ti_init_dist", dx)
+    p.set("is_free", (~wall).astype(np.int32))
+    p.set("no_slip", wall.astype(np.int32))
+    ids = np.ones(n, np.int32)
+    ids[wall] = 3
+    p.set("id", ids)
+    K0 = 1 - math.sin(phi_deg / 180.0 * math.pi)
+    sig = p.get("sigma")
+    fl = ~wall
+    sig[fl, 1, 1] = rho * -g * (H - yb[fl])
+    sig[fl, 0, 0] = K0 * rho * -g * (H - yb[fl])
+    sig[fl, 2, 2] = K0 * rho * -g * (H - yb[fl])
+    dt = 0.2 * h / cs
+    return dom, dt, {"H": H, "W": W, "K": K, "G": G, "cs": cs, "h": h, "n_soil": int(fl.sum()),
+                     "n_wall": int(wall.sum())}
