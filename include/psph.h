@@ -168,6 +168,10 @@ int64_t psph_num_particles(const psph_ctx* ctx);
  * deleted ones removed, as Array::DelItems leaves them (External/array.h:726). */
 psph_status psph_download(psph_ctx* ctx, psph_particles* out);
 
+/* Original index (position at upload) of each particle psph_download returns,
+ * in the same order; out needs psph_num_particles entries. */
+psph_status psph_original_index(psph_ctx* ctx, int64_t* out);
+
 psph_status psph_get_grid(const psph_ctx* ctx, psph_grid* grid);
 psph_status psph_get_integrator(const psph_ctx* ctx, psph_integrator* integ);
 

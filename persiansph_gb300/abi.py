@@ -150,6 +150,7 @@ def _declare(lib):
     lib.psph_num_particles.argtypes = [ctx]
     lib.psph_num_particles.restype = C.c_int64
     lib.psph_download.argtypes = [ctx, P(PsphParticles)]
+    lib.psph_original_index.argtypes = [ctx, P(C.c_int64)]
     lib.psph_get_grid.argtypes = [ctx, P(PsphGrid)]
     lib.psph_get_integrator.argtypes = [ctx, P(PsphIntegrator)]
     lib.psph_pairs_export.argtypes = [ctx, C.c_int, P(C.c_int64), C.c_int64, P(C.c_int64)]
@@ -158,7 +159,7 @@ def _declare(lib):
     lib.psph_last_launch_count.argtypes = [ctx]
     lib.psph_last_launch_count.restype = C.c_int64
     for name in ("psph_device_check", "psph_create", "psph_set_stream", "psph_set_grid", "psph_set_integrator",
-                 "psph_upload", "psph_step", "psph_download", "psph_get_grid", "psph_get_integrator",
+                 "psph_upload", "psph_step", "psph_download", "psph_original_index", "psph_get_grid", "psph_get_integrator",
                  "psph_pairs_export", "psph_enable_timing", "psph_phase_times"):
         getattr(lib, name).restype = C.c_int
 

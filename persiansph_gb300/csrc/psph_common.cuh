@@ -1,0 +1,194 @@
+// Shared device-side definitions for the GB300 hot path.
+//
+// Device data layout (structure of arrays, sorted by cell every step):
+//   X4[s]  = (x, y, z, Density)            persistent, reordered
+//   V4[s]  = (vx, vy, vz, Pressure)        persistent, reordered
+//   H4[s]  = (va|vb xyz, Densitya|Densityb) persistent, reordered (scheme's history)
+//   cls[s] = particle-class index           persistent, reordered
+//   orig[s]= original particle index        persistent, reordered
+// Per-particle constants (material, flags, EOS, viscosity, soil parameters,
+// mass, h) are de-duplicated on upload into a small class table (PClass).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "psph.h"
+
+#define PSPH_HD __host__ __device__ __forceinline__
+#define PSPH_D __device__ __forceinline__
+
+namespace psph {
+
+constexpr double kPi = 3.14159265358979323846;
+
+// Status bits raised by kernels (read back by the host after each call).
+enum : uint32_t {
+  ST_NONFINITE = 1u << 0,
+  ST_DT_COLLAPSE = 1u << 1,
+  ST_OUT_OF_GRID = 1u << 2,
+  ST_CELL_OVERFLOW = 1u << 3,
+};
+
+// Constant per-particle parameters, shared by all particles of one class.
+struct PClass {
+  double cs, p0, rho0, fpmassc, alpha, beta, mu0, mu_ref, t0, bm, csmag, ti, tin, tid;
+  double g_mod, k_mod, sigmay, coh, phi, psi, h, mass;
+  int material, is_free, no_slip, pres_eq, shepard, les, vis_m, fail, id, pad;
+};
+
+// Domain scalars advanced on the device.
+struct StepScalars {
+  double time, deltat, deltatint, deltatmin;
+  double t_stop;
+  long long steps;
+  int first_step, ct, shepard_counter, stop;
+  int n;          // particles alive (cells + orphans)
+  int n_cells;    // particles inside cells
+  int n_total;    // particles in the buffers (alive + dead)
+  uint32_t status;
+  int launches;
+  int buf;        // which persistent buffer (A=0 / B=1) holds the current sorted state
+};
+
+struct GridDev {
+  double blpf[3], trpr[3], cell_size[3], dom_size[3];
+  double hmax, cellfac;
+  int nc[3];      // real cells per axis (a periodic axis drops the reference's 2 ghost columns)
+  int cn_ref[3];  // Domain::CellNo (ghost columns included)
+  int periodic[3];
+  int ncells;     // nc[0]*nc[1]*nc[2]
+};
+
+// ---------------------------------------------------------------------------
+// SPH kernels (Source/Functions.cpp:25-186), evaluated without pow():
+// rewritten with products and the reciprocal of r; differences from the
+// reference are rounding-level (checked by the parity tests at 1e-12).
+// ---------------------------------------------------------------------------
+template <int DIM, int KT>
+struct Kern {
+  // normalisation: W = cw/h^DIM f(q); GradKernel, LaplaceKernel and
+  // SecDerivativeKernel carry cw/h^(DIM+2).
+  static constexpr double cw() {
+    return KT == 0 ? (DIM == 2 ? 10.0 / (7.0 * kPi) : 1.0 / kPi)
+         : KT == 1 ? (DIM == 2 ? 7.0 / (4.0 * kPi) : 7.0 / (8.0 * kPi))
+                   : (DIM == 2 ? 7.0 / (478.0 * kPi) : 1.0 / (120.0 * kPi));
+  }
+  static constexpr double support() { return KT == 2 ? 3.0 : 2.0; }
+
+  // Kernel W(q,h) with cwh = cw/h^DIM.
+  static PSPH_HD double W(double q, double cwh) {
+    if (KT == 0) {
+      if (q < 1.0) return cwh * (1.0 - 1.5 * q * q + 0.75 * q * q * q);
+      if (q < 2.0) { double t = 2.0 - q; return cwh * (0.25 * t * t * t); }
+      return 0.0;
+    } else if (KT == 1) {
+      if (q < 2.0) { double t = 1.0 - 0.5 * q; double t2 = t * t; return cwh * (t2 * t2) * (2.0 * q + 1.0); }
+      return 0.0;
+    } else {
+      double a = 3.0 - q, b = 2.0 - q, c = 1.0 - q;
+      double a2 = a * a, b2 = b * b, c2 = c * c;
+      if (q < 1.0) return cwh * (a2 * a2 * a - 6.0 * b2 * b2 * b + 15.0 * c2 * c2 * c);
+      if (q < 2.0) return cwh * (a2 * a2 * a - 6.0 * b2 * b2 * b);
+      if (q < 3.0) return cwh * (a2 * a2 * a);
+      return 0.0;
+    }
+  }
+  // GradKernel (1/r dW/dr) with cwg = cw/h^(DIM+2), inv_q = 1/q (unused at q==0).
+  static PSPH_HD double GK(double q, double inv_q, double cwh1) {
+    if (KT == 0) {
+      if (q < 1.0) return cwh1 * (-3.0 + 2.25 * q);
+      if (q < 2.0) { double t = 2.0 - q; return cwh1 * inv_q * (-0.75 * t * t); }
+      return 0.0;
+    } else if (KT == 1) {
+      if (q < 2.0) { double t = 1.0 - 0.5 * q; return cwh1 * -5.0 * (t * t * t); }
+      return 0.0;
+    } else {
+      double a = 3.0 - q, b = 2.0 - q, c = 1.0 - q;
+      double a2 = a * a, b2 = b * b, c2 = c * c;
+      if (q == 0.0) return cwh1 * (20.0 * a2 * a - 120.0 * b2 * b + 300.0 * c2 * c);
+      if (q < 1.0) return cwh1 * inv_q * (-5.0 * a2 * a2 + 30.0 * b2 * b2 - 75.0 * c2 * c2);
+      if (q < 2.0) return cwh1 * inv_q * (-5.0 * a2 * a2 + 30.0 * b2 * b2);
+      if (q < 3.0) return cwh1 * inv_q * (-5.0 * a2 * a2);
+      return 0.0;
+    }
+  }
+  // SecDerivativeKernel with cwh2 = cw/h^(DIM+2) (same constant as GK).
+  static PSPH_HD double D2(double q, double cwh2) {
+    if (KT == 0) {
+      if (q < 1.0) return cwh2 * (-3.0 + 4.5 * q);
+      if (q < 2.0) return cwh2 * (1.5 * (2.0 - q));
+      return 0.0;
+    } else if (KT == 1) {
+      if (q < 2.0) { double t = 1.0 - 0.5 * q; return cwh2 * (t * t) * (10.0 * q - 5.0); }
+      return 0.0;
+    } else {
+      double a = 3.0 - q, b = 2.0 - q, c = 1.0 - q;
+      if (q < 1.0) return cwh2 * (20.0 * a * a * a - 120.0 * b * b * b + 300.0 * c * c * c);
+      if (q < 2.0) return cwh2 * (20.0 * a * a * a - 120.0 * b * b * b);
+      if (q < 3.0) return cwh2 * (20.0 * a * a * a);
+      return 0.0;
+    }
+  }
+  // LaplaceKernel = D2 + (DIM-1)/q * (first derivative / h^2 form), with cwh2.
+  static PSPH_HD double Lap(double q, double inv_q, double cwh2) {
+    double first;  // dW/dq / q (per C/h^(DIM+2))
+    if (KT == 0) {
+      if (q < 1.0) first = (-3.0 + 2.25 * q);
+      else if (q < 2.0) { double t = 2.0 - q; first = inv_q * (-0.75 * t * t); }
+      else return 0.0;
+    } else if (KT == 1) {
+      if (q < 2.0) { double t = 1.0 - 0.5 * q; first = -5.0 * t * t * t; }
+      else return 0.0;
+    } else {
+      double a = 3.0 - q, b = 2.0 - q, c = 1.0 - q;
+      double a2 = a * a, b2 = b * b, c2 = c * c;
+      if (q < 1.0) first = inv_q * (-5.0 * a2 * a2 + 30.0 * b2 * b2 - 75.0 * c2 * c2);
+      else if (q < 2.0) first = inv_q * (-5.0 * a2 * a2 + 30.0 * b2 * b2);
+      else if (q < 3.0) first = inv_q * (-5.0 * a2 * a2);
+      else return 0.0;
+    }
+    return D2(q, cwh2) + cwh2 * (DIM - 1.0) * first;
+  }
+};
+
+// Kernel value with runtime kernel type (used off the hot loop).
+template <int DIM>
+PSPH_HD double kernel_w_rt(int kt, double q, double h) {
+  double hd = (DIM == 2) ? h * h : h * h * h;
+  switch (kt) {
+    case 0: return Kern<DIM, 0>::W(q, Kern<DIM, 0>::cw() / hd);
+    case 1: return Kern<DIM, 1>::W(q, Kern<DIM, 1>::cw() / hd);
+    default: return Kern<DIM, 2>::W(q, Kern<DIM, 2>::cw() / hd);
+  }
+}
+
+// EOS / SoundSpeed / DensitySolid (Source/Functions.cpp:188-264).
+PSPH_HD double pow7(double x) { double x2 = x * x; double x3 = x2 * x; return x3 * x3 * x; }
+PSPH_HD double pow6(double x) { double x2 = x * x; return x2 * x2 * x2; }
+
+PSPH_HD double eos(int eq, double cs, double p0, double rho, double rho0) {
+  switch (eq) {
+    case 0: return p0 + (cs * cs) * (rho - rho0);
+    case 1: return p0 + (rho0 * cs * cs / 7.0) * (pow7(rho / rho0) - 1.0);
+    default: return (cs * cs) * rho;
+  }
+}
+PSPH_HD double sound_speed(int eq, double cs, double rho, double rho0) {
+  if (eq == 1) return sqrt((cs * cs) * pow6(rho / rho0));
+  return cs;
+}
+PSPH_HD double density_solid(int eq, double cs, double p0, double p, double rho0) {
+  switch (eq) {
+    case 0: return (p - p0) / (cs * cs) + rho0;
+    case 1: return pow(((p - p0) * (7.0 / (rho0 * cs * cs)) + 1.0), 1.0 / 7.0) * rho0;
+    default: return p / (cs * cs);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Cell indexing
+// ---------------------------------------------------------------------------
+PSPH_HD int cell_linear(const GridDev& g, int cx, int cy, int cz) { return (cz * g.nc[1] + cy) * g.nc[0] + cx; }
+
+}  // namespace psph

@@ -1,0 +1,105 @@
+// Device state and kernel entry points of the GB300 hot path.
+#pragma once
+
+#include "psph_common.cuh"
+
+namespace psph {
+
+// Persistent per-particle arrays (reordered by the cell sort each step).
+struct Persist {
+  double4_32a* X4;   // x, y, z, Density
+  double4_32a* V4;   // vx, vy, vz, Pressure
+  double4_32a* H4;   // leapfrog: va, Densitya | Modified Verlet: vb, Densityb
+  double4_32a* H4b;  // leapfrog: vb, Densityb (wall vb is read by the soil pair force) | MVerlet: null
+  int* cls;      // class index
+  int* orig;     // original particle index
+  double* mu;    // dynamic viscosity (LES / Bingham); null when constant per class
+  // soil / solid tensors (9 doubles per particle, row-major); null without solids
+  double* sigma;
+  double* sigma_h;   // leapfrog Sigmaa | MVerlet Sigmab
+  double* strain;
+  double* strain_h;  // leapfrog Straina | MVerlet Strainb
+  double* shear;     // ShearStress (solids, Material 2)
+  double* shear_h;   // leapfrog ShearStressa | MVerlet ShearStressb
+  double* tir;       // TIR (wall values persist between updates, as in the reference)
+};
+
+// Per-step arrays (sorted order of the current step; not reordered).
+struct Scratch {
+  int* key;        // cell key per particle (pre-sort order)
+  int* count;      // ncells + 2 counters
+  int* start;      // ncells + 3 exclusive prefix
+  int* tmp_perm;
+  int* perm;
+  int* cellid;     // cell of each sorted particle (orphan/dead: -1)
+  int* block_sums;
+  double* blockmin;
+  // per-step derived / outputs
+  double* rho_eff;   // density seen by partners: own Density, or wall density from the partner EOS
+  double* prs;       // pressure (walls: interpolated)
+  double* c_eff;     // sound speed seen by partners
+  double4_32a* A4;       // ax, ay, az, dDensity
+  double* zwab;
+  double* sumden;
+  double* sumkernel;
+  double4_32a* nsv4;     // wall no-slip velocity
+  double4_32a* vxsph4;   // XSPH velocity correction
+  double* strain_rate;   // 9 per particle
+  double* rotation_rate; // 9 per particle
+  double* shear_rate;
+  double* sbar;
+  double* sigma_o;       // leapfrog Sigmab | MVerlet Sigmaa: per-step output only (9 per particle)
+  double* strain_o;      // leapfrog Strainb | MVerlet Straina
+  double* shear_o;       // leapfrog ShearStressb | MVerlet ShearStressa
+};
+
+struct Options {
+  int dim, kt, vis_eq, grad_type, scheme, wallp_physical;
+  int has_solid;      // any Material 2/3
+  int any_av;         // any alpha/beta != 0
+  int any_ti;         // any TI > 0
+  int need_sr;        // strain rate needed (fluid T0>0 or LES)
+  int any_shepard;
+  int uniform_eos;    // all free particles of the material share one EOS class
+  int eos_cls;        // that class
+  int dyn_mu;
+  int soil_pairs;     // Material 3 (soil-soil walls take the partner's density)
+  int uniform_h;      // every particle has the same h
+  double inv_h;       // 1/h when uniform
+  double xsph, sqrt_h_a;
+  double gravity[3], body_force[3];
+  int shepard_step;
+  int nclasses;
+};
+
+// Everything a launch needs, passed by value to the launch wrappers.
+struct DevView {
+  GridDev g;
+  Options o;
+  Persist PA, PB; // double-buffered persistent arrays; StepScalars::buf says which is current
+  Scratch S;
+  const PClass* cls;
+  StepScalars* sc;
+  uint8_t* alive;
+  int ncap;
+  int nclasses;
+};
+
+PSPH_D const Persist& cur_persist(const DevView& v) { return v.sc->buf ? v.PB : v.PA; }
+PSPH_D const Persist& next_persist(const DevView& v) { return v.sc->buf ? v.PA : v.PB; }
+
+// Launch wrappers (defined in the .cu files).
+void launch_sort(const DevView& v, cudaStream_t st);      // bin + scan + scatter + rank + reorder + flip
+void launch_prepare(const DevView& v, cudaStream_t st);   // per-particle derived quantities, TIR
+void launch_wall(const DevView& v, cudaStream_t st);      // wall interpolation
+void launch_forces(const DevView& v, cudaStream_t st);    // pair forces + per-block dt minimum
+void launch_dt(const DevView& v, cudaStream_t st);        // dt reduction + AdaptiveTimeStep
+void launch_update(const DevView& v, cudaStream_t st);    // Move + material update + periodic wrap + leave
+void launch_begin(const DevView& v, cudaStream_t st);     // stop test, first-step counters
+void launch_end(const DevView& v, cudaStream_t st);       // time, counters
+int forces_blocks(int ncap);
+int launches_per_step(const DevView& v);
+void launch_pairs_export(const DevView& v, int which, long long* out, long long cap, unsigned long long* counter,
+                         cudaStream_t st);
+
+}  // namespace psph

@@ -1,0 +1,775 @@
+// Gather-form pair kernels of the GB300 hot path.
+//
+// The reference walks a half stencil of cells, pushes every candidate pair into
+// per-thread lists and then scatters each pair's contribution into both
+// particles under per-particle locks (Source/Domain.cpp:808-945,
+// Source/Interaction.cpp:25-377). Here each particle gathers from the full
+// 3x3(x3) block of cells around its own, so every pair is evaluated twice (once
+// from each side) and each particle's sums are owned by one thread: no atomics,
+// no locks, deterministic results.
+//
+//   prepare_wall  free particles: partner-visible density / sound speed, TIR;
+//                 fixed particles: PrimaryComputeAcceleration's wall
+//                 interpolation (Source/Domain.cpp:1020-1059, :1164-1206)
+//   forces_fluid  CalcForce11 (Source/Interaction.cpp:25-184) from the side of
+//                 each free particle, plus the acceleration time-step bound
+//   forces_solid  CalcForce2233 (Source/Interaction.cpp:186-377)
+//   dt_finalize   LastComputeAcceleration's minimum (Source/Domain.cpp:1280-1296)
+//                 and AdaptiveTimeStep (Source/Domain.cpp:133-152)
+#include <cfloat>
+
+#include "psph_device.cuh"
+
+namespace psph {
+
+namespace {
+
+constexpr int kFT = 128;  // threads per block of the pair kernels
+
+struct CellCoord {
+  int x, y, z;
+};
+
+PSPH_D CellCoord decode(const GridDev& g, int c) {
+  CellCoord r;
+  r.x = c % g.nc[0];
+  const int t = c / g.nc[0];
+  r.y = t % g.nc[1];
+  r.z = t / g.nc[1];
+  return r;
+}
+
+// Periodic_X_Correction (Source/Domain.cpp:110-115) for the pair (P1, P2).
+PSPH_D void periodic_fix(const GridDev& g, double& x0, double& x1, double& x2, double hb, const CellCoord& c1,
+                         const CellCoord& c2) {
+  const double lim = 2 * g.cellfac * hb;
+  if (g.dom_size[0] > 0.0 && (x0 > lim || x0 < -lim)) x0 += (c1.x > c2.x) ? -g.dom_size[0] : g.dom_size[0];
+  if (g.dom_size[1] > 0.0 && (x1 > lim || x1 < -lim)) x1 += (c1.y > c2.y) ? -g.dom_size[1] : g.dom_size[1];
+  if (g.dom_size[2] > 0.0 && (x2 > lim || x2 < -lim)) x2 += (c1.z > c2.z) ? -g.dom_size[2] : g.dom_size[2];
+}
+
+// Visits the sorted index ranges of the 3 (2D) or 9 (3D) cell rows around c.
+template <int DIM, class F>
+PSPH_D void for_neighbor_ranges(const GridDev& g, const CellCoord& c, const int* __restrict__ start, F&& f) {
+  const int zlo = (DIM == 3) ? -1 : 0, zhi = (DIM == 3) ? 1 : 0;
+  for (int dz = zlo; dz <= zhi; ++dz) {
+    int z = c.z + dz;
+    if (g.periodic[2]) z = (z + g.nc[2]) % g.nc[2];
+    else if (z < 0 || z >= g.nc[2]) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      int y = c.y + dy;
+      if (g.periodic[1]) y = (y + g.nc[1]) % g.nc[1];
+      else if (y < 0 || y >= g.nc[1]) continue;
+      const int row = (z * g.nc[1] + y) * g.nc[0];
+      if (!g.periodic[0] || (c.x >= 1 && c.x <= g.nc[0] - 2)) {
+        const int x0 = max(c.x - 1, 0), x1 = min(c.x + 1, g.nc[0] - 1);
+        f(start[row + x0], start[row + x1 + 1]);
+      } else {
+        for (int dx = -1; dx <= 1; ++dx) {
+          const int x = (c.x + dx + g.nc[0]) % g.nc[0];
+          f(start[row + x], start[row + x + 1]);
+        }
+      }
+    }
+  }
+}
+
+// True when MainNeighbourSearch lists (w, f) with w first: f's cell is in w's
+// forward half stencil (Source/Domain.cpp:860-940), or, in the same cell, w
+// has the larger index (head insertion reverses index order, :736-740).
+PSPH_D bool first_of_pair(const GridDev& g, const CellCoord& cw, const CellCoord& cf, int orig_w, int orig_f) {
+  int o[3] = {cf.x - cw.x, cf.y - cw.y, cf.z - cw.z};
+  const int n[3] = {g.nc[0], g.nc[1], g.nc[2]};
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+    if (g.periodic[d]) {
+      if (o[d] > 1) o[d] -= n[d];
+      if (o[d] < -1) o[d] += n[d];
+    }
+  if (o[2] != 0) return o[2] > 0;
+  if (o[1] != 0) return o[1] > 0;
+  if (o[0] != 0) return o[0] > 0;
+  return orig_w > orig_f;
+}
+
+template <int DIM>
+PSPH_D void tensile_tir(const double* S, double TI, double rho, double* TIR) {
+  // Source/Domain.cpp:958-976 (2D); 3D via a Jacobi eigen-decomposition
+  // (the reference uses GSL's symmetric eigensolver, :979-987).
+  if (DIM == 2) {
+    double teta;
+    if ((S[0] - S[4]) != 0.0) teta = 0.5 * atan(2.0 * S[1] / (S[0] - S[4]));
+    else teta = kPi / 4.0;
+    const double C = cos(teta), Sn = sin(teta);
+    double Sxx = C * C * S[0] + 2.0 * C * Sn * S[1] + Sn * Sn * S[4];
+    double Syy = Sn * Sn * S[0] - 2.0 * C * Sn * S[1] + C * C * S[4];
+    Sxx = (Sxx > 0) ? -TI * Sxx / (rho * rho) : 0.0;
+    Syy = (Syy > 0) ? -TI * Syy / (rho * rho) : 0.0;
+    TIR[0] = C * C * Sxx + Sn * Sn * Syy;
+    TIR[4] = Sn * Sn * Sxx + C * C * Syy;
+    TIR[1] = TIR[3] = Sn * C * (Sxx - Syy);
+  } else {
+    double a[9], Q[9];
+    for (int e = 0; e < 9; ++e) {
+      a[e] = S[e];
+      Q[e] = (e % 4 == 0) ? 1.0 : 0.0;
+    }
+    for (int sweep = 0; sweep < 50; ++sweep) {
+      if (a[1] * a[1] + a[2] * a[2] + a[5] * a[5] == 0.0) break;
+      for (int p = 0; p < 3; ++p)
+        for (int r = p + 1; r < 3; ++r) {
+          const double apr = a[3 * p + r];
+          if (apr == 0.0) continue;
+          const double theta = (a[3 * r + r] - a[3 * p + p]) / (2.0 * apr);
+          const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+          const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+          for (int k = 0; k < 3; ++k) {
+            const double akp = a[3 * k + p], akr = a[3 * k + r];
+            a[3 * k + p] = c * akp - s * akr;
+            a[3 * k + r] = s * akp + c * akr;
+          }
+          for (int k = 0; k < 3; ++k) {
+            const double apk = a[3 * p + k], ark = a[3 * r + k];
+            a[3 * p + k] = c * apk - s * ark;
+            a[3 * r + k] = s * apk + c * ark;
+          }
+          for (int k = 0; k < 3; ++k) {
+            const double qkp = Q[3 * k + p], qkr = Q[3 * k + r];
+            Q[3 * k + p] = c * qkp - s * qkr;
+            Q[3 * k + r] = s * qkp + c * qkr;
+          }
+        }
+    }
+    double val[3];
+    for (int k = 0; k < 3; ++k) {
+      const double ev = a[4 * k];
+      val[k] = (ev > 0) ? -TI * ev / (rho * rho) : 0.0;
+    }
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) TIR[3 * r + c] = Q[3 * r + 0] * val[0] * Q[3 * c + 0] + Q[3 * r + 1] * val[1] * Q[3 * c + 1] + Q[3 * r + 2] * val[2] * Q[3 * c + 2];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Per-particle preparation and wall interpolation
+// ---------------------------------------------------------------------------
+template <int DIM, int KT>
+__global__ void __launch_bounds__(kFT) prepare_wall_kernel(DevView v) {
+  const StepScalars* sc = v.sc;
+  if (sc->stop) return;
+  const Persist& P = cur_persist(v);
+  const int n = sc->n;
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= n) return;
+  const GridDev& g = v.g;
+  const PClass* __restrict__ CT = v.cls;
+  const PClass& Cw = CT[P.cls[w]];
+  const PClass& Ce = CT[v.o.eos_cls];
+  if (Cw.is_free) {
+    const double rho = P.X4[w].w;
+    v.S.rho_eff[w] = rho;
+    v.S.prs[w] = P.V4[w].w;
+    v.S.c_eff[w] = sound_speed(Cw.pres_eq, Cw.cs, rho, Cw.rho0);
+    if (v.o.has_solid && Cw.material > 1 && Cw.ti > 0.0)
+      tensile_tir<DIM>(P.sigma + 9 * (size_t)w, Cw.ti, rho, P.tir + 9 * (size_t)w);
+    return;
+  }
+  // fixed particle: StartAcceleration resets (Source/Domain.cpp:989-996), then interpolation
+  const double4_32a xw = P.X4[w];
+  const int cell = v.S.cellid[w];
+  const int mat = Cw.material;
+  double sk = 0.0, p = 0.0, n0 = 0.0, n1 = 0.0, n2 = 0.0;
+  double sig[9];
+#pragma unroll
+  for (int e = 0; e < 9; ++e) sig[e] = 0.0;
+  const bool any_periodic = g.periodic[0] | g.periodic[1] | g.periodic[2];
+  if (cell >= 0) {
+    const CellCoord cw = decode(g, cell);
+    const int ow = P.orig[w];
+    const double gx = v.o.gravity[0], gy = v.o.gravity[1], gz = v.o.gravity[2];
+    for_neighbor_ranges<DIM>(g, cw, v.S.start, [&](int lo, int hi) {
+      for (int f = lo; f < hi; ++f) {
+        if (f == w) continue;
+        const PClass& Cf = CT[P.cls[f]];
+        if (!Cf.is_free || Cf.material != mat) continue;
+        const double4_32a xf = P.X4[f];
+        const double hb = (Cw.h + Cf.h) / 2.0;
+        const CellCoord cf = decode(g, v.S.cellid[f]);
+        const bool wfirst = v.o.wallp_physical ? true : first_of_pair(g, cw, cf, ow, P.orig[f]);
+        double x0, x1, x2;
+        if (wfirst) {
+          x0 = xw.x - xf.x; x1 = xw.y - xf.y; x2 = xw.z - xf.z;
+          if (any_periodic) periodic_fix(g, x0, x1, x2, hb, cw, cf);
+        } else {
+          x0 = xf.x - xw.x; x1 = xf.y - xw.y; x2 = xf.z - xw.z;
+          if (any_periodic) periodic_fix(g, x0, x1, x2, hb, cf, cw);
+        }
+        const double r = sqrt(x0 * x0 + x1 * x1 + x2 * x2);
+        const double K = kernel_w_rt<DIM>(KT, r / hb, hb);
+        if (K == 0.0) continue;
+        sk += K;
+        if (mat < 3) {
+          const double4_32a vf = P.V4[f];
+          p += vf.w * K + (gx * x0 + gy * x1 + gz * x2) * xf.w * K;
+        }
+        if (mat > 1) {
+          const double* sf = P.sigma + 9 * (size_t)f;
+#pragma unroll
+          for (int e = 0; e < 9; ++e) sig[e] += sf[e] * K;
+        }
+        if (Cw.no_slip) {
+          const double4_32a vf = P.V4[f];
+          n0 += vf.x * K; n1 += vf.y * K; n2 += vf.z * K;
+        }
+      }
+    });
+  }
+  if (sk != 0.0) {
+    if (mat < 3) p = p / sk;
+    if (mat > 1) {
+      const double s = 1.0 / sk;
+#pragma unroll
+      for (int e = 0; e < 9; ++e) sig[e] = sig[e] * s;
+    }
+    if (Cw.no_slip) { n0 = n0 / sk; n1 = n1 / sk; n2 = n2 / sk; }
+  } else {
+    p = 0.0; n0 = n1 = n2 = 0.0;
+  }
+  double4_32a vw = P.V4[w];
+  vw.w = p;
+  P.V4[w] = vw;
+  v.S.prs[w] = p;
+  v.S.sumkernel[w] = sk;
+  v.S.nsv4[w] = make_double4_32a(n0, n1, n2, 0.0);
+  if (v.o.has_solid) {
+    double* sw = P.sigma + 9 * (size_t)w;
+#pragma unroll
+    for (int e = 0; e < 9; ++e) sw[e] = sig[e];
+    if (P.shear) {
+      double* tw = P.shear + 9 * (size_t)w;
+#pragma unroll
+      for (int e = 0; e < 9; ++e) tw[e] = 0.0;
+    }
+    if (sk != 0.0 && mat > 1 && Cw.ti > 0.0) tensile_tir<DIM>(sig, Cw.ti, xw.w, P.tir + 9 * (size_t)w);
+  }
+  // density / sound speed partners see (Source/Interaction.cpp:41-61, :70-71)
+  if (v.o.uniform_eos && mat != 3) {
+    const double rw = density_solid(Ce.pres_eq, Ce.cs, Ce.p0, p, Ce.rho0);
+    v.S.rho_eff[w] = rw;
+    v.S.c_eff[w] = sound_speed(Ce.pres_eq, Ce.cs, rw, Ce.rho0);
+  } else {
+    v.S.rho_eff[w] = xw.w;
+    v.S.c_eff[w] = 0.0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Fluid pair force (CalcForce11) from the side of free particle i
+// ---------------------------------------------------------------------------
+template <int DIM, int KT>
+__global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
+  __shared__ double red[kFT / 32];
+  const StepScalars* sc = v.sc;
+  if (sc->stop) return;
+  const Persist& P = cur_persist(v);
+  const int n = sc->n;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const GridDev& g = v.g;
+  const Options& o = v.o;
+  const PClass* __restrict__ CT = v.cls;
+  double dtc = DBL_MAX;
+  if (i < n) {
+    const PClass& Ci = CT[P.cls[i]];
+    const double4_32a xi = P.X4[i];
+    if (!Ci.is_free) {
+      v.S.A4[i] = make_double4_32a(o.gravity[0], o.gravity[1], o.gravity[2], 0.0);
+      v.S.zwab[i] = 1.0;
+    } else {
+      const double4_32a vi = P.V4[i];
+      const int cell = v.S.cellid[i];
+      const double di = xi.w, mi = Ci.mass, hi = Ci.h, pi = vi.w;
+      const double mui = o.dyn_mu ? P.mu[i] : Ci.mu0;
+      const double ci_snd = v.S.c_eff[i];
+      const bool shep = Ci.shepard && (sc->shepard_counter == o.shepard_step);
+      const bool sr_self = (Ci.t0 > 0.0 || Ci.les);
+      double ax = o.gravity[0] + o.body_force[0], ay = o.gravity[1] + o.body_force[1],
+             az = o.gravity[2] + o.body_force[2];
+      double drho = 0.0, zw = 0.0, sd = 0.0, xs0 = 0.0, xs1 = 0.0, xs2 = 0.0;
+      double sr[9];
+#pragma unroll
+      for (int e = 0; e < 9; ++e) sr[e] = 0.0;
+      const bool any_periodic = g.periodic[0] | g.periodic[1] | g.periodic[2];
+      const double cf2 = g.cellfac * g.cellfac;
+      if (cell >= 0) {
+        const CellCoord ci = decode(g, cell);
+        for_neighbor_ranges<DIM>(g, ci, v.S.start, [&](int lo, int hi_) {
+          for (int j = lo; j < hi_; ++j) {
+            if (j == i) continue;
+            const double4_32a xj = P.X4[j];
+            const PClass& Cj = CT[P.cls[j]];
+            const double hb = (hi + Cj.h) / 2;
+            double x0 = xi.x - xj.x, x1 = xi.y - xj.y, x2 = xi.z - xj.z;
+            if (any_periodic) periodic_fix(g, x0, x1, x2, hb, ci, decode(g, v.S.cellid[j]));
+            const double r2 = x0 * x0 + x1 * x1 + x2 * x2;
+            if (r2 > cf2 * hb * hb * (1.0 + 1e-9)) continue;
+            const double inv_hb = o.uniform_h ? o.inv_h : 1.0 / hb;
+            const double rij = sqrt(r2);
+            const double q = rij * inv_hb;
+            if (q > g.cellfac) continue;
+            const double4_32a vj = P.V4[j];
+            const bool fj = Cj.is_free;
+            double dj, mj;
+            if (fj) { dj = xj.w; mj = Cj.mass; }
+            else {
+              dj = o.uniform_eos ? v.S.rho_eff[j] : density_solid(Ci.pres_eq, Ci.cs, Ci.p0, v.S.prs[j], Ci.rho0);
+              mj = Cj.fpmassc * mi;
+            }
+            const double pj = fj ? vj.w : v.S.prs[j];
+            const double ih2 = inv_hb * inv_hb;
+            const double cwh = Kern<DIM, KT>::cw() * (DIM == 2 ? ih2 : ih2 * inv_hb);
+            const double cwg = cwh * ih2;
+            const double inv_q = (q > 0.0) ? 1.0 / q : 0.0;
+            const double GK = Kern<DIM, KT>::GK(q, inv_q, cwg);
+            const double K = Kern<DIM, KT>::W(q, cwh);
+            const double v0 = vi.x - vj.x, v1 = vi.y - vj.y, v2 = vi.z - vj.z;
+            const double vx = v0 * x0 + v1 * x1 + v2 * x2;
+            double PI = 0.0;
+            const double Alpha = (Ci.alpha + Cj.alpha) / 2.0, Beta = (Ci.beta + Cj.beta) / 2.0;
+            if ((Alpha != 0.0 || Beta != 0.0) && vx < 0) {
+              const double cj_snd = fj ? v.S.c_eff[j]
+                                       : (o.uniform_eos ? v.S.c_eff[j] : sound_speed(Ci.pres_eq, Ci.cs, dj, Ci.rho0));
+              const double MU = hb * vx / (r2 + 0.01 * hb * hb);
+              PI = (-Alpha * 0.5 * (ci_snd + cj_snd) * MU + Beta * MU * MU) / (0.5 * (di + dj));
+            }
+            double TI = 0.0;
+            if (Ci.ti > 0.0 || Cj.ti > 0.0) {
+              double Ri = 0.0, Rj = 0.0;
+              if ((pi + pj) < 0.0) {
+                if (pi < 0.0) Ri = -pi / (di * di);
+                if (pj < 0.0) Rj = -pj / (dj * dj);
+              }
+              const double Wd = Kern<DIM, KT>::W((Ci.tid + Cj.tid) / (2.0 * hb), cwh);
+              TI = (Ci.ti * Ri + Cj.ti * Rj) * pow(K / Wd, (Ci.tin + Cj.tin) / 2.0);
+            }
+            double VI0 = 0.0, VI1 = 0.0, VI2 = 0.0;
+            double vab0 = 0.0, vab1 = 0.0, vab2 = 0.0;
+            const bool visc = (Ci.no_slip || Cj.no_slip) || fj;
+            if (visc) {
+              double Mu;
+              if (fj) {
+                vab0 = v0; vab1 = v1; vab2 = v2;
+                const double muj = o.dyn_mu ? P.mu[j] : Cj.mu0;
+                Mu = 2.0 * mui * muj / (mui + muj);
+              } else {
+                const double4_32a ns = v.S.nsv4[j];
+                vab0 = vi.x - (2.0 * vj.x - ns.x);
+                vab1 = vi.y - (2.0 * vj.y - ns.y);
+                vab2 = vi.z - (2.0 * vj.z - ns.z);
+                Mu = mui;
+              }
+              double c;
+              switch (o.vis_eq) {
+                case 0: c = 2.0 * Mu / (di * dj) * GK; break;
+                case 1: c = 8.0 * Mu / ((di + dj) * (di + dj)) * GK; break;
+                case 2: c = -Mu / (di * dj) * Kern<DIM, KT>::Lap(q, inv_q, cwg); break;
+                default: c = 0.0; break;
+              }
+              if (o.vis_eq <= 2) {
+                VI0 = c * vab0; VI1 = c * vab1; VI2 = c * vab2;
+              } else {
+                const double L = Kern<DIM, KT>::Lap(q, inv_q, cwg);
+                const double S2 = Kern<DIM, KT>::D2(q, cwg);
+                const double s = -Mu / (di * dj);
+                const double t = vx / r2 * (-GK + S2);
+                VI0 = s * (L * vab0 + (1.0 / 3.0) * (GK * v0 + t * x0));
+                VI1 = s * (L * vab1 + (1.0 / 3.0) * (GK * v1 + t * x1));
+                VI2 = s * (L * vab2 + (1.0 / 3.0) * (GK * v2 + t * x2));
+              }
+              if (sr_self) {
+                const bool want = (Ci.t0 > 0.0 || Cj.t0 > 0.0 || (Ci.les && Cj.les));
+                if (want) {
+                  const double c2 = -GK * (mj / dj);
+                  sr[0] += c2 * (2.0 * vab0 * x0);
+                  sr[1] += c2 * (vab0 * x1 + vab1 * x0);
+                  sr[2] += c2 * (vab0 * x2 + vab2 * x0);
+                  sr[4] += c2 * (2.0 * vab1 * x1);
+                  sr[5] += c2 * (vab1 * x2 + vab2 * x1);
+                  sr[8] += c2 * (2.0 * vab2 * x2);
+                }
+              }
+            }
+            if (o.xsph != 0.0 && fj) {
+              const double s = o.xsph * mj / (0.5 * (di + dj)) * K;
+              xs0 -= s * v0; xs1 -= s * v1; xs2 -= s * v2;
+            }
+            double s;
+            if (o.grad_type == 0) s = -(pi / (di * di) + pj / (dj * dj) + PI + TI) * GK;
+            else s = -((pi + pj) / (di * dj) + PI + TI) * GK;
+            ax += mj * (s * x0 + VI0);
+            ay += mj * (s * x1 + VI1);
+            if (DIM == 3) az += mj * (s * x2 + VI2);
+            drho += mj * (di / dj) * (GK * vx);
+            zw += mj / dj * K;
+            if (shep) sd += mj * K;
+          }
+        });
+      }
+      v.S.A4[i] = make_double4_32a(ax, ay, az, drho);
+      v.S.zwab[i] = zw;
+      if (o.any_shepard) v.S.sumden[i] = sd;
+      if (o.xsph != 0.0) v.S.vxsph4[i] = make_double4_32a(xs0, xs1, xs2, 0.0);
+      if (o.need_sr) {
+        double* out = v.S.strain_rate + 9 * (size_t)i;
+        out[0] = sr[0]; out[1] = sr[1]; out[2] = sr[2];
+        out[3] = sr[1]; out[4] = sr[4]; out[5] = sr[5];
+        out[6] = sr[2]; out[7] = sr[5]; out[8] = sr[8];
+      }
+      if (!(isfinite(ax) && isfinite(ay) && isfinite(az) && isfinite(drho))) atomicOr(&v.sc->status, ST_NONFINITE);
+      const double an = sqrt(ax * ax + ay * ay + az * az);
+      const double test = sqrt(hi / an);
+      const double cand = o.sqrt_h_a * test;
+      if (cand < dtc) dtc = cand;  // NaN never compares less, as in the reference
+    }
+  }
+  // block minimum of the acceleration time-step bound
+  for (int off = 16; off > 0; off >>= 1) dtc = fmin(dtc, __shfl_down_sync(0xffffffffu, dtc, off));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = dtc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = red[0];
+    for (int k = 1; k < kFT / 32; ++k) m = fmin(m, red[k]);
+    v.S.blockmin[blockIdx.x] = m;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Soil / solid pair force (CalcForce2233) from the side of free particle i
+// ---------------------------------------------------------------------------
+template <int DIM, int KT>
+__global__ void __launch_bounds__(kFT) forces_solid_kernel(DevView v) {
+  __shared__ double red[kFT / 32];
+  const StepScalars* sc = v.sc;
+  if (sc->stop) return;
+  const Persist& P = cur_persist(v);
+  const int n = sc->n;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const GridDev& g = v.g;
+  const Options& o = v.o;
+  const PClass* __restrict__ CT = v.cls;
+  double dtc = DBL_MAX;
+  if (i < n) {
+    const PClass& Ci = CT[P.cls[i]];
+    const double4_32a xi = P.X4[i];
+    if (!Ci.is_free) {
+      v.S.A4[i] = make_double4_32a(o.gravity[0], o.gravity[1], o.gravity[2], 0.0);
+      v.S.zwab[i] = 1.0;
+    } else {
+      const double4_32a vi = P.V4[i];
+      const int cell = v.S.cellid[i];
+      const double di = xi.w, mi = Ci.mass, hi = Ci.h;
+      const bool shep = Ci.shepard && (sc->shepard_counter == o.shepard_step);
+      const double* __restrict__ Si = P.sigma + 9 * (size_t)i;
+      const double* __restrict__ Ti = P.tir + 9 * (size_t)i;
+      double ax = o.gravity[0] + o.body_force[0], ay = o.gravity[1] + o.body_force[1],
+             az = o.gravity[2] + o.body_force[2];
+      double drho = 0.0, zw = 0.0, sd = 0.0, xs0 = 0.0, xs1 = 0.0, xs2 = 0.0;
+      double sr[9], rr[9];
+#pragma unroll
+      for (int e = 0; e < 9; ++e) { sr[e] = 0.0; rr[e] = 0.0; }
+      const bool any_periodic = g.periodic[0] | g.periodic[1] | g.periodic[2];
+      const double cf2 = g.cellfac * g.cellfac;
+      const double I22 = (DIM == 2) ? 0.0 : 1.0;  // Domain::I (Source/Domain.cpp:1665)
+      if (cell >= 0) {
+        const CellCoord ci = decode(g, cell);
+        for_neighbor_ranges<DIM>(g, ci, v.S.start, [&](int lo, int hi_) {
+          for (int j = lo; j < hi_; ++j) {
+            if (j == i) continue;
+            const double4_32a xj = P.X4[j];
+            const PClass& Cj = CT[P.cls[j]];
+            const double hb = (hi + Cj.h) / 2;
+            double x0 = xi.x - xj.x, x1 = xi.y - xj.y, x2 = xi.z - xj.z;
+            if (any_periodic) periodic_fix(g, x0, x1, x2, hb, ci, decode(g, v.S.cellid[j]));
+            const double r2 = x0 * x0 + x1 * x1 + x2 * x2;
+            if (r2 > cf2 * hb * hb * (1.0 + 1e-9)) continue;
+            const double inv_hb = o.uniform_h ? o.inv_h : 1.0 / hb;
+            const double rij = sqrt(r2);
+            const double q = rij * inv_hb;
+            if (q > g.cellfac) continue;
+            const double4_32a vj = P.V4[j];
+            const bool fj = Cj.is_free;
+            const bool soil = (Ci.material * Cj.material == 9);
+            double dj, mj;
+            if (fj) { dj = xj.w; mj = Cj.mass; }
+            else if (soil) { dj = di; mj = Cj.fpmassc * mi; }
+            else {
+              dj = o.uniform_eos ? v.S.rho_eff[j] : density_solid(Ci.pres_eq, Ci.cs, Ci.p0, v.S.prs[j], Ci.rho0);
+              mj = Cj.fpmassc * mi;
+            }
+            const double ih2 = inv_hb * inv_hb;
+            const double cwh = Kern<DIM, KT>::cw() * (DIM == 2 ? ih2 : ih2 * inv_hb);
+            const double cwg = cwh * ih2;
+            const double inv_q = (q > 0.0) ? 1.0 / q : 0.0;
+            const double GK = Kern<DIM, KT>::GK(q, inv_q, cwg);
+            const double K = Kern<DIM, KT>::W(q, cwh);
+            const double v0 = vi.x - vj.x, v1 = vi.y - vj.y, v2 = vi.z - vj.z;
+            const double vx = v0 * x0 + v1 * x1 + v2 * x2;
+            double PIs = 0.0;  // PIij = PIs * I
+            const double Alpha = (Ci.alpha + Cj.alpha) / 2.0, Beta = (Ci.beta + Cj.beta) / 2.0;
+            if ((Alpha != 0.0 || Beta != 0.0) && vx < 0) {
+              const double MU = hb * vx / (r2 + 0.01 * hb * hb);
+              double Cij;
+              if (soil) Cij = 0.5 * (Ci.cs + Cj.cs);
+              else {
+                const double c_i = v.S.c_eff[i];
+                const double c_j = fj ? v.S.c_eff[j] : sound_speed(Ci.pres_eq, Ci.cs, dj, Ci.rho0);
+                Cij = 0.5 * (c_i + c_j);
+              }
+              PIs = (Alpha * Cij * MU + Beta * MU * MU) / (0.5 * (di + dj));
+            }
+            double TIs = 0.0;  // TIij = TIs * (TIR_i + TIR_j)
+            const bool ti = (Ci.ti > 0.0 || Cj.ti > 0.0);
+            if (ti) {
+              const double Wd = Kern<DIM, KT>::W((Ci.tid + Cj.tid) / (2.0 * hb), cwh);
+              TIs = pow(K / Wd, (Ci.tin + Cj.tin) / 2.0);
+            }
+            double vab0, vab1, vab2;
+            if (fj) { vab0 = v0; vab1 = v1; vab2 = v2; }
+            else if (Ci.no_slip || Cj.no_slip) {
+              const double4_32a ns = v.S.nsv4[j];
+              vab0 = vi.x - (2.0 * vj.x - ns.x);
+              vab1 = vi.y - (2.0 * vj.y - ns.y);
+              vab2 = vi.z - (2.0 * vj.z - ns.z);
+            } else {
+              const double4_32a vbj = (o.scheme == PSPH_MVERLET) ? P.H4[j] : P.H4b[j];
+              vab0 = vi.x - vbj.x; vab1 = vi.y - vbj.y; vab2 = vi.z - vbj.z;
+            }
+            const double* __restrict__ Sj = P.sigma + 9 * (size_t)j;
+            const double* __restrict__ Tj = P.tir + 9 * (size_t)j;
+            double M[9];
+            if (o.grad_type == 0) {
+              const double ci2 = 1.0 / (di * di), cj2 = 1.0 / (dj * dj);
+#pragma unroll
+              for (int e = 0; e < 9; ++e) M[e] = Si[e] * ci2 + Sj[e] * cj2;
+            } else {
+              const double c = 1.0 / (di * dj);
+#pragma unroll
+              for (int e = 0; e < 9; ++e) M[e] = (Si[e] + Sj[e]) * c;
+            }
+            M[0] += PIs; M[4] += PIs; M[8] += PIs * I22;
+            if (ti) {
+#pragma unroll
+              for (int e = 0; e < 9; ++e) M[e] += (Ti[e] + Tj[e]) * TIs;
+            }
+            const double g0 = GK * x0, g1 = GK * x1, g2 = GK * x2;
+            const double t0 = g0 * M[0] + g1 * M[3] + g2 * M[6];
+            const double t1 = g0 * M[1] + g1 * M[4] + g2 * M[7];
+            const double t2 = g0 * M[2] + g1 * M[5] + g2 * M[8];
+            ax += mj * t0;
+            ay += mj * t1;
+            if (DIM == 3) az += mj * t2;
+            drho += mj * (di / dj) * (v0 * g0 + v1 * g1 + v2 * g2);
+            const double md = mj / dj;
+            zw += md * K;
+            const double c2 = -0.5 * GK * md;
+            sr[0] += c2 * (2.0 * vab0 * x0);
+            sr[1] += c2 * (vab0 * x1 + vab1 * x0);
+            sr[2] += c2 * (vab0 * x2 + vab2 * x0);
+            sr[4] += c2 * (2.0 * vab1 * x1);
+            sr[5] += c2 * (vab1 * x2 + vab2 * x1);
+            sr[8] += c2 * (2.0 * vab2 * x2);
+            rr[1] += c2 * (vab0 * x1 - vab1 * x0);
+            rr[2] += c2 * (vab0 * x2 - vab2 * x0);
+            rr[5] += c2 * (vab1 * x2 - vab2 * x1);
+            if (o.xsph != 0.0 && fj) {
+              const double s = o.xsph * mj / (0.5 * (di + dj)) * K;
+              xs0 -= s * v0; xs1 -= s * v1; xs2 -= s * v2;
+            }
+            if (shep) sd += mj * K;
+          }
+        });
+      }
+      v.S.A4[i] = make_double4_32a(ax, ay, az, drho);
+      v.S.zwab[i] = zw;
+      if (o.any_shepard) v.S.sumden[i] = sd;
+      if (o.xsph != 0.0) v.S.vxsph4[i] = make_double4_32a(xs0, xs1, xs2, 0.0);
+      double* out = v.S.strain_rate + 9 * (size_t)i;
+      out[0] = sr[0]; out[1] = sr[1]; out[2] = sr[2];
+      out[3] = sr[1]; out[4] = sr[4]; out[5] = sr[5];
+      out[6] = sr[2]; out[7] = sr[5]; out[8] = sr[8];
+      double* ro = v.S.rotation_rate + 9 * (size_t)i;
+      ro[0] = 0.0; ro[1] = rr[1]; ro[2] = rr[2];
+      ro[3] = -rr[1]; ro[4] = 0.0; ro[5] = rr[5];
+      ro[6] = -rr[2]; ro[7] = -rr[5]; ro[8] = 0.0;
+      if (!(isfinite(ax) && isfinite(ay) && isfinite(az) && isfinite(drho))) atomicOr(&v.sc->status, ST_NONFINITE);
+      const double an = sqrt(ax * ax + ay * ay + az * az);
+      const double cand = o.sqrt_h_a * sqrt(hi / an);
+      if (cand < dtc) dtc = cand;
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) dtc = fmin(dtc, __shfl_down_sync(0xffffffffu, dtc, off));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = dtc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = red[0];
+    for (int k = 1; k < kFT / 32; ++k) m = fmin(m, red[k]);
+    v.S.blockmin[blockIdx.x] = m;
+  }
+}
+
+// dt reduction + AdaptiveTimeStep (single block).
+__global__ void dt_finalize_kernel(const double* __restrict__ blockmin, int nb, StepScalars* sc) {
+  __shared__ double red[32];
+  if (sc->stop) return;
+  double m = DBL_MAX;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) m = fmin(m, blockmin[b]);
+  for (int off = 16; off > 0; off >>= 1) m = fmin(m, __shfl_down_sync(0xffffffffu, m, off));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < (int)(blockDim.x / 32); ++k) m = fmin(m, red[k]);
+    m = fmin(red[0], m);
+    double dtmin = sc->deltatint;
+    if (dtmin > m) dtmin = m;
+    sc->deltatmin = dtmin;
+    double dt = sc->deltat;
+    const double dti = sc->deltatint;
+    if (dti > dtmin) dt = (dt < dtmin) ? 2.0 * dt * dtmin / (dt + dtmin) : dtmin;
+    else dt = (dti != dt) ? 2.0 * dt * dti / (dt + dti) : dti;
+    sc->deltat = dt;
+    if (dt < (dti / 1.0e5)) {
+      sc->status |= ST_DT_COLLAPSE;
+      sc->stop = 1;  // the reference throws here (Source/Domain.cpp:150-151)
+    }
+  }
+}
+
+// Begin of step: Solve's `Time < tf` test and Move_MVerlet's first-step ct.
+__global__ void begin_kernel(StepScalars* sc, int scheme) {
+  if (sc->stop) return;
+  if (!(sc->time < sc->t_stop)) {
+    sc->stop = 1;
+    return;
+  }
+  if (scheme == PSPH_MVERLET && sc->first_step) sc->ct = 30;  // Source/Particle.cpp:191-195
+}
+
+// End of step: Time += deltat and the per-particle counters, once per domain.
+__global__ void end_kernel(StepScalars* sc, int scheme, int shepard_step) {
+  if (sc->stop) return;
+  sc->time += sc->deltat;
+  sc->steps += 1;
+  if (scheme == PSPH_MVERLET) {
+    sc->ct = (sc->ct == 30) ? 0 : sc->ct + 1;
+    sc->shepard_counter = (sc->shepard_counter == shepard_step) ? 0 : sc->shepard_counter + 1;
+  }
+  sc->first_step = 0;
+}
+
+// Pair export: candidate (which=0) or in-support (which=1) pairs in reference
+// orientation, as original indices; only pairs with at least one free particle
+// (Source/Domain.cpp:844).
+template <int DIM>
+__global__ void pairs_export_kernel(DevView v, int which, long long* out, long long cap,
+                                    unsigned long long* counter) {
+  const int n = v.sc->n;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Persist& P = cur_persist(v);
+  const GridDev& g = v.g;
+  const int cell = v.S.cellid[i];
+  if (cell < 0) return;
+  const PClass* CT = v.cls;
+  const PClass& Ci = CT[P.cls[i]];
+  const CellCoord ci = decode(g, cell);
+  const int oi = P.orig[i];
+  const double4_32a xi = P.X4[i];
+  for_neighbor_ranges<DIM>(g, ci, v.S.start, [&](int lo, int hi) {
+    for (int j = lo; j < hi; ++j) {
+      if (j == i) continue;
+      const PClass& Cj = CT[P.cls[j]];
+      if (!Ci.is_free && !Cj.is_free) continue;
+      const CellCoord cj = decode(g, v.S.cellid[j]);
+      const int oj = P.orig[j];
+      if (!first_of_pair(g, ci, cj, oi, oj)) continue;  // each unordered pair once, from its first particle
+      if (which == 1) {
+        const double4_32a xj = P.X4[j];
+        const double hb = (Ci.h + Cj.h) / 2;
+        double x0 = xi.x - xj.x, x1 = xi.y - xj.y, x2 = xi.z - xj.z;
+        periodic_fix(g, x0, x1, x2, hb, ci, cj);
+        // the reference's expression, without contraction: sqrt(dot)/h <= Cellfac
+        const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(x0, x0), __dmul_rn(x1, x1)), __dmul_rn(x2, x2));
+        if (!(__ddiv_rn(__dsqrt_rn(r2), hb) <= g.cellfac)) continue;
+      }
+      const unsigned long long slot = atomicAdd(counter, 1ull);
+      if ((long long)slot < cap) {
+        out[2 * slot] = oi;
+        out[2 * slot + 1] = oj;
+      }
+    }
+  });
+}
+
+inline int nblk(int n, int bt) { return n <= 0 ? 1 : (n + bt - 1) / bt; }
+
+template <int DIM>
+void prepare_dispatch(const DevView& v, cudaStream_t st) {
+  const int nb = nblk(v.ncap, kFT);
+  switch (v.o.kt) {
+    case 0: prepare_wall_kernel<DIM, 0><<<nb, kFT, 0, st>>>(v); break;
+    case 1: prepare_wall_kernel<DIM, 1><<<nb, kFT, 0, st>>>(v); break;
+    default: prepare_wall_kernel<DIM, 2><<<nb, kFT, 0, st>>>(v); break;
+  }
+}
+
+template <int DIM>
+void forces_dispatch(const DevView& v, cudaStream_t st) {
+  const int nb = nblk(v.ncap, kFT);
+  if (v.o.has_solid) {
+    switch (v.o.kt) {
+      case 0: forces_solid_kernel<DIM, 0><<<nb, kFT, 0, st>>>(v); break;
+      case 1: forces_solid_kernel<DIM, 1><<<nb, kFT, 0, st>>>(v); break;
+      default: forces_solid_kernel<DIM, 2><<<nb, kFT, 0, st>>>(v); break;
+    }
+  } else {
+    switch (v.o.kt) {
+      case 0: forces_fluid_kernel<DIM, 0><<<nb, kFT, 0, st>>>(v); break;
+      case 1: forces_fluid_kernel<DIM, 1><<<nb, kFT, 0, st>>>(v); break;
+      default: forces_fluid_kernel<DIM, 2><<<nb, kFT, 0, st>>>(v); break;
+    }
+  }
+}
+
+}  // namespace
+
+int forces_blocks(int ncap) { return nblk(ncap, kFT); }
+
+void launch_prepare(const DevView& v, cudaStream_t st) {
+  if (v.o.dim == 2) prepare_dispatch<2>(v, st);
+  else prepare_dispatch<3>(v, st);
+}
+
+void launch_wall(const DevView&, cudaStream_t) {}  // fused into launch_prepare
+
+void launch_forces(const DevView& v, cudaStream_t st) {
+  if (v.o.dim == 2) forces_dispatch<2>(v, st);
+  else forces_dispatch<3>(v, st);
+}
+
+void launch_dt(const DevView& v, cudaStream_t st) {
+  dt_finalize_kernel<<<1, 1024, 0, st>>>(v.S.blockmin, forces_blocks(v.ncap), v.sc);
+}
+
+void launch_begin(const DevView& v, cudaStream_t st) { begin_kernel<<<1, 1, 0, st>>>(v.sc, v.o.scheme); }
+
+void launch_end(const DevView& v, cudaStream_t st) {
+  end_kernel<<<1, 1, 0, st>>>(v.sc, v.o.scheme, v.o.shepard_step);
+}
+
+void launch_pairs_export(const DevView& v, int which, long long* out, long long cap, unsigned long long* counter,
+                         cudaStream_t st) {
+  const int nb = nblk(v.ncap, kFT);
+  if (v.o.dim == 2) pairs_export_kernel<2><<<nb, kFT, 0, st>>>(v, which, out, cap, counter);
+  else pairs_export_kernel<3><<<nb, kFT, 0, st>>>(v, which, out, cap, counter);
+}
+
+}  // namespace psph

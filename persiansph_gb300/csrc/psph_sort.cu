@@ -1,0 +1,230 @@
+// Cell list as a deterministic counting sort (replaces CellReset + ListGenerate,
+// Source/Domain.cpp:662-806, and the per-step pair arrays of MainNeighbourSearch).
+//
+//   bin      cell key per particle, exactly ListGenerate's floor/clamp rule;
+//            key = ncells for a particle that ListGenerate would drop into a
+//            periodic ghost column (it then sits in no list), ncells+1 for one
+//            that CheckParticleLeave removed.
+//   scan     exclusive prefix of the per-cell counts (3-phase, block-level).
+//   scatter  atomic slot inside its cell's segment.
+//   rank     deterministic order inside each cell: by original index, so the
+//            sorted state depends only on positions, never on atomic timing.
+//   reorder  gathers every persistent field into the new order (HBM-bound).
+#include <cstdio>
+
+#include "psph_device.cuh"
+
+namespace psph {
+
+namespace {
+
+constexpr int kBT = 256;
+
+__global__ void bin_kernel(GridDev g, DevView v, const uint8_t* __restrict__ alive,
+                           int* __restrict__ key, int* __restrict__ count, StepScalars* sc, int dim) {
+  if (sc->stop) return;
+  const double4_32a* __restrict__ X4 = cur_persist(v).X4;
+  const int n = sc->n;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    int k;
+    if (!alive[i]) {
+      k = g.ncells + 1;
+    } else {
+      const double4_32a x = X4[i];
+      const double xs[3] = {x.x, x.y, x.z};
+      int c[3] = {0, 0, 0};
+      bool orphan = false, out = false;
+      for (int d = 0; d < dim; ++d) {
+        int cd = (int)floor((xs[d] - g.blpf[d]) / g.cell_size[d]);
+        if (cd < 0) {
+          if ((g.blpf[d] - xs[d]) <= g.hmax) cd = 0;
+          else out = true;
+        }
+        if (cd >= g.cn_ref[d]) {
+          if ((xs[d] - g.trpr[d]) <= g.hmax) cd = g.cn_ref[d] - 1;
+          else out = true;
+        }
+        if (cd >= g.nc[d]) orphan = true;  // periodic ghost column: overwritten by the copy
+        c[d] = cd;
+      }
+      if (out) {
+        atomicOr(&sc->status, ST_OUT_OF_GRID);
+        k = g.ncells + 1;
+      } else if (orphan) {
+        k = g.ncells;
+      } else {
+        k = cell_linear(g, c[0], c[1], c[2]);
+      }
+    }
+    key[i] = k;
+    atomicAdd(&count[k], 1);
+  }
+}
+
+// Phase 1: in-block exclusive scan of `in` (len entries), block totals to sums.
+__global__ void scan_blocks(const int* __restrict__ in, int* __restrict__ out, int* __restrict__ sums, int len) {
+  __shared__ int warp_tot[32];
+  const int base = blockIdx.x * 1024;
+  const int t = threadIdx.x;
+  const int i = base + t;
+  int v = (i < len) ? in[i] : 0;
+  const int lane = t & 31, w = t >> 5;
+  int incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) warp_tot[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    int s = warp_tot[lane];
+    int si = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, si, o);
+      if (lane >= o) si += y;
+    }
+    warp_tot[lane] = si - s;  // exclusive warp offsets
+    if (lane == 31) sums[blockIdx.x] = si;
+  }
+  __syncthreads();
+  if (i < len) out[i] = incl - v + warp_tot[w];
+}
+
+// Phase 2: one block scans the block totals (exclusive), writes the grand total.
+__global__ void scan_sums(int* __restrict__ sums, int nb, int* __restrict__ total_out) {
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < nb; base += 1024) {
+    const int t = threadIdx.x, i = base + t;
+    int v = (i < nb) ? sums[i] : 0;
+    const int lane = t & 31, w = t >> 5;
+    __shared__ int wt[32];
+    int incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane == 31) wt[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+      int s = wt[lane], si = s;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, si, o);
+        if (lane >= o) si += y;
+      }
+      wt[lane] = si - s;
+    }
+    __syncthreads();
+    int excl = incl - v + wt[w] + carry;
+    if (i < nb) sums[i] = excl;
+    __syncthreads();
+    if (t == 1023) carry = excl + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total_out = carry;
+}
+
+__global__ void scan_add(int* __restrict__ out, const int* __restrict__ sums, int len) {
+  const int i = blockIdx.x * 1024 + threadIdx.x;
+  if (i < len) out[i] += sums[blockIdx.x];
+}
+
+__global__ void scatter_kernel(const int* __restrict__ key, const int* __restrict__ start, int* __restrict__ fill,
+                               int* __restrict__ tmp_perm, const StepScalars* sc) {
+  if (sc->stop) return;
+  const int n = sc->n;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int k = key[i];
+    tmp_perm[start[k] + atomicAdd(&fill[k], 1)] = i;
+  }
+}
+
+__global__ void rank_kernel(const int* __restrict__ key, const int* __restrict__ start,
+                            const int* __restrict__ tmp_perm, DevView v, int* __restrict__ perm,
+                            const StepScalars* sc, int ncells) {
+  if (sc->stop) return;
+  const int* __restrict__ orig = cur_persist(v).orig;
+  const int n = sc->n;
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+    const int i = tmp_perm[s];
+    const int k = key[i];
+    if (k <= ncells) {
+      const int lo = start[k], hi = start[k + 1];
+      const int mine = orig[i];
+      int r = 0;
+      for (int t = lo; t < hi; ++t) r += (orig[tmp_perm[t]] < mine);
+      perm[lo + r] = i;
+    } else {
+      perm[s] = i;
+    }
+  }
+}
+
+__global__ void reorder_kernel(DevView v, const int* __restrict__ perm, const int* __restrict__ key,
+                               const int* __restrict__ start, int* __restrict__ cellid, uint8_t* __restrict__ alive,
+                               const StepScalars* sc, int ncells, int has_solid, int dyn_mu) {
+  if (sc->stop) return;
+  const Persist& src = cur_persist(v);
+  const Persist& dst = next_persist(v);
+  const int n_new = start[ncells + 1];
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n_new; s += gridDim.x * blockDim.x) {
+    const int i = perm[s];
+    dst.X4[s] = src.X4[i];
+    dst.V4[s] = src.V4[i];
+    dst.H4[s] = src.H4[i];
+    if (src.H4b) dst.H4b[s] = src.H4b[i];
+    dst.cls[s] = src.cls[i];
+    dst.orig[s] = src.orig[i];
+    const int k = key[i];
+    cellid[s] = (k < ncells) ? k : -1;
+    alive[s] = 1;
+    if (dyn_mu) dst.mu[s] = src.mu[i];
+    if (has_solid) {
+      const double* srcs[7] = {src.sigma, src.sigma_h, src.strain, src.strain_h, src.shear, src.shear_h, src.tir};
+      double* dsts[7] = {dst.sigma, dst.sigma_h, dst.strain, dst.strain_h, dst.shear, dst.shear_h, dst.tir};
+#pragma unroll
+      for (int a = 0; a < 7; ++a)
+#pragma unroll
+        for (int e = 0; e < 9; ++e) dsts[a][9 * (size_t)s + e] = srcs[a][9 * (size_t)i + e];
+    }
+  }
+}
+
+__global__ void finish_sort_kernel(const int* __restrict__ start, StepScalars* sc, int ncells) {
+  if (sc->stop) return;
+  sc->n_cells = start[ncells];
+  sc->n = start[ncells + 1];
+  sc->buf ^= 1;
+}
+
+inline int grid_for(int n) {
+  int b = (n + kBT - 1) / kBT;
+  return b < 1 ? 1 : b;
+}
+
+}  // namespace
+
+void launch_sort(const DevView& v, cudaStream_t st) {
+  const GridDev& g = v.g;
+  const Scratch& S = v.S;
+  const int len = g.ncells + 2;
+  cudaMemsetAsync(S.count, 0, sizeof(int) * (size_t)len, st);
+  bin_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(g, v, v.alive, S.key, S.count, v.sc, v.o.dim);
+  const int nb = (len + 1023) / 1024;
+  scan_blocks<<<nb, 1024, 0, st>>>(S.count, S.start, S.block_sums, len);
+  scan_sums<<<1, 1024, 0, st>>>(S.block_sums, nb, S.start + len);
+  scan_add<<<nb, 1024, 0, st>>>(S.start, S.block_sums, len);
+  cudaMemsetAsync(S.count, 0, sizeof(int) * (size_t)len, st);
+  scatter_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(S.key, S.start, S.count, S.tmp_perm, v.sc);
+  rank_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(S.key, S.start, S.tmp_perm, v, S.perm, v.sc, g.ncells);
+  reorder_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(v, S.perm, S.key, S.start, S.cellid, v.alive, v.sc,
+                                                    g.ncells, v.o.has_solid, v.o.dyn_mu);
+  finish_sort_kernel<<<1, 1, 0, st>>>(S.start, v.sc, g.ncells);
+}
+
+}  // namespace psph

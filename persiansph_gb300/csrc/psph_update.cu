@@ -1,0 +1,349 @@
+// Fused per-particle update: Domain::Move (Source/Domain.cpp:1299-1325) ->
+// Particle::Move (Source/Particle.cpp:119-144) with Move_Leapfrog (:561-596)
+// or Move_MVerlet (:189-274), the material update Mat1 (:146-186), Mat2*
+// (:276-318, :598-639) or Mat3* (:320-482, :641-795), the periodic wrap, and
+// CheckParticleLeave's test (Source/Domain.cpp:517-547; removal happens in the
+// next cell sort). One thread per particle, state read and written once.
+#include "psph_device.cuh"
+
+namespace psph {
+
+namespace {
+
+constexpr int kUT = 128;
+
+PSPH_D void mat_mult(const double* A, const double* B, double* M) {  // External/matvec.h:814-820
+  M[0] = A[2] * B[6] + A[1] * B[3] + A[0] * B[0];
+  M[1] = A[2] * B[7] + A[1] * B[4] + A[0] * B[1];
+  M[2] = A[2] * B[8] + A[1] * B[5] + A[0] * B[2];
+  M[3] = A[5] * B[6] + B[3] * A[4] + B[0] * A[3];
+  M[4] = A[5] * B[7] + A[4] * B[4] + B[1] * A[3];
+  M[5] = A[5] * B[8] + A[4] * B[5] + B[2] * A[3];
+  M[6] = A[8] * B[6] + B[3] * A[7] + B[0] * A[6];
+  M[7] = B[7] * A[8] + B[4] * A[7] + B[1] * A[6];
+  M[8] = A[8] * B[8] + B[5] * A[7] + B[2] * A[6];
+}
+
+PSPH_D double J2of(const double* S) {
+  return 0.5 * (S[0] * S[0] + 2.0 * S[1] * S[3] + 2.0 * S[2] * S[6] + S[4] * S[4] + 2.0 * S[5] * S[7] + S[8] * S[8]);
+}
+
+PSPH_D double OIe(int e) { return (e == 0 || e == 4 || e == 8) ? 1.0 : 0.0; }
+
+// 2G(D - tr D/3 I) + S W^T + W S (solid, around ShearStress)
+PSPH_D void mat2_rate(const double* SR, const double* RR, const double* SS, double G, double* X) {
+  double RRT[9], SRT[9], RS[9];
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) RRT[3 * r + c] = RR[3 * c + r];
+  mat_mult(SS, RRT, SRT);
+  mat_mult(RR, SS, RS);
+  const double s_tr = 1.0 / 3.0 * (SR[0] + SR[4] + SR[8]);
+  const double g2 = 2.0 * G;
+  for (int e = 0; e < 9; ++e) X[e] = (((SR[e] - OIe(e) * s_tr) * g2) + SRT[e]) + RS[e];
+}
+
+// K tr(D) I + 2G(D - tr D/3 I) + Sigma W^T + W Sigma (soil, around Sigma)
+PSPH_D void mat3_rate(const double* SR, const double* RR, const double* Sg, double K, double G, double* X) {
+  double RRT[9], SRT[9], RS[9];
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) RRT[3 * r + c] = RR[3 * c + r];
+  mat_mult(Sg, RRT, SRT);
+  mat_mult(RR, Sg, RS);
+  const double I1s = SR[0] + SR[4] + SR[8];
+  const double sK = I1s * K, s3 = 1.0 / 3.0 * I1s, g2 = 2.0 * G;
+  for (int e = 0; e < 9; ++e) X[e] = ((OIe(e) * sK + ((SR[e] - OIe(e) * s3) * g2)) + SRT[e]) + RS[e];
+}
+
+PSPH_D double dp_apex(double* S, double alpha, double kf) {
+  double I1 = S[0] + S[4] + S[8];
+  if ((kf - alpha * I1) < 0.0) {
+    const double Ratio = (alpha == 0.0) ? 0.0 : kf / alpha;
+    S[0] -= 1.0 / 3.0 * (I1 - Ratio);
+    S[4] -= 1.0 / 3.0 * (I1 - Ratio);
+    S[8] -= 1.0 / 3.0 * (I1 - Ratio);
+    I1 = Ratio;
+  }
+  return I1;
+}
+
+PSPH_D void deviator(const double* S, double I1, double* D) {
+  const double s = 1.0 / 3.0 * I1;
+  for (int e = 0; e < 9; ++e) D[e] = S[e] - OIe(e) * s;
+}
+
+// Drucker-Prager return (Source/Particle.cpp:357-425 / :677-746).
+// Sig: elastic predictor (in/out); Sn: stress at the start of the step;
+// fac: dt (leapfrog / restart) or 2 dt (Verlet). Returns the last deviator.
+PSPH_D void dp_return(const PClass& C, double I22, double* Sig, const double* Sn, const double* SR, double I1strain,
+                      double fac, double* SS) {
+  double alpha, kf;
+  const double phi = C.phi, c = C.coh;
+  if (I22 == 0.0) {
+    alpha = tan(phi) / sqrt(9.0 + 12.0 * tan(phi) * tan(phi));
+    kf = 3.0 * c / sqrt(9.0 + 12.0 * tan(phi) * tan(phi));
+  } else {
+    alpha = (2.0 * sin(phi)) / (sqrt(3.0) * (3.0 - sin(phi)));
+    kf = (6.0 * c * cos(phi)) / (sqrt(3.0) * (3.0 - sin(phi)));
+  }
+  const double K = C.k_mod, G = C.g_mod;
+  double I1 = dp_apex(Sig, alpha, kf);
+  deviator(Sig, I1, SS);
+  double J2 = J2of(SS);
+  if ((sqrt(J2) + alpha * I1 - kf) > 0.0) {
+    deviator(Sn, Sn[0] + Sn[4] + Sn[8], SS);
+    J2 = J2of(SS);
+    if (sqrt(J2) > 0.0) {
+      double sum = SS[0] * SR[0];
+      for (int e = 1; e < 9; ++e) sum = sum + SS[e] * SR[e];
+      const double gj = G / sqrt(J2);
+      double dL, s;
+      if (C.fail == 2) {
+        dL = 1.0 / (9.0 * alpha * alpha * K + G) * ((3.0 * alpha * K * I1strain) + (G / sqrt(J2)) * sum);
+        s = 3.0 * alpha * K;
+      } else {
+        dL = 1.0 / (9.0 * alpha * K * 3.0 * sin(C.psi) + G) * ((3.0 * alpha * K * I1strain) + (G / sqrt(J2)) * sum);
+        s = 3.0 * 3.0 * sin(C.psi) * K;
+      }
+      for (int e = 0; e < 9; ++e) {
+        const double Ie = (e == 8) ? I22 : OIe(e);
+        Sig[e] = Sig[e] - ((Ie * s + SS[e] * gj) * dL) * fac;
+      }
+    }
+    I1 = dp_apex(Sig, alpha, kf);
+    deviator(Sig, I1, SS);
+    J2 = J2of(SS);
+    if ((sqrt(J2) + alpha * I1 - kf) > 0.0 && sqrt(J2) > 0.0) {
+      const double s1 = I1 / 3.0, s2 = (kf - alpha * I1) / sqrt(J2);
+      for (int e = 0; e < 9; ++e) Sig[e] = OIe(e) * s1 + SS[e] * s2;
+    }
+  }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kUT) update_kernel(DevView v) {
+  const StepScalars* sc = v.sc;
+  if (sc->stop) return;
+  const Persist& P = cur_persist(v);
+  const int n = sc->n;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const PClass& C = v.cls[P.cls[s]];
+  if (!C.is_free) return;
+  const Options& o = v.o;
+  const GridDev& g = v.g;
+  const double dt = sc->deltat;
+  const int first = sc->first_step;
+  const int ct = sc->ct;
+  double4_32a X = P.X4[s];
+  double4_32a V = P.V4[s];
+  double4_32a H = P.H4[s];
+  const double4_32a A = v.S.A4[s];
+  double x[3] = {X.x, X.y, X.z}, vel[3] = {V.x, V.y, V.z};
+  const double a[3] = {A.x, A.y, A.z};
+  const double drho = A.w;
+  double rho = X.w;
+  if (o.scheme == PSPH_MVERLET) {
+    // Move_MVerlet (Source/Particle.cpp:189-274)
+    double vx[3] = {0.0, 0.0, 0.0};
+    if (o.xsph != 0.0) {
+      const double4_32a w = v.S.vxsph4[s];
+      vx[0] = w.x; vx[1] = w.y; vx[2] = w.z;
+    }
+    for (int d = 0; d < 3; ++d) x[d] += dt * (vel[d] + vx[d]) + 0.5 * dt * dt * a[d];
+    const bool shep = C.shepard && (sc->shepard_counter == o.shepard_step);
+    const double zw = v.S.zwab[s];
+    double rhob = H.w;
+    double vb[3] = {H.x, H.y, H.z};
+    if (ct == 30) {
+      if (shep && zw > 0.6) {
+        const double sd = v.S.sumden[s];
+        rhob = sd / zw;
+        rho = sd / zw;
+      } else {
+        rhob = rho;
+        rho += dt * drho;
+      }
+      for (int d = 0; d < 3; ++d) {
+        vb[d] = vel[d];
+        vel[d] += dt * a[d];
+      }
+    } else {
+      if (shep && zw > 0.6) {
+        const double sd = v.S.sumden[s];
+        rhob = sd / zw;
+        rho = sd / zw;
+      } else {
+        const double dens = rho;
+        rho = rhob + 2.0 * dt * drho;
+        rhob = dens;
+      }
+      for (int d = 0; d < 3; ++d) {
+        const double t = vel[d];
+        vel[d] = vb[d] + 2 * dt * a[d];
+        vb[d] = t;
+      }
+    }
+    H = make_double4_32a(vb[0], vb[1], vb[2], rhob);
+  } else {
+    // Move_Leapfrog (Source/Particle.cpp:561-596)
+    double va[3] = {H.x, H.y, H.z};
+    double rhoa = H.w;
+    if (first) {
+      rhoa = rho - dt / 2.0 * drho;
+      for (int d = 0; d < 3; ++d) va[d] = vel[d] - dt / 2.0 * a[d];
+    }
+    const double rhob = rhoa;
+    rhoa += dt * drho;
+    rho = (rhoa + rhob) / 2.0;
+    double vb[3];
+    for (int d = 0; d < 3; ++d) {
+      vb[d] = va[d];
+      va[d] += dt * a[d];
+      vel[d] = (va[d] + vb[d]) / 2.0;
+      x[d] += dt * va[d];
+    }
+    H = make_double4_32a(va[0], va[1], va[2], rhoa);
+    P.H4b[s] = make_double4_32a(vb[0], vb[1], vb[2], rhob);
+  }
+  double p = V.w;
+  const int mat = C.material;
+  if (mat == 1) {
+    // Mat1 (Source/Particle.cpp:146-186)
+    p = eos(C.pres_eq, C.cs, C.p0, rho, C.rho0);
+    if (o.need_sr || o.dyn_mu) {
+      const double* S = v.S.strain_rate + 9 * (size_t)s;
+      double temp = 0.0;
+      if (o.need_sr)
+        temp = (S[0] * S[0] + 2.0 * S[1] * S[3] + 2.0 * S[2] * S[6] + S[4] * S[4] + 2.0 * S[5] * S[7] + S[8] * S[8]);
+      const double shear_rate = sqrt(0.5 * temp), sbar = sqrt(2.0 * temp);
+      v.S.shear_rate[s] = shear_rate;
+      v.S.sbar[s] = sbar;
+      if (o.dyn_mu) {
+        double mu = P.mu[s];
+        if (C.les) {
+          const double ch = C.csmag * C.h;
+          mu = C.mu_ref + C.rho0 * (ch * ch) * sbar;
+        }
+        if (C.t0 > 0.0) {
+          if (C.vis_m == 0) mu = (shear_rate != 0.0) ? C.mu_ref + C.t0 * (1 - exp(-C.bm * shear_rate)) / shear_rate
+                                                    : C.mu_ref + C.t0 * C.bm;
+          else mu = (1000.0 * C.mu_ref + C.mu_ref * C.mu_ref * 1000.0 / C.t0 * shear_rate) /
+                    (1 + 1000.0 * C.mu_ref / C.t0 * shear_rate);
+        }
+        P.mu[s] = mu;
+      }
+    }
+  } else {
+    const double* SR = v.S.strain_rate + 9 * (size_t)s;
+    const double* RR = v.S.rotation_rate + 9 * (size_t)s;
+    double* Sig = P.sigma + 9 * (size_t)s;
+    double* Sh = P.sigma_h + 9 * (size_t)s;
+    double* So = v.S.sigma_o + 9 * (size_t)s;
+    double* E = P.strain + 9 * (size_t)s;
+    double* Eh = P.strain_h + 9 * (size_t)s;
+    double* Eo = v.S.strain_o + 9 * (size_t)s;
+    const double I22 = (DIM == 2) ? 0.0 : 1.0;
+    const bool lf = (o.scheme != PSPH_MVERLET);
+    if (mat == 2) {
+      // Mat2Leapfrog / Mat2MVerlet (Source/Particle.cpp:598-639 / :276-318)
+      p = eos(C.pres_eq, C.cs, C.p0, rho, C.rho0);
+      double* SS = P.shear + 9 * (size_t)s;
+      double* SSh = P.shear_h + 9 * (size_t)s;
+      double* SSo = v.S.shear_o + 9 * (size_t)s;
+      double X9[9];
+      mat2_rate(SR, RR, SS, C.g_mod, X9);
+      double* target;
+      if (lf) {
+        if (first)
+          for (int e = 0; e < 9; ++e) SSh[e] = X9[e] * (-dt / 2.0) + SS[e];
+        for (int e = 0; e < 9; ++e) {
+          SSo[e] = SSh[e];
+          SSh[e] = X9[e] * dt + SSh[e];
+        }
+        target = SSh;
+      } else {
+        for (int e = 0; e < 9; ++e) {
+          const double old = SS[e];
+          SS[e] = (ct == 30) ? X9[e] * dt + SS[e] : X9[e] * (2.0 * dt) + SSh[e];
+          SSh[e] = old;
+        }
+        target = SS;
+      }
+      if (C.fail == 1) {
+        const double r = C.sigmay / sqrt(3.0 * J2of(target));
+        const double f = (1.0 < r) ? 1.0 : r;
+        for (int e = 0; e < 9; ++e) target[e] = target[e] * f;
+      }
+      if (lf)
+        for (int e = 0; e < 9; ++e) SS[e] = (SSh[e] + SSo[e]) * (1.0 / 2.0);
+      for (int e = 0; e < 9; ++e) Sig[e] = OIe(e) * -p + SS[e];
+    } else {
+      // Mat3Leapfrog / Mat3MVerlet (Source/Particle.cpp:641-795 / :320-482)
+      double X9[9], Sn[9], SSd[9];
+      mat3_rate(SR, RR, Sig, C.k_mod, C.g_mod, X9);
+      const double I1strain = SR[0] + SR[4] + SR[8];
+      for (int e = 0; e < 9; ++e) Sn[e] = Sig[e];
+      bool have_dev = false;
+      if (lf) {
+        if (first)
+          for (int e = 0; e < 9; ++e) Sh[e] = X9[e] * (-dt / 2.0) + Sig[e];
+        for (int e = 0; e < 9; ++e) {
+          So[e] = Sh[e];
+          Sh[e] = X9[e] * dt + Sh[e];
+        }
+        if (C.fail > 1) { dp_return(C, I22, Sh, Sn, SR, I1strain, dt, SSd); have_dev = true; }
+        for (int e = 0; e < 9; ++e) Sig[e] = (Sh[e] + So[e]) * (1.0 / 2.0);
+      } else {
+        for (int e = 0; e < 9; ++e) Sig[e] = (ct == 30) ? X9[e] * dt + Sig[e] : X9[e] * (2.0 * dt) + Sh[e];
+        for (int e = 0; e < 9; ++e) Sh[e] = Sn[e];
+        if (C.fail > 1) { dp_return(C, I22, Sig, Sn, SR, I1strain, (ct == 30) ? dt : 2.0 * dt, SSd); have_dev = true; }
+      }
+      if (have_dev && P.shear) {
+        double* SS = P.shear + 9 * (size_t)s;
+        for (int e = 0; e < 9; ++e) SS[e] = SSd[e];
+      }
+    }
+    // strain integration (shared by Mat2 and Mat3)
+    if (lf) {
+      if (first)
+        for (int e = 0; e < 9; ++e) Eh[e] = SR[e] * (-dt / 2.0) + E[e];
+      for (int e = 0; e < 9; ++e) {
+        Eo[e] = Eh[e];
+        Eh[e] = SR[e] * dt + Eh[e];
+        E[e] = (Eh[e] + Eo[e]) * (1.0 / 2.0);
+      }
+    } else {
+      for (int e = 0; e < 9; ++e) {
+        const double old = E[e];
+        E[e] = (ct == 30) ? SR[e] * dt + E[e] : SR[e] * (2.0 * dt) + Eh[e];
+        Eh[e] = old;
+      }
+    }
+  }
+  // periodic wrap (Source/Particle.cpp:128-142) and CheckParticleLeave's test
+  bool out = false;
+  for (int d = 0; d < 3; ++d) {
+    if (g.dom_size[d] > 0.0) {
+      if (x[d] > g.trpr[d]) x[d] -= g.dom_size[d];
+      if (x[d] < g.blpf[d]) x[d] += g.dom_size[d];
+    }
+    out |= (x[d] > g.trpr[d]) || (x[d] < g.blpf[d]);
+  }
+  if (DIM == 2) vel[2] = 0.0;  // StartAcceleration zeroes v_z in 2D (Source/Domain.cpp:1014)
+  P.X4[s] = make_double4_32a(x[0], x[1], x[2], rho);
+  P.V4[s] = make_double4_32a(vel[0], vel[1], vel[2], p);
+  P.H4[s] = H;
+  if (out) v.alive[s] = 0;
+}
+
+}  // namespace
+
+void launch_update(const DevView& v, cudaStream_t st) {
+  const int nb = (v.ncap + kUT - 1) / kUT;
+  if (v.o.dim == 2) update_kernel<2><<<nb > 0 ? nb : 1, kUT, 0, st>>>(v);
+  else update_kernel<3><<<nb > 0 ? nb : 1, kUT, 0, st>>>(v);
+}
+
+int launches_per_step(const DevView&) { return 14; }
+
+}  // namespace psph

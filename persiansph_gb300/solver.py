@@ -1,0 +1,132 @@
+"""Host side of one GPU domain: a thin owner of a psph_ctx (include/psph.h).
+
+`GpuDomain` is what `Domain.Solve` drives and what the parity tests and the
+benchmark call. Every call goes through the C ABI of the CUDA library; a
+non-zero status raises `PsphError` (the reference throws `Fatal` there).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from .abi import (ALL_FIELDS, PsphConfig, PsphError, PsphGrid, PsphIntegrator, field_dtype, field_shape,
+                  load_library, particles_struct)
+from .particles import ParticleSet
+
+
+class GpuDomain:
+    def __init__(self, cfg: PsphConfig, grid: PsphGrid | None = None, integ: PsphIntegrator | None = None):
+        self._lib = load_library()
+        self._ctx = C.c_void_p()
+        self.cfg = cfg
+        st = self._lib.psph_create(C.byref(cfg), C.byref(self._ctx))
+        self._check(st)
+        if grid is not None:
+            self._check(self._lib.psph_set_grid(self._ctx, C.byref(grid)))
+        if integ is not None:
+            self._check(self._lib.psph_set_integrator(self._ctx, C.byref(integ)))
+        self._uploaded = None
+
+    def _check(self, st: int):
+        if st != 0:
+            msg = self._lib.psph_last_error(self._ctx).decode() if self._ctx else ""
+            raise PsphError(st, msg)
+
+    def close(self):
+        if self._ctx:
+            self._lib.psph_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- data movement --------------------------------------------------------
+    def upload(self, pset: ParticleSet, initial: bool = True):
+        arrs = {f: np.ascontiguousarray(pset.get(f)) for f in ALL_FIELDS if pset.has(f)}
+        for req in ("x", "h", "density", "mass"):
+            if req not in arrs:
+                arrs[req] = np.ascontiguousarray(pset.get(req))
+        s = particles_struct(arrs, pset.n)
+        self._check(self._lib.psph_upload(self._ctx, C.byref(s), int(initial)))
+        self._uploaded = pset
+
+    def step(self, nsteps: int, t_stop: float = float("inf")) -> int:
+        done = C.c_int64(0)
+        self._check(self._lib.psph_step(self._ctx, int(nsteps), float(t_stop), C.byref(done)))
+        return done.value
+
+    @property
+    def n(self) -> int:
+        return int(self._lib.psph_num_particles(self._ctx))
+
+    def download_fields(self, fields=ALL_FIELDS) -> dict:
+        n = self.n
+        out = {f: np.zeros(field_shape(f, n), field_dtype(f)) for f in fields}
+        s = particles_struct(out, n)
+        self._check(self._lib.psph_download(self._ctx, C.byref(s)))
+        return out
+
+    def original_index(self) -> np.ndarray:
+        out = np.zeros(max(self.n, 1), np.int64)
+        self._check(self._lib.psph_original_index(self._ctx, out.ctypes.data_as(C.POINTER(C.c_int64))))
+        return out[: self.n]
+
+    def download(self, base: ParticleSet | None = None) -> ParticleSet:
+        """Current state as a ParticleSet. Fields the device does not track for
+        the chosen scheme keep their values from `base` (the uploaded set)."""
+        base = base if base is not None else self._uploaded
+        fields = self.download_fields()
+        keep = self.original_index()
+        out = ParticleSet(len(keep))
+        for f in ALL_FIELDS:
+            arr = fields[f]
+            if base is not None and base.has(f):
+                prev = base.get(f)[keep]
+                untouched = self._untracked(f)
+                arr = prev.copy() if untouched else arr
+            out._arr[f] = np.ascontiguousarray(arr)
+        return out
+
+    def _untracked(self, f: str) -> bool:
+        lf = self.cfg.scheme == 1
+        if lf:
+            return False
+        return f in ("va", "densitya", "sigmaa", "straina", "shear_stressa")
+
+    def pairs(self, which: int) -> np.ndarray:
+        total = C.c_int64(0)
+        self._check(self._lib.psph_pairs_export(self._ctx, which, None, 0, C.byref(total)))
+        buf = np.zeros((max(total.value, 1), 2), np.int64)
+        self._check(self._lib.psph_pairs_export(self._ctx, which, buf.ctypes.data_as(C.POINTER(C.c_int64)),
+                                                total.value, C.byref(total)))
+        return buf[: total.value]
+
+    def grid(self) -> PsphGrid:
+        g = PsphGrid()
+        self._check(self._lib.psph_get_grid(self._ctx, C.byref(g)))
+        return g
+
+    def integrator(self) -> PsphIntegrator:
+        it = PsphIntegrator()
+        self._check(self._lib.psph_get_integrator(self._ctx, C.byref(it)))
+        return it
+
+    @property
+    def time(self) -> float:
+        return self.integrator().time
+
+    def enable_timing(self, on: bool = True):
+        self._check(self._lib.psph_enable_timing(self._ctx, int(on)))
+
+    def phase_times(self):
+        buf = (C.c_double * 5)()
+        n = C.c_int(0)
+        self._check(self._lib.psph_phase_times(self._ctx, buf, 5, C.byref(n)))
+        return list(buf)
+
+    def last_launch_count(self) -> int:
+        return int(self._lib.psph_last_launch_count(self._ctx))

@@ -1,0 +1,100 @@
+"""Parity cases shared by the golden generator and the tests.
+
+Each case: builder() -> (Domain, dt, info), number of reference steps, and the
+steps after which the reference state is stored. The steps are chosen to cover
+the Modified Verlet restart (ct==30: steps 1 and 32), the Shepard
+re-initialisation (ShepardCounter==40: step 41) and the Leapfrog first step.
+"""
+from persiansph_gb300 import scenarios
+from persiansph_gb300.domain import Multiplied_density, Takeda, Shao, Incompressible_Full
+
+
+def dam2d():
+    return scenarios.dam_break_2d(dx=0.02, L=0.4, H=0.8, TL=1.6, TH=1.2)
+
+
+def dam2d_leapfrog():
+    return scenarios.dam_break_2d(dx=0.02, L=0.4, H=0.8, TL=1.6, TH=1.2, scheme=1, shepard=False)
+
+
+def poiseuille():
+    return scenarios.poiseuille(dx=2.5e-5)
+
+
+def granular():
+    return scenarios.granular_column(dx=0.01, W=0.2, aspect=1.0)
+
+
+def granular_lf_fail3():
+    return scenarios.granular_column(dx=0.01, W=0.2, aspect=2.0, scheme=1, fail=3, psi_deg=5.0, cohesion=100.0)
+
+
+def dam3d():
+    return scenarios.dam_break_3d(dx=0.04, L=0.24, H=0.2, W=0.16, TL=0.48, TH=0.32, TW=0.2)
+
+
+def fluid_options():
+    """Takeda viscosity, multiplied-density gradient, XSPH and LES on a small dam break."""
+    dom, dt, info = scenarios.dam_break_2d(dx=0.02, L=0.4, H=0.6, TL=1.0, TH=0.8, shepard=False)
+    dom.Viscosity_Eq_Set(Takeda)
+    dom.Gradient_Approach_Set(Multiplied_density)
+    dom.XSPH = 0.5
+    p = dom.particles
+    p.set("les", 1)
+    p.set("beta", 0.05)
+    return dom, dt, info
+
+
+def fluid_shao_bingham():
+    dom, dt, info = scenarios.dam_break_2d(dx=0.02, L=0.4, H=0.6, TL=1.0, TH=0.8, kernel=2, hfac=1.3,
+                                           scheme=1, shepard=False)
+    dom.Viscosity_Eq_Set(Shao)
+    p = dom.particles
+    p.set("t0", 5.0)
+    p.set("mu_ref", 0.05)
+    return dom, dt, info
+
+
+def fluid_incomp_quintic():
+    dom, dt, info = scenarios.dam_break_2d(dx=0.02, L=0.4, H=0.6, TL=1.0, TH=0.8, kernel=1, hfac=1.3)
+    dom.Viscosity_Eq_Set(Incompressible_Full)
+    p = dom.particles
+    p.set("ti", 0.2)
+    p.set("tin", 3.0)
+    p.set("ti_init_dist", 0.02)
+    p.set("pres_eq", 0)
+    return dom, dt, info
+
+
+def solid_block():
+    """Elastic (Material 2, von Mises cap) block resting on a fixed floor, leapfrog."""
+    dom, dt, info = scenarios.granular_column(dx=0.01, W=0.2, aspect=0.5, scheme=1, fail=1)
+    p = dom.particles
+    p.set("material", 2)
+    p.set("sigmay", 2.0e3)
+    p.set("pres_eq", 0)
+    p.set("ti", 0.0)
+    return dom, dt, info
+
+
+CASES = {
+    "dam2d": (dam2d, 42, (1, 2, 32, 41, 42)),
+    "dam2d_leapfrog": (dam2d_leapfrog, 5, (1, 2, 5)),
+    "poiseuille": (poiseuille, 20, (1, 5, 20)),
+    "granular": (granular, 40, (1, 2, 32, 40)),
+    "granular_lf_fail3": (granular_lf_fail3, 10, (1, 2, 10)),
+    "dam3d": (dam3d, 3, (1, 3)),
+    "fluid_options": (fluid_options, 5, (1, 5)),
+    "fluid_shao_bingham": (fluid_shao_bingham, 5, (1, 5)),
+    "fluid_incomp_quintic": (fluid_incomp_quintic, 5, (1, 5)),
+    "solid_block": (solid_block, 6, (1, 6)),
+}
+
+# AddBoxLength argument lists: dim, tag, V, Lx, Ly, Lz, r, rho, h, type, rotation, random, fixed
+BOXES = {
+    "cubic2d": (2, 1, (-0.03, -0.03, 0.0), 0.5, 0.3, 0.0, 0.005, 1000.0, 0.012, 1, 0, False, False),
+    "hex2d": (2, 1, (0.0, 0.0, 0.0), 0.2, 0.15, 0.0, 0.005, 1000.0, 0.012, 0, 0, False, False),
+    "hex2d_rot": (2, 1, (0.0, 0.0, 0.0), 0.2, 0.15, 0.0, 0.005, 1000.0, 0.012, 0, 90, False, False),
+    "cubic3d": (3, 1, (-0.06, -0.06, -0.06), 0.3, 0.2, 0.25, 0.01, 998.21, 0.024, 1, 0, False, False),
+    "hex3d": (3, 1, (0.0, 0.0, 0.0), 0.2, 0.15, 0.12, 0.01, 1000.0, 0.024, 0, 0, False, True),
+}
