@@ -1,0 +1,281 @@
+"""Benchmark: pair-interactions/s and steps/s of the 3D dam break on one GB300.
+
+Workload (default): tank 3.22 x 1.0 x 1.0 m, water column 1.2 x 0.55 x 1.0 m
+at dx = 5 mm -> 240 x 110 x 200 = 5,280,000 fluid particles plus 3 wall layers,
+Wendland C2 (h = 1.3 dx), Tait EOS c0 = 40 m/s, artificial viscosity 0.05,
+Morris viscosity, Modified Verlet + Shepard (the 4-DamBreak3D.cpp pattern).
+Synthetic, seeded lattice input built by persiansph_gb300.scenarios.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+Our arm: W untimed steps, then K steps timed with CUDA events on the solver's
+stream (inputs resident in HBM; the working set, several GB, exceeds the 129 MB
+L2, so no flush is needed). `e2e` repeats the measurement through the C ABI
+with host buffers: upload + K steps + download inside the timed region.
+The reference arm (--impl reference) times the reference algorithm on the host
+cores: the CPU oracle (a restatement of the reference, OpenMP) on a bounded
+sample of the same workload (the same tank at dx = 10 mm).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "pair-interactions/s @ 3D dam break (5.28M fluid particles)"
+UNIT = "pair-interactions/s"
+# FP64 operations per directed pair evaluation of the fluid kernel for this
+# workload's options (Wendland, Tait, artificial viscosity, Morris, squared
+# density): counted from forces_fluid_kernel with FMA = 2 and a division or
+# square root = 1 (measurement).
+FLOPS_PER_DIRECTED_PAIR = 90
+# algorithmic HBM bytes per particle of one force-kernel launch: read each
+# particle's inputs once (X4 32, V4 32, class 4, derived rho/c/p 24) and write
+# its outputs once (A4 32, zwab 8, sumden 8).
+FORCE_BYTES_PER_PARTICLE = 140
+
+
+def peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return {"hbm_gbs": d.get("hbm_gbs", 6800.0), "src": "measured"}
+    return {"hbm_gbs": 6800.0, "src": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region (SM clock, throttle reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        loaded = [s for s in sm if s > 0.5 * (max(mx) if mx else 1)] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def build_workload(dx):
+    from persiansph_gb300 import scenarios
+    return scenarios.dam_break_3d(dx=dx)
+
+
+def cpu_reference(dx_sample: float, steps: int, warmup: int, threads: int):
+    """Times the CPU oracle (restatement of the reference's OpenMP path) on the
+    same tank at a coarser lattice; returns pair-interactions/s and details."""
+    from oracle.oracle import OracleDomain
+    dom, dt, info = build_workload(dx_sample)
+    o = OracleDomain(dom.config(dt), dom.particles, initial=True)
+    if warmup:
+        o.step(warmup, threads)
+    npairs = len(o.pairs(3))
+    t0 = time.perf_counter()
+    o.step(steps, threads)
+    el = time.perf_counter() - t0
+    npairs2 = len(o.pairs(3))
+    pairs_per_step = 0.5 * (npairs + npairs2)
+    return {"value": pairs_per_step * steps / el, "steps_per_s": steps / el, "seconds": el,
+            "n": dom.particles.n, "n_fluid": info["n_fluid"], "pairs_per_step": pairs_per_step}
+
+
+def run_reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    steps = max(1, min(args.steps, 5))
+    r = cpu_reference(args.ref_dx, steps, max(1, min(args.warmup, 1)), threads)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": args.gpus,
+        "steps": steps, "warmup": 1, "ms_per_step": 1e3 * r["seconds"] / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic lattice (seeded)",
+        "config": {"workload": f"3D dam break, tank 3.22x1.0x1.0 m, column 1.2x0.55x1.0 m, sample dx={args.ref_dx} m",
+                   "particles": r["n"], "fluid": r["n_fluid"], "pairs_per_step": r["pairs_per_step"]},
+        "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{steps} steps of the 3D dam break at dx={args.ref_dx} m ({r['n']} particles)"},
+        "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "steps_per_s": r["steps_per_s"],
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--dx", type=float, default=0.005)
+    ap.add_argument("--ref-dx", type=float, default=0.01)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    if args.impl == "reference":
+        return run_reference_arm(args)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    from persiansph_gb300.solver import GpuDomain
+    from persiansph_gb300 import abi
+    import ctypes
+
+    dom, dt, info = build_workload(args.dx)
+    cfg = dom.config(dt)
+    n = dom.particles.n
+
+    gd = GpuDomain(cfg)
+    gd.upload(dom.particles, initial=True)
+    gd.step(args.warmup)
+    pc0 = gd.pair_count()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ms, done = gd.step_timed(args.steps)
+    torch.cuda.synchronize()
+    pc1 = gd.pair_count()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    pairs = pc1 - pc0
+    launches = gd.last_launch_count()
+    value_rank = pairs / (ms * 1e-3)
+    value = value_rank * world
+    steps_per_s = done / (ms * 1e-3)
+
+    # per-phase device times (separate short run, events between phases)
+    gd.enable_timing(True)
+    gd.step(3)
+    phases = gd.phase_times()
+    gd.enable_timing(False)
+    force_ms = phases[2] / 3.0
+    pairs_per_step = pairs / max(done, 1)
+    lib = abi.load_library()
+    fp64 = ctypes.c_double(0.0)
+    lib.psph_probe_fp64_peak(ctypes.byref(fp64))
+    pk = peaks()
+    achieved_gbs = FORCE_BYTES_PER_PARTICLE * n / (force_ms * 1e-3) / 1e9
+    fp64_tflops = 2 * pairs_per_step * FLOPS_PER_DIRECTED_PAIR / (force_ms * 1e-3) / 1e12
+    traffic = None
+    tf = os.path.join(REPO, "profiles", "force_traffic.json")
+    if os.path.exists(tf):
+        try:
+            traffic = json.load(open(tf)).get("bytes_per_launch_full")
+        except Exception:
+            traffic = None
+
+    # end to end through the C ABI with host buffers: upload + K steps + download
+    gd.close()
+    fields = ("x", "v", "density", "pressure", "a", "ddensity")
+    t0 = time.perf_counter()
+    ge = GpuDomain(cfg)
+    ge.upload(dom.particles, initial=True)
+    done_e = ge.step(args.steps)
+    out = ge.download_fields(fields)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    pe = ge.pair_count()
+    ge.close()
+    h2d = sum(dom.particles.get(f).nbytes for f in dom.particles.arrays())
+    d2h = sum(a.nbytes for a in out.values())
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": done, "warmup": args.warmup,
+        "ms_per_step": ms / max(done, 1), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic lattice (seeded); inputs larger than L2 (no flush needed)",
+        "config": {"workload": "3D dam break: tank 3.22x1.0x1.0 m, column 1.2x0.55x1.0 m, dx=%g m" % args.dx,
+                   "particles": n, "fluid": info["n_fluid"], "walls": info["n_wall"], "kernel": "Wendland C2",
+                   "h_over_dx": 1.3, "eos": "Tait c0=40", "scheme": "Modified Verlet + Shepard",
+                   "form": "FP64 plain", "parallelism": "replicas only" if world > 1 else "single GPU",
+                   "l2": "working set > L2"},
+        "steps_per_s": steps_per_s, "pairs_per_step": pairs_per_step,
+        "phase_ms": {"sort": phases[0] / 3, "wall_prepare": phases[1] / 3, "forces": force_ms,
+                     "dt": phases[3] / 3, "update": phases[4] / 3},
+        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved_gbs / pk["hbm_gbs"], "traffic": traffic,
+                     "kernel": "forces_fluid_kernel", "peak_source": pk["src"],
+                     "note": "FP64 pair kernel is FP64-pipe bound; see roofline_fp64"},
+        "roofline_fp64": {"bound": "fp64", "achieved": fp64_tflops, "peak": fp64.value, "unit": "TFLOP/s",
+                          "frac": fp64_tflops / fp64.value if fp64.value else None,
+                          "peak_source": "measured here by psph_probe_fp64_peak (DFMA chains)"},
+        "clocks": clk.summary(),
+        "e2e": {"value": pe / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d / max(done_e, 1),
+                "d2h_bytes_per_step": d2h / max(done_e, 1), "steps": done_e,
+                "note": "create + upload + steps + download through the C ABI, host wall clock"},
+        "gpu_launches": launches,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        r = cpu_reference(args.ref_dx, 2, 1, threads)
+        line["cpu_baseline"] = {"value": r["value"], "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"2 steps of the same 3D dam break at dx={args.ref_dx} m "
+                                          f"({r['n']} particles) after 1 warm-up step"}
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

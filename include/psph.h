@@ -191,6 +191,20 @@ psph_status psph_phase_times(const psph_ctx* ctx, double* ms, int cap, int* n_ph
 /* Number of kernel launches the last psph_step issued. */
 int64_t psph_last_launch_count(const psph_ctx* ctx);
 
+/* psph_step(ctx, nsteps, +inf, steps_done) bracketed by CUDA events on the
+ * context's stream; *device_ms receives the device time of the steps. */
+psph_status psph_step_timed(psph_ctx* ctx, int64_t nsteps, double* device_ms, int64_t* steps_done);
+
+/* Pair-interactions evaluated since upload: unordered pairs {i,j}, at least
+ * one free, r_ij <= Cellfac h_ij, summed over steps (the work CalcForce11 /
+ * CalcForce2233 do in LastComputeAcceleration, Source/Domain.cpp:1238-1270). */
+psph_status psph_pair_count(psph_ctx* ctx, uint64_t* pairs);
+
+/* Measurement helper with no counterpart in the reference: device FP64 FMA
+ * throughput in TFLOP/s (an FMA counts 2), the roofline denominator of the
+ * FP64 pair kernels. */
+psph_status psph_probe_fp64_peak(double* tflops);
+
 #ifdef __cplusplus
 }
 #endif

@@ -158,9 +158,13 @@ def _declare(lib):
     lib.psph_phase_times.argtypes = [ctx, P(C.c_double), C.c_int, P(C.c_int)]
     lib.psph_last_launch_count.argtypes = [ctx]
     lib.psph_last_launch_count.restype = C.c_int64
+    lib.psph_step_timed.argtypes = [ctx, C.c_int64, P(C.c_double), P(C.c_int64)]
+    lib.psph_pair_count.argtypes = [ctx, P(C.c_uint64)]
+    lib.psph_probe_fp64_peak.argtypes = [P(C.c_double)]
     for name in ("psph_device_check", "psph_create", "psph_set_stream", "psph_set_grid", "psph_set_integrator",
                  "psph_upload", "psph_step", "psph_download", "psph_original_index", "psph_get_grid", "psph_get_integrator",
-                 "psph_pairs_export", "psph_enable_timing", "psph_phase_times"):
+                 "psph_pairs_export", "psph_enable_timing", "psph_phase_times", "psph_step_timed", "psph_pair_count",
+                 "psph_probe_fp64_peak"):
         getattr(lib, name).restype = C.c_int
 
 

@@ -567,8 +567,20 @@ psph_status psph_step(psph_ctx* c, int64_t nsteps, double t_stop, int64_t* steps
   if (!c) return PSPH_ERR_INVALID_ARGUMENT;
   if (steps_done) *steps_done = 0;
   if (!c->uploaded) return set_err(c, PSPH_ERR_STATE, "psph_step before psph_upload");
-  if (nsteps <= 0) return PSPH_OK;
   psph_status st;
+  if (nsteps <= 0) {
+    if (!c->timing && !c->graph) {
+      cudaGraph_t g;
+      CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+      enqueue_step(c);
+      cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+      if (ce != cudaSuccess) return set_err(c, PSPH_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+      ce = cudaGraphInstantiate(&c->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (ce != cudaSuccess) return set_err(c, PSPH_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+    }
+    return PSPH_OK;
+  }
   if ((st = sync_scalars(c))) return st;
   const long long steps0 = c->h_sc->steps;
   arm_kernel<<<1, 1, 0, c->stream>>>(c->d_sc, t_stop);
@@ -842,5 +854,43 @@ psph_status psph_phase_times(const psph_ctx* c, double* ms, int cap, int* n_phas
 }
 
 int64_t psph_last_launch_count(const psph_ctx* c) { return c ? c->last_launches : 0; }
+
+psph_status psph_step_timed(psph_ctx* c, int64_t nsteps, double* device_ms, int64_t* steps_done) {
+  if (!c || !device_ms) return PSPH_ERR_INVALID_ARGUMENT;
+  if (!c->uploaded) return set_err(c, PSPH_ERR_STATE, "psph_step_timed before psph_upload");
+  const bool was = c->timing;
+  c->timing = false;
+  cudaEvent_t e0, e1;
+  CUDA_TRY(c, cudaEventCreate(&e0));
+  CUDA_TRY(c, cudaEventCreate(&e1));
+  // make sure the graph exists before the timed region
+  if (!c->graph) {
+    psph_status st = psph_step(c, 0, 1e300, nullptr);
+    if (st) return st;
+  }
+  CUDA_TRY(c, cudaEventRecord(e0, c->stream));
+  psph_status st = psph_step(c, nsteps, 1e300, steps_done);
+  cudaEventRecord(e1, c->stream);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c->timing = was;
+  *device_ms = ms;
+  return st;
+}
+
+psph_status psph_pair_count(psph_ctx* c, uint64_t* pairs) {
+  if (!c || !pairs) return PSPH_ERR_INVALID_ARGUMENT;
+  if (!c->uploaded) {
+    *pairs = 0;
+    return PSPH_OK;
+  }
+  psph_status st = sync_scalars(c);
+  if (st) return st;
+  *pairs = c->h_sc->pairs_x2 / 2;
+  return PSPH_OK;
+}
 
 }  // extern "C"

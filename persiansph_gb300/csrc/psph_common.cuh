@@ -49,6 +49,7 @@ struct StepScalars {
   uint32_t status;
   int launches;
   int buf;        // which persistent buffer (A=0 / B=1) holds the current sorted state
+  unsigned long long pairs_x2;  // 2 x pair-interactions evaluated since upload
 };
 
 struct GridDev {

@@ -269,6 +269,8 @@ __global__ void __launch_bounds__(kFT) prepare_wall_kernel(DevView v) {
 template <int DIM, int KT>
 __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
   __shared__ double red[kFT / 32];
+  __shared__ unsigned long long cred[kFT / 32];
+  unsigned long long npair2 = 0;  // in-support neighbours: free counted once, fixed twice
   const StepScalars* sc = v.sc;
   if (sc->stop) return;
   const Persist& P = cur_persist(v);
@@ -318,6 +320,7 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
             if (q > g.cellfac) continue;
             const double4_32a vj = P.V4[j];
             const bool fj = Cj.is_free;
+            npair2 += fj ? 1ull : 2ull;
             double dj, mj;
             if (fj) { dj = xj.w; mj = Cj.mass; }
             else {
@@ -433,12 +436,21 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
   }
   // block minimum of the acceleration time-step bound
   for (int off = 16; off > 0; off >>= 1) dtc = fmin(dtc, __shfl_down_sync(0xffffffffu, dtc, off));
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = dtc;
+  for (int off = 16; off > 0; off >>= 1) npair2 += __shfl_down_sync(0xffffffffu, npair2, off);
+  if ((threadIdx.x & 31) == 0) {
+    red[threadIdx.x >> 5] = dtc;
+    cred[threadIdx.x >> 5] = npair2;
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
     double m = red[0];
-    for (int k = 1; k < kFT / 32; ++k) m = fmin(m, red[k]);
+    unsigned long long c = cred[0];
+    for (int k = 1; k < kFT / 32; ++k) {
+      m = fmin(m, red[k]);
+      c += cred[k];
+    }
     v.S.blockmin[blockIdx.x] = m;
+    if (c) atomicAdd(&v.sc->pairs_x2, c);
   }
 }
 
@@ -448,6 +460,8 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
 template <int DIM, int KT>
 __global__ void __launch_bounds__(kFT) forces_solid_kernel(DevView v) {
   __shared__ double red[kFT / 32];
+  __shared__ unsigned long long cred[kFT / 32];
+  unsigned long long npair2 = 0;  // in-support neighbours: free counted once, fixed twice
   const StepScalars* sc = v.sc;
   if (sc->stop) return;
   const Persist& P = cur_persist(v);
@@ -497,6 +511,7 @@ __global__ void __launch_bounds__(kFT) forces_solid_kernel(DevView v) {
             if (q > g.cellfac) continue;
             const double4_32a vj = P.V4[j];
             const bool fj = Cj.is_free;
+            npair2 += fj ? 1ull : 2ull;
             const bool soil = (Ci.material * Cj.material == 9);
             double dj, mj;
             if (fj) { dj = xj.w; mj = Cj.mass; }
@@ -607,12 +622,21 @@ __global__ void __launch_bounds__(kFT) forces_solid_kernel(DevView v) {
     }
   }
   for (int off = 16; off > 0; off >>= 1) dtc = fmin(dtc, __shfl_down_sync(0xffffffffu, dtc, off));
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = dtc;
+  for (int off = 16; off > 0; off >>= 1) npair2 += __shfl_down_sync(0xffffffffu, npair2, off);
+  if ((threadIdx.x & 31) == 0) {
+    red[threadIdx.x >> 5] = dtc;
+    cred[threadIdx.x >> 5] = npair2;
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
     double m = red[0];
-    for (int k = 1; k < kFT / 32; ++k) m = fmin(m, red[k]);
+    unsigned long long c = cred[0];
+    for (int k = 1; k < kFT / 32; ++k) {
+      m = fmin(m, red[k]);
+      c += cred[k];
+    }
     v.S.blockmin[blockIdx.x] = m;
+    if (c) atomicAdd(&v.sc->pairs_x2, c);
   }
 }
 

@@ -128,5 +128,16 @@ class GpuDomain:
         self._check(self._lib.psph_phase_times(self._ctx, buf, 5, C.byref(n)))
         return list(buf)
 
+    def step_timed(self, nsteps: int):
+        ms = C.c_double(0.0)
+        done = C.c_int64(0)
+        self._check(self._lib.psph_step_timed(self._ctx, int(nsteps), C.byref(ms), C.byref(done)))
+        return ms.value, done.value
+
+    def pair_count(self) -> int:
+        v = C.c_uint64(0)
+        self._check(self._lib.psph_pair_count(self._ctx, C.byref(v)))
+        return int(v.value)
+
     def last_launch_count(self) -> int:
         return int(self._lib.psph_last_launch_count(self._ctx))

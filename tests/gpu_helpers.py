@@ -38,4 +38,12 @@ def assert_step_parity(gpu: dict, ora: dict, a_scale, dr_scale, dt, tol=1e-12, l
     assert ex <= tol, f"{label}: position rel err {ex:.3e}"
     er = np.max(np.abs(gpu["density"] - ora["density"]) / np.abs(ora["density"]))
     assert er <= tol, f"{label}: density rel err {er:.3e}"
+    # material state the next step depends on (viscosity, stress, rates): field-norm relative
+    for f in ("mu", "strain_rate", "rotation_rate", "sigma", "shear_stress", "strain", "tir", "pressure"):
+        ref, got = ora[f][free], gpu[f][free]
+        scale = np.max(np.abs(ref))
+        if scale == 0.0:
+            continue
+        e = np.max(np.abs(got - ref)) / scale
+        assert e <= 1e3 * tol, f"{label}: {f} rel err {e:.3e}"
     return ea, ed
