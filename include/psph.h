@@ -200,6 +200,23 @@ psph_status psph_step_timed(psph_ctx* ctx, int64_t nsteps, double* device_ms, in
  * CalcForce2233 do in LastComputeAcceleration, Source/Domain.cpp:1238-1270). */
 psph_status psph_pair_count(psph_ctx* ctx, uint64_t* pairs);
 
+/* Pair export that allocates no device memory. It has no counterpart in the
+ * reference: it serves callers that cannot call cudaMalloc where they need the
+ * pairs (all device memory already handed to their own pool or another
+ * framework's allocator, or a running loop that must not take cudaMalloc's
+ * device-wide synchronisation). Same pairs as psph_pairs_export, written as
+ * (first, second) int64 couples into the caller's DEVICE buffer pairs_device
+ * (at most cap pairs, in sorted-particle order); *n_total (host) receives the
+ * full count. Its scratch is one static device array for at most
+ * PSPH_NOALLOC_MAX_PARTICLES particles (about 8 MB, kept by every GPU that
+ * loads the library until exit); larger contexts get PSPH_ERR_INVALID_ARGUMENT.
+ * The first call on a device looks up that array's device address: make it
+ * before any stream capture. Calls share the array, so calls that overlap on
+ * the GPU race. */
+#define PSPH_NOALLOC_MAX_PARTICLES (1 << 20)
+psph_status psph_pairs_export_noalloc(psph_ctx* ctx, int which, int64_t* pairs_device, int64_t cap,
+                                      int64_t* n_total);
+
 /* Measurement helper with no counterpart in the reference: device FP64 FMA
  * throughput in TFLOP/s (an FMA counts 2), the roofline denominator of the
  * FP64 pair kernels. */

@@ -161,10 +161,11 @@ def _declare(lib):
     lib.psph_step_timed.argtypes = [ctx, C.c_int64, P(C.c_double), P(C.c_int64)]
     lib.psph_pair_count.argtypes = [ctx, P(C.c_uint64)]
     lib.psph_probe_fp64_peak.argtypes = [P(C.c_double)]
+    lib.psph_pairs_export_noalloc.argtypes = [ctx, C.c_int, C.c_void_p, C.c_int64, P(C.c_int64)]
     for name in ("psph_device_check", "psph_create", "psph_set_stream", "psph_set_grid", "psph_set_integrator",
                  "psph_upload", "psph_step", "psph_download", "psph_original_index", "psph_get_grid", "psph_get_integrator",
                  "psph_pairs_export", "psph_enable_timing", "psph_phase_times", "psph_step_timed", "psph_pair_count",
-                 "psph_probe_fp64_peak"):
+                 "psph_probe_fp64_peak", "psph_pairs_export_noalloc"):
         getattr(lib, name).restype = C.c_int
 
 

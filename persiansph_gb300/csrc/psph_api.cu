@@ -894,3 +894,78 @@ psph_status psph_pair_count(psph_ctx* c, uint64_t* pairs) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Pair export that allocates nothing.
+//
+// psph_pairs_export allocates its device counter and output buffer on every
+// call. Some callers cannot allocate device memory at the point where they need
+// the pairs: code that has handed all device memory to its own pool or to
+// another framework's caching allocator (where cudaMalloc fails or fragments),
+// and latency-bound loops that must not pay cudaMalloc/cudaFree's device-wide
+// synchronisation once running. psph_pairs_export_noalloc serves them: the
+// caller passes a device output buffer, the context's cell-sort buffers (made at
+// upload) are reused, and the per-particle counts and offsets it needs live in
+// one file-scope device array, sized for PSPH_NOALLOC_MAX_PARTICLES particles
+// and held by every GPU that loads this library until the process exits.
+//
+// The array's host-side name is only a stand-in for the device symbol, so the
+// address passed to the kernels is taken with cudaGetSymbolAddress, once per
+// device, by the first call on that device (with that device current); make
+// that first call before any stream capture. Every call shares the array and
+// overwrites what it needs (nothing in it has to start at zero); two calls
+// whose work overlaps on the GPU (different streams, or contexts used from
+// several threads) race on it.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kNoallocBlocks = (PSPH_NOALLOC_MAX_PARTICLES + 1023) / 1024 + 2;
+// counts[MAX] | offsets[MAX + 1] | scan block sums
+static __device__ __align__(256) int g_noalloc_scratch[2 * PSPH_NOALLOC_MAX_PARTICLES + 1 + kNoallocBlocks];
+
+constexpr int kMaxDevices = 64;
+int* g_noalloc_addr[kMaxDevices] = {};
+
+psph_status noalloc_scratch(psph_ctx* c, int** out) {
+  int dev = -1;
+  CUDA_TRY(c, cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return set_err(c, PSPH_ERR_NO_DEVICE, "device index %d out of range", dev);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    CUDA_TRY(c, cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_addr[dev] = (int*)p;
+  }
+  *out = g_noalloc_addr[dev];
+  return PSPH_OK;
+}
+
+}  // namespace
+
+extern "C" psph_status psph_pairs_export_noalloc(psph_ctx* c, int which, int64_t* pairs_device, int64_t cap,
+                                                 int64_t* n_total) {
+  if (!c || (which != 0 && which != 1) || cap < 0 || (cap > 0 && !pairs_device)) return PSPH_ERR_INVALID_ARGUMENT;
+  if (!c->uploaded) return set_err(c, PSPH_ERR_STATE, "psph_pairs_export_noalloc before psph_upload");
+  if (c->ncap > PSPH_NOALLOC_MAX_PARTICLES)
+    return set_err(c, PSPH_ERR_INVALID_ARGUMENT,
+                   "psph_pairs_export_noalloc handles at most %d particles (context holds %d); use psph_pairs_export",
+                   PSPH_NOALLOC_MAX_PARTICLES, c->ncap);
+  int* scratch = nullptr;
+  psph_status st = noalloc_scratch(c, &scratch);
+  if (st) return st;
+  int* counts = scratch;
+  int* offsets = scratch + PSPH_NOALLOC_MAX_PARTICLES;
+  int* block_sums = offsets + PSPH_NOALLOC_MAX_PARTICLES + 1;
+  cudaStream_t s = c->stream;
+  arm_kernel<<<1, 1, 0, s>>>(c->d_sc, 1e300);
+  const DevView v = view(c);
+  launch_sort(v, s);                                   // cell list of the current positions
+  launch_pairs_count(v, which, counts, s);             // pairs each sorted particle lists first
+  launch_exclusive_scan(counts, offsets, c->ncap, block_sums, s);
+  launch_pairs_write(v, which, offsets, (long long*)pairs_device, (long long)cap, s);
+  CUDA_TRY(c, cudaGetLastError());
+  int total = 0;
+  CUDA_TRY(c, cudaMemcpyAsync(&total, offsets + c->ncap, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(c, cudaStreamSynchronize(s));
+  if (n_total) *n_total = total;
+  return PSPH_OK;
+}

@@ -103,3 +103,11 @@ void launch_pairs_export(const DevView& v, int which, long long* out, long long 
                          cudaStream_t st);
 
 }  // namespace psph
+
+namespace psph {
+// Pieces of the two-pass pair export (scratch supplied by the caller).
+void launch_exclusive_scan(const int* in, int* out, int len, int* block_sums, cudaStream_t st);
+void launch_pairs_count(const DevView& v, int which, int* counts, cudaStream_t st);
+void launch_pairs_write(const DevView& v, int which, const int* offsets, long long* out, long long cap,
+                        cudaStream_t st);
+}  // namespace psph

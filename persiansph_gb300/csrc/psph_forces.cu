@@ -797,3 +797,84 @@ void launch_pairs_export(const DevView& v, int which, long long* out, long long 
 }
 
 }  // namespace psph
+
+// ---------------------------------------------------------------------------
+// Two-pass pair export (count, then write at scanned offsets): the same pairs
+// as pairs_export_kernel, in sorted-particle order, with no atomic counter.
+// Its scratch (per-particle counts and offsets) is supplied by the caller.
+// ---------------------------------------------------------------------------
+namespace psph {
+namespace {
+
+template <int DIM>
+PSPH_D int pairs_of_particle(const DevView& v, int i, int which, long long* out, long long base, long long cap) {
+  const Persist& P = cur_persist(v);
+  const GridDev& g = v.g;
+  const int cell = v.S.cellid[i];
+  if (cell < 0) return 0;
+  const PClass* CT = v.cls;
+  const PClass& Ci = CT[P.cls[i]];
+  const CellCoord ci = decode(g, cell);
+  const int oi = P.orig[i];
+  const double4_32a xi = P.X4[i];
+  int k = 0;
+  for_neighbor_ranges<DIM>(g, ci, v.S.start, [&](int lo, int hi) {
+    for (int j = lo; j < hi; ++j) {
+      if (j == i) continue;
+      const PClass& Cj = CT[P.cls[j]];
+      if (!Ci.is_free && !Cj.is_free) continue;
+      const CellCoord cj = decode(g, v.S.cellid[j]);
+      const int oj = P.orig[j];
+      if (!first_of_pair(g, ci, cj, oi, oj)) continue;
+      if (which == 1) {
+        const double4_32a xj = P.X4[j];
+        const double hb = (Ci.h + Cj.h) / 2;
+        double x0 = xi.x - xj.x, x1 = xi.y - xj.y, x2 = xi.z - xj.z;
+        periodic_fix(g, x0, x1, x2, hb, ci, cj);
+        const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(x0, x0), __dmul_rn(x1, x1)), __dmul_rn(x2, x2));
+        if (!(__ddiv_rn(__dsqrt_rn(r2), hb) <= g.cellfac)) continue;
+      }
+      if (out) {
+        const long long slot = base + k;
+        if (slot < cap) {
+          out[2 * slot] = oi;
+          out[2 * slot + 1] = oj;
+        }
+      }
+      ++k;
+    }
+  });
+  return k;
+}
+
+template <int DIM>
+__global__ void pairs_count_kernel(DevView v, int which, int* __restrict__ counts, int ncap) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ncap) return;
+  counts[i] = (i < v.sc->n) ? pairs_of_particle<DIM>(v, i, which, nullptr, 0, 0) : 0;
+}
+
+template <int DIM>
+__global__ void pairs_write_kernel(DevView v, int which, const int* __restrict__ offsets, long long* out,
+                                   long long cap) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= v.sc->n) return;
+  pairs_of_particle<DIM>(v, i, which, out, offsets[i], cap);
+}
+
+}  // namespace
+
+void launch_pairs_count(const DevView& v, int which, int* counts, cudaStream_t st) {
+  const int nb = nblk(v.ncap, kFT);
+  if (v.o.dim == 2) pairs_count_kernel<2><<<nb, kFT, 0, st>>>(v, which, counts, v.ncap);
+  else pairs_count_kernel<3><<<nb, kFT, 0, st>>>(v, which, counts, v.ncap);
+}
+
+void launch_pairs_write(const DevView& v, int which, const int* offsets, long long* out, long long cap,
+                        cudaStream_t st) {
+  const int nb = nblk(v.ncap, kFT);
+  if (v.o.dim == 2) pairs_write_kernel<2><<<nb, kFT, 0, st>>>(v, which, offsets, out, cap);
+  else pairs_write_kernel<3><<<nb, kFT, 0, st>>>(v, which, offsets, out, cap);
+}
+
+}  // namespace psph

@@ -228,3 +228,17 @@ void launch_sort(const DevView& v, cudaStream_t st) {
 }
 
 }  // namespace psph
+
+namespace psph {
+
+// Exclusive prefix of in[0..len) into out[0..len], out[len] = total, using
+// block_sums (>= ceil(len/1024) entries) as scratch. Used by the pair export
+// that takes its scratch from caller-owned or static device memory.
+void launch_exclusive_scan(const int* in, int* out, int len, int* block_sums, cudaStream_t st) {
+  const int nb = (len + 1023) / 1024 > 0 ? (len + 1023) / 1024 : 1;
+  scan_blocks<<<nb, 1024, 0, st>>>(in, out, block_sums, len);
+  scan_sums<<<1, 1024, 0, st>>>(block_sums, nb, out + len);
+  scan_add<<<nb, 1024, 0, st>>>(out, block_sums, len);
+}
+
+}  // namespace psph
