@@ -456,6 +456,18 @@ psph_status psph_upload(psph_ctx* c, const psph_particles* p, int initial) {
     }
   }
   if (o.eos_cls < 0) o.eos_cls = 0;
+  o.uniform_mu = !dyn_mu;
+  o.mu_u = 0.0;
+  {
+    bool first = true;
+    for (const PClass& C : c->classes)
+      if (C.is_free) {
+        if (first) { o.mu_u = C.mu0; first = false; }
+        else if (C.mu0 != o.mu_u) o.uniform_mu = 0;
+      }
+    // zero viscosity keeps the reference's 0/0 harmonic mean (Source/Interaction.cpp:103)
+    if (!(o.mu_u > 0.0)) o.uniform_mu = 0;
+  }
   o.inv_h = 1.0 / c->classes[0].h;
   o.nclasses = (int)c->classes.size();
 
@@ -484,7 +496,7 @@ psph_status psph_upload(psph_ctx* c, const psph_particles* p, int initial) {
   if ((st = dalloc(c, &S.key, N)) || (st = dalloc(c, &S.count, NC + 2)) || (st = dalloc(c, &S.start, NC + 3)) ||
       (st = dalloc(c, &S.tmp_perm, N)) || (st = dalloc(c, &S.perm, N)) || (st = dalloc(c, &S.cellid, N)) ||
       (st = dalloc(c, &S.block_sums, (NC + 2 + 1023) / 1024 + 1)) || (st = dalloc(c, &S.blockmin, (size_t)nb_forces)) ||
-      (st = dalloc(c, &S.rho_eff, N)) || (st = dalloc(c, &S.prs, N)) || (st = dalloc(c, &S.c_eff, N)) ||
+      (st = dalloc(c, &S.X32, N)) || (st = dalloc(c, &S.D4, N)) ||
       (st = dalloc(c, &S.A4, N)) || (st = dalloc(c, &S.zwab, N)) || (st = dalloc(c, &S.sumden, N)) ||
       (st = dalloc(c, &S.sumkernel, N)) || (st = dalloc(c, &S.nsv4, N)) || (st = dalloc(c, &S.vxsph4, N)) ||
       (st = dalloc(c, &S.shear_rate, N)) || (st = dalloc(c, &S.sbar, N)))

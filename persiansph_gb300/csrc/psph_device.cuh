@@ -35,9 +35,9 @@ struct Scratch {
   int* block_sums;
   double* blockmin;
   // per-step derived / outputs
-  double* rho_eff;   // density seen by partners: own Density, or wall density from the partner EOS
-  double* prs;       // pressure (walls: interpolated)
-  double* c_eff;     // sound speed seen by partners
+  float4* X32;       // FP32 copy of (x, y, z, h) for the conservative neighbour prefilter
+  double4_32a* D4;   // seen by partners: (1/density, pressure/density^2, sound speed, density);
+                     // a wall's density is the inverse EOS of its interpolated pressure
   double4_32a* A4;       // ax, ay, az, dDensity
   double* zwab;
   double* sumden;
@@ -65,6 +65,8 @@ struct Options {
   int dyn_mu;
   int soil_pairs;     // Material 3 (soil-soil walls take the partner's density)
   int uniform_h;      // every particle has the same h
+  int uniform_mu;     // every free particle has the same constant viscosity
+  double mu_u;        // that viscosity
   double inv_h;       // 1/h when uniform
   double xsph, sqrt_h_a;
   double gravity[3], body_force[3];

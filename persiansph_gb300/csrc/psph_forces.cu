@@ -149,81 +149,196 @@ PSPH_D void tensile_tir(const double* S, double TI, double rho, double* TIR) {
       for (int c = 0; c < 3; ++c) TIR[3 * r + c] = Q[3 * r + 0] * val[0] * Q[3 * c + 0] + Q[3 * r + 1] * val[1] * Q[3 * c + 1] + Q[3 * r + 2] * val[2] * Q[3 * c + 2];
   }
 }
+// ---------------------------------------------------------------------------
+// Candidate stream: the sorted index ranges of the 3 (2D) or 9 (3D) cell rows
+// around a cell, one row split into its 3 cells where the periodic x axis wraps.
+// Each lane walks its own stream; candidates that pass a conservative FP32
+// distance test are queued in shared memory and evaluated in FP64 by all lanes
+// of the warp together, so the FP64 work runs with (nearly) full warps instead
+// of the ~1/3 occupancy a per-candidate branch gives.
+// ---------------------------------------------------------------------------
+template <int DIM>
+struct Cands {
+  static constexpr int NR = (DIM == 3 ? 9 : 3) * 3;
+  int cx, cy, cz, r, j, jend;
+  bool wrapx;
+  PSPH_D void init(const GridDev& g, int cell) {
+    j = jend = 0;
+    if (cell < 0) {
+      r = NR;
+      cx = cy = cz = 0;
+      wrapx = false;
+      return;
+    }
+    const CellCoord c = decode(g, cell);
+    cx = c.x;
+    cy = c.y;
+    cz = c.z;
+    r = 0;
+    wrapx = g.periodic[0] && (cx == 0 || cx == g.nc[0] - 1);
+  }
+  PSPH_D bool range(const GridDev& g, const int* __restrict__ start, int rr, int& lo, int& hi) const {
+    const int row = rr / 3, sub = rr - 3 * row;
+    const int dz = (DIM == 3) ? row / 3 - 1 : 0;
+    const int dy = row % 3 - 1;
+    int z = cz + dz, y = cy + dy;
+    if (g.periodic[2]) z = (z + g.nc[2]) % g.nc[2];
+    else if (z < 0 || z >= g.nc[2]) return false;
+    if (g.periodic[1]) y = (y + g.nc[1]) % g.nc[1];
+    else if (y < 0 || y >= g.nc[1]) return false;
+    const int base = (z * g.nc[1] + y) * g.nc[0];
+    if (!wrapx) {
+      if (sub) return false;
+      const int x0 = max(cx - 1, 0), x1 = min(cx + 1, g.nc[0] - 1);
+      lo = start[base + x0];
+      hi = start[base + x1 + 1];
+    } else {
+      const int x = (cx + sub - 1 + g.nc[0]) % g.nc[0];
+      lo = start[base + x];
+      hi = start[base + x + 1];
+    }
+    return lo < hi;
+  }
+  PSPH_D int next(const GridDev& g, const int* __restrict__ start) {
+    while (j >= jend) {
+      if (r >= NR) return -1;
+      int lo, hi;
+      if (range(g, start, r++, lo, hi)) {
+        j = lo;
+        jend = hi;
+      }
+    }
+    return j++;
+  }
+};
+
+constexpr int kQN = 16;  // queued FP64 pair evaluations per lane between flushes
+
+// Conservative FP32 support test; the exact FP64 test follows for survivors.
+template <int DIM>
+PSPH_D bool near_f32(const GridDev& g, const float4& xi, const float4& xj, float cf) {
+  float d[3] = {xi.x - xj.x, xi.y - xj.y, DIM == 3 ? xi.z - xj.z : 0.0f};
+  const float hb = 0.5f * (xi.w + xj.w);
+  const float lim = 2.0f * cf * hb;
+#pragma unroll
+  for (int a = 0; a < DIM; ++a)
+    if (g.periodic[a] && fabsf(d[a]) > lim) d[a] -= copysignf((float)g.dom_size[a], d[a]);
+  const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+  const float s = cf * hb;
+  return r2 <= s * s * 1.004f;
+}
 
 // ---------------------------------------------------------------------------
 // Per-particle preparation and wall interpolation
 // ---------------------------------------------------------------------------
 template <int DIM, int KT>
 __global__ void __launch_bounds__(kFT) prepare_wall_kernel(DevView v) {
+  __shared__ int qbuf[kQN][kFT];
   const StepScalars* sc = v.sc;
   if (sc->stop) return;
   const Persist& P = cur_persist(v);
   const int n = sc->n;
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
-  if (w >= n) return;
+  const int tid = threadIdx.x;
   const GridDev& g = v.g;
+  const Options& o = v.o;
   const PClass* __restrict__ CT = v.cls;
-  const PClass& Cw = CT[P.cls[w]];
-  const PClass& Ce = CT[v.o.eos_cls];
-  if (Cw.is_free) {
-    const double rho = P.X4[w].w;
-    v.S.rho_eff[w] = rho;
-    v.S.prs[w] = P.V4[w].w;
-    v.S.c_eff[w] = sound_speed(Cw.pres_eq, Cw.cs, rho, Cw.rho0);
-    if (v.o.has_solid && Cw.material > 1 && Cw.ti > 0.0)
-      tensile_tir<DIM>(P.sigma + 9 * (size_t)w, Cw.ti, rho, P.tir + 9 * (size_t)w);
-    return;
-  }
-  // fixed particle: StartAcceleration resets (Source/Domain.cpp:989-996), then interpolation
-  const double4_32a xw = P.X4[w];
-  const int cell = v.S.cellid[w];
-  const int mat = Cw.material;
+  bool wall = false;
+  int mat = 0;
   double sk = 0.0, p = 0.0, n0 = 0.0, n1 = 0.0, n2 = 0.0;
   double sig[9];
 #pragma unroll
   for (int e = 0; e < 9; ++e) sig[e] = 0.0;
-  const bool any_periodic = g.periodic[0] | g.periodic[1] | g.periodic[2];
-  if (cell >= 0) {
-    const CellCoord cw = decode(g, cell);
-    const int ow = P.orig[w];
-    const double gx = v.o.gravity[0], gy = v.o.gravity[1], gz = v.o.gravity[2];
-    for_neighbor_ranges<DIM>(g, cw, v.S.start, [&](int lo, int hi) {
-      for (int f = lo; f < hi; ++f) {
-        if (f == w) continue;
-        const PClass& Cf = CT[P.cls[f]];
-        if (!Cf.is_free || Cf.material != mat) continue;
-        const double4_32a xf = P.X4[f];
-        const double hb = (Cw.h + Cf.h) / 2.0;
-        const CellCoord cf = decode(g, v.S.cellid[f]);
-        const bool wfirst = v.o.wallp_physical ? true : first_of_pair(g, cw, cf, ow, P.orig[f]);
-        double x0, x1, x2;
-        if (wfirst) {
-          x0 = xw.x - xf.x; x1 = xw.y - xf.y; x2 = xw.z - xf.z;
-          if (any_periodic) periodic_fix(g, x0, x1, x2, hb, cw, cf);
-        } else {
-          x0 = xf.x - xw.x; x1 = xf.y - xw.y; x2 = xf.z - xw.z;
-          if (any_periodic) periodic_fix(g, x0, x1, x2, hb, cf, cw);
-        }
-        const double r = sqrt(x0 * x0 + x1 * x1 + x2 * x2);
-        const double K = kernel_w_rt<DIM>(KT, r / hb, hb);
-        if (K == 0.0) continue;
-        sk += K;
-        if (mat < 3) {
-          const double4_32a vf = P.V4[f];
-          p += vf.w * K + (gx * x0 + gy * x1 + gz * x2) * xf.w * K;
-        }
-        if (mat > 1) {
-          const double* sf = P.sigma + 9 * (size_t)f;
-#pragma unroll
-          for (int e = 0; e < 9; ++e) sig[e] += sf[e] * K;
-        }
-        if (Cw.no_slip) {
-          const double4_32a vf = P.V4[f];
-          n0 += vf.x * K; n1 += vf.y * K; n2 += vf.z * K;
-        }
-      }
-    });
+  double4_32a xw = make_double4_32a(0, 0, 0, 0);
+  float4 xw32 = make_float4(0.f, 0.f, 0.f, 0.f);
+  int ow = 0, cell = -1;
+  double hw = 0.0;
+  bool noslip = false;
+  if (w < n) {
+    const PClass& Cw = CT[P.cls[w]];
+    if (Cw.is_free) {
+      const double rho = P.X4[w].w;
+      const double inv = 1.0 / rho;
+      const double pr = P.V4[w].w;
+      v.S.D4[w] = make_double4_32a(inv, pr * inv * inv, sound_speed(Cw.pres_eq, Cw.cs, rho, Cw.rho0), rho);
+      if (o.has_solid && Cw.material > 1 && Cw.ti > 0.0)
+        tensile_tir<DIM>(P.sigma + 9 * (size_t)w, Cw.ti, rho, P.tir + 9 * (size_t)w);
+    } else {
+      wall = true;
+      mat = Cw.material;
+      xw = P.X4[w];
+      xw32 = v.S.X32[w];
+      ow = P.orig[w];
+      cell = v.S.cellid[w];
+      hw = Cw.h;
+      noslip = Cw.no_slip;
+    }
   }
+  // Wall interpolation (FSMPairs only: free partners of the same material).
+  const bool any_periodic = g.periodic[0] | g.periodic[1] | g.periodic[2];
+  const float cff = (float)g.cellfac;
+  const double gx = o.gravity[0], gy = o.gravity[1], gz = o.gravity[2];
+  const bool need_orient = !o.wallp_physical && (gx != 0.0 || gy != 0.0 || gz != 0.0) && mat < 3;
+  Cands<DIM> cs;
+  cs.init(g, wall ? cell : -1);
+  bool more = wall && cell >= 0;
+  const CellCoord cw = decode(g, cell >= 0 ? cell : 0);
+  while (true) {
+    int qn = 0;
+    while (more && qn < kQN) {
+      const int f = cs.next(g, v.S.start);
+      if (f < 0) {
+        more = false;
+        break;
+      }
+      if (f == w) continue;
+      if (near_f32<DIM>(g, xw32, v.S.X32[f], cff)) qbuf[qn++][tid] = f;
+    }
+    const int qmax = __reduce_max_sync(0xffffffffu, qn);
+    for (int k = 0; k < qmax; ++k) {
+      if (k >= qn) continue;
+      const int f = qbuf[k][tid];
+      const PClass& Cf = CT[P.cls[f]];
+      if (!Cf.is_free || Cf.material != mat) continue;
+      const double4_32a xf = P.X4[f];
+      const double hb = (hw + Cf.h) / 2.0;
+      CellCoord cf = cw;
+      if (any_periodic || need_orient) cf = decode(g, v.S.cellid[f]);
+      const bool wfirst = need_orient ? first_of_pair(g, cw, cf, ow, P.orig[f]) : true;
+      double x0, x1, x2;
+      if (wfirst) {
+        x0 = xw.x - xf.x; x1 = xw.y - xf.y; x2 = xw.z - xf.z;
+        if (any_periodic) periodic_fix(g, x0, x1, x2, hb, cw, cf);
+      } else {
+        x0 = xf.x - xw.x; x1 = xf.y - xw.y; x2 = xf.z - xw.z;
+        if (any_periodic) periodic_fix(g, x0, x1, x2, hb, cf, cw);
+      }
+      const double r = sqrt(x0 * x0 + x1 * x1 + x2 * x2);
+      const double inv_hb = o.uniform_h ? o.inv_h : 1.0 / hb;
+      const double q = r * inv_hb;
+      const double ih2 = inv_hb * inv_hb;
+      const double K = Kern<DIM, KT>::W(q, Kern<DIM, KT>::cw() * (DIM == 2 ? ih2 : ih2 * inv_hb));
+      if (K == 0.0) continue;
+      sk += K;
+      if (mat < 3) {
+        const double4_32a vf = P.V4[f];
+        p += vf.w * K + (gx * x0 + gy * x1 + gz * x2) * xf.w * K;
+      }
+      if (mat > 1) {
+        const double* sf = P.sigma + 9 * (size_t)f;
+#pragma unroll
+        for (int e = 0; e < 9; ++e) sig[e] += sf[e] * K;
+      }
+      if (noslip) {
+        const double4_32a vf = P.V4[f];
+        n0 += vf.x * K; n1 += vf.y * K; n2 += vf.z * K;
+      }
+    }
+    if (!__any_sync(0xffffffffu, more)) break;
+  }
+  if (!wall) return;
+  const PClass& Cw = CT[P.cls[w]];
+  const PClass& Ce = CT[o.eos_cls];
   if (sk != 0.0) {
     if (mat < 3) p = p / sk;
     if (mat > 1) {
@@ -231,17 +346,16 @@ __global__ void __launch_bounds__(kFT) prepare_wall_kernel(DevView v) {
 #pragma unroll
       for (int e = 0; e < 9; ++e) sig[e] = sig[e] * s;
     }
-    if (Cw.no_slip) { n0 = n0 / sk; n1 = n1 / sk; n2 = n2 / sk; }
+    if (noslip) { n0 = n0 / sk; n1 = n1 / sk; n2 = n2 / sk; }
   } else {
     p = 0.0; n0 = n1 = n2 = 0.0;
   }
   double4_32a vw = P.V4[w];
   vw.w = p;
   P.V4[w] = vw;
-  v.S.prs[w] = p;
   v.S.sumkernel[w] = sk;
   v.S.nsv4[w] = make_double4_32a(n0, n1, n2, 0.0);
-  if (v.o.has_solid) {
+  if (o.has_solid) {
     double* sw = P.sigma + 9 * (size_t)w;
 #pragma unroll
     for (int e = 0; e < 9; ++e) sw[e] = sig[e];
@@ -252,15 +366,14 @@ __global__ void __launch_bounds__(kFT) prepare_wall_kernel(DevView v) {
     }
     if (sk != 0.0 && mat > 1 && Cw.ti > 0.0) tensile_tir<DIM>(sig, Cw.ti, xw.w, P.tir + 9 * (size_t)w);
   }
-  // density / sound speed partners see (Source/Interaction.cpp:41-61, :70-71)
-  if (v.o.uniform_eos && mat != 3) {
-    const double rw = density_solid(Ce.pres_eq, Ce.cs, Ce.p0, p, Ce.rho0);
-    v.S.rho_eff[w] = rw;
-    v.S.c_eff[w] = sound_speed(Ce.pres_eq, Ce.cs, rw, Ce.rho0);
-  } else {
-    v.S.rho_eff[w] = xw.w;
-    v.S.c_eff[w] = 0.0;
+  // density, 1/density, p/density^2 and sound speed the partners see (Source/Interaction.cpp:41-61)
+  double rw = xw.w, cwv = 0.0;
+  if (o.uniform_eos && mat != 3) {
+    rw = density_solid(Ce.pres_eq, Ce.cs, Ce.p0, p, Ce.rho0);
+    cwv = sound_speed(Ce.pres_eq, Ce.cs, rw, Ce.rho0);
   }
+  const double inv = 1.0 / rw;
+  v.S.D4[w] = make_double4_32a(inv, p * inv * inv, cwv, rw);
 }
 
 // ---------------------------------------------------------------------------
@@ -270,179 +383,205 @@ template <int DIM, int KT>
 __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
   __shared__ double red[kFT / 32];
   __shared__ unsigned long long cred[kFT / 32];
-  unsigned long long npair2 = 0;  // in-support neighbours: free counted once, fixed twice
+  __shared__ int qbuf[kQN][kFT];
   const StepScalars* sc = v.sc;
   if (sc->stop) return;
   const Persist& P = cur_persist(v);
   const int n = sc->n;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int tid = threadIdx.x;
   const GridDev& g = v.g;
   const Options& o = v.o;
   const PClass* __restrict__ CT = v.cls;
   double dtc = DBL_MAX;
+  unsigned long long npair2 = 0;
+  bool active = false;
+  int cell = -1, ci_cls = 0;
   if (i < n) {
-    const PClass& Ci = CT[P.cls[i]];
-    const double4_32a xi = P.X4[i];
-    if (!Ci.is_free) {
+    ci_cls = P.cls[i];
+    active = CT[ci_cls].is_free;
+    cell = v.S.cellid[i];
+    if (!active) {
       v.S.A4[i] = make_double4_32a(o.gravity[0], o.gravity[1], o.gravity[2], 0.0);
       v.S.zwab[i] = 1.0;
-    } else {
-      const double4_32a vi = P.V4[i];
-      const int cell = v.S.cellid[i];
-      const double di = xi.w, mi = Ci.mass, hi = Ci.h, pi = vi.w;
-      const double mui = o.dyn_mu ? P.mu[i] : Ci.mu0;
-      const double ci_snd = v.S.c_eff[i];
-      const bool shep = Ci.shepard && (sc->shepard_counter == o.shepard_step);
-      const bool sr_self = (Ci.t0 > 0.0 || Ci.les);
-      double ax = o.gravity[0] + o.body_force[0], ay = o.gravity[1] + o.body_force[1],
-             az = o.gravity[2] + o.body_force[2];
-      double drho = 0.0, zw = 0.0, sd = 0.0, xs0 = 0.0, xs1 = 0.0, xs2 = 0.0;
-      double sr[9];
-#pragma unroll
-      for (int e = 0; e < 9; ++e) sr[e] = 0.0;
-      const bool any_periodic = g.periodic[0] | g.periodic[1] | g.periodic[2];
-      const double cf2 = g.cellfac * g.cellfac;
-      if (cell >= 0) {
-        const CellCoord ci = decode(g, cell);
-        for_neighbor_ranges<DIM>(g, ci, v.S.start, [&](int lo, int hi_) {
-          for (int j = lo; j < hi_; ++j) {
-            if (j == i) continue;
-            const double4_32a xj = P.X4[j];
-            const PClass& Cj = CT[P.cls[j]];
-            const double hb = (hi + Cj.h) / 2;
-            double x0 = xi.x - xj.x, x1 = xi.y - xj.y, x2 = xi.z - xj.z;
-            if (any_periodic) periodic_fix(g, x0, x1, x2, hb, ci, decode(g, v.S.cellid[j]));
-            const double r2 = x0 * x0 + x1 * x1 + x2 * x2;
-            if (r2 > cf2 * hb * hb * (1.0 + 1e-9)) continue;
-            const double inv_hb = o.uniform_h ? o.inv_h : 1.0 / hb;
-            const double rij = sqrt(r2);
-            const double q = rij * inv_hb;
-            if (q > g.cellfac) continue;
-            const double4_32a vj = P.V4[j];
-            const bool fj = Cj.is_free;
-            npair2 += fj ? 1ull : 2ull;
-            double dj, mj;
-            if (fj) { dj = xj.w; mj = Cj.mass; }
-            else {
-              dj = o.uniform_eos ? v.S.rho_eff[j] : density_solid(Ci.pres_eq, Ci.cs, Ci.p0, v.S.prs[j], Ci.rho0);
-              mj = Cj.fpmassc * mi;
-            }
-            const double pj = fj ? vj.w : v.S.prs[j];
-            const double ih2 = inv_hb * inv_hb;
-            const double cwh = Kern<DIM, KT>::cw() * (DIM == 2 ? ih2 : ih2 * inv_hb);
-            const double cwg = cwh * ih2;
-            const double inv_q = (q > 0.0) ? 1.0 / q : 0.0;
-            const double GK = Kern<DIM, KT>::GK(q, inv_q, cwg);
-            const double K = Kern<DIM, KT>::W(q, cwh);
-            const double v0 = vi.x - vj.x, v1 = vi.y - vj.y, v2 = vi.z - vj.z;
-            const double vx = v0 * x0 + v1 * x1 + v2 * x2;
-            double PI = 0.0;
-            const double Alpha = (Ci.alpha + Cj.alpha) / 2.0, Beta = (Ci.beta + Cj.beta) / 2.0;
-            if ((Alpha != 0.0 || Beta != 0.0) && vx < 0) {
-              const double cj_snd = fj ? v.S.c_eff[j]
-                                       : (o.uniform_eos ? v.S.c_eff[j] : sound_speed(Ci.pres_eq, Ci.cs, dj, Ci.rho0));
-              const double MU = hb * vx / (r2 + 0.01 * hb * hb);
-              PI = (-Alpha * 0.5 * (ci_snd + cj_snd) * MU + Beta * MU * MU) / (0.5 * (di + dj));
-            }
-            double TI = 0.0;
-            if (Ci.ti > 0.0 || Cj.ti > 0.0) {
-              double Ri = 0.0, Rj = 0.0;
-              if ((pi + pj) < 0.0) {
-                if (pi < 0.0) Ri = -pi / (di * di);
-                if (pj < 0.0) Rj = -pj / (dj * dj);
-              }
-              const double Wd = Kern<DIM, KT>::W((Ci.tid + Cj.tid) / (2.0 * hb), cwh);
-              TI = (Ci.ti * Ri + Cj.ti * Rj) * pow(K / Wd, (Ci.tin + Cj.tin) / 2.0);
-            }
-            double VI0 = 0.0, VI1 = 0.0, VI2 = 0.0;
-            double vab0 = 0.0, vab1 = 0.0, vab2 = 0.0;
-            const bool visc = (Ci.no_slip || Cj.no_slip) || fj;
-            if (visc) {
-              double Mu;
-              if (fj) {
-                vab0 = v0; vab1 = v1; vab2 = v2;
-                const double muj = o.dyn_mu ? P.mu[j] : Cj.mu0;
-                Mu = 2.0 * mui * muj / (mui + muj);
-              } else {
-                const double4_32a ns = v.S.nsv4[j];
-                vab0 = vi.x - (2.0 * vj.x - ns.x);
-                vab1 = vi.y - (2.0 * vj.y - ns.y);
-                vab2 = vi.z - (2.0 * vj.z - ns.z);
-                Mu = mui;
-              }
-              double c;
-              switch (o.vis_eq) {
-                case 0: c = 2.0 * Mu / (di * dj) * GK; break;
-                case 1: c = 8.0 * Mu / ((di + dj) * (di + dj)) * GK; break;
-                case 2: c = -Mu / (di * dj) * Kern<DIM, KT>::Lap(q, inv_q, cwg); break;
-                default: c = 0.0; break;
-              }
-              if (o.vis_eq <= 2) {
-                VI0 = c * vab0; VI1 = c * vab1; VI2 = c * vab2;
-              } else {
-                const double L = Kern<DIM, KT>::Lap(q, inv_q, cwg);
-                const double S2 = Kern<DIM, KT>::D2(q, cwg);
-                const double s = -Mu / (di * dj);
-                const double t = vx / r2 * (-GK + S2);
-                VI0 = s * (L * vab0 + (1.0 / 3.0) * (GK * v0 + t * x0));
-                VI1 = s * (L * vab1 + (1.0 / 3.0) * (GK * v1 + t * x1));
-                VI2 = s * (L * vab2 + (1.0 / 3.0) * (GK * v2 + t * x2));
-              }
-              if (sr_self) {
-                const bool want = (Ci.t0 > 0.0 || Cj.t0 > 0.0 || (Ci.les && Cj.les));
-                if (want) {
-                  const double c2 = -GK * (mj / dj);
-                  sr[0] += c2 * (2.0 * vab0 * x0);
-                  sr[1] += c2 * (vab0 * x1 + vab1 * x0);
-                  sr[2] += c2 * (vab0 * x2 + vab2 * x0);
-                  sr[4] += c2 * (2.0 * vab1 * x1);
-                  sr[5] += c2 * (vab1 * x2 + vab2 * x1);
-                  sr[8] += c2 * (2.0 * vab2 * x2);
-                }
-              }
-            }
-            if (o.xsph != 0.0 && fj) {
-              const double s = o.xsph * mj / (0.5 * (di + dj)) * K;
-              xs0 -= s * v0; xs1 -= s * v1; xs2 -= s * v2;
-            }
-            double s;
-            if (o.grad_type == 0) s = -(pi / (di * di) + pj / (dj * dj) + PI + TI) * GK;
-            else s = -((pi + pj) / (di * dj) + PI + TI) * GK;
-            ax += mj * (s * x0 + VI0);
-            ay += mj * (s * x1 + VI1);
-            if (DIM == 3) az += mj * (s * x2 + VI2);
-            drho += mj * (di / dj) * (GK * vx);
-            zw += mj / dj * K;
-            if (shep) sd += mj * K;
-          }
-        });
-      }
-      v.S.A4[i] = make_double4_32a(ax, ay, az, drho);
-      v.S.zwab[i] = zw;
-      if (o.any_shepard) v.S.sumden[i] = sd;
-      if (o.xsph != 0.0) v.S.vxsph4[i] = make_double4_32a(xs0, xs1, xs2, 0.0);
-      if (o.need_sr) {
-        double* out = v.S.strain_rate + 9 * (size_t)i;
-        out[0] = sr[0]; out[1] = sr[1]; out[2] = sr[2];
-        out[3] = sr[1]; out[4] = sr[4]; out[5] = sr[5];
-        out[6] = sr[2]; out[7] = sr[5]; out[8] = sr[8];
-      }
-      if (!(isfinite(ax) && isfinite(ay) && isfinite(az) && isfinite(drho))) atomicOr(&v.sc->status, ST_NONFINITE);
-      const double an = sqrt(ax * ax + ay * ay + az * az);
-      const double test = sqrt(hi / an);
-      const double cand = o.sqrt_h_a * test;
-      if (cand < dtc) dtc = cand;  // NaN never compares less, as in the reference
     }
   }
-  // block minimum of the acceleration time-step bound
-  for (int off = 16; off > 0; off >>= 1) dtc = fmin(dtc, __shfl_down_sync(0xffffffffu, dtc, off));
-  for (int off = 16; off > 0; off >>= 1) npair2 += __shfl_down_sync(0xffffffffu, npair2, off);
-  if ((threadIdx.x & 31) == 0) {
-    red[threadIdx.x >> 5] = dtc;
-    cred[threadIdx.x >> 5] = npair2;
+  const PClass& Ci = CT[ci_cls];
+  const double4_32a xi = active ? P.X4[i] : make_double4_32a(0, 0, 0, 1);
+  const double4_32a vi = active ? P.V4[i] : make_double4_32a(0, 0, 0, 0);
+  const double4_32a di4 = active ? v.S.D4[i] : make_double4_32a(1, 0, 0, 1);
+  const float4 xi32 = active ? v.S.X32[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const double di = xi.w, inv_i = di4.x, Pi = di4.y, ci_snd = di4.z, pi = vi.w;
+  const double mi = Ci.mass, hi = Ci.h;
+  const double mui = o.dyn_mu ? (active ? P.mu[i] : 0.0) : Ci.mu0;
+  const bool shep = Ci.shepard && (sc->shepard_counter == o.shepard_step);
+  const bool sr_self = (Ci.t0 > 0.0 || Ci.les);
+  double ax = o.gravity[0] + o.body_force[0], ay = o.gravity[1] + o.body_force[1],
+         az = o.gravity[2] + o.body_force[2];
+  double drho = 0.0, zw = 0.0, sd = 0.0, xs0 = 0.0, xs1 = 0.0, xs2 = 0.0;
+  double sr0 = 0.0, sr1 = 0.0, sr2 = 0.0, sr4 = 0.0, sr5 = 0.0, sr8 = 0.0;
+  const bool any_periodic = g.periodic[0] | g.periodic[1] | g.periodic[2];
+  const float cff = (float)g.cellfac;
+  CellCoord cci = decode(g, cell >= 0 ? cell : 0);
+  Cands<DIM> cs;
+  cs.init(g, active ? cell : -1);
+  bool more = active && cell >= 0;
+  while (true) {
+    int qn = 0;
+    while (more && qn < kQN) {
+      const int j = cs.next(g, v.S.start);
+      if (j < 0) {
+        more = false;
+        break;
+      }
+      if (j == i) continue;
+      if (near_f32<DIM>(g, xi32, v.S.X32[j], cff)) qbuf[qn++][tid] = j;
+    }
+    const int qmax = __reduce_max_sync(0xffffffffu, qn);
+    for (int k = 0; k < qmax; ++k) {
+      if (k >= qn) continue;
+      const int j = qbuf[k][tid];
+      const double4_32a xj = P.X4[j];
+      const PClass& Cj = CT[P.cls[j]];
+      const double hb = (hi + Cj.h) / 2;
+      double x0 = xi.x - xj.x, x1 = xi.y - xj.y, x2 = xi.z - xj.z;
+      if (any_periodic) periodic_fix(g, x0, x1, x2, hb, cci, decode(g, v.S.cellid[j]));
+      const double r2 = x0 * x0 + x1 * x1 + x2 * x2;
+      const double inv_hb = o.uniform_h ? o.inv_h : 1.0 / hb;
+      double rij, inv_r = 0.0;
+      if (KT == 1 && o.vis_eq <= 1) {
+        rij = sqrt(r2);
+      } else {
+        inv_r = (r2 > 0.0) ? rsqrt(r2) : 0.0;
+        rij = r2 * inv_r;
+      }
+      const double q = rij * inv_hb;
+      if (q > g.cellfac) continue;
+      const bool fj = Cj.is_free;
+      npair2 += fj ? 1ull : 2ull;
+      const double4_32a vj = P.V4[j];
+      const double4_32a dj4 = v.S.D4[j];
+      double dj, inv_j, Pj, cj_snd;
+      const double mj = fj ? Cj.mass : Cj.fpmassc * mi;
+      const double pj = vj.w;
+      if (fj || o.uniform_eos) {
+        dj = dj4.w; inv_j = dj4.x; Pj = dj4.y; cj_snd = dj4.z;
+      } else {  // wall density from this particle's EOS (Source/Interaction.cpp:53-57)
+        dj = density_solid(Ci.pres_eq, Ci.cs, Ci.p0, pj, Ci.rho0);
+        inv_j = 1.0 / dj;
+        Pj = pj * inv_j * inv_j;
+        cj_snd = sound_speed(Ci.pres_eq, Ci.cs, dj, Ci.rho0);
+      }
+      const double ih2 = inv_hb * inv_hb;
+      const double cwh = Kern<DIM, KT>::cw() * (DIM == 2 ? ih2 : ih2 * inv_hb);
+      const double cwg = cwh * ih2;
+      const double inv_q = hb * inv_r;
+      const double GK = Kern<DIM, KT>::GK(q, inv_q, cwg);
+      const double K = Kern<DIM, KT>::W(q, cwh);
+      const double v0 = vi.x - vj.x, v1 = vi.y - vj.y, v2 = vi.z - vj.z;
+      const double vx = v0 * x0 + v1 * x1 + v2 * x2;
+      double PI = 0.0;
+      const double Alpha = (Ci.alpha + Cj.alpha) / 2.0, Beta = (Ci.beta + Cj.beta) / 2.0;
+      if ((Alpha != 0.0 || Beta != 0.0) && vx < 0) {
+        // (-a c MU + b MU^2) / rho_ij with MU = h v.x / D, as one division
+        const double D = r2 + 0.01 * hb * hb;
+        const double t = hb * vx;
+        PI = t * (-Alpha * 0.5 * (ci_snd + cj_snd) * D + Beta * t) / (D * D * (0.5 * (di + dj)));
+      }
+      double TI = 0.0;
+      if (Ci.ti > 0.0 || Cj.ti > 0.0) {
+        double Ri = 0.0, Rj = 0.0;
+        if ((pi + pj) < 0.0) {
+          if (pi < 0.0) Ri = -pi * inv_i * inv_i;
+          if (pj < 0.0) Rj = -pj * inv_j * inv_j;
+        }
+        const double Wd = Kern<DIM, KT>::W((Ci.tid + Cj.tid) / (2.0 * hb), cwh);
+        TI = (Ci.ti * Ri + Cj.ti * Rj) * pow(K / Wd, (Ci.tin + Cj.tin) / 2.0);
+      }
+      double VI0 = 0.0, VI1 = 0.0, VI2 = 0.0;
+      if ((Ci.no_slip || Cj.no_slip) || fj) {
+        double Mu, vab0, vab1, vab2;
+        if (fj) {
+          vab0 = v0; vab1 = v1; vab2 = v2;
+          if (o.uniform_mu) Mu = o.mu_u;
+          else {
+            const double muj = o.dyn_mu ? P.mu[j] : Cj.mu0;
+            Mu = 2.0 * mui * muj / (mui + muj);
+          }
+        } else {
+          const double4_32a ns = v.S.nsv4[j];
+          vab0 = vi.x - (2.0 * vj.x - ns.x);
+          vab1 = vi.y - (2.0 * vj.y - ns.y);
+          vab2 = vi.z - (2.0 * vj.z - ns.z);
+          Mu = mui;
+        }
+        if (o.vis_eq <= 2) {
+          double c;
+          if (o.vis_eq == 0) c = 2.0 * Mu * inv_i * inv_j * GK;
+          else if (o.vis_eq == 1) c = 8.0 * Mu / ((di + dj) * (di + dj)) * GK;
+          else c = -Mu * inv_i * inv_j * Kern<DIM, KT>::Lap(q, inv_q, cwg);
+          VI0 = c * vab0; VI1 = c * vab1; VI2 = c * vab2;
+        } else {
+          const double L = Kern<DIM, KT>::Lap(q, inv_q, cwg);
+          const double S2 = Kern<DIM, KT>::D2(q, cwg);
+          const double s = -Mu * inv_i * inv_j;
+          const double t = vx / r2 * (-GK + S2);
+          VI0 = s * (L * vab0 + (1.0 / 3.0) * (GK * v0 + t * x0));
+          VI1 = s * (L * vab1 + (1.0 / 3.0) * (GK * v1 + t * x1));
+          VI2 = s * (L * vab2 + (1.0 / 3.0) * (GK * v2 + t * x2));
+        }
+        if (sr_self && (Ci.t0 > 0.0 || Cj.t0 > 0.0 || (Ci.les && Cj.les))) {
+          const double c2 = -GK * (mj * inv_j);
+          sr0 += c2 * (2.0 * vab0 * x0);
+          sr1 += c2 * (vab0 * x1 + vab1 * x0);
+          sr2 += c2 * (vab0 * x2 + vab2 * x0);
+          sr4 += c2 * (2.0 * vab1 * x1);
+          sr5 += c2 * (vab1 * x2 + vab2 * x1);
+          sr8 += c2 * (2.0 * vab2 * x2);
+        }
+      }
+      if (o.xsph != 0.0 && fj) {
+        const double s = o.xsph * mj / (0.5 * (di + dj)) * K;
+        xs0 -= s * v0; xs1 -= s * v1; xs2 -= s * v2;
+      }
+      double s;
+      if (o.grad_type == 0) s = -(Pi + Pj + PI + TI) * GK;
+      else s = -((pi + pj) * inv_i * inv_j + PI + TI) * GK;
+      ax += mj * (s * x0 + VI0);
+      ay += mj * (s * x1 + VI1);
+      if (DIM == 3) az += mj * (s * x2 + VI2);
+      drho += mj * di * inv_j * (GK * vx);
+      zw += mj * inv_j * K;
+      if (shep) sd += mj * K;
+    }
+    if (!__any_sync(0xffffffffu, more)) break;
+  }
+  if (active) {
+    v.S.A4[i] = make_double4_32a(ax, ay, az, drho);
+    v.S.zwab[i] = zw;
+    if (o.any_shepard) v.S.sumden[i] = sd;
+    if (o.xsph != 0.0) v.S.vxsph4[i] = make_double4_32a(xs0, xs1, xs2, 0.0);
+    if (o.need_sr) {
+      double* out = v.S.strain_rate + 9 * (size_t)i;
+      out[0] = sr0; out[1] = sr1; out[2] = sr2;
+      out[3] = sr1; out[4] = sr4; out[5] = sr5;
+      out[6] = sr2; out[7] = sr5; out[8] = sr8;
+    }
+    if (!(isfinite(ax) && isfinite(ay) && isfinite(az) && isfinite(drho))) atomicOr(&v.sc->status, ST_NONFINITE);
+    const double an = sqrt(ax * ax + ay * ay + az * az);
+    const double cand = o.sqrt_h_a * sqrt(hi / an);
+    if (cand < dtc) dtc = cand;  // NaN never compares less, as in the reference
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    dtc = fmin(dtc, __shfl_down_sync(0xffffffffu, dtc, off));
+    npair2 += __shfl_down_sync(0xffffffffu, npair2, off);
+  }
+  if ((tid & 31) == 0) {
+    red[tid >> 5] = dtc;
+    cred[tid >> 5] = npair2;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (tid == 0) {
     double m = red[0];
     unsigned long long c = cred[0];
     for (int k = 1; k < kFT / 32; ++k) {
@@ -461,174 +600,199 @@ template <int DIM, int KT>
 __global__ void __launch_bounds__(kFT) forces_solid_kernel(DevView v) {
   __shared__ double red[kFT / 32];
   __shared__ unsigned long long cred[kFT / 32];
-  unsigned long long npair2 = 0;  // in-support neighbours: free counted once, fixed twice
+  __shared__ int qbuf[kQN][kFT];
   const StepScalars* sc = v.sc;
   if (sc->stop) return;
   const Persist& P = cur_persist(v);
   const int n = sc->n;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int tid = threadIdx.x;
   const GridDev& g = v.g;
   const Options& o = v.o;
   const PClass* __restrict__ CT = v.cls;
   double dtc = DBL_MAX;
+  unsigned long long npair2 = 0;
+  bool active = false;
+  int cell = -1, ci_cls = 0;
   if (i < n) {
-    const PClass& Ci = CT[P.cls[i]];
-    const double4_32a xi = P.X4[i];
-    if (!Ci.is_free) {
+    ci_cls = P.cls[i];
+    active = CT[ci_cls].is_free;
+    cell = v.S.cellid[i];
+    if (!active) {
       v.S.A4[i] = make_double4_32a(o.gravity[0], o.gravity[1], o.gravity[2], 0.0);
       v.S.zwab[i] = 1.0;
-    } else {
-      const double4_32a vi = P.V4[i];
-      const int cell = v.S.cellid[i];
-      const double di = xi.w, mi = Ci.mass, hi = Ci.h;
-      const bool shep = Ci.shepard && (sc->shepard_counter == o.shepard_step);
-      const double* __restrict__ Si = P.sigma + 9 * (size_t)i;
-      const double* __restrict__ Ti = P.tir + 9 * (size_t)i;
-      double ax = o.gravity[0] + o.body_force[0], ay = o.gravity[1] + o.body_force[1],
-             az = o.gravity[2] + o.body_force[2];
-      double drho = 0.0, zw = 0.0, sd = 0.0, xs0 = 0.0, xs1 = 0.0, xs2 = 0.0;
-      double sr[9], rr[9];
-#pragma unroll
-      for (int e = 0; e < 9; ++e) { sr[e] = 0.0; rr[e] = 0.0; }
-      const bool any_periodic = g.periodic[0] | g.periodic[1] | g.periodic[2];
-      const double cf2 = g.cellfac * g.cellfac;
-      const double I22 = (DIM == 2) ? 0.0 : 1.0;  // Domain::I (Source/Domain.cpp:1665)
-      if (cell >= 0) {
-        const CellCoord ci = decode(g, cell);
-        for_neighbor_ranges<DIM>(g, ci, v.S.start, [&](int lo, int hi_) {
-          for (int j = lo; j < hi_; ++j) {
-            if (j == i) continue;
-            const double4_32a xj = P.X4[j];
-            const PClass& Cj = CT[P.cls[j]];
-            const double hb = (hi + Cj.h) / 2;
-            double x0 = xi.x - xj.x, x1 = xi.y - xj.y, x2 = xi.z - xj.z;
-            if (any_periodic) periodic_fix(g, x0, x1, x2, hb, ci, decode(g, v.S.cellid[j]));
-            const double r2 = x0 * x0 + x1 * x1 + x2 * x2;
-            if (r2 > cf2 * hb * hb * (1.0 + 1e-9)) continue;
-            const double inv_hb = o.uniform_h ? o.inv_h : 1.0 / hb;
-            const double rij = sqrt(r2);
-            const double q = rij * inv_hb;
-            if (q > g.cellfac) continue;
-            const double4_32a vj = P.V4[j];
-            const bool fj = Cj.is_free;
-            npair2 += fj ? 1ull : 2ull;
-            const bool soil = (Ci.material * Cj.material == 9);
-            double dj, mj;
-            if (fj) { dj = xj.w; mj = Cj.mass; }
-            else if (soil) { dj = di; mj = Cj.fpmassc * mi; }
-            else {
-              dj = o.uniform_eos ? v.S.rho_eff[j] : density_solid(Ci.pres_eq, Ci.cs, Ci.p0, v.S.prs[j], Ci.rho0);
-              mj = Cj.fpmassc * mi;
-            }
-            const double ih2 = inv_hb * inv_hb;
-            const double cwh = Kern<DIM, KT>::cw() * (DIM == 2 ? ih2 : ih2 * inv_hb);
-            const double cwg = cwh * ih2;
-            const double inv_q = (q > 0.0) ? 1.0 / q : 0.0;
-            const double GK = Kern<DIM, KT>::GK(q, inv_q, cwg);
-            const double K = Kern<DIM, KT>::W(q, cwh);
-            const double v0 = vi.x - vj.x, v1 = vi.y - vj.y, v2 = vi.z - vj.z;
-            const double vx = v0 * x0 + v1 * x1 + v2 * x2;
-            double PIs = 0.0;  // PIij = PIs * I
-            const double Alpha = (Ci.alpha + Cj.alpha) / 2.0, Beta = (Ci.beta + Cj.beta) / 2.0;
-            if ((Alpha != 0.0 || Beta != 0.0) && vx < 0) {
-              const double MU = hb * vx / (r2 + 0.01 * hb * hb);
-              double Cij;
-              if (soil) Cij = 0.5 * (Ci.cs + Cj.cs);
-              else {
-                const double c_i = v.S.c_eff[i];
-                const double c_j = fj ? v.S.c_eff[j] : sound_speed(Ci.pres_eq, Ci.cs, dj, Ci.rho0);
-                Cij = 0.5 * (c_i + c_j);
-              }
-              PIs = (Alpha * Cij * MU + Beta * MU * MU) / (0.5 * (di + dj));
-            }
-            double TIs = 0.0;  // TIij = TIs * (TIR_i + TIR_j)
-            const bool ti = (Ci.ti > 0.0 || Cj.ti > 0.0);
-            if (ti) {
-              const double Wd = Kern<DIM, KT>::W((Ci.tid + Cj.tid) / (2.0 * hb), cwh);
-              TIs = pow(K / Wd, (Ci.tin + Cj.tin) / 2.0);
-            }
-            double vab0, vab1, vab2;
-            if (fj) { vab0 = v0; vab1 = v1; vab2 = v2; }
-            else if (Ci.no_slip || Cj.no_slip) {
-              const double4_32a ns = v.S.nsv4[j];
-              vab0 = vi.x - (2.0 * vj.x - ns.x);
-              vab1 = vi.y - (2.0 * vj.y - ns.y);
-              vab2 = vi.z - (2.0 * vj.z - ns.z);
-            } else {
-              const double4_32a vbj = (o.scheme == PSPH_MVERLET) ? P.H4[j] : P.H4b[j];
-              vab0 = vi.x - vbj.x; vab1 = vi.y - vbj.y; vab2 = vi.z - vbj.z;
-            }
-            const double* __restrict__ Sj = P.sigma + 9 * (size_t)j;
-            const double* __restrict__ Tj = P.tir + 9 * (size_t)j;
-            double M[9];
-            if (o.grad_type == 0) {
-              const double ci2 = 1.0 / (di * di), cj2 = 1.0 / (dj * dj);
-#pragma unroll
-              for (int e = 0; e < 9; ++e) M[e] = Si[e] * ci2 + Sj[e] * cj2;
-            } else {
-              const double c = 1.0 / (di * dj);
-#pragma unroll
-              for (int e = 0; e < 9; ++e) M[e] = (Si[e] + Sj[e]) * c;
-            }
-            M[0] += PIs; M[4] += PIs; M[8] += PIs * I22;
-            if (ti) {
-#pragma unroll
-              for (int e = 0; e < 9; ++e) M[e] += (Ti[e] + Tj[e]) * TIs;
-            }
-            const double g0 = GK * x0, g1 = GK * x1, g2 = GK * x2;
-            const double t0 = g0 * M[0] + g1 * M[3] + g2 * M[6];
-            const double t1 = g0 * M[1] + g1 * M[4] + g2 * M[7];
-            const double t2 = g0 * M[2] + g1 * M[5] + g2 * M[8];
-            ax += mj * t0;
-            ay += mj * t1;
-            if (DIM == 3) az += mj * t2;
-            drho += mj * (di / dj) * (v0 * g0 + v1 * g1 + v2 * g2);
-            const double md = mj / dj;
-            zw += md * K;
-            const double c2 = -0.5 * GK * md;
-            sr[0] += c2 * (2.0 * vab0 * x0);
-            sr[1] += c2 * (vab0 * x1 + vab1 * x0);
-            sr[2] += c2 * (vab0 * x2 + vab2 * x0);
-            sr[4] += c2 * (2.0 * vab1 * x1);
-            sr[5] += c2 * (vab1 * x2 + vab2 * x1);
-            sr[8] += c2 * (2.0 * vab2 * x2);
-            rr[1] += c2 * (vab0 * x1 - vab1 * x0);
-            rr[2] += c2 * (vab0 * x2 - vab2 * x0);
-            rr[5] += c2 * (vab1 * x2 - vab2 * x1);
-            if (o.xsph != 0.0 && fj) {
-              const double s = o.xsph * mj / (0.5 * (di + dj)) * K;
-              xs0 -= s * v0; xs1 -= s * v1; xs2 -= s * v2;
-            }
-            if (shep) sd += mj * K;
-          }
-        });
-      }
-      v.S.A4[i] = make_double4_32a(ax, ay, az, drho);
-      v.S.zwab[i] = zw;
-      if (o.any_shepard) v.S.sumden[i] = sd;
-      if (o.xsph != 0.0) v.S.vxsph4[i] = make_double4_32a(xs0, xs1, xs2, 0.0);
-      double* out = v.S.strain_rate + 9 * (size_t)i;
-      out[0] = sr[0]; out[1] = sr[1]; out[2] = sr[2];
-      out[3] = sr[1]; out[4] = sr[4]; out[5] = sr[5];
-      out[6] = sr[2]; out[7] = sr[5]; out[8] = sr[8];
-      double* ro = v.S.rotation_rate + 9 * (size_t)i;
-      ro[0] = 0.0; ro[1] = rr[1]; ro[2] = rr[2];
-      ro[3] = -rr[1]; ro[4] = 0.0; ro[5] = rr[5];
-      ro[6] = -rr[2]; ro[7] = -rr[5]; ro[8] = 0.0;
-      if (!(isfinite(ax) && isfinite(ay) && isfinite(az) && isfinite(drho))) atomicOr(&v.sc->status, ST_NONFINITE);
-      const double an = sqrt(ax * ax + ay * ay + az * az);
-      const double cand = o.sqrt_h_a * sqrt(hi / an);
-      if (cand < dtc) dtc = cand;
     }
   }
-  for (int off = 16; off > 0; off >>= 1) dtc = fmin(dtc, __shfl_down_sync(0xffffffffu, dtc, off));
-  for (int off = 16; off > 0; off >>= 1) npair2 += __shfl_down_sync(0xffffffffu, npair2, off);
-  if ((threadIdx.x & 31) == 0) {
-    red[threadIdx.x >> 5] = dtc;
-    cred[threadIdx.x >> 5] = npair2;
+  const PClass& Ci = CT[ci_cls];
+  const int is = active ? i : 0;
+  const double4_32a xi = P.X4[is];
+  const double4_32a vi = P.V4[is];
+  const double4_32a di4 = v.S.D4[is];
+  const float4 xi32 = v.S.X32[is];
+  const double di = xi.w, inv_i = di4.x, mi = Ci.mass, hi = Ci.h;
+  const bool shep = Ci.shepard && (sc->shepard_counter == o.shepard_step);
+  const double* __restrict__ Si = P.sigma + 9 * (size_t)is;
+  const double* __restrict__ Ti = P.tir + 9 * (size_t)is;
+  double ax = o.gravity[0] + o.body_force[0], ay = o.gravity[1] + o.body_force[1],
+         az = o.gravity[2] + o.body_force[2];
+  double drho = 0.0, zw = 0.0, sd = 0.0, xs0 = 0.0, xs1 = 0.0, xs2 = 0.0;
+  double sr[6] = {0, 0, 0, 0, 0, 0}, rr[3] = {0, 0, 0};  // sr: 00 01 02 11 12 22; rr: 01 02 12
+  const bool any_periodic = g.periodic[0] | g.periodic[1] | g.periodic[2];
+  const double I22 = (DIM == 2) ? 0.0 : 1.0;  // Domain::I (Source/Domain.cpp:1665)
+  const float cff = (float)g.cellfac;
+  CellCoord cci = decode(g, cell >= 0 ? cell : 0);
+  Cands<DIM> cs;
+  cs.init(g, active ? cell : -1);
+  bool more = active && cell >= 0;
+  while (true) {
+    int qn = 0;
+    while (more && qn < kQN) {
+      const int j = cs.next(g, v.S.start);
+      if (j < 0) {
+        more = false;
+        break;
+      }
+      if (j == i) continue;
+      if (near_f32<DIM>(g, xi32, v.S.X32[j], cff)) qbuf[qn++][tid] = j;
+    }
+    const int qmax = __reduce_max_sync(0xffffffffu, qn);
+    for (int k = 0; k < qmax; ++k) {
+      if (k >= qn) continue;
+      const int j = qbuf[k][tid];
+      const double4_32a xj = P.X4[j];
+      const PClass& Cj = CT[P.cls[j]];
+      const double hb = (hi + Cj.h) / 2;
+      double x0 = xi.x - xj.x, x1 = xi.y - xj.y, x2 = xi.z - xj.z;
+      if (any_periodic) periodic_fix(g, x0, x1, x2, hb, cci, decode(g, v.S.cellid[j]));
+      const double r2 = x0 * x0 + x1 * x1 + x2 * x2;
+      const double inv_hb = o.uniform_h ? o.inv_h : 1.0 / hb;
+      const double inv_r = (r2 > 0.0) ? rsqrt(r2) : 0.0;
+      const double q = r2 * inv_r * inv_hb;
+      if (q > g.cellfac) continue;
+      const bool fj = Cj.is_free;
+      npair2 += fj ? 1ull : 2ull;
+      const double4_32a vj = P.V4[j];
+      const bool soil = (Ci.material * Cj.material == 9);
+      double dj, inv_j, cj_snd = 0.0;
+      double mj;
+      if (fj) {
+        const double4_32a dj4 = v.S.D4[j];
+        dj = xj.w; inv_j = dj4.x; cj_snd = dj4.z; mj = Cj.mass;
+      } else if (soil) {  // soil walls take the partner's density (Source/Interaction.cpp:201-205)
+        dj = di; inv_j = inv_i; mj = Cj.fpmassc * mi;
+      } else {
+        if (o.uniform_eos) {
+          const double4_32a dj4 = v.S.D4[j];
+          dj = dj4.w; inv_j = dj4.x; cj_snd = dj4.z;
+        } else {
+          dj = density_solid(Ci.pres_eq, Ci.cs, Ci.p0, vj.w, Ci.rho0);
+          inv_j = 1.0 / dj;
+          cj_snd = sound_speed(Ci.pres_eq, Ci.cs, dj, Ci.rho0);
+        }
+        mj = Cj.fpmassc * mi;
+      }
+      const double ih2 = inv_hb * inv_hb;
+      const double cwh = Kern<DIM, KT>::cw() * (DIM == 2 ? ih2 : ih2 * inv_hb);
+      const double cwg = cwh * ih2;
+      const double GK = Kern<DIM, KT>::GK(q, hb * inv_r, cwg);
+      const double K = Kern<DIM, KT>::W(q, cwh);
+      const double v0 = vi.x - vj.x, v1 = vi.y - vj.y, v2 = vi.z - vj.z;
+      const double vx = v0 * x0 + v1 * x1 + v2 * x2;
+      double PIs = 0.0;  // PIij = PIs * I
+      const double Alpha = (Ci.alpha + Cj.alpha) / 2.0, Beta = (Ci.beta + Cj.beta) / 2.0;
+      if ((Alpha != 0.0 || Beta != 0.0) && vx < 0) {
+        const double Cij = soil ? 0.5 * (Ci.cs + Cj.cs) : 0.5 * (di4.z + cj_snd);
+        const double D = r2 + 0.01 * hb * hb;
+        const double t = hb * vx;
+        PIs = t * (Alpha * Cij * D + Beta * t) / (D * D * (0.5 * (di + dj)));
+      }
+      double TIs = 0.0;
+      const bool ti = (Ci.ti > 0.0 || Cj.ti > 0.0);
+      if (ti) {
+        const double Wd = Kern<DIM, KT>::W((Ci.tid + Cj.tid) / (2.0 * hb), cwh);
+        TIs = pow(K / Wd, (Ci.tin + Cj.tin) / 2.0);
+      }
+      double vab0, vab1, vab2;
+      if (fj) { vab0 = v0; vab1 = v1; vab2 = v2; }
+      else if (Ci.no_slip || Cj.no_slip) {
+        const double4_32a ns = v.S.nsv4[j];
+        vab0 = vi.x - (2.0 * vj.x - ns.x);
+        vab1 = vi.y - (2.0 * vj.y - ns.y);
+        vab2 = vi.z - (2.0 * vj.z - ns.z);
+      } else {
+        const double4_32a vbj = (o.scheme == PSPH_MVERLET) ? P.H4[j] : P.H4b[j];
+        vab0 = vi.x - vbj.x; vab1 = vi.y - vbj.y; vab2 = vi.z - vbj.z;
+      }
+      const double* __restrict__ Sj = P.sigma + 9 * (size_t)j;
+      const double* __restrict__ Tj = P.tir + 9 * (size_t)j;
+      double M[9];
+      if (o.grad_type == 0) {
+        const double ci2 = inv_i * inv_i, cj2 = inv_j * inv_j;
+#pragma unroll
+        for (int e = 0; e < 9; ++e) M[e] = Si[e] * ci2 + Sj[e] * cj2;
+      } else {
+        const double c = inv_i * inv_j;
+#pragma unroll
+        for (int e = 0; e < 9; ++e) M[e] = (Si[e] + Sj[e]) * c;
+      }
+      M[0] += PIs; M[4] += PIs; M[8] += PIs * I22;
+      if (ti) {
+#pragma unroll
+        for (int e = 0; e < 9; ++e) M[e] += (Ti[e] + Tj[e]) * TIs;
+      }
+      const double g0 = GK * x0, g1 = GK * x1, g2 = GK * x2;
+      ax += mj * (g0 * M[0] + g1 * M[3] + g2 * M[6]);
+      ay += mj * (g0 * M[1] + g1 * M[4] + g2 * M[7]);
+      if (DIM == 3) az += mj * (g0 * M[2] + g1 * M[5] + g2 * M[8]);
+      drho += mj * di * inv_j * (v0 * g0 + v1 * g1 + v2 * g2);
+      const double md = mj * inv_j;
+      zw += md * K;
+      const double c2 = -0.5 * GK * md;
+      sr[0] += c2 * (2.0 * vab0 * x0);
+      sr[1] += c2 * (vab0 * x1 + vab1 * x0);
+      sr[2] += c2 * (vab0 * x2 + vab2 * x0);
+      sr[3] += c2 * (2.0 * vab1 * x1);
+      sr[4] += c2 * (vab1 * x2 + vab2 * x1);
+      sr[5] += c2 * (2.0 * vab2 * x2);
+      rr[0] += c2 * (vab0 * x1 - vab1 * x0);
+      rr[1] += c2 * (vab0 * x2 - vab2 * x0);
+      rr[2] += c2 * (vab1 * x2 - vab2 * x1);
+      if (o.xsph != 0.0 && fj) {
+        const double s = o.xsph * mj / (0.5 * (di + dj)) * K;
+        xs0 -= s * v0; xs1 -= s * v1; xs2 -= s * v2;
+      }
+      if (shep) sd += mj * K;
+    }
+    if (!__any_sync(0xffffffffu, more)) break;
+  }
+  if (active) {
+    v.S.A4[i] = make_double4_32a(ax, ay, az, drho);
+    v.S.zwab[i] = zw;
+    if (o.any_shepard) v.S.sumden[i] = sd;
+    if (o.xsph != 0.0) v.S.vxsph4[i] = make_double4_32a(xs0, xs1, xs2, 0.0);
+    double* out = v.S.strain_rate + 9 * (size_t)i;
+    out[0] = sr[0]; out[1] = sr[1]; out[2] = sr[2];
+    out[3] = sr[1]; out[4] = sr[3]; out[5] = sr[4];
+    out[6] = sr[2]; out[7] = sr[4]; out[8] = sr[5];
+    double* ro = v.S.rotation_rate + 9 * (size_t)i;
+    ro[0] = 0.0; ro[1] = rr[0]; ro[2] = rr[1];
+    ro[3] = -rr[0]; ro[4] = 0.0; ro[5] = rr[2];
+    ro[6] = -rr[1]; ro[7] = -rr[2]; ro[8] = 0.0;
+    if (!(isfinite(ax) && isfinite(ay) && isfinite(az) && isfinite(drho))) atomicOr(&v.sc->status, ST_NONFINITE);
+    const double an = sqrt(ax * ax + ay * ay + az * az);
+    const double cand = o.sqrt_h_a * sqrt(hi / an);
+    if (cand < dtc) dtc = cand;
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    dtc = fmin(dtc, __shfl_down_sync(0xffffffffu, dtc, off));
+    npair2 += __shfl_down_sync(0xffffffffu, npair2, off);
+  }
+  if ((tid & 31) == 0) {
+    red[tid >> 5] = dtc;
+    cred[tid >> 5] = npair2;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (tid == 0) {
     double m = red[0];
     unsigned long long c = cred[0];
     for (int k = 1; k < kFT / 32; ++k) {

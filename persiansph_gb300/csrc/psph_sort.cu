@@ -179,6 +179,10 @@ __global__ void reorder_kernel(DevView v, const int* __restrict__ perm, const in
     dst.H4[s] = src.H4[i];
     if (src.H4b) dst.H4b[s] = src.H4b[i];
     dst.cls[s] = src.cls[i];
+    {
+      const double4_32a xs = src.X4[i];
+      v.S.X32[s] = make_float4((float)xs.x, (float)xs.y, (float)xs.z, (float)v.cls[src.cls[i]].h);
+    }
     dst.orig[s] = src.orig[i];
     const int k = key[i];
     cellid[s] = (k < ncells) ? k : -1;

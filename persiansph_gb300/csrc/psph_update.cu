@@ -225,7 +225,10 @@ __global__ void __launch_bounds__(kUT) update_kernel(DevView v) {
           mu = C.mu_ref + C.rho0 * (ch * ch) * sbar;
         }
         if (C.t0 > 0.0) {
-          if (C.vis_m == 0) mu = (shear_rate != 0.0) ? C.mu_ref + C.t0 * (1 - exp(-C.bm * shear_rate)) / shear_rate
+          // Bingham (Source/Particle.cpp:166-170): 1-exp(-m g) evaluated as -expm1(-m g),
+          // the same function without the cancellation that makes the reference's
+          // form return T0*0 instead of T0*m for shear rates below ~1e-16/m
+          if (C.vis_m == 0) mu = (shear_rate != 0.0) ? C.mu_ref + C.t0 * (-expm1(-C.bm * shear_rate)) / shear_rate
                                                     : C.mu_ref + C.t0 * C.bm;
           else mu = (1000.0 * C.mu_ref + C.mu_ref * C.mu_ref * 1000.0 / C.t0 * shear_rate) /
                     (1 + 1000.0 * C.mu_ref / C.t0 * shear_rate);
