@@ -32,17 +32,17 @@ import numpy as np
 REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
-METRIC = "pair-interactions/s @ 3D dam break (5.28M fluid particles)"
+METRIC = "pair-interactions/s @ 3D dam break (5.28M fluid particles), FP32C form; FP64 plain beside it"
 UNIT = "pair-interactions/s"
 # FP64 operations per directed pair evaluation of the fluid kernel for this
 # workload's options (Wendland, Tait, artificial viscosity, Morris, squared
 # density): counted from forces_fluid_kernel with FMA = 2 and a division or
 # square root = 1 (measurement).
 FLOPS_PER_DIRECTED_PAIR = 90
-# algorithmic HBM bytes per particle of one force-kernel launch: read each
-# particle's inputs once (X4 32, V4 32, class 4, derived rho/c/p 24) and write
-# its outputs once (A4 32, zwab 8, sumden 8).
-FORCE_BYTES_PER_PARTICLE = 140
+# algorithmic HBM bytes per particle of one FP32C force-kernel launch: read each
+# particle's inputs once (offset+h 16, v+p 16, 1/rho, p/rho^2, c, rho 16, class
+# 4, cell 4) and write its outputs once (a + drho 32, zwab 8, sumden 8).
+FORCE32_BYTES_PER_PARTICLE = 104
 
 
 def peaks():
@@ -179,43 +179,48 @@ def main():
     import ctypes
 
     dom, dt, info = build_workload(args.dx)
-    cfg = dom.config(dt)
     n = dom.particles.n
 
-    gd = GpuDomain(cfg)
-    gd.upload(dom.particles, initial=True)
-    gd.step(args.warmup)
-    pc0 = gd.pair_count()
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        ms, done = gd.step_timed(args.steps)
-    torch.cuda.synchronize()
-    pc1 = gd.pair_count()
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    pairs = pc1 - pc0
-    launches = gd.last_launch_count()
-    value_rank = pairs / (ms * 1e-3)
-    value = value_rank * world
-    steps_per_s = done / (ms * 1e-3)
+    def measure(precision):
+        cfg = dom.config(dt)
+        cfg.precision = precision
+        gd = GpuDomain(cfg)
+        gd.upload(dom.particles, initial=True)
+        gd.step(args.warmup)
+        pc0 = gd.pair_count()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        with ClockSampler(local) as clk:
+            ms, done = gd.step_timed(args.steps)
+        torch.cuda.synchronize()
+        pc1 = gd.pair_count()
+        if dist:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        launches = gd.last_launch_count()
+        # per-phase device times (separate short run, events between phases)
+        gd.enable_timing(True)
+        gd.step(3)
+        phases = [x / 3.0 for x in gd.phase_times()]
+        gd.enable_timing(False)
+        gd.close()
+        pairs = pc1 - pc0
+        return {"cfg": cfg, "ms": ms, "done": done, "pairs": pairs, "launches": launches, "phases": phases,
+                "clocks": clk.summary(), "value_rank": pairs / (ms * 1e-3), "steps_per_s": done / (ms * 1e-3),
+                "pairs_per_step": pairs / max(done, 1)}
 
-    # per-phase device times (separate short run, events between phases)
-    gd.enable_timing(True)
-    gd.step(3)
-    phases = gd.phase_times()
-    gd.enable_timing(False)
-    force_ms = phases[2] / 3.0
-    pairs_per_step = pairs / max(done, 1)
+    m32 = measure(1)   # PSPH_FP32C: the headline form
+    m64 = measure(0)   # PSPH_FP64: the plain form
     lib = abi.load_library()
     fp64 = ctypes.c_double(0.0)
     lib.psph_probe_fp64_peak(ctypes.byref(fp64))
     pk = peaks()
-    achieved_gbs = FORCE_BYTES_PER_PARTICLE * n / (force_ms * 1e-3) / 1e9
-    fp64_tflops = 2 * pairs_per_step * FLOPS_PER_DIRECTED_PAIR / (force_ms * 1e-3) / 1e12
+    force32_ms = m32["phases"][2]
+    force64_ms = m64["phases"][2]
+    achieved_gbs = FORCE32_BYTES_PER_PARTICLE * n / (force32_ms * 1e-3) / 1e9
+    fp64_tflops = 2 * m64["pairs_per_step"] * FLOPS_PER_DIRECTED_PAIR / (force64_ms * 1e-3) / 1e12
     traffic = None
     tf = os.path.join(REPO, "profiles", "force_traffic.json")
     if os.path.exists(tf):
@@ -225,10 +230,9 @@ def main():
             traffic = None
 
     # end to end through the C ABI with host buffers: upload + K steps + download
-    gd.close()
     fields = ("x", "v", "density", "pressure", "a", "ddensity")
     t0 = time.perf_counter()
-    ge = GpuDomain(cfg)
+    ge = GpuDomain(m32["cfg"])
     ge.upload(dom.particles, initial=True)
     done_e = ge.step(args.steps)
     out = ge.download_fields(fields)
@@ -239,30 +243,41 @@ def main():
     h2d = sum(dom.particles.get(f).nbytes for f in dom.particles.arrays())
     d2h = sum(a.nbytes for a in out.values())
 
+    def phase_dict(m):
+        p = m["phases"]
+        return {"sort": p[0], "prepare_walls": p[1], "forces": p[2], "dt": p[3], "update": p[4]}
+
+    world_mult = world
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": done, "warmup": args.warmup,
-        "ms_per_step": ms / max(done, 1), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic lattice (seeded); inputs larger than L2 (no flush needed)",
+        "metric": METRIC, "value": m32["value_rank"] * world_mult, "unit": UNIT, "n_gpus": world,
+        "steps": m32["done"], "warmup": args.warmup, "ms_per_step": m32["ms"] / max(m32["done"], 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 pair arithmetic (Kahan-compensated sums), f64 integration",
+        "data": "synthetic lattice (seeded); inputs larger than L2 (no flush needed)",
         "config": {"workload": "3D dam break: tank 3.22x1.0x1.0 m, column 1.2x0.55x1.0 m, dx=%g m" % args.dx,
                    "particles": n, "fluid": info["n_fluid"], "walls": info["n_wall"], "kernel": "Wendland C2",
                    "h_over_dx": 1.3, "eos": "Tait c0=40", "scheme": "Modified Verlet + Shepard",
-                   "form": "FP64 plain", "parallelism": "replicas only" if world > 1 else "single GPU",
+                   "form": "FP32C (closure off)", "parallelism": "replicas only" if world > 1 else "single GPU",
                    "l2": "working set > L2"},
-        "steps_per_s": steps_per_s, "pairs_per_step": pairs_per_step,
-        "phase_ms": {"sort": phases[0] / 3, "wall_prepare": phases[1] / 3, "forces": force_ms,
-                     "dt": phases[3] / 3, "update": phases[4] / 3},
+        "steps_per_s": m32["steps_per_s"], "pairs_per_step": m32["pairs_per_step"],
+        "phase_ms": phase_dict(m32),
+        "fp64_plain": {"value": m64["value_rank"] * world_mult, "unit": UNIT, "steps_per_s": m64["steps_per_s"],
+                       "ms_per_step": m64["ms"] / max(m64["done"], 1), "phase_ms": phase_dict(m64),
+                       "clocks": m64["clocks"]},
+        "fp32c_over_fp64_steps_per_s": m32["steps_per_s"] / m64["steps_per_s"],
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved_gbs / pk["hbm_gbs"], "traffic": traffic,
-                     "kernel": "forces_fluid_kernel", "peak_source": pk["src"],
-                     "note": "FP64 pair kernel is FP64-pipe bound; see roofline_fp64"},
-        "roofline_fp64": {"bound": "fp64", "achieved": fp64_tflops, "peak": fp64.value, "unit": "TFLOP/s",
+                     "kernel": "forces_fluid32_kernel", "peak_source": pk["src"],
+                     "bytes_per_particle": FORCE32_BYTES_PER_PARTICLE},
+        "roofline_fp64": {"bound": "fp64", "kernel": "forces_fluid_kernel", "achieved": fp64_tflops,
+                          "peak": fp64.value, "unit": "TFLOP/s",
                           "frac": fp64_tflops / fp64.value if fp64.value else None,
                           "peak_source": "measured here by psph_probe_fp64_peak (DFMA chains)"},
-        "clocks": clk.summary(),
+        "clocks": m32["clocks"],
         "e2e": {"value": pe / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d / max(done_e, 1),
                 "d2h_bytes_per_step": d2h / max(done_e, 1), "steps": done_e,
                 "note": "create + upload + steps + download through the C ABI, host wall clock"},
-        "gpu_launches": launches,
+        "gpu_launches": m32["launches"],
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1

@@ -189,9 +189,11 @@ void enqueue_step(psph_ctx* c) {
   record_phase(c, 0);
   launch_sort(v, st);
   record_phase(c, 1);
-  launch_prepare(v, st);
+  if (v.o.fp32) launch_prepare32(v, st);
+  else launch_prepare(v, st);
   record_phase(c, 2);
-  launch_forces(v, st);
+  if (v.o.fp32) launch_forces32(v, st);
+  else launch_forces(v, st);
   record_phase(c, 3);
   launch_dt(v, st);
   record_phase(c, 4);
@@ -245,7 +247,8 @@ psph_status psph_create(const psph_config* cfg, psph_ctx** out) {
   if (k.scheme != PSPH_MVERLET && k.scheme != PSPH_LEAPFROG)
     return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Scheme must be 0 (Modified Verlet) or 1 (Leapfrog)");
   if (k.swi_type != 0) return set_err(c, PSPH_ERR_UNSUPPORTED, "soil-water interaction (SWIType) is outside this build");
-  if (k.precision != PSPH_FP64) return set_err(c, PSPH_ERR_UNSUPPORTED, "only the FP64 form is in this library build");
+  if (k.precision != PSPH_FP64 && k.precision != PSPH_FP32C)
+    return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "precision must be PSPH_FP64 or PSPH_FP32C");
   if (k.dimension == 2 && k.periodic[2]) return set_err(c, PSPH_ERR_UNSUPPORTED, "periodic z in 2D");
   for (int e = 0; e < 8; ++e)
     if (k.reserved[e]) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "reserved fields must be zero");
@@ -427,6 +430,10 @@ psph_status psph_upload(psph_ctx* c, const psph_particles* p, int initial) {
   o.scheme = k.scheme;
   o.wallp_physical = (k.wall_pressure_mode == PSPH_WALLP_PHYSICAL);
   o.has_solid = (material0 > 1);
+  o.fp32 = (k.precision == PSPH_FP32C);
+  if (o.fp32 && o.has_solid)
+    return set_err(c, PSPH_ERR_UNSUPPORTED, "the FP32C form covers fluids (Material 1); use PSPH_FP64 for solids and soil");
+  if (o.fp32 && n >= (1LL << 26)) return set_err(c, PSPH_ERR_UNSUPPORTED, "the FP32C form handles fewer than 2^26 particles");
   o.soil_pairs = (material0 == 3);
   o.dyn_mu = dyn_mu;
   o.xsph = k.xsph;
@@ -503,6 +510,8 @@ psph_status psph_upload(psph_ctx* c, const psph_particles* p, int initial) {
     return st;
   if (o.need_sr || o.has_solid)
     if ((st = dalloc(c, &S.strain_rate, 9 * N))) return st;
+  if (o.fp32)
+    if ((st = dalloc(c, &S.OFF32, N)) || (st = dalloc(c, &S.V32, N)) || (st = dalloc(c, &S.D32, N))) return st;
   if (o.has_solid) {
     if ((st = dalloc(c, &S.rotation_rate, 9 * N)) || (st = dalloc(c, &S.sigma_o, 9 * N)) ||
         (st = dalloc(c, &S.strain_o, 9 * N)) || (st = dalloc(c, &S.shear_o, 9 * N)))

@@ -36,6 +36,9 @@ struct Scratch {
   double* blockmin;
   // per-step derived / outputs
   float4* X32;       // FP32 copy of (x, y, z, h) for the conservative neighbour prefilter
+  float4* OFF32;     // FP32C form: (offset from the cell origin, h)
+  float4* V32;       // FP32C form: (v, pressure)
+  float4* D32;       // FP32C form: (1/density, pressure/density^2, sound speed, density)
   double4_32a* D4;   // seen by partners: (1/density, pressure/density^2, sound speed, density);
                      // a wall's density is the inverse EOS of its interpolated pressure
   double4_32a* A4;       // ax, ay, az, dDensity
@@ -55,6 +58,7 @@ struct Scratch {
 
 struct Options {
   int dim, kt, vis_eq, grad_type, scheme, wallp_physical;
+  int fp32;           // PSPH_FP32C pair arithmetic
   int has_solid;      // any Material 2/3
   int any_av;         // any alpha/beta != 0
   int any_ti;         // any TI > 0
@@ -93,6 +97,8 @@ PSPH_D const Persist& next_persist(const DevView& v) { return v.sc->buf ? v.PA :
 // Launch wrappers (defined in the .cu files).
 void launch_sort(const DevView& v, cudaStream_t st);      // bin + scan + scatter + rank + reorder + flip
 void launch_prepare(const DevView& v, cudaStream_t st);   // per-particle derived quantities, TIR
+void launch_prepare32(const DevView& v, cudaStream_t st); // FP32C form: copies + wall interpolation
+void launch_forces32(const DevView& v, cudaStream_t st);  // FP32C form: fluid pair forces
 void launch_wall(const DevView& v, cudaStream_t st);      // wall interpolation
 void launch_forces(const DevView& v, cudaStream_t st);    // pair forces + per-block dt minimum
 void launch_dt(const DevView& v, cudaStream_t st);        // dt reduction + AdaptiveTimeStep

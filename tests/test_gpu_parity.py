@@ -123,3 +123,44 @@ def test_step_stops_at_t_stop(gpu):
     done = gd.step(1000, t_stop=5.5 * dt)
     assert done == 6  # Solve's loop runs while Time < tf
     assert gd.time == pytest.approx(6 * dt)
+
+
+FLUID_CASES = ["dam2d", "dam2d_leapfrog", "poiseuille", "dam3d", "fluid_options", "fluid_shao_bingham",
+               "fluid_incomp_quintic"]
+
+
+@pytest.mark.parametrize("name", FLUID_CASES)
+def test_fp32c_single_step_parity_1e5(gpu, name):
+    """FP32C form: accelerations and density rates within 1e-5 of the FP64
+    oracle, relative to each particle's sum of term magnitudes."""
+    builder, _, _ = CASES[name]
+    dom, dt, _ = builder()
+    cfg = dom.config(dt)
+    cfg32 = dom.config(dt)
+    cfg32.precision = 1  # PSPH_FP32C
+    for warm in (0, 3):
+        o = OracleDomain(cfg, dom.particles, initial=True)
+        if warm:
+            o.step(warm)
+            gd = continue_on_gpu(cfg32, o)
+        else:
+            gd = GpuDomain(cfg32)
+            gd.upload(dom.particles, initial=True)
+        o.step(1)
+        gd.step(1)
+        a_scale, dr_scale = o.scales()
+        g, r = gd.download_fields(), o.download()
+        free = r["is_free"] == 1
+        ea = np.max(np.linalg.norm(g["a"] - r["a"], axis=1)[free] / a_scale[free])
+        ed = np.max(np.abs(g["ddensity"] - r["ddensity"])[free] / (dr_scale[free] + 1e-30))
+        assert ea <= 1e-5, f"{name} {warm}: FP32C acceleration rel err {ea:.3e}"
+        assert ed <= 1e-5, f"{name} {warm}: FP32C density-rate rel err {ed:.3e}"
+
+
+def test_fp32c_rejects_solids(gpu):
+    dom, dt, _ = CASES["granular"][0]()
+    cfg = dom.config(dt)
+    cfg.precision = 1
+    gd = GpuDomain(cfg)
+    with pytest.raises(Exception, match="UNSUPPORTED"):
+        gd.upload(dom.particles, initial=True)
