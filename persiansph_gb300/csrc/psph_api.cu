@@ -33,6 +33,7 @@ struct psph_ctx {
   Persist PA{}, PB{};
   Scratch S{};
   PClass* d_cls = nullptr;
+  PClass32* d_cls32 = nullptr;
   StepScalars* d_sc = nullptr;
   StepScalars* h_sc = nullptr;  // pinned mirror
   uint8_t* d_alive = nullptr;
@@ -174,6 +175,7 @@ DevView view(psph_ctx* c) {
   v.PB = c->PB;
   v.S = c->S;
   v.cls = c->d_cls;
+  v.cls32 = c->d_cls32;
   v.sc = c->d_sc;
   v.alive = c->d_alive;
   v.ncap = c->ncap;
@@ -188,6 +190,7 @@ void enqueue_step(psph_ctx* c) {
   launch_begin(v, st);
   record_phase(c, 0);
   launch_sort(v, st);
+  launch_nlist(v, st);
   record_phase(c, 1);
   if (v.o.fp32) launch_prepare32(v, st);
   else launch_prepare(v, st);
@@ -433,7 +436,7 @@ psph_status psph_upload(psph_ctx* c, const psph_particles* p, int initial) {
   o.fp32 = (k.precision == PSPH_FP32C);
   if (o.fp32 && o.has_solid)
     return set_err(c, PSPH_ERR_UNSUPPORTED, "the FP32C form covers fluids (Material 1); use PSPH_FP64 for solids and soil");
-  if (o.fp32 && n >= (1LL << 26)) return set_err(c, PSPH_ERR_UNSUPPORTED, "the FP32C form handles fewer than 2^26 particles");
+  if (n >= (1LL << 26)) return set_err(c, PSPH_ERR_UNSUPPORTED, "this build handles fewer than 2^26 particles");
   o.soil_pairs = (material0 == 3);
   o.dyn_mu = dyn_mu;
   o.xsph = k.xsph;
@@ -503,7 +506,7 @@ psph_status psph_upload(psph_ctx* c, const psph_particles* p, int initial) {
   if ((st = dalloc(c, &S.key, N)) || (st = dalloc(c, &S.count, NC + 2)) || (st = dalloc(c, &S.start, NC + 3)) ||
       (st = dalloc(c, &S.tmp_perm, N)) || (st = dalloc(c, &S.perm, N)) || (st = dalloc(c, &S.cellid, N)) ||
       (st = dalloc(c, &S.block_sums, (NC + 2 + 1023) / 1024 + 1)) || (st = dalloc(c, &S.blockmin, (size_t)nb_forces)) ||
-      (st = dalloc(c, &S.X32, N)) || (st = dalloc(c, &S.D4, N)) ||
+      (st = dalloc(c, &S.OFF32, N)) || (st = dalloc(c, &S.D4, N)) || (st = dalloc(c, &S.nl_count, N)) ||
       (st = dalloc(c, &S.A4, N)) || (st = dalloc(c, &S.zwab, N)) || (st = dalloc(c, &S.sumden, N)) ||
       (st = dalloc(c, &S.sumkernel, N)) || (st = dalloc(c, &S.nsv4, N)) || (st = dalloc(c, &S.vxsph4, N)) ||
       (st = dalloc(c, &S.shear_rate, N)) || (st = dalloc(c, &S.sbar, N)))
@@ -511,7 +514,28 @@ psph_status psph_upload(psph_ctx* c, const psph_particles* p, int initial) {
   if (o.need_sr || o.has_solid)
     if ((st = dalloc(c, &S.strain_rate, 9 * N))) return st;
   if (o.fp32)
-    if ((st = dalloc(c, &S.OFF32, N)) || (st = dalloc(c, &S.V32, N)) || (st = dalloc(c, &S.D32, N))) return st;
+    if ((st = dalloc(c, &S.V32, N)) || (st = dalloc(c, &S.D32, N))) return st;
+  // neighbour lists: 3D supports hold ~80 (h = 1.3 dx) particles, 2D ~20-44;
+  // a particle with more falls back to scanning its cells
+  o.nl_cap = (k.dimension == 3) ? 128 : 64;
+  if ((st = dalloc(c, &S.nl, (size_t)o.nl_cap * N))) return st;
+  {
+    std::vector<PClass32> c32(c->classes.size());
+    for (size_t q = 0; q < c->classes.size(); ++q) {
+      const PClass& C = c->classes[q];
+      PClass32& F = c32[q];
+      F.mass = (float)C.mass; F.h = (float)C.h; F.fpmassc = (float)C.fpmassc; F.alpha = (float)C.alpha;
+      F.beta = (float)C.beta; F.mu0 = (float)C.mu0; F.ti = (float)C.ti; F.tin = (float)C.tin; F.tid = (float)C.tid;
+      F.cs = (float)C.cs; F.rho0 = (float)C.rho0; F.p0 = (float)C.p0;
+      F.flags = (C.is_free ? CF_FREE : 0) | (C.no_slip ? CF_NOSLIP : 0) | (C.les ? CF_LES : 0) |
+                (C.shepard ? CF_SHEPARD : 0) | (C.t0 > 0.0 ? CF_T0 : 0) | (C.ti > 0.0 ? CF_TI : 0);
+      F.material = C.material;
+      F.pres_eq = C.pres_eq;
+      F.pad = 0;
+    }
+    if ((st = dalloc(c, &c->d_cls32, c32.size()))) return st;
+    CUDA_TRY(c, cudaMemcpy(c->d_cls32, c32.data(), c32.size() * sizeof(PClass32), cudaMemcpyHostToDevice));
+  }
   if (o.has_solid) {
     if ((st = dalloc(c, &S.rotation_rate, 9 * N)) || (st = dalloc(c, &S.sigma_o, 9 * N)) ||
         (st = dalloc(c, &S.strain_o, 9 * N)) || (st = dalloc(c, &S.shear_o, 9 * N)))

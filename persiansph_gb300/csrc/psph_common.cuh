@@ -37,6 +37,15 @@ struct PClass {
   int material, is_free, no_slip, pres_eq, shepard, les, vis_m, fail, id, pad;
 };
 
+// FP32 copy of the class constants used inside the FP32C pair loops (so those
+// loops issue no FP64 instructions), with the boolean switches as bits.
+struct PClass32 {
+  float mass, h, fpmassc, alpha, beta, mu0, ti, tin, tid, cs, rho0, p0;
+  int flags;  // bit 0 free, 1 no-slip, 2 LES, 3 Shepard, 4 T0>0, 5 TI>0
+  int material, pres_eq, pad;
+};
+enum : int { CF_FREE = 1, CF_NOSLIP = 2, CF_LES = 4, CF_SHEPARD = 8, CF_T0 = 16, CF_TI = 32 };
+
 // Domain scalars advanced on the device.
 struct StepScalars {
   double time, deltat, deltatint, deltatmin;

@@ -35,8 +35,10 @@ struct Scratch {
   int* block_sums;
   double* blockmin;
   // per-step derived / outputs
-  float4* X32;       // FP32 copy of (x, y, z, h) for the conservative neighbour prefilter
-  float4* OFF32;     // FP32C form: (offset from the cell origin, h)
+  float4* OFF32;     // (position - cell origin, h) in FP32, written by the reorder
+  int* nl;           // per-step neighbour lists, entry k of particle i at nl[k*ncap + i]:
+                     // index | cell-offset code << 26
+  int* nl_count;     // list length, or -1 when it exceeded the capacity (scan instead)
   float4* V32;       // FP32C form: (v, pressure)
   float4* D32;       // FP32C form: (1/density, pressure/density^2, sound speed, density)
   double4_32a* D4;   // seen by partners: (1/density, pressure/density^2, sound speed, density);
@@ -72,6 +74,7 @@ struct Options {
   int uniform_mu;     // every free particle has the same constant viscosity
   double mu_u;        // that viscosity
   double inv_h;       // 1/h when uniform
+  int nl_cap;         // neighbour-list capacity per particle
   double xsph, sqrt_h_a;
   double gravity[3], body_force[3];
   int shepard_step;
@@ -85,6 +88,7 @@ struct DevView {
   Persist PA, PB; // double-buffered persistent arrays; StepScalars::buf says which is current
   Scratch S;
   const PClass* cls;
+  const PClass32* cls32;
   StepScalars* sc;
   uint8_t* alive;
   int ncap;
@@ -96,6 +100,7 @@ PSPH_D const Persist& next_persist(const DevView& v) { return v.sc->buf ? v.PA :
 
 // Launch wrappers (defined in the .cu files).
 void launch_sort(const DevView& v, cudaStream_t st);      // bin + scan + scatter + rank + reorder + flip
+void launch_nlist(const DevView& v, cudaStream_t st);     // per-step neighbour lists
 void launch_prepare(const DevView& v, cudaStream_t st);   // per-particle derived quantities, TIR
 void launch_prepare32(const DevView& v, cudaStream_t st); // FP32C form: copies + wall interpolation
 void launch_forces32(const DevView& v, cudaStream_t st);  // FP32C form: fluid pair forces

@@ -18,79 +18,13 @@
 //                 and AdaptiveTimeStep (Source/Domain.cpp:133-152)
 #include <cfloat>
 
-#include "psph_device.cuh"
+#include "psph_pairs.cuh"
 
 namespace psph {
 
 namespace {
 
 constexpr int kFT = 128;  // threads per block of the pair kernels
-
-struct CellCoord {
-  int x, y, z;
-};
-
-PSPH_D CellCoord decode(const GridDev& g, int c) {
-  CellCoord r;
-  r.x = c % g.nc[0];
-  const int t = c / g.nc[0];
-  r.y = t % g.nc[1];
-  r.z = t / g.nc[1];
-  return r;
-}
-
-// Periodic_X_Correction (Source/Domain.cpp:110-115) for the pair (P1, P2).
-PSPH_D void periodic_fix(const GridDev& g, double& x0, double& x1, double& x2, double hb, const CellCoord& c1,
-                         const CellCoord& c2) {
-  const double lim = 2 * g.cellfac * hb;
-  if (g.dom_size[0] > 0.0 && (x0 > lim || x0 < -lim)) x0 += (c1.x > c2.x) ? -g.dom_size[0] : g.dom_size[0];
-  if (g.dom_size[1] > 0.0 && (x1 > lim || x1 < -lim)) x1 += (c1.y > c2.y) ? -g.dom_size[1] : g.dom_size[1];
-  if (g.dom_size[2] > 0.0 && (x2 > lim || x2 < -lim)) x2 += (c1.z > c2.z) ? -g.dom_size[2] : g.dom_size[2];
-}
-
-// Visits the sorted index ranges of the 3 (2D) or 9 (3D) cell rows around c.
-template <int DIM, class F>
-PSPH_D void for_neighbor_ranges(const GridDev& g, const CellCoord& c, const int* __restrict__ start, F&& f) {
-  const int zlo = (DIM == 3) ? -1 : 0, zhi = (DIM == 3) ? 1 : 0;
-  for (int dz = zlo; dz <= zhi; ++dz) {
-    int z = c.z + dz;
-    if (g.periodic[2]) z = (z + g.nc[2]) % g.nc[2];
-    else if (z < 0 || z >= g.nc[2]) continue;
-    for (int dy = -1; dy <= 1; ++dy) {
-      int y = c.y + dy;
-      if (g.periodic[1]) y = (y + g.nc[1]) % g.nc[1];
-      else if (y < 0 || y >= g.nc[1]) continue;
-      const int row = (z * g.nc[1] + y) * g.nc[0];
-      if (!g.periodic[0] || (c.x >= 1 && c.x <= g.nc[0] - 2)) {
-        const int x0 = max(c.x - 1, 0), x1 = min(c.x + 1, g.nc[0] - 1);
-        f(start[row + x0], start[row + x1 + 1]);
-      } else {
-        for (int dx = -1; dx <= 1; ++dx) {
-          const int x = (c.x + dx + g.nc[0]) % g.nc[0];
-          f(start[row + x], start[row + x + 1]);
-        }
-      }
-    }
-  }
-}
-
-// True when MainNeighbourSearch lists (w, f) with w first: f's cell is in w's
-// forward half stencil (Source/Domain.cpp:860-940), or, in the same cell, w
-// has the larger index (head insertion reverses index order, :736-740).
-PSPH_D bool first_of_pair(const GridDev& g, const CellCoord& cw, const CellCoord& cf, int orig_w, int orig_f) {
-  int o[3] = {cf.x - cw.x, cf.y - cw.y, cf.z - cw.z};
-  const int n[3] = {g.nc[0], g.nc[1], g.nc[2]};
-#pragma unroll
-  for (int d = 0; d < 3; ++d)
-    if (g.periodic[d]) {
-      if (o[d] > 1) o[d] -= n[d];
-      if (o[d] < -1) o[d] += n[d];
-    }
-  if (o[2] != 0) return o[2] > 0;
-  if (o[1] != 0) return o[1] > 0;
-  if (o[0] != 0) return o[0] > 0;
-  return orig_w > orig_f;
-}
 
 template <int DIM>
 PSPH_D void tensile_tir(const double* S, double TI, double rho, double* TIR) {
@@ -149,84 +83,7 @@ PSPH_D void tensile_tir(const double* S, double TI, double rho, double* TIR) {
       for (int c = 0; c < 3; ++c) TIR[3 * r + c] = Q[3 * r + 0] * val[0] * Q[3 * c + 0] + Q[3 * r + 1] * val[1] * Q[3 * c + 1] + Q[3 * r + 2] * val[2] * Q[3 * c + 2];
   }
 }
-// ---------------------------------------------------------------------------
-// Candidate stream: the sorted index ranges of the 3 (2D) or 9 (3D) cell rows
-// around a cell, one row split into its 3 cells where the periodic x axis wraps.
-// Each lane walks its own stream; candidates that pass a conservative FP32
-// distance test are queued in shared memory and evaluated in FP64 by all lanes
-// of the warp together, so the FP64 work runs with (nearly) full warps instead
-// of the ~1/3 occupancy a per-candidate branch gives.
-// ---------------------------------------------------------------------------
-template <int DIM>
-struct Cands {
-  static constexpr int NR = (DIM == 3 ? 9 : 3) * 3;
-  int cx, cy, cz, r, j, jend;
-  bool wrapx;
-  PSPH_D void init(const GridDev& g, int cell) {
-    j = jend = 0;
-    if (cell < 0) {
-      r = NR;
-      cx = cy = cz = 0;
-      wrapx = false;
-      return;
-    }
-    const CellCoord c = decode(g, cell);
-    cx = c.x;
-    cy = c.y;
-    cz = c.z;
-    r = 0;
-    wrapx = g.periodic[0] && (cx == 0 || cx == g.nc[0] - 1);
-  }
-  PSPH_D bool range(const GridDev& g, const int* __restrict__ start, int rr, int& lo, int& hi) const {
-    const int row = rr / 3, sub = rr - 3 * row;
-    const int dz = (DIM == 3) ? row / 3 - 1 : 0;
-    const int dy = row % 3 - 1;
-    int z = cz + dz, y = cy + dy;
-    if (g.periodic[2]) z = (z + g.nc[2]) % g.nc[2];
-    else if (z < 0 || z >= g.nc[2]) return false;
-    if (g.periodic[1]) y = (y + g.nc[1]) % g.nc[1];
-    else if (y < 0 || y >= g.nc[1]) return false;
-    const int base = (z * g.nc[1] + y) * g.nc[0];
-    if (!wrapx) {
-      if (sub) return false;
-      const int x0 = max(cx - 1, 0), x1 = min(cx + 1, g.nc[0] - 1);
-      lo = start[base + x0];
-      hi = start[base + x1 + 1];
-    } else {
-      const int x = (cx + sub - 1 + g.nc[0]) % g.nc[0];
-      lo = start[base + x];
-      hi = start[base + x + 1];
-    }
-    return lo < hi;
-  }
-  PSPH_D int next(const GridDev& g, const int* __restrict__ start) {
-    while (j >= jend) {
-      if (r >= NR) return -1;
-      int lo, hi;
-      if (range(g, start, r++, lo, hi)) {
-        j = lo;
-        jend = hi;
-      }
-    }
-    return j++;
-  }
-};
-
 constexpr int kQN = 16;  // queued FP64 pair evaluations per lane between flushes
-
-// Conservative FP32 support test; the exact FP64 test follows for survivors.
-template <int DIM>
-PSPH_D bool near_f32(const GridDev& g, const float4& xi, const float4& xj, float cf) {
-  float d[3] = {xi.x - xj.x, xi.y - xj.y, DIM == 3 ? xi.z - xj.z : 0.0f};
-  const float hb = 0.5f * (xi.w + xj.w);
-  const float lim = 2.0f * cf * hb;
-#pragma unroll
-  for (int a = 0; a < DIM; ++a)
-    if (g.periodic[a] && fabsf(d[a]) > lim) d[a] -= copysignf((float)g.dom_size[a], d[a]);
-  const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-  const float s = cf * hb;
-  return r2 <= s * s * 1.004f;
-}
 
 // ---------------------------------------------------------------------------
 // Per-particle preparation and wall interpolation
@@ -250,7 +107,6 @@ __global__ void __launch_bounds__(kFT) prepare_wall_kernel(DevView v) {
 #pragma unroll
   for (int e = 0; e < 9; ++e) sig[e] = 0.0;
   double4_32a xw = make_double4_32a(0, 0, 0, 0);
-  float4 xw32 = make_float4(0.f, 0.f, 0.f, 0.f);
   int ow = 0, cell = -1;
   double hw = 0.0;
   bool noslip = false;
@@ -267,7 +123,6 @@ __global__ void __launch_bounds__(kFT) prepare_wall_kernel(DevView v) {
       wall = true;
       mat = Cw.material;
       xw = P.X4[w];
-      xw32 = v.S.X32[w];
       ow = P.orig[w];
       cell = v.S.cellid[w];
       hw = Cw.h;
@@ -276,35 +131,35 @@ __global__ void __launch_bounds__(kFT) prepare_wall_kernel(DevView v) {
   }
   // Wall interpolation (FSMPairs only: free partners of the same material).
   const bool any_periodic = g.periodic[0] | g.periodic[1] | g.periodic[2];
-  const float cff = (float)g.cellfac;
   const double gx = o.gravity[0], gy = o.gravity[1], gz = o.gravity[2];
   const bool need_orient = !o.wallp_physical && (gx != 0.0 || gy != 0.0 || gz != 0.0) && mat < 3;
-  Cands<DIM> cs;
-  cs.init(g, wall ? cell : -1);
+  NbrSource<DIM> src;
+  src.init(v, w, wall && cell >= 0, 1.004f);
   bool more = wall && cell >= 0;
   const CellCoord cw = decode(g, cell >= 0 ? cell : 0);
   while (true) {
     int qn = 0;
     while (more && qn < kQN) {
-      const int f = cs.next(g, v.S.start);
+      int code;
+      const int f = src.next(v, &code);
       if (f < 0) {
         more = false;
         break;
       }
-      if (f == w) continue;
-      if (near_f32<DIM>(g, xw32, v.S.X32[f], cff)) qbuf[qn++][tid] = f;
+      qbuf[qn++][tid] = f | (code << kCodeShift);
     }
     const int qmax = __reduce_max_sync(0xffffffffu, qn);
     for (int k = 0; k < qmax; ++k) {
       if (k >= qn) continue;
-      const int f = qbuf[k][tid];
+      const int fe = qbuf[k][tid];
+      const int f = fe & kIndexMask, fcode = fe >> kCodeShift;
       const PClass& Cf = CT[P.cls[f]];
       if (!Cf.is_free || Cf.material != mat) continue;
       const double4_32a xf = P.X4[f];
       const double hb = (hw + Cf.h) / 2.0;
       CellCoord cf = cw;
-      if (any_periodic || need_orient) cf = decode(g, v.S.cellid[f]);
-      const bool wfirst = need_orient ? first_of_pair(g, cw, cf, ow, P.orig[f]) : true;
+      if (any_periodic) cf = decode(g, v.S.cellid[f]);
+      const bool wfirst = need_orient ? first_of_pair_code(fcode, ow, P.orig[f]) : true;
       double x0, x1, x2;
       if (wfirst) {
         x0 = xw.x - xf.x; x1 = xw.y - xf.y; x2 = xw.z - xf.z;
@@ -410,7 +265,6 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
   const double4_32a xi = active ? P.X4[i] : make_double4_32a(0, 0, 0, 1);
   const double4_32a vi = active ? P.V4[i] : make_double4_32a(0, 0, 0, 0);
   const double4_32a di4 = active ? v.S.D4[i] : make_double4_32a(1, 0, 0, 1);
-  const float4 xi32 = active ? v.S.X32[i] : make_float4(0.f, 0.f, 0.f, 0.f);
   const double di = xi.w, inv_i = di4.x, Pi = di4.y, ci_snd = di4.z, pi = vi.w;
   const double mi = Ci.mass, hi = Ci.h;
   const double mui = o.dyn_mu ? (active ? P.mu[i] : 0.0) : Ci.mu0;
@@ -421,21 +275,20 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
   double drho = 0.0, zw = 0.0, sd = 0.0, xs0 = 0.0, xs1 = 0.0, xs2 = 0.0;
   double sr0 = 0.0, sr1 = 0.0, sr2 = 0.0, sr4 = 0.0, sr5 = 0.0, sr8 = 0.0;
   const bool any_periodic = g.periodic[0] | g.periodic[1] | g.periodic[2];
-  const float cff = (float)g.cellfac;
   CellCoord cci = decode(g, cell >= 0 ? cell : 0);
-  Cands<DIM> cs;
-  cs.init(g, active ? cell : -1);
+  NbrSource<DIM> src;
+  src.init(v, i, active && cell >= 0, 1.004f);
   bool more = active && cell >= 0;
   while (true) {
     int qn = 0;
     while (more && qn < kQN) {
-      const int j = cs.next(g, v.S.start);
+      int code;
+      const int j = src.next(v, &code);
       if (j < 0) {
         more = false;
         break;
       }
-      if (j == i) continue;
-      if (near_f32<DIM>(g, xi32, v.S.X32[j], cff)) qbuf[qn++][tid] = j;
+      qbuf[qn++][tid] = j;
     }
     const int qmax = __reduce_max_sync(0xffffffffu, qn);
     for (int k = 0; k < qmax; ++k) {
@@ -628,7 +481,6 @@ __global__ void __launch_bounds__(kFT) forces_solid_kernel(DevView v) {
   const double4_32a xi = P.X4[is];
   const double4_32a vi = P.V4[is];
   const double4_32a di4 = v.S.D4[is];
-  const float4 xi32 = v.S.X32[is];
   const double di = xi.w, inv_i = di4.x, mi = Ci.mass, hi = Ci.h;
   const bool shep = Ci.shepard && (sc->shepard_counter == o.shepard_step);
   const double* __restrict__ Si = P.sigma + 9 * (size_t)is;
@@ -639,21 +491,20 @@ __global__ void __launch_bounds__(kFT) forces_solid_kernel(DevView v) {
   double sr[6] = {0, 0, 0, 0, 0, 0}, rr[3] = {0, 0, 0};  // sr: 00 01 02 11 12 22; rr: 01 02 12
   const bool any_periodic = g.periodic[0] | g.periodic[1] | g.periodic[2];
   const double I22 = (DIM == 2) ? 0.0 : 1.0;  // Domain::I (Source/Domain.cpp:1665)
-  const float cff = (float)g.cellfac;
   CellCoord cci = decode(g, cell >= 0 ? cell : 0);
-  Cands<DIM> cs;
-  cs.init(g, active ? cell : -1);
+  NbrSource<DIM> src;
+  src.init(v, i, active && cell >= 0, 1.004f);
   bool more = active && cell >= 0;
   while (true) {
     int qn = 0;
     while (more && qn < kQN) {
-      const int j = cs.next(g, v.S.start);
+      int code;
+      const int j = src.next(v, &code);
       if (j < 0) {
         more = false;
         break;
       }
-      if (j == i) continue;
-      if (near_f32<DIM>(g, xi32, v.S.X32[j], cff)) qbuf[qn++][tid] = j;
+      qbuf[qn++][tid] = j;
     }
     const int qmax = __reduce_max_sync(0xffffffffu, qn);
     for (int k = 0; k < qmax; ++k) {

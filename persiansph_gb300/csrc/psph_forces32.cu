@@ -13,14 +13,14 @@
 //    (psph_update.cu, dt_finalize_kernel).
 #include <cfloat>
 
-#include "psph_device.cuh"
+#include "psph_pairs.cuh"
 
 namespace psph {
 
 namespace {
 
 constexpr int kFT32 = 128;
-constexpr int kQ32 = 16;
+constexpr int kQ32 = 16;  // queued wall-interpolation partners per lane
 
 struct Kahan {
   float s = 0.f, c = 0.f;
@@ -108,89 +108,6 @@ struct KernF {
   }
 };
 
-struct CellC {
-  int x, y, z;
-};
-
-PSPH_D CellC decode32(const GridDev& g, int c) {
-  CellC r;
-  r.x = c % g.nc[0];
-  const int t = c / g.nc[0];
-  r.y = t % g.nc[1];
-  r.z = t / g.nc[1];
-  return r;
-}
-
-// Candidate stream that also reports each candidate's cell offset relative to
-// the home cell (wrapped on periodic axes), packed with the index.
-template <int DIM>
-struct Cands32 {
-  static constexpr int NR = (DIM == 3 ? 9 : 3) * 3;
-  int cx, cy, cz, r, j, jend, base, code_yz, sub;
-  bool wrapx;
-  PSPH_D void init(const GridDev& g, int cell) {
-    j = jend = 0;
-    if (cell < 0) {
-      r = NR;
-      return;
-    }
-    const CellC c = decode32(g, cell);
-    cx = c.x;
-    cy = c.y;
-    cz = c.z;
-    r = 0;
-    wrapx = g.periodic[0] && (cx == 0 || cx == g.nc[0] - 1);
-  }
-  PSPH_D bool range(const GridDev& g, const int* __restrict__ start, int rr, int& lo, int& hi) {
-    const int row = rr / 3;
-    sub = rr - 3 * row;
-    const int dz = (DIM == 3) ? row / 3 - 1 : 0;
-    const int dy = row % 3 - 1;
-    int z = cz + dz, y = cy + dy;
-    if (g.periodic[2]) z = (z + g.nc[2]) % g.nc[2];
-    else if (z < 0 || z >= g.nc[2]) return false;
-    if (g.periodic[1]) y = (y + g.nc[1]) % g.nc[1];
-    else if (y < 0 || y >= g.nc[1]) return false;
-    base = (z * g.nc[1] + y) * g.nc[0];
-    code_yz = 3 * (dy + 1) + 9 * (dz + 1);
-    if (!wrapx) {
-      if (sub) return false;
-      const int x0 = max(cx - 1, 0), x1 = min(cx + 1, g.nc[0] - 1);
-      lo = start[base + x0];
-      hi = start[base + x1 + 1];
-    } else {
-      const int x = (cx + sub - 1 + g.nc[0]) % g.nc[0];
-      lo = start[base + x];
-      hi = start[base + x + 1];
-    }
-    return lo < hi;
-  }
-  // next candidate index, its cell offset code (dx+1) + 3(dy+1) + 9(dz+1) in *code
-  PSPH_D int next(const GridDev& g, const int* __restrict__ start, const int* __restrict__ cellid, int* code) {
-    while (j >= jend) {
-      if (r >= NR) return -1;
-      int lo, hi;
-      if (range(g, start, r++, lo, hi)) {
-        j = lo;
-        jend = hi;
-      }
-    }
-    const int jj = j++;
-    const int dxj = wrapx ? (sub - 1) : (cellid[jj] - base - cx);  // candidate cell x minus home cell x
-    *code = (dxj + 1) + code_yz;
-    return jj;
-  }
-};
-
-// relative position x_i - x_j from the cell offset code and FP32 offsets
-template <int DIM>
-PSPH_D void rel_pos(const float3& cs, const float4& oi, const float4& oj, int code, float& x0, float& x1, float& x2) {
-  const int dxc = code % 3 - 1, dyc = (code / 3) % 3 - 1, dzc = code / 9 - 1;
-  x0 = -(float)dxc * cs.x + (oi.x - oj.x);
-  x1 = -(float)dyc * cs.y + (oi.y - oj.y);
-  x2 = (DIM == 3) ? -(float)dzc * cs.z + (oi.z - oj.z) : 0.f;
-}
-
 // ---------------------------------------------------------------------------
 // Preparation (FP32 copies, partner-visible wall state) and wall interpolation
 // ---------------------------------------------------------------------------
@@ -201,29 +118,15 @@ __global__ void __launch_bounds__(kFT32) copies32_kernel(DevView v) {
   const Persist& P = cur_persist(v);
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
   if (w >= sc->n) return;
-  const GridDev& g = v.g;
-  const PClass& C = v.cls[P.cls[w]];
-  const double4_32a x = P.X4[w];
-  const int cell = v.S.cellid[w];
-  float4 oi;
-  // FP32 offset from the cell origin (a particle outside any cell keeps its absolute position)
-  if (cell >= 0) {
-    const CellC c = decode32(g, cell);
-    oi = make_float4((float)(x.x - (g.blpf[0] + c.x * g.cell_size[0])),
-                     (float)(x.y - (g.blpf[1] + c.y * g.cell_size[1])),
-                     (float)(DIM == 3 ? x.z - (g.blpf[2] + c.z * g.cell_size[2]) : 0.0), (float)C.h);
-  } else {
-    oi = make_float4((float)x.x, (float)x.y, (float)x.z, (float)C.h);
-  }
-  v.S.OFF32[w] = oi;
+  const PClass32& C = v.cls32[P.cls[w]];
   const double4_32a vv = P.V4[w];
   const float p = (float)vv.w;
   v.S.V32[w] = make_float4((float)vv.x, (float)vv.y, (float)vv.z, p);
-  if (C.is_free) {
-    const float rho = (float)x.w;
+  if (C.flags & CF_FREE) {
+    const float rho = (float)P.X4[w].w;
     const float inv = 1.f / rho;
-    const float ratio = rho / (float)C.rho0;
-    const float c = (C.pres_eq == 1) ? (float)C.cs * ratio * ratio * ratio : (float)C.cs;
+    const float ratio = rho / C.rho0;
+    const float c = (C.pres_eq == 1) ? C.cs * ratio * ratio * ratio : C.cs;
     v.S.D32[w] = make_float4(inv, p * inv * inv, c, rho);
   }
 }
@@ -239,63 +142,52 @@ __global__ void __launch_bounds__(kFT32) prepare32_kernel(DevView v) {
   const int tid = threadIdx.x;
   const GridDev& g = v.g;
   const Options& o = v.o;
-  const PClass* __restrict__ CT = v.cls;
+  const PClass32* __restrict__ CT = v.cls32;
   bool wall = false, noslip = false;
-  int cell = -1, ow = 0;
+  int cell = -1, ow = 0, mat = 0;
   float4 oi = make_float4(0.f, 0.f, 0.f, 0.f);
   if (w < n) {
-    const PClass& C = CT[P.cls[w]];
-    if (!C.is_free) {
+    const PClass32& C = CT[P.cls[w]];
+    if (!(C.flags & CF_FREE)) {
       wall = true;
-      noslip = C.no_slip;
+      noslip = C.flags & CF_NOSLIP;
+      mat = C.material;
       ow = P.orig[w];
       cell = v.S.cellid[w];
       oi = v.S.OFF32[w];
     }
   }
-  const float3 cs = make_float3((float)g.cell_size[0], (float)g.cell_size[1], (float)g.cell_size[2]);
-  const float cf = (float)g.cellfac;
+  const float3 cs = cell_size_f(g);
   const float gx = (float)o.gravity[0], gy = (float)o.gravity[1], gz = (float)o.gravity[2];
   const bool need_orient = !o.wallp_physical && (gx != 0.f || gy != 0.f || gz != 0.f);
   float sk = 0.f, p = 0.f, n0 = 0.f, n1 = 0.f, n2 = 0.f;
-  Cands32<DIM> cands;
-  cands.init(g, wall ? cell : -1);
+  NbrSource<DIM> src;
+  src.init(v, w, wall && cell >= 0, 1.0f);
   bool more = wall && cell >= 0;
-  const CellC cw = decode32(g, cell >= 0 ? cell : 0);
-  const int mat = (w < n) ? CT[P.cls[w]].material : 0;
   const float hw = oi.w;
   while (true) {
     int qn = 0;
     while (more && qn < kQ32) {
       int code;
-      const int f = cands.next(g, v.S.start, v.S.cellid, &code);
+      const int f = src.next(v, &code);
       if (f < 0) {
         more = false;
         break;
       }
-      if (f == w) continue;
-      float x0, x1, x2;
-      const float4 of = v.S.OFF32[f];
-      rel_pos<DIM>(cs, oi, of, code, x0, x1, x2);
-      const float hb = 0.5f * (hw + of.w);
-      if (x0 * x0 + x1 * x1 + x2 * x2 <= cf * cf * hb * hb) qbuf[qn++][tid] = f | (code << 26);
+      qbuf[qn++][tid] = f | (code << kCodeShift);
     }
     const int qmax = __reduce_max_sync(0xffffffffu, qn);
     for (int k = 0; k < qmax; ++k) {
       if (k >= qn) continue;
       const int e = qbuf[k][tid];
-      const int f = e & ((1 << 26) - 1), code = e >> 26;
-      const PClass& Cf = CT[P.cls[f]];
-      if (!Cf.is_free || Cf.material != mat) continue;
+      const int f = e & kIndexMask, code = e >> kCodeShift;
+      const PClass32& Cf = CT[P.cls[f]];
+      if (!(Cf.flags & CF_FREE) || Cf.material != mat) continue;
       const float4 of = v.S.OFF32[f];
       float x0, x1, x2;
       rel_pos<DIM>(cs, oi, of, code, x0, x1, x2);  // x_wall - x_fluid
-      if (need_orient) {
-        const int dxc = code % 3 - 1, dyc = (code / 3) % 3 - 1, dzc = code / 9 - 1;
-        const bool same = (dxc == 0 && dyc == 0 && dzc == 0);
-        const bool fwd = (dzc != 0) ? dzc > 0 : (dyc != 0) ? dyc > 0 : dxc > 0;
-        const bool wfirst = same ? (ow > P.orig[f]) : fwd;  // first_of_pair
-        if (!wfirst) { x0 = -x0; x1 = -x1; x2 = -x2; }
+      if (need_orient && !first_of_pair_code(code, ow, P.orig[f])) {
+        x0 = -x0; x1 = -x1; x2 = -x2;
       }
       const float hb = 0.5f * (hw + of.w);
       const float ih = 1.f / hb;
@@ -323,29 +215,28 @@ __global__ void __launch_bounds__(kFT32) prepare32_kernel(DevView v) {
   v.S.sumkernel[w] = sk;
   v.S.nsv4[w] = make_double4_32a(n0, n1, n2, 0.0);
   v.S.V32[w] = make_float4((float)vw.x, (float)vw.y, (float)vw.z, p);
-  const PClass& Ce = CT[o.eos_cls];
+  const PClass32& Ce = CT[o.eos_cls];
   float rw = (float)P.X4[w].w, cwv = 0.f;
   if (o.uniform_eos) {
     // DensitySolid / SoundSpeed of the fluid's EOS (Source/Functions.cpp:214-264), FP32
-    const float cs2 = (float)Ce.cs * (float)Ce.cs, r0 = (float)Ce.rho0, p0 = (float)Ce.p0;
+    const float cs2 = Ce.cs * Ce.cs, r0 = Ce.rho0, p0 = Ce.p0;
     if (Ce.pres_eq == 0) rw = (p - p0) / cs2 + r0;
     else if (Ce.pres_eq == 1) rw = powf((p - p0) * (7.f / (r0 * cs2)) + 1.f, 1.f / 7.f) * r0;
     else rw = p / cs2;
     const float ratio = rw / r0;
-    cwv = (Ce.pres_eq == 1) ? (float)Ce.cs * ratio * ratio * ratio : (float)Ce.cs;
+    cwv = (Ce.pres_eq == 1) ? Ce.cs * ratio * ratio * ratio : Ce.cs;
   }
   const float inv = 1.f / rw;
   v.S.D32[w] = make_float4(inv, p * inv * inv, cwv, rw);
 }
 
 // ---------------------------------------------------------------------------
-// Fluid pair force, FP32 with compensated sums
+// Fluid pair force, FP32 with compensated sums, over the neighbour lists
 // ---------------------------------------------------------------------------
 template <int DIM, int KT>
 __global__ void __launch_bounds__(kFT32) forces_fluid32_kernel(DevView v) {
   __shared__ double red[kFT32 / 32];
   __shared__ unsigned long long cred[kFT32 / 32];
-  __shared__ int qbuf[kQ32][kFT32];
   const StepScalars* sc = v.sc;
   if (sc->stop) return;
   const Persist& P = cur_persist(v);
@@ -354,158 +245,143 @@ __global__ void __launch_bounds__(kFT32) forces_fluid32_kernel(DevView v) {
   const int tid = threadIdx.x;
   const GridDev& g = v.g;
   const Options& o = v.o;
-  const PClass* __restrict__ CT = v.cls;
+  const PClass32* __restrict__ CT = v.cls32;
   double dtc = DBL_MAX;
   unsigned long long npair2 = 0;
   bool active = false;
   int cell = -1, ci_cls = 0;
   if (i < n) {
     ci_cls = P.cls[i];
-    active = CT[ci_cls].is_free;
+    active = CT[ci_cls].flags & CF_FREE;
     cell = v.S.cellid[i];
     if (!active) {
       v.S.A4[i] = make_double4_32a(o.gravity[0], o.gravity[1], o.gravity[2], 0.0);
       v.S.zwab[i] = 1.0;
     }
   }
-  const PClass& Ci = CT[ci_cls];
+  const PClass32& Ci = CT[ci_cls];
   const int is = active ? i : 0;
   const float4 oi = v.S.OFF32[is];
   const float4 vi = v.S.V32[is];
   const float4 di4 = v.S.D32[is];
   const float di = di4.w, inv_i = di4.x, Pi = di4.y, ci_snd = di4.z, pi = vi.w;
-  const float mi = (float)Ci.mass, hi = oi.w;
-  const float mui = o.dyn_mu ? (float)P.mu[is] : (float)Ci.mu0;
-  const bool shep = Ci.shepard && (sc->shepard_counter == o.shepard_step);
-  const bool sr_self = (Ci.t0 > 0.0 || Ci.les);
-  const float3 cs = make_float3((float)g.cell_size[0], (float)g.cell_size[1], (float)g.cell_size[2]);
-  const float cf = (float)g.cellfac;
-  const float ci_alpha = (float)Ci.alpha, ci_beta = (float)Ci.beta;
+  const float mi = Ci.mass, hi = oi.w;
+  const float mui = o.dyn_mu ? (float)P.mu[is] : Ci.mu0;
+  const int fi = Ci.flags;
+  const bool shep = (fi & CF_SHEPARD) && (sc->shepard_counter == o.shepard_step);
+  const bool sr_self = fi & (CF_T0 | CF_LES);
+  const bool use_sr = o.need_sr;
+  const bool xsph_on = o.xsph != 0.0;
+  const float xsph = (float)o.xsph;
+  const float3 cs = cell_size_f(g);
   const float mu_u = (float)o.mu_u;
+  const bool uniform_mu = o.uniform_mu, dyn_mu = o.dyn_mu;
+  const int vis_eq = o.vis_eq, grad_type = o.grad_type;
   Kahan ax, ay, az, dr;
   float zw = 0.f, sd = 0.f, xs0 = 0.f, xs1 = 0.f, xs2 = 0.f;
   float sr0 = 0.f, sr1 = 0.f, sr2 = 0.f, sr4 = 0.f, sr5 = 0.f, sr8 = 0.f;
-  Cands32<DIM> cands;
-  cands.init(g, active ? cell : -1);
-  bool more = active && cell >= 0;
+  NbrSource<DIM> src;
+  src.init(v, i, active && cell >= 0, 1.0f);
   while (true) {
-    int qn = 0;
-    while (more && qn < kQ32) {
-      int code;
-      const int j = cands.next(g, v.S.start, v.S.cellid, &code);
-      if (j < 0) {
-        more = false;
-        break;
-      }
-      if (j == i) continue;
-      const float4 oj = v.S.OFF32[j];
-      float x0, x1, x2;
-      rel_pos<DIM>(cs, oi, oj, code, x0, x1, x2);
-      const float hb = 0.5f * (hi + oj.w);
-      if (x0 * x0 + x1 * x1 + x2 * x2 <= cf * cf * hb * hb) qbuf[qn++][tid] = j | (code << 26);
+    int code;
+    const int j = src.next(v, &code);
+    if (j < 0) break;
+    const float4 oj = v.S.OFF32[j];
+    float x0, x1, x2;
+    rel_pos<DIM>(cs, oi, oj, code, x0, x1, x2);
+    const PClass32& Cj = CT[P.cls[j]];
+    const int fjf = Cj.flags;
+    const bool fj = fjf & CF_FREE;
+    npair2 += fj ? 1ull : 2ull;
+    const float hb = 0.5f * (hi + oj.w);
+    const float ih = 1.f / hb;
+    const float r2 = x0 * x0 + x1 * x1 + x2 * x2;
+    const float inv_r = (r2 > 0.f) ? rsqrtf(r2) : 0.f;
+    const float q = r2 * inv_r * ih;
+    const float inv_q = hb * inv_r;
+    const float ih2 = ih * ih;
+    const float cwh = KernF<DIM, KT>::cw() * (DIM == 2 ? ih2 : ih2 * ih);
+    const float cwg = cwh * ih2;
+    const float GK = KernF<DIM, KT>::GK(q, inv_q, cwg);
+    const float K = KernF<DIM, KT>::W(q, cwh);
+    const float4 vj = v.S.V32[j];
+    const float4 dj4 = v.S.D32[j];
+    const float dj = dj4.w, inv_j = dj4.x, Pj = dj4.y, cj_snd = dj4.z, pj = vj.w;
+    const float mj = fj ? Cj.mass : Cj.fpmassc * mi;
+    const float v0 = vi.x - vj.x, v1 = vi.y - vj.y, v2 = vi.z - vj.z;
+    const float vx = v0 * x0 + v1 * x1 + v2 * x2;
+    float PI = 0.f;
+    const float Alpha = 0.5f * (Ci.alpha + Cj.alpha), Beta = 0.5f * (Ci.beta + Cj.beta);
+    if ((Alpha != 0.f || Beta != 0.f) && vx < 0.f) {
+      const float D = r2 + 0.01f * hb * hb;
+      const float t = hb * vx;
+      PI = t * (-Alpha * 0.5f * (ci_snd + cj_snd) * D + Beta * t) / (D * D * (0.5f * (di + dj)));
     }
-    const int qmax = __reduce_max_sync(0xffffffffu, qn);
-    for (int k = 0; k < qmax; ++k) {
-      if (k >= qn) continue;
-      const int e = qbuf[k][tid];
-      const int j = e & ((1 << 26) - 1), code = e >> 26;
-      const float4 oj = v.S.OFF32[j];
-      float x0, x1, x2;
-      rel_pos<DIM>(cs, oi, oj, code, x0, x1, x2);
-      const PClass& Cj = CT[P.cls[j]];
-      const bool fj = Cj.is_free;
-      npair2 += fj ? 1ull : 2ull;
-      const float hb = 0.5f * (hi + oj.w);
-      const float ih = 1.f / hb;
-      const float r2 = x0 * x0 + x1 * x1 + x2 * x2;
-      const float inv_r = (r2 > 0.f) ? rsqrtf(r2) : 0.f;
-      const float q = r2 * inv_r * ih;
-      const float inv_q = hb * inv_r;
-      const float ih2 = ih * ih;
-      const float cwh = KernF<DIM, KT>::cw() * (DIM == 2 ? ih2 : ih2 * ih);
-      const float cwg = cwh * ih2;
-      const float GK = KernF<DIM, KT>::GK(q, inv_q, cwg);
-      const float K = KernF<DIM, KT>::W(q, cwh);
-      const float4 vj = v.S.V32[j];
-      const float4 dj4 = v.S.D32[j];
-      const float dj = dj4.w, inv_j = dj4.x, Pj = dj4.y, cj_snd = dj4.z, pj = vj.w;
-      const float mj = fj ? (float)Cj.mass : (float)Cj.fpmassc * mi;
-      const float v0 = vi.x - vj.x, v1 = vi.y - vj.y, v2 = vi.z - vj.z;
-      const float vx = v0 * x0 + v1 * x1 + v2 * x2;
-      float PI = 0.f;
-      const float Alpha = 0.5f * (ci_alpha + (float)Cj.alpha), Beta = 0.5f * (ci_beta + (float)Cj.beta);
-      if ((Alpha != 0.f || Beta != 0.f) && vx < 0.f) {
-        const float D = r2 + 0.01f * hb * hb;
-        const float t = hb * vx;
-        PI = t * (-Alpha * 0.5f * (ci_snd + cj_snd) * D + Beta * t) / (D * D * (0.5f * (di + dj)));
+    float TI = 0.f;
+    if ((fi | fjf) & CF_TI) {
+      float Ri = 0.f, Rj = 0.f;
+      if ((pi + pj) < 0.f) {
+        if (pi < 0.f) Ri = -pi * inv_i * inv_i;
+        if (pj < 0.f) Rj = -pj * inv_j * inv_j;
       }
-      float TI = 0.f;
-      if (Ci.ti > 0.0 || Cj.ti > 0.0) {
-        float Ri = 0.f, Rj = 0.f;
-        if ((pi + pj) < 0.f) {
-          if (pi < 0.f) Ri = -pi * inv_i * inv_i;
-          if (pj < 0.f) Rj = -pj * inv_j * inv_j;
-        }
-        const float Wd = KernF<DIM, KT>::W((float)(Ci.tid + Cj.tid) * 0.5f * ih, cwh);
-        TI = ((float)Ci.ti * Ri + (float)Cj.ti * Rj) * powf(K / Wd, (float)(Ci.tin + Cj.tin) * 0.5f);
-      }
-      float VI0 = 0.f, VI1 = 0.f, VI2 = 0.f;
-      if ((Ci.no_slip || Cj.no_slip) || fj) {
-        float Mu, vab0, vab1, vab2;
-        if (fj) {
-          vab0 = v0; vab1 = v1; vab2 = v2;
-          if (o.uniform_mu) Mu = mu_u;
-          else {
-            const float muj = o.dyn_mu ? (float)P.mu[j] : (float)Cj.mu0;
-            Mu = 2.f * mui * muj / (mui + muj);
-          }
-        } else {
-          const double4_32a ns = v.S.nsv4[j];
-          vab0 = vi.x - (2.f * vj.x - (float)ns.x);
-          vab1 = vi.y - (2.f * vj.y - (float)ns.y);
-          vab2 = vi.z - (2.f * vj.z - (float)ns.z);
-          Mu = mui;
-        }
-        if (o.vis_eq <= 2) {
-          float c;
-          if (o.vis_eq == 0) c = 2.f * Mu * inv_i * inv_j * GK;
-          else if (o.vis_eq == 1) c = 8.f * Mu / ((di + dj) * (di + dj)) * GK;
-          else c = -Mu * inv_i * inv_j * KernF<DIM, KT>::Lap(q, inv_q, cwg);
-          VI0 = c * vab0; VI1 = c * vab1; VI2 = c * vab2;
-        } else {
-          const float L = KernF<DIM, KT>::Lap(q, inv_q, cwg);
-          const float S2 = KernF<DIM, KT>::D2(q, cwg);
-          const float s = -Mu * inv_i * inv_j;
-          const float t = vx / r2 * (-GK + S2);
-          VI0 = s * (L * vab0 + (1.f / 3.f) * (GK * v0 + t * x0));
-          VI1 = s * (L * vab1 + (1.f / 3.f) * (GK * v1 + t * x1));
-          VI2 = s * (L * vab2 + (1.f / 3.f) * (GK * v2 + t * x2));
-        }
-        if (sr_self && (Ci.t0 > 0.0 || Cj.t0 > 0.0 || (Ci.les && Cj.les))) {
-          const float c2 = -GK * (mj * inv_j);
-          sr0 += c2 * (2.f * vab0 * x0);
-          sr1 += c2 * (vab0 * x1 + vab1 * x0);
-          sr2 += c2 * (vab0 * x2 + vab2 * x0);
-          sr4 += c2 * (2.f * vab1 * x1);
-          sr5 += c2 * (vab1 * x2 + vab2 * x1);
-          sr8 += c2 * (2.f * vab2 * x2);
-        }
-      }
-      if (o.xsph != 0.0 && fj) {
-        const float s = (float)o.xsph * mj / (0.5f * (di + dj)) * K;
-        xs0 -= s * v0; xs1 -= s * v1; xs2 -= s * v2;
-      }
-      float s;
-      if (o.grad_type == 0) s = -(Pi + Pj + PI + TI) * GK;
-      else s = -((pi + pj) * inv_i * inv_j + PI + TI) * GK;
-      ax.add(mj * (s * x0 + VI0));
-      ay.add(mj * (s * x1 + VI1));
-      if (DIM == 3) az.add(mj * (s * x2 + VI2));
-      dr.add(mj * di * inv_j * (GK * vx));
-      zw += mj * inv_j * K;
-      if (shep) sd += mj * K;
+      const float Wd = KernF<DIM, KT>::W((Ci.tid + Cj.tid) * 0.5f * ih, cwh);
+      TI = (Ci.ti * Ri + Cj.ti * Rj) * powf(K / Wd, (Ci.tin + Cj.tin) * 0.5f);
     }
-    if (!__any_sync(0xffffffffu, more)) break;
+    float VI0 = 0.f, VI1 = 0.f, VI2 = 0.f;
+    if (((fi | fjf) & CF_NOSLIP) || fj) {
+      float Mu, vab0, vab1, vab2;
+      if (fj) {
+        vab0 = v0; vab1 = v1; vab2 = v2;
+        if (uniform_mu) Mu = mu_u;
+        else {
+          const float muj = dyn_mu ? (float)P.mu[j] : Cj.mu0;
+          Mu = 2.f * mui * muj / (mui + muj);
+        }
+      } else {
+        const double4_32a ns = v.S.nsv4[j];
+        vab0 = vi.x - (2.f * vj.x - (float)ns.x);
+        vab1 = vi.y - (2.f * vj.y - (float)ns.y);
+        vab2 = vi.z - (2.f * vj.z - (float)ns.z);
+        Mu = mui;
+      }
+      if (vis_eq <= 2) {
+        float c;
+        if (vis_eq == 0) c = 2.f * Mu * inv_i * inv_j * GK;
+        else if (vis_eq == 1) c = 8.f * Mu / ((di + dj) * (di + dj)) * GK;
+        else c = -Mu * inv_i * inv_j * KernF<DIM, KT>::Lap(q, inv_q, cwg);
+        VI0 = c * vab0; VI1 = c * vab1; VI2 = c * vab2;
+      } else {
+        const float L = KernF<DIM, KT>::Lap(q, inv_q, cwg);
+        const float S2 = KernF<DIM, KT>::D2(q, cwg);
+        const float s = -Mu * inv_i * inv_j;
+        const float t = vx / r2 * (-GK + S2);
+        VI0 = s * (L * vab0 + (1.f / 3.f) * (GK * v0 + t * x0));
+        VI1 = s * (L * vab1 + (1.f / 3.f) * (GK * v1 + t * x1));
+        VI2 = s * (L * vab2 + (1.f / 3.f) * (GK * v2 + t * x2));
+      }
+      if (use_sr && sr_self && (((fi | fjf) & CF_T0) || ((fi & fjf) & CF_LES))) {
+        const float c2 = -GK * (mj * inv_j);
+        sr0 += c2 * (2.f * vab0 * x0);
+        sr1 += c2 * (vab0 * x1 + vab1 * x0);
+        sr2 += c2 * (vab0 * x2 + vab2 * x0);
+        sr4 += c2 * (2.f * vab1 * x1);
+        sr5 += c2 * (vab1 * x2 + vab2 * x1);
+        sr8 += c2 * (2.f * vab2 * x2);
+      }
+    }
+    if (xsph_on && fj) {
+      const float s = xsph * mj / (0.5f * (di + dj)) * K;
+      xs0 -= s * v0; xs1 -= s * v1; xs2 -= s * v2;
+    }
+    float s;
+    if (grad_type == 0) s = -(Pi + Pj + PI + TI) * GK;
+    else s = -((pi + pj) * inv_i * inv_j + PI + TI) * GK;
+    ax.add(mj * (s * x0 + VI0));
+    ay.add(mj * (s * x1 + VI1));
+    if (DIM == 3) az.add(mj * (s * x2 + VI2));
+    dr.add(mj * di * inv_j * (GK * vx));
+    zw += mj * inv_j * K;
+    if (shep) sd += mj * K;
   }
   if (active) {
     const double axd = o.gravity[0] + o.body_force[0] + ax.value();
@@ -515,8 +391,8 @@ __global__ void __launch_bounds__(kFT32) forces_fluid32_kernel(DevView v) {
     v.S.A4[i] = make_double4_32a(axd, ayd, azd, drd);
     v.S.zwab[i] = zw;
     if (o.any_shepard) v.S.sumden[i] = sd;
-    if (o.xsph != 0.0) v.S.vxsph4[i] = make_double4_32a(xs0, xs1, xs2, 0.0);
-    if (o.need_sr) {
+    if (xsph_on) v.S.vxsph4[i] = make_double4_32a(xs0, xs1, xs2, 0.0);
+    if (use_sr) {
       double* out = v.S.strain_rate + 9 * (size_t)i;
       out[0] = sr0; out[1] = sr1; out[2] = sr2;
       out[3] = sr1; out[4] = sr4; out[5] = sr5;
@@ -524,7 +400,7 @@ __global__ void __launch_bounds__(kFT32) forces_fluid32_kernel(DevView v) {
     }
     if (!(isfinite(axd) && isfinite(ayd) && isfinite(azd) && isfinite(drd))) atomicOr(&v.sc->status, ST_NONFINITE);
     const double an = sqrt(axd * axd + ayd * ayd + azd * azd);
-    const double cand = o.sqrt_h_a * sqrt(Ci.h / an);  // FP64 dt reduction
+    const double cand = o.sqrt_h_a * sqrt(v.cls[ci_cls].h / an);  // FP64 dt reduction
     if (cand < dtc) dtc = cand;
   }
   for (int off = 16; off > 0; off >>= 1) {

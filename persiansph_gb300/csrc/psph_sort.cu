@@ -180,8 +180,18 @@ __global__ void reorder_kernel(DevView v, const int* __restrict__ perm, const in
     if (src.H4b) dst.H4b[s] = src.H4b[i];
     dst.cls[s] = src.cls[i];
     {
+      // FP32 offset from the cell origin (absolute position outside any cell)
       const double4_32a xs = src.X4[i];
-      v.S.X32[s] = make_float4((float)xs.x, (float)xs.y, (float)xs.z, (float)v.cls[src.cls[i]].h);
+      const int kk = key[i];
+      const float h = (float)v.cls[src.cls[i]].h;
+      if (kk < ncells) {
+        const int cx = kk % v.g.nc[0], t = kk / v.g.nc[0], cy = t % v.g.nc[1], cz = t / v.g.nc[1];
+        v.S.OFF32[s] = make_float4((float)(xs.x - (v.g.blpf[0] + cx * v.g.cell_size[0])),
+                                   (float)(xs.y - (v.g.blpf[1] + cy * v.g.cell_size[1])),
+                                   (float)(v.o.dim == 3 ? xs.z - (v.g.blpf[2] + cz * v.g.cell_size[2]) : 0.0), h);
+      } else {
+        v.S.OFF32[s] = make_float4((float)xs.x, (float)xs.y, (float)xs.z, h);
+      }
     }
     dst.orig[s] = src.orig[i];
     const int k = key[i];

@@ -347,8 +347,8 @@ void launch_update(const DevView& v, cudaStream_t st) {
   else update_kernel<3><<<nb > 0 ? nb : 1, kUT, 0, st>>>(v);
 }
 
-// begin, bin, 3 scan, scatter, rank, reorder, finish, prepare (2 in the FP32C
-// form: copies + walls), forces, dt, update, end
-int launches_per_step(const DevView& v) { return v.o.fp32 ? 15 : 14; }
+// begin, bin, 3 scan, scatter, rank, reorder, finish, neighbour lists, prepare
+// (2 in the FP32C form: copies + walls), forces, dt, update, end
+int launches_per_step(const DevView& v) { return v.o.fp32 ? 16 : 15; }
 
 }  // namespace psph
