@@ -98,3 +98,19 @@ BOXES = {
     "cubic3d": (3, 1, (-0.06, -0.06, -0.06), 0.3, 0.2, 0.25, 0.01, 998.21, 0.024, 1, 0, False, False),
     "hex3d": (3, 1, (0.0, 0.0, 0.0), 0.2, 0.15, 0.12, 0.01, 1000.0, 0.024, 0, 0, False, True),
 }
+
+
+def surge2d():
+    """Dam break used for the surge-front check: 0.5 x 1.0 m column in a 2.0 x 1.5 m tank, dx = 10 mm."""
+    return scenarios.dam_break_2d(dx=0.01, L=0.5, H=1.0, TL=2.0, TH=1.5)
+
+
+SURGE_STEPS = tuple(range(500, 5501, 500))
+
+
+def surge_front(x, is_free, dx=0.01):
+    """Surge-front position: largest x of a free particle within 2 dx of the floor."""
+    free = is_free == 1
+    low = x[:, 1] < 2.0 * dx
+    sel = free & low
+    return float(x[sel, 0].max())

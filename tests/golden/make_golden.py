@@ -51,6 +51,22 @@ def main():
                 out[f"pairs_{k}"] = v
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
         print(name, "n", dom.particles.n, "pairs", sum(len(v) for v in pairs.values()))
+    # surge front of a longer dam break (reference run, Nproc = all host threads)
+    from tests.golden.cases import SURGE_STEPS, surge2d, surge_front
+    dom, dt, _ = surge2d()
+    cfg = dom.config(dt)
+    with tempfile.TemporaryDirectory() as d:
+        write_state_dir(os.path.join(d, "in"), cfg, dom.particles)
+        run_reference(os.path.join(d, "in"), os.path.join(d, "out"), SURGE_STEPS[-1], os.cpu_count() or 1,
+                      list(SURGE_STEPS))
+        times, fronts = [], []
+        for k in SURGE_STEPS:
+            cfgk, arrs = read_state_dir(os.path.join(d, "out", f"step_{k}"))
+            times.append(cfgk["time"][0])
+            fronts.append(surge_front(arrs["x"], arrs["is_free"]))
+    np.savez_compressed(os.path.join(HERE, "surge2d.npz"), steps=np.array(SURGE_STEPS), time=np.array(times),
+                        front=np.array(fronts))
+    print("surge2d", list(zip(times, fronts)))
     boxes = {}
     for name, args in BOXES.items():
         with tempfile.TemporaryDirectory() as d:
