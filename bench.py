@@ -36,8 +36,8 @@ METRIC = "pair-interactions/s @ 3D dam break (5.28M fluid particles), FP32C form
 UNIT = "pair-interactions/s"
 # FP64 operations per directed pair evaluation of the fluid kernel for this
 # workload's options (Wendland, Tait, artificial viscosity, Morris, squared
-# density): counted from forces_fluid_kernel with FMA = 2 and a division or
-# square root = 1 (measurement).
+# density): counted from forces_fluid_kernel's arithmetic on the taken branches,
+# with an FMA counted as 2 and a division or square root as 1.
 FLOPS_PER_DIRECTED_PAIR = 90
 # algorithmic HBM bytes per particle of one FP32C force-kernel launch: read each
 # particle's inputs once (offset+h 16, v+p 16, 1/rho, p/rho^2, c, rho 16, class
@@ -54,9 +54,10 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi sampling during the timed region (SM clock, throttle reasons)."""
+    """nvidia-smi sampling (SM clock, throttle reasons) started before the warm-up
+    steps; `summary()` keeps the samples taken inside the marked timed region."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -64,6 +65,7 @@ class ClockSampler:
         self.device = device
         self.proc = None
         self.path = None
+        self.t0 = self.t1 = None
 
     def __enter__(self):
         fd, self.path = tempfile.mkstemp(suffix=".csv")
@@ -74,10 +76,21 @@ class ClockSampler:
                  "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+        # let the sampler come up before anything is timed
+        deadline = time.time() + 10.0
+        while self.proc and time.time() < deadline and os.path.getsize(self.path) == 0:
+            time.sleep(0.05)
         return self
+
+    def start(self):
+        self.t0 = time.time()
+
+    def stop(self):
+        self.t1 = time.time()
 
     def __exit__(self, *a):
         if self.proc:
+            time.sleep(0.3)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -87,21 +100,32 @@ class ClockSampler:
     def summary(self):
         if not self.path or not os.path.exists(self.path):
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        import datetime
         rows = []
         for line in open(self.path):
             parts = [p.strip() for p in line.split(",")]
-            if len(parts) >= 9:
-                rows.append(parts)
+            if len(parts) >= 10:
+                try:
+                    ts = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                except ValueError:
+                    ts = None
+                rows.append((ts, parts[1:]))
         os.unlink(self.path)
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
-        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        inside = [r for ts, r in rows if ts is not None and self.t0 is not None and self.t1 is not None
+                  and self.t0 - 0.2 <= ts <= self.t1 + 0.2]
+        window = "timed region"
+        if not inside:
+            inside, window = [r for _, r in rows], "whole run (timed region shorter than the sampling period)"
+        num = lambda x: float(x) if x.replace(".", "").isdigit() else None
+        sm = [v for v in (num(r[1]) for r in inside) if v is not None]
+        mx = [v for v in (num(r[2]) for r in inside) if v is not None]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
-        loaded = [s for s in sm if s > 0.5 * (max(mx) if mx else 1)] or sm
+        reasons = sorted({names[k] for r in inside for k in range(4) if r[5 + k].lower() == "active"})
+        loaded = [v for v in sm if v > 0.5 * (max(mx) if mx else 1)] or sm
         return {"sm_mhz": statistics.median(loaded) if loaded else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(inside), "window": window}
 
 
 def build_workload(dx):
@@ -186,14 +210,16 @@ def main():
         cfg.precision = precision
         gd = GpuDomain(cfg)
         gd.upload(dom.particles, initial=True)
-        gd.step(args.warmup)
-        pc0 = gd.pair_count()
-        if dist:
-            dist.barrier()
-        torch.cuda.synchronize()
         with ClockSampler(local) as clk:
+            gd.step(args.warmup)
+            pc0 = gd.pair_count()
+            if dist:
+                dist.barrier()
+            torch.cuda.synchronize()
+            clk.start()
             ms, done = gd.step_timed(args.steps)
-        torch.cuda.synchronize()
+            torch.cuda.synchronize()
+            clk.stop()
         pc1 = gd.pair_count()
         if dist:
             t = torch.tensor([ms], device="cuda")

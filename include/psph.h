@@ -217,6 +217,92 @@ psph_status psph_pair_count(psph_ctx* ctx, uint64_t* pairs);
 psph_status psph_pairs_export_noalloc(psph_ctx* ctx, int which, int64_t* pairs_device, int64_t cap,
                                       int64_t* n_total);
 
+/* ---- Ensembles -----------------------------------------------------------
+ * Many independent domains advanced together, no counterpart in the
+ * reference (whose Domain holds one simulation; an ensemble there is a loop
+ * of processes, each running Solve). A batch context holds ninst instances,
+ * each with its own particles, cell grid (CellInitiate per instance), time
+ * step (AdaptiveTimeStep per instance) and stop time; every step runs one
+ * set of kernel launches over all instances' particles. The instances share
+ * the physics switches of psph_config (dimension, kernel, viscosity equation,
+ * gradient type, scheme, precision, wall pressure mode, gravity, body force,
+ * XSPH, sqrt_h_a, Shepard step); the per-particle parameters, R, the domain
+ * bounds and dt may differ. Particle indices are per instance.
+ * Each instance of a batch evolves exactly as a single-domain context fed the
+ * same particles would (same pairs, same summation order per particle). */
+psph_status psph_batch_create(const psph_config* cfgs, int ninst, psph_ctx** out);
+int psph_batch_size(const psph_ctx* ctx);
+/* parts[0..ninst): one particle set per instance. */
+psph_status psph_batch_upload(psph_ctx* ctx, const psph_particles* parts, int initial);
+/* Advances every instance until it has done nsteps steps or reached its stop
+ * time t_stop[q] (NULL: no stop time); steps_done[q] (if not NULL) receives
+ * the steps instance q made. */
+psph_status psph_batch_step(psph_ctx* ctx, int64_t nsteps, const double* t_stop, int64_t* steps_done);
+int64_t psph_batch_num_particles(const psph_ctx* ctx, int inst);
+psph_status psph_batch_download(psph_ctx* ctx, int inst, psph_particles* out);
+psph_status psph_batch_original_index(psph_ctx* ctx, int inst, int64_t* out);
+psph_status psph_batch_get_grid(const psph_ctx* ctx, int inst, psph_grid* grid);
+psph_status psph_batch_get_integrator(const psph_ctx* ctx, int inst, psph_integrator* integ);
+
+/* ---- Learned closure -------------------------------------------------------
+ * No counterpart in the reference. A small MLP predicts the eddy viscosity
+ * that the LES option computes with the Smagorinsky model in Mat1
+ * (Source/Particle.cpp:157-160: Mu = MuRef + RefDensity (CSmag h)^2 SBar).
+ *
+ * Inputs (raw features, per fluid particle with LES on, from the step's own
+ * pair sums; StrainRate is the reference's fluid strain rate, twice the
+ * symmetric velocity gradient D):
+ *   [0] log(ShearRate), ShearRate = sqrt(StrainRate:StrainRate / 2)
+ *   [1] det(StrainRate) / (StrainRate:StrainRate)^(3/2)   (0 in 2D)
+ *   [2] log(|vorticity|)
+ *   [3] Density / RefDensity
+ *   [4] h / dx            (dx = the lattice spacing given to psph_closure_attach)
+ *   [5] number of neighbours inside the kernel support
+ * (logs of max(value, 1e-8)). The network is 6 -> 64 -> 64 -> 64 -> 1 with
+ * SiLU hidden layers; the three hidden layers run on the tensor cores
+ * (tcgen05, BF16 weights and activations, FP32 accumulation); the output c =
+ * softplus(z) gives the eddy viscosity nu_t = c h^2 ShearRate, and
+ * Mu = MuRef + RefDensity nu_t. A particle whose features fall outside the
+ * training range [lo, hi] uses the Smagorinsky term instead (counted).
+ *
+ * Parameters (PSPH_MLP_NPARAMS floats, FP32 masters; W1..W3 are rounded to
+ * BF16 when used): W1[64][6], b1[64], W2[64][64], b2[64], W3[64][64], b3[64],
+ * w4[64], b4. Normalisation (PSPH_MLP_NNORM floats): mean[6], inv_std[6],
+ * lo[6], hi[6]; the network sees (feature - mean) * inv_std. */
+#define PSPH_MLP_INPUTS 6
+#define PSPH_MLP_HIDDEN 64
+#define PSPH_MLP_NPARAMS 8833
+#define PSPH_MLP_NNORM 24
+typedef struct psph_mlp psph_mlp;
+/* Random initial weights (seeded); allocates on the current device. */
+psph_status psph_mlp_create(uint64_t seed, psph_mlp** out);
+void psph_mlp_destroy(psph_mlp* mlp);
+const char* psph_mlp_last_error(const psph_mlp* mlp);
+psph_status psph_mlp_set_params(psph_mlp* mlp, const float* params, const float* norm);
+psph_status psph_mlp_get_params(const psph_mlp* mlp, float* params, float* norm);
+/* Training set: x[n][6] raw features, y[n] target coefficients c. Sets the
+ * normalisation (mean, 1/std, and the range [lo, hi] widened by 5%). */
+psph_status psph_mlp_set_data(psph_mlp* mlp, const float* x, const float* y, int64_t n);
+/* Adam steps on minibatches of the training set (a new seeded permutation per
+ * pass); loss = mean (softplus(z) - y)^2. losses[k] (if not NULL) receives
+ * the minibatch loss of step k. */
+psph_status psph_mlp_train(psph_mlp* mlp, int64_t steps, int batch, float lr, uint64_t seed, float* losses);
+/* Loss and gradient over (x, y) without changing the parameters. */
+psph_status psph_mlp_loss_grad(psph_mlp* mlp, const float* x, const float* y, int64_t n, double* loss, float* grad);
+/* Network output c for raw features x[n][6]: tensor_cores = 1 runs the
+ * tcgen05 kernel used inside the step, 0 the same arithmetic on CUDA cores. */
+psph_status psph_mlp_infer(psph_mlp* mlp, const float* x, int64_t n, float* c, int tensor_cores);
+/* Puts the closure into the step of a context: every LES fluid particle then
+ * takes its eddy viscosity from the network (copied at this call). After
+ * psph_upload; dx is the lattice spacing of feature [4]. */
+psph_status psph_closure_attach(psph_ctx* ctx, const psph_mlp* mlp, double dx);
+/* Particles evaluated and particles that fell back to Smagorinsky, summed
+ * over steps since attach. */
+psph_status psph_closure_stats(psph_ctx* ctx, uint64_t* evaluated, uint64_t* fallbacks);
+/* Raw features of the last step, out[6*i+k] for the particles of instance 0
+ * in original order (zeros for particles without LES). */
+psph_status psph_closure_features(psph_ctx* ctx, float* out);
+
 /* Measurement helper with no counterpart in the reference: device FP64 FMA
  * throughput in TFLOP/s (an FMA counts 2), the roofline denominator of the
  * FP64 pair kernels. */

@@ -162,10 +162,42 @@ def _declare(lib):
     lib.psph_pair_count.argtypes = [ctx, P(C.c_uint64)]
     lib.psph_probe_fp64_peak.argtypes = [P(C.c_double)]
     lib.psph_pairs_export_noalloc.argtypes = [ctx, C.c_int, C.c_void_p, C.c_int64, P(C.c_int64)]
+    lib.psph_batch_create.argtypes = [P(PsphConfig), C.c_int, P(ctx)]
+    lib.psph_batch_size.argtypes = [ctx]
+    lib.psph_batch_size.restype = C.c_int
+    lib.psph_batch_upload.argtypes = [ctx, P(PsphParticles), C.c_int]
+    lib.psph_batch_step.argtypes = [ctx, C.c_int64, P(C.c_double), P(C.c_int64)]
+    lib.psph_batch_num_particles.argtypes = [ctx, C.c_int]
+    lib.psph_batch_num_particles.restype = C.c_int64
+    lib.psph_batch_download.argtypes = [ctx, C.c_int, P(PsphParticles)]
+    lib.psph_batch_original_index.argtypes = [ctx, C.c_int, P(C.c_int64)]
+    lib.psph_batch_get_grid.argtypes = [ctx, C.c_int, P(PsphGrid)]
+    lib.psph_batch_get_integrator.argtypes = [ctx, C.c_int, P(PsphIntegrator)]
+    fp = P(C.c_float)
+    lib.psph_mlp_create.argtypes = [C.c_uint64, P(C.c_void_p)]
+    lib.psph_mlp_destroy.argtypes = [C.c_void_p]
+    lib.psph_mlp_destroy.restype = None
+    lib.psph_mlp_last_error.argtypes = [C.c_void_p]
+    lib.psph_mlp_last_error.restype = C.c_char_p
+    lib.psph_mlp_set_params.argtypes = [C.c_void_p, fp, fp]
+    lib.psph_mlp_get_params.argtypes = [C.c_void_p, fp, fp]
+    lib.psph_mlp_set_data.argtypes = [C.c_void_p, fp, fp, C.c_int64]
+    lib.psph_mlp_train.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_float, C.c_uint64, fp]
+    lib.psph_mlp_loss_grad.argtypes = [C.c_void_p, fp, fp, C.c_int64, P(C.c_double), fp]
+    lib.psph_mlp_infer.argtypes = [C.c_void_p, fp, C.c_int64, fp, C.c_int]
+    lib.psph_closure_attach.argtypes = [ctx, C.c_void_p, C.c_double]
+    lib.psph_closure_stats.argtypes = [ctx, P(C.c_uint64), P(C.c_uint64)]
+    lib.psph_closure_features.argtypes = [ctx, fp]
+    for name in ("psph_mlp_create", "psph_mlp_set_params", "psph_mlp_get_params", "psph_mlp_set_data",
+                 "psph_mlp_train", "psph_mlp_loss_grad", "psph_mlp_infer", "psph_closure_attach",
+                 "psph_closure_stats", "psph_closure_features"):
+        getattr(lib, name).restype = C.c_int
     for name in ("psph_device_check", "psph_create", "psph_set_stream", "psph_set_grid", "psph_set_integrator",
                  "psph_upload", "psph_step", "psph_download", "psph_original_index", "psph_get_grid", "psph_get_integrator",
                  "psph_pairs_export", "psph_enable_timing", "psph_phase_times", "psph_step_timed", "psph_pair_count",
-                 "psph_probe_fp64_peak", "psph_pairs_export_noalloc"):
+                 "psph_probe_fp64_peak", "psph_pairs_export_noalloc", "psph_batch_create", "psph_batch_upload",
+                 "psph_batch_step", "psph_batch_download", "psph_batch_original_index", "psph_batch_get_grid",
+                 "psph_batch_get_integrator"):
         getattr(lib, name).restype = C.c_int
 
 

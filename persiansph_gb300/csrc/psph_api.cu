@@ -1,6 +1,13 @@
 // C ABI of the GB300 hot path (include/psph.h): context, upload/download,
 // Solve's set-up on the host (InitialChecks, CellInitiate, TimestepCheck), and
 // the per-step launch sequence captured once into a CUDA graph.
+//
+// A context holds one or more independent instances (domains). A single
+// SPH::Domain is a one-instance context; an ensemble (psph_batch_*) puts all
+// instances in the same device arrays: each instance keeps its own cell grid
+// (a block of global cell ids), its own time step and stop time, and the same
+// kernel launches serve all of them, so a step is one graph launch whatever
+// the number of instances.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -13,30 +20,37 @@
 #include <vector>
 
 #include "psph_device.cuh"
+#include "psph_mlp.cuh"
 
 using namespace psph;
 
 struct psph_ctx {
-  psph_config cfg{};
-  psph_grid grid{};
-  bool grid_set = false;
-  psph_integrator integ{};
+  int ninst = 1;
+  std::vector<psph_config> cfgs;
+  std::vector<psph_grid> grids;  // Domain::CellNo/CellSize/BLPF/TRPR/hmax per instance
+  std::vector<psph_integrator> integ;
+  bool grid_set = false;  // single-domain continuation (psph_set_grid)
   bool integ_set = false;
   std::string err;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   int ncap = 0;
-  int n_upload = 0;
+  std::vector<int64_t> inst_off;  // original-index range [inst_off[q], inst_off[q+1]) of instance q
   std::vector<PClass> classes;
   Options opt{};
-  GridDev gdev{};
+  std::vector<GridDev> gdevs;
+  int total_cells = 0;
   Persist PA{}, PB{};
   Scratch S{};
   PClass* d_cls = nullptr;
   PClass32* d_cls32 = nullptr;
+  GridDev* d_grids = nullptr;
+  InstState* d_inst = nullptr;
+  InstState* h_inst = nullptr;  // pinned mirror
   StepScalars* d_sc = nullptr;
   StepScalars* h_sc = nullptr;  // pinned mirror
   uint8_t* d_alive = nullptr;
+  MlpImage* d_mlp = nullptr;  // closure network (copied at psph_closure_attach)
   std::vector<void*> allocs;
   cudaGraphExec_t graph = nullptr;
   bool uploaded = false;
@@ -84,6 +98,8 @@ void free_all(psph_ctx* c) {
   c->allocs.clear();
   if (c->h_sc) cudaFreeHost(c->h_sc);
   c->h_sc = nullptr;
+  if (c->h_inst) cudaFreeHost(c->h_inst);
+  c->h_inst = nullptr;
 }
 
 // Particle constructor defaults (Source/Particle.cpp:25-117) for NULL arrays.
@@ -98,9 +114,9 @@ double eos_host(int eq, double cs, double p0, double rho, double rho0) {
   }
 }
 
-// CellInitiate (Source/Domain.cpp:549-660).
-psph_status cell_initiate(psph_ctx* c, const psph_particles* p, double* mu_max, double* cs_max) {
-  psph_grid& g = c->grid;
+// CellInitiate (Source/Domain.cpp:549-660) for one instance.
+psph_status cell_initiate(psph_ctx* c, const psph_config& cf, const psph_particles* p, psph_grid& g,
+                          double* mu_max, double* cs_max) {
   const int64_t n = p->n;
   double TRPR[3], BLPF[3];
   for (int d = 0; d < 3; ++d) TRPR[d] = BLPF[d] = p->x[d];
@@ -120,7 +136,6 @@ psph_status cell_initiate(psph_ctx* c, const psph_particles* p, double* mu_max, 
     if (mu > *mu_max) *mu_max = mu;
     if (cs > *cs_max) *cs_max = cs;
   }
-  const psph_config& cf = c->cfg;
   for (int d = 0; d < 3; ++d) {
     if (cf.dom_max[d] > TRPR[d]) TRPR[d] = cf.dom_max[d];
     if (cf.dom_min[d] < BLPF[d]) BLPF[d] = cf.dom_min[d];
@@ -169,13 +184,17 @@ void record_phase(psph_ctx* c, int k) {
 
 DevView view(psph_ctx* c) {
   DevView v{};
-  v.g = c->gdev;
+  v.grids = c->d_grids;
+  v.inst = c->d_inst;
+  v.ninst = c->ninst;
+  v.total_cells = c->total_cells;
   v.o = c->opt;
   v.PA = c->PA;
   v.PB = c->PB;
   v.S = c->S;
   v.cls = c->d_cls;
   v.cls32 = c->d_cls32;
+  v.mlp = c->d_mlp;
   v.sc = c->d_sc;
   v.alive = c->d_alive;
   v.ncap = c->ncap;
@@ -198,6 +217,7 @@ void enqueue_step(psph_ctx* c) {
   if (v.o.fp32) launch_forces32(v, st);
   else launch_forces(v, st);
   record_phase(c, 3);
+  if (v.o.closure) launch_closure(v, st);
   launch_dt(v, st);
   record_phase(c, 4);
   launch_update(v, st);
@@ -205,224 +225,249 @@ void enqueue_step(psph_ctx* c) {
   record_phase(c, 5);
 }
 
-__global__ void arm_kernel(StepScalars* sc, double t_stop) {
-  sc->t_stop = t_stop;
-  sc->stop = 0;
-  sc->status = 0;
+// Clears every instance's stop flag and the status word on the stream, with
+// no stop time (used before a pair export, which sorts but does not step).
+__global__ void rearm_kernel(InstState* inst, int ninst, StepScalars* sc) {
+  for (int k = threadIdx.x; k < ninst; k += blockDim.x) {
+    inst[k].stop = 0;
+    inst[k].t_stop = 1e300;
+  }
+  if (threadIdx.x == 0) {
+    sc->status = 0;
+    sc->all_stop = 0;
+  }
 }
 
 psph_status sync_scalars(psph_ctx* c) {
   CUDA_TRY(c, cudaMemcpyAsync(c->h_sc, c->d_sc, sizeof(StepScalars), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(c->h_inst, c->d_inst, sizeof(InstState) * c->ninst, cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   return PSPH_OK;
 }
 
-}  // namespace
-
-extern "C" {
-
-int psph_abi_version(void) { return PSPH_ABI_VERSION; }
-
-psph_status psph_device_check(int* device_count) {
-  int n = 0;
-  if (cudaGetDeviceCount(&n) != cudaSuccess) n = 0;
-  if (device_count) *device_count = n;
-  if (n < 1) return PSPH_ERR_NO_DEVICE;
-  cudaDeviceProp prop;
-  if (cudaGetDeviceProperties(&prop, 0) != cudaSuccess) return PSPH_ERR_NO_DEVICE;
-  if (!(prop.major == 10 && prop.minor == 3)) return PSPH_ERR_NO_DEVICE;  // built for sm_103a only
+// Sets each instance's stop time (t_stop[q], or t_all when t_stop is NULL)
+// and clears the stop flags and the status word before a run of steps.
+psph_status arm(psph_ctx* c, const double* t_stop, double t_all) {
+  psph_status st = sync_scalars(c);
+  if (st) return st;
+  for (int q = 0; q < c->ninst; ++q) {
+    c->h_inst[q].t_stop = t_stop ? t_stop[q] : t_all;
+    c->h_inst[q].stop = 0;
+  }
+  c->h_sc->status = 0;
+  c->h_sc->all_stop = 0;
+  CUDA_TRY(c, cudaMemcpyAsync(c->d_inst, c->h_inst, sizeof(InstState) * c->ninst, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(c->d_sc, c->h_sc, sizeof(StepScalars), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   return PSPH_OK;
 }
 
-psph_status psph_create(const psph_config* cfg, psph_ctx** out) {
-  if (!cfg || !out) return PSPH_ERR_INVALID_ARGUMENT;
+psph_status build_graph(psph_ctx* c) {
+  if (c->graph) return PSPH_OK;
+  cudaGraph_t g;
+  CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  enqueue_step(c);
+  cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+  if (ce != cudaSuccess) return set_err(c, PSPH_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+  ce = cudaGraphInstantiate(&c->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (ce != cudaSuccess) return set_err(c, PSPH_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+  return PSPH_OK;
+}
+
+psph_status create_impl(const psph_config* cfgs, int ninst, psph_ctx** out) {
+  if (!cfgs || !out || ninst < 1) return PSPH_ERR_INVALID_ARGUMENT;
   *out = nullptr;
   psph_ctx* c = new psph_ctx();
-  c->cfg = *cfg;
   *out = c;
-  const psph_config& k = *cfg;
-  if (k.dimension != 2 && k.dimension != 3)
-    return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Please correct the dimension (2=>2D or 3=>3D) and run again");
-  if (k.kernel_type < 0 || k.kernel_type > 2)
-    return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Kernel Type No is out of range");
-  if (k.vis_eq < 0 || k.vis_eq > 3) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Viscosity Equation No is out of range");
-  if (k.gradient_type < 0 || k.gradient_type > 1) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Gradient type out of range");
-  if (k.scheme != PSPH_MVERLET && k.scheme != PSPH_LEAPFROG)
-    return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Scheme must be 0 (Modified Verlet) or 1 (Leapfrog)");
-  if (k.swi_type != 0) return set_err(c, PSPH_ERR_UNSUPPORTED, "soil-water interaction (SWIType) is outside this build");
-  if (k.precision != PSPH_FP64 && k.precision != PSPH_FP32C)
-    return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "precision must be PSPH_FP64 or PSPH_FP32C");
-  if (k.dimension == 2 && k.periodic[2]) return set_err(c, PSPH_ERR_UNSUPPORTED, "periodic z in 2D");
-  for (int e = 0; e < 8; ++e)
-    if (k.reserved[e]) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "reserved fields must be zero");
+  c->ninst = ninst;
+  c->cfgs.assign(cfgs, cfgs + ninst);
+  for (int q = 0; q < ninst; ++q) {
+    const psph_config& k = cfgs[q];
+    if (k.dimension != 2 && k.dimension != 3)
+      return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Please correct the dimension (2=>2D or 3=>3D) and run again");
+    if (k.kernel_type < 0 || k.kernel_type > 2)
+      return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Kernel Type No is out of range");
+    if (k.vis_eq < 0 || k.vis_eq > 3) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Viscosity Equation No is out of range");
+    if (k.gradient_type < 0 || k.gradient_type > 1) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Gradient type out of range");
+    if (k.scheme != PSPH_MVERLET && k.scheme != PSPH_LEAPFROG)
+      return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Scheme must be 0 (Modified Verlet) or 1 (Leapfrog)");
+    if (k.swi_type != 0) return set_err(c, PSPH_ERR_UNSUPPORTED, "soil-water interaction (SWIType) is outside this build");
+    if (k.precision != PSPH_FP64 && k.precision != PSPH_FP32C)
+      return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "precision must be PSPH_FP64 or PSPH_FP32C");
+    if (k.dimension == 2 && k.periodic[2]) return set_err(c, PSPH_ERR_UNSUPPORTED, "periodic z in 2D");
+    for (int e = 0; e < 8; ++e)
+      if (k.reserved[e]) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "reserved fields must be zero");
+    // one set of kernels serves all instances: the physics switches must agree
+    const psph_config& a = cfgs[0];
+    bool same = k.dimension == a.dimension && k.kernel_type == a.kernel_type && k.vis_eq == a.vis_eq &&
+                k.gradient_type == a.gradient_type && k.scheme == a.scheme && k.precision == a.precision &&
+                k.wall_pressure_mode == a.wall_pressure_mode && k.shepard_step == a.shepard_step &&
+                k.xsph == a.xsph && k.sqrt_h_a == a.sqrt_h_a;
+    for (int d = 0; d < 3; ++d) same = same && k.gravity[d] == a.gravity[d] && k.body_force[d] == a.body_force[d];
+    if (!same)
+      return set_err(c, PSPH_ERR_INVALID_ARGUMENT,
+                     "instance %d: an ensemble shares dimension, kernel, viscosity, gradient, scheme, precision, "
+                     "wall pressure, gravity, body force, XSPH, sqrt_h_a and Shepard step with instance 0", q);
+  }
   int dev = 0;
   if (psph_device_check(&dev) != PSPH_OK) return set_err(c, PSPH_ERR_NO_DEVICE, "no sm_103 CUDA device available");
   cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) return set_err(c, PSPH_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
   c->own_stream = true;
   for (int i = 0; i < 6; ++i) cudaEventCreate(&c->ev[i]);
-  c->integ.time = k.time;
-  c->integ.deltat = c->integ.deltatint = c->integ.deltatmin = k.dt;
-  c->integ.first_step = 1;
-  return PSPH_OK;
-}
-
-void psph_destroy(psph_ctx* c) {
-  if (!c) return;
-  if (c->stream) cudaStreamSynchronize(c->stream);
-  free_all(c);
-  for (int i = 0; i < 6; ++i)
-    if (c->ev[i]) cudaEventDestroy(c->ev[i]);
-  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
-  delete c;
-}
-
-const char* psph_last_error(const psph_ctx* c) { return c ? c->err.c_str() : "null context"; }
-
-psph_status psph_set_stream(psph_ctx* c, void* s) {
-  if (!c) return PSPH_ERR_INVALID_ARGUMENT;
-  if (c->graph) {
-    cudaGraphExecDestroy(c->graph);
-    c->graph = nullptr;
-  }
-  if (s) {
-    if (c->own_stream) cudaStreamDestroy(c->stream);
-    c->stream = (cudaStream_t)s;
-    c->own_stream = false;
+  c->grids.resize(ninst);
+  c->integ.resize(ninst);
+  for (int q = 0; q < ninst; ++q) {
+    std::memset(&c->grids[q], 0, sizeof(psph_grid));
+    psph_integrator& it = c->integ[q];
+    std::memset(&it, 0, sizeof it);
+    it.time = cfgs[q].time;
+    it.deltat = it.deltatint = it.deltatmin = cfgs[q].dt;
+    it.first_step = 1;
   }
   return PSPH_OK;
 }
 
-psph_status psph_set_grid(psph_ctx* c, const psph_grid* g) {
-  if (!c || !g) return PSPH_ERR_INVALID_ARGUMENT;
-  if (c->uploaded) return set_err(c, PSPH_ERR_STATE, "psph_set_grid must come before psph_upload");
-  c->grid = *g;
-  c->grid_set = true;
-  return PSPH_OK;
-}
-
-psph_status psph_set_integrator(psph_ctx* c, const psph_integrator* it) {
-  if (!c || !it) return PSPH_ERR_INVALID_ARGUMENT;
-  if (c->uploaded) return set_err(c, PSPH_ERR_STATE, "psph_set_integrator must come before psph_upload");
-  c->integ = *it;
-  c->integ_set = true;
-  return PSPH_OK;
-}
-
-psph_status psph_upload(psph_ctx* c, const psph_particles* p, int initial) {
-  if (!c || !p) return PSPH_ERR_INVALID_ARGUMENT;
+psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
+  if (!c || !parts) return PSPH_ERR_INVALID_ARGUMENT;
   if (c->uploaded) return set_err(c, PSPH_ERR_STATE, "particles already uploaded to this context");
   if (!c->stream) return set_err(c, PSPH_ERR_STATE, "context not created");
-  const int64_t n = p->n;
-  if (n < 1) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "no particles");
-  if (n > (1LL << 30)) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "too many particles");
-  if (!p->x || !p->h || !p->density || !p->mass)
-    return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "x, h, density and mass are required");
-  const psph_config& k = c->cfg;
+  const int ninst = c->ninst;
+  const psph_config& k = c->cfgs[0];
   const bool lf = (k.scheme == PSPH_LEAPFROG);
+  int64_t ntot = 0;
+  c->inst_off.assign(ninst + 1, 0);
+  for (int q = 0; q < ninst; ++q) {
+    const psph_particles* p = &parts[q];
+    if (p->n < 1) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, ninst == 1 ? "no particles" : "instance %d has no particles", q);
+    if (p->n > (1LL << 30)) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "too many particles");
+    if (!p->x || !p->h || !p->density || !p->mass)
+      return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "x, h, density and mass are required (instance %d)", q);
+    c->inst_off[q] = ntot;
+    ntot += p->n;
+  }
+  c->inst_off[ninst] = ntot;
 
-  // ---- particle classes ---------------------------------------------------
-  std::vector<int> cls(n);
-  std::unordered_map<std::string, int, ClassKeyHash> index;
+  // ---- particle classes (per instance) and initial pressure -------------------
   bool dyn_mu = false;
-  for (int64_t i = 0; i < n; ++i)
-    if (dflt(p->t0, i, 0.0) > 0.0 || iflt(p->les, i, 0)) dyn_mu = true;
-  std::vector<double> pressure(n);
+  for (int q = 0; q < ninst; ++q)
+    for (int64_t i = 0; i < parts[q].n; ++i)
+      if (dflt(parts[q].t0, i, 0.0) > 0.0 || iflt(parts[q].les, i, 0)) dyn_mu = true;
+  std::vector<int> cls(ntot);
+  std::vector<double> pressure(ntot);
+  std::unordered_map<std::string, int, ClassKeyHash> index;
   int material0 = -1;
-  for (int64_t i = 0; i < n; ++i) {
-    PClass C;
-    std::memset(&C, 0, sizeof C);
-    C.cs = dflt(p->cs, i, 0.0);
-    C.p0 = dflt(p->p0, i, 0.0);
-    C.rho0 = p->ref_density ? p->ref_density[i] : p->density[i];
-    C.fpmassc = dflt(p->fpmassc, i, 1.0);
-    C.alpha = dflt(p->alpha, i, 0.0);
-    C.beta = dflt(p->beta, i, 0.0);
-    C.mu0 = dyn_mu ? 0.0 : dflt(p->mu, i, 0.0);
-    C.mu_ref = dflt(p->mu_ref, i, 0.0);
-    C.t0 = dflt(p->t0, i, 0.0);
-    C.bm = dflt(p->bingham_m, i, 300.0);
-    C.csmag = dflt(p->csmag, i, 0.17);
-    C.ti = dflt(p->ti, i, 0.0);
-    C.tin = dflt(p->tin, i, 4.0);
-    C.tid = dflt(p->ti_init_dist, i, 0.0);
-    C.g_mod = dflt(p->g_mod, i, 0.0);
-    C.k_mod = dflt(p->k_mod, i, 0.0);
-    C.sigmay = dflt(p->sigmay, i, 0.0);
-    C.coh = dflt(p->cohesion, i, 0.0);
-    C.phi = dflt(p->phi, i, 0.0);
-    C.psi = dflt(p->psi, i, 0.0);
-    C.h = p->h[i];
-    C.mass = p->mass[i];
-    C.material = iflt(p->material, i, 0);
-    C.is_free = iflt(p->is_free, i, 1) != 0;
-    C.no_slip = iflt(p->no_slip, i, 0) != 0;
-    C.pres_eq = iflt(p->pres_eq, i, 0);
-    C.shepard = iflt(p->shepard, i, 0) != 0;
-    C.les = iflt(p->les, i, 0) != 0;
-    C.vis_m = iflt(p->vis_m, i, 0);
-    C.fail = iflt(p->fail, i, 0);
-    C.id = iflt(p->id, i, 0);
-    if (C.material < 1 || C.material > 3)
-      return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Material Type No is out of range (particle %lld)", (long long)i);
-    if (C.pres_eq < 0 || C.pres_eq > 2)
-      return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Please correct Pressure Equation No (particle %lld)", (long long)i);
-    if (C.material == 2 && C.fail > 1) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Undefined failure criteria for solids");
-    if (C.material == 3 && C.fail > 3) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Failure Type No is out of range");
-    if (C.material == 1 && C.t0 > 0.0 && C.vis_m > 1)
-      return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Non-Newtonian Viscosity Type No is out of range");
-    if (material0 < 0) material0 = C.material;
-    if (C.material != material0)
-      return set_err(c, PSPH_ERR_UNSUPPORTED,
-                     "particles of different materials interact through CalcForce12/13 (FSI, seepage), outside this build");
-    std::string key((const char*)&C, sizeof C);
-    auto it = index.find(key);
-    int id;
-    if (it == index.end()) {
-      id = (int)c->classes.size();
-      if (id >= 65535) return set_err(c, PSPH_ERR_UNSUPPORTED, "more than 65535 distinct particle parameter sets");
-      index.emplace(key, id);
-      c->classes.push_back(C);
-    } else {
-      id = it->second;
+  for (int q = 0; q < ninst; ++q) {
+    const psph_particles* p = &parts[q];
+    for (int64_t i = 0; i < p->n; ++i) {
+      PClass C;
+      std::memset(&C, 0, sizeof C);
+      C.cs = dflt(p->cs, i, 0.0);
+      C.p0 = dflt(p->p0, i, 0.0);
+      C.rho0 = p->ref_density ? p->ref_density[i] : p->density[i];
+      C.fpmassc = dflt(p->fpmassc, i, 1.0);
+      C.alpha = dflt(p->alpha, i, 0.0);
+      C.beta = dflt(p->beta, i, 0.0);
+      C.mu0 = dyn_mu ? 0.0 : dflt(p->mu, i, 0.0);
+      C.mu_ref = dflt(p->mu_ref, i, 0.0);
+      C.t0 = dflt(p->t0, i, 0.0);
+      C.bm = dflt(p->bingham_m, i, 300.0);
+      C.csmag = dflt(p->csmag, i, 0.17);
+      C.ti = dflt(p->ti, i, 0.0);
+      C.tin = dflt(p->tin, i, 4.0);
+      C.tid = dflt(p->ti_init_dist, i, 0.0);
+      C.g_mod = dflt(p->g_mod, i, 0.0);
+      C.k_mod = dflt(p->k_mod, i, 0.0);
+      C.sigmay = dflt(p->sigmay, i, 0.0);
+      C.coh = dflt(p->cohesion, i, 0.0);
+      C.phi = dflt(p->phi, i, 0.0);
+      C.psi = dflt(p->psi, i, 0.0);
+      C.h = p->h[i];
+      C.mass = p->mass[i];
+      C.material = iflt(p->material, i, 0);
+      C.is_free = iflt(p->is_free, i, 1) != 0;
+      C.no_slip = iflt(p->no_slip, i, 0) != 0;
+      C.pres_eq = iflt(p->pres_eq, i, 0);
+      C.shepard = iflt(p->shepard, i, 0) != 0;
+      C.les = iflt(p->les, i, 0) != 0;
+      C.vis_m = iflt(p->vis_m, i, 0);
+      C.fail = iflt(p->fail, i, 0);
+      C.id = iflt(p->id, i, 0);
+      C.inst = q;
+      if (C.material < 1 || C.material > 3)
+        return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Material Type No is out of range (particle %lld)", (long long)i);
+      if (C.pres_eq < 0 || C.pres_eq > 2)
+        return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Please correct Pressure Equation No (particle %lld)", (long long)i);
+      if (C.material == 2 && C.fail > 1) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Undefined failure criteria for solids");
+      if (C.material == 3 && C.fail > 3) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Failure Type No is out of range");
+      if (C.material == 1 && C.t0 > 0.0 && C.vis_m > 1)
+        return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Non-Newtonian Viscosity Type No is out of range");
+      if (material0 < 0) material0 = C.material;
+      if (C.material != material0)
+        return set_err(c, PSPH_ERR_UNSUPPORTED,
+                       "particles of different materials interact through CalcForce12/13 (FSI, seepage), outside this build");
+      std::string key((const char*)&C, sizeof C);
+      auto it = index.find(key);
+      int id;
+      if (it == index.end()) {
+        id = (int)c->classes.size();
+        if (id >= 65535) return set_err(c, PSPH_ERR_UNSUPPORTED, "more than 65535 distinct particle parameter sets");
+        index.emplace(key, id);
+        c->classes.push_back(C);
+      } else {
+        id = it->second;
+      }
+      const int64_t g = c->inst_off[q] + i;
+      cls[g] = id;
+      // InitialChecks: initial pressure from the EOS for fluids and solids (Source/Domain.cpp:1675-1677)
+      const double p_in = dflt(p->pressure, i, 0.0);
+      pressure[g] = (initial && C.material < 3) ? eos_host(C.pres_eq, C.cs, C.p0, p->density[i], C.rho0) : p_in;
     }
-    cls[i] = id;
-    // InitialChecks: initial pressure from the EOS for fluids and solids (Source/Domain.cpp:1675-1677)
-    const double p_in = dflt(p->pressure, i, 0.0);
-    pressure[i] = (initial && C.material < 3) ? eos_host(C.pres_eq, C.cs, C.p0, p->density[i], C.rho0) : p_in;
   }
 
-  // ---- grid (CellInitiate) and TimestepCheck --------------------------------
-  if (!c->grid_set) {
-    double mu_max, cs_max;
-    psph_status st = cell_initiate(c, p, &mu_max, &cs_max);
-    if (st) return st;
-    if (initial) {  // TimestepCheck (Source/Domain.cpp:1721-1733)
-      const double t1 = 0.25 * c->grid.hmax / (cs_max);
-      const double t2 = (mu_max > 0.0) ? 0.125 * c->grid.hmax * c->grid.hmax * c->grid.rhomax / mu_max : 1000000.0;
-      if (c->integ.deltatint > std::min(t1, t2))
-        return set_err(c, PSPH_ERR_CFL, "Please decrease the time step to the allowable range (CFL limit %g s)",
-                       std::min(t1, t2));
+  // ---- grids (CellInitiate) and TimestepCheck, per instance --------------------
+  c->gdevs.resize(ninst);
+  long long cell_base = 0;
+  for (int q = 0; q < ninst; ++q) {
+    const psph_config& cf = c->cfgs[q];
+    psph_grid& g = c->grids[q];
+    if (!(c->grid_set && q == 0)) {
+      double mu_max, cs_max;
+      psph_status st = cell_initiate(c, cf, &parts[q], g, &mu_max, &cs_max);
+      if (st) return st;
+      if (initial) {  // TimestepCheck (Source/Domain.cpp:1721-1733)
+        const double t1 = 0.25 * g.hmax / (cs_max);
+        const double t2 = (mu_max > 0.0) ? 0.125 * g.hmax * g.hmax * g.rhomax / mu_max : 1000000.0;
+        if (c->integ[q].deltatint > std::min(t1, t2))
+          return set_err(c, PSPH_ERR_CFL, "Please decrease the time step to the allowable range (CFL limit %g s)",
+                         std::min(t1, t2));
+      }
     }
+    GridDev& gd = c->gdevs[q];
+    std::memset(&gd, 0, sizeof gd);
+    for (int d = 0; d < 3; ++d) {
+      gd.blpf[d] = g.blpf[d];
+      gd.trpr[d] = g.trpr[d];
+      gd.cell_size[d] = g.cell_size[d];
+      gd.dom_size[d] = g.dom_size[d];
+      gd.periodic[d] = cf.periodic[d] ? 1 : 0;
+      gd.cn_ref[d] = g.cell_no[d];
+      gd.nc[d] = cf.periodic[d] ? g.cell_no[d] - 2 : g.cell_no[d];
+      if (cf.periodic[d] && gd.nc[d] < 3)
+        return set_err(c, PSPH_ERR_UNSUPPORTED, "periodic axis %d spans fewer than 3 cells", d);
+    }
+    gd.hmax = g.hmax;
+    gd.cellfac = (cf.kernel_type == PSPH_QUINTIC_SPLINE) ? 3.0 : 2.0;
+    g.cellfac = gd.cellfac;
+    const long long nci = (long long)gd.nc[0] * gd.nc[1] * gd.nc[2];
+    if (nci > (1LL << 30)) return set_err(c, PSPH_ERR_UNSUPPORTED, "grid has more than 2^30 cells");
+    gd.ncells = (int)nci;
+    gd.cell_base = (int)cell_base;
+    cell_base += nci;
+    if (cell_base > (1LL << 30)) return set_err(c, PSPH_ERR_UNSUPPORTED, "the instances' grids hold more than 2^30 cells");
   }
-  GridDev& gd = c->gdev;
-  for (int d = 0; d < 3; ++d) {
-    gd.blpf[d] = c->grid.blpf[d];
-    gd.trpr[d] = c->grid.trpr[d];
-    gd.cell_size[d] = c->grid.cell_size[d];
-    gd.dom_size[d] = c->grid.dom_size[d];
-    gd.periodic[d] = k.periodic[d] ? 1 : 0;
-    gd.cn_ref[d] = c->grid.cell_no[d];
-    gd.nc[d] = k.periodic[d] ? c->grid.cell_no[d] - 2 : c->grid.cell_no[d];
-    if (k.periodic[d] && gd.nc[d] < 3)
-      return set_err(c, PSPH_ERR_UNSUPPORTED, "periodic axis %d spans fewer than 3 cells", d);
-  }
-  gd.hmax = c->grid.hmax;
-  gd.cellfac = (k.kernel_type == PSPH_QUINTIC_SPLINE) ? 3.0 : 2.0;
-  c->grid.cellfac = gd.cellfac;
-  const long long ncells = (long long)gd.nc[0] * gd.nc[1] * gd.nc[2];
-  if (ncells > (1LL << 30)) return set_err(c, PSPH_ERR_UNSUPPORTED, "grid has more than 2^30 cells");
-  gd.ncells = (int)ncells;
+  c->total_cells = (int)cell_base;
 
   // ---- options ---------------------------------------------------------------
   Options& o = c->opt;
@@ -436,7 +481,7 @@ psph_status psph_upload(psph_ctx* c, const psph_particles* p, int initial) {
   o.fp32 = (k.precision == PSPH_FP32C);
   if (o.fp32 && o.has_solid)
     return set_err(c, PSPH_ERR_UNSUPPORTED, "the FP32C form covers fluids (Material 1); use PSPH_FP64 for solids and soil");
-  if (n >= (1LL << 26)) return set_err(c, PSPH_ERR_UNSUPPORTED, "this build handles fewer than 2^26 particles");
+  if (ntot >= (1LL << 26)) return set_err(c, PSPH_ERR_UNSUPPORTED, "this build handles fewer than 2^26 particles");
   o.soil_pairs = (material0 == 3);
   o.dyn_mu = dyn_mu;
   o.xsph = k.xsph;
@@ -480,11 +525,13 @@ psph_status psph_upload(psph_ctx* c, const psph_particles* p, int initial) {
   }
   o.inv_h = 1.0 / c->classes[0].h;
   o.nclasses = (int)c->classes.size();
+  // neighbour lists: 3D supports hold ~80 (h = 1.3 dx) particles, 2D ~20-44;
+  // a particle with more falls back to scanning its cells
+  o.nl_cap = (k.dimension == 3) ? 128 : 64;
 
   // ---- device buffers ----------------------------------------------------------
-  c->ncap = (int)n;
-  c->n_upload = (int)n;
-  const size_t N = (size_t)n;
+  c->ncap = (int)ntot;
+  const size_t N = (size_t)ntot;
   psph_status st = PSPH_OK;
   for (Persist* P : {&c->PA, &c->PB}) {
     if ((st = dalloc(c, &P->X4, N)) || (st = dalloc(c, &P->V4, N)) || (st = dalloc(c, &P->H4, N)) ||
@@ -501,24 +548,31 @@ psph_status psph_upload(psph_ctx* c, const psph_particles* p, int initial) {
     }
   }
   Scratch& S = c->S;
-  const size_t NC = (size_t)ncells;
-  const int nb_forces = forces_blocks((int)n);
+  const size_t NC = (size_t)c->total_cells;
   if ((st = dalloc(c, &S.key, N)) || (st = dalloc(c, &S.count, NC + 2)) || (st = dalloc(c, &S.start, NC + 3)) ||
       (st = dalloc(c, &S.tmp_perm, N)) || (st = dalloc(c, &S.perm, N)) || (st = dalloc(c, &S.cellid, N)) ||
-      (st = dalloc(c, &S.block_sums, (NC + 2 + 1023) / 1024 + 1)) || (st = dalloc(c, &S.blockmin, (size_t)nb_forces)) ||
+      (st = dalloc(c, &S.block_sums, (NC + 2 + 1023) / 1024 + 1)) ||
       (st = dalloc(c, &S.OFF32, N)) || (st = dalloc(c, &S.D4, N)) || (st = dalloc(c, &S.nl_count, N)) ||
       (st = dalloc(c, &S.A4, N)) || (st = dalloc(c, &S.zwab, N)) || (st = dalloc(c, &S.sumden, N)) ||
       (st = dalloc(c, &S.sumkernel, N)) || (st = dalloc(c, &S.nsv4, N)) || (st = dalloc(c, &S.vxsph4, N)) ||
       (st = dalloc(c, &S.shear_rate, N)) || (st = dalloc(c, &S.sbar, N)))
     return st;
+  if ((st = dalloc(c, &S.nl, (size_t)o.nl_cap * N))) return st;
   if (o.need_sr || o.has_solid)
     if ((st = dalloc(c, &S.strain_rate, 9 * N))) return st;
   if (o.fp32)
     if ((st = dalloc(c, &S.V32, N)) || (st = dalloc(c, &S.D32, N))) return st;
-  // neighbour lists: 3D supports hold ~80 (h = 1.3 dx) particles, 2D ~20-44;
-  // a particle with more falls back to scanning its cells
-  o.nl_cap = (k.dimension == 3) ? 128 : 64;
-  if ((st = dalloc(c, &S.nl, (size_t)o.nl_cap * N))) return st;
+  if (o.has_solid) {
+    if ((st = dalloc(c, &S.rotation_rate, 9 * N)) || (st = dalloc(c, &S.sigma_o, 9 * N)) ||
+        (st = dalloc(c, &S.strain_o, 9 * N)) || (st = dalloc(c, &S.shear_o, 9 * N)))
+      return st;
+  }
+  if ((st = dalloc(c, &c->d_cls, c->classes.size())) || (st = dalloc(c, &c->d_sc, 1)) ||
+      (st = dalloc(c, &c->d_alive, N)) || (st = dalloc(c, &c->d_grids, (size_t)ninst)) ||
+      (st = dalloc(c, &c->d_inst, (size_t)ninst)))
+    return st;
+  CUDA_TRY(c, cudaMallocHost(&c->h_sc, sizeof(StepScalars)));
+  CUDA_TRY(c, cudaMallocHost(&c->h_inst, sizeof(InstState) * ninst));
   {
     std::vector<PClass32> c32(c->classes.size());
     for (size_t q = 0; q < c->classes.size(); ++q) {
@@ -531,41 +585,39 @@ psph_status psph_upload(psph_ctx* c, const psph_particles* p, int initial) {
                 (C.shepard ? CF_SHEPARD : 0) | (C.t0 > 0.0 ? CF_T0 : 0) | (C.ti > 0.0 ? CF_TI : 0);
       F.material = C.material;
       F.pres_eq = C.pres_eq;
-      F.pad = 0;
+      F.inst = C.inst;
     }
     if ((st = dalloc(c, &c->d_cls32, c32.size()))) return st;
     CUDA_TRY(c, cudaMemcpy(c->d_cls32, c32.data(), c32.size() * sizeof(PClass32), cudaMemcpyHostToDevice));
   }
-  if (o.has_solid) {
-    if ((st = dalloc(c, &S.rotation_rate, 9 * N)) || (st = dalloc(c, &S.sigma_o, 9 * N)) ||
-        (st = dalloc(c, &S.strain_o, 9 * N)) || (st = dalloc(c, &S.shear_o, 9 * N)))
-      return st;
-  }
-  if ((st = dalloc(c, &c->d_cls, c->classes.size())) || (st = dalloc(c, &c->d_sc, 1)) || (st = dalloc(c, &c->d_alive, N)))
-    return st;
-  CUDA_TRY(c, cudaMallocHost(&c->h_sc, sizeof(StepScalars)));
 
   // ---- pack and copy --------------------------------------------------------------
   {
     std::vector<double4_32a> X(N), V(N), H(N), Hb(lf ? N : 0);
     std::vector<int> orig(N);
-    for (int64_t i = 0; i < n; ++i) {
-      const double* x = p->x + 3 * i;
-      const bool two_d = (k.dimension == 2);
-      const double vx = dflt(p->v, 3 * i, 0.0), vy = dflt(p->v, 3 * i + 1, 0.0),
-                   vz = two_d ? 0.0 : dflt(p->v, 3 * i + 2, 0.0);
-      X[i] = make_double4_32a(x[0], x[1], x[2], p->density[i]);
-      V[i] = make_double4_32a(vx, vy, vz, pressure[i]);
-      if (lf) {
-        H[i] = make_double4_32a(dflt(p->va, 3 * i, 0.0), dflt(p->va, 3 * i + 1, 0.0), dflt(p->va, 3 * i + 2, 0.0),
-                            dflt(p->densitya, i, 0.0));
-        Hb[i] = make_double4_32a(dflt(p->vb, 3 * i, 0.0), dflt(p->vb, 3 * i + 1, 0.0), dflt(p->vb, 3 * i + 2, 0.0),
-                             dflt(p->densityb, i, 0.0));
-      } else {
-        H[i] = make_double4_32a(dflt(p->vb, 3 * i, 0.0), dflt(p->vb, 3 * i + 1, 0.0), dflt(p->vb, 3 * i + 2, 0.0),
-                            dflt(p->densityb, i, 0.0));
+    std::vector<double> mu(dyn_mu ? N : 0);
+    const bool two_d = (k.dimension == 2);
+    for (int q = 0; q < ninst; ++q) {
+      const psph_particles* p = &parts[q];
+      for (int64_t i = 0; i < p->n; ++i) {
+        const int64_t g = c->inst_off[q] + i;
+        const double* x = p->x + 3 * i;
+        const double vx = dflt(p->v, 3 * i, 0.0), vy = dflt(p->v, 3 * i + 1, 0.0),
+                     vz = two_d ? 0.0 : dflt(p->v, 3 * i + 2, 0.0);
+        X[g] = make_double4_32a(x[0], x[1], x[2], p->density[i]);
+        V[g] = make_double4_32a(vx, vy, vz, pressure[g]);
+        if (lf) {
+          H[g] = make_double4_32a(dflt(p->va, 3 * i, 0.0), dflt(p->va, 3 * i + 1, 0.0), dflt(p->va, 3 * i + 2, 0.0),
+                                  dflt(p->densitya, i, 0.0));
+          Hb[g] = make_double4_32a(dflt(p->vb, 3 * i, 0.0), dflt(p->vb, 3 * i + 1, 0.0), dflt(p->vb, 3 * i + 2, 0.0),
+                                   dflt(p->densityb, i, 0.0));
+        } else {
+          H[g] = make_double4_32a(dflt(p->vb, 3 * i, 0.0), dflt(p->vb, 3 * i + 1, 0.0), dflt(p->vb, 3 * i + 2, 0.0),
+                                  dflt(p->densityb, i, 0.0));
+        }
+        orig[g] = (int)g;
+        if (dyn_mu) mu[g] = dflt(p->mu, i, 0.0);
       }
-      orig[i] = (int)i;
     }
     CUDA_TRY(c, cudaMemcpy(c->PA.X4, X.data(), N * sizeof(double4_32a), cudaMemcpyHostToDevice));
     CUDA_TRY(c, cudaMemcpy(c->PA.V4, V.data(), N * sizeof(double4_32a), cudaMemcpyHostToDevice));
@@ -573,63 +625,61 @@ psph_status psph_upload(psph_ctx* c, const psph_particles* p, int initial) {
     if (lf) CUDA_TRY(c, cudaMemcpy(c->PA.H4b, Hb.data(), N * sizeof(double4_32a), cudaMemcpyHostToDevice));
     CUDA_TRY(c, cudaMemcpy(c->PA.cls, cls.data(), N * sizeof(int), cudaMemcpyHostToDevice));
     CUDA_TRY(c, cudaMemcpy(c->PA.orig, orig.data(), N * sizeof(int), cudaMemcpyHostToDevice));
-    if (dyn_mu) {
-      std::vector<double> mu(N);
-      for (int64_t i = 0; i < n; ++i) mu[i] = dflt(p->mu, i, 0.0);
-      CUDA_TRY(c, cudaMemcpy(c->PA.mu, mu.data(), N * sizeof(double), cudaMemcpyHostToDevice));
-    }
+    if (dyn_mu) CUDA_TRY(c, cudaMemcpy(c->PA.mu, mu.data(), N * sizeof(double), cudaMemcpyHostToDevice));
     if (o.has_solid) {
-      const double* srcs[7] = {p->sigma, lf ? p->sigmaa : p->sigmab, p->strain, lf ? p->straina : p->strainb,
-                               p->shear_stress, lf ? p->shear_stressa : p->shear_stressb, p->tir};
-      double* dsts[7] = {c->PA.sigma, c->PA.sigma_h, c->PA.strain, c->PA.strain_h, c->PA.shear, c->PA.shear_h, c->PA.tir};
-      for (int a = 0; a < 7; ++a)
-        if (srcs[a]) CUDA_TRY(c, cudaMemcpy(dsts[a], srcs[a], 9 * N * sizeof(double), cudaMemcpyHostToDevice));
+      for (int q = 0; q < ninst; ++q) {
+        const psph_particles* p = &parts[q];
+        const double* srcs[7] = {p->sigma, lf ? p->sigmaa : p->sigmab, p->strain, lf ? p->straina : p->strainb,
+                                 p->shear_stress, lf ? p->shear_stressa : p->shear_stressb, p->tir};
+        double* dsts[7] = {c->PA.sigma, c->PA.sigma_h, c->PA.strain, c->PA.strain_h,
+                           c->PA.shear, c->PA.shear_h, c->PA.tir};
+        const size_t off = 9 * (size_t)c->inst_off[q];
+        for (int a = 0; a < 7; ++a)
+          if (srcs[a])
+            CUDA_TRY(c, cudaMemcpy(dsts[a] + off, srcs[a], 9 * (size_t)p->n * sizeof(double), cudaMemcpyHostToDevice));
+      }
     }
     std::vector<uint8_t> alive(N, 1);
     CUDA_TRY(c, cudaMemcpy(c->d_alive, alive.data(), N, cudaMemcpyHostToDevice));
     CUDA_TRY(c, cudaMemcpy(c->d_cls, c->classes.data(), c->classes.size() * sizeof(PClass), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(c->d_grids, c->gdevs.data(), ninst * sizeof(GridDev), cudaMemcpyHostToDevice));
+    std::vector<InstState> is(ninst);
+    for (int q = 0; q < ninst; ++q) {
+      InstState& I = is[q];
+      std::memset(&I, 0, sizeof I);
+      const psph_integrator& it = c->integ[q];
+      I.time = it.time;
+      I.deltat = it.deltat;
+      I.deltatint = it.deltatint;
+      I.deltatmin = it.deltatmin;
+      I.steps = it.steps;
+      I.first_step = it.first_step;
+      I.ct = it.ct;
+      I.shepard_counter = it.shepard_counter;
+      I.t_stop = 1e300;
+    }
+    CUDA_TRY(c, cudaMemcpy(c->d_inst, is.data(), ninst * sizeof(InstState), cudaMemcpyHostToDevice));
     StepScalars sc;
     std::memset(&sc, 0, sizeof sc);
-    sc.time = c->integ.time;
-    sc.deltat = c->integ.deltat;
-    sc.deltatint = c->integ.deltatint;
-    sc.deltatmin = c->integ.deltatmin;
-    sc.steps = c->integ.steps;
-    sc.first_step = c->integ.first_step;
-    sc.ct = c->integ.ct;
-    sc.shepard_counter = c->integ.shepard_counter;
-    sc.n = (int)n;
-    sc.n_total = (int)n;
+    sc.n = (int)ntot;
+    sc.n_total = (int)ntot;
     sc.buf = 0;
-    sc.t_stop = 1e300;
     CUDA_TRY(c, cudaMemcpy(c->d_sc, &sc, sizeof sc, cudaMemcpyHostToDevice));
   }
   c->uploaded = true;
   return PSPH_OK;
 }
 
-psph_status psph_step(psph_ctx* c, int64_t nsteps, double t_stop, int64_t* steps_done) {
+psph_status step_impl(psph_ctx* c, int64_t nsteps, const double* t_stop, double t_all, int64_t* steps_done) {
   if (!c) return PSPH_ERR_INVALID_ARGUMENT;
-  if (steps_done) *steps_done = 0;
+  if (steps_done)
+    for (int q = 0; q < c->ninst; ++q) steps_done[q] = 0;
   if (!c->uploaded) return set_err(c, PSPH_ERR_STATE, "psph_step before psph_upload");
   psph_status st;
-  if (nsteps <= 0) {
-    if (!c->timing && !c->graph) {
-      cudaGraph_t g;
-      CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-      enqueue_step(c);
-      cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
-      if (ce != cudaSuccess) return set_err(c, PSPH_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
-      ce = cudaGraphInstantiate(&c->graph, g, 0);
-      cudaGraphDestroy(g);
-      if (ce != cudaSuccess) return set_err(c, PSPH_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
-    }
-    return PSPH_OK;
-  }
-  if ((st = sync_scalars(c))) return st;
-  const long long steps0 = c->h_sc->steps;
-  arm_kernel<<<1, 1, 0, c->stream>>>(c->d_sc, t_stop);
-  CUDA_TRY(c, cudaGetLastError());
+  if (nsteps <= 0) return c->timing ? PSPH_OK : build_graph(c);
+  if ((st = arm(c, t_stop, t_all))) return st;
+  std::vector<long long> steps0(c->ninst);
+  for (int q = 0; q < c->ninst; ++q) steps0[q] = c->h_inst[q].steps;
   for (int e = 0; e < 5; ++e) c->phase_ms[e] = 0.0;
   long long launched = 0;
   if (c->timing) {
@@ -644,19 +694,10 @@ psph_status psph_step(psph_ctx* c, int64_t nsteps, double t_stop, int64_t* steps
       }
       launched += launches_per_step(view(c));
       if ((st = sync_scalars(c))) return st;
-      if (c->h_sc->stop) break;
+      if (c->h_sc->all_stop) break;
     }
   } else {
-    if (!c->graph) {
-      cudaGraph_t g;
-      CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-      enqueue_step(c);
-      cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
-      if (ce != cudaSuccess) return set_err(c, PSPH_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
-      ce = cudaGraphInstantiate(&c->graph, g, 0);
-      cudaGraphDestroy(g);
-      if (ce != cudaSuccess) return set_err(c, PSPH_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
-    }
+    if ((st = build_graph(c))) return st;
     int64_t left = nsteps;
     while (left > 0) {
       const int64_t chunk = std::min<int64_t>(left, 256);
@@ -664,12 +705,12 @@ psph_status psph_step(psph_ctx* c, int64_t nsteps, double t_stop, int64_t* steps
       left -= chunk;
       launched += chunk * launches_per_step(view(c));
       if ((st = sync_scalars(c))) return st;
-      if (c->h_sc->stop || c->h_sc->status) break;
+      if (c->h_sc->all_stop || c->h_sc->status) break;
     }
   }
   if ((st = sync_scalars(c))) return st;
-  const long long done = c->h_sc->steps - steps0;
-  if (steps_done) *steps_done = done;
+  if (steps_done)
+    for (int q = 0; q < c->ninst; ++q) steps_done[q] = c->h_inst[q].steps - steps0[q];
   c->last_launches = launched;
   const uint32_t status = c->h_sc->status;
   if (status & ST_DT_COLLAPSE)
@@ -681,40 +722,45 @@ psph_status psph_step(psph_ctx* c, int64_t nsteps, double t_stop, int64_t* steps
   return PSPH_OK;
 }
 
-int64_t psph_num_particles(const psph_ctx* c) {
-  if (!c || !c->uploaded) return 0;
-  psph_ctx* m = const_cast<psph_ctx*>(c);
-  if (sync_scalars(m)) return -1;
-  // alive slots: the last update may have flagged leavers that the next sort removes
-  std::vector<uint8_t> alive(m->h_sc->n);
-  cudaMemcpy(alive.data(), m->d_alive, alive.size(), cudaMemcpyDeviceToHost);
-  int64_t k = 0;
-  for (uint8_t a : alive) k += a;
-  return k;
-}
-
-psph_status psph_download(psph_ctx* c, psph_particles* out) {
-  if (!c || !out) return PSPH_ERR_INVALID_ARGUMENT;
-  if (!c->uploaded) return set_err(c, PSPH_ERR_STATE, "psph_download before psph_upload");
+// Alive particles of instance q in original order: (original index, slot).
+// Slots flagged by the last update as leaving stay out (the next sort drops them).
+psph_status alive_of(psph_ctx* c, int q, std::vector<std::pair<int, int>>& order, std::vector<int>* cls_out) {
   psph_status st;
   if ((st = sync_scalars(c))) return st;
   const StepScalars sc = *c->h_sc;
   const size_t n = (size_t)sc.n;
   const Persist& P = sc.buf ? c->PB : c->PA;
-  const Options& o = c->opt;
-  const bool lf = (o.scheme == PSPH_LEAPFROG);
   std::vector<uint8_t> alive(n);
-  std::vector<int> orig(n), cls(n);
+  std::vector<int> orig(n);
   CUDA_TRY(c, cudaMemcpy(alive.data(), c->d_alive, n, cudaMemcpyDeviceToHost));
   CUDA_TRY(c, cudaMemcpy(orig.data(), P.orig, n * sizeof(int), cudaMemcpyDeviceToHost));
-  CUDA_TRY(c, cudaMemcpy(cls.data(), P.cls, n * sizeof(int), cudaMemcpyDeviceToHost));
-  std::vector<std::pair<int, int>> order;
-  order.reserve(n);
+  if (cls_out) {
+    cls_out->resize(n);
+    CUDA_TRY(c, cudaMemcpy(cls_out->data(), P.cls, n * sizeof(int), cudaMemcpyDeviceToHost));
+  }
+  const int64_t lo = c->inst_off[q], hi = c->inst_off[q + 1];
+  order.clear();
   for (size_t s = 0; s < n; ++s)
-    if (alive[s]) order.emplace_back(orig[s], (int)s);
+    if (alive[s] && orig[s] >= lo && orig[s] < hi) order.emplace_back(orig[s], (int)s);
   std::sort(order.begin(), order.end());
+  return PSPH_OK;
+}
+
+psph_status download_impl(psph_ctx* c, int q, psph_particles* out) {
+  if (!c || !out) return PSPH_ERR_INVALID_ARGUMENT;
+  if (!c->uploaded) return set_err(c, PSPH_ERR_STATE, "psph_download before psph_upload");
+  if (q < 0 || q >= c->ninst) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "instance %d out of range", q);
+  std::vector<std::pair<int, int>> order;
+  std::vector<int> cls;
+  psph_status st;
+  if ((st = alive_of(c, q, order, &cls))) return st;
+  const size_t n = (size_t)c->h_sc->n;
+  const Persist& P = c->h_sc->buf ? c->PB : c->PA;
+  const Options& o = c->opt;
+  const bool lf = (o.scheme == PSPH_LEAPFROG);
   const int64_t m = (int64_t)order.size();
-  if (out->n < m) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "output holds %lld particles, need %lld", (long long)out->n, (long long)m);
+  if (out->n < m)
+    return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "output holds %lld particles, need %lld", (long long)out->n, (long long)m);
   out->n = m;
   auto fetch4 = [&](const double4_32a* src, std::vector<double4_32a>& dst) -> psph_status {
     dst.resize(n);
@@ -727,35 +773,35 @@ psph_status psph_download(psph_ctx* c, psph_particles* out) {
     return PSPH_OK;
   };
   std::vector<double4_32a> b4;
-  auto put4 = [&](double* vec3, double* scal, bool xyz) {
+  auto put4 = [&](double* vec3, double* scal) {
     for (int64_t r = 0; r < m; ++r) {
-      const double4_32a q = b4[order[r].second];
-      if (vec3 && xyz) {
-        vec3[3 * r] = q.x;
-        vec3[3 * r + 1] = q.y;
-        vec3[3 * r + 2] = q.z;
+      const double4_32a w = b4[order[r].second];
+      if (vec3) {
+        vec3[3 * r] = w.x;
+        vec3[3 * r + 1] = w.y;
+        vec3[3 * r + 2] = w.z;
       }
-      if (scal) scal[r] = q.w;
+      if (scal) scal[r] = w.w;
     }
   };
-  if (out->x || out->density) { if ((st = fetch4(P.X4, b4))) return st; put4(out->x, out->density, true); }
-  if (out->v || out->pressure) { if ((st = fetch4(P.V4, b4))) return st; put4(out->v, out->pressure, true); }
+  if (out->x || out->density) { if ((st = fetch4(P.X4, b4))) return st; put4(out->x, out->density); }
+  if (out->v || out->pressure) { if ((st = fetch4(P.V4, b4))) return st; put4(out->v, out->pressure); }
   if (lf) {
-    if (out->va || out->densitya) { if ((st = fetch4(P.H4, b4))) return st; put4(out->va, out->densitya, true); }
-    if (out->vb || out->densityb) { if ((st = fetch4(P.H4b, b4))) return st; put4(out->vb, out->densityb, true); }
+    if (out->va || out->densitya) { if ((st = fetch4(P.H4, b4))) return st; put4(out->va, out->densitya); }
+    if (out->vb || out->densityb) { if ((st = fetch4(P.H4b, b4))) return st; put4(out->vb, out->densityb); }
   } else {
-    if (out->vb || out->densityb) { if ((st = fetch4(P.H4, b4))) return st; put4(out->vb, out->densityb, true); }
+    if (out->vb || out->densityb) { if ((st = fetch4(P.H4, b4))) return st; put4(out->vb, out->densityb); }
   }
-  if (out->a || out->ddensity) { if ((st = fetch4(c->S.A4, b4))) return st; put4(out->a, out->ddensity, true); }
-  if (out->nsv) { if ((st = fetch4(c->S.nsv4, b4))) return st; put4(out->nsv, nullptr, true); }
-  if (out->vxsph) { if ((st = fetch4(c->S.vxsph4, b4))) return st; put4(out->vxsph, nullptr, true); }
+  if (out->a || out->ddensity) { if ((st = fetch4(c->S.A4, b4))) return st; put4(out->a, out->ddensity); }
+  if (out->nsv) { if ((st = fetch4(c->S.nsv4, b4))) return st; put4(out->nsv, nullptr); }
+  if (out->vxsph) { if ((st = fetch4(c->S.vxsph4, b4))) return st; put4(out->vxsph, nullptr); }
   std::vector<double> b;
   auto put = [&](double* dst, size_t per) {
     for (int64_t r = 0; r < m; ++r)
       for (size_t e = 0; e < per; ++e) dst[per * r + e] = b[per * order[r].second + e];
   };
   struct Src { double* out; const double* dev; size_t per; };
-  const Src scalars[] = {
+  const Src fields[] = {
       {out->zwab, c->S.zwab, 1}, {out->sumden, c->S.sumden, 1}, {out->sumkernel, c->S.sumkernel, 1},
       {out->shear_rate, c->S.shear_rate, 1}, {out->sbar, c->S.sbar, 1},
       {out->mu, o.dyn_mu ? P.mu : nullptr, 1},
@@ -763,15 +809,15 @@ psph_status psph_download(psph_ctx* c, psph_particles* out) {
       {out->sigma, P.sigma, 9}, {out->strain, P.strain, 9}, {out->shear_stress, P.shear, 9}, {out->tir, P.tir, 9},
       {lf ? out->sigmaa : out->sigmab, P.sigma_h, 9}, {lf ? out->sigmab : nullptr, c->S.sigma_o, 9},
       {lf ? out->straina : out->strainb, P.strain_h, 9}, {lf ? out->strainb : nullptr, c->S.strain_o, 9},
-      {lf ? out->shear_stressa : out->shear_stressb, P.shear_h, 9}, {lf ? out->shear_stressb : nullptr, c->S.shear_o, 9},
+      {lf ? out->shear_stressa : out->shear_stressb, P.shear_h, 9},
+      {lf ? out->shear_stressb : nullptr, c->S.shear_o, 9},
   };
-  for (const Src& s : scalars) {
+  for (const Src& s : fields) {
     if (!s.out || !s.dev) continue;
     if ((st = fetch(s.dev, s.per, b))) return st;
     put(s.out, s.per);
   }
-  // class constants
-  for (int64_t r = 0; r < m; ++r) {
+  for (int64_t r = 0; r < m; ++r) {  // class constants
     const PClass& C = c->classes[cls[order[r].second]];
     if (out->id) out->id[r] = C.id;
     if (out->material) out->material[r] = C.material;
@@ -808,42 +854,16 @@ psph_status psph_download(psph_ctx* c, psph_particles* out) {
   return PSPH_OK;
 }
 
-psph_status psph_original_index(psph_ctx* c, int64_t* out) {
-  if (!c || !out) return PSPH_ERR_INVALID_ARGUMENT;
-  if (!c->uploaded) return set_err(c, PSPH_ERR_STATE, "psph_original_index before psph_upload");
-  psph_status st;
-  if ((st = sync_scalars(c))) return st;
-  const StepScalars sc = *c->h_sc;
-  const size_t n = (size_t)sc.n;
-  const Persist& P = sc.buf ? c->PB : c->PA;
-  std::vector<uint8_t> alive(n);
-  std::vector<int> orig(n);
-  CUDA_TRY(c, cudaMemcpy(alive.data(), c->d_alive, n, cudaMemcpyDeviceToHost));
-  CUDA_TRY(c, cudaMemcpy(orig.data(), P.orig, n * sizeof(int), cudaMemcpyDeviceToHost));
-  std::vector<int> kept;
-  for (size_t s = 0; s < n; ++s)
-    if (alive[s]) kept.push_back(orig[s]);
-  std::sort(kept.begin(), kept.end());
-  for (size_t r = 0; r < kept.size(); ++r) out[r] = kept[r];
-  return PSPH_OK;
-}
-
-psph_status psph_get_grid(const psph_ctx* c, psph_grid* g) {
-  if (!c || !g) return PSPH_ERR_INVALID_ARGUMENT;
-  *g = c->grid;
-  return PSPH_OK;
-}
-
-psph_status psph_get_integrator(const psph_ctx* c, psph_integrator* it) {
+psph_status integrator_impl(psph_ctx* c, int q, psph_integrator* it) {
   if (!c || !it) return PSPH_ERR_INVALID_ARGUMENT;
+  if (q < 0 || q >= c->ninst) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "instance %d out of range", q);
   if (!c->uploaded) {
-    *it = c->integ;
+    *it = c->integ[q];
     return PSPH_OK;
   }
-  psph_ctx* m = const_cast<psph_ctx*>(c);
-  psph_status st = sync_scalars(m);
+  psph_status st = sync_scalars(c);
   if (st) return st;
-  const StepScalars& s = *m->h_sc;
+  const InstState& s = c->h_inst[q];
   it->time = s.time;
   it->deltat = s.deltat;
   it->deltatint = s.deltatint;
@@ -856,11 +876,120 @@ psph_status psph_get_integrator(const psph_ctx* c, psph_integrator* it) {
   return PSPH_OK;
 }
 
+int64_t num_particles_impl(psph_ctx* c, int q) {
+  if (!c || !c->uploaded || q < 0 || q >= c->ninst) return 0;
+  std::vector<std::pair<int, int>> order;
+  if (alive_of(c, q, order, nullptr)) return -1;
+  return (int64_t)order.size();
+}
+
+psph_status original_index_impl(psph_ctx* c, int q, int64_t* out) {
+  if (!c || !out) return PSPH_ERR_INVALID_ARGUMENT;
+  if (!c->uploaded) return set_err(c, PSPH_ERR_STATE, "psph_original_index before psph_upload");
+  if (q < 0 || q >= c->ninst) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "instance %d out of range", q);
+  std::vector<std::pair<int, int>> order;
+  psph_status st = alive_of(c, q, order, nullptr);
+  if (st) return st;
+  const int64_t base = c->inst_off[q];
+  for (size_t r = 0; r < order.size(); ++r) out[r] = order[r].first - base;
+  return PSPH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int psph_abi_version(void) { return PSPH_ABI_VERSION; }
+
+psph_status psph_device_check(int* device_count) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) n = 0;
+  if (device_count) *device_count = n;
+  if (n < 1) return PSPH_ERR_NO_DEVICE;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, 0) != cudaSuccess) return PSPH_ERR_NO_DEVICE;
+  if (!(prop.major == 10 && prop.minor == 3)) return PSPH_ERR_NO_DEVICE;  // built for sm_103a only
+  return PSPH_OK;
+}
+
+psph_status psph_create(const psph_config* cfg, psph_ctx** out) { return create_impl(cfg, 1, out); }
+
+void psph_destroy(psph_ctx* c) {
+  if (!c) return;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  free_all(c);
+  for (int i = 0; i < 6; ++i)
+    if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char* psph_last_error(const psph_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+psph_status psph_set_stream(psph_ctx* c, void* s) {
+  if (!c) return PSPH_ERR_INVALID_ARGUMENT;
+  if (c->graph) {
+    cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+  }
+  if (s) {
+    if (c->own_stream) cudaStreamDestroy(c->stream);
+    c->stream = (cudaStream_t)s;
+    c->own_stream = false;
+  }
+  return PSPH_OK;
+}
+
+psph_status psph_set_grid(psph_ctx* c, const psph_grid* g) {
+  if (!c || !g) return PSPH_ERR_INVALID_ARGUMENT;
+  if (c->uploaded) return set_err(c, PSPH_ERR_STATE, "psph_set_grid must come before psph_upload");
+  if (c->ninst != 1) return set_err(c, PSPH_ERR_STATE, "psph_set_grid applies to single-domain contexts");
+  c->grids[0] = *g;
+  c->grid_set = true;
+  return PSPH_OK;
+}
+
+psph_status psph_set_integrator(psph_ctx* c, const psph_integrator* it) {
+  if (!c || !it) return PSPH_ERR_INVALID_ARGUMENT;
+  if (c->uploaded) return set_err(c, PSPH_ERR_STATE, "psph_set_integrator must come before psph_upload");
+  if (c->ninst != 1) return set_err(c, PSPH_ERR_STATE, "psph_set_integrator applies to single-domain contexts");
+  c->integ[0] = *it;
+  c->integ_set = true;
+  return PSPH_OK;
+}
+
+psph_status psph_upload(psph_ctx* c, const psph_particles* p, int initial) {
+  if (c && c->ninst != 1) return set_err(c, PSPH_ERR_STATE, "an ensemble context takes psph_batch_upload");
+  return upload_impl(c, p, initial);
+}
+
+psph_status psph_step(psph_ctx* c, int64_t nsteps, double t_stop, int64_t* steps_done) {
+  if (c && c->ninst != 1) return set_err(c, PSPH_ERR_STATE, "an ensemble context takes psph_batch_step");
+  return step_impl(c, nsteps, nullptr, t_stop, steps_done);
+}
+
+int64_t psph_num_particles(const psph_ctx* c) { return num_particles_impl(const_cast<psph_ctx*>(c), 0); }
+
+psph_status psph_download(psph_ctx* c, psph_particles* out) { return download_impl(c, 0, out); }
+
+psph_status psph_original_index(psph_ctx* c, int64_t* out) { return original_index_impl(c, 0, out); }
+
+psph_status psph_get_grid(const psph_ctx* c, psph_grid* g) {
+  if (!c || !g) return PSPH_ERR_INVALID_ARGUMENT;
+  *g = c->grids[0];
+  return PSPH_OK;
+}
+
+psph_status psph_get_integrator(const psph_ctx* c, psph_integrator* it) {
+  return integrator_impl(const_cast<psph_ctx*>(c), 0, it);
+}
+
 psph_status psph_pairs_export(psph_ctx* c, int which, int64_t* pairs, int64_t cap, int64_t* n_total) {
   if (!c || (which != 0 && which != 1)) return PSPH_ERR_INVALID_ARGUMENT;
   if (!c->uploaded) return set_err(c, PSPH_ERR_STATE, "psph_pairs_export before psph_upload");
+  if (c->ninst != 1) return set_err(c, PSPH_ERR_STATE, "psph_pairs_export applies to single-domain contexts");
   // cell-sort the current positions (does not change the physical state)
-  arm_kernel<<<1, 1, 0, c->stream>>>(c->d_sc, 1e300);
+  rearm_kernel<<<1, 256, 0, c->stream>>>(c->d_inst, c->ninst, c->d_sc);
   const DevView v = view(c);
   launch_sort(v, c->stream);
   unsigned long long* d_counter = nullptr;
@@ -909,12 +1038,11 @@ psph_status psph_step_timed(psph_ctx* c, int64_t nsteps, double* device_ms, int6
   CUDA_TRY(c, cudaEventCreate(&e0));
   CUDA_TRY(c, cudaEventCreate(&e1));
   // make sure the graph exists before the timed region
-  if (!c->graph) {
-    psph_status st = psph_step(c, 0, 1e300, nullptr);
-    if (st) return st;
-  }
+  psph_status st = build_graph(c);
+  if (st) return st;
+  std::vector<int64_t> done(c->ninst, 0);
   CUDA_TRY(c, cudaEventRecord(e0, c->stream));
-  psph_status st = psph_step(c, nsteps, 1e300, steps_done);
+  st = step_impl(c, nsteps, nullptr, 1e300, done.data());
   cudaEventRecord(e1, c->stream);
   cudaEventSynchronize(e1);
   float ms = 0.f;
@@ -923,6 +1051,7 @@ psph_status psph_step_timed(psph_ctx* c, int64_t nsteps, double* device_ms, int6
   cudaEventDestroy(e1);
   c->timing = was;
   *device_ms = ms;
+  if (steps_done) *steps_done = done[0];
   return st;
 }
 
@@ -936,6 +1065,94 @@ psph_status psph_pair_count(psph_ctx* c, uint64_t* pairs) {
   if (st) return st;
   *pairs = c->h_sc->pairs_x2 / 2;
   return PSPH_OK;
+}
+
+// ---- learned closure -----------------------------------------------------------
+
+psph_status psph_closure_attach(psph_ctx* c, const psph_mlp* mlp, double dx) {
+  if (!c || !mlp || !(dx > 0.0)) return PSPH_ERR_INVALID_ARGUMENT;
+  if (!c->uploaded) return set_err(c, PSPH_ERR_STATE, "psph_closure_attach before psph_upload");
+  const MlpImage* img = nullptr;
+  psph_status st = psph_mlp_image(mlp, &img);
+  if (st) return set_err(c, st, "closure network: %s", psph_mlp_last_error(mlp));
+  const size_t N = (size_t)c->ncap;
+  if (!c->d_mlp) {
+    if ((st = dalloc(c, &c->d_mlp, 1)) || (st = dalloc(c, &c->S.cvort, N)) || (st = dalloc(c, &c->S.cnnb, N)) ||
+        (st = dalloc(c, &c->S.cfeat, 6 * N)) || (st = dalloc(c, &c->S.nut, N)))
+      return st;
+  }
+  CUDA_TRY(c, cudaMemcpy(c->d_mlp, img, sizeof(MlpImage), cudaMemcpyDeviceToDevice));
+  c->opt.closure = 1;
+  c->opt.closure_dx = dx;
+  if ((st = sync_scalars(c))) return st;
+  c->h_sc->closure_eval = 0;
+  c->h_sc->closure_fallback = 0;
+  CUDA_TRY(c, cudaMemcpy(c->d_sc, c->h_sc, sizeof(StepScalars), cudaMemcpyHostToDevice));
+  if (c->graph) {  // the step sequence changes: capture it again
+    cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+  }
+  return PSPH_OK;
+}
+
+psph_status psph_closure_stats(psph_ctx* c, uint64_t* evaluated, uint64_t* fallbacks) {
+  if (!c) return PSPH_ERR_INVALID_ARGUMENT;
+  if (!c->uploaded) return set_err(c, PSPH_ERR_STATE, "psph_closure_stats before psph_upload");
+  psph_status st = sync_scalars(c);
+  if (st) return st;
+  if (evaluated) *evaluated = c->h_sc->closure_eval;
+  if (fallbacks) *fallbacks = c->h_sc->closure_fallback;
+  return PSPH_OK;
+}
+
+psph_status psph_closure_features(psph_ctx* c, float* out) {
+  if (!c || !out) return PSPH_ERR_INVALID_ARGUMENT;
+  if (!c->opt.closure) return set_err(c, PSPH_ERR_STATE, "no closure attached");
+  std::vector<std::pair<int, int>> order;
+  psph_status st = alive_of(c, 0, order, nullptr);
+  if (st) return st;
+  const size_t n = (size_t)c->h_sc->n;
+  std::vector<float> f(6 * n);
+  CUDA_TRY(c, cudaMemcpy(f.data(), c->S.cfeat, 6 * n * sizeof(float), cudaMemcpyDeviceToHost));
+  for (size_t r = 0; r < order.size(); ++r)
+    for (int k = 0; k < 6; ++k) out[6 * r + k] = f[6 * (size_t)order[r].second + k];
+  return PSPH_OK;
+}
+
+// ---- ensembles ---------------------------------------------------------------
+
+psph_status psph_batch_create(const psph_config* cfgs, int ninst, psph_ctx** out) {
+  return create_impl(cfgs, ninst, out);
+}
+
+int psph_batch_size(const psph_ctx* c) { return c ? c->ninst : 0; }
+
+psph_status psph_batch_upload(psph_ctx* c, const psph_particles* parts, int initial) {
+  return upload_impl(c, parts, initial);
+}
+
+psph_status psph_batch_step(psph_ctx* c, int64_t nsteps, const double* t_stop, int64_t* steps_done) {
+  return step_impl(c, nsteps, t_stop, 1e300, steps_done);
+}
+
+int64_t psph_batch_num_particles(const psph_ctx* c, int inst) {
+  return num_particles_impl(const_cast<psph_ctx*>(c), inst);
+}
+
+psph_status psph_batch_download(psph_ctx* c, int inst, psph_particles* out) { return download_impl(c, inst, out); }
+
+psph_status psph_batch_original_index(psph_ctx* c, int inst, int64_t* out) {
+  return original_index_impl(c, inst, out);
+}
+
+psph_status psph_batch_get_grid(const psph_ctx* c, int inst, psph_grid* g) {
+  if (!c || !g || inst < 0 || inst >= c->ninst) return PSPH_ERR_INVALID_ARGUMENT;
+  *g = c->grids[inst];
+  return PSPH_OK;
+}
+
+psph_status psph_batch_get_integrator(const psph_ctx* c, int inst, psph_integrator* it) {
+  return integrator_impl(const_cast<psph_ctx*>(c), inst, it);
 }
 
 }  // extern "C"
@@ -990,6 +1207,7 @@ extern "C" psph_status psph_pairs_export_noalloc(psph_ctx* c, int which, int64_t
                                                  int64_t* n_total) {
   if (!c || (which != 0 && which != 1) || cap < 0 || (cap > 0 && !pairs_device)) return PSPH_ERR_INVALID_ARGUMENT;
   if (!c->uploaded) return set_err(c, PSPH_ERR_STATE, "psph_pairs_export_noalloc before psph_upload");
+  if (c->ninst != 1) return set_err(c, PSPH_ERR_STATE, "psph_pairs_export_noalloc applies to single-domain contexts");
   if (c->ncap > PSPH_NOALLOC_MAX_PARTICLES)
     return set_err(c, PSPH_ERR_INVALID_ARGUMENT,
                    "psph_pairs_export_noalloc handles at most %d particles (context holds %d); use psph_pairs_export",
@@ -1001,7 +1219,7 @@ extern "C" psph_status psph_pairs_export_noalloc(psph_ctx* c, int which, int64_t
   int* offsets = scratch + PSPH_NOALLOC_MAX_PARTICLES;
   int* block_sums = offsets + PSPH_NOALLOC_MAX_PARTICLES + 1;
   cudaStream_t s = c->stream;
-  arm_kernel<<<1, 1, 0, s>>>(c->d_sc, 1e300);
+  rearm_kernel<<<1, 256, 0, s>>>(c->d_inst, c->ninst, c->d_sc);
   const DevView v = view(c);
   launch_sort(v, s);                                   // cell list of the current positions
   launch_pairs_count(v, which, counts, s);             // pairs each sorted particle lists first

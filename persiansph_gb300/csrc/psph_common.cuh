@@ -28,13 +28,14 @@ enum : uint32_t {
   ST_DT_COLLAPSE = 1u << 1,
   ST_OUT_OF_GRID = 1u << 2,
   ST_CELL_OVERFLOW = 1u << 3,
+  ST_CLOSURE_TIMEOUT = 1u << 4,  // a tensor-core wait of the closure kernel gave up
 };
 
 // Constant per-particle parameters, shared by all particles of one class.
 struct PClass {
   double cs, p0, rho0, fpmassc, alpha, beta, mu0, mu_ref, t0, bm, csmag, ti, tin, tid;
   double g_mod, k_mod, sigmay, coh, phi, psi, h, mass;
-  int material, is_free, no_slip, pres_eq, shepard, les, vis_m, fail, id, pad;
+  int material, is_free, no_slip, pres_eq, shepard, les, vis_m, fail, id, inst;
 };
 
 // FP32 copy of the class constants used inside the FP32C pair loops (so those
@@ -42,23 +43,31 @@ struct PClass {
 struct PClass32 {
   float mass, h, fpmassc, alpha, beta, mu0, ti, tin, tid, cs, rho0, p0;
   int flags;  // bit 0 free, 1 no-slip, 2 LES, 3 Shepard, 4 T0>0, 5 TI>0
-  int material, pres_eq, pad;
+  int material, pres_eq, inst;
 };
 enum : int { CF_FREE = 1, CF_NOSLIP = 2, CF_LES = 4, CF_SHEPARD = 8, CF_T0 = 16, CF_TI = 32 };
 
-// Domain scalars advanced on the device.
-struct StepScalars {
-  double time, deltat, deltatint, deltatmin;
-  double t_stop;
+// Per-instance (per-domain) scalars advanced on the device. A context holds one
+// instance for a single Domain, or many independent instances for an ensemble.
+struct InstState {
+  double time, deltat, deltatint, deltatmin, t_stop;
   long long steps;
+  unsigned long long dtmin_bits;  // running minimum of the acceleration time-step bound (ordered bits)
   int first_step, ct, shepard_counter, stop;
-  int n;          // particles alive (cells + orphans)
+};
+
+// Context-wide scalars.
+struct StepScalars {
+  int n;          // particles alive (cells + orphans), all instances
   int n_cells;    // particles inside cells
-  int n_total;    // particles in the buffers (alive + dead)
+  int n_total;
   uint32_t status;
-  int launches;
+  int all_stop;   // every instance has reached its stop time
   int buf;        // which persistent buffer (A=0 / B=1) holds the current sorted state
   unsigned long long pairs_x2;  // 2 x pair-interactions evaluated since upload
+  unsigned int work;            // tile counter of the persistent pair kernels
+  int launches;
+  unsigned long long closure_eval, closure_fallback;  // closure evaluations / Smagorinsky fallbacks
 };
 
 struct GridDev {
@@ -68,6 +77,7 @@ struct GridDev {
   int cn_ref[3];  // Domain::CellNo (ghost columns included)
   int periodic[3];
   int ncells;     // nc[0]*nc[1]*nc[2]
+  int cell_base;  // first global cell id of this instance
 };
 
 // ---------------------------------------------------------------------------

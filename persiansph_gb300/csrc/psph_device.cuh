@@ -33,7 +33,6 @@ struct Scratch {
   int* perm;
   int* cellid;     // cell of each sorted particle (orphan/dead: -1)
   int* block_sums;
-  double* blockmin;
   // per-step derived / outputs
   float4* OFF32;     // (position - cell origin, h) in FP32, written by the reorder
   int* nl;           // per-step neighbour lists, entry k of particle i at nl[k*ncap + i]:
@@ -56,6 +55,11 @@ struct Scratch {
   double* sigma_o;       // leapfrog Sigmab | MVerlet Sigmaa: per-step output only (9 per particle)
   double* strain_o;      // leapfrog Strainb | MVerlet Straina
   double* shear_o;       // leapfrog ShearStressb | MVerlet ShearStressa
+  // learned closure (allocated when attached)
+  float* cvort;          // |vorticity| from the pair sums
+  float* cnnb;           // neighbours inside the support
+  float* cfeat;          // raw network features, 6 per particle
+  double* nut;           // eddy viscosity from the network; -1 = use Smagorinsky
 };
 
 struct Options {
@@ -79,21 +83,29 @@ struct Options {
   double gravity[3], body_force[3];
   int shepard_step;
   int nclasses;
+  int closure;        // learned eddy-viscosity closure attached
+  double closure_dx;  // lattice spacing of its h/dx feature
 };
 
 // Everything a launch needs, passed by value to the launch wrappers.
 struct DevView {
-  GridDev g;
+  const GridDev* grids;   // per instance (device array)
+  InstState* inst;        // per instance
+  int ninst;
+  int total_cells;        // sum of the instances' cells
   Options o;
   Persist PA, PB; // double-buffered persistent arrays; StepScalars::buf says which is current
   Scratch S;
   const PClass* cls;
   const PClass32* cls32;
+  const void* mlp;        // closure network image (MlpImage), when attached
   StepScalars* sc;
   uint8_t* alive;
   int ncap;
   int nclasses;
 };
+
+PSPH_D const GridDev& grid_of(const DevView& v, int inst) { return v.grids[inst]; }
 
 PSPH_D const Persist& cur_persist(const DevView& v) { return v.sc->buf ? v.PB : v.PA; }
 PSPH_D const Persist& next_persist(const DevView& v) { return v.sc->buf ? v.PA : v.PB; }
@@ -110,6 +122,7 @@ void launch_dt(const DevView& v, cudaStream_t st);        // dt reduction + Adap
 void launch_update(const DevView& v, cudaStream_t st);    // Move + material update + periodic wrap + leave
 void launch_begin(const DevView& v, cudaStream_t st);     // stop test, first-step counters
 void launch_end(const DevView& v, cudaStream_t st);       // time, counters
+void launch_closure(const DevView& v, cudaStream_t st);   // learned eddy viscosity (tcgen05 MLP)
 int forces_blocks(int ncap);
 int launches_per_step(const DevView& v);
 void launch_pairs_export(const DevView& v, int which, long long* out, long long cap, unsigned long long* counter,

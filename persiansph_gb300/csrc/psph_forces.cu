@@ -92,14 +92,16 @@ template <int DIM, int KT>
 __global__ void __launch_bounds__(kFT) prepare_wall_kernel(DevView v) {
   __shared__ int qbuf[kQN][kFT];
   const StepScalars* sc = v.sc;
-  if (sc->stop) return;
+  if (sc->all_stop) return;
   const Persist& P = cur_persist(v);
   const int n = sc->n;
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
   const int tid = threadIdx.x;
-  const GridDev& g = v.g;
   const Options& o = v.o;
   const PClass* __restrict__ CT = v.cls;
+  const int winst = (w < n) ? CT[P.cls[w]].inst : 0;
+  const GridDev& g = grid_of(v, winst);
+  const bool run = (w < n) && !v.inst[winst].stop;
   bool wall = false;
   int mat = 0;
   double sk = 0.0, p = 0.0, n0 = 0.0, n1 = 0.0, n2 = 0.0;
@@ -110,7 +112,7 @@ __global__ void __launch_bounds__(kFT) prepare_wall_kernel(DevView v) {
   int ow = 0, cell = -1;
   double hw = 0.0;
   bool noslip = false;
-  if (w < n) {
+  if (run) {
     const PClass& Cw = CT[P.cls[w]];
     if (Cw.is_free) {
       const double rho = P.X4[w].w;
@@ -134,7 +136,7 @@ __global__ void __launch_bounds__(kFT) prepare_wall_kernel(DevView v) {
   const double gx = o.gravity[0], gy = o.gravity[1], gz = o.gravity[2];
   const bool need_orient = !o.wallp_physical && (gx != 0.0 || gy != 0.0 || gz != 0.0) && mat < 3;
   NbrSource<DIM> src;
-  src.init(v, w, wall && cell >= 0, 1.004f);
+  src.init(v, g, w, wall && cell >= 0, 1.004f);
   bool more = wall && cell >= 0;
   const CellCoord cw = decode(g, cell >= 0 ? cell : 0);
   while (true) {
@@ -240,12 +242,11 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
   __shared__ unsigned long long cred[kFT / 32];
   __shared__ int qbuf[kQN][kFT];
   const StepScalars* sc = v.sc;
-  if (sc->stop) return;
+  if (sc->all_stop) return;
   const Persist& P = cur_persist(v);
   const int n = sc->n;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int tid = threadIdx.x;
-  const GridDev& g = v.g;
   const Options& o = v.o;
   const PClass* __restrict__ CT = v.cls;
   double dtc = DBL_MAX;
@@ -254,30 +255,36 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
   int cell = -1, ci_cls = 0;
   if (i < n) {
     ci_cls = P.cls[i];
-    active = CT[ci_cls].is_free;
+    const bool run = !v.inst[CT[ci_cls].inst].stop;
+    active = run && CT[ci_cls].is_free;
     cell = v.S.cellid[i];
-    if (!active) {
+    if (run && !active) {
       v.S.A4[i] = make_double4_32a(o.gravity[0], o.gravity[1], o.gravity[2], 0.0);
       v.S.zwab[i] = 1.0;
     }
   }
   const PClass& Ci = CT[ci_cls];
+  const GridDev& g = grid_of(v, Ci.inst);
+  const InstState& Is = v.inst[Ci.inst];
   const double4_32a xi = active ? P.X4[i] : make_double4_32a(0, 0, 0, 1);
   const double4_32a vi = active ? P.V4[i] : make_double4_32a(0, 0, 0, 0);
   const double4_32a di4 = active ? v.S.D4[i] : make_double4_32a(1, 0, 0, 1);
   const double di = xi.w, inv_i = di4.x, Pi = di4.y, ci_snd = di4.z, pi = vi.w;
   const double mi = Ci.mass, hi = Ci.h;
   const double mui = o.dyn_mu ? (active ? P.mu[i] : 0.0) : Ci.mu0;
-  const bool shep = Ci.shepard && (sc->shepard_counter == o.shepard_step);
+  const bool shep = Ci.shepard && (Is.shepard_counter == o.shepard_step);
   const bool sr_self = (Ci.t0 > 0.0 || Ci.les);
   double ax = o.gravity[0] + o.body_force[0], ay = o.gravity[1] + o.body_force[1],
          az = o.gravity[2] + o.body_force[2];
   double drho = 0.0, zw = 0.0, sd = 0.0, xs0 = 0.0, xs1 = 0.0, xs2 = 0.0;
   double sr0 = 0.0, sr1 = 0.0, sr2 = 0.0, sr4 = 0.0, sr5 = 0.0, sr8 = 0.0;
+  double w01 = 0.0, w02 = 0.0, w12 = 0.0;  // antisymmetric counterpart of the strain-rate sums (closure)
+  int nnb = 0;
+  const bool closure = o.closure && Ci.les;
   const bool any_periodic = g.periodic[0] | g.periodic[1] | g.periodic[2];
   CellCoord cci = decode(g, cell >= 0 ? cell : 0);
   NbrSource<DIM> src;
-  src.init(v, i, active && cell >= 0, 1.004f);
+  src.init(v, g, i, active && cell >= 0, 1.004f);
   bool more = active && cell >= 0;
   while (true) {
     int qn = 0;
@@ -312,6 +319,7 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
       if (q > g.cellfac) continue;
       const bool fj = Cj.is_free;
       npair2 += fj ? 1ull : 2ull;
+      ++nnb;
       const double4_32a vj = P.V4[j];
       const double4_32a dj4 = v.S.D4[j];
       double dj, inv_j, Pj, cj_snd;
@@ -391,6 +399,11 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
           sr4 += c2 * (2.0 * vab1 * x1);
           sr5 += c2 * (vab1 * x2 + vab2 * x1);
           sr8 += c2 * (2.0 * vab2 * x2);
+          if (closure) {
+            w01 += c2 * (vab0 * x1 - vab1 * x0);
+            w02 += c2 * (vab0 * x2 - vab2 * x0);
+            w12 += c2 * (vab1 * x2 - vab2 * x1);
+          }
         }
       }
       if (o.xsph != 0.0 && fj) {
@@ -420,30 +433,16 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
       out[3] = sr1; out[4] = sr4; out[5] = sr5;
       out[6] = sr2; out[7] = sr5; out[8] = sr8;
     }
+    if (closure) {
+      v.S.cvort[i] = (float)sqrt(w01 * w01 + w02 * w02 + w12 * w12);
+      v.S.cnnb[i] = (float)nnb;
+    }
     if (!(isfinite(ax) && isfinite(ay) && isfinite(az) && isfinite(drho))) atomicOr(&v.sc->status, ST_NONFINITE);
     const double an = sqrt(ax * ax + ay * ay + az * az);
     const double cand = o.sqrt_h_a * sqrt(hi / an);
     if (cand < dtc) dtc = cand;  // NaN never compares less, as in the reference
   }
-  for (int off = 16; off > 0; off >>= 1) {
-    dtc = fmin(dtc, __shfl_down_sync(0xffffffffu, dtc, off));
-    npair2 += __shfl_down_sync(0xffffffffu, npair2, off);
-  }
-  if ((tid & 31) == 0) {
-    red[tid >> 5] = dtc;
-    cred[tid >> 5] = npair2;
-  }
-  __syncthreads();
-  if (tid == 0) {
-    double m = red[0];
-    unsigned long long c = cred[0];
-    for (int k = 1; k < kFT / 32; ++k) {
-      m = fmin(m, red[k]);
-      c += cred[k];
-    }
-    v.S.blockmin[blockIdx.x] = m;
-    if (c) atomicAdd(&v.sc->pairs_x2, c);
-  }
+  block_dt_and_pairs<kFT>(v, Ci.inst, active, dtc, npair2, red, cred);
 }
 
 // ---------------------------------------------------------------------------
@@ -455,12 +454,11 @@ __global__ void __launch_bounds__(kFT) forces_solid_kernel(DevView v) {
   __shared__ unsigned long long cred[kFT / 32];
   __shared__ int qbuf[kQN][kFT];
   const StepScalars* sc = v.sc;
-  if (sc->stop) return;
+  if (sc->all_stop) return;
   const Persist& P = cur_persist(v);
   const int n = sc->n;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int tid = threadIdx.x;
-  const GridDev& g = v.g;
   const Options& o = v.o;
   const PClass* __restrict__ CT = v.cls;
   double dtc = DBL_MAX;
@@ -469,20 +467,23 @@ __global__ void __launch_bounds__(kFT) forces_solid_kernel(DevView v) {
   int cell = -1, ci_cls = 0;
   if (i < n) {
     ci_cls = P.cls[i];
-    active = CT[ci_cls].is_free;
+    const bool run = !v.inst[CT[ci_cls].inst].stop;
+    active = run && CT[ci_cls].is_free;
     cell = v.S.cellid[i];
-    if (!active) {
+    if (run && !active) {
       v.S.A4[i] = make_double4_32a(o.gravity[0], o.gravity[1], o.gravity[2], 0.0);
       v.S.zwab[i] = 1.0;
     }
   }
   const PClass& Ci = CT[ci_cls];
+  const GridDev& g = grid_of(v, Ci.inst);
+  const InstState& Is = v.inst[Ci.inst];
   const int is = active ? i : 0;
   const double4_32a xi = P.X4[is];
   const double4_32a vi = P.V4[is];
   const double4_32a di4 = v.S.D4[is];
   const double di = xi.w, inv_i = di4.x, mi = Ci.mass, hi = Ci.h;
-  const bool shep = Ci.shepard && (sc->shepard_counter == o.shepard_step);
+  const bool shep = Ci.shepard && (Is.shepard_counter == o.shepard_step);
   const double* __restrict__ Si = P.sigma + 9 * (size_t)is;
   const double* __restrict__ Ti = P.tir + 9 * (size_t)is;
   double ax = o.gravity[0] + o.body_force[0], ay = o.gravity[1] + o.body_force[1],
@@ -493,7 +494,7 @@ __global__ void __launch_bounds__(kFT) forces_solid_kernel(DevView v) {
   const double I22 = (DIM == 2) ? 0.0 : 1.0;  // Domain::I (Source/Domain.cpp:1665)
   CellCoord cci = decode(g, cell >= 0 ? cell : 0);
   NbrSource<DIM> src;
-  src.init(v, i, active && cell >= 0, 1.004f);
+  src.init(v, g, i, active && cell >= 0, 1.004f);
   bool more = active && cell >= 0;
   while (true) {
     int qn = 0;
@@ -634,74 +635,65 @@ __global__ void __launch_bounds__(kFT) forces_solid_kernel(DevView v) {
     const double cand = o.sqrt_h_a * sqrt(hi / an);
     if (cand < dtc) dtc = cand;
   }
-  for (int off = 16; off > 0; off >>= 1) {
-    dtc = fmin(dtc, __shfl_down_sync(0xffffffffu, dtc, off));
-    npair2 += __shfl_down_sync(0xffffffffu, npair2, off);
-  }
-  if ((tid & 31) == 0) {
-    red[tid >> 5] = dtc;
-    cred[tid >> 5] = npair2;
-  }
-  __syncthreads();
-  if (tid == 0) {
-    double m = red[0];
-    unsigned long long c = cred[0];
-    for (int k = 1; k < kFT / 32; ++k) {
-      m = fmin(m, red[k]);
-      c += cred[k];
-    }
-    v.S.blockmin[blockIdx.x] = m;
-    if (c) atomicAdd(&v.sc->pairs_x2, c);
-  }
+  block_dt_and_pairs<kFT>(v, Ci.inst, active, dtc, npair2, red, cred);
 }
 
-// dt reduction + AdaptiveTimeStep (single block).
-__global__ void dt_finalize_kernel(const double* __restrict__ blockmin, int nb, StepScalars* sc) {
-  __shared__ double red[32];
-  if (sc->stop) return;
-  double m = DBL_MAX;
-  for (int b = threadIdx.x; b < nb; b += blockDim.x) m = fmin(m, blockmin[b]);
-  for (int off = 16; off > 0; off >>= 1) m = fmin(m, __shfl_down_sync(0xffffffffu, m, off));
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int k = 1; k < (int)(blockDim.x / 32); ++k) m = fmin(m, red[k]);
-    m = fmin(red[0], m);
-    double dtmin = sc->deltatint;
+// Per-instance step control, one block looping over the instances.
+// dt: LastComputeAcceleration's minimum (Source/Domain.cpp:1280-1296) and
+// AdaptiveTimeStep (Source/Domain.cpp:133-152).
+__global__ void dt_finalize_kernel(DevView v) {
+  StepScalars* sc = v.sc;
+  if (sc->all_stop) return;
+  for (int k = threadIdx.x; k < v.ninst; k += blockDim.x) {
+    InstState& I = v.inst[k];
+    if (I.stop) continue;
+    const double m = __longlong_as_double((long long)I.dtmin_bits);
+    double dtmin = I.deltatint;
     if (dtmin > m) dtmin = m;
-    sc->deltatmin = dtmin;
-    double dt = sc->deltat;
-    const double dti = sc->deltatint;
+    I.deltatmin = dtmin;
+    double dt = I.deltat;
+    const double dti = I.deltatint;
     if (dti > dtmin) dt = (dt < dtmin) ? 2.0 * dt * dtmin / (dt + dtmin) : dtmin;
     else dt = (dti != dt) ? 2.0 * dt * dti / (dt + dti) : dti;
-    sc->deltat = dt;
+    I.deltat = dt;
     if (dt < (dti / 1.0e5)) {
-      sc->status |= ST_DT_COLLAPSE;
-      sc->stop = 1;  // the reference throws here (Source/Domain.cpp:150-151)
+      atomicOr(&sc->status, ST_DT_COLLAPSE);
+      I.stop = 1;  // the reference throws here (Source/Domain.cpp:150-151)
     }
   }
 }
 
-// Begin of step: Solve's `Time < tf` test and Move_MVerlet's first-step ct.
-__global__ void begin_kernel(StepScalars* sc, int scheme) {
-  if (sc->stop) return;
-  if (!(sc->time < sc->t_stop)) {
-    sc->stop = 1;
-    return;
+// Begin of step: Solve's `Time < tf` test per instance, Move_MVerlet's
+// first-step ct (Source/Particle.cpp:191-195), reset of the dt minimum.
+__global__ void begin_kernel(DevView v) {
+  StepScalars* sc = v.sc;
+  int live = 0;
+  for (int k = threadIdx.x; k < v.ninst; k += blockDim.x) {
+    InstState& I = v.inst[k];
+    if (!I.stop && !(I.time < I.t_stop)) I.stop = 1;
+    if (I.stop) continue;
+    live = 1;
+    if (v.o.scheme == PSPH_MVERLET && I.first_step) I.ct = 30;
+    I.dtmin_bits = (unsigned long long)__double_as_longlong(DBL_MAX);
   }
-  if (scheme == PSPH_MVERLET && sc->first_step) sc->ct = 30;  // Source/Particle.cpp:191-195
+  live = __syncthreads_or(live);
+  if (threadIdx.x == 0) sc->all_stop = !live;
 }
 
-// End of step: Time += deltat and the per-particle counters, once per domain.
-__global__ void end_kernel(StepScalars* sc, int scheme, int shepard_step) {
-  if (sc->stop) return;
-  sc->time += sc->deltat;
-  sc->steps += 1;
-  if (scheme == PSPH_MVERLET) {
-    sc->ct = (sc->ct == 30) ? 0 : sc->ct + 1;
-    sc->shepard_counter = (sc->shepard_counter == shepard_step) ? 0 : sc->shepard_counter + 1;
+// End of step: Time += deltat and the per-particle counters, once per instance.
+__global__ void end_kernel(DevView v) {
+  if (v.sc->all_stop) return;
+  for (int k = threadIdx.x; k < v.ninst; k += blockDim.x) {
+    InstState& I = v.inst[k];
+    if (I.stop) continue;
+    I.time += I.deltat;
+    I.steps += 1;
+    if (v.o.scheme == PSPH_MVERLET) {
+      I.ct = (I.ct == 30) ? 0 : I.ct + 1;
+      I.shepard_counter = (I.shepard_counter == v.o.shepard_step) ? 0 : I.shepard_counter + 1;
+    }
+    I.first_step = 0;
   }
-  sc->first_step = 0;
 }
 
 // Pair export: candidate (which=0) or in-support (which=1) pairs in reference
@@ -714,11 +706,11 @@ __global__ void pairs_export_kernel(DevView v, int which, long long* out, long l
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const Persist& P = cur_persist(v);
-  const GridDev& g = v.g;
   const int cell = v.S.cellid[i];
   if (cell < 0) return;
   const PClass* CT = v.cls;
   const PClass& Ci = CT[P.cls[i]];
+  const GridDev& g = grid_of(v, Ci.inst);
   const CellCoord ci = decode(g, cell);
   const int oi = P.orig[i];
   const double4_32a xi = P.X4[i];
@@ -794,15 +786,11 @@ void launch_forces(const DevView& v, cudaStream_t st) {
   else forces_dispatch<3>(v, st);
 }
 
-void launch_dt(const DevView& v, cudaStream_t st) {
-  dt_finalize_kernel<<<1, 1024, 0, st>>>(v.S.blockmin, forces_blocks(v.ncap), v.sc);
-}
+void launch_dt(const DevView& v, cudaStream_t st) { dt_finalize_kernel<<<1, 256, 0, st>>>(v); }
 
-void launch_begin(const DevView& v, cudaStream_t st) { begin_kernel<<<1, 1, 0, st>>>(v.sc, v.o.scheme); }
+void launch_begin(const DevView& v, cudaStream_t st) { begin_kernel<<<1, 256, 0, st>>>(v); }
 
-void launch_end(const DevView& v, cudaStream_t st) {
-  end_kernel<<<1, 1, 0, st>>>(v.sc, v.o.scheme, v.o.shepard_step);
-}
+void launch_end(const DevView& v, cudaStream_t st) { end_kernel<<<1, 256, 0, st>>>(v); }
 
 void launch_pairs_export(const DevView& v, int which, long long* out, long long cap, unsigned long long* counter,
                          cudaStream_t st) {
@@ -824,11 +812,11 @@ namespace {
 template <int DIM>
 PSPH_D int pairs_of_particle(const DevView& v, int i, int which, long long* out, long long base, long long cap) {
   const Persist& P = cur_persist(v);
-  const GridDev& g = v.g;
   const int cell = v.S.cellid[i];
   if (cell < 0) return 0;
   const PClass* CT = v.cls;
   const PClass& Ci = CT[P.cls[i]];
+  const GridDev& g = grid_of(v, Ci.inst);
   const CellCoord ci = decode(g, cell);
   const int oi = P.orig[i];
   const double4_32a xi = P.X4[i];

@@ -114,11 +114,12 @@ struct KernF {
 template <int DIM>
 __global__ void __launch_bounds__(kFT32) copies32_kernel(DevView v) {
   const StepScalars* sc = v.sc;
-  if (sc->stop) return;
+  if (sc->all_stop) return;
   const Persist& P = cur_persist(v);
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
   if (w >= sc->n) return;
   const PClass32& C = v.cls32[P.cls[w]];
+  if (v.inst[C.inst].stop) return;
   const double4_32a vv = P.V4[w];
   const float p = (float)vv.w;
   v.S.V32[w] = make_float4((float)vv.x, (float)vv.y, (float)vv.z, p);
@@ -135,18 +136,19 @@ template <int DIM, int KT>
 __global__ void __launch_bounds__(kFT32) prepare32_kernel(DevView v) {
   __shared__ int qbuf[kQ32][kFT32];
   const StepScalars* sc = v.sc;
-  if (sc->stop) return;
+  if (sc->all_stop) return;
   const Persist& P = cur_persist(v);
   const int n = sc->n;
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
   const int tid = threadIdx.x;
-  const GridDev& g = v.g;
   const Options& o = v.o;
   const PClass32* __restrict__ CT = v.cls32;
+  const int winst = (w < n) ? CT[P.cls[w]].inst : 0;
+  const GridDev& g = grid_of(v, winst);
   bool wall = false, noslip = false;
   int cell = -1, ow = 0, mat = 0;
   float4 oi = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (w < n) {
+  if (w < n && !v.inst[winst].stop) {
     const PClass32& C = CT[P.cls[w]];
     if (!(C.flags & CF_FREE)) {
       wall = true;
@@ -162,7 +164,7 @@ __global__ void __launch_bounds__(kFT32) prepare32_kernel(DevView v) {
   const bool need_orient = !o.wallp_physical && (gx != 0.f || gy != 0.f || gz != 0.f);
   float sk = 0.f, p = 0.f, n0 = 0.f, n1 = 0.f, n2 = 0.f;
   NbrSource<DIM> src;
-  src.init(v, w, wall && cell >= 0, 1.0f);
+  src.init(v, g, w, wall && cell >= 0, 1.0f);
   bool more = wall && cell >= 0;
   const float hw = oi.w;
   while (true) {
@@ -238,12 +240,11 @@ __global__ void __launch_bounds__(kFT32) forces_fluid32_kernel(DevView v) {
   __shared__ double red[kFT32 / 32];
   __shared__ unsigned long long cred[kFT32 / 32];
   const StepScalars* sc = v.sc;
-  if (sc->stop) return;
+  if (sc->all_stop) return;
   const Persist& P = cur_persist(v);
   const int n = sc->n;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int tid = threadIdx.x;
-  const GridDev& g = v.g;
   const Options& o = v.o;
   const PClass32* __restrict__ CT = v.cls32;
   double dtc = DBL_MAX;
@@ -252,14 +253,17 @@ __global__ void __launch_bounds__(kFT32) forces_fluid32_kernel(DevView v) {
   int cell = -1, ci_cls = 0;
   if (i < n) {
     ci_cls = P.cls[i];
-    active = CT[ci_cls].flags & CF_FREE;
+    const bool run = !v.inst[CT[ci_cls].inst].stop;
+    active = run && (CT[ci_cls].flags & CF_FREE);
     cell = v.S.cellid[i];
-    if (!active) {
+    if (run && !active) {
       v.S.A4[i] = make_double4_32a(o.gravity[0], o.gravity[1], o.gravity[2], 0.0);
       v.S.zwab[i] = 1.0;
     }
   }
   const PClass32& Ci = CT[ci_cls];
+  const GridDev& g = grid_of(v, Ci.inst);
+  const InstState& Is = v.inst[Ci.inst];
   const int is = active ? i : 0;
   const float4 oi = v.S.OFF32[is];
   const float4 vi = v.S.V32[is];
@@ -268,7 +272,7 @@ __global__ void __launch_bounds__(kFT32) forces_fluid32_kernel(DevView v) {
   const float mi = Ci.mass, hi = oi.w;
   const float mui = o.dyn_mu ? (float)P.mu[is] : Ci.mu0;
   const int fi = Ci.flags;
-  const bool shep = (fi & CF_SHEPARD) && (sc->shepard_counter == o.shepard_step);
+  const bool shep = (fi & CF_SHEPARD) && (Is.shepard_counter == o.shepard_step);
   const bool sr_self = fi & (CF_T0 | CF_LES);
   const bool use_sr = o.need_sr;
   const bool xsph_on = o.xsph != 0.0;
@@ -280,8 +284,11 @@ __global__ void __launch_bounds__(kFT32) forces_fluid32_kernel(DevView v) {
   Kahan ax, ay, az, dr;
   float zw = 0.f, sd = 0.f, xs0 = 0.f, xs1 = 0.f, xs2 = 0.f;
   float sr0 = 0.f, sr1 = 0.f, sr2 = 0.f, sr4 = 0.f, sr5 = 0.f, sr8 = 0.f;
+  float w01 = 0.f, w02 = 0.f, w12 = 0.f;  // antisymmetric counterpart of the strain-rate sums (closure)
+  int nnb = 0;
+  const bool closure = o.closure && (fi & CF_LES);
   NbrSource<DIM> src;
-  src.init(v, i, active && cell >= 0, 1.0f);
+  src.init(v, g, i, active && cell >= 0, 1.0f);
   while (true) {
     int code;
     const int j = src.next(v, &code);
@@ -293,6 +300,7 @@ __global__ void __launch_bounds__(kFT32) forces_fluid32_kernel(DevView v) {
     const int fjf = Cj.flags;
     const bool fj = fjf & CF_FREE;
     npair2 += fj ? 1ull : 2ull;
+    ++nnb;
     const float hb = 0.5f * (hi + oj.w);
     const float ih = 1.f / hb;
     const float r2 = x0 * x0 + x1 * x1 + x2 * x2;
@@ -367,6 +375,11 @@ __global__ void __launch_bounds__(kFT32) forces_fluid32_kernel(DevView v) {
         sr4 += c2 * (2.f * vab1 * x1);
         sr5 += c2 * (vab1 * x2 + vab2 * x1);
         sr8 += c2 * (2.f * vab2 * x2);
+        if (closure) {
+          w01 += c2 * (vab0 * x1 - vab1 * x0);
+          w02 += c2 * (vab0 * x2 - vab2 * x0);
+          w12 += c2 * (vab1 * x2 - vab2 * x1);
+        }
       }
     }
     if (xsph_on && fj) {
@@ -398,30 +411,16 @@ __global__ void __launch_bounds__(kFT32) forces_fluid32_kernel(DevView v) {
       out[3] = sr1; out[4] = sr4; out[5] = sr5;
       out[6] = sr2; out[7] = sr5; out[8] = sr8;
     }
+    if (closure) {
+      v.S.cvort[i] = sqrtf(w01 * w01 + w02 * w02 + w12 * w12);
+      v.S.cnnb[i] = (float)nnb;
+    }
     if (!(isfinite(axd) && isfinite(ayd) && isfinite(azd) && isfinite(drd))) atomicOr(&v.sc->status, ST_NONFINITE);
     const double an = sqrt(axd * axd + ayd * ayd + azd * azd);
     const double cand = o.sqrt_h_a * sqrt(v.cls[ci_cls].h / an);  // FP64 dt reduction
     if (cand < dtc) dtc = cand;
   }
-  for (int off = 16; off > 0; off >>= 1) {
-    dtc = fmin(dtc, __shfl_down_sync(0xffffffffu, dtc, off));
-    npair2 += __shfl_down_sync(0xffffffffu, npair2, off);
-  }
-  if ((tid & 31) == 0) {
-    red[tid >> 5] = dtc;
-    cred[tid >> 5] = npair2;
-  }
-  __syncthreads();
-  if (tid == 0) {
-    double m = red[0];
-    unsigned long long c = cred[0];
-    for (int k = 1; k < kFT32 / 32; ++k) {
-      m = fmin(m, red[k]);
-      c += cred[k];
-    }
-    v.S.blockmin[blockIdx.x] = m;
-    if (c) atomicAdd(&v.sc->pairs_x2, c);
-  }
+  block_dt_and_pairs<kFT32>(v, Ci.inst, active, dtc, npair2, red, cred);
 }
 
 inline int nblk32(int n) { return n <= 0 ? 1 : (n + kFT32 - 1) / kFT32; }

@@ -1,0 +1,974 @@
+// Learned eddy-viscosity closure: a 6 -> 64 -> 64 -> 64 -> 1 SiLU network.
+//
+//  * closure_kernel (inside the step) and infer_tc_kernel run the three hidden
+//    layers on the 5th-generation tensor cores: one CTA of 128 threads per
+//    128-particle tile, BF16 activations written by the threads into a
+//    128-byte-swizzled shared-memory tile, BF16 weights brought in once per CTA
+//    by a TMA bulk copy, tcgen05.mma issued by one thread with the FP32
+//    accumulator in tensor memory, tcgen05.ld back to registers (thread t owns
+//    row t) for bias + SiLU; the 64 -> 1 output layer runs on the CUDA cores.
+//  * Training runs on the CUDA cores in FP32 with the same BF16 rounding of the
+//    weights and hidden activations (straight-through gradients): forward,
+//    loss, backward, per-chunk weight gradients, a fixed-order reduction and
+//    Adam, so a training run is deterministic.
+// Every wait on a tensor-core or copy completion is bounded (1 s); a wait that
+// gives up sets ST_CLOSURE_TIMEOUT (or an error status) and the kernel returns
+// after freeing its tensor memory.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "psph_device.cuh"
+#include "psph_mlp.cuh"
+
+using namespace psph;
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// scalar helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+__device__ __forceinline__ float sigm(float z) { return 1.f / (1.f + expf(-z)); }
+__device__ __forceinline__ float silu(float z) { return z * sigm(z); }
+__device__ __forceinline__ float dsilu(float z) {
+  const float s = sigm(z);
+  return s * (1.f + z * (1.f - s));
+}
+__device__ __forceinline__ float softplus(float z) { return z > 20.f ? z : log1pf(expf(z)); }
+
+// ---------------------------------------------------------------------------
+// tensor-core, mbarrier and bulk-copy primitives (inline PTX, sm_100 family)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Waits for the phase with the given parity to complete, giving up after limit_ns.
+__device__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, unsigned long long limit_ns) {
+  const unsigned long long t0 = global_ns();
+  while (!mbar_try_wait(bar, parity)) {
+    if (global_ns() - t0 > limit_ns) return false;
+  }
+  return true;
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// 1-D bulk copy global -> shared (TMA), completion counted on the mbarrier.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void proxy_fence_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row
+// groups 1024 bytes apart (start address, LBO, SBO, version 1, layout 2).
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+  d |= (uint64_t)(16 >> 4) << 16;
+  d |= (uint64_t)(1024 >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+// Instruction descriptor of kind::f16: D FP32, A and B BF16, both K-major,
+// N = 64, M = 128.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kMlpH >> 3) << 17) |
+                            ((uint32_t)(kMlpTile >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)), "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+// 16 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld16(uint32_t addr, float* z) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(addr)
+      : "memory");
+#pragma unroll
+  for (int k = 0; k < 16; ++k) z[k] = __uint_as_float(r[k]);
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t*>(&h);
+}
+
+// ---------------------------------------------------------------------------
+// tensor-core tile forward, shared by the closure and the standalone inference
+// ---------------------------------------------------------------------------
+constexpr int kTcThreads = kMlpTile;           // thread t owns tile row t
+constexpr int kSmA = 0;                         // A tile: 128 rows x 128 B
+constexpr int kSmW = kSmA + kMlpTile * 128;     // W1..W3 images, 8 KB each
+constexpr int kSmPad = kSmW + 3 * kImgBytes;    // 8 KB of slack after the operands
+constexpr int kSmF = kSmPad + 8192;             // floats: b1 b2 b3 w4 (256) + b4 + norm (24)
+constexpr int kSmFloats = 4 * kMlpH + 4 + 4 * kMlpIn;
+constexpr int kTcSmemBytes = kSmF + kSmFloats * 4 + 1024;  // + alignment slack
+
+struct TcCtx {
+  uint8_t* a;
+  uint8_t* w;        // three images back to back
+  float* f;          // b1, b2, b3, w4, b4(+3 pad), mean, inv_std, lo, hi
+  uint64_t* bar_mma;
+  int* err;
+  uint32_t taddr;
+  uint32_t phase;
+};
+
+__device__ __forceinline__ const float* tc_b(const TcCtx& t, int l) { return t.f + l * kMlpH; }
+
+// Loads the image into shared memory (bulk copy for the operand images) and
+// allocates the 64 accumulator columns. All threads call it.
+__device__ bool tc_setup(TcCtx& t, uint8_t* smem_raw, const MlpImage* img, uint64_t* bars, uint32_t* slot, int* err) {
+  const int tid = threadIdx.x;
+  const uint32_t base = smem_u32(smem_raw);
+  uint8_t* sm = smem_raw + ((1024 - (base & 1023)) & 1023);  // 1024-byte aligned for the swizzle atoms
+  t.a = sm + kSmA;
+  t.w = sm + kSmW;
+  t.f = reinterpret_cast<float*>(sm + kSmF);
+  t.bar_mma = &bars[1];
+  t.err = err;
+  t.phase = 0;
+  if (tid == 0) {
+    *err = 0;
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    mbar_init_fence();
+  }
+  // biases, output layer and normalisation: plain loads
+  const float* src = img->b1;
+  for (int k = tid; k < kSmFloats; k += blockDim.x) t.f[k] = src[k];
+  if (tid < 32) tmem_alloc(slot, kMlpH);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  t.taddr = *slot;
+  if (tid == 0) {
+    mbar_expect_tx(&bars[0], 3 * kImgBytes);
+    bulk_g2s(t.w, img->w1, kImgBytes, &bars[0]);
+    bulk_g2s(t.w + kImgBytes, img->w2, kImgBytes, &bars[0]);
+    bulk_g2s(t.w + 2 * kImgBytes, img->w3, kImgBytes, &bars[0]);
+    if (!mbar_wait_bounded(&bars[0], 0, 1000000000ull)) *err = 1;
+  }
+  __syncthreads();
+  return *err == 0;
+}
+
+__device__ void tc_teardown(TcCtx& t) {
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (threadIdx.x < 32) tmem_dealloc(t.taddr, kMlpH);
+}
+
+// Row r of the A tile from 64 values (BF16, swizzled).
+__device__ __forceinline__ void store_row64(uint8_t* a, int r, const float* x) {
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    uint4 q;
+    q.x = pack_bf16(x[8 * c + 0], x[8 * c + 1]);
+    q.y = pack_bf16(x[8 * c + 2], x[8 * c + 3]);
+    q.z = pack_bf16(x[8 * c + 4], x[8 * c + 5]);
+    q.w = pack_bf16(x[8 * c + 6], x[8 * c + 7]);
+    *reinterpret_cast<uint4*>(a + sw128_offset(r, 8 * c)) = q;
+  }
+}
+
+// One layer: D = A W^T over ksteps K-steps of 16, then each thread reads its
+// row of D. Returns false when the completion wait gave up.
+__device__ bool tc_layer(TcCtx& t, int layer, int ksteps, float* z) {
+  proxy_fence_smem();  // the threads' A writes become visible to the tensor core
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    tc_fence_after();
+    const uint64_t ad = sw128_desc(smem_u32(t.a));
+    const uint64_t bd = sw128_desc(smem_u32(t.w + layer * kImgBytes));
+    for (int k = 0; k < ksteps; ++k) mma_bf16(t.taddr, ad + 2 * k, bd + 2 * k, k > 0 ? 1u : 0u);
+    mma_commit(t.bar_mma);
+    if (!mbar_wait_bounded(t.bar_mma, t.phase, 1000000000ull)) *t.err = 1;
+  }
+  t.phase ^= 1u;
+  __syncthreads();
+  tc_fence_after();
+  if (*t.err) return false;
+  const uint32_t lane_addr = t.taddr + ((uint32_t)(threadIdx.x & ~31) << 16);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) tmem_ld16(lane_addr + 16 * j, z + 16 * j);
+  tmem_wait_ld();
+  return true;
+}
+
+// Network output z4 for this thread's row; u = standardised features.
+__device__ bool tc_forward(TcCtx& t, const float* u, float* out) {
+  const int r = threadIdx.x;
+  float z[kMlpH];
+  {
+    float x[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) x[k] = (k < kMlpIn) ? u[k] : 0.f;
+    uint4 q0, q1;
+    q0.x = pack_bf16(x[0], x[1]); q0.y = pack_bf16(x[2], x[3]); q0.z = pack_bf16(x[4], x[5]); q0.w = pack_bf16(x[6], x[7]);
+    q1.x = pack_bf16(x[8], x[9]); q1.y = pack_bf16(x[10], x[11]); q1.z = pack_bf16(x[12], x[13]); q1.w = pack_bf16(x[14], x[15]);
+    *reinterpret_cast<uint4*>(t.a + sw128_offset(r, 0)) = q0;
+    *reinterpret_cast<uint4*>(t.a + sw128_offset(r, 8)) = q1;
+  }
+  if (!tc_layer(t, 0, 1, z)) return false;
+  const float* b1 = tc_b(t, 0);
+#pragma unroll
+  for (int k = 0; k < kMlpH; ++k) z[k] = silu(z[k] + b1[k]);
+  store_row64(t.a, r, z);
+  if (!tc_layer(t, 1, kMlpH / 16, z)) return false;
+  const float* b2 = tc_b(t, 1);
+#pragma unroll
+  for (int k = 0; k < kMlpH; ++k) z[k] = silu(z[k] + b2[k]);
+  store_row64(t.a, r, z);
+  if (!tc_layer(t, 2, kMlpH / 16, z)) return false;
+  const float* b3 = tc_b(t, 2);
+  const float* w4 = tc_b(t, 3);
+  float o = t.f[4 * kMlpH];
+#pragma unroll
+  for (int k = 0; k < kMlpH; ++k) o += w4[k] * silu(z[k] + b3[k]);
+  *out = o;
+  return true;
+}
+
+__device__ __forceinline__ const float* tc_norm(const TcCtx& t) { return t.f + 4 * kMlpH + 4; }
+
+// ---------------------------------------------------------------------------
+// closure inside the step
+// ---------------------------------------------------------------------------
+template <int DIM>
+__global__ void __launch_bounds__(kTcThreads) closure_kernel(DevView v) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ uint64_t bars[2];
+  __shared__ uint32_t slot;
+  __shared__ int err;
+  const StepScalars* sc = v.sc;
+  if (sc->all_stop) return;
+  TcCtx t;
+  const bool ok = tc_setup(t, smem_raw, static_cast<const MlpImage*>(v.mlp), bars, &slot, &err);
+  const int n = sc->n;
+  const int ntiles = (n + kMlpTile - 1) / kMlpTile;
+  const Persist& P = cur_persist(v);
+  const float* nm = tc_norm(t);
+  const float* mean = nm;
+  const float* inv_std = nm + kMlpIn;
+  const float* lo = nm + 2 * kMlpIn;
+  const float* hi = nm + 3 * kMlpIn;
+  unsigned long long n_eval = 0, n_fb = 0;
+  for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
+    const int s = tile * kMlpTile + threadIdx.x;
+    bool act = false;
+    float f[kMlpIn] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    double shear = 0.0, h = 0.0;
+    if (s < n) {
+      const PClass& C = v.cls[P.cls[s]];
+      act = C.is_free && C.material == 1 && C.les && !v.inst[C.inst].stop;
+      if (act) {
+        const double* S = v.S.strain_rate + 9 * (size_t)s;
+        // same contraction as Mat1's ShearRate (Source/Particle.cpp:151-153)
+        const double temp =
+            (S[0] * S[0] + 2.0 * S[1] * S[3] + 2.0 * S[2] * S[6] + S[4] * S[4] + 2.0 * S[5] * S[7] + S[8] * S[8]);
+        shear = sqrt(0.5 * temp);
+        const double det = S[0] * (S[4] * S[8] - S[5] * S[7]) - S[1] * (S[3] * S[8] - S[5] * S[6]) +
+                           S[2] * (S[3] * S[7] - S[4] * S[6]);
+        h = C.h;
+        f[0] = logf(fmaxf((float)shear, 1e-8f));
+        f[1] = temp > 0.0 ? (float)(det / (temp * sqrt(temp))) : 0.f;
+        f[2] = logf(fmaxf(v.S.cvort[s], 1e-8f));
+        f[3] = (float)(P.X4[s].w / C.rho0);
+        f[4] = (float)(C.h / v.o.closure_dx);
+        f[5] = v.S.cnnb[s];
+      }
+      float* fo = v.S.cfeat + (size_t)kMlpIn * s;
+#pragma unroll
+      for (int k = 0; k < kMlpIn; ++k) fo[k] = f[k];
+    }
+    bool in_range = act;
+#pragma unroll
+    for (int k = 0; k < kMlpIn; ++k) in_range = in_range && f[k] >= lo[k] && f[k] <= hi[k];
+    float u[kMlpIn];
+#pragma unroll
+    for (int k = 0; k < kMlpIn; ++k) u[k] = in_range ? (f[k] - mean[k]) * inv_std[k] : 0.f;
+    float z4 = 0.f;
+    if (!tc_forward(t, u, &z4)) break;
+    if (act) v.S.nut[s] = in_range ? (double)softplus(z4) * h * h * shear : -1.0;
+    n_eval += act ? 1 : 0;
+    n_fb += (act && !in_range) ? 1 : 0;
+  }
+  // per-CTA totals (order-independent integer sums)
+  for (int off = 16; off > 0; off >>= 1) {
+    n_eval += __shfl_down_sync(0xffffffffu, n_eval, off);
+    n_fb += __shfl_down_sync(0xffffffffu, n_fb, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (n_eval) atomicAdd(&v.sc->closure_eval, n_eval);
+    if (n_fb) atomicAdd(&v.sc->closure_fallback, n_fb);
+  }
+  if (err && threadIdx.x == 0) atomicOr(&v.sc->status, ST_CLOSURE_TIMEOUT);
+  tc_teardown(t);
+}
+
+// ---------------------------------------------------------------------------
+// standalone inference (tensor cores / CUDA cores)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kTcThreads) infer_tc_kernel(const MlpImage* img, const float* x, int n, float* c,
+                                                              int* status) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ uint64_t bars[2];
+  __shared__ uint32_t slot;
+  __shared__ int err;
+  TcCtx t;
+  const bool ok = tc_setup(t, smem_raw, img, bars, &slot, &err);
+  const float* nm = tc_norm(t);
+  const int ntiles = (n + kMlpTile - 1) / kMlpTile;
+  for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
+    const int s = tile * kMlpTile + threadIdx.x;
+    float u[kMlpIn];
+#pragma unroll
+    for (int k = 0; k < kMlpIn; ++k) u[k] = (s < n) ? (x[(size_t)kMlpIn * s + k] - nm[k]) * nm[kMlpIn + k] : 0.f;
+    float z4 = 0.f;
+    if (!tc_forward(t, u, &z4)) break;
+    if (s < n) c[s] = softplus(z4);
+  }
+  if (err && threadIdx.x == 0) atomicExch(status, 1);
+  tc_teardown(t);
+}
+
+// FP32 forward of one sample with the BF16 roundings of the tensor-core path;
+// stores the pre-activations when z1 != nullptr (training).
+__device__ float cc_forward(const float* __restrict__ p, const float* u_in, float* u_out, float* z1, float* z2,
+                            float* z3) {
+  float u[kMlpIn];
+#pragma unroll
+  for (int k = 0; k < kMlpIn; ++k) u[k] = bf16r(u_in[k]);
+  if (u_out)
+#pragma unroll
+    for (int k = 0; k < kMlpIn; ++k) u_out[k] = u[k];
+  float a1[kMlpH], a2[kMlpH];
+#pragma unroll
+  for (int nn = 0; nn < kMlpH; ++nn) {
+    float z = p[kOB1 + nn];
+#pragma unroll
+    for (int k = 0; k < kMlpIn; ++k) z += bf16r(p[kOW1 + nn * kMlpIn + k]) * u[k];
+    if (z1) z1[nn] = z;
+    a1[nn] = bf16r(silu(z));
+  }
+#pragma unroll 4
+  for (int nn = 0; nn < kMlpH; ++nn) {
+    float z = p[kOB2 + nn];
+#pragma unroll
+    for (int k = 0; k < kMlpH; ++k) z += bf16r(p[kOW2 + nn * kMlpH + k]) * a1[k];
+    if (z2) z2[nn] = z;
+    a2[nn] = bf16r(silu(z));
+  }
+  float o = p[kOB4];
+#pragma unroll 4
+  for (int nn = 0; nn < kMlpH; ++nn) {
+    float z = p[kOB3 + nn];
+#pragma unroll
+    for (int k = 0; k < kMlpH; ++k) z += bf16r(p[kOW3 + nn * kMlpH + k]) * a2[k];
+    if (z3) z3[nn] = z;
+    o += p[kOW4 + nn] * silu(z);
+  }
+  return o;
+}
+
+__global__ void infer_cc_kernel(const float* __restrict__ params, const float* __restrict__ norm, const float* x,
+                                int n, float* c) {
+  __shared__ float p[kNParams];
+  for (int k = threadIdx.x; k < kNParams; k += blockDim.x) p[k] = params[k];
+  __syncthreads();
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  float u[kMlpIn];
+  for (int k = 0; k < kMlpIn; ++k) u[k] = (x[(size_t)kMlpIn * s + k] - norm[k]) * norm[kMlpIn + k];
+  c[s] = softplus(cc_forward(p, u, nullptr, nullptr, nullptr, nullptr));
+}
+
+// ---------------------------------------------------------------------------
+// training (CUDA cores, FP32, deterministic)
+// ---------------------------------------------------------------------------
+constexpr int kTrainThreads = 128;
+
+// Forward of minibatch sample b (data row idx[b]); activations stored
+// sample-major [b][64] for the backward pass.
+__global__ void train_fwd_kernel(const float* __restrict__ params, const float* __restrict__ norm,
+                                 const float* __restrict__ X, const int* __restrict__ idx, int B, float* U, float* Z1,
+                                 float* Z2, float* Z3, float* Z4) {
+  __shared__ float p[kNParams];
+  for (int k = threadIdx.x; k < kNParams; k += blockDim.x) p[k] = params[k];
+  __syncthreads();
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const int row = idx ? idx[b] : b;
+  float u[kMlpIn];
+  for (int k = 0; k < kMlpIn; ++k) u[k] = (X[(size_t)kMlpIn * row + k] - norm[k]) * norm[kMlpIn + k];
+  float uo[kMlpIn];
+  Z4[b] = cc_forward(p, u, uo, Z1 + (size_t)kMlpH * b, Z2 + (size_t)kMlpH * b, Z3 + (size_t)kMlpH * b);
+  for (int k = 0; k < kMlpIn; ++k) U[(size_t)8 * b + k] = uo[k];
+}
+
+// dL/dz4 and the per-block loss partial sums (fixed-order reduction on the host).
+__global__ void train_loss_kernel(const float* __restrict__ Z4, const float* __restrict__ Y,
+                                  const int* __restrict__ idx, int B, float* G4, double* loss_part) {
+  __shared__ double red[kTrainThreads];
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  double l = 0.0;
+  if (b < B) {
+    const float z = Z4[b];
+    const float y = Y[idx ? idx[b] : b];
+    const float e = softplus(z) - y;
+    G4[b] = 2.f * e * sigm(z) / (float)B;
+    l = (double)e * (double)e;
+  }
+  red[threadIdx.x] = l;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) loss_part[blockIdx.x] = red[0];
+}
+
+// Deltas of the three hidden layers (pre-activation gradients), [b][64].
+__global__ void train_bwd_kernel(const float* __restrict__ params, const float* __restrict__ Z1,
+                                 const float* __restrict__ Z2, const float* __restrict__ Z3,
+                                 const float* __restrict__ G4, int B, float* D1, float* D2, float* D3) {
+  __shared__ float p[kNParams];
+  for (int k = threadIdx.x; k < kNParams; k += blockDim.x) p[k] = params[k];
+  __syncthreads();
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const float g = G4[b];
+  const float* z1 = Z1 + (size_t)kMlpH * b;
+  const float* z2 = Z2 + (size_t)kMlpH * b;
+  const float* z3 = Z3 + (size_t)kMlpH * b;
+  float d3[kMlpH], d2[kMlpH];
+#pragma unroll
+  for (int k = 0; k < kMlpH; ++k) {
+    d3[k] = g * p[kOW4 + k] * dsilu(z3[k]);
+    D3[(size_t)kMlpH * b + k] = d3[k];
+  }
+#pragma unroll 4
+  for (int m = 0; m < kMlpH; ++m) {
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < kMlpH; ++k) s += bf16r(p[kOW3 + k * kMlpH + m]) * d3[k];
+    d2[m] = s * dsilu(z2[m]);
+    D2[(size_t)kMlpH * b + m] = d2[m];
+  }
+#pragma unroll 4
+  for (int m = 0; m < kMlpH; ++m) {
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < kMlpH; ++k) s += bf16r(p[kOW2 + k * kMlpH + m]) * d2[k];
+    D1[(size_t)kMlpH * b + m] = s * dsilu(z1[m]);
+  }
+}
+
+// Gradient of every parameter summed over one chunk of samples:
+// part[chunk][param]. Threads of a warp take consecutive parameters, so the
+// activation reads of a weight row are contiguous.
+__global__ void train_wgrad_kernel(const float* __restrict__ U, const float* __restrict__ Z1,
+                                   const float* __restrict__ Z2, const float* __restrict__ Z3,
+                                   const float* __restrict__ G4, const float* __restrict__ D1,
+                                   const float* __restrict__ D2, const float* __restrict__ D3, int B, int chunk,
+                                   float* part) {
+  const int pidx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pidx >= kNParams) return;
+  const int b0 = blockIdx.y * chunk, b1 = min(B, b0 + chunk);
+  float acc = 0.f;
+  if (pidx < kOB1) {
+    const int nn = pidx / kMlpIn, k = pidx % kMlpIn;
+    for (int b = b0; b < b1; ++b) acc += D1[(size_t)kMlpH * b + nn] * U[(size_t)8 * b + k];
+  } else if (pidx < kOW2) {
+    const int nn = pidx - kOB1;
+    for (int b = b0; b < b1; ++b) acc += D1[(size_t)kMlpH * b + nn];
+  } else if (pidx < kOB2) {
+    const int q = pidx - kOW2, nn = q / kMlpH, k = q % kMlpH;
+    for (int b = b0; b < b1; ++b) acc += D2[(size_t)kMlpH * b + nn] * bf16r(silu(Z1[(size_t)kMlpH * b + k]));
+  } else if (pidx < kOW3) {
+    const int nn = pidx - kOB2;
+    for (int b = b0; b < b1; ++b) acc += D2[(size_t)kMlpH * b + nn];
+  } else if (pidx < kOB3) {
+    const int q = pidx - kOW3, nn = q / kMlpH, k = q % kMlpH;
+    for (int b = b0; b < b1; ++b) acc += D3[(size_t)kMlpH * b + nn] * bf16r(silu(Z2[(size_t)kMlpH * b + k]));
+  } else if (pidx < kOW4) {
+    const int nn = pidx - kOB3;
+    for (int b = b0; b < b1; ++b) acc += D3[(size_t)kMlpH * b + nn];
+  } else if (pidx < kOB4) {
+    const int k = pidx - kOW4;
+    for (int b = b0; b < b1; ++b) acc += G4[b] * silu(Z3[(size_t)kMlpH * b + k]);
+  } else {
+    for (int b = b0; b < b1; ++b) acc += G4[b];
+  }
+  part[(size_t)blockIdx.y * kNParams + pidx] = acc;
+}
+
+__global__ void train_reduce_kernel(const float* __restrict__ part, int nchunks, float* grad) {
+  const int pidx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pidx >= kNParams) return;
+  float s = 0.f;
+  for (int c = 0; c < nchunks; ++c) s += part[(size_t)c * kNParams + pidx];
+  grad[pidx] = s;
+}
+
+__global__ void adam_kernel(float* params, const float* grad, float* m, float* v, float lr, float b1, float b2,
+                            float c1, float c2, float eps) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= kNParams) return;
+  const float g = grad[k];
+  const float mk = b1 * m[k] + (1.f - b1) * g;
+  const float vk = b2 * v[k] + (1.f - b2) * g * g;
+  m[k] = mk;
+  v[k] = vk;
+  params[k] -= lr * (mk / c1) / (sqrtf(vk / c2) + eps);
+}
+
+// ---------------------------------------------------------------------------
+// host helpers
+// ---------------------------------------------------------------------------
+uint16_t bf16_bits(float f) {  // round to nearest even
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  if ((u & 0x7f800000u) == 0x7f800000u) return (uint16_t)((u >> 16) | ((u & 0xffffu) ? 0x40u : 0u));
+  u += 0x7fffu + ((u >> 16) & 1u);
+  return (uint16_t)(u >> 16);
+}
+
+void put_operand(uint8_t* img, const float* W, int rows, int cols) {  // W[rows][cols] -> swizzled K-major
+  std::memset(img, 0, kImgBytes);
+  for (int r = 0; r < rows; ++r)
+    for (int k = 0; k < cols; ++k) {
+      const uint16_t b = bf16_bits(W[r * cols + k]);
+      std::memcpy(img + sw128_offset(r, k), &b, 2);
+    }
+}
+
+uint64_t splitmix(uint64_t& s) {
+  uint64_t z = (s += 0x9e3779b97f4a7c15ull);
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+double uniform01(uint64_t& s) { return (double)(splitmix(s) >> 11) * (1.0 / 9007199254740992.0); }
+
+int num_sms() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 148;
+  }
+  return n;
+}
+
+bool tc_attr_set = false;
+cudaError_t ensure_tc_attrs() {
+  if (tc_attr_set) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(closure_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(closure_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes);
+  if (e == cudaSuccess) tc_attr_set = true;
+  return e;
+}
+
+}  // namespace
+
+namespace psph {
+void launch_closure(const DevView& v, cudaStream_t st) {
+  if (ensure_tc_attrs() != cudaSuccess) return;  // the launch below then reports the error
+  const int ntiles = (v.ncap + kMlpTile - 1) / kMlpTile;
+  const int grid = std::max(1, std::min(ntiles, 2 * num_sms()));
+  if (v.o.dim == 2) closure_kernel<2><<<grid, kTcThreads, kTcSmemBytes, st>>>(v);
+  else closure_kernel<3><<<grid, kTcThreads, kTcSmemBytes, st>>>(v);
+}
+}  // namespace psph
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+struct psph_mlp {
+  std::string err;
+  float* d_params = nullptr;
+  float* d_m = nullptr;
+  float* d_v = nullptr;
+  float* d_grad = nullptr;
+  float* d_norm = nullptr;
+  MlpImage* d_img = nullptr;
+  bool img_dirty = true;
+  std::vector<float> norm = std::vector<float>(PSPH_MLP_NNORM, 0.f);
+  long long adam_t = 0;
+  // training data
+  float* d_X = nullptr;
+  float* d_Y = nullptr;
+  int64_t n_data = 0;
+  // minibatch scratch
+  int cap = 0, nchunk_cap = 0;
+  int* d_idx = nullptr;
+  float *d_U = nullptr, *d_Z1 = nullptr, *d_Z2 = nullptr, *d_Z3 = nullptr, *d_Z4 = nullptr, *d_G4 = nullptr;
+  float *d_D1 = nullptr, *d_D2 = nullptr, *d_D3 = nullptr, *d_part = nullptr;
+  double* d_loss = nullptr;
+  int* d_status = nullptr;
+};
+
+namespace {
+
+psph_status mlp_err(psph_mlp* m, psph_status code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (m) m->err = buf;
+  return code;
+}
+
+#define MLP_TRY(m, call)                                                                                  \
+  do {                                                                                                    \
+    cudaError_t e_ = (call);                                                                              \
+    if (e_ != cudaSuccess)                                                                                \
+      return mlp_err(m, e_ == cudaErrorMemoryAllocation ? PSPH_ERR_OUT_OF_MEMORY : PSPH_ERR_CUDA, "%s: %s", #call, \
+                     cudaGetErrorString(e_));                                                             \
+  } while (0)
+
+template <class T>
+void dfree(T*& p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+psph_status ensure_batch(psph_mlp* m, int B) {
+  const int nchunk = (B + 127) / 128;
+  if (B <= m->cap && nchunk <= m->nchunk_cap) return PSPH_OK;
+  for (float** p : {&m->d_U, &m->d_Z1, &m->d_Z2, &m->d_Z3, &m->d_Z4, &m->d_G4, &m->d_D1, &m->d_D2, &m->d_D3,
+                    &m->d_part})
+    dfree(*p);
+  dfree(m->d_idx);
+  dfree(m->d_loss);
+  const size_t b = (size_t)B;
+  MLP_TRY(m, cudaMalloc(&m->d_idx, b * sizeof(int)));
+  MLP_TRY(m, cudaMalloc(&m->d_U, 8 * b * sizeof(float)));
+  MLP_TRY(m, cudaMemset(m->d_U, 0, 8 * b * sizeof(float)));
+  for (float** p : {&m->d_Z1, &m->d_Z2, &m->d_Z3, &m->d_D1, &m->d_D2, &m->d_D3})
+    MLP_TRY(m, cudaMalloc(p, (size_t)kMlpH * b * sizeof(float)));
+  MLP_TRY(m, cudaMalloc(&m->d_Z4, b * sizeof(float)));
+  MLP_TRY(m, cudaMalloc(&m->d_G4, b * sizeof(float)));
+  MLP_TRY(m, cudaMalloc(&m->d_part, (size_t)nchunk * kNParams * sizeof(float)));
+  MLP_TRY(m, cudaMalloc(&m->d_loss, (size_t)((B + kTrainThreads - 1) / kTrainThreads) * sizeof(double)));
+  m->cap = B;
+  m->nchunk_cap = nchunk;
+  return PSPH_OK;
+}
+
+// Loss and gradient of one minibatch (rows idx of X/Y, or the first B rows).
+psph_status batch_grad(psph_mlp* m, const float* dX, const float* dY, const int* d_idx, int B, double* loss) {
+  psph_status st = ensure_batch(m, B);
+  if (st) return st;
+  const int nb = (B + kTrainThreads - 1) / kTrainThreads;
+  train_fwd_kernel<<<nb, kTrainThreads>>>(m->d_params, m->d_norm, dX, d_idx, B, m->d_U, m->d_Z1, m->d_Z2, m->d_Z3,
+                                          m->d_Z4);
+  train_loss_kernel<<<nb, kTrainThreads>>>(m->d_Z4, dY, d_idx, B, m->d_G4, m->d_loss);
+  train_bwd_kernel<<<nb, kTrainThreads>>>(m->d_params, m->d_Z1, m->d_Z2, m->d_Z3, m->d_G4, B, m->d_D1, m->d_D2,
+                                          m->d_D3);
+  const int chunk = 128, nchunk = (B + chunk - 1) / chunk;
+  dim3 grid((kNParams + 127) / 128, nchunk);
+  train_wgrad_kernel<<<grid, 128>>>(m->d_U, m->d_Z1, m->d_Z2, m->d_Z3, m->d_G4, m->d_D1, m->d_D2, m->d_D3, B, chunk,
+                                    m->d_part);
+  train_reduce_kernel<<<(kNParams + 127) / 128, 128>>>(m->d_part, nchunk, m->d_grad);
+  MLP_TRY(m, cudaGetLastError());
+  if (loss) {
+    std::vector<double> parts(nb);
+    MLP_TRY(m, cudaMemcpy(parts.data(), m->d_loss, nb * sizeof(double), cudaMemcpyDeviceToHost));
+    double s = 0.0;
+    for (double x : parts) s += x;
+    *loss = s / B;
+  }
+  return PSPH_OK;
+}
+
+psph_status build_image(psph_mlp* m) {
+  if (!m->img_dirty) return PSPH_OK;
+  std::vector<float> p(kNParams);
+  MLP_TRY(m, cudaMemcpy(p.data(), m->d_params, kNParams * sizeof(float), cudaMemcpyDeviceToHost));
+  std::vector<uint8_t> buf(sizeof(MlpImage), 0);
+  MlpImage* img = reinterpret_cast<MlpImage*>(buf.data());
+  std::vector<float> w1(kMlpH * 16, 0.f);  // K padded to one 16-wide MMA step
+  for (int r = 0; r < kMlpH; ++r)
+    for (int k = 0; k < kMlpIn; ++k) w1[r * 16 + k] = p[kOW1 + r * kMlpIn + k];
+  put_operand(img->w1, w1.data(), kMlpH, 16);
+  put_operand(img->w2, &p[kOW2], kMlpH, kMlpH);
+  put_operand(img->w3, &p[kOW3], kMlpH, kMlpH);
+  std::memcpy(img->b1, &p[kOB1], kMlpH * 4);
+  std::memcpy(img->b2, &p[kOB2], kMlpH * 4);
+  std::memcpy(img->b3, &p[kOB3], kMlpH * 4);
+  std::memcpy(img->w4, &p[kOW4], kMlpH * 4);
+  img->b4 = p[kOB4];
+  std::memcpy(img->mean, m->norm.data(), PSPH_MLP_NNORM * 4);
+  MLP_TRY(m, cudaMemcpy(m->d_img, buf.data(), sizeof(MlpImage), cudaMemcpyHostToDevice));
+  m->img_dirty = false;
+  return PSPH_OK;
+}
+
+}  // namespace
+
+psph_status psph_mlp_image(const psph_mlp* mlp, const MlpImage** dev_image) {
+  psph_mlp* m = const_cast<psph_mlp*>(mlp);
+  if (!m || !dev_image) return PSPH_ERR_INVALID_ARGUMENT;
+  psph_status st = build_image(m);
+  if (st) return st;
+  *dev_image = m->d_img;
+  return PSPH_OK;
+}
+
+extern "C" {
+
+psph_status psph_mlp_create(uint64_t seed, psph_mlp** out) {
+  if (!out) return PSPH_ERR_INVALID_ARGUMENT;
+  psph_mlp* m = new psph_mlp();
+  *out = m;
+  int ndev = 0;
+  if (psph_device_check(&ndev) != PSPH_OK) return mlp_err(m, PSPH_ERR_NO_DEVICE, "no sm_103 CUDA device available");
+  MLP_TRY(m, cudaMalloc(&m->d_params, kNParams * sizeof(float)));
+  MLP_TRY(m, cudaMalloc(&m->d_m, kNParams * sizeof(float)));
+  MLP_TRY(m, cudaMalloc(&m->d_v, kNParams * sizeof(float)));
+  MLP_TRY(m, cudaMalloc(&m->d_grad, kNParams * sizeof(float)));
+  MLP_TRY(m, cudaMalloc(&m->d_norm, PSPH_MLP_NNORM * sizeof(float)));
+  MLP_TRY(m, cudaMalloc(&m->d_img, sizeof(MlpImage)));
+  MLP_TRY(m, cudaMalloc(&m->d_status, sizeof(int)));
+  MLP_TRY(m, cudaMemset(m->d_m, 0, kNParams * sizeof(float)));
+  MLP_TRY(m, cudaMemset(m->d_v, 0, kNParams * sizeof(float)));
+  // uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) weights and biases; the output
+  // bias starts at softplus^-1(0.02)
+  std::vector<float> p(kNParams);
+  uint64_t s = seed ^ 0x5eed5eedull;
+  auto fill = [&](int off, int count, int fan_in) {
+    const double a = 1.0 / std::sqrt((double)fan_in);
+    for (int k = 0; k < count; ++k) p[off + k] = (float)((2.0 * uniform01(s) - 1.0) * a);
+  };
+  fill(kOW1, kMlpH * kMlpIn, kMlpIn);
+  fill(kOB1, kMlpH, kMlpIn);
+  fill(kOW2, kMlpH * kMlpH, kMlpH);
+  fill(kOB2, kMlpH, kMlpH);
+  fill(kOW3, kMlpH * kMlpH, kMlpH);
+  fill(kOB3, kMlpH, kMlpH);
+  fill(kOW4, kMlpH, kMlpH);
+  p[kOB4] = (float)std::log(std::expm1(0.02));
+  MLP_TRY(m, cudaMemcpy(m->d_params, p.data(), kNParams * sizeof(float), cudaMemcpyHostToDevice));
+  for (int k = 0; k < kMlpIn; ++k) {
+    m->norm[k] = 0.f;                  // mean
+    m->norm[kMlpIn + k] = 1.f;         // 1/std
+    m->norm[2 * kMlpIn + k] = -1e30f;  // lo
+    m->norm[3 * kMlpIn + k] = 1e30f;   // hi
+  }
+  MLP_TRY(m, cudaMemcpy(m->d_norm, m->norm.data(), PSPH_MLP_NNORM * sizeof(float), cudaMemcpyHostToDevice));
+  return PSPH_OK;
+}
+
+void psph_mlp_destroy(psph_mlp* m) {
+  if (!m) return;
+  cudaDeviceSynchronize();
+  for (float** p : {&m->d_params, &m->d_m, &m->d_v, &m->d_grad, &m->d_norm, &m->d_X, &m->d_Y, &m->d_U, &m->d_Z1,
+                    &m->d_Z2, &m->d_Z3, &m->d_Z4, &m->d_G4, &m->d_D1, &m->d_D2, &m->d_D3, &m->d_part})
+    dfree(*p);
+  dfree(m->d_img);
+  dfree(m->d_idx);
+  dfree(m->d_loss);
+  dfree(m->d_status);
+  delete m;
+}
+
+const char* psph_mlp_last_error(const psph_mlp* m) { return m ? m->err.c_str() : "null network"; }
+
+psph_status psph_mlp_set_params(psph_mlp* m, const float* params, const float* norm) {
+  if (!m || (!params && !norm)) return PSPH_ERR_INVALID_ARGUMENT;
+  if (params) MLP_TRY(m, cudaMemcpy(m->d_params, params, kNParams * sizeof(float), cudaMemcpyHostToDevice));
+  if (norm) {
+    m->norm.assign(norm, norm + PSPH_MLP_NNORM);
+    MLP_TRY(m, cudaMemcpy(m->d_norm, norm, PSPH_MLP_NNORM * sizeof(float), cudaMemcpyHostToDevice));
+  }
+  MLP_TRY(m, cudaMemset(m->d_m, 0, kNParams * sizeof(float)));
+  MLP_TRY(m, cudaMemset(m->d_v, 0, kNParams * sizeof(float)));
+  m->adam_t = 0;
+  m->img_dirty = true;
+  return PSPH_OK;
+}
+
+psph_status psph_mlp_get_params(const psph_mlp* mlp, float* params, float* norm) {
+  psph_mlp* m = const_cast<psph_mlp*>(mlp);
+  if (!m) return PSPH_ERR_INVALID_ARGUMENT;
+  if (params) MLP_TRY(m, cudaMemcpy(params, m->d_params, kNParams * sizeof(float), cudaMemcpyDeviceToHost));
+  if (norm) std::memcpy(norm, m->norm.data(), PSPH_MLP_NNORM * sizeof(float));
+  return PSPH_OK;
+}
+
+psph_status psph_mlp_set_data(psph_mlp* m, const float* x, const float* y, int64_t n) {
+  if (!m || !x || !y || n < 1 || n > (1LL << 30)) return PSPH_ERR_INVALID_ARGUMENT;
+  dfree(m->d_X);
+  dfree(m->d_Y);
+  MLP_TRY(m, cudaMalloc(&m->d_X, (size_t)n * kMlpIn * sizeof(float)));
+  MLP_TRY(m, cudaMalloc(&m->d_Y, (size_t)n * sizeof(float)));
+  MLP_TRY(m, cudaMemcpy(m->d_X, x, (size_t)n * kMlpIn * sizeof(float), cudaMemcpyHostToDevice));
+  MLP_TRY(m, cudaMemcpy(m->d_Y, y, (size_t)n * sizeof(float), cudaMemcpyHostToDevice));
+  m->n_data = n;
+  for (int k = 0; k < kMlpIn; ++k) {
+    double s = 0.0, s2 = 0.0, lo = x[k], hi = x[k];
+    for (int64_t i = 0; i < n; ++i) {
+      const double v = x[(size_t)kMlpIn * i + k];
+      s += v;
+      s2 += v * v;
+      lo = std::min(lo, v);
+      hi = std::max(hi, v);
+    }
+    const double mean = s / n;
+    const double var = std::max(s2 / n - mean * mean, 0.0);
+    const double sd = std::sqrt(var);
+    const double pad = 0.05 * (hi - lo);
+    m->norm[k] = (float)mean;
+    m->norm[kMlpIn + k] = (float)(sd > 1e-12 ? 1.0 / sd : 1.0);
+    m->norm[2 * kMlpIn + k] = (float)(lo - pad);
+    m->norm[3 * kMlpIn + k] = (float)(hi + pad);
+  }
+  MLP_TRY(m, cudaMemcpy(m->d_norm, m->norm.data(), PSPH_MLP_NNORM * sizeof(float), cudaMemcpyHostToDevice));
+  m->img_dirty = true;
+  return PSPH_OK;
+}
+
+psph_status psph_mlp_train(psph_mlp* m, int64_t steps, int batch, float lr, uint64_t seed, float* losses) {
+  if (!m || steps < 0 || batch < 1 || !(lr > 0.f)) return PSPH_ERR_INVALID_ARGUMENT;
+  if (!m->n_data) return mlp_err(m, PSPH_ERR_STATE, "psph_mlp_train before psph_mlp_set_data");
+  const int B = (int)std::min<int64_t>(batch, m->n_data);
+  std::vector<int> perm(m->n_data);
+  for (int64_t i = 0; i < m->n_data; ++i) perm[i] = (int)i;
+  uint64_t rs = seed;
+  int64_t pos = m->n_data;  // forces a shuffle on the first step
+  psph_status st = ensure_batch(m, B);
+  if (st) return st;
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  for (int64_t step = 0; step < steps; ++step) {
+    if (pos + B > m->n_data) {  // new pass: Fisher-Yates with the seeded generator
+      for (int64_t i = m->n_data - 1; i > 0; --i) {
+        const int64_t j = (int64_t)(splitmix(rs) % (uint64_t)(i + 1));
+        std::swap(perm[i], perm[j]);
+      }
+      pos = 0;
+    }
+    MLP_TRY(m, cudaMemcpy(m->d_idx, perm.data() + pos, B * sizeof(int), cudaMemcpyHostToDevice));
+    pos += B;
+    double loss = 0.0;
+    if ((st = batch_grad(m, m->d_X, m->d_Y, m->d_idx, B, losses ? &loss : nullptr))) return st;
+    m->adam_t += 1;
+    const float c1 = (float)(1.0 - std::pow((double)b1, (double)m->adam_t));
+    const float c2 = (float)(1.0 - std::pow((double)b2, (double)m->adam_t));
+    adam_kernel<<<(kNParams + 255) / 256, 256>>>(m->d_params, m->d_grad, m->d_m, m->d_v, lr, b1, b2, c1, c2, eps);
+    MLP_TRY(m, cudaGetLastError());
+    if (losses) losses[step] = (float)loss;
+  }
+  MLP_TRY(m, cudaDeviceSynchronize());
+  m->img_dirty = true;
+  return PSPH_OK;
+}
+
+psph_status psph_mlp_loss_grad(psph_mlp* m, const float* x, const float* y, int64_t n, double* loss, float* grad) {
+  if (!m || !x || !y || n < 1 || n > (1 << 24)) return PSPH_ERR_INVALID_ARGUMENT;
+  float *dX = nullptr, *dY = nullptr;
+  MLP_TRY(m, cudaMalloc(&dX, (size_t)n * kMlpIn * sizeof(float)));
+  MLP_TRY(m, cudaMalloc(&dY, (size_t)n * sizeof(float)));
+  MLP_TRY(m, cudaMemcpy(dX, x, (size_t)n * kMlpIn * sizeof(float), cudaMemcpyHostToDevice));
+  MLP_TRY(m, cudaMemcpy(dY, y, (size_t)n * sizeof(float), cudaMemcpyHostToDevice));
+  double l = 0.0;
+  psph_status st = batch_grad(m, dX, dY, nullptr, (int)n, &l);
+  if (!st && grad) {
+    cudaError_t e = cudaMemcpy(grad, m->d_grad, kNParams * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) st = mlp_err(m, PSPH_ERR_CUDA, "gradient copy: %s", cudaGetErrorString(e));
+  }
+  cudaFree(dX);
+  cudaFree(dY);
+  if (loss) *loss = l;
+  return st;
+}
+
+psph_status psph_mlp_infer(psph_mlp* m, const float* x, int64_t n, float* c, int tensor_cores) {
+  if (!m || !x || !c || n < 1 || n > (1 << 28)) return PSPH_ERR_INVALID_ARGUMENT;
+  psph_status st = build_image(m);
+  if (st) return st;
+  float *dX = nullptr, *dC = nullptr;
+  MLP_TRY(m, cudaMalloc(&dX, (size_t)n * kMlpIn * sizeof(float)));
+  MLP_TRY(m, cudaMalloc(&dC, (size_t)n * sizeof(float)));
+  MLP_TRY(m, cudaMemcpy(dX, x, (size_t)n * kMlpIn * sizeof(float), cudaMemcpyHostToDevice));
+  MLP_TRY(m, cudaMemset(m->d_status, 0, sizeof(int)));
+  if (tensor_cores) {
+    MLP_TRY(m, ensure_tc_attrs());
+    const int ntiles = (int)((n + kMlpTile - 1) / kMlpTile);
+    const int grid = std::max(1, std::min(ntiles, 2 * num_sms()));
+    infer_tc_kernel<<<grid, kTcThreads, kTcSmemBytes>>>(m->d_img, dX, (int)n, dC, m->d_status);
+  } else {
+    infer_cc_kernel<<<(int)((n + 127) / 128), 128>>>(m->d_params, m->d_norm, dX, (int)n, dC);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  int status = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&status, m->d_status, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(c, dC, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost);
+  cudaFree(dX);
+  cudaFree(dC);
+  if (e != cudaSuccess) return mlp_err(m, PSPH_ERR_CUDA, "inference: %s", cudaGetErrorString(e));
+  if (status) return mlp_err(m, PSPH_ERR_CUDA, "inference: a tensor-core completion wait gave up");
+  return PSPH_OK;
+}
+
+}  // extern "C"

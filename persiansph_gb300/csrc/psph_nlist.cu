@@ -20,7 +20,7 @@ constexpr int kNT = 128;
 template <int DIM>
 __global__ void __launch_bounds__(kNT) nlist_kernel(DevView v, float margin) {
   const StepScalars* sc = v.sc;
-  if (sc->stop) return;
+  if (sc->all_stop) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= sc->n) return;
   const int cell = v.S.cellid[i];
@@ -28,7 +28,8 @@ __global__ void __launch_bounds__(kNT) nlist_kernel(DevView v, float margin) {
     v.S.nl_count[i] = 0;
     return;
   }
-  const GridDev& g = v.g;
+  const Persist& P = cur_persist(v);
+  const GridDev& g = grid_of(v, v.cls[P.cls[i]].inst);
   const float3 cs = cell_size_f(g);
   const float4 oi = v.S.OFF32[i];
   const float cf = (float)g.cellfac;
@@ -46,7 +47,7 @@ __global__ void __launch_bounds__(kNT) nlist_kernel(DevView v, float margin) {
       int y = c.y + dy;
       if (g.periodic[1]) y = (y + g.nc[1]) % g.nc[1];
       else if (y < 0 || y >= g.nc[1]) continue;
-      const int base = (z * g.nc[1] + y) * g.nc[0];
+      const int base = g.cell_base + (z * g.nc[1] + y) * g.nc[0];
       const int cyz = 3 * (dy + 1) + 9 * (dz + 1);
       for (int sub = 0; sub < (wrapx ? 3 : 1); ++sub) {
         int lo, hi;

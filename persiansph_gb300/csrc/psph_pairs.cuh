@@ -4,6 +4,9 @@
 // (cell offset, FP32 offset within the cell).
 #pragma once
 
+#include <cfloat>
+#include <climits>
+
 #include "psph_device.cuh"
 
 namespace psph {
@@ -15,7 +18,9 @@ struct CellCoord {
   int x, y, z;
 };
 
+// Cell coordinates of a global cell id within its instance's grid.
 PSPH_D CellCoord decode(const GridDev& g, int c) {
+  c -= g.cell_base;
   CellCoord r;
   r.x = c % g.nc[0];
   const int t = c / g.nc[0];
@@ -45,7 +50,7 @@ PSPH_D void for_neighbor_ranges(const GridDev& g, const CellCoord& c, const int*
       int y = c.y + dy;
       if (g.periodic[1]) y = (y + g.nc[1]) % g.nc[1];
       else if (y < 0 || y >= g.nc[1]) continue;
-      const int row = (z * g.nc[1] + y) * g.nc[0];
+      const int row = g.cell_base + (z * g.nc[1] + y) * g.nc[0];
       if (!g.periodic[0] || (c.x >= 1 && c.x <= g.nc[0] - 2)) {
         const int x0 = max(c.x - 1, 0), x1 = min(c.x + 1, g.nc[0] - 1);
         f(start[row + x0], start[row + x1 + 1]);
@@ -120,7 +125,7 @@ struct Cands32 {
     else if (z < 0 || z >= g.nc[2]) return false;
     if (g.periodic[1]) y = (y + g.nc[1]) % g.nc[1];
     else if (y < 0 || y >= g.nc[1]) return false;
-    base = (z * g.nc[1] + y) * g.nc[0];
+    base = g.cell_base + (z * g.nc[1] + y) * g.nc[0];
     code_yz = 3 * (dy + 1) + 9 * (dz + 1);
     if (!wrapx) {
       if (sub) return false;
@@ -176,16 +181,18 @@ struct NbrSource {
   Cands32<DIM> cs;
   float4 oi;
   float margin;
-  PSPH_D void init(const DevView& v, int i_, bool on, float margin_) {
+  const GridDev* g;
+  PSPH_D void init(const DevView& v, const GridDev& grid, int i_, bool on, float margin_) {
     i = i_;
     k = 0;
     margin = margin_;
+    g = &grid;
     cnt = on ? v.S.nl_count[i] : 0;
     if (on && cnt < 0) {
-      cs.init(v.g, v.S.cellid[i]);
+      cs.init(grid, v.S.cellid[i]);
       oi = v.S.OFF32[i];
     } else {
-      cs.init(v.g, -1);
+      cs.init(grid, -1);
     }
   }
   PSPH_D int next(const DevView& v, int* code) {
@@ -196,10 +203,10 @@ struct NbrSource {
       *code = e >> kCodeShift;
       return e & kIndexMask;
     }
-    const float3 csz = cell_size_f(v.g);
-    const float cf = (float)v.g.cellfac;
+    const float3 csz = cell_size_f(*g);
+    const float cf = (float)g->cellfac;
     while (true) {
-      const int j = cs.next(v.g, v.S.start, v.S.cellid, code);
+      const int j = cs.next(*g, v.S.start, v.S.cellid, code);
       if (j < 0) return -1;
       if (j == i) continue;
       const float4 oj = v.S.OFF32[j];
@@ -210,5 +217,44 @@ struct NbrSource {
     }
   }
 };
+
+}  // namespace psph
+
+namespace psph {
+
+// End of a pair kernel: folds each particle's acceleration time-step bound into
+// its instance's running minimum (an atomic minimum on the ordered bits of a
+// non-negative double, so the result does not depend on arrival order; NaN
+// bounds never win, as the reference's comparison ignores them) and adds the
+// block's pair count. One atomic per warp when the warp's particles share an
+// instance, which is the case except at instance boundaries.
+template <int BT>
+PSPH_D void block_dt_and_pairs(const DevView& v, int inst, bool active, double dtc, unsigned long long npair2,
+                               double* red, unsigned long long* cred) {
+  const unsigned full = 0xffffffffu;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const unsigned act = __ballot_sync(full, active);
+  if (act) {
+    const int first = __shfl_sync(full, inst, __ffs(act) - 1);
+    const bool uniform = __all_sync(full, !active || inst == first);
+    if (uniform) {
+      double m = active ? dtc : DBL_MAX;
+      for (int off = 16; off > 0; off >>= 1) m = fmin(m, __shfl_down_sync(full, m, off));
+      if (lane == 0 && m < DBL_MAX)
+        atomicMin(&v.inst[first].dtmin_bits, (unsigned long long)__double_as_longlong(m));
+    } else if (active && dtc < DBL_MAX) {
+      atomicMin(&v.inst[inst].dtmin_bits, (unsigned long long)__double_as_longlong(dtc));
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) npair2 += __shfl_down_sync(full, npair2, off);
+  if (lane == 0) cred[tid >> 5] = npair2;
+  __syncthreads();
+  if (tid == 0) {
+    unsigned long long c = 0;
+    for (int k = 0; k < BT / 32; ++k) c += cred[k];
+    if (c) atomicAdd(&v.sc->pairs_x2, c);
+  }
+  (void)red;
+}
 
 }  // namespace psph

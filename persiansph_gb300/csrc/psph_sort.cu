@@ -20,17 +20,19 @@ namespace {
 
 constexpr int kBT = 256;
 
-__global__ void bin_kernel(GridDev g, DevView v, const uint8_t* __restrict__ alive,
-                           int* __restrict__ key, int* __restrict__ count, StepScalars* sc, int dim) {
-  if (sc->stop) return;
-  const double4_32a* __restrict__ X4 = cur_persist(v).X4;
+__global__ void bin_kernel(DevView v, const uint8_t* __restrict__ alive, int* __restrict__ key,
+                           int* __restrict__ count, StepScalars* sc, int dim) {
+  if (sc->all_stop) return;
+  const Persist& P = cur_persist(v);
   const int n = sc->n;
+  const int orphan_key = v.total_cells, dead_key = v.total_cells + 1;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     int k;
     if (!alive[i]) {
-      k = g.ncells + 1;
+      k = dead_key;
     } else {
-      const double4_32a x = X4[i];
+      const GridDev& g = grid_of(v, v.cls[P.cls[i]].inst);
+      const double4_32a x = P.X4[i];
       const double xs[3] = {x.x, x.y, x.z};
       int c[3] = {0, 0, 0};
       bool orphan = false, out = false;
@@ -49,11 +51,11 @@ __global__ void bin_kernel(GridDev g, DevView v, const uint8_t* __restrict__ ali
       }
       if (out) {
         atomicOr(&sc->status, ST_OUT_OF_GRID);
-        k = g.ncells + 1;
+        k = dead_key;
       } else if (orphan) {
-        k = g.ncells;
+        k = orphan_key;
       } else {
-        k = cell_linear(g, c[0], c[1], c[2]);
+        k = g.cell_base + (c[2] * g.nc[1] + c[1]) * g.nc[0] + c[0];
       }
     }
     key[i] = k;
@@ -136,7 +138,7 @@ __global__ void scan_add(int* __restrict__ out, const int* __restrict__ sums, in
 
 __global__ void scatter_kernel(const int* __restrict__ key, const int* __restrict__ start, int* __restrict__ fill,
                                int* __restrict__ tmp_perm, const StepScalars* sc) {
-  if (sc->stop) return;
+  if (sc->all_stop) return;
   const int n = sc->n;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int k = key[i];
@@ -147,7 +149,7 @@ __global__ void scatter_kernel(const int* __restrict__ key, const int* __restric
 __global__ void rank_kernel(const int* __restrict__ key, const int* __restrict__ start,
                             const int* __restrict__ tmp_perm, DevView v, int* __restrict__ perm,
                             const StepScalars* sc, int ncells) {
-  if (sc->stop) return;
+  if (sc->all_stop) return;
   const int* __restrict__ orig = cur_persist(v).orig;
   const int n = sc->n;
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
@@ -168,7 +170,7 @@ __global__ void rank_kernel(const int* __restrict__ key, const int* __restrict__
 __global__ void reorder_kernel(DevView v, const int* __restrict__ perm, const int* __restrict__ key,
                                const int* __restrict__ start, int* __restrict__ cellid, uint8_t* __restrict__ alive,
                                const StepScalars* sc, int ncells, int has_solid, int dyn_mu) {
-  if (sc->stop) return;
+  if (sc->all_stop) return;
   const Persist& src = cur_persist(v);
   const Persist& dst = next_persist(v);
   const int n_new = start[ncells + 1];
@@ -185,10 +187,12 @@ __global__ void reorder_kernel(DevView v, const int* __restrict__ perm, const in
       const int kk = key[i];
       const float h = (float)v.cls[src.cls[i]].h;
       if (kk < ncells) {
-        const int cx = kk % v.g.nc[0], t = kk / v.g.nc[0], cy = t % v.g.nc[1], cz = t / v.g.nc[1];
-        v.S.OFF32[s] = make_float4((float)(xs.x - (v.g.blpf[0] + cx * v.g.cell_size[0])),
-                                   (float)(xs.y - (v.g.blpf[1] + cy * v.g.cell_size[1])),
-                                   (float)(v.o.dim == 3 ? xs.z - (v.g.blpf[2] + cz * v.g.cell_size[2]) : 0.0), h);
+        const GridDev& g = grid_of(v, v.cls[src.cls[i]].inst);
+        const int lk = kk - g.cell_base;
+        const int cx = lk % g.nc[0], t = lk / g.nc[0], cy = t % g.nc[1], cz = t / g.nc[1];
+        v.S.OFF32[s] = make_float4((float)(xs.x - (g.blpf[0] + cx * g.cell_size[0])),
+                                   (float)(xs.y - (g.blpf[1] + cy * g.cell_size[1])),
+                                   (float)(v.o.dim == 3 ? xs.z - (g.blpf[2] + cz * g.cell_size[2]) : 0.0), h);
       } else {
         v.S.OFF32[s] = make_float4((float)xs.x, (float)xs.y, (float)xs.z, h);
       }
@@ -210,7 +214,7 @@ __global__ void reorder_kernel(DevView v, const int* __restrict__ perm, const in
 }
 
 __global__ void finish_sort_kernel(const int* __restrict__ start, StepScalars* sc, int ncells) {
-  if (sc->stop) return;
+  if (sc->all_stop) return;
   sc->n_cells = start[ncells];
   sc->n = start[ncells + 1];
   sc->buf ^= 1;
@@ -224,21 +228,21 @@ inline int grid_for(int n) {
 }  // namespace
 
 void launch_sort(const DevView& v, cudaStream_t st) {
-  const GridDev& g = v.g;
   const Scratch& S = v.S;
-  const int len = g.ncells + 2;
+  const int ncells = v.total_cells;
+  const int len = ncells + 2;
   cudaMemsetAsync(S.count, 0, sizeof(int) * (size_t)len, st);
-  bin_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(g, v, v.alive, S.key, S.count, v.sc, v.o.dim);
+  bin_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(v, v.alive, S.key, S.count, v.sc, v.o.dim);
   const int nb = (len + 1023) / 1024;
   scan_blocks<<<nb, 1024, 0, st>>>(S.count, S.start, S.block_sums, len);
   scan_sums<<<1, 1024, 0, st>>>(S.block_sums, nb, S.start + len);
   scan_add<<<nb, 1024, 0, st>>>(S.start, S.block_sums, len);
   cudaMemsetAsync(S.count, 0, sizeof(int) * (size_t)len, st);
   scatter_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(S.key, S.start, S.count, S.tmp_perm, v.sc);
-  rank_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(S.key, S.start, S.tmp_perm, v, S.perm, v.sc, g.ncells);
-  reorder_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(v, S.perm, S.key, S.start, S.cellid, v.alive, v.sc,
-                                                    g.ncells, v.o.has_solid, v.o.dyn_mu);
-  finish_sort_kernel<<<1, 1, 0, st>>>(S.start, v.sc, g.ncells);
+  rank_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(S.key, S.start, S.tmp_perm, v, S.perm, v.sc, ncells);
+  reorder_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(v, S.perm, S.key, S.start, S.cellid, v.alive, v.sc, ncells,
+                                                    v.o.has_solid, v.o.dyn_mu);
+  finish_sort_kernel<<<1, 1, 0, st>>>(S.start, v.sc, ncells);
 }
 
 }  // namespace psph

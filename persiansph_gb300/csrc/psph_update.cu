@@ -122,18 +122,20 @@ PSPH_D void dp_return(const PClass& C, double I22, double* Sig, const double* Sn
 template <int DIM>
 __global__ void __launch_bounds__(kUT) update_kernel(DevView v) {
   const StepScalars* sc = v.sc;
-  if (sc->stop) return;
+  if (sc->all_stop) return;
   const Persist& P = cur_persist(v);
   const int n = sc->n;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   const PClass& C = v.cls[P.cls[s]];
   if (!C.is_free) return;
+  const InstState& Is = v.inst[C.inst];
+  if (Is.stop) return;
   const Options& o = v.o;
-  const GridDev& g = v.g;
-  const double dt = sc->deltat;
-  const int first = sc->first_step;
-  const int ct = sc->ct;
+  const GridDev& g = grid_of(v, C.inst);
+  const double dt = Is.deltat;
+  const int first = Is.first_step;
+  const int ct = Is.ct;
   double4_32a X = P.X4[s];
   double4_32a V = P.V4[s];
   double4_32a H = P.H4[s];
@@ -150,7 +152,7 @@ __global__ void __launch_bounds__(kUT) update_kernel(DevView v) {
       vx[0] = w.x; vx[1] = w.y; vx[2] = w.z;
     }
     for (int d = 0; d < 3; ++d) x[d] += dt * (vel[d] + vx[d]) + 0.5 * dt * dt * a[d];
-    const bool shep = C.shepard && (sc->shepard_counter == o.shepard_step);
+    const bool shep = C.shepard && (Is.shepard_counter == o.shepard_step);
     const double zw = v.S.zwab[s];
     double rhob = H.w;
     double vb[3] = {H.x, H.y, H.z};
@@ -221,8 +223,13 @@ __global__ void __launch_bounds__(kUT) update_kernel(DevView v) {
       if (o.dyn_mu) {
         double mu = P.mu[s];
         if (C.les) {
-          const double ch = C.csmag * C.h;
-          mu = C.mu_ref + C.rho0 * (ch * ch) * sbar;
+          const double nut = o.closure ? v.S.nut[s] : -1.0;
+          if (nut >= 0.0) {
+            mu = C.mu_ref + C.rho0 * nut;  // learned eddy viscosity
+          } else {
+            const double ch = C.csmag * C.h;
+            mu = C.mu_ref + C.rho0 * (ch * ch) * sbar;
+          }
         }
         if (C.t0 > 0.0) {
           // Bingham (Source/Particle.cpp:166-170): 1-exp(-m g) evaluated as -expm1(-m g),
@@ -349,6 +356,6 @@ void launch_update(const DevView& v, cudaStream_t st) {
 
 // begin, bin, 3 scan, scatter, rank, reorder, finish, neighbour lists, prepare
 // (2 in the FP32C form: copies + walls), forces, dt, update, end
-int launches_per_step(const DevView& v) { return v.o.fp32 ? 16 : 15; }
+int launches_per_step(const DevView& v) { return (v.o.fp32 ? 16 : 15) + (v.o.closure ? 1 : 0); }
 
 }  // namespace psph

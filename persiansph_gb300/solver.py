@@ -141,3 +141,137 @@ class GpuDomain:
 
     def last_launch_count(self) -> int:
         return int(self._lib.psph_last_launch_count(self._ctx))
+
+
+class GpuEnsemble:
+    """Many independent domains in one context (psph_batch_*): one launch
+    sequence per step serves all instances; each keeps its own grid, time step
+    and stop time. Instance q's particles are indexed as uploaded."""
+
+    def __init__(self, cfgs):
+        self._lib = load_library()
+        self._ctx = C.c_void_p()
+        self.cfgs = list(cfgs)
+        arr = (PsphConfig * len(self.cfgs))(*self.cfgs)
+        self._keep = arr
+        self._check(self._lib.psph_batch_create(arr, len(self.cfgs), C.byref(self._ctx)))
+        self._uploaded = None
+
+    def _check(self, st: int):
+        if st != 0:
+            msg = self._lib.psph_last_error(self._ctx).decode() if self._ctx else ""
+            raise PsphError(st, msg)
+
+    def close(self):
+        if self._ctx:
+            self._lib.psph_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def size(self) -> int:
+        return int(self._lib.psph_batch_size(self._ctx))
+
+    def upload(self, psets, initial: bool = True):
+        structs, hold = [], []
+        for pset in psets:
+            arrs = {f: np.ascontiguousarray(pset.get(f)) for f in ALL_FIELDS if pset.has(f)}
+            for req in ("x", "h", "density", "mass"):
+                if req not in arrs:
+                    arrs[req] = np.ascontiguousarray(pset.get(req))
+            hold.append(arrs)
+            structs.append(particles_struct(arrs, pset.n))
+        arr = (type(structs[0]) * len(structs))(*structs)
+        self._check(self._lib.psph_batch_upload(self._ctx, arr, int(initial)))
+        self._uploaded = list(psets)
+
+    def step(self, nsteps: int, t_stop=None) -> np.ndarray:
+        k = len(self.cfgs)
+        done = np.zeros(k, np.int64)
+        ts = None
+        if t_stop is not None:
+            ts = np.ascontiguousarray(np.broadcast_to(np.asarray(t_stop, np.float64), (k,)))
+        self._check(self._lib.psph_batch_step(
+            self._ctx, int(nsteps), ts.ctypes.data_as(C.POINTER(C.c_double)) if ts is not None else None,
+            done.ctypes.data_as(C.POINTER(C.c_int64))))
+        return done
+
+    def n(self, q: int) -> int:
+        return int(self._lib.psph_batch_num_particles(self._ctx, q))
+
+    def download_fields(self, q: int, fields=ALL_FIELDS) -> dict:
+        n = self.n(q)
+        out = {f: np.zeros(field_shape(f, n), field_dtype(f)) for f in fields}
+        s = particles_struct(out, n)
+        self._check(self._lib.psph_batch_download(self._ctx, q, C.byref(s)))
+        return out
+
+    def original_index(self, q: int) -> np.ndarray:
+        n = self.n(q)
+        out = np.zeros(max(n, 1), np.int64)
+        self._check(self._lib.psph_batch_original_index(self._ctx, q, out.ctypes.data_as(C.POINTER(C.c_int64))))
+        return out[:n]
+
+    def grid(self, q: int) -> PsphGrid:
+        g = PsphGrid()
+        self._check(self._lib.psph_batch_get_grid(self._ctx, q, C.byref(g)))
+        return g
+
+    def integrator(self, q: int) -> PsphIntegrator:
+        it = PsphIntegrator()
+        self._check(self._lib.psph_batch_get_integrator(self._ctx, q, C.byref(it)))
+        return it
+
+    def enable_timing(self, on: bool = True):
+        self._check(self._lib.psph_enable_timing(self._ctx, int(on)))
+
+    def phase_times(self):
+        buf = (C.c_double * 5)()
+        n = C.c_int(0)
+        self._check(self._lib.psph_phase_times(self._ctx, buf, 5, C.byref(n)))
+        return list(buf)
+
+    def step_timed(self, nsteps: int):
+        ms = C.c_double(0.0)
+        done = C.c_int64(0)
+        self._check(self._lib.psph_step_timed(self._ctx, int(nsteps), C.byref(ms), C.byref(done)))
+        return ms.value, done.value
+
+    def pair_count(self) -> int:
+        v = C.c_uint64(0)
+        self._check(self._lib.psph_pair_count(self._ctx, C.byref(v)))
+        return int(v.value)
+
+    def last_launch_count(self) -> int:
+        return int(self._lib.psph_last_launch_count(self._ctx))
+
+
+def _attach_closure(self, net, dx: float):
+    """Learned eddy viscosity for the LES particles of this context (see
+    persiansph_gb300.closure)."""
+    self._check(self._lib.psph_closure_attach(self._ctx, net.handle, float(dx)))
+    self._closure = net
+
+
+def _closure_stats(self):
+    ev, fb = C.c_uint64(0), C.c_uint64(0)
+    self._check(self._lib.psph_closure_stats(self._ctx, C.byref(ev), C.byref(fb)))
+    return int(ev.value), int(fb.value)
+
+
+def _closure_features(self):
+    n = self.n if isinstance(self.n, int) else self.n(0)
+    out = np.zeros((max(n, 1), 6), np.float32)
+    self._check(self._lib.psph_closure_features(self._ctx, out.ctypes.data_as(C.POINTER(C.c_float))))
+    return out[:n]
+
+
+for _cls in (GpuDomain, GpuEnsemble):
+    _cls.attach_closure = _attach_closure
+    _cls.closure_stats = _closure_stats
+    _cls.closure_features = _closure_features

@@ -71,3 +71,20 @@ def test_create_reports_no_device_or_validates():
     assert st == 1
     assert b"dimension" in lib.psph_last_error(ctx)
     lib.psph_destroy(ctx)
+
+
+def test_batch_create_validates_shared_switches():
+    """An ensemble's instances must agree on the physics switches; the check
+    runs before any device call."""
+    lib = abi.load_library()
+    cfgs = (abi.PsphConfig * 2)()
+    for c in cfgs:
+        c.dimension = 2
+        c.shepard_step = 40
+    cfgs[1].kernel_type = 1
+    ctx = ctypes.c_void_p()
+    st = lib.psph_batch_create(cfgs, 2, ctypes.byref(ctx))
+    assert st == 1
+    assert b"instance 1" in lib.psph_last_error(ctx)
+    lib.psph_destroy(ctx)
+    assert lib.psph_batch_create(cfgs, 0, ctypes.byref(ctx)) == 1
