@@ -1,0 +1,504 @@
+/*
+ * SPH::Domain for GB300: the reference's driver-facing API (Source/Domain.h)
+ * with the per-step body of Solve on the GPU through the C ABI (psph.h).
+ *
+ * A driver written for the reference (`#include "Domain.h"`, fill
+ * dom.Particles, call dom.Solve) compiles unchanged with
+ *   g++ -std=c++14 driver.cpp -I include/persiansph -I include
+ *       -L persiansph_gb300/_build -lpsph_gb300
+ * Kept: the enums and selectors (Kernel_Set, Viscosity_Eq_Set,
+ * Gradient_Approach_Set), AddSingleParticle / AddBoxLength / AddBoxNo /
+ * DelParticles, the public data drivers set (Particles, Dimension, Gravity,
+ * Scheme, BC.Periodic, XSPH, InitialDist, DomMax/DomMin, sqrt_h_a, Nproc,
+ * SWIType, FSI) and the hooks (GeneralBefore, GeneralAfter, UserOutput).
+ * Solve (Source/Domain.cpp:1735-1797) keeps its outer loop over output times;
+ * each stretch between outputs is one psph_step call, and the particles are
+ * copied back into dom.Particles at every output time and at the end.
+ *
+ * Differences a driver can see:
+ *  - GeneralBefore / GeneralAfter run on the host in the reference, every
+ *    step. Here Solve calls each hook once on a probe copy of the particles:
+ *    a hook that adds the same acceleration to every free particle and changes
+ *    nothing else (the 1-Poiseuille.cpp UserAcc pattern) becomes a device-side
+ *    body force; any other hook is rejected with a Fatal.
+ *  - Output: the reference writes XDMF/HDF5 snapshots (WriteXDMF); this
+ *    build does not link HDF5 and calls UserOutput-free output hooks only
+ *    through OutputHook (an addition), with the particles already copied back.
+ *  - Additions: Precision (PSPH_FP64 / PSPH_FP32C), BodyForce,
+ *    WallPressureMode, ShepardStep, Time (public), OutputHook.
+ *  - Nproc is accepted and ignored (the work runs on the GPU).
+ */
+#ifndef PERSIANSPH_DOMAIN_H
+#define PERSIANSPH_DOMAIN_H
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <functional>
+#include <iostream>
+#include <utility>
+#include <vector>
+
+#include "Particle.h"
+#include "psph.h"
+
+enum Kernels_Type { Qubic_Spline = 0, Quintic = 1, Quintic_Spline = 2 };
+enum Viscosity_Eq_Type { Morris = 0, Shao = 1, Incompressible_Full = 2, Takeda = 3 };
+enum Gradient_Type { Squared_density = 0, Multiplied_density = 1 };
+
+namespace SPH {
+
+// Boundary (Source/Boundary_Condition.h:25-55); only Periodic is used by the
+// hot path, InOutFlow != 0 is rejected.
+class Boundary {
+ public:
+  double inDensity = 0.0, outDensity = 0.0, allDensity = 0.0;
+  Vec3_t inv, outv, allv;
+  bool Periodic[3] = {false, false, false};
+  int InOutFlow = 0;
+  double InFlowLoc1 = 0.0, InFlowLoc2 = 0.0, InFlowLoc3 = 0.0, OutFlowLoc = 0.0;
+  double cellfac = 3.9;
+  int inoutcounter = 0;
+  bool MassConservation = false;
+};
+
+class Domain;
+inline void General(Domain&) {}
+inline void OutPut(Particle*, double& a, double& b, double& c) { a = b = c = 0.0; }
+inline void InFlowCon(Vec3_t&, Vec3_t&, double&, Boundary&) {}
+
+class Domain {
+ public:
+  typedef void (*PtVel)(Vec3_t& position, Vec3_t& Vel, double& Den, Boundary& bdry);
+  typedef void (*PtOut)(Particle* Particles, double& Prop1, double& Prop2, double& Prop3);
+  typedef void (*PtDom)(Domain& dom);
+
+  Domain() {
+    OutputName[0] = "Property1";
+    OutputName[1] = "Property2";
+    OutputName[2] = "Property3";
+    DomMax = -100000000000.0;
+    DomMin = 100000000000.0;
+  }
+  ~Domain() {
+    for (Particle* p : Particles) delete p;
+  }
+  Domain(const Domain&) = delete;
+  Domain& operator=(const Domain&) = delete;
+
+  // -- selectors (Source/Domain.cpp:117-131) ----------------------------------
+  void Kernel_Set(Kernels_Type const& KT) { KernelType = (int)KT; }
+  void Viscosity_Eq_Set(Viscosity_Eq_Type const& VQ) { VisEq = (int)VQ; }
+  void Gradient_Approach_Set(Gradient_Type const& GT) { GradientType = (int)GT; }
+
+  // -- particle generation ----------------------------------------------------
+  void AddSingleParticle(int tag, Vec3_t const& x, double Mass, double Density, double h, bool Fixed) {
+    Particles.Push(new Particle(tag, x, Vec3_t(0, 0, 0), Mass, Density, h, Fixed));
+  }
+  void AddBoxLength(int tag, Vec3_t const& V, double Lx, double Ly, double Lz, double r, double Density, double h,
+                    int type, int rotation, bool random, bool Fixed);
+  void AddBoxNo(int tag, Vec3_t const& V, size_t nx, size_t ny, size_t nz, double r, double Density, double h,
+                int type, int rotation, bool random, bool Fixed);
+  void DelParticles(int const& Tags);
+
+  // -- solve ------------------------------------------------------------------
+  void Solve(double tf, double dt, double dtOut, char const* TheFileKey, size_t maxidx);
+
+  // -- data (Source/Domain.h:93-145) --------------------------------------------
+  Array<Particle*> Particles;
+  double R = 0.0;
+  double sqrt_h_a = 0.0025;
+  int Dimension = 2;
+  Vec3_t Gravity;
+  size_t SWIType = 0;
+  bool FSI = false;
+  double XSPH = 0.0;
+  double InitialDist = 0.0;
+  size_t Nproc = 1;
+  Boundary BC;
+  PtOut UserOutput = &OutPut;
+  PtVel InCon = &InFlowCon;
+  PtVel OutCon = &InFlowCon;
+  PtVel AllCon = &InFlowCon;
+  Vec3_t DomMax, DomMin;
+  PtDom GeneralBefore = &General;
+  PtDom GeneralAfter = &General;
+  size_t Scheme = 0;
+  String OutputName[3];
+  double Time = 0.0;
+
+  // -- additions of this build ------------------------------------------------
+  int Precision = PSPH_FP64;            // PSPH_FP32C: FP32 pair arithmetic, compensated sums
+  Vec3_t BodyForce;                     // constant acceleration of free particles, on the device
+  int WallPressureMode = PSPH_WALLP_REFERENCE;
+  int ShepardStep = 40;                 // Particle::ShepardStep, uniform over particles
+  std::function<void(Domain&, size_t)> OutputHook;  // called at output times (particles copied back)
+
+ private:
+  int KernelType = 0, VisEq = 0, GradientType = 0;
+
+  // host SoA image of the particles for the C ABI
+  struct Pack {
+    std::vector<int32_t> id, material, is_free, no_slip, pres_eq, shepard, les, vis_m, fail;
+    std::vector<double> vec[7];     // x v va vb a nsv vxsph
+    std::vector<double> sca[32];
+    std::vector<double> ten[12];
+    psph_particles view;
+  };
+  void pack(Pack& pk) const;
+  void unpack(const Pack& pk);
+  Vec3_t hook_acceleration(PtDom hook, const char* name);
+  static void check(psph_status st, psph_ctx* ctx) {
+    if (st != PSPH_OK) {
+      const std::string msg = psph_last_error(ctx);
+      throw new Fatal("%s", msg.c_str());
+    }
+  }
+};
+
+// ---- field tables: SPH::Particle member <-> psph_particles array ----------------
+namespace detail {
+struct VecF { Vec3_t Particle::*m; double* psph_particles::*p; };
+struct ScaF { double Particle::*m; double* psph_particles::*p; };
+struct TenF { Mat3_t Particle::*m; double* psph_particles::*p; };
+inline const VecF* vec_fields() {
+  static const VecF f[7] = {{&Particle::x, &psph_particles::x},     {&Particle::v, &psph_particles::v},
+                            {&Particle::va, &psph_particles::va},   {&Particle::vb, &psph_particles::vb},
+                            {&Particle::a, &psph_particles::a},     {&Particle::NSv, &psph_particles::nsv},
+                            {&Particle::VXSPH, &psph_particles::vxsph}};
+  return f;
+}
+inline const ScaF* sca_fields() {
+  static const ScaF f[32] = {
+      {&Particle::Density, &psph_particles::density},       {&Particle::Densitya, &psph_particles::densitya},
+      {&Particle::Densityb, &psph_particles::densityb},     {&Particle::dDensity, &psph_particles::ddensity},
+      {&Particle::Pressure, &psph_particles::pressure},     {&Particle::Mass, &psph_particles::mass},
+      {&Particle::h, &psph_particles::h},                   {&Particle::Cs, &psph_particles::cs},
+      {&Particle::P0, &psph_particles::p0},                 {&Particle::RefDensity, &psph_particles::ref_density},
+      {&Particle::FPMassC, &psph_particles::fpmassc},       {&Particle::Alpha, &psph_particles::alpha},
+      {&Particle::Beta, &psph_particles::beta},             {&Particle::Mu, &psph_particles::mu},
+      {&Particle::MuRef, &psph_particles::mu_ref},          {&Particle::T0, &psph_particles::t0},
+      {&Particle::m, &psph_particles::bingham_m},           {&Particle::CSmag, &psph_particles::csmag},
+      {&Particle::TI, &psph_particles::ti},                 {&Particle::TIn, &psph_particles::tin},
+      {&Particle::TIInitDist, &psph_particles::ti_init_dist}, {&Particle::G, &psph_particles::g_mod},
+      {&Particle::K, &psph_particles::k_mod},               {&Particle::Sigmay, &psph_particles::sigmay},
+      {&Particle::c, &psph_particles::cohesion},            {&Particle::phi, &psph_particles::phi},
+      {&Particle::psi, &psph_particles::psi},               {&Particle::ZWab, &psph_particles::zwab},
+      {&Particle::SumDen, &psph_particles::sumden},         {&Particle::SumKernel, &psph_particles::sumkernel},
+      {&Particle::ShearRate, &psph_particles::shear_rate},  {&Particle::SBar, &psph_particles::sbar}};
+  return f;
+}
+inline const TenF* ten_fields() {
+  static const TenF f[12] = {
+      {&Particle::Sigma, &psph_particles::sigma},               {&Particle::Sigmaa, &psph_particles::sigmaa},
+      {&Particle::Sigmab, &psph_particles::sigmab},             {&Particle::ShearStress, &psph_particles::shear_stress},
+      {&Particle::ShearStressa, &psph_particles::shear_stressa}, {&Particle::ShearStressb, &psph_particles::shear_stressb},
+      {&Particle::Strain, &psph_particles::strain},             {&Particle::Straina, &psph_particles::straina},
+      {&Particle::Strainb, &psph_particles::strainb},           {&Particle::StrainRate, &psph_particles::strain_rate},
+      {&Particle::RotationRate, &psph_particles::rotation_rate}, {&Particle::TIR, &psph_particles::tir}};
+  return f;
+}
+// while (p <= limit) loop count with p = start, then p = pos(i) (the generators' loop form)
+template <class F>
+inline size_t lattice_count(double start, double limit, F pos) {
+  size_t i = 0;
+  double p = start;
+  while (p <= limit) {
+    ++i;
+    p = pos(i);
+  }
+  return i;
+}
+}  // namespace detail
+
+inline void Domain::pack(Pack& pk) const {
+  const size_t n = Particles.Size();
+  std::memset(&pk.view, 0, sizeof pk.view);
+  pk.view.n = (int64_t)n;
+  auto ints = [&](std::vector<int32_t>& v, int32_t* psph_particles::*p, auto get) {
+    v.resize(n);
+    for (size_t i = 0; i < n; ++i) v[i] = (int32_t)get(*Particles[i]);
+    pk.view.*p = v.data();
+  };
+  ints(pk.id, &psph_particles::id, [](const Particle& q) { return q.ID; });
+  ints(pk.material, &psph_particles::material, [](const Particle& q) { return q.Material; });
+  ints(pk.is_free, &psph_particles::is_free, [](const Particle& q) { return q.IsFree ? 1 : 0; });
+  ints(pk.no_slip, &psph_particles::no_slip, [](const Particle& q) { return q.NoSlip ? 1 : 0; });
+  ints(pk.pres_eq, &psph_particles::pres_eq, [](const Particle& q) { return q.PresEq; });
+  ints(pk.shepard, &psph_particles::shepard, [](const Particle& q) { return q.Shepard ? 1 : 0; });
+  ints(pk.les, &psph_particles::les, [](const Particle& q) { return q.LES ? 1 : 0; });
+  ints(pk.vis_m, &psph_particles::vis_m, [](const Particle& q) { return (int)q.VisM; });
+  ints(pk.fail, &psph_particles::fail, [](const Particle& q) { return (int)q.Fail; });
+  for (int f = 0; f < 7; ++f) {
+    const detail::VecF& F = detail::vec_fields()[f];
+    pk.vec[f].resize(3 * n);
+    for (size_t i = 0; i < n; ++i)
+      for (int d = 0; d < 3; ++d) pk.vec[f][3 * i + d] = ((*Particles[i]).*F.m)(d);
+    pk.view.*F.p = pk.vec[f].data();
+  }
+  for (int f = 0; f < 32; ++f) {
+    const detail::ScaF& F = detail::sca_fields()[f];
+    pk.sca[f].resize(n);
+    for (size_t i = 0; i < n; ++i) pk.sca[f][i] = (*Particles[i]).*F.m;
+    pk.view.*F.p = pk.sca[f].data();
+  }
+  for (int f = 0; f < 12; ++f) {
+    const detail::TenF& F = detail::ten_fields()[f];
+    pk.ten[f].resize(9 * n);
+    for (size_t i = 0; i < n; ++i) std::memcpy(&pk.ten[f][9 * i], ((*Particles[i]).*F.m).data(), 9 * sizeof(double));
+    pk.view.*F.p = pk.ten[f].data();
+  }
+}
+
+// Copies a downloaded image (original order, leavers removed) back into the
+// particle objects; particles that left the domain are deleted as
+// CheckParticleLeave does (Source/Domain.cpp:517-547).
+inline void Domain::unpack(const Pack& pk) {
+  const size_t n = (size_t)pk.view.n;
+  for (size_t i = 0; i < n; ++i) {
+    Particle& q = *Particles[i];
+    for (int f = 0; f < 7; ++f) {
+      const detail::VecF& F = detail::vec_fields()[f];
+      for (int d = 0; d < 3; ++d) (q.*F.m)(d) = pk.vec[f][3 * i + d];
+    }
+    for (int f = 0; f < 32; ++f) q.*(detail::sca_fields()[f].m) = pk.sca[f][i];
+    for (int f = 0; f < 12; ++f) std::memcpy((q.*(detail::ten_fields()[f].m)).data(), &pk.ten[f][9 * i], 9 * sizeof(double));
+  }
+}
+
+// The acceleration a host hook adds to every free particle, found by running
+// it once on the particles with a = 0; throws if the hook does anything else.
+inline Vec3_t Domain::hook_acceleration(PtDom hook, const char* name) {
+  if (hook == &General) return Vec3_t(0, 0, 0);
+  const size_t n = Particles.Size();
+  std::vector<Vec3_t> a0(n), x0(n), v0(n);
+  std::vector<double> rho0(n), mu0(n);
+  for (size_t i = 0; i < n; ++i) {
+    a0[i] = Particles[i]->a;
+    x0[i] = Particles[i]->x;
+    v0[i] = Particles[i]->v;
+    rho0[i] = Particles[i]->Density;
+    mu0[i] = Particles[i]->Mu;
+    Particles[i]->a = 0.0;
+  }
+  hook(*this);
+  bool ok = true, have = false;
+  Vec3_t acc(0, 0, 0);
+  for (size_t i = 0; i < n && ok; ++i) {
+    const Particle& q = *Particles[i];
+    ok = (q.x(0) == x0[i](0) && q.x(1) == x0[i](1) && q.x(2) == x0[i](2) && q.v(0) == v0[i](0) &&
+          q.v(1) == v0[i](1) && q.v(2) == v0[i](2) && q.Density == rho0[i] && q.Mu == mu0[i]);
+    if (!ok) break;
+    if (q.IsFree) {
+      if (!have) {
+        acc = q.a;
+        have = true;
+      } else {
+        ok = (q.a(0) == acc(0) && q.a(1) == acc(1) && q.a(2) == acc(2));
+      }
+    } else {
+      ok = (q.a(0) == 0.0 && q.a(1) == 0.0 && q.a(2) == 0.0);
+    }
+  }
+  if (Particles.Size() != n) ok = false;
+  for (size_t i = 0; i < std::min(n, Particles.Size()); ++i) Particles[i]->a = a0[i];
+  if (!ok)
+    throw new Fatal(
+        "%s: a host hook runs every step in the reference; on the GPU only a hook that adds one constant "
+        "acceleration to the free particles is supported (set Domain::BodyForce for that)",
+        name);
+  return acc;
+}
+
+inline void Domain::AddBoxLength(int tag, Vec3_t const& V, double Lx, double Ly, double Lz, double r, double Density,
+                                 double h, int type, int rotation, bool random, bool Fixed) {
+  // Source/Domain.cpp:294-495: hexagonal (type 0) or cubic (type 1) lattice
+  if (!(type == 0 || type == 1)) throw new Fatal("Packing Type is out of range. Please correct it and run again");
+  if (!(rotation == 0 || rotation == 90))
+    throw new Fatal("Packing Rotation Angle is out of range. Please correct it and run again");
+  const size_t pre = Particles.Size();
+  const double sq3 = std::sqrt(3.0);
+  std::vector<Vec3_t> pts;
+  double mass = 0.0;
+  if (Dimension == 3) {
+    if (type == 0) {
+      const double dz = 2.0 * std::sqrt(6.0) / 3.0;
+      for (int k = 0;; ++k) {
+        const double zp = (k == 0) ? V(2) : V(2) + (dz * k + 1) * r;
+        if (!(zp <= V(2) + Lz - r)) break;
+        for (int j = 0;; ++j) {
+          const double yp = (j == 0) ? V(1) : V(1) + (sq3 * (j + (1.0 / 3.0) * (k % 2)) + 1) * r;
+          if (!(yp <= V(1) + Ly - r)) break;
+          const bool odd = (k % 2 != 0) && (j % 2 != 0);
+          const int off = (j % 2) + (k % 2) + (odd ? -1 : 1);
+          const size_t ni = detail::lattice_count(V(0), V(0) + Lx - r, [&](size_t i) { return V(0) + (2.0 * i + off) * r; });
+          for (size_t i = 0; i < ni; ++i)
+            pts.push_back(Vec3_t(V(0) + (2 * (double)i + off) * r, V(1) + (sq3 * (j + (1.0 / 3.0) * (k % 2)) + 1) * r,
+                                 V(2) + (dz * k + 1) * r));
+        }
+      }
+    } else {
+      const size_t nx = detail::lattice_count(V(0), V(0) + Lx - r, [&](size_t i) { return V(0) + (2.0 * i + 1) * r; });
+      const size_t ny = detail::lattice_count(V(1), V(1) + Ly - r, [&](size_t j) { return V(1) + (2.0 * j + 1) * r; });
+      const size_t nz = detail::lattice_count(V(2), V(2) + Lz - r, [&](size_t k) { return V(2) + (2.0 * k + 1) * r; });
+      for (size_t k = 0; k < nz; ++k)
+        for (size_t j = 0; j < ny; ++j)
+          for (size_t i = 0; i < nx; ++i)
+            pts.push_back(Vec3_t(V(0) + (2.0 * i + 1) * r, V(1) + (2.0 * j + 1) * r, V(2) + (2.0 * k + 1) * r));
+    }
+  } else {
+    if (type == 0) {
+      mass = (sq3 * r * r) * Density;
+      if (rotation == 0) {
+        for (int j = 0;; ++j) {
+          const double yp = (j == 0) ? V(1) : V(1) + (sq3 * j + 1) * r;
+          if (!(yp <= V(1) + Ly - r)) break;
+          const int off = (j % 2) + 1;
+          const size_t ni = detail::lattice_count(V(0), V(0) + Lx - r, [&](size_t i) { return V(0) + (2.0 * i + off) * r; });
+          for (size_t i = 0; i < ni; ++i) pts.push_back(Vec3_t(V(0) + (2 * (double)i + off) * r, V(1) + (sq3 * j + 1) * r, 0.0));
+        }
+      } else {
+        for (int i = 0;; ++i) {
+          const double xp = (i == 0) ? V(0) : V(0) + (sq3 * i + 1) * r;
+          if (!(xp <= V(0) + Lx - r)) break;
+          const int off = (i % 2) + 1;
+          const size_t nj = detail::lattice_count(V(1), V(1) + Ly - r, [&](size_t j) { return V(1) + (2.0 * j + off) * r; });
+          for (size_t j = 0; j < nj; ++j) pts.push_back(Vec3_t(V(0) + (sq3 * i + 1) * r, V(1) + (2 * (double)j + off) * r, 0.0));
+        }
+      }
+    } else {
+      mass = random ? (sq3 * r * r) * Density : 2.0 * r * 2.0 * r * Density;
+      const size_t nx = detail::lattice_count(V(0), V(0) + Lx - r, [&](size_t i) { return V(0) + (2.0 * i + 1) * r; });
+      const size_t ny = detail::lattice_count(V(1), V(1) + Ly - r, [&](size_t j) { return V(1) + (2.0 * j + 1) * r; });
+      for (size_t j = 0; j < ny; ++j)
+        for (size_t i = 0; i < nx; ++i) pts.push_back(Vec3_t(V(0) + (2.0 * i + 1) * r, V(1) + (2.0 * j + 1) * r, 0.0));
+    }
+  }
+  if (random) {  // srand(100), then rand() per jittered coordinate (Source/Domain.cpp:329-330)
+    std::srand(100);
+    const double qin = 0.03;
+    const int ncomp = (Dimension == 3) ? 3 : 2;
+    for (Vec3_t& p : pts)
+      for (int d = 0; d < ncomp; ++d) p(d) = p(d) + qin * r * double(std::rand()) / RAND_MAX;
+  }
+  for (const Vec3_t& p : pts) Particles.Push(new Particle(tag, p, Vec3_t(0, 0, 0), mass, Density, h, Fixed));
+  if (Dimension == 3 && Particles.Size() > pre) {  // 3D mass from the bounding box (Source/Domain.cpp:399-415)
+    Vec3_t mx = V;
+    for (size_t i = pre; i < Particles.Size(); ++i)
+      for (int d = 0; d < 3; ++d)
+        if (Particles[i]->x(d) > mx(d)) mx(d) = Particles[i]->x(d);
+    const double m3 = ((mx(0) + r) - V(0)) * ((mx(1) + r) - V(1)) * ((mx(2) + r) - V(2)) * Density /
+                      (double)(Particles.Size() - pre);
+    for (size_t i = pre; i < Particles.Size(); ++i) Particles[i]->Mass = m3;
+  }
+  R = r;
+}
+
+inline void Domain::AddBoxNo(int tag, Vec3_t const& V, size_t nx, size_t ny, size_t nz, double r, double Density,
+                             double h, int type, int rotation, bool random, bool Fixed) {
+  // Source/Domain.cpp:159-292 with cubic packing; the hexagonal form takes AddBoxLength
+  if (!(type == 0 || type == 1)) throw new Fatal("Packing Type is out of range. Please correct it and run again");
+  if (!(rotation == 0 || rotation == 90))
+    throw new Fatal("Packing Rotation Angle is out of range. Please correct it and run again");
+  if (type != 1) throw new Fatal("AddBoxNo with hexagonal packing: use AddBoxLength");
+  const Vec3_t L((2.0 * nx) * r + r / 10.0, (2.0 * ny) * r + r / 10.0, (2.0 * nz) * r + r / 10.0);
+  AddBoxLength(tag, V, L(0), L(1), Dimension == 3 ? L(2) : 0.0, r, Density, h, type, rotation, random, Fixed);
+}
+
+inline void Domain::DelParticles(int const& Tags) {
+  // Source/Domain.cpp:497-515: order-preserving removal by tag
+  Array<Particle*> kept;
+  for (Particle* p : Particles) {
+    if (p->ID == Tags) delete p;
+    else kept.Push(p);
+  }
+  if (kept.Size() == Particles.Size()) throw new Fatal("Domain::DelParticles: Could not find any particles to delete");
+  Particles.swap(kept);
+}
+
+inline void Domain::Solve(double tf, double dt, double dtOut, char const* TheFileKey, size_t maxidx) {
+  std::cout << "\n--------------Solving---------------------------------------------------------------" << std::endl;
+  if (SWIType != 0 || FSI) throw new Fatal("soil-water interaction and FSI are outside this build");
+  if (BC.InOutFlow != 0) throw new Fatal("in/out-flow boundaries are outside this build");
+  const Vec3_t body = BodyForce + hook_acceleration(GeneralBefore, "GeneralBefore") +
+                      hook_acceleration(GeneralAfter, "GeneralAfter");
+  psph_config cfg;
+  std::memset(&cfg, 0, sizeof cfg);
+  cfg.dimension = Dimension;
+  cfg.kernel_type = KernelType;
+  cfg.vis_eq = VisEq;
+  cfg.gradient_type = GradientType;
+  cfg.scheme = (int)Scheme;
+  for (int d = 0; d < 3; ++d) {
+    cfg.periodic[d] = BC.Periodic[d] ? 1 : 0;
+    cfg.gravity[d] = Gravity(d);
+    cfg.body_force[d] = body(d);
+    cfg.dom_max[d] = DomMax(d);
+    cfg.dom_min[d] = DomMin(d);
+  }
+  cfg.shepard_step = ShepardStep;
+  cfg.precision = Precision;
+  cfg.wall_pressure_mode = WallPressureMode;
+  cfg.xsph = XSPH;
+  cfg.sqrt_h_a = sqrt_h_a;
+  cfg.R = R;
+  cfg.dt = dt;
+  cfg.time = Time;
+
+  psph_ctx* ctx = nullptr;
+  Pack pk;
+  try {
+    const psph_status cst = psph_create(&cfg, &ctx);
+    check(cst, ctx);
+    pack(pk);
+    check(psph_upload(ctx, &pk.view, 1), ctx);
+    size_t idx_out = 1;
+    double tout = Time;
+    auto copy_back = [&]() {
+      const int64_t n = psph_num_particles(ctx);
+      if (n < 0) check(PSPH_ERR_CUDA, ctx);
+      std::vector<int64_t> orig((size_t)std::max<int64_t>(n, 1));
+      check(psph_original_index(ctx, orig.data()), ctx);
+      if ((size_t)n != Particles.Size()) {  // CheckParticleLeave removed some: keep the survivors in order
+        Array<Particle*> kept;
+        std::vector<char> alive(Particles.Size(), 0);
+        for (int64_t r = 0; r < n; ++r) alive[(size_t)orig[(size_t)r]] = 1;
+        for (size_t i = 0; i < Particles.Size(); ++i) {
+          if (alive[i]) kept.Push(Particles[i]);
+          else delete Particles[i];
+        }
+        Particles.swap(kept);
+        pack(pk);
+      }
+      pk.view.n = n;
+      check(psph_download(ctx, &pk.view), ctx);
+      unpack(pk);
+    };
+    while (Time < tf && idx_out <= maxidx) {
+      if (Time >= tout) {
+        copy_back();
+        if (OutputHook) OutputHook(*this, idx_out);
+        if (TheFileKey != nullptr) std::cout << "\nOutput No. " << idx_out << " at " << Time << " has been generated" << std::endl;
+        idx_out++;
+        tout += dtOut;
+      }
+      int64_t done = 0;
+      check(psph_step(ctx, (int64_t)1 << 40, std::min(tf, tout), &done), ctx);
+      psph_integrator it;
+      check(psph_get_integrator(ctx, &it), ctx);
+      Time = it.time;
+      if (done == 0) break;
+    }
+    copy_back();
+  } catch (...) {
+    psph_destroy(ctx);
+    throw;
+  }
+  psph_destroy(ctx);
+  std::cout << "\n--------------Solving is finished---------------------------------------------------" << std::endl;
+}
+
+}  // namespace SPH
+
+#endif  // PERSIANSPH_DOMAIN_H
