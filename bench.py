@@ -43,6 +43,11 @@ FLOPS_PER_DIRECTED_PAIR = 90
 # particle's inputs once (offset+h 16, v+p 16, 1/rho, p/rho^2, c, rho 16, class
 # 4, cell 4) and write its outputs once (a + drho 32, zwab 8, sumden 8).
 FORCE32_BYTES_PER_PARTICLE = 104
+# DRAM bytes per particle one force-kernel launch actually moved: an ncu
+# capture of the same kernel on the same tank at dx = 10 mm (1,021,104
+# particles), dram__bytes_read.sum + dram__bytes_write.sum per particle; the
+# traffic grows with the particle count, so a full-size launch moves this x n.
+FORCE32_TRAFFIC_BYTES_PER_PARTICLE = 304.6
 
 
 def peaks():
@@ -247,13 +252,7 @@ def main():
     force64_ms = m64["phases"][2]
     achieved_gbs = FORCE32_BYTES_PER_PARTICLE * n / (force32_ms * 1e-3) / 1e9
     fp64_tflops = 2 * m64["pairs_per_step"] * FLOPS_PER_DIRECTED_PAIR / (force64_ms * 1e-3) / 1e12
-    traffic = None
-    tf = os.path.join(REPO, "profiles", "force_traffic.json")
-    if os.path.exists(tf):
-        try:
-            traffic = json.load(open(tf)).get("bytes_per_launch_full")
-        except Exception:
-            traffic = None
+    traffic = FORCE32_TRAFFIC_BYTES_PER_PARTICLE * n
 
     # end to end through the C ABI with host buffers: upload + K steps + download
     fields = ("x", "v", "density", "pressure", "a", "ddensity")
