@@ -27,6 +27,11 @@
  *  - Additions: Precision (PSPH_FP64 / PSPH_FP32C), BodyForce,
  *    WallPressureMode, ShepardStep, Time (public), OutputHook.
  *  - Nproc is accepted and ignored (the work runs on the GPU).
+ *
+ * AddBoxLength's lattice arithmetic runs in the driver's own compilation. Arm
+ * compilers fuse x0 + i*2r into one FMA by default, which moves positions by
+ * an ulp against an x86 build of the reference; add -ffp-contract=off for
+ * bit-identical lattices on both.
  */
 #ifndef PERSIANSPH_DOMAIN_H
 #define PERSIANSPH_DOMAIN_H

@@ -283,8 +283,11 @@ psph_status psph_mlp_get_params(const psph_mlp* mlp, float* params, float* norm)
 /* Training set: x[n][6] raw features, y[n] target coefficients c. Sets the
  * normalisation (mean, 1/std, and the range [lo, hi] widened by 5%). */
 psph_status psph_mlp_set_data(psph_mlp* mlp, const float* x, const float* y, int64_t n);
+/* Per-sample loss weights w[n] of the training set (scaled to mean 1; NULL
+ * drops them): loss = mean w (softplus(z) - y)^2. */
+psph_status psph_mlp_set_weights(psph_mlp* mlp, const float* w);
 /* Adam steps on minibatches of the training set (a new seeded permutation per
- * pass); loss = mean (softplus(z) - y)^2. losses[k] (if not NULL) receives
+ * pass); loss = mean w (softplus(z) - y)^2. losses[k] (if not NULL) receives
  * the minibatch loss of step k. */
 psph_status psph_mlp_train(psph_mlp* mlp, int64_t steps, int batch, float lr, uint64_t seed, float* losses);
 /* Loss and gradient over (x, y) without changing the parameters. */

@@ -110,7 +110,9 @@ LIB_NAME = "libpsph_gb300.so"
 
 
 def library_path() -> str:
-    return os.path.join(_HERE, "_build", LIB_NAME)
+    """The in-tree build, or the file PSPH_LIBRARY names (another build of the
+    same sources, e.g. with different tuning flags)."""
+    return os.environ.get("PSPH_LIBRARY") or os.path.join(_HERE, "_build", LIB_NAME)
 
 
 _lib = None
@@ -182,6 +184,7 @@ def _declare(lib):
     lib.psph_mlp_set_params.argtypes = [C.c_void_p, fp, fp]
     lib.psph_mlp_get_params.argtypes = [C.c_void_p, fp, fp]
     lib.psph_mlp_set_data.argtypes = [C.c_void_p, fp, fp, C.c_int64]
+    lib.psph_mlp_set_weights.argtypes = [C.c_void_p, fp]
     lib.psph_mlp_train.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_float, C.c_uint64, fp]
     lib.psph_mlp_loss_grad.argtypes = [C.c_void_p, fp, fp, C.c_int64, P(C.c_double), fp]
     lib.psph_mlp_infer.argtypes = [C.c_void_p, fp, C.c_int64, fp, C.c_int]
@@ -189,6 +192,7 @@ def _declare(lib):
     lib.psph_closure_stats.argtypes = [ctx, P(C.c_uint64), P(C.c_uint64)]
     lib.psph_closure_features.argtypes = [ctx, fp]
     for name in ("psph_mlp_create", "psph_mlp_set_params", "psph_mlp_get_params", "psph_mlp_set_data",
+                 "psph_mlp_set_weights",
                  "psph_mlp_train", "psph_mlp_loss_grad", "psph_mlp_infer", "psph_closure_attach",
                  "psph_closure_stats", "psph_closure_features"):
         getattr(lib, name).restype = C.c_int

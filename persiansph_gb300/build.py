@@ -40,17 +40,20 @@ def _stale(lib, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
-    os.makedirs(OUT, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, extra_flags=(), out_dir=None) -> str:
+    """Compiles the library into out_dir (default persiansph_gb300/_build)."""
+    out = out_dir or OUT
+    lib_path = os.path.join(out, "libpsph_gb300.so")
+    os.makedirs(out, exist_ok=True)
     srcs = sources()
     deps = srcs + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))] + \
         [os.path.join(REPO, "include", f) for f in os.listdir(os.path.join(REPO, "include"))]
-    if not force and not _stale(LIB, deps):
-        return LIB
+    if not force and not _stale(lib_path, deps):
+        return lib_path
     nv = nvcc()
 
     def compile_one(src):
-        obj = os.path.join(OUT, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(out, os.path.basename(src)[:-3] + ".o")
         cmd = [nv, *ARCH, *NVCC_FLAGS, *extra_flags, "-c", src, "-o", obj]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
@@ -61,13 +64,13 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
 
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(compile_one, srcs))
-    tmp = LIB + ".tmp"
+    tmp = lib_path + ".tmp"
     cmd = [nv, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":

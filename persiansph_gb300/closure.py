@@ -84,6 +84,14 @@ class ClosureNet:
         assert len(x) == len(y)
         self._check(self._lib.psph_mlp_set_data(self._h, _fp(x), _fp(y), len(y)))
 
+    def set_weights(self, w=None):
+        """Per-sample loss weights of the training set (None: uniform)."""
+        if w is None:
+            self._check(self._lib.psph_mlp_set_weights(self._h, None))
+            return
+        w = np.ascontiguousarray(w, np.float32).reshape(-1)
+        self._check(self._lib.psph_mlp_set_weights(self._h, _fp(w)))
+
     def train(self, steps: int, batch: int = 4096, lr: float = 1e-3, seed: int = 0) -> np.ndarray:
         losses = np.zeros(max(steps, 1), np.float32)
         self._check(self._lib.psph_mlp_train(self._h, int(steps), int(batch), float(lr), C.c_uint64(seed),

@@ -123,12 +123,14 @@ def main(argv=None):
 
     net = ClosureNet(seed=args.seed)
     net.set_data(X, Y)
+    # the loss in eddy-viscosity units: nu = c h^2 ShearRate, so weight (h^2 ShearRate)^2
+    w = H * H * S
+    net.set_weights(w * w)
     t1 = time.perf_counter()
     losses = net.train(args.steps, batch=min(args.batch, len(Y)), lr=args.lr, seed=args.seed + 1)
     report["train_seconds"] = time.perf_counter() - t1
     report["loss_first"] = float(np.mean(losses[:20]))
     report["loss_last"] = float(np.mean(losses[-100:]))
-    w = H * H * S
     c_const = float(np.sum(Y * w * w) / np.sum(w * w))
     report["c_const"] = c_const
     report["apriori_held_out"] = apriori_errors(net, Xh, Yh, Hh, Sh, c_const)

@@ -20,6 +20,11 @@ namespace psph {
 namespace {
 
 constexpr int kFT32 = 128;
+// Minimum resident blocks per SM asked of the register allocator for the pair
+// kernel (1 = no limit: ~123 registers, 4 blocks per SM).
+#ifndef PSPH_FT32_MINB
+#define PSPH_FT32_MINB 1
+#endif
 constexpr int kQ32 = 16;  // queued wall-interpolation partners per lane
 
 struct Kahan {
@@ -236,7 +241,7 @@ __global__ void __launch_bounds__(kFT32) prepare32_kernel(DevView v) {
 // Fluid pair force, FP32 with compensated sums, over the neighbour lists
 // ---------------------------------------------------------------------------
 template <int DIM, int KT>
-__global__ void __launch_bounds__(kFT32) forces_fluid32_kernel(DevView v) {
+__global__ void __launch_bounds__(kFT32, PSPH_FT32_MINB) forces_fluid32_kernel(DevView v) {
   __shared__ double red[kFT32 / 32];
   __shared__ unsigned long long cred[kFT32 / 32];
   const StepScalars* sc = v.sc;

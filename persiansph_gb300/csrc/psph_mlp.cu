@@ -461,16 +461,19 @@ __global__ void train_fwd_kernel(const float* __restrict__ params, const float* 
 
 // dL/dz4 and the per-block loss partial sums (fixed-order reduction on the host).
 __global__ void train_loss_kernel(const float* __restrict__ Z4, const float* __restrict__ Y,
-                                  const int* __restrict__ idx, int B, float* G4, double* loss_part) {
+                                  const float* __restrict__ W, const int* __restrict__ idx, int B, float* G4,
+                                  double* loss_part) {
   __shared__ double red[kTrainThreads];
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   double l = 0.0;
   if (b < B) {
+    const int row = idx ? idx[b] : b;
     const float z = Z4[b];
-    const float y = Y[idx ? idx[b] : b];
+    const float y = Y[row];
+    const float w = W ? W[row] : 1.f;
     const float e = softplus(z) - y;
-    G4[b] = 2.f * e * sigm(z) / (float)B;
-    l = (double)e * (double)e;
+    G4[b] = 2.f * w * e * sigm(z) / (float)B;
+    l = (double)w * (double)e * (double)e;
   }
   red[threadIdx.x] = l;
   __syncthreads();
@@ -656,6 +659,7 @@ struct psph_mlp {
   // training data
   float* d_X = nullptr;
   float* d_Y = nullptr;
+  float* d_W = nullptr;  // per-sample loss weights (mean 1), or none
   int64_t n_data = 0;
   // minibatch scratch
   int cap = 0, nchunk_cap = 0;
@@ -716,13 +720,14 @@ psph_status ensure_batch(psph_mlp* m, int B) {
 }
 
 // Loss and gradient of one minibatch (rows idx of X/Y, or the first B rows).
-psph_status batch_grad(psph_mlp* m, const float* dX, const float* dY, const int* d_idx, int B, double* loss) {
+psph_status batch_grad(psph_mlp* m, const float* dX, const float* dY, const float* dW, const int* d_idx, int B,
+                       double* loss) {
   psph_status st = ensure_batch(m, B);
   if (st) return st;
   const int nb = (B + kTrainThreads - 1) / kTrainThreads;
   train_fwd_kernel<<<nb, kTrainThreads>>>(m->d_params, m->d_norm, dX, d_idx, B, m->d_U, m->d_Z1, m->d_Z2, m->d_Z3,
                                           m->d_Z4);
-  train_loss_kernel<<<nb, kTrainThreads>>>(m->d_Z4, dY, d_idx, B, m->d_G4, m->d_loss);
+  train_loss_kernel<<<nb, kTrainThreads>>>(m->d_Z4, dY, dW, d_idx, B, m->d_G4, m->d_loss);
   train_bwd_kernel<<<nb, kTrainThreads>>>(m->d_params, m->d_Z1, m->d_Z2, m->d_Z3, m->d_G4, B, m->d_D1, m->d_D2,
                                           m->d_D3);
   const int chunk = 128, nchunk = (B + chunk - 1) / chunk;
@@ -822,7 +827,7 @@ psph_status psph_mlp_create(uint64_t seed, psph_mlp** out) {
 void psph_mlp_destroy(psph_mlp* m) {
   if (!m) return;
   cudaDeviceSynchronize();
-  for (float** p : {&m->d_params, &m->d_m, &m->d_v, &m->d_grad, &m->d_norm, &m->d_X, &m->d_Y, &m->d_U, &m->d_Z1,
+  for (float** p : {&m->d_params, &m->d_m, &m->d_v, &m->d_grad, &m->d_norm, &m->d_X, &m->d_Y, &m->d_W, &m->d_U, &m->d_Z1,
                     &m->d_Z2, &m->d_Z3, &m->d_Z4, &m->d_G4, &m->d_D1, &m->d_D2, &m->d_D3, &m->d_part})
     dfree(*p);
   dfree(m->d_img);
@@ -860,6 +865,7 @@ psph_status psph_mlp_set_data(psph_mlp* m, const float* x, const float* y, int64
   if (!m || !x || !y || n < 1 || n > (1LL << 30)) return PSPH_ERR_INVALID_ARGUMENT;
   dfree(m->d_X);
   dfree(m->d_Y);
+  dfree(m->d_W);
   MLP_TRY(m, cudaMalloc(&m->d_X, (size_t)n * kMlpIn * sizeof(float)));
   MLP_TRY(m, cudaMalloc(&m->d_Y, (size_t)n * sizeof(float)));
   MLP_TRY(m, cudaMemcpy(m->d_X, x, (size_t)n * kMlpIn * sizeof(float), cudaMemcpyHostToDevice));
@@ -888,6 +894,25 @@ psph_status psph_mlp_set_data(psph_mlp* m, const float* x, const float* y, int64
   return PSPH_OK;
 }
 
+psph_status psph_mlp_set_weights(psph_mlp* m, const float* w) {
+  if (!m) return PSPH_ERR_INVALID_ARGUMENT;
+  if (!m->n_data) return mlp_err(m, PSPH_ERR_STATE, "psph_mlp_set_weights before psph_mlp_set_data");
+  dfree(m->d_W);
+  if (!w) return PSPH_OK;
+  double s = 0.0;
+  for (int64_t i = 0; i < m->n_data; ++i) {
+    if (!(w[i] >= 0.0f) || !std::isfinite(w[i])) return mlp_err(m, PSPH_ERR_INVALID_ARGUMENT, "weight %lld is not a finite non-negative number", (long long)i);
+    s += w[i];
+  }
+  if (!(s > 0.0)) return mlp_err(m, PSPH_ERR_INVALID_ARGUMENT, "weights sum to zero");
+  std::vector<float> wn(m->n_data);
+  const double scale = (double)m->n_data / s;  // mean weight 1
+  for (int64_t i = 0; i < m->n_data; ++i) wn[i] = (float)(w[i] * scale);
+  MLP_TRY(m, cudaMalloc(&m->d_W, (size_t)m->n_data * sizeof(float)));
+  MLP_TRY(m, cudaMemcpy(m->d_W, wn.data(), (size_t)m->n_data * sizeof(float), cudaMemcpyHostToDevice));
+  return PSPH_OK;
+}
+
 psph_status psph_mlp_train(psph_mlp* m, int64_t steps, int batch, float lr, uint64_t seed, float* losses) {
   if (!m || steps < 0 || batch < 1 || !(lr > 0.f)) return PSPH_ERR_INVALID_ARGUMENT;
   if (!m->n_data) return mlp_err(m, PSPH_ERR_STATE, "psph_mlp_train before psph_mlp_set_data");
@@ -910,7 +935,7 @@ psph_status psph_mlp_train(psph_mlp* m, int64_t steps, int batch, float lr, uint
     MLP_TRY(m, cudaMemcpy(m->d_idx, perm.data() + pos, B * sizeof(int), cudaMemcpyHostToDevice));
     pos += B;
     double loss = 0.0;
-    if ((st = batch_grad(m, m->d_X, m->d_Y, m->d_idx, B, losses ? &loss : nullptr))) return st;
+    if ((st = batch_grad(m, m->d_X, m->d_Y, m->d_W, m->d_idx, B, losses ? &loss : nullptr))) return st;
     m->adam_t += 1;
     const float c1 = (float)(1.0 - std::pow((double)b1, (double)m->adam_t));
     const float c2 = (float)(1.0 - std::pow((double)b2, (double)m->adam_t));
@@ -931,7 +956,7 @@ psph_status psph_mlp_loss_grad(psph_mlp* m, const float* x, const float* y, int6
   MLP_TRY(m, cudaMemcpy(dX, x, (size_t)n * kMlpIn * sizeof(float), cudaMemcpyHostToDevice));
   MLP_TRY(m, cudaMemcpy(dY, y, (size_t)n * sizeof(float), cudaMemcpyHostToDevice));
   double l = 0.0;
-  psph_status st = batch_grad(m, dX, dY, nullptr, (int)n, &l);
+  psph_status st = batch_grad(m, dX, dY, nullptr, nullptr, (int)n, &l);
   if (!st && grad) {
     cudaError_t e = cudaMemcpy(grad, m->d_grad, kNParams * sizeof(float), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) st = mlp_err(m, PSPH_ERR_CUDA, "gradient copy: %s", cudaGetErrorString(e));

@@ -17,7 +17,7 @@ namespace {
 
 constexpr int kNT = 128;
 
-template <int DIM>
+template <int DIM, bool UNIFORM_H>
 __global__ void __launch_bounds__(kNT) nlist_kernel(DevView v, float margin) {
   const StepScalars* sc = v.sc;
   if (sc->all_stop) return;
@@ -33,40 +33,58 @@ __global__ void __launch_bounds__(kNT) nlist_kernel(DevView v, float margin) {
   const float3 cs = cell_size_f(g);
   const float4 oi = v.S.OFF32[i];
   const float cf = (float)g.cellfac;
+  // support test r^2 <= (Cellfac hb)^2 margin; with one h everywhere it is a constant
+  const float thr_u = cf * cf * oi.w * oi.w * margin;
   const int N = v.ncap, cap = v.o.nl_cap;
   const CellCoord c = decode(g, cell);
-  const bool wrapx = g.periodic[0] && (c.x == 0 || c.x == g.nc[0] - 1);
+  const float4* __restrict__ off = v.S.OFF32;
+  const int* __restrict__ start = v.S.start;
   int* __restrict__ out = v.S.nl + i;
+  // Whole cells whose nearest point lies outside the support are skipped. The
+  // bound assumes the in-cell offset of i lies in [0, cell size), which holds
+  // away from the grid faces (ListGenerate clamps only there); a neighbour
+  // cell's clamped particles lie beyond its outer face, farther from i.
+  const bool inner = c.x > 0 && c.x < g.nc[0] - 1 && c.y > 0 && c.y < g.nc[1] - 1 &&
+                     (DIM == 2 || (c.z > 0 && c.z < g.nc[2] - 1));
+  const bool cull = UNIFORM_H && inner;
+  const float thr_cull = thr_u * 1.0001f;
   int k = 0;
   const int zlo = (DIM == 3) ? -1 : 0, zhi = (DIM == 3) ? 1 : 0;
   for (int dz = zlo; dz <= zhi; ++dz) {
     int z = c.z + dz;
     if (g.periodic[2]) z = (z + g.nc[2]) % g.nc[2];
     else if (z < 0 || z >= g.nc[2]) continue;
+    const float gz = (DIM == 3) ? (dz < 0 ? oi.z : (dz > 0 ? cs.z - oi.z : 0.f)) : 0.f;
     for (int dy = -1; dy <= 1; ++dy) {
       int y = c.y + dy;
       if (g.periodic[1]) y = (y + g.nc[1]) % g.nc[1];
       else if (y < 0 || y >= g.nc[1]) continue;
+      const float gy = dy < 0 ? oi.y : (dy > 0 ? cs.y - oi.y : 0.f);
       const int base = g.cell_base + (z * g.nc[1] + y) * g.nc[0];
       const int cyz = 3 * (dy + 1) + 9 * (dz + 1);
-      for (int sub = 0; sub < (wrapx ? 3 : 1); ++sub) {
-        int lo, hi;
-        if (!wrapx) {
-          lo = v.S.start[base + max(c.x - 1, 0)];
-          hi = v.S.start[base + min(c.x + 1, g.nc[0] - 1) + 1];
-        } else {
-          const int x = (c.x + sub - 1 + g.nc[0]) % g.nc[0];
-          lo = v.S.start[base + x];
-          hi = v.S.start[base + x + 1];
+      const float cy = -(float)dy * cs.y, cz = -(float)dz * cs.z;  // exact: dy, dz in {-1, 0, 1}
+      for (int dx = -1; dx <= 1; ++dx) {
+        int x = c.x + dx;
+        if (g.periodic[0]) x = (x + g.nc[0]) % g.nc[0];
+        else if (x < 0 || x >= g.nc[0]) continue;
+        if (cull) {
+          const float gx = dx < 0 ? oi.x : (dx > 0 ? cs.x - oi.x : 0.f);
+          if (gx * gx + gy * gy + gz * gz > thr_cull) continue;
         }
+        const int lo = start[base + x], hi = start[base + x + 1];
+        const int code = (dx + 1) + cyz;
+        const float cx = -(float)dx * cs.x;
         for (int j = lo; j < hi; ++j) {
-          const int dxc = wrapx ? sub - 1 : v.S.cellid[j] - base - c.x;
-          const int code = (dxc + 1) + cyz;
-          const float4 oj = v.S.OFF32[j];
-          float x0, x1, x2;
-          rel_pos<DIM>(cs, oi, oj, code, x0, x1, x2);
-          const float hb = 0.5f * (oi.w + oj.w);
-          if (x0 * x0 + x1 * x1 + x2 * x2 <= cf * cf * hb * hb * margin && j != i) {
+          const float4 oj = off[j];
+          // x_i - x_j as rel_pos forms it: cell offset + (offset_i - offset_j)
+          const float x0 = cx + (oi.x - oj.x), x1 = cy + (oi.y - oj.y);
+          const float x2 = (DIM == 3) ? cz + (oi.z - oj.z) : 0.f;
+          float thr = thr_u;
+          if (!UNIFORM_H) {
+            const float hb = 0.5f * (oi.w + oj.w);
+            thr = cf * cf * hb * hb * margin;
+          }
+          if (x0 * x0 + x1 * x1 + x2 * x2 <= thr && j != i) {
             if (k < cap) out[(size_t)k * N] = j | (code << kCodeShift);
             ++k;
           }
@@ -82,8 +100,14 @@ __global__ void __launch_bounds__(kNT) nlist_kernel(DevView v, float margin) {
 void launch_nlist(const DevView& v, cudaStream_t st) {
   const int nb = v.ncap > 0 ? (v.ncap + kNT - 1) / kNT : 1;
   const float margin = v.o.fp32 ? 1.0f : 1.004f;
-  if (v.o.dim == 2) nlist_kernel<2><<<nb, kNT, 0, st>>>(v, margin);
-  else nlist_kernel<3><<<nb, kNT, 0, st>>>(v, margin);
+  const bool uh = v.o.uniform_h;
+  if (v.o.dim == 2) {
+    if (uh) nlist_kernel<2, true><<<nb, kNT, 0, st>>>(v, margin);
+    else nlist_kernel<2, false><<<nb, kNT, 0, st>>>(v, margin);
+  } else {
+    if (uh) nlist_kernel<3, true><<<nb, kNT, 0, st>>>(v, margin);
+    else nlist_kernel<3, false><<<nb, kNT, 0, st>>>(v, margin);
+  }
 }
 
 }  // namespace psph

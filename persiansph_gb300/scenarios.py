@@ -263,3 +263,21 @@ def granular_column(dx=1e-3, W=0.2, aspect=1.0, TL_factor=4.0, wall_layers=3, rh
     dt = 0.2 * h / cs
     return dom, dt, {"H": H, "W": W, "K": K, "G": G, "cs": cs, "h": h, "n_soil": int(fl.sum()),
                      "n_wall": int(wall.sum())}
+
+
+def granular_ensemble(n=256, seed=0, dx=1e-3, W=0.2, aspect=(0.5, 4.0), phi_deg=(20.0, 40.0), fail=2, **kw):
+    """The batched granular-column workload: n independent 2D columns of width W
+    at lattice spacing dx, aspect ratio H/W and friction angle drawn uniformly
+    from the given ranges (numpy default_rng(seed)), cohesion 0, rho 1850,
+    E 0.84 MPa, nu 0.3, Monaghan tensile-instability correction on. Particle
+    counts follow from the geometry: W = 0.2 m at dx = 1 mm gives 200 x 100 to
+    200 x 800 soil particles per column. Returns [(domain, dt, info)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        a = float(rng.uniform(*aspect))
+        phi = float(rng.uniform(*phi_deg))
+        dom, dt, info = granular_column(dx=dx, W=W, aspect=a, phi_deg=phi, fail=fail, cohesion=0.0, **kw)
+        info.update({"aspect": a, "phi_deg": phi})
+        out.append((dom, dt, info))
+    return out

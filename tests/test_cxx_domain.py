@@ -21,7 +21,9 @@ GOLD = os.path.join(REPO, "tests", "golden")
 def build(src, out):
     lib = os.path.dirname(abi.library_path())
     abi.load_library()  # builds the library when it is missing or stale
-    cmd = ["g++", "-std=c++14", "-O2", "-Wall", "-I", os.path.join(REPO, "include", "persiansph"), "-I",
+    # -ffp-contract=off: no fused multiply-add in the lattice arithmetic (Arm
+    # compilers contract by default), so positions match the x86 build bit for bit
+    cmd = ["g++", "-std=c++14", "-O2", "-Wall", "-ffp-contract=off", "-I", os.path.join(REPO, "include", "persiansph"), "-I",
            os.path.join(REPO, "include"), src, "-L", lib, "-lpsph_gb300", f"-Wl,-rpath,{lib}", "-o", out]
     subprocess.run(cmd, check=True, capture_output=True, text=True)
     return out

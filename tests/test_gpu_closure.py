@@ -211,9 +211,10 @@ def test_closure_gain_over_smagorinsky(gpu):
     assert len(Y) > 1000 and len(Yh) > 200
     net = ClosureNet(seed=21)
     net.set_data(X, Y)
+    w = H * H * S
+    net.set_weights(w * w)  # loss in eddy-viscosity units
     losses = net.train(1500, batch=min(2048, len(Y)), lr=2e-3, seed=22)
     assert np.mean(losses[-50:]) < np.mean(losses[:10])
-    w = H * H * S
     c_const = float(np.sum(Y * w * w) / np.sum(w * w))  # best constant coefficient (least squares in nu)
     errs = apriori_errors(net, Xh, Yh, Hh, Sh, c_const)
     assert errs["network"] < errs["smagorinsky"], errs
