@@ -32,7 +32,8 @@ import numpy as np
 REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
-METRIC = "pair-interactions/s @ 3D dam break (5.28M fluid particles), FP32C form; FP64 plain beside it"
+METRIC = ("pair-interactions/s @ 3D dam break (5.28M fluid particles), FP32C form with the learned closure; "
+          "FP64 plain beside it")
 UNIT = "pair-interactions/s"
 # FP64 operations per directed pair evaluation of the fluid kernel for this
 # workload's options (Wendland, Tait, artificial viscosity, Morris, squared
@@ -138,6 +139,41 @@ def build_workload(dx):
     return scenarios.dam_break_3d(dx=dx)
 
 
+def measure_ensemble(n_inst: int, dx: float, steps: int, warmup: int):
+    """The batched granular-column workload (CalcForce2233 + Mat3): n_inst
+    independent 2D columns in one context, FP32C pair sums with the FP64
+    stress return mapping, each step one CUDA-graph launch sequence for all
+    instances. Returns its line object."""
+    from persiansph_gb300 import scenarios
+    from persiansph_gb300.solver import GpuEnsemble
+    cases = scenarios.granular_ensemble(n=n_inst, seed=0, dx=dx)
+    cfgs = []
+    for dom, dt, _ in cases:
+        cfg = dom.config(dt)
+        cfg.precision = 1  # PSPH_FP32C
+        cfgs.append(cfg)
+    ens = GpuEnsemble(cfgs)
+    ens.upload([d.particles for d, _, _ in cases], initial=True)
+    ens.step(warmup)
+    pc0 = ens.pair_count()
+    ms, done = ens.step_timed(steps)
+    pairs = ens.pair_count() - pc0
+    launches = ens.last_launch_count()
+    ens.enable_timing(True)
+    ens.step(2)
+    phases = {k: x / 2.0 for k, x in ens.phase_times().items()}
+    ens.close()
+    counts = [d.particles.n for d, _, _ in cases]
+    soil = [i["n_soil"] for _, _, i in cases]
+    return {"workload": f"{n_inst} 2D granular columns (Drucker-Prager soil, Fail 2, TI on), W=0.2 m, "
+                        f"H/W ~ U[0.5,4], phi ~ U[20,40] deg, dx={dx} m (seed 0)",
+            "instances": n_inst, "particles": int(sum(counts)), "soil_per_instance": [int(min(soil)), int(max(soil))],
+            "form": "FP32C pair sums, FP64 stress return mapping", "steps": done,
+            "ms_per_step": ms / max(done, 1), "steps_per_s": done / (ms * 1e-3),
+            "pair_interactions_per_s": pairs / (ms * 1e-3), "pairs_per_step": pairs / max(done, 1),
+            "gpu_launches_per_step": launches / max(done, 1), "phase_ms": phases}
+
+
 def cpu_reference(dx_sample: float, steps: int, warmup: int, threads: int):
     """Times the CPU oracle (restatement of the reference's OpenMP path) on the
     same tank at a coarser lattice; returns pair-interactions/s and details."""
@@ -187,6 +223,9 @@ def main():
     ap.add_argument("--dx", type=float, default=0.005)
     ap.add_argument("--ref-dx", type=float, default=0.01)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the batched granular-column line")
+    ap.add_argument("--ens-n", type=int, default=256)
+    ap.add_argument("--ens-dx", type=float, default=1e-3)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -209,12 +248,23 @@ def main():
 
     dom, dt, info = build_workload(args.dx)
     n = dom.particles.n
+    from persiansph_gb300.closure import ClosureNet, default_network_path
+    net = ClosureNet.load(default_network_path())
+    les_particles = dom.particles.copy()
+    les_particles.set("les", 1)  # every fluid particle takes its eddy viscosity from the network
 
-    def measure(precision):
+    def open_domain(precision, closure):
         cfg = dom.config(dt)
         cfg.precision = precision
         gd = GpuDomain(cfg)
-        gd.upload(dom.particles, initial=True)
+        gd.upload(les_particles if closure else dom.particles, initial=True)
+        if closure:
+            gd.attach_closure(net, args.dx)
+        return cfg, gd
+
+    def measure(precision, closure=False):
+        cfg, gd = open_domain(precision, closure)
+        tuning = gd.autotune(3)  # launch shapes timed on this workload's own (untimed) steps
         with ClockSampler(local) as clk:
             gd.step(args.warmup)
             pc0 = gd.pair_count()
@@ -234,22 +284,24 @@ def main():
         # per-phase device times (separate short run, events between phases)
         gd.enable_timing(True)
         gd.step(3)
-        phases = [x / 3.0 for x in gd.phase_times()]
+        phases = {k: x / 3.0 for k, x in gd.phase_times().items()}
         gd.enable_timing(False)
-        gd.close()
         pairs = pc1 - pc0
-        return {"cfg": cfg, "ms": ms, "done": done, "pairs": pairs, "launches": launches, "phases": phases,
+        cstats = gd.closure_stats() if closure else (0, 0)
+        gd.close()
+        return {"cfg": cfg, "tuning": tuning, "closure_evaluated": cstats[0], "closure_fallbacks": cstats[1], "ms": ms, "done": done, "pairs": pairs, "launches": launches, "phases": phases,
                 "clocks": clk.summary(), "value_rank": pairs / (ms * 1e-3), "steps_per_s": done / (ms * 1e-3),
                 "pairs_per_step": pairs / max(done, 1)}
 
-    m32 = measure(1)   # PSPH_FP32C: the headline form
-    m64 = measure(0)   # PSPH_FP64: the plain form
+    m32 = measure(1, closure=True)  # PSPH_FP32C + learned closure: the headline form
+    m32n = measure(1)                # PSPH_FP32C without the closure (LES off)
+    m64 = measure(0)                 # PSPH_FP64: the plain form
     lib = abi.load_library()
     fp64 = ctypes.c_double(0.0)
     lib.psph_probe_fp64_peak(ctypes.byref(fp64))
     pk = peaks()
-    force32_ms = m32["phases"][2]
-    force64_ms = m64["phases"][2]
+    force32_ms = m32["phases"]["forces"]
+    force64_ms = m64["phases"]["forces"]
     achieved_gbs = FORCE32_BYTES_PER_PARTICLE * n / (force32_ms * 1e-3) / 1e9
     fp64_tflops = 2 * m64["pairs_per_step"] * FLOPS_PER_DIRECTED_PAIR / (force64_ms * 1e-3) / 1e12
     traffic = FORCE32_TRAFFIC_BYTES_PER_PARTICLE * n
@@ -257,8 +309,7 @@ def main():
     # end to end through the C ABI with host buffers: upload + K steps + download
     fields = ("x", "v", "density", "pressure", "a", "ddensity")
     t0 = time.perf_counter()
-    ge = GpuDomain(m32["cfg"])
-    ge.upload(dom.particles, initial=True)
+    _, ge = open_domain(1, True)
     done_e = ge.step(args.steps)
     out = ge.download_fields(fields)
     torch.cuda.synchronize()
@@ -269,8 +320,7 @@ def main():
     d2h = sum(a.nbytes for a in out.values())
 
     def phase_dict(m):
-        p = m["phases"]
-        return {"sort": p[0], "prepare_walls": p[1], "forces": p[2], "dt": p[3], "update": p[4]}
+        return dict(m["phases"])
 
     world_mult = world
     line = {
@@ -282,14 +332,19 @@ def main():
         "config": {"workload": "3D dam break: tank 3.22x1.0x1.0 m, column 1.2x0.55x1.0 m, dx=%g m" % args.dx,
                    "particles": n, "fluid": info["n_fluid"], "walls": info["n_wall"], "kernel": "Wendland C2",
                    "h_over_dx": 1.3, "eos": "Tait c0=40", "scheme": "Modified Verlet + Shepard",
-                   "form": "FP32C (closure off)", "parallelism": "replicas only" if world > 1 else "single GPU",
+                   "form": "FP32C + learned eddy-viscosity closure (LES on every fluid particle)", "parallelism": "replicas only" if world > 1 else "single GPU",
                    "l2": "working set > L2"},
-        "steps_per_s": m32["steps_per_s"], "pairs_per_step": m32["pairs_per_step"],
+        "steps_per_s": m32["steps_per_s"], "pairs_per_step": m32["pairs_per_step"], "tuning": m32["tuning"],
         "phase_ms": phase_dict(m32),
+        "closure": {"evaluated": m32["closure_evaluated"], "fallbacks": m32["closure_fallbacks"],
+                    "network": os.path.relpath(default_network_path(), REPO)},
+        "fp32c_no_closure": {"value": m32n["value_rank"] * world_mult, "unit": UNIT,
+                             "steps_per_s": m32n["steps_per_s"], "ms_per_step": m32n["ms"] / max(m32n["done"], 1),
+                             "phase_ms": phase_dict(m32n)},
         "fp64_plain": {"value": m64["value_rank"] * world_mult, "unit": UNIT, "steps_per_s": m64["steps_per_s"],
                        "ms_per_step": m64["ms"] / max(m64["done"], 1), "phase_ms": phase_dict(m64),
                        "clocks": m64["clocks"]},
-        "fp32c_over_fp64_steps_per_s": m32["steps_per_s"] / m64["steps_per_s"],
+        "fp32c_closure_over_fp64_steps_per_s": m32["steps_per_s"] / m64["steps_per_s"],
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved_gbs / pk["hbm_gbs"], "traffic": traffic,
                      "kernel": "forces_fluid32_kernel", "peak_source": pk["src"],
@@ -304,6 +359,8 @@ def main():
                 "note": "create + upload + steps + download through the C ABI, host wall clock"},
         "gpu_launches": m32["launches"],
     }
+    if not args.no_ensemble:
+        line["ensemble"] = measure_ensemble(args.ens_n, args.ens_dx, max(args.steps // 2, 5), args.warmup)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         r = cpu_reference(args.ref_dx, 2, 1, threads)

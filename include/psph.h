@@ -184,8 +184,9 @@ psph_status psph_get_integrator(const psph_ctx* ctx, psph_integrator* integ);
 psph_status psph_pairs_export(psph_ctx* ctx, int which, int64_t* pairs, int64_t cap, int64_t* n_total);
 
 /* Device time of each phase of the last psph_step call, in ms: [0] cell sort +
- * reorder, [1] wall interpolation, [2] pair forces, [3] dt reduction, [4]
- * update; n_phases receives 5. Timing is recorded only when enabled. */
+ * reorder, [1] neighbour lists, [2] wall interpolation (and the FP32C copies),
+ * [3] pair forces, [4] learned closure, [5] dt reduction, [6] update;
+ * n_phases receives 7. Timing is recorded only when enabled. */
 psph_status psph_enable_timing(psph_ctx* ctx, int enable);
 psph_status psph_phase_times(const psph_ctx* ctx, double* ms, int cap, int* n_phases);
 /* Number of kernel launches the last psph_step issued. */
@@ -194,6 +195,27 @@ int64_t psph_last_launch_count(const psph_ctx* ctx);
 /* psph_step(ctx, nsteps, +inf, steps_done) bracketed by CUDA events on the
  * context's stream; *device_ms receives the device time of the steps. */
 psph_status psph_step_timed(psph_ctx* ctx, int64_t nsteps, double* device_ms, int64_t* steps_done);
+
+/* ---- Launch tuning -----------------------------------------------------------
+ * No counterpart in the reference (its loops run on OpenMP threads). The
+ * launch shape of the FP32C pair kernels and the granularity of the cell sort
+ * are chosen per context; psph_autotune measures the candidates on the
+ * context's own workload. The cell grid itself stays the reference's
+ * (CellInitiate): its cell size fixes the candidate pairs the FP64 form
+ * reproduces; only the order inside a cell follows the split. */
+typedef struct {
+  int32_t pair_block;   /* threads per block of the FP32C pair kernels: 64, 128 or 256 */
+  int32_t cell_split;   /* x-slabs per cell in the sort (1, 2 or 4): the neighbour-list walk
+                           skips slabs out of reach */
+  double ms_per_step;   /* psph_autotune: device time per step of the chosen setting */
+} psph_tuning;
+psph_status psph_get_tuning(const psph_ctx* ctx, psph_tuning* out);
+/* Applies a setting (the step graph is captured again at the next step). */
+psph_status psph_set_tuning(psph_ctx* ctx, const psph_tuning* t);
+/* Runs steps_per_trial timed steps (after one untimed step) with every
+ * candidate setting and keeps the fastest; *chosen (if not NULL) receives it.
+ * The trial steps are real steps of the simulation: they advance its time. */
+psph_status psph_autotune(psph_ctx* ctx, int64_t steps_per_trial, psph_tuning* chosen);
 
 /* Pair-interactions evaluated since upload: unordered pairs {i,j}, at least
  * one free, r_ij <= Cellfac h_ij, summed over steps (the work CalcForce11 /
@@ -252,18 +274,21 @@ psph_status psph_batch_get_integrator(const psph_ctx* ctx, int inst, psph_integr
  * Inputs (raw features, per fluid particle with LES on, from the step's own
  * pair sums; StrainRate is the reference's fluid strain rate, twice the
  * symmetric velocity gradient D):
- *   [0] log(ShearRate), ShearRate = sqrt(StrainRate:StrainRate / 2)
+ *   [0] log(ShearRate h / Cs), ShearRate = sqrt(StrainRate:StrainRate / 2)
  *   [1] det(StrainRate) / (StrainRate:StrainRate)^(3/2)   (0 in 2D)
- *   [2] log(|vorticity|)
+ *   [2] log(|vorticity| h / Cs)
  *   [3] Density / RefDensity
  *   [4] h / dx            (dx = the lattice spacing given to psph_closure_attach)
  *   [5] number of neighbours inside the kernel support
- * (logs of max(value, 1e-8)). The network is 6 -> 64 -> 64 -> 64 -> 1 with
+ * (logs of max(value, 1e-12); the rates are in units of the acoustic rate
+ * Cs / h, so the features of one flow change little with the lattice). The network is 6 -> 64 -> 64 -> 64 -> 1 with
  * SiLU hidden layers; the three hidden layers run on the tensor cores
  * (tcgen05, BF16 weights and activations, FP32 accumulation); the output c =
  * softplus(z) gives the eddy viscosity nu_t = c h^2 ShearRate, and
  * Mu = MuRef + RefDensity nu_t. A particle whose features fall outside the
- * training range [lo, hi] uses the Smagorinsky term instead (counted).
+ * training range [lo, hi] uses the Smagorinsky term instead (counted), except
+ * that rates below the range (fluid at rest, where nu_t vanishes with
+ * ShearRate) are raised to its floor.
  *
  * Parameters (PSPH_MLP_NPARAMS floats, FP32 masters; W1..W3 are rounded to
  * BF16 when used): W1[64][6], b1[64], W2[64][64], b2[64], W3[64][64], b3[64],

@@ -105,9 +105,10 @@ def loss_grad(params, norm, x, y, quantize=True):
     return loss, grad
 
 
-def features(strain_rate, vort, density, rho0, h, dx, nnb):
+def features(strain_rate, vort, density, rho0, h, dx, nnb, cs):
     """Raw closure features from per-particle fields (strain_rate (n, 9), the
-    reference's fluid StrainRate); same definitions as the closure kernel."""
+    reference's fluid StrainRate; vort = |vorticity|; cs = sound speed Cs);
+    same definitions as the closure kernel: rates in units of Cs / h."""
     S = np.asarray(strain_rate, np.float64).reshape(-1, 9)
     temp = (S[:, 0] ** 2 + 2 * S[:, 1] * S[:, 3] + 2 * S[:, 2] * S[:, 6] + S[:, 4] ** 2 + 2 * S[:, 5] * S[:, 7]
             + S[:, 8] ** 2)
@@ -116,6 +117,7 @@ def features(strain_rate, vort, density, rho0, h, dx, nnb):
            + S[:, 2] * (S[:, 3] * S[:, 7] - S[:, 4] * S[:, 6]))
     with np.errstate(divide="ignore", invalid="ignore"):
         r3 = np.where(temp > 0, det / (temp * np.sqrt(temp)), 0.0)
-    f = np.stack([np.log(np.maximum(shear, 1e-8)), r3, np.log(np.maximum(vort, 1e-8)),
+    ts = np.asarray(h, np.float64) / np.asarray(cs, np.float64)
+    f = np.stack([np.log(np.maximum(shear * ts, 1e-12)), r3, np.log(np.maximum(vort * ts, 1e-12)),
                   np.asarray(density) / rho0, np.asarray(h) / dx + 0 * shear, np.asarray(nnb, np.float64)], axis=1)
     return f, shear

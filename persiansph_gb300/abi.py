@@ -62,6 +62,10 @@ class PsphIntegrator(C.Structure):
     ]
 
 
+class PsphTuning(C.Structure):
+    _fields_ = [("pair_block", C.c_int32), ("cell_split", C.c_int32), ("ms_per_step", C.c_double)]
+
+
 class PsphParticles(C.Structure):
     _fields_ = (
         [("n", C.c_int64)]
@@ -181,6 +185,11 @@ def _declare(lib):
     lib.psph_mlp_destroy.restype = None
     lib.psph_mlp_last_error.argtypes = [C.c_void_p]
     lib.psph_mlp_last_error.restype = C.c_char_p
+    lib.psph_get_tuning.argtypes = [ctx, P(PsphTuning)]
+    lib.psph_set_tuning.argtypes = [ctx, P(PsphTuning)]
+    lib.psph_autotune.argtypes = [ctx, C.c_int64, P(PsphTuning)]
+    for name in ("psph_get_tuning", "psph_set_tuning", "psph_autotune"):
+        getattr(lib, name).restype = C.c_int
     lib.psph_mlp_set_params.argtypes = [C.c_void_p, fp, fp]
     lib.psph_mlp_get_params.argtypes = [C.c_void_p, fp, fp]
     lib.psph_mlp_set_data.argtypes = [C.c_void_p, fp, fp, C.c_int64]

@@ -20,7 +20,17 @@ from .abi import PsphError, load_library
 NIN = 6
 NPARAMS = 8833
 NNORM = 24
-FEATURES = ("log_shear_rate", "strain_rate_r3", "log_vorticity", "density_ratio", "h_over_dx", "neighbours")
+# shear rate and vorticity enter in units of the acoustic rate Cs / h
+FEATURES = ("log_shear_rate_h_over_cs", "strain_rate_r3", "log_vorticity_h_over_cs", "density_ratio", "h_over_dx",
+            "neighbours")
+
+
+def default_network_path() -> str:
+    """The network shipped with the package: trained by
+    `python -m persiansph_gb300.closure_train --steps 6000` (eight fine plain
+    runs at dx = 10 mm box-filtered to dx = 20 mm; its report lies beside it)."""
+    import os
+    return os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "closure_dam3d.npz")
 
 
 def _fp(a):

@@ -1,13 +1,17 @@
 """Trains the learned eddy-viscosity closure for the coarse 3D dam break and
 evaluates it (a priori on a held-out fine run, a posteriori by coarse runs).
 
-  python -m persiansph_gb300.closure_train [--dx-fine 0.01] [--dx-coarse 0.02]
+  python -m persiansph_gb300.closure_train [--pairs 0.01:0.02,0.005:0.01]
          [--cases 8] [--t-end 0.4] [--out persiansph_gb300/data/closure_dam3d.npz]
 
 1. Fine runs of the plain method (LES on, FP32C pair arithmetic), generated as
-   one ensemble by the batched solver: columns L = 0.3 m wide with aspect H/L
-   drawn from U[1, 3] and c0 from U[30, 50] m/s (seeded), in a 1.6 x 1.0 x 1.0 m
-   tank, snapshots every 0.05 s.
+   one ensemble by the batched solver for each (fine, coarse) lattice pair:
+   columns L = 0.3 m wide with aspect H/L drawn from U[1, 3] and c0 from
+   U[30, 50] m/s (seeded), in a 1.6 x 1.0 x 1.0 m tank (0.3 m deep, column
+   and tank, for fine spacings below 7.5 mm, which bounds the particle count),
+   snapshots every 0.05 s. Two lattice pairs put coarse spacings of 20 mm
+   (the coarse dam break) and 10 mm into one training set; the rate features
+   are in units of Cs / h, so the network also serves finer lattices.
 2. Each snapshot is box-filtered onto the coarse lattice; the coarse particle
    set gets its features from one step of the runtime kernels, and the target
    eddy viscosity is the one that best matches the filtered subgrid stress.
@@ -92,8 +96,9 @@ def filtered_velocity_error(fine, coarse, dx_c):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--dx-fine", type=float, default=0.01)
-    ap.add_argument("--dx-coarse", type=float, default=0.02)
+    ap.add_argument("--pairs", default="0.01:0.02,0.005:0.01",
+                    help="fine:coarse lattice spacings of the training runs; the first pair also serves the "
+                         "held-out evaluation")
     ap.add_argument("--cases", type=int, default=8)
     ap.add_argument("--t-end", type=float, default=0.4)
     ap.add_argument("--dt-snap", type=float, default=0.05)
@@ -107,25 +112,38 @@ def main(argv=None):
     rng = np.random.default_rng(args.seed)
     times = [round(args.dt_snap * (k + 1), 10) for k in range(int(round(args.t_end / args.dt_snap)))]
     cases = [dict(aspect=float(rng.uniform(1.0, 3.0)), c0=float(rng.uniform(30.0, 50.0))) for _ in range(args.cases)]
-    report = {"dx_fine": args.dx_fine, "dx_coarse": args.dx_coarse, "cases": cases, "times": times}
+    pairs = [tuple(float(v) for v in p.split(":")) for p in args.pairs.split(",")]
+    dx_fine, dx_coarse = pairs[0]
+    report = {"pairs": pairs, "cases": cases, "times": times, "fine_particles": {}, "fine_seconds": {},
+              "samples": {}}
 
-    t0 = time.perf_counter()
-    snaps, infos = fine_snapshots(cases, args.dx_fine, times)
-    report["fine_particles"] = [int(i["n_fluid"] + i["n_wall"]) for i in infos]
-    report["fine_seconds"] = time.perf_counter() - t0
-    X, Y, H, S = samples_from_snapshots(cases, snaps, args.dx_fine, args.dx_coarse)
-    report["samples"] = int(len(Y))
+    parts = []
+    for dx_f, dx_c in pairs:
+        geo = {} if dx_f >= 0.0075 else dict(W=0.3, TW=0.3)
+        pcases = [dict(c, **geo) for c in cases]
+        t0 = time.perf_counter()
+        snaps, infos = fine_snapshots(pcases, dx_f, times)
+        key = f"{dx_f}:{dx_c}"
+        report["fine_particles"][key] = [int(i["n_fluid"] + i["n_wall"]) for i in infos]
+        report["fine_seconds"][key] = time.perf_counter() - t0
+        parts.append(samples_from_snapshots(pcases, snaps, dx_f, dx_c))
+        report["samples"][key] = int(len(parts[-1][1]))
+        del snaps
+    X, Y, H, S = (np.concatenate([p[k] for p in parts]) for k in range(4))
 
-    hsnaps, hinfos = fine_snapshots([HELD_OUT], args.dx_fine, times)
-    Xh, Yh, Hh, Sh = samples_from_snapshots([HELD_OUT], hsnaps, args.dx_fine, args.dx_coarse)
+    hsnaps, hinfos = fine_snapshots([HELD_OUT], dx_fine, times)
+    Xh, Yh, Hh, Sh = samples_from_snapshots([HELD_OUT], hsnaps, dx_fine, dx_coarse)
     report["held_out_samples"] = int(len(Yh))
     report["held_out_fine_particles"] = int(hinfos[0]["n_fluid"] + hinfos[0]["n_wall"])
 
     net = ClosureNet(seed=args.seed)
     net.set_data(X, Y)
-    # the loss in eddy-viscosity units: nu = c h^2 ShearRate, so weight (h^2 ShearRate)^2
+    # the loss in eddy-viscosity units: nu = c h^2 ShearRate, so weight
+    # (h^2 ShearRate)^2, scaled to mean 1 within each lattice pair (so that
+    # the finer pair, with smaller h, counts as much as the coarser one)
+    wp = [(p[2] * p[2] * p[3]) ** 2 for p in parts]
+    net.set_weights(np.concatenate([a / np.mean(a) for a in wp]))
     w = H * H * S
-    net.set_weights(w * w)
     t1 = time.perf_counter()
     losses = net.train(args.steps, batch=min(args.batch, len(Y)), lr=args.lr, seed=args.seed + 1)
     report["train_seconds"] = time.perf_counter() - t1
@@ -135,16 +153,16 @@ def main(argv=None):
     report["c_const"] = c_const
     report["apriori_held_out"] = apriori_errors(net, Xh, Yh, Hh, Sh, c_const)
 
-    fine_front = [surge_front(s["x"], args.dx_fine) for s in hsnaps[0]]
+    fine_front = [surge_front(s["x"], dx_fine) for s in hsnaps[0]]
     report["fine_front"] = fine_front
     post = {}
     for mode in ("closure", "smagorinsky", "laminar"):
-        runs, info = coarse_run(mode, args.dx_coarse, times, net)
+        runs, info = coarse_run(mode, dx_coarse, times, net)
         fr = [r["front"] for r in runs]
         post[mode] = {
             "front": fr,
             "front_rel_err_max": float(np.max(np.abs(np.array(fr) - fine_front) / np.array(fine_front))),
-            "filtered_velocity_rel_l2": [filtered_velocity_error(f, c, args.dx_coarse) for f, c in zip(hsnaps[0], runs)],
+            "filtered_velocity_rel_l2": [filtered_velocity_error(f, c, dx_coarse) for f, c in zip(hsnaps[0], runs)],
             **info,
         }
     report["aposteriori"] = post

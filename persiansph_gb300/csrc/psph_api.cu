@@ -24,6 +24,12 @@
 
 using namespace psph;
 
+// Phases timed by psph_phase_times: sort, neighbour lists, prepare, pair
+// forces, closure, dt, update.
+constexpr int kNumPhases = 7;
+// Finest split of the cells into x-slabs in the sort (Options::xsub).
+constexpr int kMaxXsub = 4;
+
 struct psph_ctx {
   int ninst = 1;
   std::vector<psph_config> cfgs;
@@ -55,9 +61,10 @@ struct psph_ctx {
   cudaGraphExec_t graph = nullptr;
   bool uploaded = false;
   bool timing = false;
-  double phase_ms[5] = {0, 0, 0, 0, 0};
+  double phase_ms[kNumPhases] = {};
+  double tuned_ms = 0.0;  // psph_autotune's measured time per step
   long long last_launches = 0;
-  cudaEvent_t ev[6] = {};
+  cudaEvent_t ev[kNumPhases + 1] = {};
 };
 
 namespace {
@@ -209,20 +216,22 @@ void enqueue_step(psph_ctx* c) {
   launch_begin(v, st);
   record_phase(c, 0);
   launch_sort(v, st);
-  launch_nlist(v, st);
   record_phase(c, 1);
+  launch_nlist(v, st);
+  record_phase(c, 2);
   if (v.o.fp32) launch_prepare32(v, st);
   else launch_prepare(v, st);
-  record_phase(c, 2);
+  record_phase(c, 3);
   if (v.o.fp32) launch_forces32(v, st);
   else launch_forces(v, st);
-  record_phase(c, 3);
-  if (v.o.closure) launch_closure(v, st);
-  launch_dt(v, st);
   record_phase(c, 4);
+  if (v.o.closure) launch_closure(v, st);
+  record_phase(c, 5);
+  launch_dt(v, st);
+  record_phase(c, 6);
   launch_update(v, st);
   launch_end(v, st);
-  record_phase(c, 5);
+  record_phase(c, 7);
 }
 
 // Clears every instance's stop flag and the status word on the stream, with
@@ -315,7 +324,7 @@ psph_status create_impl(const psph_config* cfgs, int ninst, psph_ctx** out) {
   cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) return set_err(c, PSPH_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
   c->own_stream = true;
-  for (int i = 0; i < 6; ++i) cudaEventCreate(&c->ev[i]);
+  for (int i = 0; i <= kNumPhases; ++i) cudaEventCreate(&c->ev[i]);
   c->grids.resize(ninst);
   c->integ.resize(ninst);
   for (int q = 0; q < ninst; ++q) {
@@ -461,11 +470,12 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
     gd.cellfac = (cf.kernel_type == PSPH_QUINTIC_SPLINE) ? 3.0 : 2.0;
     g.cellfac = gd.cellfac;
     const long long nci = (long long)gd.nc[0] * gd.nc[1] * gd.nc[2];
-    if (nci > (1LL << 30)) return set_err(c, PSPH_ERR_UNSUPPORTED, "grid has more than 2^30 cells");
+    if (nci > (1LL << 28)) return set_err(c, PSPH_ERR_UNSUPPORTED, "grid has more than 2^28 cells");
     gd.ncells = (int)nci;
     gd.cell_base = (int)cell_base;
     cell_base += nci;
-    if (cell_base > (1LL << 30)) return set_err(c, PSPH_ERR_UNSUPPORTED, "the instances' grids hold more than 2^30 cells");
+    if (cell_base > (1LL << 28))
+      return set_err(c, PSPH_ERR_UNSUPPORTED, "the instances' grids hold more than 2^28 cells");
   }
   c->total_cells = (int)cell_base;
 
@@ -479,8 +489,6 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
   o.wallp_physical = (k.wall_pressure_mode == PSPH_WALLP_PHYSICAL);
   o.has_solid = (material0 > 1);
   o.fp32 = (k.precision == PSPH_FP32C);
-  if (o.fp32 && o.has_solid)
-    return set_err(c, PSPH_ERR_UNSUPPORTED, "the FP32C form covers fluids (Material 1); use PSPH_FP64 for solids and soil");
   if (ntot >= (1LL << 26)) return set_err(c, PSPH_ERR_UNSUPPORTED, "this build handles fewer than 2^26 particles");
   o.soil_pairs = (material0 == 3);
   o.dyn_mu = dyn_mu;
@@ -494,6 +502,9 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
   o.uniform_eos = 1;
   o.eos_cls = -1;
   o.uniform_h = 1;
+  o.any_periodic = 0;
+  for (const GridDev& gd : c->gdevs)
+    if (gd.periodic[0] || gd.periodic[1] || gd.periodic[2]) o.any_periodic = 1;
   o.any_av = o.any_ti = o.need_sr = o.any_shepard = 0;
   for (size_t q = 0; q < c->classes.size(); ++q) {
     const PClass& C = c->classes[q];
@@ -528,6 +539,8 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
   // neighbour lists: 3D supports hold ~80 (h = 1.3 dx) particles, 2D ~20-44;
   // a particle with more falls back to scanning its cells
   o.nl_cap = (k.dimension == 3) ? 128 : 64;
+  o.pair_block = 128;
+  o.xsub = 1;
 
   // ---- device buffers ----------------------------------------------------------
   c->ncap = (int)ntot;
@@ -549,9 +562,11 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
   }
   Scratch& S = c->S;
   const size_t NC = (size_t)c->total_cells;
-  if ((st = dalloc(c, &S.key, N)) || (st = dalloc(c, &S.count, NC + 2)) || (st = dalloc(c, &S.start, NC + 3)) ||
+  const size_t NB = NC * kMaxXsub;  // sort bins at the finest x-slab split
+  if ((st = dalloc(c, &S.key, N)) || (st = dalloc(c, &S.count, NB + 2)) || (st = dalloc(c, &S.start, NC + 3)) ||
+      (st = dalloc(c, &S.sstart, NB + 3)) ||
       (st = dalloc(c, &S.tmp_perm, N)) || (st = dalloc(c, &S.perm, N)) || (st = dalloc(c, &S.cellid, N)) ||
-      (st = dalloc(c, &S.block_sums, (NC + 2 + 1023) / 1024 + 1)) ||
+      (st = dalloc(c, &S.block_sums, (NB + 2 + 1023) / 1024 + 1)) ||
       (st = dalloc(c, &S.OFF32, N)) || (st = dalloc(c, &S.D4, N)) || (st = dalloc(c, &S.nl_count, N)) ||
       (st = dalloc(c, &S.A4, N)) || (st = dalloc(c, &S.zwab, N)) || (st = dalloc(c, &S.sumden, N)) ||
       (st = dalloc(c, &S.sumkernel, N)) || (st = dalloc(c, &S.nsv4, N)) || (st = dalloc(c, &S.vxsph4, N)) ||
@@ -562,6 +577,11 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
     if ((st = dalloc(c, &S.strain_rate, 9 * N))) return st;
   if (o.fp32)
     if ((st = dalloc(c, &S.V32, N)) || (st = dalloc(c, &S.D32, N))) return st;
+  if (o.fp32 && o.has_solid) {
+    if ((st = dalloc(c, &S.SIG32, 2 * N)) || (st = dalloc(c, &S.VB32, N)) || (st = dalloc(c, &S.V32LO, N)))
+      return st;
+    if (o.any_ti && (st = dalloc(c, &S.TIR32, 2 * N))) return st;
+  }
   if (o.has_solid) {
     if ((st = dalloc(c, &S.rotation_rate, 9 * N)) || (st = dalloc(c, &S.sigma_o, 9 * N)) ||
         (st = dalloc(c, &S.strain_o, 9 * N)) || (st = dalloc(c, &S.shear_o, 9 * N)))
@@ -680,14 +700,14 @@ psph_status step_impl(psph_ctx* c, int64_t nsteps, const double* t_stop, double 
   if ((st = arm(c, t_stop, t_all))) return st;
   std::vector<long long> steps0(c->ninst);
   for (int q = 0; q < c->ninst; ++q) steps0[q] = c->h_inst[q].steps;
-  for (int e = 0; e < 5; ++e) c->phase_ms[e] = 0.0;
+  for (int e = 0; e < kNumPhases; ++e) c->phase_ms[e] = 0.0;
   long long launched = 0;
   if (c->timing) {
     for (int64_t s = 0; s < nsteps; ++s) {
       enqueue_step(c);
       CUDA_TRY(c, cudaGetLastError());
       CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-      for (int e = 0; e < 5; ++e) {
+      for (int e = 0; e < kNumPhases; ++e) {
         float ms = 0.f;
         cudaEventElapsedTime(&ms, c->ev[e], c->ev[e + 1]);
         c->phase_ms[e] += ms;
@@ -1022,8 +1042,8 @@ psph_status psph_enable_timing(psph_ctx* c, int enable) {
 
 psph_status psph_phase_times(const psph_ctx* c, double* ms, int cap, int* n_phases) {
   if (!c) return PSPH_ERR_INVALID_ARGUMENT;
-  for (int e = 0; e < 5 && e < cap; ++e) ms[e] = c->phase_ms[e];
-  if (n_phases) *n_phases = 5;
+  for (int e = 0; e < kNumPhases && e < cap; ++e) ms[e] = c->phase_ms[e];
+  if (n_phases) *n_phases = kNumPhases;
   return PSPH_OK;
 }
 
@@ -1053,6 +1073,70 @@ psph_status psph_step_timed(psph_ctx* c, int64_t nsteps, double* device_ms, int6
   *device_ms = ms;
   if (steps_done) *steps_done = done[0];
   return st;
+}
+
+psph_status psph_get_tuning(const psph_ctx* c, psph_tuning* out) {
+  if (!c || !out) return PSPH_ERR_INVALID_ARGUMENT;
+  out->pair_block = c->opt.pair_block;
+  out->cell_split = c->opt.xsub;
+  out->ms_per_step = c->tuned_ms;
+  return PSPH_OK;
+}
+
+psph_status psph_set_tuning(psph_ctx* c, const psph_tuning* t) {
+  if (!c || !t) return PSPH_ERR_INVALID_ARGUMENT;
+  if (t->pair_block != 64 && t->pair_block != 128 && t->pair_block != 256)
+    return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "pair_block must be 64, 128 or 256 (got %d)", t->pair_block);
+  if (t->cell_split != 1 && t->cell_split != 2 && t->cell_split != kMaxXsub)
+    return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "cell_split must be 1, 2 or 4 (got %d)", t->cell_split);
+  if (c->opt.pair_block != t->pair_block || c->opt.xsub != t->cell_split) {
+    c->opt.pair_block = t->pair_block;
+    c->opt.xsub = t->cell_split;
+    if (c->graph) {  // launch parameters change: capture the step again
+      cudaGraphExecDestroy(c->graph);
+      c->graph = nullptr;
+    }
+  }
+  return PSPH_OK;
+}
+
+psph_status psph_autotune(psph_ctx* c, int64_t steps_per_trial, psph_tuning* chosen) {
+  if (!c || steps_per_trial < 1) return PSPH_ERR_INVALID_ARGUMENT;
+  if (!c->uploaded) return set_err(c, PSPH_ERR_STATE, "psph_autotune before psph_upload");
+  std::vector<psph_tuning> cands;
+  for (int split : {1, 2, kMaxXsub}) {
+    // the pair block only matters for the FP32C pair kernels
+    for (int block : {64, 128, 256}) {
+      if (!c->opt.fp32 && block != 128) continue;
+      psph_tuning t{};
+      t.pair_block = block;
+      t.cell_split = split;
+      cands.push_back(t);
+    }
+  }
+  psph_tuning best{};
+  double best_ms = 1e300;
+  for (const psph_tuning& t : cands) {
+    psph_status st = psph_set_tuning(c, &t);
+    if (st) return st;
+    double ms = 0.0;
+    int64_t done = 0;
+    if ((st = psph_step_timed(c, 1, &ms, &done))) return st;  // capture + first launch, untimed
+    if ((st = psph_step_timed(c, steps_per_trial, &ms, &done))) return st;
+    if (done < steps_per_trial) break;  // the run ended; keep what was measured
+    const double per = ms / (double)done;
+    if (per < best_ms) {
+      best_ms = per;
+      best = t;
+    }
+  }
+  if (best_ms == 1e300) best = cands.front();
+  psph_status st = psph_set_tuning(c, &best);
+  if (st) return st;
+  c->tuned_ms = best_ms < 1e300 ? best_ms : 0.0;
+  best.ms_per_step = c->tuned_ms;
+  if (chosen) *chosen = best;
+  return PSPH_OK;
 }
 
 psph_status psph_pair_count(psph_ctx* c, uint64_t* pairs) {

@@ -28,7 +28,8 @@ struct Persist {
 struct Scratch {
   int* key;        // cell key per particle (pre-sort order)
   int* count;      // ncells + 2 counters
-  int* start;      // ncells + 3 exclusive prefix
+  int* start;      // ncells + 3 exclusive prefix: cell c's particles are [start[c], start[c+1])
+  int* sstart;     // ncells * xsub + 3 exclusive prefix over the x-slabs of the cells (xsub > 1)
   int* tmp_perm;
   int* perm;
   int* cellid;     // cell of each sorted particle (orphan/dead: -1)
@@ -40,6 +41,10 @@ struct Scratch {
   int* nl_count;     // list length, or -1 when it exceeded the capacity (scan instead)
   float4* V32;       // FP32C form: (v, pressure)
   float4* D32;       // FP32C form: (1/density, pressure/density^2, sound speed, density)
+  float4* SIG32;     // FP32C solids: symmetric Sigma, 2 per particle (00 01 02 11 | 12 22 - -)
+  float4* TIR32;     // FP32C solids with TI: symmetric TIR, same layout
+  float4* VB32;      // FP32C solids: wall history velocity (MVerlet vb / leapfrog vb)
+  float4* V32LO;     // FP32C solids: v - (float)v, the low-order part of the velocity
   double4_32a* D4;   // seen by partners: (1/density, pressure/density^2, sound speed, density);
                      // a wall's density is the inverse EOS of its interpolated pressure
   double4_32a* A4;       // ax, ay, az, dDensity
@@ -75,10 +80,13 @@ struct Options {
   int dyn_mu;
   int soil_pairs;     // Material 3 (soil-soil walls take the partner's density)
   int uniform_h;      // every particle has the same h
+  int any_periodic;   // some instance has a periodic axis
   int uniform_mu;     // every free particle has the same constant viscosity
   double mu_u;        // that viscosity
   double inv_h;       // 1/h when uniform
   int nl_cap;         // neighbour-list capacity per particle
+  int pair_block;     // threads per block of the FP32C pair kernels (psph_autotune)
+  int xsub;           // x-slabs per cell in the sort (1, 2 or 4; psph_autotune)
   double xsph, sqrt_h_a;
   double gravity[3], body_force[3];
   int shepard_step;

@@ -1,4 +1,5 @@
-// FP32-compensated form of the fluid pair path (precision = PSPH_FP32C).
+// FP32-compensated form of the pair path (precision = PSPH_FP32C): fluids
+// (CalcForce11) and soil / solids (CalcForce2233).
 //
 // Same algorithm as psph_forces.cu (CalcForce11, Source/Interaction.cpp:25-184,
 // and the wall interpolation of PrimaryComputeAcceleration,
@@ -19,12 +20,12 @@ namespace psph {
 
 namespace {
 
-constexpr int kFT32 = 128;
-// Minimum resident blocks per SM asked of the register allocator for the pair
-// kernel (1 = no limit: ~123 registers, 4 blocks per SM).
-#ifndef PSPH_FT32_MINB
-#define PSPH_FT32_MINB 1
-#endif
+constexpr int kFT32 = 128;  // block size of the copy and wall-interpolation kernels
+// The pair kernels take their block size at launch (Options::pair_block, 64 to
+// 256 threads, picked by psph_autotune); the specialised fluid kernels are
+// capped at 96 registers (20 resident warps per SM at 128- or 64-thread
+// blocks), the general ones at 128.
+constexpr int kMaxPairBlock = 256;
 constexpr int kQ32 = 16;  // queued wall-interpolation partners per lane
 
 struct Kahan {
@@ -240,16 +241,22 @@ __global__ void __launch_bounds__(kFT32) prepare32_kernel(DevView v) {
 // ---------------------------------------------------------------------------
 // Fluid pair force, FP32 with compensated sums, over the neighbour lists
 // ---------------------------------------------------------------------------
-template <int DIM, int KT>
-__global__ void __launch_bounds__(kFT32, PSPH_FT32_MINB) forces_fluid32_kernel(DevView v) {
-  __shared__ double red[kFT32 / 32];
-  __shared__ unsigned long long cred[kFT32 / 32];
+// FL selects a compile-time specialisation: 0 = every option read at run time;
+// 1 and 2 = Morris viscosity, squared-density gradient, no tensile-instability
+// term and no XSPH (the dam-break configuration), without (1) or with (2) the
+// strain-rate sums of the LES / Bingham options. The list walk is a counted
+// loop so that the next neighbour's loads can be issued before this one's
+// arithmetic.
+template <int DIM, int KT, int FL>
+__global__ void __maxnreg__(FL == 0 ? 128 : 96) forces_fluid32_kernel(DevView v) {
+  constexpr bool SPEC = FL != 0;
+  __shared__ double red[32];
+  __shared__ unsigned long long cred[32];
   const StepScalars* sc = v.sc;
   if (sc->all_stop) return;
   const Persist& P = cur_persist(v);
   const int n = sc->n;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int tid = threadIdx.x;
   const Options& o = v.o;
   const PClass32* __restrict__ CT = v.cls32;
   double dtc = DBL_MAX;
@@ -279,36 +286,34 @@ __global__ void __launch_bounds__(kFT32, PSPH_FT32_MINB) forces_fluid32_kernel(D
   const int fi = Ci.flags;
   const bool shep = (fi & CF_SHEPARD) && (Is.shepard_counter == o.shepard_step);
   const bool sr_self = fi & (CF_T0 | CF_LES);
-  const bool use_sr = o.need_sr;
-  const bool xsph_on = o.xsph != 0.0;
+  const bool use_sr = SPEC ? (FL == 2) : (bool)o.need_sr;
+  const bool xsph_on = SPEC ? false : o.xsph != 0.0;
   const float xsph = (float)o.xsph;
   const float3 cs = cell_size_f(g);
   const float mu_u = (float)o.mu_u;
   const bool uniform_mu = o.uniform_mu, dyn_mu = o.dyn_mu;
-  const int vis_eq = o.vis_eq, grad_type = o.grad_type;
+  const int vis_eq = SPEC ? 0 : o.vis_eq, grad_type = SPEC ? 0 : o.grad_type;
   Kahan ax, ay, az, dr;
   float zw = 0.f, sd = 0.f, xs0 = 0.f, xs1 = 0.f, xs2 = 0.f;
   float sr0 = 0.f, sr1 = 0.f, sr2 = 0.f, sr4 = 0.f, sr5 = 0.f, sr8 = 0.f;
   float w01 = 0.f, w02 = 0.f, w12 = 0.f;  // antisymmetric counterpart of the strain-rate sums (closure)
   int nnb = 0;
   const bool closure = o.closure && (fi & CF_LES);
-  NbrSource<DIM> src;
-  src.init(v, g, i, active && cell >= 0, 1.0f);
-  while (true) {
-    int code;
-    const int j = src.next(v, &code);
-    if (j < 0) break;
+  const float cf2 = (float)(g.cellfac * g.cellfac);
+  auto pair = [&](const int j, const int code) {
     const float4 oj = v.S.OFF32[j];
     float x0, x1, x2;
     rel_pos<DIM>(cs, oi, oj, code, x0, x1, x2);
+    const float hb = 0.5f * (hi + oj.w);
+    const float r2 = x0 * x0 + x1 * x1 + x2 * x2;
+    // the list's own support test (exact in FP32; lists with a skin hold more)
+    if (r2 > cf2 * hb * hb) return;
     const PClass32& Cj = CT[P.cls[j]];
     const int fjf = Cj.flags;
     const bool fj = fjf & CF_FREE;
     npair2 += fj ? 1ull : 2ull;
     ++nnb;
-    const float hb = 0.5f * (hi + oj.w);
     const float ih = 1.f / hb;
-    const float r2 = x0 * x0 + x1 * x1 + x2 * x2;
     const float inv_r = (r2 > 0.f) ? rsqrtf(r2) : 0.f;
     const float q = r2 * inv_r * ih;
     const float inv_q = hb * inv_r;
@@ -331,7 +336,7 @@ __global__ void __launch_bounds__(kFT32, PSPH_FT32_MINB) forces_fluid32_kernel(D
       PI = t * (-Alpha * 0.5f * (ci_snd + cj_snd) * D + Beta * t) / (D * D * (0.5f * (di + dj)));
     }
     float TI = 0.f;
-    if ((fi | fjf) & CF_TI) {
+    if (!SPEC && ((fi | fjf) & CF_TI)) {
       float Ri = 0.f, Rj = 0.f;
       if ((pi + pj) < 0.f) {
         if (pi < 0.f) Ri = -pi * inv_i * inv_i;
@@ -400,6 +405,29 @@ __global__ void __launch_bounds__(kFT32, PSPH_FT32_MINB) forces_fluid32_kernel(D
     dr.add(mj * di * inv_j * (GK * vx));
     zw += mj * inv_j * K;
     if (shep) sd += mj * K;
+  };
+  const int cnt = (active && cell >= 0) ? v.S.nl_count[i] : 0;
+  if (cnt >= 0) {
+    const int4* __restrict__ nl4 = reinterpret_cast<const int4*>(v.S.nl) + i;
+    const size_t N = (size_t)v.ncap;
+    const int nch = (cnt + 3) >> 2;
+    for (int c = 0; c < nch; ++c) {  // one 16-byte chunk of 4 entries per load
+      const int4 q = nl4[(size_t)c * N];
+      const int rem = cnt - 4 * c;
+      pair(q.x & kIndexMask, q.x >> kCodeShift);
+      if (rem > 1) pair(q.y & kIndexMask, q.y >> kCodeShift);
+      if (rem > 2) pair(q.z & kIndexMask, q.z >> kCodeShift);
+      if (rem > 3) pair(q.w & kIndexMask, q.w >> kCodeShift);
+    }
+  } else {  // list overflow: scan the cells
+    NbrSource<DIM> src;
+    src.init(v, g, i, true, 1.0f);
+    while (true) {
+      int code;
+      const int j = src.next(v, &code);
+      if (j < 0) break;
+      pair(j, code);
+    }
   }
   if (active) {
     const double axd = o.gravity[0] + o.body_force[0] + ax.value();
@@ -425,7 +453,235 @@ __global__ void __launch_bounds__(kFT32, PSPH_FT32_MINB) forces_fluid32_kernel(D
     const double cand = o.sqrt_h_a * sqrt(v.cls[ci_cls].h / an);  // FP64 dt reduction
     if (cand < dtc) dtc = cand;
   }
-  block_dt_and_pairs<kFT32>(v, Ci.inst, active, dtc, npair2, red, cred);
+  block_dt_and_pairs<0>(v, Ci.inst, active, dtc, npair2, red, cred);
+}
+
+// ---------------------------------------------------------------------------
+// Soil / solid pair force (CalcForce2233, Source/Interaction.cpp:186-377) in
+// FP32 with compensated sums. The FP64 preparation (prepare_wall_kernel:
+// wall stress interpolation, partner-visible wall density, TIR) runs first;
+// solid_copies32_kernel then takes the FP32 copies the pair loop reads.
+// ---------------------------------------------------------------------------
+// Symmetric 3x3 tensor (the stresses and TIR are symmetric: Jaumann rate of a
+// symmetric stress, R diag R^T) as 6 floats in two float4: 00 01 02 11 | 12 22.
+PSPH_D void sym_store(float4* dst, size_t w, const double* m) {
+  dst[2 * w] = make_float4((float)m[0], (float)(0.5 * (m[1] + m[3])), (float)(0.5 * (m[2] + m[6])), (float)m[4]);
+  dst[2 * w + 1] = make_float4((float)(0.5 * (m[5] + m[7])), (float)m[8], 0.f, 0.f);
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kFT32) solid_copies32_kernel(DevView v) {
+  const StepScalars* sc = v.sc;
+  if (sc->all_stop) return;
+  const Persist& P = cur_persist(v);
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= sc->n) return;
+  const PClass32& C = v.cls32[P.cls[w]];
+  if (v.inst[C.inst].stop) return;
+  const double4_32a vv = P.V4[w];
+  const float vx = (float)vv.x, vy = (float)vv.y, vz = (float)vv.z;
+  v.S.V32[w] = make_float4(vx, vy, vz, (float)vv.w);
+  // the velocity's low-order part: near-rigid motion (a column settling as one
+  // body) makes v_i - v_j far smaller than v, and the pair differences take
+  // (hi_i - hi_j) + (lo_i - lo_j), exact to ~2^-48 of |v|
+  v.S.V32LO[w] = make_float4((float)(vv.x - (double)vx), (float)(vv.y - (double)vy), (float)(vv.z - (double)vz), 0.f);
+  const double4_32a d = v.S.D4[w];
+  v.S.D32[w] = make_float4((float)d.x, (float)d.y, (float)d.z, (float)d.w);
+  sym_store(v.S.SIG32, (size_t)w, P.sigma + 9 * (size_t)w);
+  if (v.o.any_ti) sym_store(v.S.TIR32, (size_t)w, P.tir + 9 * (size_t)w);
+  if (!(C.flags & CF_FREE)) {
+    const double4_32a vb = (v.o.scheme == PSPH_MVERLET) ? P.H4[w] : P.H4b[w];
+    v.S.VB32[w] = make_float4((float)vb.x, (float)vb.y, (float)vb.z, 0.f);
+  }
+}
+
+template <int DIM, int KT>
+__global__ void __maxnreg__(128) forces_solid32_kernel(DevView v) {
+  __shared__ double red[32];
+  __shared__ unsigned long long cred[32];
+  const StepScalars* sc = v.sc;
+  if (sc->all_stop) return;
+  const Persist& P = cur_persist(v);
+  const int n = sc->n;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const Options& o = v.o;
+  const PClass32* __restrict__ CT = v.cls32;
+  double dtc = DBL_MAX;
+  unsigned long long npair2 = 0;
+  bool active = false;
+  int cell = -1, ci_cls = 0;
+  if (i < n) {
+    ci_cls = P.cls[i];
+    const bool run = !v.inst[CT[ci_cls].inst].stop;
+    active = run && (CT[ci_cls].flags & CF_FREE);
+    cell = v.S.cellid[i];
+    if (run && !active) {
+      v.S.A4[i] = make_double4_32a(o.gravity[0], o.gravity[1], o.gravity[2], 0.0);
+      v.S.zwab[i] = 1.0;
+    }
+  }
+  const PClass32& Ci = CT[ci_cls];
+  const GridDev& g = grid_of(v, Ci.inst);
+  const InstState& Is = v.inst[Ci.inst];
+  const int is = active ? i : 0;
+  const float4 oi = v.S.OFF32[is];
+  const float4 vi = v.S.V32[is];
+  const float4 vil = v.S.V32LO[is];
+  const float4 di4 = v.S.D32[is];
+  const float di = di4.w, inv_i = di4.x, ci_snd = di4.z;
+  const float mi = Ci.mass, hi = oi.w;
+  const bool shep = (Ci.flags & CF_SHEPARD) && (Is.shepard_counter == o.shepard_step);
+  const float4 sa = v.S.SIG32[2 * (size_t)is], sb = v.S.SIG32[2 * (size_t)is + 1];
+  const float Si[6] = {sa.x, sa.y, sa.z, sa.w, sb.x, sb.y};
+  float Ti[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if (o.any_ti) {
+    const float4 ta = v.S.TIR32[2 * (size_t)is], tb = v.S.TIR32[2 * (size_t)is + 1];
+    Ti[0] = ta.x; Ti[1] = ta.y; Ti[2] = ta.z; Ti[3] = ta.w; Ti[4] = tb.x; Ti[5] = tb.y;
+  }
+  const float I22 = (DIM == 2) ? 0.f : 1.f;  // Domain::I (Source/Domain.cpp:1665)
+  const float3 cs = cell_size_f(g);
+  const bool xsph_on = o.xsph != 0.0;
+  const float xsph = (float)o.xsph;
+  const int grad_type = o.grad_type;
+  Kahan ax, ay, az, dr;
+  float zw = 0.f, sd = 0.f, xs0 = 0.f, xs1 = 0.f, xs2 = 0.f;
+  float sr0 = 0.f, sr1 = 0.f, sr2 = 0.f, sr3 = 0.f, sr4 = 0.f, sr5 = 0.f;  // 00 01 02 11 12 22
+  float rr0 = 0.f, rr1 = 0.f, rr2 = 0.f;                                  // 01 02 12
+  NbrSource<DIM> src;
+  src.init(v, g, i, active && cell >= 0, 1.0f);
+  while (true) {
+    int code;
+    const int j = src.next(v, &code);
+    if (j < 0) break;
+    const float4 oj = v.S.OFF32[j];
+    float x0, x1, x2;
+    rel_pos<DIM>(cs, oi, oj, code, x0, x1, x2);
+    const PClass32& Cj = CT[P.cls[j]];
+    const int fjf = Cj.flags;
+    const bool fj = fjf & CF_FREE;
+    npair2 += fj ? 1ull : 2ull;
+    const float hb = 0.5f * (hi + oj.w);
+    const float ih = 1.f / hb;
+    const float r2 = x0 * x0 + x1 * x1 + x2 * x2;
+    const float inv_r = (r2 > 0.f) ? rsqrtf(r2) : 0.f;
+    const float q = r2 * inv_r * ih;
+    const float ih2 = ih * ih;
+    const float cwh = KernF<DIM, KT>::cw() * (DIM == 2 ? ih2 : ih2 * ih);
+    const float cwg = cwh * ih2;
+    const float GK = KernF<DIM, KT>::GK(q, hb * inv_r, cwg);
+    const float K = KernF<DIM, KT>::W(q, cwh);
+    const float4 vj = v.S.V32[j];
+    const bool soil = (Ci.material * Cj.material == 9);
+    float dj, inv_j, cj_snd = 0.f, mj;
+    if (fj) {
+      const float4 dj4 = v.S.D32[j];
+      dj = dj4.w; inv_j = dj4.x; cj_snd = dj4.z; mj = Cj.mass;
+    } else if (soil) {  // soil walls take the partner's density (Source/Interaction.cpp:201-205)
+      dj = di; inv_j = inv_i; mj = Cj.fpmassc * mi;
+    } else {
+      if (o.uniform_eos) {
+        const float4 dj4 = v.S.D32[j];
+        dj = dj4.w; inv_j = dj4.x; cj_snd = dj4.z;
+      } else {
+        const PClass& C64 = v.cls[ci_cls];
+        const double d64 = density_solid(C64.pres_eq, C64.cs, C64.p0, (double)vj.w, C64.rho0);
+        dj = (float)d64;
+        inv_j = 1.f / dj;
+        cj_snd = (float)sound_speed(C64.pres_eq, C64.cs, d64, C64.rho0);
+      }
+      mj = Cj.fpmassc * mi;
+    }
+    const float4 vjl = v.S.V32LO[j];
+    const float v0 = (vi.x - vj.x) + (vil.x - vjl.x), v1 = (vi.y - vj.y) + (vil.y - vjl.y),
+                v2 = (vi.z - vj.z) + (vil.z - vjl.z);
+    const float vx = v0 * x0 + v1 * x1 + v2 * x2;
+    float PIs = 0.f;  // PIij = PIs I
+    const float Alpha = 0.5f * (Ci.alpha + Cj.alpha), Beta = 0.5f * (Ci.beta + Cj.beta);
+    if ((Alpha != 0.f || Beta != 0.f) && vx < 0.f) {
+      const float Cij = soil ? 0.5f * (Ci.cs + Cj.cs) : 0.5f * (ci_snd + cj_snd);
+      const float D = r2 + 0.01f * hb * hb;
+      const float t = hb * vx;
+      PIs = t * (Alpha * Cij * D + Beta * t) / (D * D * (0.5f * (di + dj)));
+    }
+    float vab0, vab1, vab2;
+    if (fj) { vab0 = v0; vab1 = v1; vab2 = v2; }
+    else if ((Ci.flags | fjf) & CF_NOSLIP) {
+      const double4_32a ns = v.S.nsv4[j];
+      vab0 = vi.x - (2.f * vj.x - (float)ns.x);
+      vab1 = vi.y - (2.f * vj.y - (float)ns.y);
+      vab2 = vi.z - (2.f * vj.z - (float)ns.z);
+    } else {
+      const float4 vbj = v.S.VB32[j];
+      vab0 = vi.x - vbj.x; vab1 = vi.y - vbj.y; vab2 = vi.z - vbj.z;
+    }
+    const float4 sja = v.S.SIG32[2 * (size_t)j], sjb = v.S.SIG32[2 * (size_t)j + 1];
+    const float Sj[6] = {sja.x, sja.y, sja.z, sja.w, sjb.x, sjb.y};
+    float M[6];
+    if (grad_type == 0) {
+      const float ci2 = inv_i * inv_i, cj2 = inv_j * inv_j;
+#pragma unroll
+      for (int e = 0; e < 6; ++e) M[e] = Si[e] * ci2 + Sj[e] * cj2;
+    } else {
+      const float c = inv_i * inv_j;
+#pragma unroll
+      for (int e = 0; e < 6; ++e) M[e] = (Si[e] + Sj[e]) * c;
+    }
+    M[0] += PIs; M[3] += PIs; M[5] += PIs * I22;
+    if ((Ci.flags | fjf) & CF_TI) {
+      const float Wd = KernF<DIM, KT>::W((Ci.tid + Cj.tid) * 0.5f * ih, cwh);
+      const float TIs = powf(K / Wd, (Ci.tin + Cj.tin) * 0.5f);
+      const float4 tja = v.S.TIR32[2 * (size_t)j], tjb = v.S.TIR32[2 * (size_t)j + 1];
+      const float Tj[6] = {tja.x, tja.y, tja.z, tja.w, tjb.x, tjb.y};
+#pragma unroll
+      for (int e = 0; e < 6; ++e) M[e] += (Ti[e] + Tj[e]) * TIs;
+    }
+    const float g0 = GK * x0, g1 = GK * x1, g2 = GK * x2;
+    // row vector (GK x_ij) times M (Mult, External/matvec.h:806)
+    ax.add(mj * (g0 * M[0] + g1 * M[1] + g2 * M[2]));
+    ay.add(mj * (g0 * M[1] + g1 * M[3] + g2 * M[4]));
+    if (DIM == 3) az.add(mj * (g0 * M[2] + g1 * M[4] + g2 * M[5]));
+    dr.add(mj * di * inv_j * (v0 * g0 + v1 * g1 + v2 * g2));
+    const float md = mj * inv_j;
+    zw += md * K;
+    const float c2 = -0.5f * GK * md;
+    sr0 += c2 * (2.f * vab0 * x0);
+    sr1 += c2 * (vab0 * x1 + vab1 * x0);
+    sr2 += c2 * (vab0 * x2 + vab2 * x0);
+    sr3 += c2 * (2.f * vab1 * x1);
+    sr4 += c2 * (vab1 * x2 + vab2 * x1);
+    sr5 += c2 * (2.f * vab2 * x2);
+    rr0 += c2 * (vab0 * x1 - vab1 * x0);
+    rr1 += c2 * (vab0 * x2 - vab2 * x0);
+    rr2 += c2 * (vab1 * x2 - vab2 * x1);
+    if (xsph_on && fj) {
+      const float s = xsph * mj / (0.5f * (di + dj)) * K;
+      xs0 -= s * v0; xs1 -= s * v1; xs2 -= s * v2;
+    }
+    if (shep) sd += mj * K;
+  }
+  if (active) {
+    const double axd = o.gravity[0] + o.body_force[0] + ax.value();
+    const double ayd = o.gravity[1] + o.body_force[1] + ay.value();
+    const double azd = o.gravity[2] + o.body_force[2] + az.value();
+    const double drd = dr.value();
+    v.S.A4[i] = make_double4_32a(axd, ayd, azd, drd);
+    v.S.zwab[i] = zw;
+    if (o.any_shepard) v.S.sumden[i] = sd;
+    if (xsph_on) v.S.vxsph4[i] = make_double4_32a(xs0, xs1, xs2, 0.0);
+    double* out = v.S.strain_rate + 9 * (size_t)i;
+    out[0] = sr0; out[1] = sr1; out[2] = sr2;
+    out[3] = sr1; out[4] = sr3; out[5] = sr4;
+    out[6] = sr2; out[7] = sr4; out[8] = sr5;
+    double* ro = v.S.rotation_rate + 9 * (size_t)i;
+    ro[0] = 0.0; ro[1] = rr0; ro[2] = rr1;
+    ro[3] = -(double)rr0; ro[4] = 0.0; ro[5] = rr2;
+    ro[6] = -(double)rr1; ro[7] = -(double)rr2; ro[8] = 0.0;
+    if (!(isfinite(axd) && isfinite(ayd) && isfinite(azd) && isfinite(drd))) atomicOr(&v.sc->status, ST_NONFINITE);
+    const double an = sqrt(axd * axd + ayd * ayd + azd * azd);
+    const double cand = o.sqrt_h_a * sqrt(v.cls[ci_cls].h / an);  // FP64 dt reduction
+    if (cand < dtc) dtc = cand;
+  }
+  block_dt_and_pairs<0>(v, Ci.inst, active, dtc, npair2, red, cred);
 }
 
 inline int nblk32(int n) { return n <= 0 ? 1 : (n + kFT32 - 1) / kFT32; }
@@ -443,17 +699,42 @@ void prepare32_dispatch(const DevView& v, cudaStream_t st) {
 
 template <int DIM>
 void forces32_dispatch(const DevView& v, cudaStream_t st) {
-  const int nb = nblk32(v.ncap);
-  switch (v.o.kt) {
-    case 0: forces_fluid32_kernel<DIM, 0><<<nb, kFT32, 0, st>>>(v); break;
-    case 1: forces_fluid32_kernel<DIM, 1><<<nb, kFT32, 0, st>>>(v); break;
-    default: forces_fluid32_kernel<DIM, 2><<<nb, kFT32, 0, st>>>(v); break;
+  const int bt = (v.o.pair_block >= 32 && v.o.pair_block <= kMaxPairBlock) ? v.o.pair_block : kFT32;
+  const int nb = v.ncap <= 0 ? 1 : (v.ncap + bt - 1) / bt;
+  if (v.o.has_solid) {
+    switch (v.o.kt) {
+      case 0: forces_solid32_kernel<DIM, 0><<<nb, bt, 0, st>>>(v); break;
+      case 1: forces_solid32_kernel<DIM, 1><<<nb, bt, 0, st>>>(v); break;
+      default: forces_solid32_kernel<DIM, 2><<<nb, bt, 0, st>>>(v); break;
+    }
+    return;
+  }
+  const Options& o = v.o;
+  const bool spec = o.vis_eq == 0 && o.grad_type == 0 && !o.any_ti && o.xsph == 0.0;
+  const int fl = spec ? (o.need_sr ? 2 : 1) : 0;
+  switch (o.kt * 3 + fl) {
+    case 0: forces_fluid32_kernel<DIM, 0, 0><<<nb, bt, 0, st>>>(v); break;
+    case 1: forces_fluid32_kernel<DIM, 0, 1><<<nb, bt, 0, st>>>(v); break;
+    case 2: forces_fluid32_kernel<DIM, 0, 2><<<nb, bt, 0, st>>>(v); break;
+    case 3: forces_fluid32_kernel<DIM, 1, 0><<<nb, bt, 0, st>>>(v); break;
+    case 4: forces_fluid32_kernel<DIM, 1, 1><<<nb, bt, 0, st>>>(v); break;
+    case 5: forces_fluid32_kernel<DIM, 1, 2><<<nb, bt, 0, st>>>(v); break;
+    case 6: forces_fluid32_kernel<DIM, 2, 0><<<nb, bt, 0, st>>>(v); break;
+    case 7: forces_fluid32_kernel<DIM, 2, 1><<<nb, bt, 0, st>>>(v); break;
+    default: forces_fluid32_kernel<DIM, 2, 2><<<nb, bt, 0, st>>>(v); break;
   }
 }
 
 }  // namespace
 
 void launch_prepare32(const DevView& v, cudaStream_t st) {
+  if (v.o.has_solid) {  // FP64 wall stress interpolation and TIR, then the FP32 copies
+    launch_prepare(v, st);
+    const int nb = nblk32(v.ncap);
+    if (v.o.dim == 2) solid_copies32_kernel<2><<<nb, kFT32, 0, st>>>(v);
+    else solid_copies32_kernel<3><<<nb, kFT32, 0, st>>>(v);
+    return;
+  }
   if (v.o.dim == 2) prepare32_dispatch<2>(v, st);
   else prepare32_dispatch<3>(v, st);
 }

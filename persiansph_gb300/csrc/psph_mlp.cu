@@ -42,6 +42,10 @@ __device__ __forceinline__ float dsilu(float z) {
   const float s = sigm(z);
   return s * (1.f + z * (1.f - s));
 }
+// SiLU of the tensor-core inference epilogues: hardware exp2 and reciprocal
+// approximations (relative error ~1e-7, far below the BF16 rounding of the
+// activations that follows).
+__device__ __forceinline__ float silu_fast(float z) { return z * __frcp_rn(1.f + __expf(-z)); }
 __device__ __forceinline__ float softplus(float z) { return z > 20.f ? z : log1pf(expf(z)); }
 
 // ---------------------------------------------------------------------------
@@ -265,19 +269,19 @@ __device__ bool tc_forward(TcCtx& t, const float* u, float* out) {
   if (!tc_layer(t, 0, 1, z)) return false;
   const float* b1 = tc_b(t, 0);
 #pragma unroll
-  for (int k = 0; k < kMlpH; ++k) z[k] = silu(z[k] + b1[k]);
+  for (int k = 0; k < kMlpH; ++k) z[k] = silu_fast(z[k] + b1[k]);
   store_row64(t.a, r, z);
   if (!tc_layer(t, 1, kMlpH / 16, z)) return false;
   const float* b2 = tc_b(t, 1);
 #pragma unroll
-  for (int k = 0; k < kMlpH; ++k) z[k] = silu(z[k] + b2[k]);
+  for (int k = 0; k < kMlpH; ++k) z[k] = silu_fast(z[k] + b2[k]);
   store_row64(t.a, r, z);
   if (!tc_layer(t, 2, kMlpH / 16, z)) return false;
   const float* b3 = tc_b(t, 2);
   const float* w4 = tc_b(t, 3);
   float o = t.f[4 * kMlpH];
 #pragma unroll
-  for (int k = 0; k < kMlpH; ++k) o += w4[k] * silu(z[k] + b3[k]);
+  for (int k = 0; k < kMlpH; ++k) o += w4[k] * silu_fast(z[k] + b3[k]);
   *out = o;
   return true;
 }
@@ -323,9 +327,12 @@ __global__ void __launch_bounds__(kTcThreads) closure_kernel(DevView v) {
         const double det = S[0] * (S[4] * S[8] - S[5] * S[7]) - S[1] * (S[3] * S[8] - S[5] * S[6]) +
                            S[2] * (S[3] * S[7] - S[4] * S[6]);
         h = C.h;
-        f[0] = logf(fmaxf((float)shear, 1e-8f));
+        // rates in units of the acoustic rate Cs/h (the lattice-independent
+        // form: the same flow resolved at another dx keeps its features)
+        const double tscale = C.cs > 0.0 ? C.h / C.cs : 1.0;
+        f[0] = logf(fmaxf((float)(shear * tscale), 1e-12f));
         f[1] = temp > 0.0 ? (float)(det / (temp * sqrt(temp))) : 0.f;
-        f[2] = logf(fmaxf(v.S.cvort[s], 1e-8f));
+        f[2] = logf(fmaxf(v.S.cvort[s] * (float)tscale, 1e-12f));
         f[3] = (float)(P.X4[s].w / C.rho0);
         f[4] = (float)(C.h / v.o.closure_dx);
         f[5] = v.S.cnnb[s];
@@ -334,6 +341,12 @@ __global__ void __launch_bounds__(kTcThreads) closure_kernel(DevView v) {
 #pragma unroll
       for (int k = 0; k < kMlpIn; ++k) fo[k] = f[k];
     }
+    // A shear rate or vorticity below the trained range is fluid at rest: the
+    // eddy viscosity c h^2 ShearRate vanishes with it whatever c is, so the
+    // two rate features are raised to the range's floor instead of falling
+    // back; anything else outside [lo, hi] takes the Smagorinsky term.
+    f[0] = fmaxf(f[0], lo[0]);
+    f[2] = fmaxf(f[2], lo[2]);
     bool in_range = act;
 #pragma unroll
     for (int k = 0; k < kMlpIn; ++k) in_range = in_range && f[k] >= lo[k] && f[k] <= hi[k];
@@ -636,7 +649,9 @@ namespace psph {
 void launch_closure(const DevView& v, cudaStream_t st) {
   if (ensure_tc_attrs() != cudaSuccess) return;  // the launch below then reports the error
   const int ntiles = (v.ncap + kMlpTile - 1) / kMlpTile;
-  const int grid = std::max(1, std::min(ntiles, 2 * num_sms()));
+  // four CTAs per SM (128 registers x 128 threads, ~52 KB shared memory and 64
+  // TMEM columns each): while one waits on its MMAs the others run epilogues
+  const int grid = std::max(1, std::min(ntiles, 4 * num_sms()));
   if (v.o.dim == 2) closure_kernel<2><<<grid, kTcThreads, kTcSmemBytes, st>>>(v);
   else closure_kernel<3><<<grid, kTcThreads, kTcSmemBytes, st>>>(v);
 }

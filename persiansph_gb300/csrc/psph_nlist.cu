@@ -2,11 +2,14 @@
 // NSMPairs of MainNeighbourSearch, Source/Domain.cpp:808-945).
 //
 // Each particle scans the sorted ranges of its 3x3(x3) cell block once per step
-// and keeps the candidates inside the kernel support, tested in FP32 on
+// (the rows and x-slabs of it that can reach the support) and keeps the
+// candidates inside the kernel support, tested in FP32 on
 // (cell offset, FP32 offset) separations: exactly for the FP32C form, with a
 // 0.4 % margin on r^2 for the FP64 form (whose pair kernel then applies the
-// exact FP64 test). Lists are laid out entry-major (nl[k*ncap + i]) so a warp
-// reading entry k of 32 consecutive particles touches consecutive words. The
+// exact FP64 test). Lists are written in 16-byte chunks of 4 entries, chunk-
+// major across particles (nl_index), so a warp reading chunk c of 32
+// consecutive particles touches 512 contiguous bytes and each store fills
+// half a sector. The
 // scan is cheap integer/FP32 work; the pair kernels then walk lists of nearly
 // equal length instead of branching per candidate.
 #include "psph_pairs.cuh"
@@ -38,16 +41,21 @@ __global__ void __launch_bounds__(kNT) nlist_kernel(DevView v, float margin) {
   const int N = v.ncap, cap = v.o.nl_cap;
   const CellCoord c = decode(g, cell);
   const float4* __restrict__ off = v.S.OFF32;
-  const int* __restrict__ start = v.S.start;
-  int* __restrict__ out = v.S.nl + i;
-  // Whole cells whose nearest point lies outside the support are skipped. The
-  // bound assumes the in-cell offset of i lies in [0, cell size), which holds
-  // away from the grid faces (ListGenerate clamps only there); a neighbour
-  // cell's clamped particles lie beyond its outer face, farther from i.
+  int4* __restrict__ out = reinterpret_cast<int4*>(v.S.nl) + i;  // chunk c at out[c * N]
+  int b0 = 0, b1 = 0, b2 = 0, b3 = 0;  // the chunk being filled
+  // Rows of cells and x-slabs of cells whose nearest point lies outside the
+  // support are skipped (cells are sorted slab by slab, xsub slabs along x).
+  // The bound assumes the in-cell offset of i lies in [0, cell size), which
+  // holds away from the grid faces (ListGenerate clamps only there); a
+  // neighbour cell's clamped particles lie beyond its outer face, farther
+  // from i than the slab they are counted in.
   const bool inner = c.x > 0 && c.x < g.nc[0] - 1 && c.y > 0 && c.y < g.nc[1] - 1 &&
                      (DIM == 2 || (c.z > 0 && c.z < g.nc[2] - 1));
   const bool cull = UNIFORM_H && inner;
   const float thr_cull = thr_u * 1.0001f;
+  const int xs = v.o.xsub;
+  const int* __restrict__ sstart = xs > 1 ? v.S.sstart : v.S.start;
+  const float inv_sw = (float)xs / cs.x;  // 1 / slab width
   int k = 0;
   const int zlo = (DIM == 3) ? -1 : 0, zhi = (DIM == 3) ? 1 : 0;
   for (int dz = zlo; dz <= zhi; ++dz) {
@@ -63,17 +71,25 @@ __global__ void __launch_bounds__(kNT) nlist_kernel(DevView v, float margin) {
       const int base = g.cell_base + (z * g.nc[1] + y) * g.nc[0];
       const int cyz = 3 * (dy + 1) + 9 * (dz + 1);
       const float cy = -(float)dy * cs.y, cz = -(float)dz * cs.z;  // exact: dy, dz in {-1, 0, 1}
+      // slabs in reach along x, counted from the first slab of i's cell
+      int slo = -xs, shi = 2 * xs - 1;
+      if (cull) {
+        const float rx2 = thr_cull - gy * gy - gz * gz;
+        if (rx2 < 0.f) continue;
+        const float rx = sqrtf(rx2);
+        slo = max(slo, (int)floorf((oi.x - rx) * inv_sw - 1e-3f));
+        shi = min(shi, (int)floorf((oi.x + rx) * inv_sw + 1e-3f));
+      }
       for (int dx = -1; dx <= 1; ++dx) {
         int x = c.x + dx;
         if (g.periodic[0]) x = (x + g.nc[0]) % g.nc[0];
         else if (x < 0 || x >= g.nc[0]) continue;
-        if (cull) {
-          const float gx = dx < 0 ? oi.x : (dx > 0 ? cs.x - oi.x : 0.f);
-          if (gx * gx + gy * gy + gz * gz > thr_cull) continue;
-        }
-        const int lo = start[base + x], hi = start[base + x + 1];
+        const int s0 = max(slo - dx * xs, 0), s1 = min(shi - dx * xs, xs - 1);
+        if (s0 > s1) continue;
+        const int lo = sstart[(base + x) * xs + s0], hi = sstart[(base + x) * xs + s1 + 1];
         const int code = (dx + 1) + cyz;
         const float cx = -(float)dx * cs.x;
+#pragma unroll 4
         for (int j = lo; j < hi; ++j) {
           const float4 oj = off[j];
           // x_i - x_j as rel_pos forms it: cell offset + (offset_i - offset_j)
@@ -85,13 +101,21 @@ __global__ void __launch_bounds__(kNT) nlist_kernel(DevView v, float margin) {
             thr = cf * cf * hb * hb * margin;
           }
           if (x0 * x0 + x1 * x1 + x2 * x2 <= thr && j != i) {
-            if (k < cap) out[(size_t)k * N] = j | (code << kCodeShift);
+            if (k < cap) {
+              const int e = j | (code << kCodeShift), m = k & 3;
+              b0 = m == 0 ? e : b0;
+              b1 = m == 1 ? e : b1;
+              b2 = m == 2 ? e : b2;
+              b3 = m == 3 ? e : b3;
+              if (m == 3) out[(size_t)(k >> 2) * N] = make_int4(b0, b1, b2, b3);
+            }
             ++k;
           }
         }
       }
     }
   }
+  if (k <= cap && (k & 3)) out[(size_t)(k >> 2) * N] = make_int4(b0, b1, b2, b3);  // last, partial chunk
   v.S.nl_count[i] = (k <= cap) ? k : -1;
 }
 

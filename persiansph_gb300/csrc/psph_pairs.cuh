@@ -14,6 +14,12 @@ namespace psph {
 constexpr int kCodeShift = 26;  // neighbour-list entry: index | code << 26 (index < 2^26)
 constexpr int kIndexMask = (1 << kCodeShift) - 1;
 
+// Neighbour-list layout: chunks of 4 consecutive entries of one particle (16
+// bytes), chunk-major across particles, so entry k of particle i sits at
+// ((k / 4) * ncap + i) * 4 + k % 4. A lane writes and reads whole chunks, and
+// chunk c of a warp's 32 consecutive particles is 512 contiguous bytes.
+PSPH_HD size_t nl_index(int ncap, int i, int k) { return (((size_t)(k >> 2) * ncap + i) << 2) + (k & 3); }
+
 struct CellCoord {
   int x, y, z;
 };
@@ -198,7 +204,7 @@ struct NbrSource {
   PSPH_D int next(const DevView& v, int* code) {
     if (cnt >= 0) {
       if (k >= cnt) return -1;
-      const int e = v.S.nl[(size_t)k * v.ncap + i];
+      const int e = v.S.nl[nl_index(v.ncap, i, k)];
       ++k;
       *code = e >> kCodeShift;
       return e & kIndexMask;
@@ -227,7 +233,9 @@ namespace psph {
 // non-negative double, so the result does not depend on arrival order; NaN
 // bounds never win, as the reference's comparison ignores them) and adds the
 // block's pair count. One atomic per warp when the warp's particles share an
-// instance, which is the case except at instance boundaries.
+// instance, which is the case except at instance boundaries. BT is the block
+// size, or 0 for a kernel whose block size is chosen at launch (cred then
+// holds 32 entries).
 template <int BT>
 PSPH_D void block_dt_and_pairs(const DevView& v, int inst, bool active, double dtc, unsigned long long npair2,
                                double* red, unsigned long long* cred) {
@@ -251,7 +259,8 @@ PSPH_D void block_dt_and_pairs(const DevView& v, int inst, bool active, double d
   __syncthreads();
   if (tid == 0) {
     unsigned long long c = 0;
-    for (int k = 0; k < BT / 32; ++k) c += cred[k];
+    const int nw = BT > 0 ? BT / 32 : (int)(blockDim.x >> 5);  // BT = 0: the launch's block size
+    for (int k = 0; k < nw; ++k) c += cred[k];
     if (c) atomicAdd(&v.sc->pairs_x2, c);
   }
   (void)red;

@@ -2,13 +2,18 @@
 // Source/Domain.cpp:662-806, and the per-step pair arrays of MainNeighbourSearch).
 //
 //   bin      cell key per particle, exactly ListGenerate's floor/clamp rule;
-//            key = ncells for a particle that ListGenerate would drop into a
-//            periodic ghost column (it then sits in no list), ncells+1 for one
-//            that CheckParticleLeave removed.
+//            each cell is split into xsub slabs along x (the key counts
+//            slabs: cell * xsub + slab), so the particles of a cell lie in
+//            x-slab order and the neighbour-list walk can skip slabs out of
+//            reach; key = nbins (= ncells * xsub) for a particle that
+//            ListGenerate would drop into a periodic ghost column (it then
+//            sits in no list), nbins+1 for one that CheckParticleLeave removed.
 //   scan     exclusive prefix of the per-cell counts (3-phase, block-level).
 //   scatter  atomic slot inside its cell's segment.
-//   rank     deterministic order inside each cell: by original index, so the
+//   rank     deterministic order inside each slab: by original index, so the
 //            sorted state depends only on positions, never on atomic timing.
+//   starts   per-cell segment starts (start[c] = slab start of c's first slab)
+//            for everything that walks whole cells.
 //   reorder  gathers every persistent field into the new order (HBM-bound).
 #include <cstdio>
 
@@ -21,11 +26,12 @@ namespace {
 constexpr int kBT = 256;
 
 __global__ void bin_kernel(DevView v, const uint8_t* __restrict__ alive, int* __restrict__ key,
-                           int* __restrict__ count, StepScalars* sc, int dim) {
+                           int* __restrict__ count, StepScalars* sc, int dim, int xsub) {
   if (sc->all_stop) return;
   const Persist& P = cur_persist(v);
   const int n = sc->n;
-  const int orphan_key = v.total_cells, dead_key = v.total_cells + 1;
+  const int nbins = v.total_cells * xsub;
+  const int orphan_key = nbins, dead_key = nbins + 1;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     int k;
     if (!alive[i]) {
@@ -55,11 +61,19 @@ __global__ void bin_kernel(DevView v, const uint8_t* __restrict__ alive, int* __
       } else if (orphan) {
         k = orphan_key;
       } else {
-        k = g.cell_base + (c[2] * g.nc[1] + c[1]) * g.nc[0] + c[0];
+        int slab = 0;
+        if (xsub > 1) {  // x-slab inside the cell (clamped for particles outside it)
+          const double ox = (xs[0] - g.blpf[0]) - c[0] * g.cell_size[0];
+          slab = min(max((int)floor(ox * xsub / g.cell_size[0]), 0), xsub - 1);
+        }
+        k = (g.cell_base + (c[2] * g.nc[1] + c[1]) * g.nc[0] + c[0]) * xsub + slab;
       }
     }
     key[i] = k;
-    atomicAdd(&count[k], 1);
+    // one atomic per distinct cell of the warp: consecutive particles (sorted
+    // by the previous step) mostly share their cell
+    const unsigned peers = __match_any_sync(__activemask(), k);
+    if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&count[k], __popc(peers));
   }
 }
 
@@ -142,7 +156,13 @@ __global__ void scatter_kernel(const int* __restrict__ key, const int* __restric
   const int n = sc->n;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int k = key[i];
-    tmp_perm[start[k] + atomicAdd(&fill[k], 1)] = i;
+    // warp-aggregated slot claim (the order inside a cell is fixed by rank_kernel)
+    const unsigned peers = __match_any_sync(__activemask(), k);
+    const int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&fill[k], __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    tmp_perm[start[k] + base + __popc(peers & ((1u << lane) - 1u))] = i;
   }
 }
 
@@ -169,11 +189,11 @@ __global__ void rank_kernel(const int* __restrict__ key, const int* __restrict__
 
 __global__ void reorder_kernel(DevView v, const int* __restrict__ perm, const int* __restrict__ key,
                                const int* __restrict__ start, int* __restrict__ cellid, uint8_t* __restrict__ alive,
-                               const StepScalars* sc, int ncells, int has_solid, int dyn_mu) {
+                               const StepScalars* sc, int nbins, int xsub, int has_solid, int dyn_mu) {
   if (sc->all_stop) return;
   const Persist& src = cur_persist(v);
   const Persist& dst = next_persist(v);
-  const int n_new = start[ncells + 1];
+  const int n_new = start[nbins + 1];
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n_new; s += gridDim.x * blockDim.x) {
     const int i = perm[s];
     dst.X4[s] = src.X4[i];
@@ -186,9 +206,9 @@ __global__ void reorder_kernel(DevView v, const int* __restrict__ perm, const in
       const double4_32a xs = src.X4[i];
       const int kk = key[i];
       const float h = (float)v.cls[src.cls[i]].h;
-      if (kk < ncells) {
+      if (kk < nbins) {
         const GridDev& g = grid_of(v, v.cls[src.cls[i]].inst);
-        const int lk = kk - g.cell_base;
+        const int lk = kk / xsub - g.cell_base;
         const int cx = lk % g.nc[0], t = lk / g.nc[0], cy = t % g.nc[1], cz = t / g.nc[1];
         v.S.OFF32[s] = make_float4((float)(xs.x - (g.blpf[0] + cx * g.cell_size[0])),
                                    (float)(xs.y - (g.blpf[1] + cy * g.cell_size[1])),
@@ -199,7 +219,7 @@ __global__ void reorder_kernel(DevView v, const int* __restrict__ perm, const in
     }
     dst.orig[s] = src.orig[i];
     const int k = key[i];
-    cellid[s] = (k < ncells) ? k : -1;
+    cellid[s] = (k < nbins) ? k / xsub : -1;
     alive[s] = 1;
     if (dyn_mu) dst.mu[s] = src.mu[i];
     if (has_solid) {
@@ -213,11 +233,21 @@ __global__ void reorder_kernel(DevView v, const int* __restrict__ perm, const in
   }
 }
 
-__global__ void finish_sort_kernel(const int* __restrict__ start, StepScalars* sc, int ncells) {
+__global__ void finish_sort_kernel(const int* __restrict__ start, StepScalars* sc, int nbins) {
   if (sc->all_stop) return;
-  sc->n_cells = start[ncells];
-  sc->n = start[ncells + 1];
+  sc->n_cells = start[nbins];
+  sc->n = start[nbins + 1];
   sc->buf ^= 1;
+}
+
+// Per-cell segment starts from the slab starts: start[c] = sstart[c * xsub]
+// for c <= ncells, and the orphan / dead / total boundaries after them.
+__global__ void cell_starts_kernel(const int* __restrict__ sstart, int* __restrict__ start, int ncells, int xsub,
+                                   const StepScalars* sc) {
+  if (sc->all_stop) return;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c <= ncells) start[c] = sstart[(size_t)c * xsub];
+  else if (c <= ncells + 2) start[c] = sstart[(size_t)ncells * xsub + (c - ncells)];
 }
 
 inline int grid_for(int n) {
@@ -230,19 +260,23 @@ inline int grid_for(int n) {
 void launch_sort(const DevView& v, cudaStream_t st) {
   const Scratch& S = v.S;
   const int ncells = v.total_cells;
-  const int len = ncells + 2;
+  const int xsub = v.o.xsub;
+  const int nbins = ncells * xsub;
+  const int len = nbins + 2;
+  int* sstart = xsub > 1 ? S.sstart : S.start;  // one slab per cell: the slab starts are the cell starts
   cudaMemsetAsync(S.count, 0, sizeof(int) * (size_t)len, st);
-  bin_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(v, v.alive, S.key, S.count, v.sc, v.o.dim);
+  bin_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(v, v.alive, S.key, S.count, v.sc, v.o.dim, xsub);
   const int nb = (len + 1023) / 1024;
-  scan_blocks<<<nb, 1024, 0, st>>>(S.count, S.start, S.block_sums, len);
-  scan_sums<<<1, 1024, 0, st>>>(S.block_sums, nb, S.start + len);
-  scan_add<<<nb, 1024, 0, st>>>(S.start, S.block_sums, len);
+  scan_blocks<<<nb, 1024, 0, st>>>(S.count, sstart, S.block_sums, len);
+  scan_sums<<<1, 1024, 0, st>>>(S.block_sums, nb, sstart + len);
+  scan_add<<<nb, 1024, 0, st>>>(sstart, S.block_sums, len);
   cudaMemsetAsync(S.count, 0, sizeof(int) * (size_t)len, st);
-  scatter_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(S.key, S.start, S.count, S.tmp_perm, v.sc);
-  rank_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(S.key, S.start, S.tmp_perm, v, S.perm, v.sc, ncells);
-  reorder_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(v, S.perm, S.key, S.start, S.cellid, v.alive, v.sc, ncells,
+  scatter_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(S.key, sstart, S.count, S.tmp_perm, v.sc);
+  rank_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(S.key, sstart, S.tmp_perm, v, S.perm, v.sc, nbins);
+  reorder_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(v, S.perm, S.key, sstart, S.cellid, v.alive, v.sc, nbins, xsub,
                                                     v.o.has_solid, v.o.dyn_mu);
-  finish_sort_kernel<<<1, 1, 0, st>>>(S.start, v.sc, ncells);
+  finish_sort_kernel<<<1, 1, 0, st>>>(sstart, v.sc, nbins);
+  if (xsub > 1) cell_starts_kernel<<<grid_for(ncells + 3), kBT, 0, st>>>(sstart, S.start, ncells, xsub, v.sc);
 }
 
 }  // namespace psph

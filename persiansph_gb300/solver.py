@@ -10,10 +10,13 @@ import ctypes as C
 
 import numpy as np
 
-from .abi import (ALL_FIELDS, PsphConfig, PsphError, PsphGrid, PsphIntegrator, field_dtype, field_shape,
+from .abi import (ALL_FIELDS, PsphConfig, PsphError, PsphGrid, PsphIntegrator, PsphTuning, field_dtype, field_shape,
                   load_library, particles_struct)
 from .particles import ParticleSet
 
+
+# the step phases psph_phase_times reports, in order
+PHASES = ("sort", "nlist", "prepare", "forces", "closure", "dt", "update")
 
 class GpuDomain:
     def __init__(self, cfg: PsphConfig, grid: PsphGrid | None = None, integ: PsphIntegrator | None = None):
@@ -123,10 +126,12 @@ class GpuDomain:
         self._check(self._lib.psph_enable_timing(self._ctx, int(on)))
 
     def phase_times(self):
-        buf = (C.c_double * 5)()
+        """Device ms of the last step call's phases (timing enabled), keyed by
+        PHASES."""
+        buf = (C.c_double * len(PHASES))()
         n = C.c_int(0)
-        self._check(self._lib.psph_phase_times(self._ctx, buf, 5, C.byref(n)))
-        return list(buf)
+        self._check(self._lib.psph_phase_times(self._ctx, buf, len(buf), C.byref(n)))
+        return dict(zip(PHASES, list(buf)[: n.value]))
 
     def step_timed(self, nsteps: int):
         ms = C.c_double(0.0)
@@ -231,10 +236,12 @@ class GpuEnsemble:
         self._check(self._lib.psph_enable_timing(self._ctx, int(on)))
 
     def phase_times(self):
-        buf = (C.c_double * 5)()
+        """Device ms of the last step call's phases (timing enabled), keyed by
+        PHASES."""
+        buf = (C.c_double * len(PHASES))()
         n = C.c_int(0)
-        self._check(self._lib.psph_phase_times(self._ctx, buf, 5, C.byref(n)))
-        return list(buf)
+        self._check(self._lib.psph_phase_times(self._ctx, buf, len(buf), C.byref(n)))
+        return dict(zip(PHASES, list(buf)[: n.value]))
 
     def step_timed(self, nsteps: int):
         ms = C.c_double(0.0)
@@ -271,7 +278,64 @@ def _closure_features(self):
     return out[:n]
 
 
+def _workload_key(self) -> str:
+    """Signature of the workload a tuning result belongs to: the switches that
+    select kernels and the particle count (to the nearest 2^k)."""
+    cfg = self.cfg if hasattr(self, "cfg") else self.cfgs[0]
+    n = self.n if isinstance(self.n, int) else sum(self.n(q) for q in range(len(self.cfgs)))
+    return (f"dim{cfg.dimension}-kt{cfg.kernel_type}-vis{cfg.vis_eq}-grad{cfg.gradient_type}-"
+            f"prec{cfg.precision}-per{int(any(cfg.periodic))}-inst{1 if hasattr(self, 'cfg') else len(self.cfgs)}-"
+            f"n2^{max(int(n), 1).bit_length()}-closure{int(getattr(self, '_closure', None) is not None)}")
+
+
+def _autotune(self, steps_per_trial: int = 5, cache: str | None = None) -> dict:
+    """psph_autotune: times every candidate launch setting on this context's
+    own steps (which advance the simulation) and keeps the fastest. With
+    `cache` (a JSON file), a setting stored for the same workload signature is
+    applied without trials, and a new result is stored there."""
+    import json
+    import os
+    key = _workload_key(self)
+    if cache and os.path.exists(cache):
+        try:
+            known = json.load(open(cache))
+        except (OSError, ValueError):
+            known = {}
+        if key in known:
+            t = known[key]
+            self.set_tuning(t["pair_block"], t["cell_split"])
+            return dict(t, cached=True)
+    t = PsphTuning()
+    self._check(self._lib.psph_autotune(self._ctx, int(steps_per_trial), C.byref(t)))
+    out = {"pair_block": t.pair_block, "cell_split": t.cell_split, "ms_per_step": t.ms_per_step}
+    if cache:
+        known = {}
+        if os.path.exists(cache):
+            try:
+                known = json.load(open(cache))
+            except (OSError, ValueError):
+                known = {}
+        known[key] = out
+        with open(cache, "w") as f:
+            json.dump(known, f, indent=1, sort_keys=True)
+    return out
+
+
+def _tuning(self) -> dict:
+    t = PsphTuning()
+    self._check(self._lib.psph_get_tuning(self._ctx, C.byref(t)))
+    return {"pair_block": t.pair_block, "cell_split": t.cell_split, "ms_per_step": t.ms_per_step}
+
+
+def _set_tuning(self, pair_block: int = 128, cell_split: int = 1):
+    t = PsphTuning(pair_block, cell_split, 0.0)
+    self._check(self._lib.psph_set_tuning(self._ctx, C.byref(t)))
+
+
 for _cls in (GpuDomain, GpuEnsemble):
+    _cls.autotune = _autotune
+    _cls.tuning = _tuning
+    _cls.set_tuning = _set_tuning
     _cls.attach_closure = _attach_closure
     _cls.closure_stats = _closure_stats
     _cls.closure_features = _closure_features

@@ -37,8 +37,9 @@ def test_struct_layouts_match_header():
 #include <stddef.h>
 #include "psph.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu\n", sizeof(psph_config), sizeof(psph_grid), sizeof(psph_integrator),
-         sizeof(psph_particles), offsetof(psph_config, gravity), offsetof(psph_particles, sigma));
+  printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(psph_config), sizeof(psph_grid), sizeof(psph_integrator),
+         sizeof(psph_particles), offsetof(psph_config, gravity), offsetof(psph_particles, sigma),
+         sizeof(psph_tuning));
   return 0;
 }
 '''
@@ -54,6 +55,7 @@ int main(void) {
     assert out[3] == ctypes.sizeof(abi.PsphParticles)
     assert out[4] == abi.PsphConfig.gravity.offset
     assert out[5] == abi.PsphParticles.sigma.offset
+    assert out[6] == ctypes.sizeof(abi.PsphTuning)
 
 
 def test_abi_version():

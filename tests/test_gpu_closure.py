@@ -120,8 +120,8 @@ def test_closure_features_and_viscosity_fp64(gpu):
     free = ro["is_free"] == 1
     # neighbour counts: in-support pairs of the reference's pair list, per particle
     cnt = np.bincount(o.pairs(3).ravel(), minlength=len(free))
-    f_o, shear = mo.features(ro["strain_rate"], np.exp(feats[:, 2]), rho_before, ro["ref_density"], ro["h"], dx,
-                             cnt)
+    vort = np.exp(feats[:, 2].astype(np.float64)) * ro["cs"] / ro["h"]  # |vorticity| from its feature
+    f_o, shear = mo.features(ro["strain_rate"], vort, rho_before, ro["ref_density"], ro["h"], dx, cnt, ro["cs"])
     assert np.max(shear[free]) > 0.0
     np.testing.assert_array_equal(feats[free, 5], cnt[free].astype(np.float32))
     assert np.max(np.abs(feats[free, 0] - f_o[free, 0])) <= 1e-5
@@ -192,7 +192,7 @@ def test_closure_vorticity_rigid_rotation(gpu, precision):
     lo, hi = np.full(3, 2 * h), np.full(3, 0.4 - 2 * h)
     inner = free & np.all((x >= lo) & (x <= hi), axis=1)
     assert inner.sum() > 100
-    w = np.exp(feats[inner, 2].astype(np.float64))
+    w = np.exp(feats[inner, 2].astype(np.float64)) * p.get("cs")[inner] / h  # feature = |vorticity| h / Cs
     assert np.max(np.abs(w / (2 * omega) - 1.0)) <= 0.03
 
 

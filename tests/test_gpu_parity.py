@@ -157,10 +157,104 @@ def test_fp32c_single_step_parity_1e5(gpu, name):
         assert ed <= 1e-5, f"{name} {warm}: FP32C density-rate rel err {ed:.3e}"
 
 
-def test_fp32c_rejects_solids(gpu):
-    dom, dt, _ = CASES["granular"][0]()
+SOLID_CASES = ["granular", "granular_lf_fail3", "solid_block"]
+
+
+@pytest.mark.parametrize("name", SOLID_CASES)
+def test_fp32c_solid_single_step_parity_1e5(gpu, name):
+    """FP32C form of the soil / solid pair force (CalcForce2233) against the
+    FP64 oracle. Accelerations: within 1e-5 of each particle's sum of term
+    magnitudes. Density rates: the same per-particle bound for particles
+    whose term sum is at least 1e-6 of the largest, and 1e-5 of the term sums
+    norm-wise over all free particles. (Below that, a particle and its neighbours move as one
+    body: their velocity differences are a few ulps of the velocities, and the
+    oracle's density rate is the rounding noise of its FP64 velocities, which
+    48-bit FP32 velocity pairs cannot resolve.) Strain and rotation rates
+    within 1e-5 of the largest oracle rate; the FP64 stress update that
+    follows keeps the step's stresses within 1e-5 of the largest stress."""
+    builder, _, _ = CASES[name]
+    dom, dt, _ = builder()
+    cfg = dom.config(dt)
+    cfg32 = dom.config(dt)
+    cfg32.precision = 1  # PSPH_FP32C
+    for warm in (0, 3):
+        o = OracleDomain(cfg, dom.particles, initial=True)
+        if warm:
+            o.step(warm)
+            gd = continue_on_gpu(cfg32, o)
+        else:
+            gd = GpuDomain(cfg32)
+            gd.upload(dom.particles, initial=True)
+        o.step(1)
+        gd.step(1)
+        a_scale, dr_scale = o.scales()
+        g, r = gd.download_fields(), o.download()
+        free = r["is_free"] == 1
+        ea = np.max(np.linalg.norm(g["a"] - r["a"], axis=1)[free] / a_scale[free])
+        assert ea <= 1e-5, f"{name} {warm}: FP32C acceleration rel err {ea:.3e}"
+        resolved = free & (dr_scale > 0.0) & (dr_scale >= 1e-6 * np.max(dr_scale[free]))
+        if resolved.any():
+            ed = np.max(np.abs(g["ddensity"] - r["ddensity"])[resolved] / dr_scale[resolved])
+            assert ed <= 1e-5, f"{name} {warm}: FP32C density-rate rel err {ed:.3e}"
+        dn = np.linalg.norm((g["ddensity"] - r["ddensity"])[free]) / (np.linalg.norm(dr_scale[free]) + 1e-300)
+        assert dn <= 1e-5, f"{name} {warm}: FP32C density-rate norm-wise rel err {dn:.3e}"
+        for f in ("strain_rate", "rotation_rate", "sigma"):
+            ref = np.max(np.abs(r[f][free]))
+            if ref > 0:
+                e = np.max(np.abs(g[f][free] - r[f][free])) / ref
+                assert e <= 1e-5, f"{name} {warm}: FP32C {f} rel err {e:.3e}"
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_launch_tuning_does_not_change_results(gpu, precision):
+    """The block size of the pair kernels is a launch choice only: states are
+    bit-identical. The x-slab split of the cells reorders each particle's
+    neighbours, so only the rounding of the sums changes: after 4 steps every
+    field agrees within 1e-12 (FP64) / 1e-5 (FP32C) of its largest magnitude.
+    psph_autotune returns one of the candidate settings."""
+    dom, dt, _ = CASES["dam3d"][0]()
+    cfg = dom.config(dt)
+    cfg.precision = precision
+    states = {}
+    for block, split in [(128, 1), (64, 1), (256, 2), (128, 4)]:
+        gd = GpuDomain(cfg)
+        gd.upload(dom.particles, initial=True)
+        gd.set_tuning(block, split)
+        gd.step(4)
+        states[(block, split)] = gd.download_fields(("x", "v", "density", "a", "ddensity"))
+        gd.close()
+    ref = states[(128, 1)]
+    for f in ref:
+        np.testing.assert_array_equal(states[(64, 1)][f], ref[f])
+    tol = 1e-12 if precision == 0 else 1e-5
+    for key in [(256, 2), (128, 4)]:
+        for f in ref:
+            scale = np.max(np.abs(ref[f])) + 1e-300
+            err = np.max(np.abs(states[key][f] - ref[f])) / scale
+            assert err <= tol, f"split {key}: {f} differs by {err:.2e} of its scale"
+    gd = GpuDomain(cfg)
+    gd.upload(dom.particles, initial=True)
+    t = gd.autotune(2)
+    assert t["pair_block"] in (64, 128, 256) and t["cell_split"] in (1, 2, 4) and t["ms_per_step"] > 0
+    assert gd.tuning()["pair_block"] == t["pair_block"] and gd.tuning()["cell_split"] == t["cell_split"]
+    gd.close()
+
+
+def test_autotune_cache(gpu, tmp_path):
+    """A tuning result stored for a workload signature is reused without
+    trials by a context of the same workload."""
+    dom, dt, _ = CASES["dam3d"][0]()
     cfg = dom.config(dt)
     cfg.precision = 1
-    gd = GpuDomain(cfg)
-    with pytest.raises(Exception, match="UNSUPPORTED"):
-        gd.upload(dom.particles, initial=True)
+    cache = str(tmp_path / "tuning.json")
+    first = GpuDomain(cfg)
+    first.upload(dom.particles, initial=True)
+    t1 = first.autotune(2, cache=cache)
+    first.close()
+    second = GpuDomain(cfg)
+    second.upload(dom.particles, initial=True)
+    t2 = second.autotune(2, cache=cache)
+    assert t2.get("cached") and t2["pair_block"] == t1["pair_block"] and t2["cell_split"] == t1["cell_split"]
+    assert second.tuning()["pair_block"] == t1["pair_block"]
+    assert second.integrator().steps == 0  # no trial steps were run
+    second.close()
