@@ -224,6 +224,8 @@ def main():
     ap.add_argument("--ref-dx", type=float, default=0.01)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched granular-column line")
+    ap.add_argument("--tuning", default="auto",
+                    help="'auto' (psph_autotune on the workload's own steps) or BLOCK:SPLIT to fix the launch shape")
     ap.add_argument("--ens-n", type=int, default=256)
     ap.add_argument("--ens-dx", type=float, default=1e-3)
     args = ap.parse_args()
@@ -264,7 +266,12 @@ def main():
 
     def measure(precision, closure=False):
         cfg, gd = open_domain(precision, closure)
-        tuning = gd.autotune(3)  # launch shapes timed on this workload's own (untimed) steps
+        if args.tuning == "auto":
+            tuning = gd.autotune(3)  # launch shapes timed on this workload's own (untimed) steps
+        else:
+            block, split = (int(x) for x in args.tuning.split(":"))
+            gd.set_tuning(block, split)
+            tuning = gd.tuning()
         with ClockSampler(local) as clk:
             gd.step(args.warmup)
             pc0 = gd.pair_count()

@@ -467,6 +467,7 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
         return set_err(c, PSPH_ERR_UNSUPPORTED, "periodic axis %d spans fewer than 3 cells", d);
     }
     gd.hmax = g.hmax;
+    for (int d = 0; d < 3; ++d) gd.inv_cell_size32[d] = (float)(1.0 / g.cell_size[d]);
     gd.cellfac = (cf.kernel_type == PSPH_QUINTIC_SPLINE) ? 3.0 : 2.0;
     g.cellfac = gd.cellfac;
     const long long nci = (long long)gd.nc[0] * gd.nc[1] * gd.nc[2];
@@ -575,8 +576,10 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
   if ((st = dalloc(c, &S.nl, (size_t)o.nl_cap * N))) return st;
   if (o.need_sr || o.has_solid)
     if ((st = dalloc(c, &S.strain_rate, 9 * N))) return st;
-  if (o.fp32)
-    if ((st = dalloc(c, &S.V32, N)) || (st = dalloc(c, &S.D32, N))) return st;
+  if (o.fp32) {
+    if ((st = dalloc(c, &S.V32, N)) || (st = dalloc(c, &S.D32, N)) || (st = dalloc(c, &S.NSV32, N))) return st;
+    if (dyn_mu && (st = dalloc(c, &S.MU32, N))) return st;
+  }
   if (o.fp32 && o.has_solid) {
     if ((st = dalloc(c, &S.SIG32, 2 * N)) || (st = dalloc(c, &S.VB32, N)) || (st = dalloc(c, &S.V32LO, N)))
       return st;
@@ -606,6 +609,7 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
       F.material = C.material;
       F.pres_eq = C.pres_eq;
       F.inst = C.inst;
+      F.h_over_dx = c->opt.closure ? (float)(C.h / c->opt.closure_dx) : 0.f;
     }
     if ((st = dalloc(c, &c->d_cls32, c32.size()))) return st;
     CUDA_TRY(c, cudaMemcpy(c->d_cls32, c32.data(), c32.size() * sizeof(PClass32), cudaMemcpyHostToDevice));
@@ -1162,12 +1166,19 @@ psph_status psph_closure_attach(psph_ctx* c, const psph_mlp* mlp, double dx) {
   const size_t N = (size_t)c->ncap;
   if (!c->d_mlp) {
     if ((st = dalloc(c, &c->d_mlp, 1)) || (st = dalloc(c, &c->S.cvort, N)) || (st = dalloc(c, &c->S.cnnb, N)) ||
+        (st = dalloc(c, &c->S.cshear, N)) || (st = dalloc(c, &c->S.cr3, N)) ||
         (st = dalloc(c, &c->S.cfeat, 6 * N)) || (st = dalloc(c, &c->S.nut, N)))
       return st;
   }
   CUDA_TRY(c, cudaMemcpy(c->d_mlp, img, sizeof(MlpImage), cudaMemcpyDeviceToDevice));
   c->opt.closure = 1;
   c->opt.closure_dx = dx;
+  {  // the h/dx feature per class, as the FP64 form rounds it
+    std::vector<PClass32> c32(c->classes.size());
+    CUDA_TRY(c, cudaMemcpy(c32.data(), c->d_cls32, c32.size() * sizeof(PClass32), cudaMemcpyDeviceToHost));
+    for (size_t q = 0; q < c32.size(); ++q) c32[q].h_over_dx = (float)(c->classes[q].h / dx);
+    CUDA_TRY(c, cudaMemcpy(c->d_cls32, c32.data(), c32.size() * sizeof(PClass32), cudaMemcpyHostToDevice));
+  }
   if ((st = sync_scalars(c))) return st;
   c->h_sc->closure_eval = 0;
   c->h_sc->closure_fallback = 0;

@@ -42,6 +42,7 @@ struct PClass {
 // loops issue no FP64 instructions), with the boolean switches as bits.
 struct PClass32 {
   float mass, h, fpmassc, alpha, beta, mu0, ti, tin, tid, cs, rho0, p0;
+  float h_over_dx;  // closure feature h / dx, rounded from FP64 as the FP64 form does (set at attach)
   int flags;  // bit 0 free, 1 no-slip, 2 LES, 3 Shepard, 4 T0>0, 5 TI>0
   int material, pres_eq, inst;
 };
@@ -78,6 +79,7 @@ struct GridDev {
   int periodic[3];
   int ncells;     // nc[0]*nc[1]*nc[2]
   int cell_base;  // first global cell id of this instance
+  float inv_cell_size32[3];  // 1 / cell_size in FP32 (cell-index estimate of the sort)
 };
 
 // ---------------------------------------------------------------------------

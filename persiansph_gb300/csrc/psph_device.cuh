@@ -45,6 +45,8 @@ struct Scratch {
   float4* TIR32;     // FP32C solids with TI: symmetric TIR, same layout
   float4* VB32;      // FP32C solids: wall history velocity (MVerlet vb / leapfrog vb)
   float4* V32LO;     // FP32C solids: v - (float)v, the low-order part of the velocity
+  float* MU32;       // FP32C, per-particle viscosity (LES / Bingham): FP32 copy of Persist::mu
+  float4* NSV32;     // FP32C: wall no-slip velocity in FP32
   double4_32a* D4;   // seen by partners: (1/density, pressure/density^2, sound speed, density);
                      // a wall's density is the inverse EOS of its interpolated pressure
   double4_32a* A4;       // ax, ay, az, dDensity
@@ -63,6 +65,8 @@ struct Scratch {
   // learned closure (allocated when attached)
   float* cvort;          // |vorticity| from the pair sums
   float* cnnb;           // neighbours inside the support
+  float* cshear;         // FP32C: ShearRate of the strain-rate sums
+  float* cr3;            // FP32C: det(StrainRate) / (StrainRate:StrainRate)^(3/2)
   float* cfeat;          // raw network features, 6 per particle
   double* nut;           // eddy viscosity from the network; -1 = use Smagorinsky
 };

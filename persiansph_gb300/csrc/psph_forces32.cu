@@ -136,6 +136,9 @@ __global__ void __launch_bounds__(kFT32) copies32_kernel(DevView v) {
     const float c = (C.pres_eq == 1) ? C.cs * ratio * ratio * ratio : C.cs;
     v.S.D32[w] = make_float4(inv, p * inv * inv, c, rho);
   }
+  // FP32 copy of a per-particle viscosity: the pair loop then converts nothing
+  // (a double-to-float conversion runs on the FP64 pipe, 1/64 of the FP32 rate)
+  if (v.o.dyn_mu) v.S.MU32[w] = (float)P.mu[w];
 }
 
 template <int DIM, int KT>
@@ -222,6 +225,7 @@ __global__ void __launch_bounds__(kFT32) prepare32_kernel(DevView v) {
   P.V4[w] = vw;
   v.S.sumkernel[w] = sk;
   v.S.nsv4[w] = make_double4_32a(n0, n1, n2, 0.0);
+  v.S.NSV32[w] = make_float4(n0, n1, n2, 0.f);
   v.S.V32[w] = make_float4((float)vw.x, (float)vw.y, (float)vw.z, p);
   const PClass32& Ce = CT[o.eos_cls];
   float rw = (float)P.X4[w].w, cwv = 0.f;
@@ -282,7 +286,7 @@ __global__ void __maxnreg__(FL == 0 ? 128 : 96) forces_fluid32_kernel(DevView v)
   const float4 di4 = v.S.D32[is];
   const float di = di4.w, inv_i = di4.x, Pi = di4.y, ci_snd = di4.z, pi = vi.w;
   const float mi = Ci.mass, hi = oi.w;
-  const float mui = o.dyn_mu ? (float)P.mu[is] : Ci.mu0;
+  const float mui = o.dyn_mu ? v.S.MU32[is] : Ci.mu0;
   const int fi = Ci.flags;
   const bool shep = (fi & CF_SHEPARD) && (Is.shepard_counter == o.shepard_step);
   const bool sr_self = fi & (CF_T0 | CF_LES);
@@ -352,14 +356,14 @@ __global__ void __maxnreg__(FL == 0 ? 128 : 96) forces_fluid32_kernel(DevView v)
         vab0 = v0; vab1 = v1; vab2 = v2;
         if (uniform_mu) Mu = mu_u;
         else {
-          const float muj = dyn_mu ? (float)P.mu[j] : Cj.mu0;
+          const float muj = dyn_mu ? v.S.MU32[j] : Cj.mu0;
           Mu = 2.f * mui * muj / (mui + muj);
         }
       } else {
-        const double4_32a ns = v.S.nsv4[j];
-        vab0 = vi.x - (2.f * vj.x - (float)ns.x);
-        vab1 = vi.y - (2.f * vj.y - (float)ns.y);
-        vab2 = vi.z - (2.f * vj.z - (float)ns.z);
+        const float4 ns = v.S.NSV32[j];
+        vab0 = vi.x - (2.f * vj.x - ns.x);
+        vab1 = vi.y - (2.f * vj.y - ns.y);
+        vab2 = vi.z - (2.f * vj.z - ns.z);
         Mu = mui;
       }
       if (vis_eq <= 2) {
@@ -447,10 +451,19 @@ __global__ void __maxnreg__(FL == 0 ? 128 : 96) forces_fluid32_kernel(DevView v)
     if (closure) {
       v.S.cvort[i] = sqrtf(w01 * w01 + w02 * w02 + w12 * w12);
       v.S.cnnb[i] = (float)nnb;
+      // the closure's shear-rate features from the (symmetric) strain-rate
+      // sums, in FP32: the same contractions as its FP64 form
+      const float temp = sr0 * sr0 + 2.f * sr1 * sr1 + 2.f * sr2 * sr2 + sr4 * sr4 + 2.f * sr5 * sr5 + sr8 * sr8;
+      const float det = sr0 * (sr4 * sr8 - sr5 * sr5) - sr1 * (sr1 * sr8 - sr5 * sr2) + sr2 * (sr1 * sr5 - sr4 * sr2);
+      v.S.cshear[i] = sqrtf(0.5f * temp);
+      v.S.cr3[i] = temp > 0.f ? det / (temp * sqrtf(temp)) : 0.f;
     }
     if (!(isfinite(axd) && isfinite(ayd) && isfinite(azd) && isfinite(drd))) atomicOr(&v.sc->status, ST_NONFINITE);
-    const double an = sqrt(axd * axd + ayd * ayd + azd * azd);
-    const double cand = o.sqrt_h_a * sqrt(v.cls[ci_cls].h / an);  // FP64 dt reduction
+    // this particle's time-step bound sqrt_h_a sqrt(h/|a|) in FP32; the
+    // minimum over particles and AdaptiveTimeStep stay FP64
+    const float ax32 = (float)axd, ay32 = (float)ayd, az32 = (float)azd;
+    const float an = sqrtf(ax32 * ax32 + ay32 * ay32 + az32 * az32);
+    const double cand = (double)((float)o.sqrt_h_a * sqrtf(Ci.h / an));
     if (cand < dtc) dtc = cand;
   }
   block_dt_and_pairs<0>(v, Ci.inst, active, dtc, npair2, red, cred);
@@ -492,6 +505,8 @@ __global__ void __launch_bounds__(kFT32) solid_copies32_kernel(DevView v) {
   if (!(C.flags & CF_FREE)) {
     const double4_32a vb = (v.o.scheme == PSPH_MVERLET) ? P.H4[w] : P.H4b[w];
     v.S.VB32[w] = make_float4((float)vb.x, (float)vb.y, (float)vb.z, 0.f);
+    const double4_32a ns = v.S.nsv4[w];
+    v.S.NSV32[w] = make_float4((float)ns.x, (float)ns.y, (float)ns.z, 0.f);
   }
 }
 
@@ -606,10 +621,10 @@ __global__ void __maxnreg__(128) forces_solid32_kernel(DevView v) {
     float vab0, vab1, vab2;
     if (fj) { vab0 = v0; vab1 = v1; vab2 = v2; }
     else if ((Ci.flags | fjf) & CF_NOSLIP) {
-      const double4_32a ns = v.S.nsv4[j];
-      vab0 = vi.x - (2.f * vj.x - (float)ns.x);
-      vab1 = vi.y - (2.f * vj.y - (float)ns.y);
-      vab2 = vi.z - (2.f * vj.z - (float)ns.z);
+      const float4 ns = v.S.NSV32[j];
+      vab0 = vi.x - (2.f * vj.x - ns.x);
+      vab1 = vi.y - (2.f * vj.y - ns.y);
+      vab2 = vi.z - (2.f * vj.z - ns.z);
     } else {
       const float4 vbj = v.S.VB32[j];
       vab0 = vi.x - vbj.x; vab1 = vi.y - vbj.y; vab2 = vi.z - vbj.z;
@@ -677,8 +692,11 @@ __global__ void __maxnreg__(128) forces_solid32_kernel(DevView v) {
     ro[3] = -(double)rr0; ro[4] = 0.0; ro[5] = rr2;
     ro[6] = -(double)rr1; ro[7] = -(double)rr2; ro[8] = 0.0;
     if (!(isfinite(axd) && isfinite(ayd) && isfinite(azd) && isfinite(drd))) atomicOr(&v.sc->status, ST_NONFINITE);
-    const double an = sqrt(axd * axd + ayd * ayd + azd * azd);
-    const double cand = o.sqrt_h_a * sqrt(v.cls[ci_cls].h / an);  // FP64 dt reduction
+    // this particle's time-step bound sqrt_h_a sqrt(h/|a|) in FP32; the
+    // minimum over particles and AdaptiveTimeStep stay FP64
+    const float ax32 = (float)axd, ay32 = (float)ayd, az32 = (float)azd;
+    const float an = sqrtf(ax32 * ax32 + ay32 * ay32 + az32 * az32);
+    const double cand = (double)((float)o.sqrt_h_a * sqrtf(Ci.h / an));
     if (cand < dtc) dtc = cand;
   }
   block_dt_and_pairs<0>(v, Ci.inst, active, dtc, npair2, red, cred);

@@ -291,7 +291,10 @@ __device__ __forceinline__ const float* tc_norm(const TcCtx& t) { return t.f + 4
 // ---------------------------------------------------------------------------
 // closure inside the step
 // ---------------------------------------------------------------------------
-template <int DIM>
+// F32: the FP32C form, whose pair kernel leaves the shear-rate features in
+// FP32 (no FP64 arithmetic here); otherwise the features come from the FP64
+// strain-rate sums with FP64 contractions.
+template <int DIM, bool F32>
 __global__ void __launch_bounds__(kTcThreads) closure_kernel(DevView v) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t bars[2];
@@ -315,7 +318,26 @@ __global__ void __launch_bounds__(kTcThreads) closure_kernel(DevView v) {
     bool act = false;
     float f[kMlpIn] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     double shear = 0.0, h = 0.0;
-    if (s < n) {
+    if (s < n && F32) {
+      const PClass32& C = v.cls32[P.cls[s]];
+      act = (C.flags & CF_FREE) && C.material == 1 && (C.flags & CF_LES) && !v.inst[C.inst].stop;
+      float sh32 = 0.f;
+      if (act) {
+        sh32 = v.S.cshear[s];
+        const float tscale = C.cs > 0.f ? C.h / C.cs : 1.f;
+        f[0] = logf(fmaxf(sh32 * tscale, 1e-12f));
+        f[1] = v.S.cr3[s];
+        f[2] = logf(fmaxf(v.S.cvort[s] * tscale, 1e-12f));
+        f[3] = v.S.D32[s].w / C.rho0;
+        f[4] = C.h_over_dx;
+        f[5] = v.S.cnnb[s];
+      }
+      shear = sh32;
+      h = C.h;
+      float* fo = v.S.cfeat + (size_t)kMlpIn * s;
+#pragma unroll
+      for (int k = 0; k < kMlpIn; ++k) fo[k] = f[k];
+    } else if (s < n) {
       const PClass& C = v.cls[P.cls[s]];
       act = C.is_free && C.material == 1 && C.les && !v.inst[C.inst].stop;
       if (act) {
@@ -355,7 +377,10 @@ __global__ void __launch_bounds__(kTcThreads) closure_kernel(DevView v) {
     for (int k = 0; k < kMlpIn; ++k) u[k] = in_range ? (f[k] - mean[k]) * inv_std[k] : 0.f;
     float z4 = 0.f;
     if (!tc_forward(t, u, &z4)) break;
-    if (act) v.S.nut[s] = in_range ? (double)softplus(z4) * h * h * shear : -1.0;
+    if (act) {
+      if (F32) v.S.nut[s] = in_range ? (double)(softplus(z4) * (float)h * (float)h * (float)shear) : -1.0;
+      else v.S.nut[s] = in_range ? (double)softplus(z4) * h * h * shear : -1.0;
+    }
     n_eval += act ? 1 : 0;
     n_fb += (act && !in_range) ? 1 : 0;
   }
@@ -636,9 +661,13 @@ cudaError_t ensure_tc_attrs() {
   if (tc_attr_set) return cudaSuccess;
   cudaError_t e = cudaFuncSetAttribute(infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(closure_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes);
+    e = cudaFuncSetAttribute(closure_kernel<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(closure_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes);
+    e = cudaFuncSetAttribute(closure_kernel<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(closure_kernel<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(closure_kernel<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes);
   if (e == cudaSuccess) tc_attr_set = true;
   return e;
 }
@@ -652,8 +681,13 @@ void launch_closure(const DevView& v, cudaStream_t st) {
   // four CTAs per SM (128 registers x 128 threads, ~52 KB shared memory and 64
   // TMEM columns each): while one waits on its MMAs the others run epilogues
   const int grid = std::max(1, std::min(ntiles, 4 * num_sms()));
-  if (v.o.dim == 2) closure_kernel<2><<<grid, kTcThreads, kTcSmemBytes, st>>>(v);
-  else closure_kernel<3><<<grid, kTcThreads, kTcSmemBytes, st>>>(v);
+  if (v.o.fp32) {
+    if (v.o.dim == 2) closure_kernel<2, true><<<grid, kTcThreads, kTcSmemBytes, st>>>(v);
+    else closure_kernel<3, true><<<grid, kTcThreads, kTcSmemBytes, st>>>(v);
+  } else {
+    if (v.o.dim == 2) closure_kernel<2, false><<<grid, kTcThreads, kTcSmemBytes, st>>>(v);
+    else closure_kernel<3, false><<<grid, kTcThreads, kTcSmemBytes, st>>>(v);
+  }
 }
 }  // namespace psph
 

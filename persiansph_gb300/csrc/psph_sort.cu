@@ -43,7 +43,15 @@ __global__ void bin_kernel(DevView v, const uint8_t* __restrict__ alive, int* __
       int c[3] = {0, 0, 0};
       bool orphan = false, out = false;
       for (int d = 0; d < dim; ++d) {
-        int cd = (int)floor((xs[d] - g.blpf[d]) / g.cell_size[d]);
+        // ListGenerate's floor((x - BLPF) / CellSize) (Source/Domain.cpp:669-691).
+        // An FP32 estimate decides it unless the quotient lies within the
+        // estimate's error of an integer; only then the FP64 division runs
+        // (a division costs tens of operations on the FP64 pipe).
+        const double a = xs[d] - g.blpf[d];
+        const float t = (float)a * g.inv_cell_size32[d];
+        const float ft = floorf(t), fr = t - ft, tol = 1e-3f + 4e-7f * fabsf(t);
+        int cd = (int)ft;
+        if (!(fr >= tol && fr <= 1.f - tol)) cd = (int)floor(a / g.cell_size[d]);
         if (cd < 0) {
           if ((g.blpf[d] - xs[d]) <= g.hmax) cd = 0;
           else out = true;
@@ -62,9 +70,9 @@ __global__ void bin_kernel(DevView v, const uint8_t* __restrict__ alive, int* __
         k = orphan_key;
       } else {
         int slab = 0;
-        if (xsub > 1) {  // x-slab inside the cell (clamped for particles outside it)
-          const double ox = (xs[0] - g.blpf[0]) - c[0] * g.cell_size[0];
-          slab = min(max((int)floor(ox * xsub / g.cell_size[0]), 0), xsub - 1);
+        if (xsub > 1) {  // x-slab inside the cell (clamped for particles outside it), in FP32
+          const float ox = (float)((xs[0] - g.blpf[0]) - c[0] * g.cell_size[0]);
+          slab = min(max((int)floorf(ox * (float)xsub * g.inv_cell_size32[0]), 0), xsub - 1);
         }
         k = (g.cell_base + (c[2] * g.nc[1] + c[1]) * g.nc[0] + c[0]) * xsub + slab;
       }

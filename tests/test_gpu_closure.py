@@ -218,3 +218,33 @@ def test_closure_gain_over_smagorinsky(gpu):
     c_const = float(np.sum(Y * w * w) / np.sum(w * w))  # best constant coefficient (least squares in nu)
     errs = apriori_errors(net, Xh, Yh, Hh, Sh, c_const)
     assert errs["network"] < errs["smagorinsky"], errs
+
+
+def test_closure_fp32c_features_match_fp64(gpu):
+    """The FP32C form computes the closure's shear-rate features in FP32 from
+    its own strain-rate sums: from the same state they agree with the FP64
+    form's features, and so do the eddy viscosities (1e-4 relative)."""
+    dx = 0.04
+    dom, dt, cfg = les_dam3d()
+    o = OracleDomain(dom.config(dt), dom.particles, initial=True)
+    o.step(5)
+    net = ClosureNet(seed=13)
+    out = {}
+    for prec in (0, 1):
+        c = dom.config(dt)
+        c.precision = prec
+        gd = continue_on_gpu(c, o)
+        gd.attach_closure(net, dx)
+        gd.step(1)
+        out[prec] = (gd.closure_features(), gd.download_fields(("mu", "is_free")))
+        gd.close()
+    f64, f32 = out[0][0], out[1][0]
+    free = out[0][1]["is_free"] == 1
+    assert np.max(np.abs(f32[free, 0] - f64[free, 0])) <= 1e-3
+    assert np.max(np.abs(f32[free, 1] - f64[free, 1])) <= 1e-3
+    assert np.max(np.abs(f32[free, 2] - f64[free, 2])) <= 1e-3
+    assert np.max(np.abs(f32[free, 3] - f64[free, 3])) <= 1e-6
+    np.testing.assert_array_equal(f32[free, 4], f64[free, 4])
+    assert np.max(np.abs(f32[free, 5] - f64[free, 5])) <= 1  # a pair at the support edge may differ
+    mu64, mu32 = out[0][1]["mu"][free], out[1][1]["mu"][free]
+    assert np.max(np.abs(mu32 - mu64) / mu64) <= 1e-4
