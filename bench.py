@@ -7,6 +7,7 @@ Morris viscosity, Modified Verlet + Shepard (the 4-DamBreak3D.cpp pattern).
 Synthetic, seeded lattice input built by persiansph_gb300.scenarios.
 
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+  python bench.py --workload dam2d|poiseuille2d|dam3d_coarse   (the smaller configurations)
 
 Our arm: W untimed steps, then K steps timed with CUDA events on the solver's
 stream (inputs resident in HBM; the working set, several GB, exceeds the 129 MB
@@ -34,6 +35,12 @@ sys.path.insert(0, REPO)
 
 METRIC = ("pair-interactions/s @ 3D dam break (5.28M fluid particles), FP32C form with the learned closure; "
           "FP64 plain beside it")
+
+
+def metric_name(workload: str) -> str:
+    if workload == "dam3d":
+        return METRIC
+    return f"pair-interactions/s @ {workload}, FP32C form; FP64 plain beside it"
 UNIT = "pair-interactions/s"
 # FP64 operations per directed pair evaluation of the fluid kernel for this
 # workload's options (Wendland, Tait, artificial viscosity, Morris, squared
@@ -134,9 +141,37 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(inside), "window": window}
 
 
-def build_workload(dx):
+# The workloads --workload selects. "dam3d" (the default) is the headline: the
+# 3D dam break the metric is quoted on; the others are the smaller benchmark
+# configurations, measured with the same contract.
+WORKLOADS = {
+    "dam3d": {"desc": "3D dam break: tank 3.22x1.0x1.0 m, column 1.2x0.55x1.0 m, dx=%g m", "dx": 0.005,
+              "ref_dx": 0.01, "closure": True},
+    "dam3d_coarse": {"desc": "3D dam break, LES on, learned closure: tank 3.22x1.0x1.0 m, column 1.2x0.55x1.0 m, "
+                             "dx=%g m", "dx": 0.02, "ref_dx": 0.02, "closure": True},
+    "dam2d": {"desc": "2D dam break: tank 4.0x3.0 m, column 1.0x2.0 m, cubic spline h=1.2dx, dx=%g m",
+              "dx": 0.005, "ref_dx": 0.005, "closure": False},
+    "poiseuille2d": {"desc": "2D Poiseuille flow: channel 1.0e-3 m, periodic 0.5e-3 m, quintic spline h=1.3dx, "
+                             "dx=%g m", "dx": 2.5e-5, "ref_dx": 2.5e-5, "closure": False},
+}
+
+
+def build_workload(dx, name="dam3d"):
     from persiansph_gb300 import scenarios
-    return scenarios.dam_break_3d(dx=dx)
+    if name == "dam3d":
+        return scenarios.dam_break_3d(dx=dx)
+    if name == "dam3d_coarse":
+        from persiansph_gb300.closure import les_case
+        return les_case(dx, L=1.2, H=0.55, W=1.0, TL=3.22, TH=1.0, TW=1.0, c0=40.0)
+    if name == "dam2d":
+        return scenarios.dam_break_2d(dx=dx)
+    if name == "poiseuille2d":
+        dom, dt, info = scenarios.poiseuille(dx=dx)
+        free = dom.particles.get("is_free") == 1
+        info.setdefault("n_fluid", int(free.sum()))
+        info.setdefault("n_wall", int((~free).sum()))
+        return dom, dt, info
+    raise ValueError(name)
 
 
 def measure_ensemble(n_inst: int, dx: float, steps: int, warmup: int):
@@ -174,11 +209,12 @@ def measure_ensemble(n_inst: int, dx: float, steps: int, warmup: int):
             "gpu_launches_per_step": launches / max(done, 1), "phase_ms": phases}
 
 
-def cpu_reference(dx_sample: float, steps: int, warmup: int, threads: int):
+def cpu_reference(dx_sample: float, steps: int, warmup: int, threads: int, workload: str = "dam3d"):
     """Times the CPU oracle (restatement of the reference's OpenMP path) on the
-    same tank at a coarser lattice; returns pair-interactions/s and details."""
+    same workload (the 3D dam break at a coarser lattice); returns
+    pair-interactions/s and details."""
     from oracle.oracle import OracleDomain
-    dom, dt, info = build_workload(dx_sample)
+    dom, dt, info = build_workload(dx_sample, workload)
     o = OracleDomain(dom.config(dt), dom.particles, initial=True)
     if warmup:
         o.step(warmup, threads)
@@ -197,16 +233,20 @@ def run_reference_arm(args):
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
-    steps = max(1, min(args.steps, 5))
-    r = cpu_reference(args.ref_dx, steps, max(1, min(args.warmup, 1)), threads)
+    wl = WORKLOADS[args.workload]
+    ref_dx = args.ref_dx if args.ref_dx else wl["ref_dx"]
+    steps = max(1, min(args.steps, 5 if args.workload == "dam3d" else 20))
+    r = cpu_reference(ref_dx, steps, max(1, min(args.warmup, 1)), threads, args.workload)
     line = {
-        "impl": "reference", "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": args.gpus,
+        "impl": "reference", "metric": metric_name(args.workload), "value": r["value"], "unit": UNIT,
+        "n_gpus": args.gpus,
         "steps": steps, "warmup": 1, "ms_per_step": 1e3 * r["seconds"] / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic lattice (seeded)",
-        "config": {"workload": f"3D dam break, tank 3.22x1.0x1.0 m, column 1.2x0.55x1.0 m, sample dx={args.ref_dx} m",
+        "config": {"workload": "sample of the " + wl["desc"] % ref_dx,
                    "particles": r["n"], "fluid": r["n_fluid"], "pairs_per_step": r["pairs_per_step"]},
         "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{steps} steps of the 3D dam break at dx={args.ref_dx} m ({r['n']} particles)"},
+                         "sample": f"{steps} steps of the {args.workload} workload at dx={ref_dx} m "
+                                   f"({r['n']} particles)"},
         "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "steps_per_s": r["steps_per_s"],
     }
@@ -220,8 +260,9 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--dx", type=float, default=0.005)
-    ap.add_argument("--ref-dx", type=float, default=0.01)
+    ap.add_argument("--workload", default="dam3d", choices=sorted(WORKLOADS))
+    ap.add_argument("--dx", type=float, default=None, help="lattice spacing (default: the workload's)")
+    ap.add_argument("--ref-dx", type=float, default=None, help="lattice spacing of the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched granular-column line")
     ap.add_argument("--tuning", default="auto",
@@ -230,6 +271,8 @@ def main():
     ap.add_argument("--ens-dx", type=float, default=1e-3)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.dx is None:
+        args.dx = WORKLOADS[args.workload]["dx"]
 
     if args.impl == "reference":
         return run_reference_arm(args)
@@ -248,7 +291,8 @@ def main():
     from persiansph_gb300 import abi
     import ctypes
 
-    dom, dt, info = build_workload(args.dx)
+    wl = WORKLOADS[args.workload]
+    dom, dt, info = build_workload(args.dx, args.workload)
     n = dom.particles.n
     from persiansph_gb300.closure import ClosureNet, default_network_path
     net = ClosureNet.load(default_network_path())
@@ -300,7 +344,7 @@ def main():
                 "clocks": clk.summary(), "value_rank": pairs / (ms * 1e-3), "steps_per_s": done / (ms * 1e-3),
                 "pairs_per_step": pairs / max(done, 1)}
 
-    m32 = measure(1, closure=True)  # PSPH_FP32C + learned closure: the headline form
+    m32 = measure(1, closure=wl["closure"])  # PSPH_FP32C + learned closure: the headline form
     m32n = measure(1)                # PSPH_FP32C without the closure (LES off)
     m64 = measure(0)                 # PSPH_FP64: the plain form
     lib = abi.load_library()
@@ -316,7 +360,7 @@ def main():
     # end to end through the C ABI with host buffers: upload + K steps + download
     fields = ("x", "v", "density", "pressure", "a", "ddensity")
     t0 = time.perf_counter()
-    _, ge = open_domain(1, True)
+    _, ge = open_domain(1, wl["closure"])
     done_e = ge.step(args.steps)
     out = ge.download_fields(fields)
     torch.cuda.synchronize()
@@ -331,16 +375,18 @@ def main():
 
     world_mult = world
     line = {
-        "metric": METRIC, "value": m32["value_rank"] * world_mult, "unit": UNIT, "n_gpus": world,
+        "metric": metric_name(args.workload), "value": m32["value_rank"] * world_mult, "unit": UNIT,
+        "n_gpus": world,
         "steps": m32["done"], "warmup": args.warmup, "ms_per_step": m32["ms"] / max(m32["done"], 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 pair arithmetic (Kahan-compensated sums), f64 integration",
         "data": "synthetic lattice (seeded); inputs larger than L2 (no flush needed)",
-        "config": {"workload": "3D dam break: tank 3.22x1.0x1.0 m, column 1.2x0.55x1.0 m, dx=%g m" % args.dx,
-                   "particles": n, "fluid": info["n_fluid"], "walls": info["n_wall"], "kernel": "Wendland C2",
-                   "h_over_dx": 1.3, "eos": "Tait c0=40", "scheme": "Modified Verlet + Shepard",
-                   "form": "FP32C + learned eddy-viscosity closure (LES on every fluid particle)", "parallelism": "replicas only" if world > 1 else "single GPU",
-                   "l2": "working set > L2"},
+        "config": {"workload": wl["desc"] % args.dx, "particles": n, "fluid": info.get("n_fluid"),
+                   "walls": info.get("n_wall"),
+                   "form": ("FP32C + learned eddy-viscosity closure (LES on every fluid particle)" if wl["closure"]
+                            else "FP32C"),
+                   "parallelism": "replicas only" if world > 1 else "single GPU",
+                   "l2": "working set > L2" if n * 300 > 129e6 else "working set fits in L2"},
         "steps_per_s": m32["steps_per_s"], "pairs_per_step": m32["pairs_per_step"], "tuning": m32["tuning"],
         "phase_ms": phase_dict(m32),
         "closure": {"evaluated": m32["closure_evaluated"], "fallbacks": m32["closure_fallbacks"],
@@ -366,13 +412,16 @@ def main():
                 "note": "create + upload + steps + download through the C ABI, host wall clock"},
         "gpu_launches": m32["launches"],
     }
-    if not args.no_ensemble:
+    if not args.no_ensemble and args.workload == "dam3d":
         line["ensemble"] = measure_ensemble(args.ens_n, args.ens_dx, max(args.steps // 2, 5), args.warmup)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        r = cpu_reference(args.ref_dx, 2, 1, threads)
+        ref_dx = args.ref_dx if args.ref_dx else wl["ref_dx"]
+        cpu_steps = 2 if args.workload == "dam3d" else 10
+        r = cpu_reference(ref_dx, cpu_steps, 1, threads, args.workload)
         line["cpu_baseline"] = {"value": r["value"], "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": f"2 steps of the same 3D dam break at dx={args.ref_dx} m "
+                                "steps_per_s": r["steps_per_s"],
+                                "sample": f"{cpu_steps} steps of the same workload ({args.workload}) at dx={ref_dx} m "
                                           f"({r['n']} particles) after 1 warm-up step"}
     if rank == 0:
         print(json.dumps(line))

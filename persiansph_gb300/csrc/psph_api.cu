@@ -366,6 +366,9 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
   std::vector<int> cls(ntot);
   std::vector<double> pressure(ntot);
   std::unordered_map<std::string, int, ClassKeyHash> index;
+  PClass last_cls;
+  std::memset(&last_cls, 0, sizeof last_cls);
+  int last_id = -1;
   int material0 = -1;
   for (int q = 0; q < ninst; ++q) {
     const psph_particles* p = &parts[q];
@@ -416,16 +419,24 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
       if (C.material != material0)
         return set_err(c, PSPH_ERR_UNSUPPORTED,
                        "particles of different materials interact through CalcForce12/13 (FSI, seepage), outside this build");
-      std::string key((const char*)&C, sizeof C);
-      auto it = index.find(key);
       int id;
-      if (it == index.end()) {
-        id = (int)c->classes.size();
-        if (id >= 65535) return set_err(c, PSPH_ERR_UNSUPPORTED, "more than 65535 distinct particle parameter sets");
-        index.emplace(key, id);
-        c->classes.push_back(C);
+      // consecutive particles mostly share their parameters: compare with the
+      // previous particle's before building and hashing the key
+      if (last_id >= 0 && std::memcmp(&C, &last_cls, sizeof C) == 0) {
+        id = last_id;
       } else {
-        id = it->second;
+        std::string key((const char*)&C, sizeof C);
+        auto it = index.find(key);
+        if (it == index.end()) {
+          id = (int)c->classes.size();
+          if (id >= 65535) return set_err(c, PSPH_ERR_UNSUPPORTED, "more than 65535 distinct particle parameter sets");
+          index.emplace(key, id);
+          c->classes.push_back(C);
+        } else {
+          id = it->second;
+        }
+        last_id = id;
+        last_cls = C;
       }
       const int64_t g = c->inst_off[q] + i;
       cls[g] = id;
@@ -651,6 +662,21 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
     CUDA_TRY(c, cudaMemcpy(c->PA.orig, orig.data(), N * sizeof(int), cudaMemcpyHostToDevice));
     if (dyn_mu) CUDA_TRY(c, cudaMemcpy(c->PA.mu, mu.data(), N * sizeof(double), cudaMemcpyHostToDevice));
     if (o.has_solid) {
+      // Mat3 neither reads nor writes the ShearStress history: a soil domain
+      // whose uploaded history is zero does not carry it through the sort
+      o.carry_shear_h = 1;
+      if (o.soil_pairs) {
+        o.carry_shear_h = 0;
+        for (int q = 0; q < ninst && !o.carry_shear_h; ++q) {
+          const double* hs = lf ? parts[q].shear_stressa : parts[q].shear_stressb;
+          if (hs)
+            for (size_t e = 0; e < 9 * (size_t)parts[q].n; ++e)
+              if (hs[e] != 0.0) {
+                o.carry_shear_h = 1;
+                break;
+              }
+        }
+      }
       for (int q = 0; q < ninst; ++q) {
         const psph_particles* p = &parts[q];
         const double* srcs[7] = {p->sigma, lf ? p->sigmaa : p->sigmab, p->strain, lf ? p->straina : p->strainb,
@@ -666,6 +692,9 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
     std::vector<uint8_t> alive(N, 1);
     CUDA_TRY(c, cudaMemcpy(c->d_alive, alive.data(), N, cudaMemcpyHostToDevice));
     CUDA_TRY(c, cudaMemcpy(c->d_cls, c->classes.data(), c->classes.size() * sizeof(PClass), cudaMemcpyHostToDevice));
+    launch_class_constants(c->d_cls, (int)c->classes.size(), o.dim, c->stream);
+    CUDA_TRY(c, cudaGetLastError());
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     CUDA_TRY(c, cudaMemcpy(c->d_grids, c->gdevs.data(), ninst * sizeof(GridDev), cudaMemcpyHostToDevice));
     std::vector<InstState> is(ninst);
     for (int q = 0; q < ninst; ++q) {

@@ -35,6 +35,10 @@ enum : uint32_t {
 struct PClass {
   double cs, p0, rho0, fpmassc, alpha, beta, mu0, mu_ref, t0, bm, csmag, ti, tin, tid;
   double g_mod, k_mod, sigmay, coh, phi, psi, h, mass;
+  // Drucker-Prager constants of the class (alpha, k_f, sin psi), derived on the
+  // device once after upload with the same expressions the return mapping
+  // used per particle (zero while the table is built on the host)
+  double dp_alpha, dp_kf, dp_sin_psi;
   int material, is_free, no_slip, pres_eq, shepard, les, vis_m, fail, id, inst;
 };
 

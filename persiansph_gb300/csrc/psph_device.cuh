@@ -83,6 +83,7 @@ struct Options {
   int eos_cls;        // that class
   int dyn_mu;
   int soil_pairs;     // Material 3 (soil-soil walls take the partner's density)
+  int carry_shear_h;  // the sort moves the ShearStress history (Mat2, or a non-zero upload)
   int uniform_h;      // every particle has the same h
   int any_periodic;   // some instance has a periodic axis
   int uniform_mu;     // every free particle has the same constant viscosity
@@ -136,6 +137,7 @@ void launch_begin(const DevView& v, cudaStream_t st);     // stop test, first-st
 void launch_end(const DevView& v, cudaStream_t st);       // time, counters
 void launch_closure(const DevView& v, cudaStream_t st);   // learned eddy viscosity (tcgen05 MLP)
 int forces_blocks(int ncap);
+void launch_class_constants(PClass* cls, int n, int dim, cudaStream_t st);  // derived class constants, once per upload
 int launches_per_step(const DevView& v);
 void launch_pairs_export(const DevView& v, int which, long long* out, long long cap, unsigned long long* counter,
                          cudaStream_t st);

@@ -30,6 +30,30 @@ template <int DIM>
 PSPH_D void tensile_tir(const double* S, double TI, double rho, double* TIR) {
   // Source/Domain.cpp:958-976 (2D); 3D via a Jacobi eigen-decomposition
   // (the reference uses GSL's symmetric eigensolver, :979-987).
+  // No principal stress in tension (the usual state of a soil column): the
+  // reference's R diag(0) R^T is zero. The bound is conservative by 1e-12 of
+  // the stress scale, far above the rounding of either eigen-decomposition,
+  // and skips the FP64 trigonometry or Jacobi sweeps for these particles.
+  {
+    double bound, scale;
+    if (DIM == 2) {
+      const double m = 0.5 * (S[0] + S[4]), d = 0.5 * (S[0] - S[4]);
+      bound = m + sqrt(d * d + S[1] * S[1]);  // the larger in-plane eigenvalue
+      scale = fabs(S[0]) + fabs(S[4]) + fabs(S[1]);
+    } else {  // Gershgorin: every eigenvalue is below the largest row bound
+      const double r0 = S[0] + fabs(S[1]) + fabs(S[2]);
+      const double r1 = S[4] + fabs(S[3]) + fabs(S[5]);
+      const double r2 = S[8] + fabs(S[6]) + fabs(S[7]);
+      bound = fmax(r0, fmax(r1, r2));
+      scale = fabs(S[0]) + fabs(S[4]) + fabs(S[8]) + fabs(S[1]) + fabs(S[2]) + fabs(S[5]);
+    }
+    if (bound < -1e-12 * scale) {
+      if (DIM == 2) TIR[0] = TIR[1] = TIR[3] = TIR[4] = 0.0;  // the entries the 2D rotation writes
+      else
+        for (int e = 0; e < 9; ++e) TIR[e] = 0.0;
+      return;
+    }
+  }
   if (DIM == 2) {
     double teta;
     if ((S[0] - S[4]) != 0.0) teta = 0.5 * atan(2.0 * S[1] / (S[0] - S[4]));

@@ -22,9 +22,7 @@ namespace {
 
 constexpr int kFT32 = 128;  // block size of the copy and wall-interpolation kernels
 // The pair kernels take their block size at launch (Options::pair_block, 64 to
-// 256 threads, picked by psph_autotune); the specialised fluid kernels are
-// capped at 96 registers (20 resident warps per SM at 128- or 64-thread
-// blocks), the general ones at 128.
+// 256 threads, picked by psph_autotune); register caps are set per kernel.
 constexpr int kMaxPairBlock = 256;
 constexpr int kQ32 = 16;  // queued wall-interpolation partners per lane
 
@@ -251,8 +249,11 @@ __global__ void __launch_bounds__(kFT32) prepare32_kernel(DevView v) {
 // strain-rate sums of the LES / Bingham options. The list walk is a counted
 // loop so that the next neighbour's loads can be issued before this one's
 // arithmetic.
+// Register caps measured on the 6.7M-particle dam break: the strain-rate
+// flavour runs best at 96 (20 warps/SM), the plain one at 72 (28 warps/SM,
+// a few spilled values in L1), the general one at 128.
 template <int DIM, int KT, int FL>
-__global__ void __maxnreg__(FL == 0 ? 128 : 96) forces_fluid32_kernel(DevView v) {
+__global__ void __maxnreg__(FL == 0 ? 128 : (FL == 1 ? 72 : 96)) forces_fluid32_kernel(DevView v) {
   constexpr bool SPEC = FL != 0;
   __shared__ double red[32];
   __shared__ unsigned long long cred[32];
@@ -304,6 +305,8 @@ __global__ void __maxnreg__(FL == 0 ? 128 : 96) forces_fluid32_kernel(DevView v)
   int nnb = 0;
   const bool closure = o.closure && (fi & CF_LES);
   const float cf2 = (float)(g.cellfac * g.cellfac);
+  const bool uniform_h = o.uniform_h;
+  const float ih_u = (float)o.inv_h;
   auto pair = [&](const int j, const int code) {
     const float4 oj = v.S.OFF32[j];
     float x0, x1, x2;
@@ -317,7 +320,8 @@ __global__ void __maxnreg__(FL == 0 ? 128 : 96) forces_fluid32_kernel(DevView v)
     const bool fj = fjf & CF_FREE;
     npair2 += fj ? 1ull : 2ull;
     ++nnb;
-    const float ih = 1.f / hb;
+    // FP32C divisions use the hardware reciprocal (2 ulp; the form's bound is 1e-5)
+    const float ih = uniform_h ? ih_u : __fdividef(1.f, hb);
     const float inv_r = (r2 > 0.f) ? rsqrtf(r2) : 0.f;
     const float q = r2 * inv_r * ih;
     const float inv_q = hb * inv_r;
@@ -337,7 +341,7 @@ __global__ void __maxnreg__(FL == 0 ? 128 : 96) forces_fluid32_kernel(DevView v)
     if ((Alpha != 0.f || Beta != 0.f) && vx < 0.f) {
       const float D = r2 + 0.01f * hb * hb;
       const float t = hb * vx;
-      PI = t * (-Alpha * 0.5f * (ci_snd + cj_snd) * D + Beta * t) / (D * D * (0.5f * (di + dj)));
+      PI = __fdividef(t * (-Alpha * 0.5f * (ci_snd + cj_snd) * D + Beta * t), D * D * (0.5f * (di + dj)));
     }
     float TI = 0.f;
     if (!SPEC && ((fi | fjf) & CF_TI)) {
@@ -357,7 +361,7 @@ __global__ void __maxnreg__(FL == 0 ? 128 : 96) forces_fluid32_kernel(DevView v)
         if (uniform_mu) Mu = mu_u;
         else {
           const float muj = dyn_mu ? v.S.MU32[j] : Cj.mu0;
-          Mu = 2.f * mui * muj / (mui + muj);
+          Mu = __fdividef(2.f * mui * muj, mui + muj);
         }
       } else {
         const float4 ns = v.S.NSV32[j];
@@ -562,6 +566,7 @@ __global__ void __maxnreg__(128) forces_solid32_kernel(DevView v) {
   float zw = 0.f, sd = 0.f, xs0 = 0.f, xs1 = 0.f, xs2 = 0.f;
   float sr0 = 0.f, sr1 = 0.f, sr2 = 0.f, sr3 = 0.f, sr4 = 0.f, sr5 = 0.f;  // 00 01 02 11 12 22
   float rr0 = 0.f, rr1 = 0.f, rr2 = 0.f;                                  // 01 02 12
+  const float cf2 = (float)(g.cellfac * g.cellfac);
   NbrSource<DIM> src;
   src.init(v, g, i, active && cell >= 0, 1.0f);
   while (true) {
@@ -571,13 +576,14 @@ __global__ void __maxnreg__(128) forces_solid32_kernel(DevView v) {
     const float4 oj = v.S.OFF32[j];
     float x0, x1, x2;
     rel_pos<DIM>(cs, oi, oj, code, x0, x1, x2);
+    const float hb = 0.5f * (hi + oj.w);
+    const float r2 = x0 * x0 + x1 * x1 + x2 * x2;
+    if (r2 > cf2 * hb * hb) continue;  // the support test (the list holds a margin)
     const PClass32& Cj = CT[P.cls[j]];
     const int fjf = Cj.flags;
     const bool fj = fjf & CF_FREE;
     npair2 += fj ? 1ull : 2ull;
-    const float hb = 0.5f * (hi + oj.w);
     const float ih = 1.f / hb;
-    const float r2 = x0 * x0 + x1 * x1 + x2 * x2;
     const float inv_r = (r2 > 0.f) ? rsqrtf(r2) : 0.f;
     const float q = r2 * inv_r * ih;
     const float ih2 = ih * ih;

@@ -43,9 +43,10 @@ __device__ __forceinline__ float dsilu(float z) {
   return s * (1.f + z * (1.f - s));
 }
 // SiLU of the tensor-core inference epilogues: hardware exp2 and reciprocal
-// approximations (relative error ~1e-7, far below the BF16 rounding of the
-// activations that follows).
-__device__ __forceinline__ float silu_fast(float z) { return z * __frcp_rn(1.f + __expf(-z)); }
+// approximations (relative error ~1e-6, far below the BF16 rounding of the
+// activations that follows). z is clamped at -80 so 1 + exp(-z) stays a
+// normal float, where the approximate division is defined.
+__device__ __forceinline__ float silu_fast(float z) { return z * __fdividef(1.f, 1.f + __expf(-fmaxf(z, -80.f))); }
 __device__ __forceinline__ float softplus(float z) { return z > 20.f ? z : log1pf(expf(z)); }
 
 // ---------------------------------------------------------------------------

@@ -4,9 +4,9 @@
 // Each particle scans the sorted ranges of its 3x3(x3) cell block once per step
 // (the rows and x-slabs of it that can reach the support) and keeps the
 // candidates inside the kernel support, tested in FP32 on
-// (cell offset, FP32 offset) separations: exactly for the FP32C form, with a
-// 0.4 % margin on r^2 for the FP64 form (whose pair kernel then applies the
-// exact FP64 test). Lists are written in 16-byte chunks of 4 entries, chunk-
+// (cell offset, FP32 offset) separations with a margin on r^2 (0.02 % for the
+// FP32C form, 0.4 % for the FP64 form); the pair kernels then apply the exact
+// test of their form. Lists are written in 16-byte chunks of 4 entries, chunk-
 // major across particles (nl_index), so a warp reading chunk c of 32
 // consecutive particles touches 512 contiguous bytes and each store fills
 // half a sector. The
@@ -22,6 +22,7 @@ constexpr int kNT = 128;
 
 template <int DIM, bool UNIFORM_H>
 __global__ void __launch_bounds__(kNT) nlist_kernel(DevView v, float margin) {
+  __shared__ int4 chunk[kNT];  // each lane's chunk being filled
   const StepScalars* sc = v.sc;
   if (sc->all_stop) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -42,7 +43,7 @@ __global__ void __launch_bounds__(kNT) nlist_kernel(DevView v, float margin) {
   const CellCoord c = decode(g, cell);
   const float4* __restrict__ off = v.S.OFF32;
   int4* __restrict__ out = reinterpret_cast<int4*>(v.S.nl) + i;  // chunk c at out[c * N]
-  int b0 = 0, b1 = 0, b2 = 0, b3 = 0;  // the chunk being filled
+  int* mine = reinterpret_cast<int*>(&chunk[threadIdx.x]);
   // Rows of cells and x-slabs of cells whose nearest point lies outside the
   // support are skipped (cells are sorted slab by slab, xsub slabs along x).
   // The bound assumes the in-cell offset of i lies in [0, cell size), which
@@ -86,36 +87,41 @@ __global__ void __launch_bounds__(kNT) nlist_kernel(DevView v, float margin) {
         else if (x < 0 || x >= g.nc[0]) continue;
         const int s0 = max(slo - dx * xs, 0), s1 = min(shi - dx * xs, xs - 1);
         if (s0 > s1) continue;
-        const int lo = sstart[(base + x) * xs + s0], hi = sstart[(base + x) * xs + s1 + 1];
-        const int code = (dx + 1) + cyz;
-        const float cx = -(float)dx * cs.x;
-#pragma unroll 4
-        for (int j = lo; j < hi; ++j) {
+        int lo = sstart[(base + x) * xs + s0];
+        const int hi = sstart[(base + x) * xs + s1 + 1];
+        const int tag = ((dx + 1) + cyz) << kCodeShift;
+        // i's position relative to this cell's origin: x_i - x_j = a - off_j
+        // (one rounding away from rel_pos's form, which the pair kernels
+        // apply exactly; the list's margin covers the difference)
+        const float ax = oi.x - (float)dx * cs.x, ay = oi.y + cy, az = oi.z + cz;
+        auto visit = [&](int j) {
           const float4 oj = off[j];
-          // x_i - x_j as rel_pos forms it: cell offset + (offset_i - offset_j)
-          const float x0 = cx + (oi.x - oj.x), x1 = cy + (oi.y - oj.y);
-          const float x2 = (DIM == 3) ? cz + (oi.z - oj.z) : 0.f;
+          const float x0 = ax - oj.x, x1 = ay - oj.y, x2 = (DIM == 3) ? az - oj.z : 0.f;
           float thr = thr_u;
           if (!UNIFORM_H) {
             const float hb = 0.5f * (oi.w + oj.w);
             thr = cf * cf * hb * hb * margin;
           }
-          if (x0 * x0 + x1 * x1 + x2 * x2 <= thr && j != i) {
+          if (x0 * x0 + x1 * x1 + x2 * x2 <= thr) {
             if (k < cap) {
-              const int e = j | (code << kCodeShift), m = k & 3;
-              b0 = m == 0 ? e : b0;
-              b1 = m == 1 ? e : b1;
-              b2 = m == 2 ? e : b2;
-              b3 = m == 3 ? e : b3;
-              if (m == 3) out[(size_t)(k >> 2) * N] = make_int4(b0, b1, b2, b3);
+              const int m = k & 3;
+              mine[m] = j | tag;
+              if (m == 3) out[(size_t)(k >> 2) * N] = chunk[threadIdx.x];
             }
             ++k;
           }
+        };
+        if (dx == 0 && dy == 0 && dz == 0 && lo <= i && i < hi) {  // the home cell: skip i itself
+#pragma unroll 4
+          for (int j = lo; j < i; ++j) visit(j);
+          lo = i + 1;
         }
+#pragma unroll 4
+        for (int j = lo; j < hi; ++j) visit(j);
       }
     }
   }
-  if (k <= cap && (k & 3)) out[(size_t)(k >> 2) * N] = make_int4(b0, b1, b2, b3);  // last, partial chunk
+  if (k <= cap && (k & 3)) out[(size_t)(k >> 2) * N] = chunk[threadIdx.x];  // last, partial chunk
   v.S.nl_count[i] = (k <= cap) ? k : -1;
 }
 
@@ -123,7 +129,9 @@ __global__ void __launch_bounds__(kNT) nlist_kernel(DevView v, float margin) {
 
 void launch_nlist(const DevView& v, cudaStream_t st) {
   const int nb = v.ncap > 0 ? (v.ncap + kNT - 1) / kNT : 1;
-  const float margin = v.o.fp32 ? 1.0f : 1.004f;
+  // a superset of the support: the pair kernels apply the exact test (FP32 in
+  // the FP32C form, FP64 in the plain form)
+  const float margin = v.o.fp32 ? 1.0002f : 1.004f;
   const bool uh = v.o.uniform_h;
   if (v.o.dim == 2) {
     if (uh) nlist_kernel<2, true><<<nb, kNT, 0, st>>>(v, margin);

@@ -231,12 +231,16 @@ __global__ void reorder_kernel(DevView v, const int* __restrict__ perm, const in
     alive[s] = 1;
     if (dyn_mu) dst.mu[s] = src.mu[i];
     if (has_solid) {
-      const double* srcs[7] = {src.sigma, src.sigma_h, src.strain, src.strain_h, src.shear, src.shear_h, src.tir};
-      double* dsts[7] = {dst.sigma, dst.sigma_h, dst.strain, dst.strain_h, dst.shear, dst.shear_h, dst.tir};
+      const double* srcs[7] = {src.sigma, src.sigma_h, src.strain, src.strain_h, src.shear, src.tir, src.shear_h};
+      double* dsts[7] = {dst.sigma, dst.sigma_h, dst.strain, dst.strain_h, dst.shear, dst.tir, dst.shear_h};
+      // the ShearStress history serves Mat2 only (a zero history of a soil domain stays behind)
+      const int nt = v.o.carry_shear_h ? 7 : 6;
 #pragma unroll
-      for (int a = 0; a < 7; ++a)
+      for (int a = 0; a < 7; ++a) {
+        if (a >= nt) break;
 #pragma unroll
         for (int e = 0; e < 9; ++e) dsts[a][9 * (size_t)s + e] = srcs[a][9 * (size_t)i + e];
+      }
     }
   }
 }

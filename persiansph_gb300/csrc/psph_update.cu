@@ -74,17 +74,21 @@ PSPH_D void deviator(const double* S, double I1, double* D) {
 // Drucker-Prager return (Source/Particle.cpp:357-425 / :677-746).
 // Sig: elastic predictor (in/out); Sn: stress at the start of the step;
 // fac: dt (leapfrog / restart) or 2 dt (Verlet). Returns the last deviator.
+// Drucker-Prager alpha and k_f: plane strain when I(2,2) == 0 (2D), else
+// the compression-cone fit (Source/Particle.cpp:663-674).
+PSPH_D void dp_constants(double phi, double c, double I22, double* alpha, double* kf) {
+  if (I22 == 0.0) {
+    *alpha = tan(phi) / sqrt(9.0 + 12.0 * tan(phi) * tan(phi));
+    *kf = 3.0 * c / sqrt(9.0 + 12.0 * tan(phi) * tan(phi));
+  } else {
+    *alpha = (2.0 * sin(phi)) / (sqrt(3.0) * (3.0 - sin(phi)));
+    *kf = (6.0 * c * cos(phi)) / (sqrt(3.0) * (3.0 - sin(phi)));
+  }
+}
+
 PSPH_D void dp_return(const PClass& C, double I22, double* Sig, const double* Sn, const double* SR, double I1strain,
                       double fac, double* SS) {
-  double alpha, kf;
-  const double phi = C.phi, c = C.coh;
-  if (I22 == 0.0) {
-    alpha = tan(phi) / sqrt(9.0 + 12.0 * tan(phi) * tan(phi));
-    kf = 3.0 * c / sqrt(9.0 + 12.0 * tan(phi) * tan(phi));
-  } else {
-    alpha = (2.0 * sin(phi)) / (sqrt(3.0) * (3.0 - sin(phi)));
-    kf = (6.0 * c * cos(phi)) / (sqrt(3.0) * (3.0 - sin(phi)));
-  }
+  const double alpha = C.dp_alpha, kf = C.dp_kf;  // dp_constants of the class (class_constants_kernel)
   const double K = C.k_mod, G = C.g_mod;
   double I1 = dp_apex(Sig, alpha, kf);
   deviator(Sig, I1, SS);
@@ -101,8 +105,8 @@ PSPH_D void dp_return(const PClass& C, double I22, double* Sig, const double* Sn
         dL = 1.0 / (9.0 * alpha * alpha * K + G) * ((3.0 * alpha * K * I1strain) + (G / sqrt(J2)) * sum);
         s = 3.0 * alpha * K;
       } else {
-        dL = 1.0 / (9.0 * alpha * K * 3.0 * sin(C.psi) + G) * ((3.0 * alpha * K * I1strain) + (G / sqrt(J2)) * sum);
-        s = 3.0 * 3.0 * sin(C.psi) * K;
+        dL = 1.0 / (9.0 * alpha * K * 3.0 * C.dp_sin_psi + G) * ((3.0 * alpha * K * I1strain) + (G / sqrt(J2)) * sum);
+        s = 3.0 * 3.0 * C.dp_sin_psi * K;
       }
       for (int e = 0; e < 9; ++e) {
         const double Ie = (e == 8) ? I22 : OIe(e);
@@ -356,6 +360,20 @@ void launch_update(const DevView& v, cudaStream_t st) {
 
 // begin, bin, 3 scan, scatter, rank, reorder, finish, neighbour lists, prepare
 // (2 in the FP32C form: copies + walls), forces, dt, update, end
+namespace {
+__global__ void class_constants_kernel(PClass* cls, int n, int dim) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  PClass& C = cls[k];
+  dp_constants(C.phi, C.coh, dim == 2 ? 0.0 : 1.0, &C.dp_alpha, &C.dp_kf);
+  C.dp_sin_psi = sin(C.psi);
+}
+}  // namespace
+
+void launch_class_constants(PClass* cls, int n, int dim, cudaStream_t st) {
+  if (n > 0) class_constants_kernel<<<(n + 127) / 128, 128, 0, st>>>(cls, n, dim);
+}
+
 int launches_per_step(const DevView& v) { return (v.o.fp32 ? 16 : 15) + (v.o.closure ? 1 : 0); }
 
 }  // namespace psph
