@@ -47,15 +47,22 @@ UNIT = "pair-interactions/s"
 # density): counted from forces_fluid_kernel's arithmetic on the taken branches,
 # with an FMA counted as 2 and a division or square root as 1.
 FLOPS_PER_DIRECTED_PAIR = 90
-# algorithmic HBM bytes per particle of one FP32C force-kernel launch: read each
-# particle's inputs once (offset+h 16, v+p 16, 1/rho, p/rho^2, c, rho 16, class
-# 4, cell 4) and write its outputs once (a + drho 32, zwab 8, sumden 8).
-FORCE32_BYTES_PER_PARTICLE = 104
-# DRAM bytes per particle one force-kernel launch actually moved: an ncu
-# capture of the same kernel on the same tank at dx = 10 mm (1,021,104
-# particles), dram__bytes_read.sum + dram__bytes_write.sum per particle; the
-# traffic grows with the particle count, so a full-size launch moves this x n.
-FORCE32_TRAFFIC_BYTES_PER_PARTICLE = 304.6
+# Algorithmic HBM bytes per particle of one FP32C fluid pair-kernel launch:
+# read each particle's inputs once (offset+h 16, v+p 16, 1/rho, p/rho^2, c, rho
+# 16, class 4, cell 4) and write its outputs once (a + drho 32, zwab 8, sumden
+# 8) = 104 B; with LES and the closure also the viscosity (4), the strain rate
+# (72) and the closure's four features (16) = 196 B.
+FORCE32_BYTES_PER_PARTICLE = {False: 104, True: 196}
+# DRAM bytes per particle one launch actually moved: ncu captures of the same
+# kernels on the same tank at dx = 10 mm (1,021,104 particles),
+# dram__bytes_read.sum + dram__bytes_write.sum per particle (LES + closure
+# flavour: 269.46 + 79.33 MB); the traffic grows with the particle count, so
+# a full-size launch moves this x n.
+FORCE32_TRAFFIC_BYTES_PER_PARTICLE = {False: 304.6, True: 341.6}
+# Pipe activity of that launch (LES + closure flavour) and of the FP64 pair
+# kernel in the same capture series (sm__pipe_*_cycles_active, % of peak).
+FORCE32_NCU = {"issue_active": 0.541, "fma_pipe": 0.313, "fp64_pipe": 0.243, "warps_active": 0.298}
+FORCE64_NCU_FP64_PIPE = 0.854
 
 
 def peaks():
@@ -353,9 +360,10 @@ def main():
     pk = peaks()
     force32_ms = m32["phases"]["forces"]
     force64_ms = m64["phases"]["forces"]
-    achieved_gbs = FORCE32_BYTES_PER_PARTICLE * n / (force32_ms * 1e-3) / 1e9
+    cl = bool(wl["closure"])
+    achieved_gbs = FORCE32_BYTES_PER_PARTICLE[cl] * n / (force32_ms * 1e-3) / 1e9
     fp64_tflops = 2 * m64["pairs_per_step"] * FLOPS_PER_DIRECTED_PAIR / (force64_ms * 1e-3) / 1e12
-    traffic = FORCE32_TRAFFIC_BYTES_PER_PARTICLE * n
+    traffic = FORCE32_TRAFFIC_BYTES_PER_PARTICLE[cl] * n
 
     # end to end through the C ABI with host buffers: upload + K steps + download
     fields = ("x", "v", "density", "pressure", "a", "ddensity")
@@ -401,11 +409,17 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved_gbs / pk["hbm_gbs"], "traffic": traffic,
                      "kernel": "forces_fluid32_kernel", "peak_source": pk["src"],
-                     "bytes_per_particle": FORCE32_BYTES_PER_PARTICLE},
+                     "bytes_per_particle": FORCE32_BYTES_PER_PARTICLE[cl],
+                     "note": "latency-bound gather kernel (neither HBM nor tensor bound); ncu pipe activity of "
+                             "the same kernel at dx=10 mm in ncu_small_case",
+                     "ncu_small_case": FORCE32_NCU},
         "roofline_fp64": {"bound": "fp64", "kernel": "forces_fluid_kernel", "achieved": fp64_tflops,
                           "peak": fp64.value, "unit": "TFLOP/s",
                           "frac": fp64_tflops / fp64.value if fp64.value else None,
-                          "peak_source": "measured here by psph_probe_fp64_peak (DFMA chains)"},
+                          "peak_source": "measured here by psph_probe_fp64_peak (DFMA chains)",
+                          "fp64_pipe_active_ncu_small_case": FORCE64_NCU_FP64_PIPE,
+                          "note": "frac counts 90 algorithmic FP64 flops per directed pair against the DFMA rate; "
+                                  "the FP64 pipe itself is 85 % busy (sqrt, divisions, conversions)"},
         "clocks": m32["clocks"],
         "e2e": {"value": pe / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d / max(done_e, 1),
                 "d2h_bytes_per_step": d2h / max(done_e, 1), "steps": done_e,
