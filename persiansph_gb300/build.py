@@ -65,7 +65,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=(), out_dir=No
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = lib_path + ".tmp"
-    cmd = [nv, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
+    cmd = [nv, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lpthread"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stderr}")

@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -338,6 +339,25 @@ psph_status create_impl(const psph_config* cfgs, int ninst, psph_ctx** out) {
   return PSPH_OK;
 }
 
+// Threads for the per-particle host loops of an upload (one per ~200k
+// particles, at most the hardware's).
+int host_threads(int64_t n) {
+  const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+  return (int)std::max<int64_t>(1, std::min<int64_t>(hw, n / 200000 + 1));
+}
+
+template <class F>
+void run_threads(int n, F&& f) {
+  if (n <= 1) {
+    f(0);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (int t = 1; t < n; ++t) th.emplace_back(f, t);
+  f(0);
+  for (auto& x : th) x.join();
+}
+
 psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
   if (!c || !parts) return PSPH_ERR_INVALID_ARGUMENT;
   if (c->uploaded) return set_err(c, PSPH_ERR_STATE, "particles already uploaded to this context");
@@ -359,20 +379,48 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
   c->inst_off[ninst] = ntot;
 
   // ---- particle classes (per instance) and initial pressure -------------------
+  // Host work over every particle, split across threads: each thread
+  // de-duplicates the parameter sets of its contiguous chunk; the chunks'
+  // tables merge in chunk order, so class ids do not depend on scheduling.
   bool dyn_mu = false;
-  for (int q = 0; q < ninst; ++q)
+  for (int q = 0; q < ninst && !dyn_mu; ++q)
     for (int64_t i = 0; i < parts[q].n; ++i)
-      if (dflt(parts[q].t0, i, 0.0) > 0.0 || iflt(parts[q].les, i, 0)) dyn_mu = true;
+      if (dflt(parts[q].t0, i, 0.0) > 0.0 || iflt(parts[q].les, i, 0)) {
+        dyn_mu = true;
+        break;
+      }
   std::vector<int> cls(ntot);
   std::vector<double> pressure(ntot);
-  std::unordered_map<std::string, int, ClassKeyHash> index;
-  PClass last_cls;
-  std::memset(&last_cls, 0, sizeof last_cls);
-  int last_id = -1;
-  int material0 = -1;
-  for (int q = 0; q < ninst; ++q) {
-    const psph_particles* p = &parts[q];
-    for (int64_t i = 0; i < p->n; ++i) {
+  struct Worker {
+    std::vector<PClass> classes;
+    std::unordered_map<std::string, int, ClassKeyHash> index;
+    int material = -1;
+    bool mixed = false;
+    int64_t err_at = -1;
+    psph_status err = PSPH_OK;
+    char msg[160] = {0};
+  };
+  const int nthreads = host_threads(ntot);
+  std::vector<Worker> workers(nthreads);
+  auto work = [&](int t) {
+    Worker& W = workers[t];
+    const int64_t g0 = ntot * t / nthreads, g1 = ntot * (t + 1) / nthreads;
+    PClass last;
+    std::memset(&last, 0, sizeof last);
+    int last_id = -1;
+    int q = 0;
+    while (q + 1 < ninst && g0 >= c->inst_off[q + 1]) ++q;
+    for (int64_t g = g0; g < g1; ++g) {
+      while (g >= c->inst_off[q + 1]) ++q;  // the instance of particle g
+      const psph_particles* p = &parts[q];
+      const int64_t i = g - c->inst_off[q];
+#define FAIL(code, ...)                                   \
+  do {                                                    \
+    W.err = code;                                         \
+    W.err_at = g;                                         \
+    std::snprintf(W.msg, sizeof W.msg, __VA_ARGS__);      \
+    return;                                               \
+  } while (0)
       PClass C;
       std::memset(&C, 0, sizeof C);
       C.cs = dflt(p->cs, i, 0.0);
@@ -408,41 +456,70 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
       C.id = iflt(p->id, i, 0);
       C.inst = q;
       if (C.material < 1 || C.material > 3)
-        return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Material Type No is out of range (particle %lld)", (long long)i);
+        FAIL(PSPH_ERR_INVALID_ARGUMENT, "Material Type No is out of range (particle %lld)", (long long)i);
       if (C.pres_eq < 0 || C.pres_eq > 2)
-        return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Please correct Pressure Equation No (particle %lld)", (long long)i);
-      if (C.material == 2 && C.fail > 1) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Undefined failure criteria for solids");
-      if (C.material == 3 && C.fail > 3) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Failure Type No is out of range");
+        FAIL(PSPH_ERR_INVALID_ARGUMENT, "Please correct Pressure Equation No (particle %lld)", (long long)i);
+      if (C.material == 2 && C.fail > 1) FAIL(PSPH_ERR_INVALID_ARGUMENT, "Undefined failure criteria for solids");
+      if (C.material == 3 && C.fail > 3) FAIL(PSPH_ERR_INVALID_ARGUMENT, "Failure Type No is out of range");
       if (C.material == 1 && C.t0 > 0.0 && C.vis_m > 1)
-        return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Non-Newtonian Viscosity Type No is out of range");
-      if (material0 < 0) material0 = C.material;
-      if (C.material != material0)
-        return set_err(c, PSPH_ERR_UNSUPPORTED,
-                       "particles of different materials interact through CalcForce12/13 (FSI, seepage), outside this build");
+        FAIL(PSPH_ERR_INVALID_ARGUMENT, "Non-Newtonian Viscosity Type No is out of range");
+      if (W.material < 0) W.material = C.material;
+      if (C.material != W.material) W.mixed = true;
+#undef FAIL
       int id;
       // consecutive particles mostly share their parameters: compare with the
       // previous particle's before building and hashing the key
-      if (last_id >= 0 && std::memcmp(&C, &last_cls, sizeof C) == 0) {
+      if (last_id >= 0 && std::memcmp(&C, &last, sizeof C) == 0) {
         id = last_id;
       } else {
         std::string key((const char*)&C, sizeof C);
-        auto it = index.find(key);
-        if (it == index.end()) {
-          id = (int)c->classes.size();
-          if (id >= 65535) return set_err(c, PSPH_ERR_UNSUPPORTED, "more than 65535 distinct particle parameter sets");
-          index.emplace(key, id);
-          c->classes.push_back(C);
+        auto it = W.index.find(key);
+        if (it == W.index.end()) {
+          id = (int)W.classes.size();
+          W.index.emplace(key, id);
+          W.classes.push_back(C);
         } else {
           id = it->second;
         }
         last_id = id;
-        last_cls = C;
+        last = C;
       }
-      const int64_t g = c->inst_off[q] + i;
-      cls[g] = id;
+      cls[g] = id;  // local to the chunk until the merge below
       // InitialChecks: initial pressure from the EOS for fluids and solids (Source/Domain.cpp:1675-1677)
       const double p_in = dflt(p->pressure, i, 0.0);
       pressure[g] = (initial && C.material < 3) ? eos_host(C.pres_eq, C.cs, C.p0, p->density[i], C.rho0) : p_in;
+    }
+  };
+  run_threads(nthreads, work);
+  int material0 = -1;
+  {
+    std::unordered_map<std::string, int, ClassKeyHash> index;
+    for (int t = 0; t < nthreads; ++t) {
+      const Worker& W = workers[t];
+      if (W.err) return set_err(c, W.err, "%s", W.msg);
+      if (W.material >= 0) {
+        if (material0 < 0) material0 = W.material;
+        if (W.mixed || W.material != material0)
+          return set_err(c, PSPH_ERR_UNSUPPORTED,
+                         "particles of different materials interact through CalcForce12/13 (FSI, seepage), outside "
+                         "this build");
+      }
+      std::vector<int> remap(W.classes.size());
+      for (size_t k = 0; k < W.classes.size(); ++k) {
+        std::string key((const char*)&W.classes[k], sizeof(PClass));
+        auto it = index.find(key);
+        if (it == index.end()) {
+          const int id = (int)c->classes.size();
+          if (id >= 65535) return set_err(c, PSPH_ERR_UNSUPPORTED, "more than 65535 distinct particle parameter sets");
+          index.emplace(key, id);
+          c->classes.push_back(W.classes[k]);
+          remap[k] = id;
+        } else {
+          remap[k] = it->second;
+        }
+      }
+      const int64_t g0 = ntot * t / nthreads, g1 = ntot * (t + 1) / nthreads;
+      for (int64_t g = g0; g < g1; ++g) cls[g] = remap[cls[g]];
     }
   }
 
@@ -632,10 +709,15 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
     std::vector<int> orig(N);
     std::vector<double> mu(dyn_mu ? N : 0);
     const bool two_d = (k.dimension == 2);
-    for (int q = 0; q < ninst; ++q) {
-      const psph_particles* p = &parts[q];
-      for (int64_t i = 0; i < p->n; ++i) {
-        const int64_t g = c->inst_off[q] + i;
+    const int nthreads_pack = host_threads(ntot);
+    run_threads(nthreads_pack, [&](int t) {
+      const int64_t g0 = ntot * t / nthreads_pack, g1 = ntot * (t + 1) / nthreads_pack;
+      int q = 0;
+      while (q + 1 < ninst && g0 >= c->inst_off[q + 1]) ++q;
+      for (int64_t g = g0; g < g1; ++g) {
+        while (g >= c->inst_off[q + 1]) ++q;
+        const psph_particles* p = &parts[q];
+        const int64_t i = g - c->inst_off[q];
         const double* x = p->x + 3 * i;
         const double vx = dflt(p->v, 3 * i, 0.0), vy = dflt(p->v, 3 * i + 1, 0.0),
                      vz = two_d ? 0.0 : dflt(p->v, 3 * i + 2, 0.0);
@@ -653,7 +735,7 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
         orig[g] = (int)g;
         if (dyn_mu) mu[g] = dflt(p->mu, i, 0.0);
       }
-    }
+    });
     CUDA_TRY(c, cudaMemcpy(c->PA.X4, X.data(), N * sizeof(double4_32a), cudaMemcpyHostToDevice));
     CUDA_TRY(c, cudaMemcpy(c->PA.V4, V.data(), N * sizeof(double4_32a), cudaMemcpyHostToDevice));
     CUDA_TRY(c, cudaMemcpy(c->PA.H4, H.data(), N * sizeof(double4_32a), cudaMemcpyHostToDevice));
@@ -766,12 +848,13 @@ psph_status step_impl(psph_ctx* c, int64_t nsteps, const double* t_stop, double 
     for (int q = 0; q < c->ninst; ++q) steps_done[q] = c->h_inst[q].steps - steps0[q];
   c->last_launches = launched;
   const uint32_t status = c->h_sc->status;
+  // the root cause first: a non-finite state also throws particles off the grid
+  if (status & ST_NONFINITE) return set_err(c, PSPH_ERR_NONFINITE, "non-finite acceleration or density rate");
   if (status & ST_DT_COLLAPSE)
     return set_err(c, PSPH_ERR_DT_COLLAPSE,
                    "Too small time step, please choose a smaller time step initially to make the simulation more stable");
   if (status & ST_OUT_OF_GRID)
     return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "a particle lies more than hmax outside the cell grid");
-  if (status & ST_NONFINITE) return set_err(c, PSPH_ERR_NONFINITE, "non-finite acceleration or density rate");
   return PSPH_OK;
 }
 
@@ -791,11 +874,16 @@ psph_status alive_of(psph_ctx* c, int q, std::vector<std::pair<int, int>>& order
     cls_out->resize(n);
     CUDA_TRY(c, cudaMemcpy(cls_out->data(), P.cls, n * sizeof(int), cudaMemcpyDeviceToHost));
   }
+  // original indices are unique: place each alive slot at its original index
+  // (a counting sort, linear in n) instead of sorting the pairs
   const int64_t lo = c->inst_off[q], hi = c->inst_off[q + 1];
-  order.clear();
+  std::vector<int> slot_of((size_t)(hi - lo), -1);
   for (size_t s = 0; s < n; ++s)
-    if (alive[s] && orig[s] >= lo && orig[s] < hi) order.emplace_back(orig[s], (int)s);
-  std::sort(order.begin(), order.end());
+    if (alive[s] && orig[s] >= lo && orig[s] < hi) slot_of[(size_t)(orig[s] - lo)] = (int)s;
+  order.clear();
+  order.reserve(slot_of.size());
+  for (size_t k = 0; k < slot_of.size(); ++k)
+    if (slot_of[k] >= 0) order.emplace_back((int)(lo + (int64_t)k), slot_of[k]);
   return PSPH_OK;
 }
 
@@ -826,16 +914,19 @@ psph_status download_impl(psph_ctx* c, int q, psph_particles* out) {
     return PSPH_OK;
   };
   std::vector<double4_32a> b4;
+  const int nth = host_threads(m);
   auto put4 = [&](double* vec3, double* scal) {
-    for (int64_t r = 0; r < m; ++r) {
-      const double4_32a w = b4[order[r].second];
-      if (vec3) {
-        vec3[3 * r] = w.x;
-        vec3[3 * r + 1] = w.y;
-        vec3[3 * r + 2] = w.z;
+    run_threads(nth, [&](int t) {
+      for (int64_t r = m * t / nth; r < m * (t + 1) / nth; ++r) {
+        const double4_32a w = b4[order[r].second];
+        if (vec3) {
+          vec3[3 * r] = w.x;
+          vec3[3 * r + 1] = w.y;
+          vec3[3 * r + 2] = w.z;
+        }
+        if (scal) scal[r] = w.w;
       }
-      if (scal) scal[r] = w.w;
-    }
+    });
   };
   if (out->x || out->density) { if ((st = fetch4(P.X4, b4))) return st; put4(out->x, out->density); }
   if (out->v || out->pressure) { if ((st = fetch4(P.V4, b4))) return st; put4(out->v, out->pressure); }
@@ -850,8 +941,10 @@ psph_status download_impl(psph_ctx* c, int q, psph_particles* out) {
   if (out->vxsph) { if ((st = fetch4(c->S.vxsph4, b4))) return st; put4(out->vxsph, nullptr); }
   std::vector<double> b;
   auto put = [&](double* dst, size_t per) {
-    for (int64_t r = 0; r < m; ++r)
-      for (size_t e = 0; e < per; ++e) dst[per * r + e] = b[per * order[r].second + e];
+    run_threads(nth, [&](int t) {
+      for (int64_t r = m * t / nth; r < m * (t + 1) / nth; ++r)
+        for (size_t e = 0; e < per; ++e) dst[per * r + e] = b[per * order[r].second + e];
+    });
   };
   struct Src { double* out; const double* dev; size_t per; };
   const Src fields[] = {
