@@ -21,7 +21,7 @@ namespace {
 constexpr int kNT = 128;
 
 template <int DIM, bool UNIFORM_H>
-__global__ void __launch_bounds__(kNT) nlist_kernel(DevView v, float margin) {
+__global__ void __launch_bounds__(kNT, 8) nlist_kernel(DevView v, float margin) {
   __shared__ int4 chunk[kNT];  // each lane's chunk being filled
   const StepScalars* sc = v.sc;
   if (sc->all_stop) return;
@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(kNT) nlist_kernel(DevView v, float margin) {
   const int N = v.ncap, cap = v.o.nl_cap;
   const CellCoord c = decode(g, cell);
   const float4* __restrict__ off = v.S.OFF32;
-  int4* __restrict__ out = reinterpret_cast<int4*>(v.S.nl) + i;  // chunk c at out[c * N]
+  int4* __restrict__ out = reinterpret_cast<int4*>(v.S.nl) + i;  // the next chunk to fill; chunk c at nl + c * N + i
   int* mine = reinterpret_cast<int*>(&chunk[threadIdx.x]);
   // Rows of cells and x-slabs of cells whose nearest point lies outside the
   // support are skipped (cells are sorted slab by slab, xsub slabs along x).
@@ -102,13 +102,15 @@ __global__ void __launch_bounds__(kNT) nlist_kernel(DevView v, float margin) {
             const float hb = 0.5f * (oi.w + oj.w);
             thr = cf * cf * hb * hb * margin;
           }
-          if (x0 * x0 + x1 * x1 + x2 * x2 <= thr) {
-            if (k < cap) {
-              const int m = k & 3;
-              mine[m] = j | tag;
-              if (m == 3) out[(size_t)(k >> 2) * N] = chunk[threadIdx.x];
-            }
-            ++k;
+          // branch-free push: the slot k & 3 is written for every candidate
+          // and kept only when the candidate is inside (k advances); a full
+          // chunk goes out as one 16-byte store while the list fits its cap
+          const bool in = x0 * x0 + x1 * x1 + x2 * x2 <= thr;
+          mine[k & 3] = j | tag;
+          k += in ? 1 : 0;
+          if (in && (k & 3) == 0 && k <= cap) {
+            *out = chunk[threadIdx.x];
+            out += N;
           }
         };
         if (dx == 0 && dy == 0 && dz == 0 && lo <= i && i < hi) {  // the home cell: skip i itself
@@ -121,7 +123,7 @@ __global__ void __launch_bounds__(kNT) nlist_kernel(DevView v, float margin) {
       }
     }
   }
-  if (k <= cap && (k & 3)) out[(size_t)(k >> 2) * N] = chunk[threadIdx.x];  // last, partial chunk
+  if (k <= cap && (k & 3)) *out = chunk[threadIdx.x];  // last, partial chunk
   v.S.nl_count[i] = (k <= cap) ? k : -1;
 }
 
