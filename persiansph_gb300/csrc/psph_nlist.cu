@@ -22,7 +22,11 @@ constexpr int kNT = 128;
 
 template <int DIM, bool UNIFORM_H>
 __global__ void __launch_bounds__(kNT, 8) nlist_kernel(DevView v, float margin) {
-  __shared__ int4 chunk[kNT];  // each lane's chunk being filled
+  // Entries go through an 8-slot ring per lane, lane-interleaved (slot s of
+  // lane l at ring[s][l], so the per-candidate stores are bank-conflict free);
+  // the ring holds the chunk being filled and the next one, and a completed
+  // chunk goes out as one 16-byte store.
+  __shared__ int ring[8][kNT];
   const StepScalars* sc = v.sc;
   if (sc->all_stop) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -42,8 +46,8 @@ __global__ void __launch_bounds__(kNT, 8) nlist_kernel(DevView v, float margin) 
   const int N = v.ncap, cap = v.o.nl_cap;
   const CellCoord c = decode(g, cell);
   const float4* __restrict__ off = v.S.OFF32;
-  int4* __restrict__ out = reinterpret_cast<int4*>(v.S.nl) + i;  // the next chunk to fill; chunk c at nl + c * N + i
-  int* mine = reinterpret_cast<int*>(&chunk[threadIdx.x]);
+  int4* __restrict__ out = reinterpret_cast<int4*>(v.S.nl) + i;  // the next chunk to write; chunk c at nl + c * N + i
+  int* const rp = &ring[0][threadIdx.x];                            // slot s at rp[s * kNT]
   // Rows of cells and x-slabs of cells whose nearest point lies outside the
   // support are skipped (cells are sorted slab by slab, xsub slabs along x).
   // The bound assumes the in-cell offset of i lies in [0, cell size), which
@@ -58,6 +62,21 @@ __global__ void __launch_bounds__(kNT, 8) nlist_kernel(DevView v, float margin) 
   const int* __restrict__ sstart = xs > 1 ? v.S.sstart : v.S.start;
   const float inv_sw = (float)xs / cs.x;  // 1 / slab width
   int k = 0;
+  // the entry is written to the next free slot for every candidate and kept
+  // (k advances) only when the candidate is inside
+  auto put = [&](int e, bool in) {
+    rp[(k & 7) * kNT] = e;
+    k += in ? 1 : 0;
+  };
+  // after candidates that started at count k0 (at most 4 of them): the chunk
+  // k0 / 4, if they completed it and it fits the capacity
+  auto flush = [&](int k0) {
+    if (((k0 ^ k) & 4) && k0 < cap) {
+      const int b = (k0 & 4) * kNT;
+      *out = make_int4(rp[b], rp[b + kNT], rp[b + 2 * kNT], rp[b + 3 * kNT]);
+      out += N;
+    }
+  };
   const int zlo = (DIM == 3) ? -1 : 0, zhi = (DIM == 3) ? 1 : 0;
   for (int dz = zlo; dz <= zhi; ++dz) {
     int z = c.z + dz;
@@ -94,7 +113,7 @@ __global__ void __launch_bounds__(kNT, 8) nlist_kernel(DevView v, float margin) 
         // (one rounding away from rel_pos's form, which the pair kernels
         // apply exactly; the list's margin covers the difference)
         const float ax = oi.x - (float)dx * cs.x, ay = oi.y + cy, az = oi.z + cz;
-        auto visit = [&](int j) {
+        auto inside = [&](int j) {
           const float4 oj = off[j];
           const float x0 = ax - oj.x, x1 = ay - oj.y, x2 = (DIM == 3) ? az - oj.z : 0.f;
           float thr = thr_u;
@@ -102,28 +121,35 @@ __global__ void __launch_bounds__(kNT, 8) nlist_kernel(DevView v, float margin) 
             const float hb = 0.5f * (oi.w + oj.w);
             thr = cf * cf * hb * hb * margin;
           }
-          // branch-free push: the slot k & 3 is written for every candidate
-          // and kept only when the candidate is inside (k advances); a full
-          // chunk goes out as one 16-byte store while the list fits its cap
-          const bool in = x0 * x0 + x1 * x1 + x2 * x2 <= thr;
-          mine[k & 3] = j | tag;
-          k += in ? 1 : 0;
-          if (in && (k & 3) == 0 && k <= cap) {
-            *out = chunk[threadIdx.x];
-            out += N;
-          }
+          return x0 * x0 + x1 * x1 + x2 * x2 <= thr;
+        };
+        auto one = [&](int j) {
+          const int k0 = k;
+          put(j | tag, inside(j));
+          flush(k0);
         };
         if (dx == 0 && dy == 0 && dz == 0 && lo <= i && i < hi) {  // the home cell: skip i itself
-#pragma unroll 4
-          for (int j = lo; j < i; ++j) visit(j);
+          for (int j = lo; j < i; ++j) one(j);
           lo = i + 1;
         }
-#pragma unroll 4
-        for (int j = lo; j < hi; ++j) visit(j);
+        int j = lo;
+        for (; j + 4 <= hi; j += 4) {  // groups of 4: one chunk check per group
+          const bool in0 = inside(j), in1 = inside(j + 1), in2 = inside(j + 2), in3 = inside(j + 3);
+          const int k0 = k;
+          put(j | tag, in0);
+          put((j + 1) | tag, in1);
+          put((j + 2) | tag, in2);
+          put((j + 3) | tag, in3);
+          flush(k0);
+        }
+        for (; j < hi; ++j) one(j);
       }
     }
   }
-  if (k <= cap && (k & 3)) *out = chunk[threadIdx.x];  // last, partial chunk
+  if (k <= cap && (k & 3)) {  // last, partial chunk
+    const int b = (k & 4) * kNT;
+    *out = make_int4(rp[b], rp[b + kNT], rp[b + 2 * kNT], rp[b + 3 * kNT]);
+  }
   v.S.nl_count[i] = (k <= cap) ? k : -1;
 }
 
