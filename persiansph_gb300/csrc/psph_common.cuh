@@ -73,6 +73,7 @@ struct StepScalars {
   unsigned int work;            // tile counter of the persistent pair kernels
   int launches;
   unsigned long long closure_eval, closure_fallback;  // closure evaluations / Smagorinsky fallbacks
+  int nl_rest;    // particles left to the per-particle neighbour-list pass this step
 };
 
 struct GridDev {

@@ -12,6 +12,8 @@
 // half a sector. The
 // scan is cheap integer/FP32 work; the pair kernels then walk lists of nearly
 // equal length instead of branching per candidate.
+#include <algorithm>
+
 #include "psph_pairs.cuh"
 
 namespace psph {
@@ -20,17 +22,59 @@ namespace {
 
 constexpr int kNT = 128;
 
+// Shared pieces of both scans. The 8-slot entry ring of a lane is
+// lane-interleaved (slot s of lane l at ring[s][l], so the per-candidate
+// stores are bank-conflict free); it holds the chunk being filled and the next
+// one, and a completed chunk goes out as one 16-byte store.
+struct ListWriter {
+  int* rp;    // this lane's slot 0; slot s at rp[s * kNT]
+  int4* out;  // the next chunk to write; chunk c of particle i at nl + c * N + i
+  int k = 0;  // entries kept
+  // the entry goes to the next free slot for every candidate and is kept (k
+  // advances) only when the candidate is inside
+  __device__ __forceinline__ void put(int e, bool in) {
+    rp[(k & 7) * kNT] = e;
+    k += in ? 1 : 0;
+  }
+  // after at most 4 candidates that started at count k0: the chunk k0 / 4, if
+  // they completed it and it fits the capacity
+  __device__ __forceinline__ void flush(int k0, int cap, int N) {
+    if (((k0 ^ k) & 4) && k0 < cap) {
+      const int b = (k0 & 4) * kNT;
+      *out = make_int4(rp[b], rp[b + kNT], rp[b + 2 * kNT], rp[b + 3 * kNT]);
+      out += N;
+    }
+  }
+  __device__ __forceinline__ void finish(int cap, int* count) {
+    if (k <= cap && (k & 3)) {  // last, partial chunk
+      const int b = (k & 4) * kNT;
+      *out = make_int4(rp[b], rp[b + kNT], rp[b + 2 * kNT], rp[b + 3 * kNT]);
+    }
+    *count = (k <= cap) ? k : -1;
+  }
+};
+
+// Rows of cells and x-slabs of cells whose nearest point lies outside the
+// support are skipped (cells are sorted slab by slab, xsub slabs along x).
+// The bound assumes the in-cell offset lies in [0, cell size), which holds
+// away from the grid faces (ListGenerate clamps only there); a neighbour
+// cell's clamped particles lie beyond its outer face, farther than the slab
+// they are counted in. Returns false when the row is out of reach, else the
+// slabs in reach along x, counted from the first slab of the particle's cell.
+__device__ __forceinline__ bool slab_reach(float ox, float gy, float gz, float thr_cull, float inv_sw, int* slo,
+                                           int* shi) {
+  const float rx2 = thr_cull - gy * gy - gz * gz;
+  if (rx2 < 0.f) return false;
+  const float rx = sqrtf(rx2);
+  *slo = (int)floorf((ox - rx) * inv_sw - 1e-3f);
+  *shi = (int)floorf((ox + rx) * inv_sw + 1e-3f);
+  return true;
+}
+
+// One particle's list: the candidates of its 3x3(x3) cell block inside the
+// support, tested in FP32 on (cell offset, FP32 offset) separations.
 template <int DIM, bool UNIFORM_H>
-__global__ void __launch_bounds__(kNT, 8) nlist_kernel(DevView v, float margin) {
-  // Entries go through an 8-slot ring per lane, lane-interleaved (slot s of
-  // lane l at ring[s][l], so the per-candidate stores are bank-conflict free);
-  // the ring holds the chunk being filled and the next one, and a completed
-  // chunk goes out as one 16-byte store.
-  __shared__ int ring[8][kNT];
-  const StepScalars* sc = v.sc;
-  if (sc->all_stop) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= sc->n) return;
+__device__ __forceinline__ void list_one(const DevView& v, int i, float margin, int* rp) {
   const int cell = v.S.cellid[i];
   if (cell < 0) {
     v.S.nl_count[i] = 0;
@@ -46,14 +90,7 @@ __global__ void __launch_bounds__(kNT, 8) nlist_kernel(DevView v, float margin) 
   const int N = v.ncap, cap = v.o.nl_cap;
   const CellCoord c = decode(g, cell);
   const float4* __restrict__ off = v.S.OFF32;
-  int4* __restrict__ out = reinterpret_cast<int4*>(v.S.nl) + i;  // the next chunk to write; chunk c at nl + c * N + i
-  int* const rp = &ring[0][threadIdx.x];                            // slot s at rp[s * kNT]
-  // Rows of cells and x-slabs of cells whose nearest point lies outside the
-  // support are skipped (cells are sorted slab by slab, xsub slabs along x).
-  // The bound assumes the in-cell offset of i lies in [0, cell size), which
-  // holds away from the grid faces (ListGenerate clamps only there); a
-  // neighbour cell's clamped particles lie beyond its outer face, farther
-  // from i than the slab they are counted in.
+  ListWriter w{rp, reinterpret_cast<int4*>(v.S.nl) + i};
   const bool inner = c.x > 0 && c.x < g.nc[0] - 1 && c.y > 0 && c.y < g.nc[1] - 1 &&
                      (DIM == 2 || (c.z > 0 && c.z < g.nc[2] - 1));
   const bool cull = UNIFORM_H && inner;
@@ -61,22 +98,6 @@ __global__ void __launch_bounds__(kNT, 8) nlist_kernel(DevView v, float margin) 
   const int xs = v.o.xsub;
   const int* __restrict__ sstart = xs > 1 ? v.S.sstart : v.S.start;
   const float inv_sw = (float)xs / cs.x;  // 1 / slab width
-  int k = 0;
-  // the entry is written to the next free slot for every candidate and kept
-  // (k advances) only when the candidate is inside
-  auto put = [&](int e, bool in) {
-    rp[(k & 7) * kNT] = e;
-    k += in ? 1 : 0;
-  };
-  // after candidates that started at count k0 (at most 4 of them): the chunk
-  // k0 / 4, if they completed it and it fits the capacity
-  auto flush = [&](int k0) {
-    if (((k0 ^ k) & 4) && k0 < cap) {
-      const int b = (k0 & 4) * kNT;
-      *out = make_int4(rp[b], rp[b + kNT], rp[b + 2 * kNT], rp[b + 3 * kNT]);
-      out += N;
-    }
-  };
   const int zlo = (DIM == 3) ? -1 : 0, zhi = (DIM == 3) ? 1 : 0;
   for (int dz = zlo; dz <= zhi; ++dz) {
     int z = c.z + dz;
@@ -91,14 +112,12 @@ __global__ void __launch_bounds__(kNT, 8) nlist_kernel(DevView v, float margin) 
       const int base = g.cell_base + (z * g.nc[1] + y) * g.nc[0];
       const int cyz = 3 * (dy + 1) + 9 * (dz + 1);
       const float cy = -(float)dy * cs.y, cz = -(float)dz * cs.z;  // exact: dy, dz in {-1, 0, 1}
-      // slabs in reach along x, counted from the first slab of i's cell
       int slo = -xs, shi = 2 * xs - 1;
       if (cull) {
-        const float rx2 = thr_cull - gy * gy - gz * gz;
-        if (rx2 < 0.f) continue;
-        const float rx = sqrtf(rx2);
-        slo = max(slo, (int)floorf((oi.x - rx) * inv_sw - 1e-3f));
-        shi = min(shi, (int)floorf((oi.x + rx) * inv_sw + 1e-3f));
+        int lo_, hi_;
+        if (!slab_reach(oi.x, gy, gz, thr_cull, inv_sw, &lo_, &hi_)) continue;
+        slo = max(slo, lo_);
+        shi = min(shi, hi_);
       }
       for (int dx = -1; dx <= 1; ++dx) {
         int x = c.x + dx;
@@ -124,9 +143,9 @@ __global__ void __launch_bounds__(kNT, 8) nlist_kernel(DevView v, float margin) 
           return x0 * x0 + x1 * x1 + x2 * x2 <= thr;
         };
         auto one = [&](int j) {
-          const int k0 = k;
-          put(j | tag, inside(j));
-          flush(k0);
+          const int k0 = w.k;
+          w.put(j | tag, inside(j));
+          w.flush(k0, cap, N);
         };
         if (dx == 0 && dy == 0 && dz == 0 && lo <= i && i < hi) {  // the home cell: skip i itself
           for (int j = lo; j < i; ++j) one(j);
@@ -135,39 +154,218 @@ __global__ void __launch_bounds__(kNT, 8) nlist_kernel(DevView v, float margin) 
         int j = lo;
         for (; j + 4 <= hi; j += 4) {  // groups of 4: one chunk check per group
           const bool in0 = inside(j), in1 = inside(j + 1), in2 = inside(j + 2), in3 = inside(j + 3);
-          const int k0 = k;
-          put(j | tag, in0);
-          put((j + 1) | tag, in1);
-          put((j + 2) | tag, in2);
-          put((j + 3) | tag, in3);
-          flush(k0);
+          const int k0 = w.k;
+          w.put(j | tag, in0);
+          w.put((j + 1) | tag, in1);
+          w.put((j + 2) | tag, in2);
+          w.put((j + 3) | tag, in3);
+          w.flush(k0, cap, N);
         }
         for (; j < hi; ++j) one(j);
       }
     }
   }
-  if (k <= cap && (k & 3)) {  // last, partial chunk
-    const int b = (k & 4) * kNT;
-    *out = make_int4(rp[b], rp[b + kNT], rp[b + 2 * kNT], rp[b + 3 * kNT]);
+  w.finish(cap, v.S.nl_count + i);
+}
+
+template <int DIM, bool UNIFORM_H>
+__global__ void __launch_bounds__(kNT, 8) nlist_kernel(DevView v, float margin) {
+  __shared__ int ring[8][kNT];
+  if (v.sc->all_stop) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= v.sc->n) return;
+  list_one<DIM, UNIFORM_H>(v, i, margin, &ring[0][threadIdx.x]);
+}
+
+// One h everywhere: a lane builds the lists of sorted particles 2t and 2t+1
+// when they share a cell. Both scan the same cell block, so each candidate is
+// loaded once and tested against both, and the rows and slabs walked are the
+// union of the two particles' reach. A particle 2t+1 in another cell than 2t
+// is appended to a compact list (S.tmp_perm, free after the sort) that
+// nlist_rest_kernel walks densely.
+template <int DIM>
+__global__ void __launch_bounds__(kNT, 8) nlist_pair_kernel(DevView v, float margin) {
+  __shared__ int ring[2][8][kNT];
+  StepScalars* sc = v.sc;
+  if (sc->all_stop) return;
+  const int n = sc->n;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ia = 2 * t, ib = ia + 1;
+  if (ia >= n) return;
+  const int cell = v.S.cellid[ia];
+  const bool pair = ib < n && cell >= 0 && v.S.cellid[ib] == cell;
+  {
+    const bool rest = ib < n && !pair;
+    const unsigned want = __ballot_sync(__activemask(), rest);
+    if (rest) {  // one atomic per warp
+      const int lane = threadIdx.x & 31, leader = __ffs(want) - 1;
+      int base = 0;
+      if (lane == leader) base = atomicAdd(&sc->nl_rest, __popc(want));
+      base = __shfl_sync(want, base, leader);
+      v.S.tmp_perm[base + __popc(want & ((1u << lane) - 1u))] = ib;
+    }
   }
-  v.S.nl_count[i] = (k <= cap) ? k : -1;
+  if (cell < 0) {
+    v.S.nl_count[ia] = 0;
+    return;
+  }
+  const Persist& P = cur_persist(v);
+  const GridDev& g = grid_of(v, v.cls[P.cls[ia]].inst);
+  const float3 cs = cell_size_f(g);
+  // particle b far away when it is not paired: its tests always fail
+  constexpr float kFar = 1e18f;
+  const float4 oa = v.S.OFF32[ia];
+  const float4 ob = pair ? v.S.OFF32[ib] : make_float4(kFar, kFar, kFar, oa.w);
+  const float cf = (float)g.cellfac;
+  const float thr = cf * cf * oa.w * oa.w * margin;
+  const int N = v.ncap, cap = v.o.nl_cap;
+  const CellCoord c = decode(g, cell);
+  const float4* __restrict__ off = v.S.OFF32;
+  int4* const nl4 = reinterpret_cast<int4*>(v.S.nl);
+  ListWriter wa{&ring[0][0][threadIdx.x], nl4 + ia};
+  ListWriter wb{&ring[1][0][threadIdx.x], nl4 + ib};
+  const bool cull = c.x > 0 && c.x < g.nc[0] - 1 && c.y > 0 && c.y < g.nc[1] - 1 &&
+                    (DIM == 2 || (c.z > 0 && c.z < g.nc[2] - 1));
+  const float thr_cull = thr * 1.0001f;
+  const int xs = v.o.xsub;
+  const int* __restrict__ sstart = xs > 1 ? v.S.sstart : v.S.start;
+  const float inv_sw = (float)xs / cs.x;
+  const int zlo = (DIM == 3) ? -1 : 0, zhi = (DIM == 3) ? 1 : 0;
+  for (int dz = zlo; dz <= zhi; ++dz) {
+    int z = c.z + dz;
+    if (g.periodic[2]) z = (z + g.nc[2]) % g.nc[2];
+    else if (z < 0 || z >= g.nc[2]) continue;
+    const float gza = (DIM == 3) ? (dz < 0 ? oa.z : (dz > 0 ? cs.z - oa.z : 0.f)) : 0.f;
+    const float gzb = (DIM == 3) ? (dz < 0 ? ob.z : (dz > 0 ? cs.z - ob.z : 0.f)) : 0.f;
+    for (int dy = -1; dy <= 1; ++dy) {
+      int y = c.y + dy;
+      if (g.periodic[1]) y = (y + g.nc[1]) % g.nc[1];
+      else if (y < 0 || y >= g.nc[1]) continue;
+      const float gya = dy < 0 ? oa.y : (dy > 0 ? cs.y - oa.y : 0.f);
+      const float gyb = dy < 0 ? ob.y : (dy > 0 ? cs.y - ob.y : 0.f);
+      const int base = g.cell_base + (z * g.nc[1] + y) * g.nc[0];
+      const int cyz = 3 * (dy + 1) + 9 * (dz + 1);
+      const float cy = -(float)dy * cs.y, cz = -(float)dz * cs.z;
+      int slo = -xs, shi = 2 * xs - 1;
+      if (cull) {  // the union of the two particles' reach
+        int la, ha, lb, hb;
+        const bool ra = slab_reach(oa.x, gya, gza, thr_cull, inv_sw, &la, &ha);
+        const bool rb = pair && slab_reach(ob.x, gyb, gzb, thr_cull, inv_sw, &lb, &hb);
+        if (!ra && !rb) continue;
+        if (!ra) la = lb, ha = hb;
+        else if (rb) la = min(la, lb), ha = max(ha, hb);
+        slo = max(slo, la);
+        shi = min(shi, ha);
+      }
+      for (int dx = -1; dx <= 1; ++dx) {
+        int x = c.x + dx;
+        if (g.periodic[0]) x = (x + g.nc[0]) % g.nc[0];
+        else if (x < 0 || x >= g.nc[0]) continue;
+        const int s0 = max(slo - dx * xs, 0), s1 = min(shi - dx * xs, xs - 1);
+        if (s0 > s1) continue;
+        int lo = sstart[(base + x) * xs + s0];
+        const int hi = sstart[(base + x) * xs + s1 + 1];
+        const int tag = ((dx + 1) + cyz) << kCodeShift;
+        const float cx = -(float)dx * cs.x;
+        const float axa = oa.x + cx, aya = oa.y + cy, aza = oa.z + cz;
+        const float axb = ob.x + cx, ayb = ob.y + cy, azb = ob.z + cz;
+        auto test = [&](int j, bool& ina, bool& inb) {
+          const float4 oj = off[j];
+          const float xa = axa - oj.x, ya = aya - oj.y, za = (DIM == 3) ? aza - oj.z : 0.f;
+          const float xb = axb - oj.x, yb = ayb - oj.y, zb = (DIM == 3) ? azb - oj.z : 0.f;
+          ina = xa * xa + ya * ya + za * za <= thr;
+          inb = xb * xb + yb * yb + zb * zb <= thr;
+        };
+        auto one = [&](int j, bool ena, bool enb) {
+          bool ina, inb;
+          test(j, ina, inb);
+          const int ka = wa.k, kb = wb.k;
+          wa.put(j | tag, ina && ena);
+          wb.put(j | tag, inb && enb);
+          wa.flush(ka, cap, N);
+          wb.flush(kb, cap, N);
+        };
+        if (dx == 0 && dy == 0 && dz == 0) {  // the home cell: neither particle lists itself
+          const int e0 = min(ia, hi);
+          for (int j = lo; j < e0; ++j) one(j, true, true);
+          if (lo <= ia && ia < hi) one(ia, false, true);
+          int nx = ia + 1;
+          if (pair) {
+            if (lo <= ib && ib < hi) one(ib, true, false);
+            nx = ib + 1;
+          }
+          lo = max(lo, nx);
+        }
+        int j = lo;
+        for (; j + 4 <= hi; j += 4) {
+          bool a0, a1, a2, a3, b0, b1, b2, b3;
+          test(j, a0, b0);
+          test(j + 1, a1, b1);
+          test(j + 2, a2, b2);
+          test(j + 3, a3, b3);
+          const int ka = wa.k, kb = wb.k;
+          wa.put(j | tag, a0);
+          wa.put((j + 1) | tag, a1);
+          wa.put((j + 2) | tag, a2);
+          wa.put((j + 3) | tag, a3);
+          wb.put(j | tag, b0);
+          wb.put((j + 1) | tag, b1);
+          wb.put((j + 2) | tag, b2);
+          wb.put((j + 3) | tag, b3);
+          wa.flush(ka, cap, N);
+          wb.flush(kb, cap, N);
+        }
+        for (; j < hi; ++j) one(j, true, true);
+      }
+    }
+  }
+  wa.finish(cap, v.S.nl_count + ia);
+  if (pair) wb.finish(cap, v.S.nl_count + ib);
+}
+
+// The particles the pair kernel left (2t+1 not in 2t's cell), one per lane.
+template <int DIM>
+__global__ void __launch_bounds__(kNT, 8) nlist_rest_kernel(DevView v, float margin) {
+  __shared__ int ring[8][kNT];
+  if (v.sc->all_stop) return;
+  const int m = v.sc->nl_rest;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < m; q += gridDim.x * blockDim.x)
+    list_one<DIM, true>(v, v.S.tmp_perm[q], margin, &ring[0][threadIdx.x]);
+}
+
+int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
 }
 
 }  // namespace
 
 void launch_nlist(const DevView& v, cudaStream_t st) {
-  const int nb = v.ncap > 0 ? (v.ncap + kNT - 1) / kNT : 1;
   // a superset of the support: the pair kernels apply the exact test (FP32 in
   // the FP32C form, FP64 in the plain form)
   const float margin = v.o.fp32 ? 1.0002f : 1.004f;
-  const bool uh = v.o.uniform_h;
-  if (v.o.dim == 2) {
-    if (uh) nlist_kernel<2, true><<<nb, kNT, 0, st>>>(v, margin);
-    else nlist_kernel<2, false><<<nb, kNT, 0, st>>>(v, margin);
-  } else {
-    if (uh) nlist_kernel<3, true><<<nb, kNT, 0, st>>>(v, margin);
-    else nlist_kernel<3, false><<<nb, kNT, 0, st>>>(v, margin);
+  if (v.o.uniform_h) {  // two particles per lane, then the leftovers
+    const int half = (v.ncap + 1) / 2;
+    const int nb = half > 0 ? (half + kNT - 1) / kNT : 1;
+    const int nr = std::max(1, std::min(nb, 8 * sm_count()));
+    if (v.o.dim == 2) {
+      nlist_pair_kernel<2><<<nb, kNT, 0, st>>>(v, margin);
+      nlist_rest_kernel<2><<<nr, kNT, 0, st>>>(v, margin);
+    } else {
+      nlist_pair_kernel<3><<<nb, kNT, 0, st>>>(v, margin);
+      nlist_rest_kernel<3><<<nr, kNT, 0, st>>>(v, margin);
+    }
+    return;
   }
+  const int nb = v.ncap > 0 ? (v.ncap + kNT - 1) / kNT : 1;
+  if (v.o.dim == 2) nlist_kernel<2, false><<<nb, kNT, 0, st>>>(v, margin);
+  else nlist_kernel<3, false><<<nb, kNT, 0, st>>>(v, margin);
 }
 
 }  // namespace psph

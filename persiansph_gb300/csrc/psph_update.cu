@@ -358,8 +358,9 @@ void launch_update(const DevView& v, cudaStream_t st) {
   else update_kernel<3><<<nb > 0 ? nb : 1, kUT, 0, st>>>(v);
 }
 
-// begin, bin, 3 scan, scatter, rank, reorder, finish, neighbour lists, prepare
-// (2 in the FP32C form: copies + walls), forces, dt, update, end
+// begin, bin, 3 scan, scatter, rank, reorder, finish, cell starts (split
+// cells), neighbour lists (2 with one h: pairs + rest), prepare (2 in the
+// FP32C form: copies + walls), forces, closure, dt, update, end
 namespace {
 __global__ void class_constants_kernel(PClass* cls, int n, int dim) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -374,6 +375,8 @@ void launch_class_constants(PClass* cls, int n, int dim, cudaStream_t st) {
   if (n > 0) class_constants_kernel<<<(n + 127) / 128, 128, 0, st>>>(cls, n, dim);
 }
 
-int launches_per_step(const DevView& v) { return (v.o.fp32 ? 16 : 15) + (v.o.closure ? 1 : 0); }
+int launches_per_step(const DevView& v) {
+  return (v.o.fp32 ? 16 : 15) + (v.o.closure ? 1 : 0) + (v.o.xsub > 1 ? 1 : 0) + (v.o.uniform_h ? 1 : 0);
+}
 
 }  // namespace psph
