@@ -73,7 +73,7 @@ struct StepScalars {
   unsigned int work;            // tile counter of the persistent pair kernels
   int launches;
   unsigned long long closure_eval, closure_fallback;  // closure evaluations / Smagorinsky fallbacks
-  int nl_rest;    // particles left to the per-particle neighbour-list pass this step
+  int nl_rest;    // particles the neighbour-list scan handles one per lane (set by the sort)
 };
 
 struct GridDev {

@@ -701,10 +701,7 @@ __global__ void begin_kernel(DevView v) {
     I.dtmin_bits = (unsigned long long)__double_as_longlong(DBL_MAX);
   }
   live = __syncthreads_or(live);
-  if (threadIdx.x == 0) {
-    sc->all_stop = !live;
-    sc->nl_rest = 0;
-  }
+  if (threadIdx.x == 0) sc->all_stop = !live;
 }
 
 // End of step: Time += deltat and the per-particle counters, once per instance.

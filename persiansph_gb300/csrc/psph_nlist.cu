@@ -180,31 +180,29 @@ __global__ void __launch_bounds__(kNT, 8) nlist_kernel(DevView v, float margin) 
 // One h everywhere: a lane builds the lists of sorted particles 2t and 2t+1
 // when they share a cell. Both scan the same cell block, so each candidate is
 // loaded once and tested against both, and the rows and slabs walked are the
-// union of the two particles' reach. A particle 2t+1 in another cell than 2t
-// is appended to a compact list (S.tmp_perm, free after the sort) that
-// nlist_rest_kernel walks densely.
+// union of the two particles' reach. The odd particles whose cell starts at
+// them (listed by the sort, nl_rest of them in S.tmp_perm) get a lane of their
+// own in the first nr blocks of the grid, which the hardware starts first, so
+// their scans run beside the pairs instead of after them.
 template <int DIM>
-__global__ void __launch_bounds__(kNT, 8) nlist_pair_kernel(DevView v, float margin) {
+__global__ void __launch_bounds__(kNT, 8) nlist_pair_kernel(DevView v, float margin, int nr) {
   __shared__ int ring[2][8][kNT];
-  StepScalars* sc = v.sc;
+  const StepScalars* sc = v.sc;
   if (sc->all_stop) return;
+  if ((int)blockIdx.x < nr) {
+    const int m = min(sc->nl_rest, v.ncap);
+    for (int q = blockIdx.x * kNT + threadIdx.x; q < m; q += nr * kNT)
+      list_one<DIM, true>(v, v.S.tmp_perm[q], margin, &ring[0][0][threadIdx.x]);
+    return;
+  }
   const int n = sc->n;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = (blockIdx.x - nr) * kNT + threadIdx.x;
   const int ia = 2 * t, ib = ia + 1;
   if (ia >= n) return;
   const int cell = v.S.cellid[ia];
-  const bool pair = ib < n && cell >= 0 && v.S.cellid[ib] == cell;
-  {
-    const bool rest = ib < n && !pair;
-    const unsigned want = __ballot_sync(__activemask(), rest);
-    if (rest) {  // one atomic per warp
-      const int lane = threadIdx.x & 31, leader = __ffs(want) - 1;
-      int base = 0;
-      if (lane == leader) base = atomicAdd(&sc->nl_rest, __popc(want));
-      base = __shfl_sync(want, base, leader);
-      v.S.tmp_perm[base + __popc(want & ((1u << lane) - 1u))] = ib;
-    }
-  }
+  const int cellb = ib < n ? v.S.cellid[ib] : -1;
+  const bool pair = cell >= 0 && cellb == cell;
+  if (ib < n && cellb < 0) v.S.nl_count[ib] = 0;  // in no cell (sorted after every cell)
   if (cell < 0) {
     v.S.nl_count[ia] = 0;
     return;
@@ -323,16 +321,6 @@ __global__ void __launch_bounds__(kNT, 8) nlist_pair_kernel(DevView v, float mar
   if (pair) wb.finish(cap, v.S.nl_count + ib);
 }
 
-// The particles the pair kernel left (2t+1 not in 2t's cell), one per lane.
-template <int DIM>
-__global__ void __launch_bounds__(kNT, 8) nlist_rest_kernel(DevView v, float margin) {
-  __shared__ int ring[8][kNT];
-  if (v.sc->all_stop) return;
-  const int m = v.sc->nl_rest;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < m; q += gridDim.x * blockDim.x)
-    list_one<DIM, true>(v, v.S.tmp_perm[q], margin, &ring[0][threadIdx.x]);
-}
-
 int sm_count() {
   static int n = 0;
   if (!n) {
@@ -350,17 +338,12 @@ void launch_nlist(const DevView& v, cudaStream_t st) {
   // a superset of the support: the pair kernels apply the exact test (FP32 in
   // the FP32C form, FP64 in the plain form)
   const float margin = v.o.fp32 ? 1.0002f : 1.004f;
-  if (v.o.uniform_h) {  // two particles per lane, then the leftovers
+  if (v.o.uniform_h) {  // two particles per lane; the leftovers' blocks first
     const int half = (v.ncap + 1) / 2;
-    const int nb = half > 0 ? (half + kNT - 1) / kNT : 1;
-    const int nr = std::max(1, std::min(nb, 8 * sm_count()));
-    if (v.o.dim == 2) {
-      nlist_pair_kernel<2><<<nb, kNT, 0, st>>>(v, margin);
-      nlist_rest_kernel<2><<<nr, kNT, 0, st>>>(v, margin);
-    } else {
-      nlist_pair_kernel<3><<<nb, kNT, 0, st>>>(v, margin);
-      nlist_rest_kernel<3><<<nr, kNT, 0, st>>>(v, margin);
-    }
+    const int nr = 2 * sm_count();
+    const int nb = nr + (half > 0 ? (half + kNT - 1) / kNT : 1);
+    if (v.o.dim == 2) nlist_pair_kernel<2><<<nb, kNT, 0, st>>>(v, margin, nr);
+    else nlist_pair_kernel<3><<<nb, kNT, 0, st>>>(v, margin, nr);
     return;
   }
   const int nb = v.ncap > 0 ? (v.ncap + kNT - 1) / kNT : 1;

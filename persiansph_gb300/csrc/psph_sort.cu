@@ -13,7 +13,8 @@
 //   rank     deterministic order inside each slab: by original index, so the
 //            sorted state depends only on positions, never on atomic timing.
 //   starts   per-cell segment starts (start[c] = slab start of c's first slab)
-//            for everything that walks whole cells.
+//            for everything that walks whole cells, and the particles the
+//            neighbour-list scan handles one per lane.
 //   reorder  gathers every persistent field into the new order (HBM-bound).
 #include <cstdio>
 
@@ -250,16 +251,38 @@ __global__ void finish_sort_kernel(const int* __restrict__ start, StepScalars* s
   sc->n_cells = start[nbins];
   sc->n = start[nbins + 1];
   sc->buf ^= 1;
+  sc->nl_rest = 0;
 }
 
-// Per-cell segment starts from the slab starts: start[c] = sstart[c * xsub]
-// for c <= ncells, and the orphan / dead / total boundaries after them.
+// Per-cell segment starts from the slab starts (split cells): start[c] =
+// sstart[c * xsub] for c <= ncells, and the orphan / dead / total boundaries
+// after them. Also lists the particles the two-per-lane neighbour-list scan
+// leaves to a lane of their own: lanes take sorted particles 2t and 2t+1
+// together when they share a cell, so the odd particles left are exactly the
+// cells' first particles at odd indices (into rest, at most cap of them).
 __global__ void cell_starts_kernel(const int* __restrict__ sstart, int* __restrict__ start, int ncells, int xsub,
-                                   const StepScalars* sc) {
+                                   StepScalars* sc, int* __restrict__ rest, int cap) {
   if (sc->all_stop) return;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c <= ncells) start[c] = sstart[(size_t)c * xsub];
-  else if (c <= ncells + 2) start[c] = sstart[(size_t)ncells * xsub + (c - ncells)];
+  if (xsub > 1) {
+    if (c <= ncells) start[c] = sstart[(size_t)c * xsub];
+    else if (c <= ncells + 2) start[c] = sstart[(size_t)ncells * xsub + (c - ncells)];
+  }
+  bool odd_first = false;
+  int s0 = 0;
+  if (c < ncells) {
+    s0 = sstart[(size_t)c * xsub];
+    odd_first = (s0 & 1) && sstart[(size_t)(c + 1) * xsub] > s0;
+  }
+  const unsigned want = __ballot_sync(0xffffffffu, odd_first);  // every lane of the grid gets here
+  if (odd_first) {  // one atomic per warp
+    const int lane = threadIdx.x & 31, leader = __ffs(want) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&sc->nl_rest, __popc(want));
+    base = __shfl_sync(want, base, leader);
+    const int slot = base + __popc(want & ((1u << lane) - 1u));
+    if (slot < cap) rest[slot] = s0;
+  }
 }
 
 inline int grid_for(int n) {
@@ -288,7 +311,7 @@ void launch_sort(const DevView& v, cudaStream_t st) {
   reorder_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(v, S.perm, S.key, sstart, S.cellid, v.alive, v.sc, nbins, xsub,
                                                     v.o.has_solid, v.o.dyn_mu);
   finish_sort_kernel<<<1, 1, 0, st>>>(sstart, v.sc, nbins);
-  if (xsub > 1) cell_starts_kernel<<<grid_for(ncells + 3), kBT, 0, st>>>(sstart, S.start, ncells, xsub, v.sc);
+  cell_starts_kernel<<<grid_for(ncells + 3), kBT, 0, st>>>(sstart, S.start, ncells, xsub, v.sc, S.tmp_perm, v.ncap);
 }
 
 }  // namespace psph

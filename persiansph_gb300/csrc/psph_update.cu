@@ -358,9 +358,9 @@ void launch_update(const DevView& v, cudaStream_t st) {
   else update_kernel<3><<<nb > 0 ? nb : 1, kUT, 0, st>>>(v);
 }
 
-// begin, bin, 3 scan, scatter, rank, reorder, finish, cell starts (split
-// cells), neighbour lists (2 with one h: pairs + rest), prepare (2 in the
-// FP32C form: copies + walls), forces, closure, dt, update, end
+// begin, bin, 3 scan, scatter, rank, reorder, finish, cell starts, neighbour
+// lists, prepare (2 in the FP32C form: copies + walls), forces, closure, dt,
+// update, end
 namespace {
 __global__ void class_constants_kernel(PClass* cls, int n, int dim) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -376,7 +376,7 @@ void launch_class_constants(PClass* cls, int n, int dim, cudaStream_t st) {
 }
 
 int launches_per_step(const DevView& v) {
-  return (v.o.fp32 ? 16 : 15) + (v.o.closure ? 1 : 0) + (v.o.xsub > 1 ? 1 : 0) + (v.o.uniform_h ? 1 : 0);
+  return (v.o.fp32 ? 17 : 16) + (v.o.closure ? 1 : 0);
 }
 
 }  // namespace psph
