@@ -667,6 +667,7 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
   if (o.fp32) {
     if ((st = dalloc(c, &S.V32, N)) || (st = dalloc(c, &S.D32, N)) || (st = dalloc(c, &S.NSV32, N))) return st;
     if (dyn_mu && (st = dalloc(c, &S.MU32, N))) return st;
+    if (o.need_sr && !o.has_solid && (st = dalloc(c, &S.cshear, N))) return st;  // FP32 ShearRate (fluid kernel)
   }
   if (o.fp32 && o.has_solid) {
     if ((st = dalloc(c, &S.SIG32, 2 * N)) || (st = dalloc(c, &S.VB32, N)) || (st = dalloc(c, &S.V32LO, N)))
@@ -1288,7 +1289,7 @@ psph_status psph_closure_attach(psph_ctx* c, const psph_mlp* mlp, double dx) {
   const size_t N = (size_t)c->ncap;
   if (!c->d_mlp) {
     if ((st = dalloc(c, &c->d_mlp, 1)) || (st = dalloc(c, &c->S.cvort, N)) || (st = dalloc(c, &c->S.cnnb, N)) ||
-        (st = dalloc(c, &c->S.cshear, N)) || (st = dalloc(c, &c->S.cr3, N)) ||
+        (!c->S.cshear && (st = dalloc(c, &c->S.cshear, N))) || (st = dalloc(c, &c->S.cr3, N)) ||
         (st = dalloc(c, &c->S.cfeat, 6 * N)) || (st = dalloc(c, &c->S.nut, N)))
       return st;
   }

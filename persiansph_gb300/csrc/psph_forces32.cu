@@ -451,16 +451,17 @@ __global__ void __maxnreg__(FL == 0 ? 128 : (FL == 1 ? 72 : 96)) forces_fluid32_
       out[0] = sr0; out[1] = sr1; out[2] = sr2;
       out[3] = sr1; out[4] = sr4; out[5] = sr5;
       out[6] = sr2; out[7] = sr5; out[8] = sr8;
-    }
-    if (closure) {
-      v.S.cvort[i] = sqrtf(w01 * w01 + w02 * w02 + w12 * w12);
-      v.S.cnnb[i] = (float)nnb;
-      // the closure's shear-rate features from the (symmetric) strain-rate
-      // sums, in FP32: the same contractions as its FP64 form
+      // Mat1's ShearRate contraction (Source/Particle.cpp:151-153) of the
+      // symmetric sums, in FP32: the update and the closure take it from here
       const float temp = sr0 * sr0 + 2.f * sr1 * sr1 + 2.f * sr2 * sr2 + sr4 * sr4 + 2.f * sr5 * sr5 + sr8 * sr8;
-      const float det = sr0 * (sr4 * sr8 - sr5 * sr5) - sr1 * (sr1 * sr8 - sr5 * sr2) + sr2 * (sr1 * sr5 - sr4 * sr2);
       v.S.cshear[i] = sqrtf(0.5f * temp);
-      v.S.cr3[i] = temp > 0.f ? det / (temp * sqrtf(temp)) : 0.f;
+      if (closure) {
+        v.S.cvort[i] = sqrtf(w01 * w01 + w02 * w02 + w12 * w12);
+        v.S.cnnb[i] = (float)nnb;
+        const float det =
+            sr0 * (sr4 * sr8 - sr5 * sr5) - sr1 * (sr1 * sr8 - sr5 * sr2) + sr2 * (sr1 * sr5 - sr4 * sr2);
+        v.S.cr3[i] = temp > 0.f ? det / (temp * sqrtf(temp)) : 0.f;
+      }
     }
     if (!(isfinite(axd) && isfinite(ayd) && isfinite(azd) && isfinite(drd))) atomicOr(&v.sc->status, ST_NONFINITE);
     // this particle's time-step bound sqrt_h_a sqrt(h/|a|) in FP32; the

@@ -217,11 +217,19 @@ __global__ void __launch_bounds__(kUT) update_kernel(DevView v) {
     // Mat1 (Source/Particle.cpp:146-186)
     p = eos(C.pres_eq, C.cs, C.p0, rho, C.rho0);
     if (o.need_sr || o.dyn_mu) {
-      const double* S = v.S.strain_rate + 9 * (size_t)s;
-      double temp = 0.0;
-      if (o.need_sr)
-        temp = (S[0] * S[0] + 2.0 * S[1] * S[3] + 2.0 * S[2] * S[6] + S[4] * S[4] + 2.0 * S[5] * S[7] + S[8] * S[8]);
-      const double shear_rate = sqrt(0.5 * temp), sbar = sqrt(2.0 * temp);
+      double shear_rate = 0.0, sbar = 0.0;
+      if (o.need_sr && o.fp32 && !o.has_solid) {
+        // FP32C fluid pair kernel: its FP32 contraction of its FP32 sums (two
+        // FP64 square roots per particle less); Sbar = sqrt(2 temp) = 2 ShearRate
+        shear_rate = (double)v.S.cshear[s];
+        sbar = 2.0 * shear_rate;
+      } else if (o.need_sr) {
+        const double* S = v.S.strain_rate + 9 * (size_t)s;
+        const double temp =
+            (S[0] * S[0] + 2.0 * S[1] * S[3] + 2.0 * S[2] * S[6] + S[4] * S[4] + 2.0 * S[5] * S[7] + S[8] * S[8]);
+        shear_rate = sqrt(0.5 * temp);
+        sbar = sqrt(2.0 * temp);
+      }
       v.S.shear_rate[s] = shear_rate;
       v.S.sbar[s] = sbar;
       if (o.dyn_mu) {
