@@ -24,7 +24,6 @@ constexpr int kFT32 = 128;  // block size of the copy and wall-interpolation ker
 // The pair kernels take their block size at launch (Options::pair_block, 64 to
 // 256 threads, picked by psph_autotune); register caps are set per kernel.
 constexpr int kMaxPairBlock = 256;
-constexpr int kQ32 = 16;  // queued wall-interpolation partners per lane
 
 struct Kahan {
   float s = 0.f, c = 0.f;
@@ -36,6 +35,27 @@ struct Kahan {
   }
   PSPH_D double value() const { return (double)s - (double)c; }
 };
+
+// Loads issued where they stand: the neighbour's velocity, density and class
+// go out together with its position, ahead of the support test, so the pair
+// waits for one memory round trip instead of two (a plain load would be sunk
+// below the test's branch). Read-only for the kernel's lifetime.
+PSPH_D float4 ld_early(const float4* p) {
+  float4 r;
+  asm volatile("ld.global.nc.v4.f32 {%0,%1,%2,%3}, [%4];" : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w) : "l"(p));
+  return r;
+}
+PSPH_D int ld_early(const int* p) {
+  int r;
+  asm volatile("ld.global.nc.b32 %0, [%1];" : "=r"(r) : "l"(p));
+  return r;
+}
+// the same for an array the kernel itself writes elsewhere (coherent path)
+PSPH_D float4 ld_early_coherent(const float4* p) {
+  float4 r;
+  asm volatile("ld.global.v4.f32 {%0,%1,%2,%3}, [%4];" : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w) : "l"(p));
+  return r;
+}
 
 template <int DIM, int KT>
 struct KernF {
@@ -141,13 +161,11 @@ __global__ void __launch_bounds__(kFT32) copies32_kernel(DevView v) {
 
 template <int DIM, int KT>
 __global__ void __launch_bounds__(kFT32) prepare32_kernel(DevView v) {
-  __shared__ int qbuf[kQ32][kFT32];
   const StepScalars* sc = v.sc;
   if (sc->all_stop) return;
   const Persist& P = cur_persist(v);
   const int n = sc->n;
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
-  const int tid = threadIdx.x;
   const Options& o = v.o;
   const PClass32* __restrict__ CT = v.cls32;
   const int winst = (w < n) ? CT[P.cls[w]].inst : 0;
@@ -170,46 +188,53 @@ __global__ void __launch_bounds__(kFT32) prepare32_kernel(DevView v) {
   const float gx = (float)o.gravity[0], gy = (float)o.gravity[1], gz = (float)o.gravity[2];
   const bool need_orient = !o.wallp_physical && (gx != 0.f || gy != 0.f || gz != 0.f);
   float sk = 0.f, p = 0.f, n0 = 0.f, n1 = 0.f, n2 = 0.f;
-  NbrSource<DIM> src;
-  src.init(v, g, w, wall && cell >= 0, 1.0f);
-  bool more = wall && cell >= 0;
   const float hw = oi.w;
-  while (true) {
-    int qn = 0;
-    while (more && qn < kQ32) {
+  // one fluid neighbour of the same material: its position, velocity and
+  // density loads go out together (this kernel writes the walls' own V32 /
+  // D32, which the class test then rejects, so those two take the coherent path)
+  auto visit = [&](const int f, const int code) {
+    const int clsf = ld_early(P.cls + f);
+    const float4 of = v.S.OFF32[f];
+    const float4 vf = ld_early_coherent(v.S.V32 + f);
+    const float4 df = ld_early_coherent(v.S.D32 + f);
+    const PClass32& Cf = CT[clsf];
+    if (!(Cf.flags & CF_FREE) || Cf.material != mat) return;
+    float x0, x1, x2;
+    rel_pos<DIM>(cs, oi, of, code, x0, x1, x2);  // x_wall - x_fluid
+    if (need_orient && !first_of_pair_code(code, ow, P.orig[f])) {
+      x0 = -x0; x1 = -x1; x2 = -x2;
+    }
+    const float hb = 0.5f * (hw + of.w);
+    const float ih = 1.f / hb;
+    const float q = sqrtf(x0 * x0 + x1 * x1 + x2 * x2) * ih;
+    const float K = KernF<DIM, KT>::W(q, KernF<DIM, KT>::cw() * (DIM == 2 ? ih * ih : ih * ih * ih));
+    if (K == 0.f) return;
+    sk += K;
+    p += vf.w * K + (gx * x0 + gy * x1 + gz * x2) * df.w * K;
+    if (noslip) { n0 += vf.x * K; n1 += vf.y * K; n2 += vf.z * K; }
+  };
+  const int cnt = (wall && cell >= 0) ? v.S.nl_count[w] : 0;
+  if (cnt >= 0) {  // the neighbour list, 4 entries per 16-byte load
+    const int4* __restrict__ nl4 = reinterpret_cast<const int4*>(v.S.nl) + w;
+    const size_t N = (size_t)v.ncap;
+    const int nch = (cnt + 3) >> 2;
+    for (int c = 0; c < nch; ++c) {
+      const int4 q = nl4[(size_t)c * N];
+      const int rem = cnt - 4 * c;
+      visit(q.x & kIndexMask, q.x >> kCodeShift);
+      if (rem > 1) visit(q.y & kIndexMask, q.y >> kCodeShift);
+      if (rem > 2) visit(q.z & kIndexMask, q.z >> kCodeShift);
+      if (rem > 3) visit(q.w & kIndexMask, q.w >> kCodeShift);
+    }
+  } else {  // list overflow: scan the cells
+    NbrSource<DIM> src;
+    src.init(v, g, w, true, 1.0f);
+    while (true) {
       int code;
       const int f = src.next(v, &code);
-      if (f < 0) {
-        more = false;
-        break;
-      }
-      qbuf[qn++][tid] = f | (code << kCodeShift);
+      if (f < 0) break;
+      visit(f, code);
     }
-    const int qmax = __reduce_max_sync(0xffffffffu, qn);
-    for (int k = 0; k < qmax; ++k) {
-      if (k >= qn) continue;
-      const int e = qbuf[k][tid];
-      const int f = e & kIndexMask, code = e >> kCodeShift;
-      const PClass32& Cf = CT[P.cls[f]];
-      if (!(Cf.flags & CF_FREE) || Cf.material != mat) continue;
-      const float4 of = v.S.OFF32[f];
-      float x0, x1, x2;
-      rel_pos<DIM>(cs, oi, of, code, x0, x1, x2);  // x_wall - x_fluid
-      if (need_orient && !first_of_pair_code(code, ow, P.orig[f])) {
-        x0 = -x0; x1 = -x1; x2 = -x2;
-      }
-      const float hb = 0.5f * (hw + of.w);
-      const float ih = 1.f / hb;
-      const float q = sqrtf(x0 * x0 + x1 * x1 + x2 * x2) * ih;
-      const float K = KernF<DIM, KT>::W(q, KernF<DIM, KT>::cw() * (DIM == 2 ? ih * ih : ih * ih * ih));
-      if (K == 0.f) continue;
-      const float4 vf = v.S.V32[f];
-      const float4 df = v.S.D32[f];
-      sk += K;
-      p += vf.w * K + (gx * x0 + gy * x1 + gz * x2) * df.w * K;
-      if (noslip) { n0 += vf.x * K; n1 += vf.y * K; n2 += vf.z * K; }
-    }
-    if (!__any_sync(0xffffffffu, more)) break;
   }
   if (!wall) return;
   if (sk != 0.f) {
@@ -248,7 +273,8 @@ __global__ void __launch_bounds__(kFT32) prepare32_kernel(DevView v) {
 // term and no XSPH (the dam-break configuration), without (1) or with (2) the
 // strain-rate sums of the LES / Bingham options. The list walk is a counted
 // loop so that the next neighbour's loads can be issued before this one's
-// arithmetic.
+// arithmetic; each pair issues all of its neighbour loads before the support
+// test (ld_early).
 // Register caps measured on the 6.7M-particle dam break: the strain-rate
 // flavour runs best at 96 (20 warps/SM), the plain one at 72 (28 warps/SM,
 // a few spilled values in L1), the general one at 128.
@@ -309,13 +335,16 @@ __global__ void __maxnreg__(FL == 0 ? 128 : (FL == 1 ? 72 : 96)) forces_fluid32_
   const float ih_u = (float)o.inv_h;
   auto pair = [&](const int j, const int code) {
     const float4 oj = v.S.OFF32[j];
+    const int clsj = ld_early(P.cls + j);
+    const float4 vj = ld_early(v.S.V32 + j);
+    const float4 dj4 = ld_early(v.S.D32 + j);
     float x0, x1, x2;
     rel_pos<DIM>(cs, oi, oj, code, x0, x1, x2);
     const float hb = 0.5f * (hi + oj.w);
     const float r2 = x0 * x0 + x1 * x1 + x2 * x2;
     // the list's own support test (exact in FP32; lists with a skin hold more)
     if (r2 > cf2 * hb * hb) return;
-    const PClass32& Cj = CT[P.cls[j]];
+    const PClass32& Cj = CT[clsj];
     const int fjf = Cj.flags;
     const bool fj = fjf & CF_FREE;
     npair2 += fj ? 1ull : 2ull;
@@ -330,8 +359,6 @@ __global__ void __maxnreg__(FL == 0 ? 128 : (FL == 1 ? 72 : 96)) forces_fluid32_
     const float cwg = cwh * ih2;
     const float GK = KernF<DIM, KT>::GK(q, inv_q, cwg);
     const float K = KernF<DIM, KT>::W(q, cwh);
-    const float4 vj = v.S.V32[j];
-    const float4 dj4 = v.S.D32[j];
     const float dj = dj4.w, inv_j = dj4.x, Pj = dj4.y, cj_snd = dj4.z, pj = vj.w;
     const float mj = fj ? Cj.mass : Cj.fpmassc * mi;
     const float v0 = vi.x - vj.x, v1 = vi.y - vj.y, v2 = vi.z - vj.z;
@@ -419,8 +446,18 @@ __global__ void __maxnreg__(FL == 0 ? 128 : (FL == 1 ? 72 : 96)) forces_fluid32_
     const int4* __restrict__ nl4 = reinterpret_cast<const int4*>(v.S.nl) + i;
     const size_t N = (size_t)v.ncap;
     const int nch = (cnt + 3) >> 2;
+    // the strain-rate flavour loads the next chunk one chunk ahead (measured:
+    // it helps there and costs the plain flavour a little)
+    constexpr bool kAhead = FL == 2;
+    int4 qn = (kAhead && nch > 0) ? nl4[0] : make_int4(0, 0, 0, 0);
     for (int c = 0; c < nch; ++c) {  // one 16-byte chunk of 4 entries per load
-      const int4 q = nl4[(size_t)c * N];
+      int4 q;
+      if (kAhead) {
+        q = qn;
+        if (c + 1 < nch) qn = nl4[(size_t)(c + 1) * N];
+      } else {
+        q = nl4[(size_t)c * N];
+      }
       const int rem = cnt - 4 * c;
       pair(q.x & kIndexMask, q.x >> kCodeShift);
       if (rem > 1) pair(q.y & kIndexMask, q.y >> kCodeShift);
