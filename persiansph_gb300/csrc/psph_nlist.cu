@@ -267,12 +267,23 @@ __global__ void __launch_bounds__(kNT, 8) nlist_pair_kernel(DevView v, float mar
         const float cx = -(float)dx * cs.x;
         const float axa = oa.x + cx, aya = oa.y + cy, aza = oa.z + cz;
         const float axb = ob.x + cx, ayb = ob.y + cy, azb = ob.z + cz;
+        // both particles' separations in packed FP32x2 arithmetic: a - off_j
+        // as fma(off_j, -1, a) (one rounding, the subtraction's), then the
+        // squared distances, one instruction for both particles' values
+        const float2 AX = make_float2(axa, axb), AY = make_float2(aya, ayb), AZ = make_float2(aza, azb);
+        const float2 M1 = make_float2(-1.f, -1.f);
         auto test = [&](int j, bool& ina, bool& inb) {
           const float4 oj = off[j];
-          const float xa = axa - oj.x, ya = aya - oj.y, za = (DIM == 3) ? aza - oj.z : 0.f;
-          const float xb = axb - oj.x, yb = ayb - oj.y, zb = (DIM == 3) ? azb - oj.z : 0.f;
-          ina = xa * xa + ya * ya + za * za <= thr;
-          inb = xb * xb + yb * yb + zb * zb <= thr;
+          const float2 ex = __ffma2_rn(make_float2(oj.x, oj.x), M1, AX);
+          const float2 ey = __ffma2_rn(make_float2(oj.y, oj.y), M1, AY);
+          float2 d2 = __fmul2_rn(ex, ex);
+          d2 = __ffma2_rn(ey, ey, d2);
+          if (DIM == 3) {
+            const float2 ez = __ffma2_rn(make_float2(oj.z, oj.z), M1, AZ);
+            d2 = __ffma2_rn(ez, ez, d2);
+          }
+          ina = d2.x <= thr;
+          inb = d2.y <= thr;
         };
         auto one = [&](int j, bool ena, bool enb) {
           bool ina, inb;
