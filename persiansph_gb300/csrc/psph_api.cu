@@ -556,7 +556,9 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
     }
     gd.hmax = g.hmax;
     for (int d = 0; d < 3; ++d) gd.inv_cell_size32[d] = (float)(1.0 / g.cell_size[d]);
+    for (int d = 0; d < 3; ++d) gd.cell_size32[d] = (float)g.cell_size[d];
     gd.cellfac = (cf.kernel_type == PSPH_QUINTIC_SPLINE) ? 3.0 : 2.0;
+    gd.cellfac2_32 = (float)(gd.cellfac * gd.cellfac);
     g.cellfac = gd.cellfac;
     const long long nci = (long long)gd.nc[0] * gd.nc[1] * gd.nc[2];
     if (nci > (1LL << 28)) return set_err(c, PSPH_ERR_UNSUPPORTED, "grid has more than 2^28 cells");
@@ -624,6 +626,14 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
     if (!(o.mu_u > 0.0)) o.uniform_mu = 0;
   }
   o.inv_h = 1.0 / c->classes[0].h;
+  for (int d = 0; d < 3; ++d) {
+    o.gb[d] = o.gravity[d] + o.body_force[d];
+    o.gravity32[d] = (float)o.gravity[d];
+  }
+  o.inv_h32 = (float)o.inv_h;
+  o.mu_u32 = (float)o.mu_u;
+  o.xsph32 = (float)o.xsph;
+  o.sqrt_h_a32 = (float)o.sqrt_h_a;
   o.nclasses = (int)c->classes.size();
   // neighbour lists: 3D supports hold ~80 (h = 1.3 dx) particles, 2D ~20-44;
   // a particle with more falls back to scanning its cells

@@ -85,6 +85,8 @@ struct GridDev {
   int ncells;     // nc[0]*nc[1]*nc[2]
   int cell_base;  // first global cell id of this instance
   float inv_cell_size32[3];  // 1 / cell_size in FP32 (cell-index estimate of the sort)
+  float cell_size32[3];      // cell_size rounded to FP32 (on the host)
+  float cellfac2_32;         // Cellfac^2 in FP32
 };
 
 // ---------------------------------------------------------------------------

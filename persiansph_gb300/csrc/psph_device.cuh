@@ -94,6 +94,10 @@ struct Options {
   int xsub;           // x-slabs per cell in the sort (1, 2 or 4; psph_autotune)
   double xsph, sqrt_h_a;
   double gravity[3], body_force[3];
+  double gb[3];       // gravity + body force (the sum every pair kernel starts from)
+  // FP32 copies for the FP32C kernels, converted once on the host (a
+  // double-to-float conversion on the device runs on the FP64 pipe)
+  float inv_h32, mu_u32, xsph32, sqrt_h_a32, gravity32[3];
   int shepard_step;
   int nclasses;
   int closure;        // learned eddy-viscosity closure attached

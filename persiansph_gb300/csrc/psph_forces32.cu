@@ -281,7 +281,6 @@ __global__ void __launch_bounds__(kFT32) prepare32_kernel(DevView v) {
 template <int DIM, int KT, int FL>
 __global__ void __maxnreg__(FL == 0 ? 128 : (FL == 1 ? 72 : 96)) forces_fluid32_kernel(DevView v) {
   constexpr bool SPEC = FL != 0;
-  __shared__ double red[32];
   __shared__ unsigned long long cred[32];
   const StepScalars* sc = v.sc;
   if (sc->all_stop) return;
@@ -290,7 +289,7 @@ __global__ void __maxnreg__(FL == 0 ? 128 : (FL == 1 ? 72 : 96)) forces_fluid32_
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const Options& o = v.o;
   const PClass32* __restrict__ CT = v.cls32;
-  double dtc = DBL_MAX;
+  float dtc = FLT_MAX;
   unsigned long long npair2 = 0;
   bool active = false;
   int cell = -1, ci_cls = 0;
@@ -319,9 +318,9 @@ __global__ void __maxnreg__(FL == 0 ? 128 : (FL == 1 ? 72 : 96)) forces_fluid32_
   const bool sr_self = fi & (CF_T0 | CF_LES);
   const bool use_sr = SPEC ? (FL == 2) : (bool)o.need_sr;
   const bool xsph_on = SPEC ? false : o.xsph != 0.0;
-  const float xsph = (float)o.xsph;
+  const float xsph = o.xsph32;
   const float3 cs = cell_size_f(g);
-  const float mu_u = (float)o.mu_u;
+  const float mu_u = o.mu_u32;
   const bool uniform_mu = o.uniform_mu, dyn_mu = o.dyn_mu;
   const int vis_eq = SPEC ? 0 : o.vis_eq, grad_type = SPEC ? 0 : o.grad_type;
   Kahan ax, ay, az, dr;
@@ -330,9 +329,9 @@ __global__ void __maxnreg__(FL == 0 ? 128 : (FL == 1 ? 72 : 96)) forces_fluid32_
   float w01 = 0.f, w02 = 0.f, w12 = 0.f;  // antisymmetric counterpart of the strain-rate sums (closure)
   int nnb = 0;
   const bool closure = o.closure && (fi & CF_LES);
-  const float cf2 = (float)(g.cellfac * g.cellfac);
+  const float cf2 = g.cellfac2_32;
   const bool uniform_h = o.uniform_h;
-  const float ih_u = (float)o.inv_h;
+  const float ih_u = o.inv_h32;
   auto pair = [&](const int j, const int code) {
     const float4 oj = v.S.OFF32[j];
     const int clsj = ld_early(P.cls + j);
@@ -475,9 +474,9 @@ __global__ void __maxnreg__(FL == 0 ? 128 : (FL == 1 ? 72 : 96)) forces_fluid32_
     }
   }
   if (active) {
-    const double axd = o.gravity[0] + o.body_force[0] + ax.value();
-    const double ayd = o.gravity[1] + o.body_force[1] + ay.value();
-    const double azd = o.gravity[2] + o.body_force[2] + az.value();
+    const double axd = o.gb[0] + ax.value();
+    const double ayd = o.gb[1] + ay.value();
+    const double azd = o.gb[2] + az.value();
     const double drd = dr.value();
     v.S.A4[i] = make_double4_32a(axd, ayd, azd, drd);
     v.S.zwab[i] = zw;
@@ -500,15 +499,18 @@ __global__ void __maxnreg__(FL == 0 ? 128 : (FL == 1 ? 72 : 96)) forces_fluid32_
         v.S.cr3[i] = temp > 0.f ? det / (temp * sqrtf(temp)) : 0.f;
       }
     }
-    if (!(isfinite(axd) && isfinite(ayd) && isfinite(azd) && isfinite(drd))) atomicOr(&v.sc->status, ST_NONFINITE);
+    // the FP64 sums are finite exactly when their FP32 parts are (checked in FP32)
+    const float fin = (ax.s - ax.s) + (ax.c - ax.c) + (ay.s - ay.s) + (ay.c - ay.c) + (az.s - az.s) +
+                      (az.c - az.c) + (dr.s - dr.s) + (dr.c - dr.c);
+    if (!(fin == 0.f)) atomicOr(&v.sc->status, ST_NONFINITE);
     // this particle's time-step bound sqrt_h_a sqrt(h/|a|) in FP32; the
-    // minimum over particles and AdaptiveTimeStep stay FP64
+    // minimum over particles (FP32 within a warp) and AdaptiveTimeStep stay FP64
     const float ax32 = (float)axd, ay32 = (float)ayd, az32 = (float)azd;
     const float an = sqrtf(ax32 * ax32 + ay32 * ay32 + az32 * az32);
-    const double cand = (double)((float)o.sqrt_h_a * sqrtf(Ci.h / an));
+    const float cand = o.sqrt_h_a32 * sqrtf(Ci.h / an);
     if (cand < dtc) dtc = cand;
   }
-  block_dt_and_pairs<0>(v, Ci.inst, active, dtc, npair2, red, cred);
+  block_dt32_and_pairs(v, Ci.inst, active, dtc, npair2, cred);
 }
 
 // ---------------------------------------------------------------------------

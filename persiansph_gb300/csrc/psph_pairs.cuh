@@ -171,7 +171,7 @@ PSPH_D void rel_pos(const float3& cs, const float4& oi, const float4& oj, int co
 }
 
 PSPH_HD float3 cell_size_f(const GridDev& g) {
-  return make_float3((float)g.cell_size[0], (float)g.cell_size[1], (float)g.cell_size[2]);
+  return make_float3(g.cell_size32[0], g.cell_size32[1], g.cell_size32[2]);
 }
 
 }  // namespace psph
@@ -264,6 +264,38 @@ PSPH_D void block_dt_and_pairs(const DevView& v, int inst, bool active, double d
     if (c) atomicAdd(&v.sc->pairs_x2, c);
   }
   (void)red;
+}
+
+
+// FP32C form of the same: the candidates are FP32 values, so their minimum is
+// taken in FP32 (FLT_MAX for none) and converted to double once per warp; a
+// conversion is exact and monotonic, so the FP64 minimum is the same value.
+PSPH_D void block_dt32_and_pairs(const DevView& v, int inst, bool active, float dtc, unsigned long long npair2,
+                                 unsigned long long* cred) {
+  const unsigned full = 0xffffffffu;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const unsigned act = __ballot_sync(full, active);
+  if (act) {
+    const int first = __shfl_sync(full, inst, __ffs(act) - 1);
+    const bool uniform = __all_sync(full, !active || inst == first);
+    if (uniform) {
+      float m = active ? dtc : FLT_MAX;
+      for (int off = 16; off > 0; off >>= 1) m = fminf(m, __shfl_down_sync(full, m, off));
+      if (lane == 0 && m < FLT_MAX)
+        atomicMin(&v.inst[first].dtmin_bits, (unsigned long long)__double_as_longlong((double)m));
+    } else if (active && dtc < FLT_MAX) {
+      atomicMin(&v.inst[inst].dtmin_bits, (unsigned long long)__double_as_longlong((double)dtc));
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) npair2 += __shfl_down_sync(full, npair2, off);
+  if (lane == 0) cred[tid >> 5] = npair2;
+  __syncthreads();
+  if (tid == 0) {
+    unsigned long long c = 0;
+    const int nw = (int)(blockDim.x >> 5);
+    for (int k = 0; k < nw; ++k) c += cred[k];
+    if (c) atomicAdd(&v.sc->pairs_x2, c);
+  }
 }
 
 }  // namespace psph
