@@ -677,7 +677,9 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
   if (o.fp32) {
     if ((st = dalloc(c, &S.V32, N)) || (st = dalloc(c, &S.D32, N)) || (st = dalloc(c, &S.NSV32, N))) return st;
     if (dyn_mu && (st = dalloc(c, &S.MU32, N))) return st;
-    if (o.need_sr && !o.has_solid && (st = dalloc(c, &S.cshear, N))) return st;  // FP32 ShearRate (fluid kernel)
+    if (o.need_sr && !o.has_solid &&  // FP32 ShearRate and strain-rate sums of the fluid kernel
+        ((st = dalloc(c, &S.cshear, N)) || (st = dalloc(c, &S.sr32, 6 * N))))
+      return st;
   }
   if (o.fp32 && o.has_solid) {
     if ((st = dalloc(c, &S.SIG32, 2 * N)) || (st = dalloc(c, &S.VB32, N)) || (st = dalloc(c, &S.V32LO, N)))
@@ -971,6 +973,11 @@ psph_status download_impl(psph_ctx* c, int q, psph_particles* out) {
   };
   for (const Src& s : fields) {
     if (!s.out || !s.dev) continue;
+    // the FP32C fluid kernel keeps its strain-rate sums in FP32: expand them first
+    if (s.dev == c->S.strain_rate && c->S.sr32) {
+      launch_expand_sr32(view(c), (int)n, c->stream);
+      CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    }
     if ((st = fetch(s.dev, s.per, b))) return st;
     put(s.out, s.per);
   }

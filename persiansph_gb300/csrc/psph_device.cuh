@@ -66,6 +66,7 @@ struct Scratch {
   float* cvort;          // |vorticity| from the pair sums
   float* cnnb;           // neighbours inside the support
   float* cshear;         // FP32C: ShearRate of the strain-rate sums
+  float* sr32;           // FP32C fluid: the strain-rate sums xx, xy, xz, yy, yz, zz (6 per particle)
   float* cr3;            // FP32C: det(StrainRate) / (StrainRate:StrainRate)^(3/2)
   float* cfeat;          // raw network features, 6 per particle
   double* nut;           // eddy viscosity from the network; -1 = use Smagorinsky
@@ -133,6 +134,7 @@ void launch_nlist(const DevView& v, cudaStream_t st);     // per-step neighbour 
 void launch_prepare(const DevView& v, cudaStream_t st);   // per-particle derived quantities, TIR
 void launch_prepare32(const DevView& v, cudaStream_t st); // FP32C form: copies + wall interpolation
 void launch_forces32(const DevView& v, cudaStream_t st);  // FP32C form: fluid pair forces
+void launch_expand_sr32(const DevView& v, int n, cudaStream_t st);  // sr32 -> the FP64 strain_rate tensors
 void launch_wall(const DevView& v, cudaStream_t st);      // wall interpolation
 void launch_forces(const DevView& v, cudaStream_t st);    // pair forces + per-block dt minimum
 void launch_dt(const DevView& v, cudaStream_t st);        // dt reduction + AdaptiveTimeStep

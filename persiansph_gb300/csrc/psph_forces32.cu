@@ -483,10 +483,11 @@ __global__ void __maxnreg__(FL == 0 ? 128 : (FL == 1 ? 72 : 96)) forces_fluid32_
     if (o.any_shepard) v.S.sumden[i] = sd;
     if (xsph_on) v.S.vxsph4[i] = make_double4_32a(xs0, xs1, xs2, 0.0);
     if (use_sr) {
-      double* out = v.S.strain_rate + 9 * (size_t)i;
-      out[0] = sr0; out[1] = sr1; out[2] = sr2;
-      out[3] = sr1; out[4] = sr4; out[5] = sr5;
-      out[6] = sr2; out[7] = sr5; out[8] = sr8;
+      // the 6 distinct sums in FP32 (the FP64 tensor is built on download)
+      float2* out = reinterpret_cast<float2*>(v.S.sr32 + 6 * (size_t)i);
+      out[0] = make_float2(sr0, sr1);
+      out[1] = make_float2(sr2, sr4);
+      out[2] = make_float2(sr5, sr8);
       // Mat1's ShearRate contraction (Source/Particle.cpp:151-153) of the
       // symmetric sums, in FP32: the update and the closure take it from here
       const float temp = sr0 * sr0 + 2.f * sr1 * sr1 + 2.f * sr2 * sr2 + sr4 * sr4 + 2.f * sr5 * sr5 + sr8 * sr8;
@@ -801,6 +802,23 @@ void launch_prepare32(const DevView& v, cudaStream_t st) {
   }
   if (v.o.dim == 2) prepare32_dispatch<2>(v, st);
   else prepare32_dispatch<3>(v, st);
+}
+
+namespace {
+__global__ void expand_sr32_kernel(const float* __restrict__ sr32, double* __restrict__ sr, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float* a = sr32 + 6 * (size_t)i;
+  double* o = sr + 9 * (size_t)i;
+  o[0] = a[0]; o[1] = a[1]; o[2] = a[2];
+  o[3] = a[1]; o[4] = a[3]; o[5] = a[4];
+  o[6] = a[2]; o[7] = a[4]; o[8] = a[5];
+}
+}  // namespace
+
+void launch_expand_sr32(const DevView& v, int n, cudaStream_t st) {
+  if (n > 0 && v.S.sr32 && v.S.strain_rate)
+    expand_sr32_kernel<<<(n + 255) / 256, 256, 0, st>>>(v.S.sr32, v.S.strain_rate, n);
 }
 
 void launch_forces32(const DevView& v, cudaStream_t st) {
