@@ -50,9 +50,9 @@ FLOPS_PER_DIRECTED_PAIR = 90
 # Algorithmic HBM bytes per particle of one FP32C fluid pair-kernel launch:
 # read each particle's inputs once (offset+h 16, v+p 16, 1/rho, p/rho^2, c, rho
 # 16, class 4, cell 4) and write its outputs once (a + drho 32, zwab 8, sumden
-# 8) = 104 B; with LES and the closure also the viscosity (4), the strain rate
-# (72) and the closure's four features (16) = 196 B.
-FORCE32_BYTES_PER_PARTICLE = {False: 104, True: 196}
+# 8) = 104 B; with LES and the closure also the viscosity (4), the strain-rate
+# sums (6 x 4) and the closure's four features (16) = 148 B.
+FORCE32_BYTES_PER_PARTICLE = {False: 104, True: 148}
 # DRAM bytes per particle one launch actually moved: ncu captures of the same
 # kernels on the same tank at dx = 10 mm (1,021,104 particles),
 # dram__bytes_read.sum + dram__bytes_write.sum per particle (LES + closure
