@@ -206,6 +206,7 @@ DevView view(psph_ctx* c) {
   v.sc = c->d_sc;
   v.alive = c->d_alive;
   v.ncap = c->ncap;
+  v.nl_stride = nl_stride_of(c->ncap);
   v.nclasses = (int)c->classes.size();
   return v;
 }
@@ -671,7 +672,7 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
       (st = dalloc(c, &S.sumkernel, N)) || (st = dalloc(c, &S.nsv4, N)) || (st = dalloc(c, &S.vxsph4, N)) ||
       (st = dalloc(c, &S.shear_rate, N)) || (st = dalloc(c, &S.sbar, N)))
     return st;
-  if ((st = dalloc(c, &S.nl, (size_t)o.nl_cap * N))) return st;
+  if ((st = dalloc(c, &S.nl, (size_t)o.nl_cap * nl_stride_of(c->ncap)))) return st;
   if (o.need_sr || o.has_solid)
     if ((st = dalloc(c, &S.strain_rate, 9 * N))) return st;
   if (o.fp32) {

@@ -105,6 +105,10 @@ struct Options {
   double closure_dx;  // lattice spacing of its h/dx feature
 };
 
+// Chunk stride of the neighbour lists (nl_slot permutes particles inside
+// blocks of 64): the capacity rounded up to a multiple of 64.
+inline int nl_stride_of(int ncap) { return (ncap + 63) & ~63; }
+
 // Everything a launch needs, passed by value to the launch wrappers.
 struct DevView {
   const GridDev* grids;   // per instance (device array)
@@ -120,6 +124,7 @@ struct DevView {
   StepScalars* sc;
   uint8_t* alive;
   int ncap;
+  int nl_stride;          // neighbour-list chunk stride: ncap rounded up to a multiple of 64 (nl_slot)
   int nclasses;
 };
 

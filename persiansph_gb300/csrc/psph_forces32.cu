@@ -215,8 +215,8 @@ __global__ void __launch_bounds__(kFT32) prepare32_kernel(DevView v) {
   };
   const int cnt = (wall && cell >= 0) ? v.S.nl_count[w] : 0;
   if (cnt >= 0) {  // the neighbour list, 4 entries per 16-byte load
-    const int4* __restrict__ nl4 = reinterpret_cast<const int4*>(v.S.nl) + w;
-    const size_t N = (size_t)v.ncap;
+    const int4* __restrict__ nl4 = reinterpret_cast<const int4*>(v.S.nl) + nl_slot(w);
+    const size_t N = (size_t)v.nl_stride;
     const int nch = (cnt + 3) >> 2;
     for (int c = 0; c < nch; ++c) {
       const int4 q = nl4[(size_t)c * N];
@@ -442,8 +442,8 @@ __global__ void __maxnreg__(FL == 0 ? 128 : (FL == 1 ? 72 : 96)) forces_fluid32_
   };
   const int cnt = (active && cell >= 0) ? v.S.nl_count[i] : 0;
   if (cnt >= 0) {
-    const int4* __restrict__ nl4 = reinterpret_cast<const int4*>(v.S.nl) + i;
-    const size_t N = (size_t)v.ncap;
+    const int4* __restrict__ nl4 = reinterpret_cast<const int4*>(v.S.nl) + nl_slot(i);
+    const size_t N = (size_t)v.nl_stride;
     const int nch = (cnt + 3) >> 2;
     // the strain-rate flavour loads the next chunk one chunk ahead (measured:
     // it helps there and costs the plain flavour a little)

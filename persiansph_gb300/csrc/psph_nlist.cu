@@ -7,11 +7,10 @@
 // (cell offset, FP32 offset) separations with a margin on r^2 (0.02 % for the
 // FP32C form, 0.4 % for the FP64 form); the pair kernels then apply the exact
 // test of their form. Lists are written in 16-byte chunks of 4 entries, chunk-
-// major across particles (nl_index), so a warp reading chunk c of 32
-// consecutive particles touches 512 contiguous bytes and each store fills
-// half a sector. The
-// scan is cheap integer/FP32 work; the pair kernels then walk lists of nearly
-// equal length instead of branching per candidate.
+// major across particles (nl_index / nl_slot), so every store and every
+// reader's load covers whole 32-byte sectors. The scan is cheap integer/FP32
+// work; the pair kernels then walk lists of nearly equal length instead of
+// branching per candidate.
 #include <algorithm>
 
 #include "psph_pairs.cuh"
@@ -28,7 +27,7 @@ constexpr int kNT = 128;
 // one, and a completed chunk goes out as one 16-byte store.
 struct ListWriter {
   int* rp;    // this lane's slot 0; slot s at rp[s * kNT]
-  int4* out;  // the next chunk to write; chunk c of particle i at nl + c * N + i
+  int4* out;  // the next chunk to write; chunk c of particle i at nl + c * stride + nl_slot(i)
   int k = 0;  // entries kept
   // the entry goes to the next free slot for every candidate and is kept (k
   // advances) only when the candidate is inside
@@ -41,14 +40,14 @@ struct ListWriter {
   __device__ __forceinline__ void flush(int k0, int cap, int N) {
     if (((k0 ^ k) & 4) && k0 < cap) {
       const int b = (k0 & 4) * kNT;
-      *out = make_int4(rp[b], rp[b + kNT], rp[b + 2 * kNT], rp[b + 3 * kNT]);
+      __stcs(out, make_int4(rp[b], rp[b + kNT], rp[b + 2 * kNT], rp[b + 3 * kNT]));
       out += N;
     }
   }
   __device__ __forceinline__ void finish(int cap, int* count) {
     if (k <= cap && (k & 3)) {  // last, partial chunk
       const int b = (k & 4) * kNT;
-      *out = make_int4(rp[b], rp[b + kNT], rp[b + 2 * kNT], rp[b + 3 * kNT]);
+      __stcs(out, make_int4(rp[b], rp[b + kNT], rp[b + 2 * kNT], rp[b + 3 * kNT]));
     }
     *count = (k <= cap) ? k : -1;
   }
@@ -87,10 +86,10 @@ __device__ __forceinline__ void list_one(const DevView& v, int i, float margin, 
   const float cf = (float)g.cellfac;
   // support test r^2 <= (Cellfac hb)^2 margin; with one h everywhere it is a constant
   const float thr_u = cf * cf * oi.w * oi.w * margin;
-  const int N = v.ncap, cap = v.o.nl_cap;
+  const int N = v.nl_stride, cap = v.o.nl_cap;
   const CellCoord c = decode(g, cell);
   const float4* __restrict__ off = v.S.OFF32;
-  ListWriter w{rp, reinterpret_cast<int4*>(v.S.nl) + i};
+  ListWriter w{rp, reinterpret_cast<int4*>(v.S.nl) + nl_slot(i)};
   const bool inner = c.x > 0 && c.x < g.nc[0] - 1 && c.y > 0 && c.y < g.nc[1] - 1 &&
                      (DIM == 2 || (c.z > 0 && c.z < g.nc[2] - 1));
   const bool cull = UNIFORM_H && inner;
@@ -216,12 +215,12 @@ __global__ void __launch_bounds__(kNT, 8) nlist_pair_kernel(DevView v, float mar
   const float4 ob = pair ? v.S.OFF32[ib] : make_float4(kFar, kFar, kFar, oa.w);
   const float cf = (float)g.cellfac;
   const float thr = cf * cf * oa.w * oa.w * margin;
-  const int N = v.ncap, cap = v.o.nl_cap;
+  const int N = v.nl_stride, cap = v.o.nl_cap;
   const CellCoord c = decode(g, cell);
   const float4* __restrict__ off = v.S.OFF32;
   int4* const nl4 = reinterpret_cast<int4*>(v.S.nl);
-  ListWriter wa{&ring[0][0][threadIdx.x], nl4 + ia};
-  ListWriter wb{&ring[1][0][threadIdx.x], nl4 + ib};
+  ListWriter wa{&ring[0][0][threadIdx.x], nl4 + nl_slot(ia)};
+  ListWriter wb{&ring[1][0][threadIdx.x], nl4 + nl_slot(ib)};
   const bool cull = c.x > 0 && c.x < g.nc[0] - 1 && c.y > 0 && c.y < g.nc[1] - 1 &&
                     (DIM == 2 || (c.z > 0 && c.z < g.nc[2] - 1));
   const float thr_cull = thr * 1.0001f;

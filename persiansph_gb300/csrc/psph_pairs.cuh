@@ -15,10 +15,18 @@ constexpr int kCodeShift = 26;  // neighbour-list entry: index | code << 26 (ind
 constexpr int kIndexMask = (1 << kCodeShift) - 1;
 
 // Neighbour-list layout: chunks of 4 consecutive entries of one particle (16
-// bytes), chunk-major across particles, so entry k of particle i sits at
-// ((k / 4) * ncap + i) * 4 + k % 4. A lane writes and reads whole chunks, and
-// chunk c of a warp's 32 consecutive particles is 512 contiguous bytes.
-PSPH_HD size_t nl_index(int ncap, int i, int k) { return (((size_t)(k >> 2) * ncap + i) << 2) + (k & 3); }
+// bytes), chunk-major across particles: chunk c of particle i is int4 number
+// c * stride + nl_slot(i), so entry k sits at ((k / 4) * stride + nl_slot(i)) * 4
+// + k % 4. Inside each block of 64 particles the even ones take slots 0-31 and
+// the odd ones slots 32-63: the list scan, whose lanes own particles 2t and
+// 2t+1, stores chunk c of a warp's even (odd) particles as 512 contiguous
+// bytes, and a reader warp of 32 consecutive particles loads two runs of 256
+// bytes; every access covers whole 32-byte sectors. stride = capacity rounded
+// up to a multiple of 64.
+PSPH_HD int nl_slot(int i) { return (i & ~63) | ((i & 1) << 5) | ((i >> 1) & 31); }
+PSPH_HD size_t nl_index(int stride, int i, int k) {
+  return (((size_t)(k >> 2) * stride + nl_slot(i)) << 2) + (k & 3);
+}
 
 struct CellCoord {
   int x, y, z;
@@ -204,7 +212,7 @@ struct NbrSource {
   PSPH_D int next(const DevView& v, int* code) {
     if (cnt >= 0) {
       if (k >= cnt) return -1;
-      const int e = v.S.nl[nl_index(v.ncap, i, k)];
+      const int e = v.S.nl[nl_index(v.nl_stride, i, k)];
       ++k;
       *code = e >> kCodeShift;
       return e & kIndexMask;
