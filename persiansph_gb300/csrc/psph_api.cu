@@ -43,6 +43,11 @@ struct psph_ctx {
   bool own_stream = false;
   int ncap = 0;
   std::vector<int64_t> inst_off;  // original-index range [inst_off[q], inst_off[q+1]) of instance q
+  // download scratch (allocated at the first download): output row of each
+  // sorted particle, its scan, and a staging buffer in the caller's layout
+  int *dl_flag = nullptr, *dl_rank = nullptr, *dl_row = nullptr, *dl_bs = nullptr;
+  double* dl_buf = nullptr;
+  int dl_width = 0;
   std::vector<PClass> classes;
   Options opt{};
   std::vector<GridDev> gdevs;
@@ -122,27 +127,70 @@ double eos_host(int eq, double cs, double p0, double rho, double rho0) {
   }
 }
 
+// Threads for the per-particle host loops of an upload (one per ~200k
+// particles, at most the hardware's).
+int host_threads(int64_t n) {
+  const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+  return (int)std::max<int64_t>(1, std::min<int64_t>(hw, n / 200000 + 1));
+}
+
+template <class F>
+void run_threads(int n, F&& f) {
+  if (n <= 1) {
+    f(0);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (int t = 1; t < n; ++t) th.emplace_back(f, t);
+  f(0);
+  for (auto& x : th) x.join();
+}
+
 // CellInitiate (Source/Domain.cpp:549-660) for one instance.
 psph_status cell_initiate(psph_ctx* c, const psph_config& cf, const psph_particles* p, psph_grid& g,
                           double* mu_max, double* cs_max) {
   const int64_t n = p->n;
+  // extremes over the particles, per thread chunk then merged (the same
+  // comparisons, so the result does not depend on the split)
+  struct Ext {
+    double TRPR[3], BLPF[3], hmax, rhomax, mu_max, cs_max;
+  };
+  const int nth = host_threads(n);
+  std::vector<Ext> part(nth);
+  run_threads(nth, [&](int t) {
+    Ext& E = part[t];
+    for (int d = 0; d < 3; ++d) E.TRPR[d] = E.BLPF[d] = p->x[d];
+    E.hmax = p->h[0];
+    E.rhomax = p->density[0];
+    E.mu_max = E.cs_max = 0.0;
+    for (int64_t i = n * t / nth; i < n * (t + 1) / nth; ++i) {
+      for (int d = 0; d < 3; ++d) {
+        const double xd = p->x[3 * i + d];
+        if (xd > E.TRPR[d]) E.TRPR[d] = xd;
+        if (xd < E.BLPF[d]) E.BLPF[d] = xd;
+      }
+      if (p->h[i] > E.hmax) E.hmax = p->h[i];
+      if (p->density[i] > E.rhomax) E.rhomax = p->density[i];
+      const double mu = dflt(p->mu, i, 0.0), cs = dflt(p->cs, i, 0.0);
+      if (mu > E.mu_max) E.mu_max = mu;
+      if (cs > E.cs_max) E.cs_max = cs;
+    }
+  });
   double TRPR[3], BLPF[3];
   for (int d = 0; d < 3; ++d) TRPR[d] = BLPF[d] = p->x[d];
   double hmax = p->h[0];
   double rhomax = p->density[0];
   *mu_max = 0.0;
   *cs_max = 0.0;
-  for (int64_t i = 0; i < n; ++i) {
+  for (const Ext& E : part) {
     for (int d = 0; d < 3; ++d) {
-      const double xd = p->x[3 * i + d];
-      if (xd > TRPR[d]) TRPR[d] = xd;
-      if (xd < BLPF[d]) BLPF[d] = xd;
+      if (E.TRPR[d] > TRPR[d]) TRPR[d] = E.TRPR[d];
+      if (E.BLPF[d] < BLPF[d]) BLPF[d] = E.BLPF[d];
     }
-    if (p->h[i] > hmax) hmax = p->h[i];
-    if (p->density[i] > rhomax) rhomax = p->density[i];
-    const double mu = dflt(p->mu, i, 0.0), cs = dflt(p->cs, i, 0.0);
-    if (mu > *mu_max) *mu_max = mu;
-    if (cs > *cs_max) *cs_max = cs;
+    if (E.hmax > hmax) hmax = E.hmax;
+    if (E.rhomax > rhomax) rhomax = E.rhomax;
+    if (E.mu_max > *mu_max) *mu_max = E.mu_max;
+    if (E.cs_max > *cs_max) *cs_max = E.cs_max;
   }
   for (int d = 0; d < 3; ++d) {
     if (cf.dom_max[d] > TRPR[d]) TRPR[d] = cf.dom_max[d];
@@ -340,24 +388,6 @@ psph_status create_impl(const psph_config* cfgs, int ninst, psph_ctx** out) {
   return PSPH_OK;
 }
 
-// Threads for the per-particle host loops of an upload (one per ~200k
-// particles, at most the hardware's).
-int host_threads(int64_t n) {
-  const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
-  return (int)std::max<int64_t>(1, std::min<int64_t>(hw, n / 200000 + 1));
-}
-
-template <class F>
-void run_threads(int n, F&& f) {
-  if (n <= 1) {
-    f(0);
-    return;
-  }
-  std::vector<std::thread> th;
-  for (int t = 1; t < n; ++t) th.emplace_back(f, t);
-  f(0);
-  for (auto& x : th) x.join();
-}
 
 psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
   if (!c || !parts) return PSPH_ERR_INVALID_ARGUMENT;
@@ -384,12 +414,20 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
   // de-duplicates the parameter sets of its contiguous chunk; the chunks'
   // tables merge in chunk order, so class ids do not depend on scheduling.
   bool dyn_mu = false;
-  for (int q = 0; q < ninst && !dyn_mu; ++q)
-    for (int64_t i = 0; i < parts[q].n; ++i)
-      if (dflt(parts[q].t0, i, 0.0) > 0.0 || iflt(parts[q].les, i, 0)) {
-        dyn_mu = true;
-        break;
-      }
+  for (int q = 0; q < ninst && !dyn_mu; ++q) {
+    const psph_particles& pq = parts[q];
+    if (!pq.t0 && !pq.les) continue;
+    const int nth = host_threads(pq.n);
+    std::vector<char> found(nth, 0);
+    run_threads(nth, [&](int t) {
+      for (int64_t i = pq.n * t / nth; i < pq.n * (t + 1) / nth; ++i)
+        if (dflt(pq.t0, i, 0.0) > 0.0 || iflt(pq.les, i, 0)) {
+          found[t] = 1;
+          break;
+        }
+    });
+    for (char f : found) dyn_mu = dyn_mu || f;
+  }
   std::vector<int> cls(ntot);
   std::vector<double> pressure(ntot);
   struct Worker {
@@ -719,44 +757,40 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
 
   // ---- pack and copy --------------------------------------------------------------
   {
-    std::vector<double4_32a> X(N), V(N), H(N), Hb(lf ? N : 0);
-    std::vector<int> orig(N);
-    std::vector<double> mu(dyn_mu ? N : 0);
-    const bool two_d = (k.dimension == 2);
-    const int nthreads_pack = host_threads(ntot);
-    run_threads(nthreads_pack, [&](int t) {
-      const int64_t g0 = ntot * t / nthreads_pack, g1 = ntot * (t + 1) / nthreads_pack;
-      int q = 0;
-      while (q + 1 < ninst && g0 >= c->inst_off[q + 1]) ++q;
-      for (int64_t g = g0; g < g1; ++g) {
-        while (g >= c->inst_off[q + 1]) ++q;
-        const psph_particles* p = &parts[q];
-        const int64_t i = g - c->inst_off[q];
-        const double* x = p->x + 3 * i;
-        const double vx = dflt(p->v, 3 * i, 0.0), vy = dflt(p->v, 3 * i + 1, 0.0),
-                     vz = two_d ? 0.0 : dflt(p->v, 3 * i + 2, 0.0);
-        X[g] = make_double4_32a(x[0], x[1], x[2], p->density[i]);
-        V[g] = make_double4_32a(vx, vy, vz, pressure[g]);
-        if (lf) {
-          H[g] = make_double4_32a(dflt(p->va, 3 * i, 0.0), dflt(p->va, 3 * i + 1, 0.0), dflt(p->va, 3 * i + 2, 0.0),
-                                  dflt(p->densitya, i, 0.0));
-          Hb[g] = make_double4_32a(dflt(p->vb, 3 * i, 0.0), dflt(p->vb, 3 * i + 1, 0.0), dflt(p->vb, 3 * i + 2, 0.0),
-                                   dflt(p->densityb, i, 0.0));
-        } else {
-          H[g] = make_double4_32a(dflt(p->vb, 3 * i, 0.0), dflt(p->vb, 3 * i + 1, 0.0), dflt(p->vb, 3 * i + 2, 0.0),
-                                  dflt(p->densityb, i, 0.0));
-        }
-        orig[g] = (int)g;
-        if (dyn_mu) mu[g] = dflt(p->mu, i, 0.0);
-      }
-    });
-    CUDA_TRY(c, cudaMemcpy(c->PA.X4, X.data(), N * sizeof(double4_32a), cudaMemcpyHostToDevice));
-    CUDA_TRY(c, cudaMemcpy(c->PA.V4, V.data(), N * sizeof(double4_32a), cudaMemcpyHostToDevice));
-    CUDA_TRY(c, cudaMemcpy(c->PA.H4, H.data(), N * sizeof(double4_32a), cudaMemcpyHostToDevice));
-    if (lf) CUDA_TRY(c, cudaMemcpy(c->PA.H4b, Hb.data(), N * sizeof(double4_32a), cudaMemcpyHostToDevice));
-    CUDA_TRY(c, cudaMemcpy(c->PA.cls, cls.data(), N * sizeof(int), cudaMemcpyHostToDevice));
-    CUDA_TRY(c, cudaMemcpy(c->PA.orig, orig.data(), N * sizeof(int), cudaMemcpyHostToDevice));
-    if (dyn_mu) CUDA_TRY(c, cudaMemcpy(c->PA.mu, mu.data(), N * sizeof(double), cudaMemcpyHostToDevice));
+    // The caller's arrays go to the device as they are, into the neighbour-list
+    // buffer (free until the first step; 17 doubles per particle fit in its
+    // >= 256 bytes), and upload_pack_kernel builds the persistent layout.
+    const size_t NN = N;
+    double* const sx = reinterpret_cast<double*>(c->S.nl);  // x (3N)
+    double* const sd = sx + 3 * NN;                         // density
+    double* const sp = sd + NN;                             // initial pressure (from the host loop above)
+    double* const sv = sp + NN;                             // v (3N)
+    double* const sh1 = sv + 3 * NN;                        // the scheme's history: va (Leapfrog) or vb
+    double* const sh1s = sh1 + 3 * NN;                      // densitya or densityb
+    double* const sh2 = sh1s + NN;                          // Leapfrog vb
+    double* const sh2s = sh2 + 3 * NN;                      // Leapfrog densityb
+    double* const smu = sh2s + NN;                          // mu
+    auto put = [&](double* dst, const double* src, size_t cnt) -> psph_status {
+      if (src) CUDA_TRY(c, cudaMemcpyAsync(dst, src, cnt * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+      else CUDA_TRY(c, cudaMemsetAsync(dst, 0, cnt * sizeof(double), c->stream));  // the constructor's zero
+      return PSPH_OK;
+    };
+    for (int q = 0; q < ninst; ++q) {
+      const psph_particles* p = &parts[q];
+      const size_t off = (size_t)c->inst_off[q], m = (size_t)p->n;
+      if ((st = put(sx + 3 * off, p->x, 3 * m)) || (st = put(sd + off, p->density, m)) ||
+          (st = put(sv + 3 * off, p->v, 3 * m)) || (st = put(sh1 + 3 * off, lf ? p->va : p->vb, 3 * m)) ||
+          (st = put(sh1s + off, lf ? p->densitya : p->densityb, m)))
+        return st;
+      if (lf && ((st = put(sh2 + 3 * off, p->vb, 3 * m)) || (st = put(sh2s + off, p->densityb, m)))) return st;
+      if (dyn_mu && (st = put(smu + off, p->mu, m))) return st;
+    }
+    if ((st = put(sp, pressure.data(), NN))) return st;
+    launch_upload_pack(sx, sd, sp, sv, sh1, sh1s, sh2, sh2s, smu, c->PA, (int)N, k.dimension == 2, lf, dyn_mu,
+                       c->stream);
+    CUDA_TRY(c, cudaMemcpyAsync(c->PA.cls, cls.data(), N * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaMemsetAsync(c->d_alive, 1, N, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     if (o.has_solid) {
       // Mat3 neither reads nor writes the ShearStress history: a soil domain
       // whose uploaded history is zero does not carry it through the sort
@@ -785,8 +819,6 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
             CUDA_TRY(c, cudaMemcpy(dsts[a] + off, srcs[a], 9 * (size_t)p->n * sizeof(double), cudaMemcpyHostToDevice));
       }
     }
-    std::vector<uint8_t> alive(N, 1);
-    CUDA_TRY(c, cudaMemcpy(c->d_alive, alive.data(), N, cudaMemcpyHostToDevice));
     CUDA_TRY(c, cudaMemcpy(c->d_cls, c->classes.data(), c->classes.size() * sizeof(PClass), cudaMemcpyHostToDevice));
     launch_class_constants(c->d_cls, (int)c->classes.size(), o.dim, c->stream);
     CUDA_TRY(c, cudaGetLastError());
@@ -901,121 +933,136 @@ psph_status alive_of(psph_ctx* c, int q, std::vector<std::pair<int, int>>& order
   return PSPH_OK;
 }
 
+// Download on the device: each sorted particle's output row (its rank by
+// original index among the instance's alive particles, Array::DelItems'
+// order), then per requested field one gather into a staging buffer laid out
+// as the caller's array and one copy into that array.
+__global__ void dl_flag_kernel(const uint8_t* __restrict__ alive, const int* __restrict__ orig, int n, int lo,
+                               int hi, int* __restrict__ flag) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n && alive[s] && orig[s] >= lo && orig[s] < hi) flag[orig[s] - lo] = 1;
+}
+__global__ void dl_row_kernel(const uint8_t* __restrict__ alive, const int* __restrict__ orig, int n, int lo, int hi,
+                              const int* __restrict__ rank, int* __restrict__ row) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) row[s] = (alive[s] && orig[s] >= lo && orig[s] < hi) ? rank[orig[s] - lo] : -1;
+}
+// dst[row * width + e] = src[s * stride + off + e]
+__global__ void dl_gather_kernel(const double* __restrict__ src, int stride, int off, int width,
+                                 double* __restrict__ dst, const int* __restrict__ row, int n) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const int r = row[s];
+  if (r < 0) return;
+  for (int e = 0; e < width; ++e) dst[(size_t)r * width + e] = src[(size_t)s * stride + off + e];
+}
+// a class constant (int or double at byte offset off of PClass) per row
+__global__ void dl_class_kernel(const PClass* __restrict__ tab, const int* __restrict__ cls, size_t off, int is_int,
+                                void* __restrict__ dst, const int* __restrict__ row, int n) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const int r = row[s];
+  if (r < 0) return;
+  const char* rec = reinterpret_cast<const char*>(tab + cls[s]) + off;
+  if (is_int) static_cast<int32_t*>(dst)[r] = *reinterpret_cast<const int*>(rec);
+  else static_cast<double*>(dst)[r] = *reinterpret_cast<const double*>(rec);
+}
+
 psph_status download_impl(psph_ctx* c, int q, psph_particles* out) {
   if (!c || !out) return PSPH_ERR_INVALID_ARGUMENT;
   if (!c->uploaded) return set_err(c, PSPH_ERR_STATE, "psph_download before psph_upload");
   if (q < 0 || q >= c->ninst) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "instance %d out of range", q);
-  std::vector<std::pair<int, int>> order;
-  std::vector<int> cls;
   psph_status st;
-  if ((st = alive_of(c, q, order, &cls))) return st;
-  const size_t n = (size_t)c->h_sc->n;
+  if ((st = sync_scalars(c))) return st;
+  const int n = c->h_sc->n;
   const Persist& P = c->h_sc->buf ? c->PB : c->PA;
   const Options& o = c->opt;
   const bool lf = (o.scheme == PSPH_LEAPFROG);
-  const int64_t m = (int64_t)order.size();
+  cudaStream_t s = c->stream;
+  const size_t N = (size_t)c->ncap;
+  if (!c->dl_row) {
+    if ((st = dalloc(c, &c->dl_flag, N + 1)) || (st = dalloc(c, &c->dl_rank, N + 1)) ||
+        (st = dalloc(c, &c->dl_row, N)) || (st = dalloc(c, &c->dl_bs, N / 1024 + 2)))
+      return st;
+  }
+  const int lo = (int)c->inst_off[q], hi = (int)c->inst_off[q + 1], len = hi - lo;
+  const int nb = n > 0 ? (n + 255) / 256 : 1;
+  CUDA_TRY(c, cudaMemsetAsync(c->dl_flag, 0, sizeof(int) * (size_t)(len + 1), s));
+  if (n > 0) dl_flag_kernel<<<nb, 256, 0, s>>>(c->d_alive, P.orig, n, lo, hi, c->dl_flag);
+  launch_exclusive_scan(c->dl_flag, c->dl_rank, len, c->dl_bs, s);
+  if (n > 0) dl_row_kernel<<<nb, 256, 0, s>>>(c->d_alive, P.orig, n, lo, hi, c->dl_rank, c->dl_row);
+  int m32 = 0;
+  CUDA_TRY(c, cudaMemcpyAsync(&m32, c->dl_rank + len, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(c, cudaStreamSynchronize(s));
+  const int64_t m = m32;
   if (out->n < m)
     return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "output holds %lld particles, need %lld", (long long)out->n, (long long)m);
   out->n = m;
-  auto fetch4 = [&](const double4_32a* src, std::vector<double4_32a>& dst) -> psph_status {
-    dst.resize(n);
-    CUDA_TRY(c, cudaMemcpy(dst.data(), src, n * sizeof(double4_32a), cudaMemcpyDeviceToHost));
-    return PSPH_OK;
+  if (m == 0) return PSPH_OK;
+
+  // (destination, source, source stride, offset, width)
+  struct F { double* out; const double* dev; int stride, off, width; };
+  auto d4 = [](const double4_32a* p) { return reinterpret_cast<const double*>(p); };
+  const F fields[] = {
+      {out->x, d4(P.X4), 4, 0, 3}, {out->density, d4(P.X4), 4, 3, 1},
+      {out->v, d4(P.V4), 4, 0, 3}, {out->pressure, d4(P.V4), 4, 3, 1},
+      {lf ? out->va : out->vb, d4(P.H4), 4, 0, 3}, {lf ? out->densitya : out->densityb, d4(P.H4), 4, 3, 1},
+      {lf ? out->vb : nullptr, d4(P.H4b), 4, 0, 3}, {lf ? out->densityb : nullptr, d4(P.H4b), 4, 3, 1},
+      {out->a, d4(c->S.A4), 4, 0, 3}, {out->ddensity, d4(c->S.A4), 4, 3, 1},
+      {out->nsv, d4(c->S.nsv4), 4, 0, 3}, {out->vxsph, d4(c->S.vxsph4), 4, 0, 3},
+      {out->zwab, c->S.zwab, 1, 0, 1}, {out->sumden, c->S.sumden, 1, 0, 1}, {out->sumkernel, c->S.sumkernel, 1, 0, 1},
+      {out->shear_rate, c->S.shear_rate, 1, 0, 1}, {out->sbar, c->S.sbar, 1, 0, 1},
+      {out->mu, o.dyn_mu ? P.mu : nullptr, 1, 0, 1},
+      {out->strain_rate, c->S.strain_rate, 9, 0, 9}, {out->rotation_rate, c->S.rotation_rate, 9, 0, 9},
+      {out->sigma, P.sigma, 9, 0, 9}, {out->strain, P.strain, 9, 0, 9}, {out->shear_stress, P.shear, 9, 0, 9},
+      {out->tir, P.tir, 9, 0, 9},
+      {lf ? out->sigmaa : out->sigmab, P.sigma_h, 9, 0, 9}, {lf ? out->sigmab : nullptr, c->S.sigma_o, 9, 0, 9},
+      {lf ? out->straina : out->strainb, P.strain_h, 9, 0, 9}, {lf ? out->strainb : nullptr, c->S.strain_o, 9, 0, 9},
+      {lf ? out->shear_stressa : out->shear_stressb, P.shear_h, 9, 0, 9},
+      {lf ? out->shear_stressb : nullptr, c->S.shear_o, 9, 0, 9},
   };
-  auto fetch = [&](const double* src, size_t per, std::vector<double>& dst) -> psph_status {
-    dst.resize(n * per);
-    CUDA_TRY(c, cudaMemcpy(dst.data(), src, n * per * sizeof(double), cudaMemcpyDeviceToHost));
-    return PSPH_OK;
-  };
-  std::vector<double4_32a> b4;
-  const int nth = host_threads(m);
-  auto put4 = [&](double* vec3, double* scal) {
-    run_threads(nth, [&](int t) {
-      for (int64_t r = m * t / nth; r < m * (t + 1) / nth; ++r) {
-        const double4_32a w = b4[order[r].second];
-        if (vec3) {
-          vec3[3 * r] = w.x;
-          vec3[3 * r + 1] = w.y;
-          vec3[3 * r + 2] = w.z;
-        }
-        if (scal) scal[r] = w.w;
-      }
-    });
-  };
-  if (out->x || out->density) { if ((st = fetch4(P.X4, b4))) return st; put4(out->x, out->density); }
-  if (out->v || out->pressure) { if ((st = fetch4(P.V4, b4))) return st; put4(out->v, out->pressure); }
-  if (lf) {
-    if (out->va || out->densitya) { if ((st = fetch4(P.H4, b4))) return st; put4(out->va, out->densitya); }
-    if (out->vb || out->densityb) { if ((st = fetch4(P.H4b, b4))) return st; put4(out->vb, out->densityb); }
-  } else {
-    if (out->vb || out->densityb) { if ((st = fetch4(P.H4, b4))) return st; put4(out->vb, out->densityb); }
+  int width = 1;
+  for (const F& f : fields)
+    if (f.out && f.dev && f.width > width) width = f.width;
+  if (width > c->dl_width) {
+    if ((st = dalloc(c, &c->dl_buf, N * (size_t)width))) return st;
+    c->dl_width = width;
   }
-  if (out->a || out->ddensity) { if ((st = fetch4(c->S.A4, b4))) return st; put4(out->a, out->ddensity); }
-  if (out->nsv) { if ((st = fetch4(c->S.nsv4, b4))) return st; put4(out->nsv, nullptr); }
-  if (out->vxsph) { if ((st = fetch4(c->S.vxsph4, b4))) return st; put4(out->vxsph, nullptr); }
-  std::vector<double> b;
-  auto put = [&](double* dst, size_t per) {
-    run_threads(nth, [&](int t) {
-      for (int64_t r = m * t / nth; r < m * (t + 1) / nth; ++r)
-        for (size_t e = 0; e < per; ++e) dst[per * r + e] = b[per * order[r].second + e];
-    });
-  };
-  struct Src { double* out; const double* dev; size_t per; };
-  const Src fields[] = {
-      {out->zwab, c->S.zwab, 1}, {out->sumden, c->S.sumden, 1}, {out->sumkernel, c->S.sumkernel, 1},
-      {out->shear_rate, c->S.shear_rate, 1}, {out->sbar, c->S.sbar, 1},
-      {out->mu, o.dyn_mu ? P.mu : nullptr, 1},
-      {out->strain_rate, c->S.strain_rate, 9}, {out->rotation_rate, c->S.rotation_rate, 9},
-      {out->sigma, P.sigma, 9}, {out->strain, P.strain, 9}, {out->shear_stress, P.shear, 9}, {out->tir, P.tir, 9},
-      {lf ? out->sigmaa : out->sigmab, P.sigma_h, 9}, {lf ? out->sigmab : nullptr, c->S.sigma_o, 9},
-      {lf ? out->straina : out->strainb, P.strain_h, 9}, {lf ? out->strainb : nullptr, c->S.strain_o, 9},
-      {lf ? out->shear_stressa : out->shear_stressb, P.shear_h, 9},
-      {lf ? out->shear_stressb : nullptr, c->S.shear_o, 9},
-  };
-  for (const Src& s : fields) {
-    if (!s.out || !s.dev) continue;
+  for (const F& f : fields) {
+    if (!f.out || !f.dev) continue;
     // the FP32C fluid kernel keeps its strain-rate sums in FP32: expand them first
-    if (s.dev == c->S.strain_rate && c->S.sr32) {
-      launch_expand_sr32(view(c), (int)n, c->stream);
-      CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-    }
-    if ((st = fetch(s.dev, s.per, b))) return st;
-    put(s.out, s.per);
+    if (f.dev == c->S.strain_rate && c->S.sr32) launch_expand_sr32(view(c), n, s);
+    dl_gather_kernel<<<nb, 256, 0, s>>>(f.dev, f.stride, f.off, f.width, c->dl_buf, c->dl_row, n);
+    CUDA_TRY(c, cudaMemcpyAsync(f.out, c->dl_buf, (size_t)m * f.width * sizeof(double), cudaMemcpyDeviceToHost, s));
   }
-  for (int64_t r = 0; r < m; ++r) {  // class constants
-    const PClass& C = c->classes[cls[order[r].second]];
-    if (out->id) out->id[r] = C.id;
-    if (out->material) out->material[r] = C.material;
-    if (out->is_free) out->is_free[r] = C.is_free;
-    if (out->no_slip) out->no_slip[r] = C.no_slip;
-    if (out->pres_eq) out->pres_eq[r] = C.pres_eq;
-    if (out->shepard) out->shepard[r] = C.shepard;
-    if (out->les) out->les[r] = C.les;
-    if (out->vis_m) out->vis_m[r] = C.vis_m;
-    if (out->fail) out->fail[r] = C.fail;
-    if (out->mass) out->mass[r] = C.mass;
-    if (out->h) out->h[r] = C.h;
-    if (out->cs) out->cs[r] = C.cs;
-    if (out->p0) out->p0[r] = C.p0;
-    if (out->ref_density) out->ref_density[r] = C.rho0;
-    if (out->fpmassc) out->fpmassc[r] = C.fpmassc;
-    if (out->alpha) out->alpha[r] = C.alpha;
-    if (out->beta) out->beta[r] = C.beta;
-    if (out->mu && !o.dyn_mu) out->mu[r] = C.mu0;
-    if (out->mu_ref) out->mu_ref[r] = C.mu_ref;
-    if (out->t0) out->t0[r] = C.t0;
-    if (out->bingham_m) out->bingham_m[r] = C.bm;
-    if (out->csmag) out->csmag[r] = C.csmag;
-    if (out->ti) out->ti[r] = C.ti;
-    if (out->tin) out->tin[r] = C.tin;
-    if (out->ti_init_dist) out->ti_init_dist[r] = C.tid;
-    if (out->g_mod) out->g_mod[r] = C.g_mod;
-    if (out->k_mod) out->k_mod[r] = C.k_mod;
-    if (out->sigmay) out->sigmay[r] = C.sigmay;
-    if (out->cohesion) out->cohesion[r] = C.coh;
-    if (out->phi) out->phi[r] = C.phi;
-    if (out->psi) out->psi[r] = C.psi;
+  // class constants, gathered from the device class table
+  struct K { void* out; size_t off; int is_int; };
+  const K consts[] = {
+      {out->id, offsetof(PClass, id), 1}, {out->material, offsetof(PClass, material), 1},
+      {out->is_free, offsetof(PClass, is_free), 1}, {out->no_slip, offsetof(PClass, no_slip), 1},
+      {out->pres_eq, offsetof(PClass, pres_eq), 1}, {out->shepard, offsetof(PClass, shepard), 1},
+      {out->les, offsetof(PClass, les), 1}, {out->vis_m, offsetof(PClass, vis_m), 1},
+      {out->fail, offsetof(PClass, fail), 1},
+      {out->mass, offsetof(PClass, mass), 0}, {out->h, offsetof(PClass, h), 0}, {out->cs, offsetof(PClass, cs), 0},
+      {out->p0, offsetof(PClass, p0), 0}, {out->ref_density, offsetof(PClass, rho0), 0},
+      {out->fpmassc, offsetof(PClass, fpmassc), 0}, {out->alpha, offsetof(PClass, alpha), 0},
+      {out->beta, offsetof(PClass, beta), 0}, {o.dyn_mu ? nullptr : out->mu, offsetof(PClass, mu0), 0},
+      {out->mu_ref, offsetof(PClass, mu_ref), 0}, {out->t0, offsetof(PClass, t0), 0},
+      {out->bingham_m, offsetof(PClass, bm), 0}, {out->csmag, offsetof(PClass, csmag), 0},
+      {out->ti, offsetof(PClass, ti), 0}, {out->tin, offsetof(PClass, tin), 0},
+      {out->ti_init_dist, offsetof(PClass, tid), 0}, {out->g_mod, offsetof(PClass, g_mod), 0},
+      {out->k_mod, offsetof(PClass, k_mod), 0}, {out->sigmay, offsetof(PClass, sigmay), 0},
+      {out->cohesion, offsetof(PClass, coh), 0}, {out->phi, offsetof(PClass, phi), 0},
+      {out->psi, offsetof(PClass, psi), 0},
+  };
+  for (const K& k : consts) {
+    if (!k.out) continue;
+    dl_class_kernel<<<nb, 256, 0, s>>>(c->d_cls, P.cls, k.off, k.is_int, c->dl_buf, c->dl_row, n);
+    CUDA_TRY(c, cudaMemcpyAsync(k.out, c->dl_buf, (size_t)m * (k.is_int ? sizeof(int32_t) : sizeof(double)),
+                                cudaMemcpyDeviceToHost, s));
   }
+  CUDA_TRY(c, cudaStreamSynchronize(s));
+  CUDA_TRY(c, cudaGetLastError());
   return PSPH_OK;
 }
 

@@ -158,6 +158,10 @@ void launch_pairs_export(const DevView& v, int which, long long* out, long long 
 namespace psph {
 // Pieces of the two-pass pair export (scratch supplied by the caller).
 void launch_exclusive_scan(const int* in, int* out, int len, int* block_sums, cudaStream_t st);
+// upload: the caller's arrays, copied to the device as they are, into the persistent layout
+void launch_upload_pack(const double* sx, const double* sd, const double* sp, const double* sv, const double* sh1,
+                        const double* sh1s, const double* sh2, const double* sh2s, const double* smu, const Persist& P,
+                        int n, bool two_d, bool lf, bool dyn_mu, cudaStream_t st);
 void launch_pairs_count(const DevView& v, int which, int* counts, cudaStream_t st);
 void launch_pairs_write(const DevView& v, int which, const int* offsets, long long* out, long long cap,
                         cudaStream_t st);

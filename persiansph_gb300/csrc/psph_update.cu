@@ -383,6 +383,34 @@ void launch_class_constants(PClass* cls, int n, int dim, cudaStream_t st) {
   if (n > 0) class_constants_kernel<<<(n + 127) / 128, 128, 0, st>>>(cls, n, dim);
 }
 
+namespace {
+// Upload: the caller's arrays (copied as they are) into the persistent
+// double4 layout, the particle's original index = its position.
+__global__ void upload_pack_kernel(const double* __restrict__ sx, const double* __restrict__ sd,
+                                   const double* __restrict__ sp, const double* __restrict__ sv,
+                                   const double* __restrict__ sh1, const double* __restrict__ sh1s,
+                                   const double* __restrict__ sh2, const double* __restrict__ sh2s,
+                                   const double* __restrict__ smu, Persist P, int n, int two_d, int lf, int dyn_mu) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n) return;
+  const size_t g3 = 3 * (size_t)g;
+  P.X4[g] = make_double4_32a(sx[g3], sx[g3 + 1], sx[g3 + 2], sd[g]);
+  P.V4[g] = make_double4_32a(sv[g3], sv[g3 + 1], two_d ? 0.0 : sv[g3 + 2], sp[g]);
+  P.H4[g] = make_double4_32a(sh1[g3], sh1[g3 + 1], sh1[g3 + 2], sh1s[g]);
+  if (lf) P.H4b[g] = make_double4_32a(sh2[g3], sh2[g3 + 1], sh2[g3 + 2], sh2s[g]);
+  P.orig[g] = g;
+  if (dyn_mu) P.mu[g] = smu[g];
+}
+}  // namespace
+
+void launch_upload_pack(const double* sx, const double* sd, const double* sp, const double* sv, const double* sh1,
+                        const double* sh1s, const double* sh2, const double* sh2s, const double* smu, const Persist& P,
+                        int n, bool two_d, bool lf, bool dyn_mu, cudaStream_t st) {
+  if (n > 0)
+    upload_pack_kernel<<<(n + 255) / 256, 256, 0, st>>>(sx, sd, sp, sv, sh1, sh1s, sh2, sh2s, smu, P, n, two_d, lf,
+                                                        dyn_mu);
+}
+
 int launches_per_step(const DevView& v) {
   return (v.o.fp32 ? 17 : 16) + (v.o.closure ? 1 : 0);
 }
