@@ -17,6 +17,7 @@
 #include <cstring>
 #include <string>
 #include <thread>
+#include <unistd.h>
 #include <unordered_map>
 #include <vector>
 
@@ -1024,6 +1025,25 @@ psph_status download_impl(psph_ctx* c, int q, psph_particles* out) {
   int width = 1;
   for (const F& f : fields)
     if (f.out && f.dev && f.width > width) width = f.width;
+  {
+    // Fresh output pages are populated here by host threads in parallel (one
+    // write per page; the copies overwrite them): a device copy into
+    // untouched pageable memory would take each page fault in turn.
+    std::vector<std::pair<char*, size_t>> ranges;
+    for (const F& f : fields)
+      if (f.out && f.dev) ranges.emplace_back(reinterpret_cast<char*>(f.out), (size_t)m * f.width * sizeof(double));
+    size_t total = 0;
+    for (const auto& r : ranges) total += r.second;
+    const size_t page = (size_t)std::max(4096L, sysconf(_SC_PAGESIZE));
+    const int nth = host_threads((int64_t)(total / 64));
+    if (nth > 1)
+      run_threads(nth, [&](int t) {
+        for (const auto& r : ranges) {
+          const size_t a = r.second * t / nth, b = r.second * (t + 1) / nth;
+          for (size_t off = a; off < b; off += page) reinterpret_cast<volatile char*>(r.first)[off] = 0;
+        }
+      });
+  }
   if (width > c->dl_width) {
     if ((st = dalloc(c, &c->dl_buf, N * (size_t)width))) return st;
     c->dl_width = width;
