@@ -231,16 +231,38 @@ __global__ void reorder_kernel(DevView v, const int* __restrict__ perm, const in
     cellid[s] = (k < nbins) ? k / xsub : -1;
     alive[s] = 1;
     if (dyn_mu) dst.mu[s] = src.mu[i];
-    if (has_solid) {
-      const double* srcs[7] = {src.sigma, src.sigma_h, src.strain, src.strain_h, src.shear, src.tir, src.shear_h};
-      double* dsts[7] = {dst.sigma, dst.sigma_h, dst.strain, dst.strain_h, dst.shear, dst.tir, dst.shear_h};
-      // the ShearStress history serves Mat2 only (a zero history of a soil domain stays behind)
-      const int nt = v.o.carry_shear_h ? 7 : 6;
+  }
+}
+
+// The 3x3 tensors of solids (9 doubles a row) in the new order, a warp per 32
+// rows: lane l moves words l, l+32, ... of the warp's 288, so the stores are
+// contiguous and the loads too wherever the permutation keeps neighbours
+// together (it mostly does: particles move little between steps).
+__global__ void reorder_tensors_kernel(DevView v, const int* __restrict__ perm, const int* __restrict__ start,
+                                       const StepScalars* sc, int nbins) {
+  if (sc->all_stop) return;
+  const Persist& src = cur_persist(v);
+  const Persist& dst = next_persist(v);
+  const int n_new = start[nbins + 1];
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const double* srcs[7] = {src.sigma, src.sigma_h, src.strain, src.strain_h, src.shear, src.tir, src.shear_h};
+  double* dsts[7] = {dst.sigma, dst.sigma_h, dst.strain, dst.strain_h, dst.shear, dst.tir, dst.shear_h};
+  // the ShearStress history serves Mat2 only (a zero history of a soil domain stays behind)
+  const int nt = v.o.carry_shear_h ? 7 : 6;
+  for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; 32 * w < n_new; w += nwarps) {
+    const int base = 32 * w;
+    const int rows = min(32, n_new - base);
+    const int mine = lane < rows ? perm[base + lane] : 0;  // the source row of this lane's destination row
+    for (int a = 0; a < nt; ++a) {
+      const double* __restrict__ sa = srcs[a];
+      double* __restrict__ da = dsts[a] + 9 * (size_t)base;
 #pragma unroll
-      for (int a = 0; a < 7; ++a) {
-        if (a >= nt) break;
-#pragma unroll
-        for (int e = 0; e < 9; ++e) dsts[a][9 * (size_t)s + e] = srcs[a][9 * (size_t)i + e];
+      for (int k = 0; k < 9; ++k) {
+        const int word = lane + 32 * k;       // of the warp's 288
+        const int r = word / 9, e = word - 9 * r;
+        const int from = __shfl_sync(0xffffffffu, mine, r & 31);
+        if (r < rows) da[word] = sa[9 * (size_t)from + e];
       }
     }
   }
@@ -310,6 +332,7 @@ void launch_sort(const DevView& v, cudaStream_t st) {
   rank_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(S.key, sstart, S.tmp_perm, v, S.perm, v.sc, nbins);
   reorder_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(v, S.perm, S.key, sstart, S.cellid, v.alive, v.sc, nbins, xsub,
                                                     v.o.has_solid, v.o.dyn_mu);
+  if (v.o.has_solid) reorder_tensors_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(v, S.perm, sstart, v.sc, nbins);
   finish_sort_kernel<<<1, 1, 0, st>>>(sstart, v.sc, nbins);
   cell_starts_kernel<<<grid_for(ncells + 3), kBT, 0, st>>>(sstart, S.start, ncells, xsub, v.sc, S.tmp_perm, v.ncap);
 }

@@ -366,9 +366,9 @@ void launch_update(const DevView& v, cudaStream_t st) {
   else update_kernel<3><<<nb > 0 ? nb : 1, kUT, 0, st>>>(v);
 }
 
-// begin, bin, 3 scan, scatter, rank, reorder, finish, cell starts, neighbour
-// lists, prepare (2 in the FP32C form: copies + walls), forces, closure, dt,
-// update, end
+// begin, bin, 3 scan, scatter, rank, reorder (+ the solids' tensors), finish,
+// cell starts, neighbour lists, prepare (2 in the FP32C form: copies + walls),
+// forces, closure, dt, update, end
 namespace {
 __global__ void class_constants_kernel(PClass* cls, int n, int dim) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -412,7 +412,7 @@ void launch_upload_pack(const double* sx, const double* sd, const double* sp, co
 }
 
 int launches_per_step(const DevView& v) {
-  return (v.o.fp32 ? 17 : 16) + (v.o.closure ? 1 : 0);
+  return (v.o.fp32 ? 17 : 16) + (v.o.closure ? 1 : 0) + (v.o.has_solid ? 1 : 0);
 }
 
 }  // namespace psph
