@@ -114,13 +114,11 @@ constexpr int kQN = 16;  // queued FP64 pair evaluations per lane between flushe
 // ---------------------------------------------------------------------------
 template <int DIM, int KT>
 __global__ void __launch_bounds__(kFT) prepare_wall_kernel(DevView v) {
-  __shared__ int qbuf[kQN][kFT];
   const StepScalars* sc = v.sc;
   if (sc->all_stop) return;
   const Persist& P = cur_persist(v);
   const int n = sc->n;
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
-  const int tid = threadIdx.x;
   const Options& o = v.o;
   const PClass* __restrict__ CT = v.cls;
   const int winst = (w < n) ? CT[P.cls[w]].inst : 0;
@@ -159,63 +157,64 @@ __global__ void __launch_bounds__(kFT) prepare_wall_kernel(DevView v) {
   const bool any_periodic = g.periodic[0] | g.periodic[1] | g.periodic[2];
   const double gx = o.gravity[0], gy = o.gravity[1], gz = o.gravity[2];
   const bool need_orient = !o.wallp_physical && (gx != 0.0 || gy != 0.0 || gz != 0.0) && mat < 3;
-  NbrSource<DIM> src;
-  src.init(v, g, w, wall && cell >= 0, 1.004f);
-  bool more = wall && cell >= 0;
   const CellCoord cw = decode(g, cell >= 0 ? cell : 0);
-  while (true) {
-    int qn = 0;
-    while (more && qn < kQN) {
+  // one neighbour (a free particle of the same material contributes): its
+  // position and velocity loads go out with its class, ahead of the class test
+  auto visit = [&](const int f, const int fcode) {
+    const int clsf = P.cls[f];
+    const double4_32a xf = P.X4[f];
+    const double4_32a vf = P.V4[f];
+    const PClass& Cf = CT[clsf];
+    if (!Cf.is_free || Cf.material != mat) return;
+    const double hb = (hw + Cf.h) / 2.0;
+    CellCoord cf = cw;
+    if (any_periodic) cf = decode(g, v.S.cellid[f]);
+    const bool wfirst = need_orient ? first_of_pair_code(fcode, ow, P.orig[f]) : true;
+    double x0, x1, x2;
+    if (wfirst) {
+      x0 = xw.x - xf.x; x1 = xw.y - xf.y; x2 = xw.z - xf.z;
+      if (any_periodic) periodic_fix(g, x0, x1, x2, hb, cw, cf);
+    } else {
+      x0 = xf.x - xw.x; x1 = xf.y - xw.y; x2 = xf.z - xw.z;
+      if (any_periodic) periodic_fix(g, x0, x1, x2, hb, cf, cw);
+    }
+    const double r = sqrt(x0 * x0 + x1 * x1 + x2 * x2);
+    const double inv_hb = o.uniform_h ? o.inv_h : 1.0 / hb;
+    const double q = r * inv_hb;
+    const double ih2 = inv_hb * inv_hb;
+    const double K = Kern<DIM, KT>::W(q, Kern<DIM, KT>::cw() * (DIM == 2 ? ih2 : ih2 * inv_hb));
+    if (K == 0.0) return;
+    sk += K;
+    if (mat < 3) p += vf.w * K + (gx * x0 + gy * x1 + gz * x2) * xf.w * K;
+    if (mat > 1) {
+      const double* sf = P.sigma + 9 * (size_t)f;
+#pragma unroll
+      for (int e = 0; e < 9; ++e) sig[e] += sf[e] * K;
+    }
+    if (noslip) { n0 += vf.x * K; n1 += vf.y * K; n2 += vf.z * K; }
+  };
+  const int cnt = (wall && cell >= 0) ? v.S.nl_count[w] : 0;
+  if (cnt >= 0) {  // the neighbour list, 4 entries per 16-byte load
+    const int4* __restrict__ nl4 = reinterpret_cast<const int4*>(v.S.nl) + nl_slot(w);
+    const size_t N = (size_t)v.nl_stride;
+    const int nch = (cnt + 3) >> 2;
+    for (int ch = 0; ch < nch; ++ch) {
+      const int4 qe = nl4[(size_t)ch * N];
+      const int rem = cnt - 4 * ch;
+      visit(qe.x & kIndexMask, qe.x >> kCodeShift);
+      if (rem > 1) visit(qe.y & kIndexMask, qe.y >> kCodeShift);
+      if (rem > 2) visit(qe.z & kIndexMask, qe.z >> kCodeShift);
+      if (rem > 3) visit(qe.w & kIndexMask, qe.w >> kCodeShift);
+    }
+  } else {  // list overflow: scan the cells
+    NbrSource<DIM> src;
+    src.init(v, g, w, true, 1.004f);
+    while (true) {
       int code;
       const int f = src.next(v, &code);
-      if (f < 0) {
-        more = false;
-        break;
-      }
-      qbuf[qn++][tid] = f | (code << kCodeShift);
+      if (f < 0) break;
+      visit(f, code);
     }
-    const int qmax = __reduce_max_sync(0xffffffffu, qn);
-    for (int k = 0; k < qmax; ++k) {
-      if (k >= qn) continue;
-      const int fe = qbuf[k][tid];
-      const int f = fe & kIndexMask, fcode = fe >> kCodeShift;
-      const PClass& Cf = CT[P.cls[f]];
-      if (!Cf.is_free || Cf.material != mat) continue;
-      const double4_32a xf = P.X4[f];
-      const double hb = (hw + Cf.h) / 2.0;
-      CellCoord cf = cw;
-      if (any_periodic) cf = decode(g, v.S.cellid[f]);
-      const bool wfirst = need_orient ? first_of_pair_code(fcode, ow, P.orig[f]) : true;
-      double x0, x1, x2;
-      if (wfirst) {
-        x0 = xw.x - xf.x; x1 = xw.y - xf.y; x2 = xw.z - xf.z;
-        if (any_periodic) periodic_fix(g, x0, x1, x2, hb, cw, cf);
-      } else {
-        x0 = xf.x - xw.x; x1 = xf.y - xw.y; x2 = xf.z - xw.z;
-        if (any_periodic) periodic_fix(g, x0, x1, x2, hb, cf, cw);
-      }
-      const double r = sqrt(x0 * x0 + x1 * x1 + x2 * x2);
-      const double inv_hb = o.uniform_h ? o.inv_h : 1.0 / hb;
-      const double q = r * inv_hb;
-      const double ih2 = inv_hb * inv_hb;
-      const double K = Kern<DIM, KT>::W(q, Kern<DIM, KT>::cw() * (DIM == 2 ? ih2 : ih2 * inv_hb));
-      if (K == 0.0) continue;
-      sk += K;
-      if (mat < 3) {
-        const double4_32a vf = P.V4[f];
-        p += vf.w * K + (gx * x0 + gy * x1 + gz * x2) * xf.w * K;
-      }
-      if (mat > 1) {
-        const double* sf = P.sigma + 9 * (size_t)f;
-#pragma unroll
-        for (int e = 0; e < 9; ++e) sig[e] += sf[e] * K;
-      }
-      if (noslip) {
-        const double4_32a vf = P.V4[f];
-        n0 += vf.x * K; n1 += vf.y * K; n2 += vf.z * K;
-      }
-    }
-    if (!__any_sync(0xffffffffu, more)) break;
   }
   if (!wall) return;
   const PClass& Cw = CT[P.cls[w]];
