@@ -84,3 +84,9 @@ def test_particle_leaving_the_domain_is_removed(gpu):
     orig = gd.original_index()
     assert k not in set(orig.tolist())
     assert gd.n == len(orig) < n0
+    # downloaded rows follow original_index after the removal: fixed wall
+    # particles never move, so their rows hold exactly their uploaded positions
+    got = gd.download_fields(("x", "is_free"))
+    walls = got["is_free"] == 0
+    assert walls.sum() > 0
+    np.testing.assert_array_equal(got["x"][walls], x[orig[walls]])
