@@ -39,6 +39,10 @@ struct PClass {
   // device once after upload with the same expressions the return mapping
   // used per particle (zero while the table is built on the host)
   double dp_alpha, dp_kf, dp_sin_psi;
+  // Tait EOS constants of the class for the FP32C update (class_constants_kernel):
+  // B = rho0 cs^2 / 7 (the reference's expression), 1/rho0, B in FP32
+  double eos_b, eos_inv_rho0;
+  float eos_b32;
   int material, is_free, no_slip, pres_eq, shepard, les, vis_m, fail, id, inst;
 };
 
