@@ -155,6 +155,12 @@ def test_fp32c_single_step_parity_1e5(gpu, name):
         ed = np.max(np.abs(g["ddensity"] - r["ddensity"])[free] / (dr_scale[free] + 1e-30))
         assert ea <= 1e-5, f"{name} {warm}: FP32C acceleration rel err {ea:.3e}"
         assert ed <= 1e-5, f"{name} {warm}: FP32C density-rate rel err {ed:.3e}"
+        # the step's pressure (the FP32C update's EOS, from the FP64 density),
+        # relative to the largest pressure (absolute when every pressure is 0)
+        dp = np.max(np.abs(g["pressure"] - r["pressure"])[free])
+        pmax = np.max(np.abs(r["pressure"][free]))
+        ep = dp / pmax if pmax > 0.0 else dp
+        assert ep <= 1e-5, f"{name} {warm}: FP32C pressure rel err {ep:.3e}"
 
 
 SOLID_CASES = ["granular", "granular_lf_fail3", "solid_block"]
