@@ -56,12 +56,12 @@ FORCE32_BYTES_PER_PARTICLE = {False: 104, True: 148}
 # DRAM bytes per particle one launch actually moved: ncu captures of the same
 # kernels on the same tank at dx = 10 mm (1,021,104 particles),
 # dram__bytes_read.sum + dram__bytes_write.sum per particle (LES + closure
-# flavour: 269.45 + 56.42 MB); the traffic grows with the particle count, so
+# flavour: 271.24 + 56.53 MB); the traffic grows with the particle count, so
 # a full-size launch moves this x n.
-FORCE32_TRAFFIC_BYTES_PER_PARTICLE = {False: 304.6, True: 319.1}
+FORCE32_TRAFFIC_BYTES_PER_PARTICLE = {False: 304.6, True: 321.0}
 # Pipe activity of that launch (LES + closure flavour) and of the FP64 pair
 # kernel in the same capture series (sm__pipe_*_cycles_active, % of peak).
-FORCE32_NCU = {"issue_active": 0.634, "fma_pipe": 0.343, "fp64_pipe": 0.040, "warps_active": 0.297}
+FORCE32_NCU = {"issue_active": 0.640, "fma_pipe": 0.346, "fp64_pipe": 0.040, "warps_active": 0.297}
 FORCE64_NCU_FP64_PIPE = 0.854
 
 
