@@ -11,6 +11,9 @@
 // reader's load covers whole 32-byte sectors. The scan is cheap integer/FP32
 // work; the pair kernels then walk lists of nearly equal length instead of
 // branching per candidate.
+//
+// With one h everywhere (nlist_pair_kernel) a lane scans for two particles of
+// one cell at once; otherwise (nlist_kernel) a lane scans for one particle.
 #include <algorithm>
 
 #include "psph_pairs.cuh"
