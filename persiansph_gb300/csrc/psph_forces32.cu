@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(kFT32) prepare32_kernel(DevView v) {
     }
   }
   const float3 cs = cell_size_f(g);
-  const float gx = (float)o.gravity[0], gy = (float)o.gravity[1], gz = (float)o.gravity[2];
+  const float gx = o.gravity32[0], gy = o.gravity32[1], gz = o.gravity32[2];
   const bool need_orient = !o.wallp_physical && (gx != 0.f || gy != 0.f || gz != 0.f);
   float sk = 0.f, p = 0.f, n0 = 0.f, n1 = 0.f, n2 = 0.f;
   const float hw = oi.w;
