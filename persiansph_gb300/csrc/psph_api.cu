@@ -1150,7 +1150,7 @@ void psph_destroy(psph_ctx* c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
   free_all(c);
-  for (int i = 0; i < 6; ++i)
+  for (int i = 0; i <= kNumPhases; ++i)
     if (c->ev[i]) cudaEventDestroy(c->ev[i]);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
