@@ -229,13 +229,18 @@ psph_status psph_pair_count(psph_ctx* ctx, uint64_t* pairs);
  * device-wide synchronisation). Same pairs as psph_pairs_export, written as
  * (first, second) int64 couples into the caller's DEVICE buffer pairs_device
  * (at most cap pairs, in sorted-particle order); *n_total (host) receives the
- * full count. Its scratch is one static device array for at most
- * PSPH_NOALLOC_MAX_PARTICLES particles (about 8 MB, kept by every GPU that
- * loads the library until exit); larger contexts get PSPH_ERR_INVALID_ARGUMENT.
- * The first call on a device looks up that array's device address: make it
- * before any stream capture. Calls share the array, so calls that overlap on
+ * full count, also when cap < count (truncated output) or cap = 0 (count
+ * only; pairs_device may then be NULL). Its scratch is one static device
+ * array for at most PSPH_NOALLOC_MAX_PARTICLES particles (about 8 MB, kept by
+ * every GPU that loads the library until exit); larger contexts, and exports
+ * of more than PSPH_NOALLOC_MAX_PAIRS pairs (its offsets are 32-bit), get
+ * PSPH_ERR_INVALID_ARGUMENT with nothing written. The first call on a device
+ * looks up that array's device address (once per device, safe from several
+ * threads): make it before any stream capture, and do not use the entry point
+ * across a cudaDeviceReset. Calls share the array, so calls that overlap on
  * the GPU race. */
 #define PSPH_NOALLOC_MAX_PARTICLES (1 << 20)
+#define PSPH_NOALLOC_MAX_PAIRS 2147483647
 psph_status psph_pairs_export_noalloc(psph_ctx* ctx, int which, int64_t* pairs_device, int64_t cap,
                                       int64_t* n_total);
 

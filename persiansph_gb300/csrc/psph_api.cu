@@ -19,6 +19,7 @@
 #include <thread>
 #include <unistd.h>
 #include <unordered_map>
+#include <mutex>
 #include <vector>
 
 #include "psph_device.cuh"
@@ -285,17 +286,16 @@ void enqueue_step(psph_ctx* c) {
   record_phase(c, 7);
 }
 
-// Clears every instance's stop flag and the status word on the stream, with
-// no stop time (used before a pair export, which sorts but does not step).
+// Clears every instance's stop flag on the stream, with no stop time (used
+// before a pair export, which sorts but does not step). The status word is
+// left as the last step set it: an export does not hide a pending error, and
+// psph_step clears it when it arms the next run.
 __global__ void rearm_kernel(InstState* inst, int ninst, StepScalars* sc) {
   for (int k = threadIdx.x; k < ninst; k += blockDim.x) {
     inst[k].stop = 0;
     inst[k].t_stop = 1e300;
   }
-  if (threadIdx.x == 0) {
-    sc->status = 0;
-    sc->all_stop = 0;
-  }
+  if (threadIdx.x == 0) sc->all_stop = 0;
 }
 
 psph_status sync_scalars(psph_ctx* c) {
@@ -1476,32 +1476,62 @@ psph_status psph_batch_get_integrator(const psph_ctx* c, int inst, psph_integrat
 //
 // The array's host-side name is only a stand-in for the device symbol, so the
 // address passed to the kernels is taken with cudaGetSymbolAddress, once per
-// device, by the first call on that device (with that device current); make
-// that first call before any stream capture. Every call shares the array and
-// overwrites what it needs (nothing in it has to start at zero); two calls
-// whose work overlaps on the GPU (different streams, or contexts used from
-// several threads) race on it.
+// device (std::call_once, so threads making their first call at the same time
+// are safe), by the first call on that device (with that device current); make
+// that first call before any stream capture. The address is kept for the
+// process: after cudaDeviceReset the module is loaded again and the kept
+// address is stale, so the entry point is not for use across a device reset.
+// Every call shares the array and overwrites what it needs (nothing in it has
+// to start at zero); two calls whose work overlaps on the GPU (different
+// streams, or contexts used from several threads) race on it.
+//
+// The offsets are 32-bit: the pair total is summed in 64 bits first, and a
+// total above INT_MAX (PSPH_NOALLOC_MAX_PAIRS) is refused before any pair is
+// written.
 // ---------------------------------------------------------------------------
 namespace {
 
 constexpr int kNoallocBlocks = (PSPH_NOALLOC_MAX_PARTICLES + 1023) / 1024 + 2;
-// counts[MAX] | offsets[MAX + 1] | scan block sums
-static __device__ __align__(256) int g_noalloc_scratch[2 * PSPH_NOALLOC_MAX_PARTICLES + 1 + kNoallocBlocks];
+constexpr int kNoallocHead = 64;  // ints before the counts: the 64-bit pair total, 256-byte aligned
+// total (64-bit) | counts[MAX] | offsets[MAX + 1] | scan block sums
+static __device__ __align__(256) int
+    g_noalloc_scratch[kNoallocHead + 2 * PSPH_NOALLOC_MAX_PARTICLES + 1 + kNoallocBlocks];
 
 constexpr int kMaxDevices = 64;
+std::once_flag g_noalloc_once[kMaxDevices];
 int* g_noalloc_addr[kMaxDevices] = {};
+cudaError_t g_noalloc_err[kMaxDevices] = {};
 
 psph_status noalloc_scratch(psph_ctx* c, int** out) {
   int dev = -1;
   CUDA_TRY(c, cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) return set_err(c, PSPH_ERR_NO_DEVICE, "device index %d out of range", dev);
-  if (!g_noalloc_addr[dev]) {
+  std::call_once(g_noalloc_once[dev], [dev] {
     void* p = nullptr;
-    CUDA_TRY(c, cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_err[dev] = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     g_noalloc_addr[dev] = (int*)p;
-  }
+  });
+  if (g_noalloc_err[dev] != cudaSuccess || !g_noalloc_addr[dev])
+    return set_err(c, PSPH_ERR_CUDA, "cudaGetSymbolAddress of the static pair-export scratch: %s",
+                   cudaGetErrorString(g_noalloc_err[dev]));
   *out = g_noalloc_addr[dev];
   return PSPH_OK;
+}
+
+// The pair total in 64 bits (one block, a fixed reduction order).
+__global__ void __launch_bounds__(1024) noalloc_total_kernel(const int* __restrict__ counts, int n,
+                                                             unsigned long long* total) {
+  __shared__ unsigned long long part[32];
+  unsigned long long s = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += (unsigned)counts[i];
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long t = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += part[k];
+    *total = t;
+  }
 }
 
 }  // namespace
@@ -1518,20 +1548,31 @@ extern "C" psph_status psph_pairs_export_noalloc(psph_ctx* c, int which, int64_t
   int* scratch = nullptr;
   psph_status st = noalloc_scratch(c, &scratch);
   if (st) return st;
-  int* counts = scratch;
-  int* offsets = scratch + PSPH_NOALLOC_MAX_PARTICLES;
+  unsigned long long* d_total = reinterpret_cast<unsigned long long*>(scratch);
+  int* counts = scratch + kNoallocHead;
+  int* offsets = counts + PSPH_NOALLOC_MAX_PARTICLES;
   int* block_sums = offsets + PSPH_NOALLOC_MAX_PARTICLES + 1;
   cudaStream_t s = c->stream;
   rearm_kernel<<<1, 256, 0, s>>>(c->d_inst, c->ninst, c->d_sc);
   const DevView v = view(c);
   launch_sort(v, s);                                   // cell list of the current positions
   launch_pairs_count(v, which, counts, s);             // pairs each sorted particle lists first
-  launch_exclusive_scan(counts, offsets, c->ncap, block_sums, s);
-  launch_pairs_write(v, which, offsets, (long long*)pairs_device, (long long)cap, s);
+  noalloc_total_kernel<<<1, 1024, 0, s>>>(counts, c->ncap, d_total);
   CUDA_TRY(c, cudaGetLastError());
-  int total = 0;
-  CUDA_TRY(c, cudaMemcpyAsync(&total, offsets + c->ncap, sizeof(int), cudaMemcpyDeviceToHost, s));
+  unsigned long long total = 0;
+  CUDA_TRY(c, cudaMemcpyAsync(&total, d_total, sizeof total, cudaMemcpyDeviceToHost, s));
   CUDA_TRY(c, cudaStreamSynchronize(s));
-  if (n_total) *n_total = total;
+  if (total > (unsigned long long)PSPH_NOALLOC_MAX_PAIRS)
+    return set_err(c, PSPH_ERR_INVALID_ARGUMENT,
+                   "psph_pairs_export_noalloc: %llu pairs exceed its 32-bit offsets (at most %d); use "
+                   "psph_pairs_export",
+                   total, PSPH_NOALLOC_MAX_PAIRS);
+  if (cap > 0 && total > 0) {
+    launch_exclusive_scan(counts, offsets, c->ncap, block_sums, s);
+    launch_pairs_write(v, which, offsets, (long long*)pairs_device, (long long)cap, s);
+    CUDA_TRY(c, cudaGetLastError());
+    CUDA_TRY(c, cudaStreamSynchronize(s));
+  }
+  if (n_total) *n_total = (int64_t)total;
   return PSPH_OK;
 }

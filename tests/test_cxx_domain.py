@@ -69,15 +69,28 @@ def test_driver_builds_and_reports_missing_device(bindir):
     assert "Fatal: no sm_103 CUDA device available" in res.stdout
 
 
+def reference_dir():
+    """The reference checkout: PSPH_REFERENCE_DIR, else the directory the
+    oracle recipe (oracle/build_ref.sh) built the reference from."""
+    env = os.environ.get("PSPH_REFERENCE_DIR")
+    if env:
+        return env
+    rec = os.path.join(REPO, "oracle", "_ref", "REFERENCE_DIR")
+    if os.path.exists(rec):
+        with open(rec) as f:
+            return f.read().strip()
+    return None
+
+
 REFERENCE_DRIVERS = ("1-Poiseuille.cpp", "2-Couette.cpp", "3-DamBreak.cpp", "4-DamBreak3D.cpp")
 
 
 @pytest.mark.parametrize("name", REFERENCE_DRIVERS)
 def test_reference_drivers_compile_unchanged(bindir, name):
     """The reference's own example drivers, read where the reference is
-    checked out (PSPH_REFERENCE_DIR), compile against this Domain.h."""
-    ref = os.environ.get("PSPH_REFERENCE_DIR", "/root/reference")
-    src = os.path.join(ref, name)
+    checked out (PSPH_REFERENCE_DIR, else where oracle/build_ref.sh found it),
+    compile against this Domain.h."""
+    src = os.path.join(reference_dir() or "", name)
     if not os.path.exists(src):
         pytest.skip("reference sources not present")
     cmd = ["g++", "-std=c++14", "-fsyntax-only", "-I", os.path.join(REPO, "include", "persiansph"), "-I",

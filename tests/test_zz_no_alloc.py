@@ -45,6 +45,19 @@ def test_noalloc_export_matches_allocating_export(gpu, name):
             got = buf[:n].cpu().numpy()
             assert set(map(tuple, got.tolist())) == ref_set
             assert (buf[n:].cpu().numpy() == -7).all()  # nothing written past the pairs
+        # count only: no buffer, the full count
+        st, n = _noalloc(gd, which, 0, 0)
+        assert st == 0 and n == len(ref)
+        # truncated output: exactly cap pairs of the set, nothing past cap, the full count
+        cap = len(ref) // 2
+        buf.fill_(-7)
+        torch.cuda.synchronize()
+        st, n = _noalloc(gd, which, buf.data_ptr(), cap)
+        assert st == 0 and n == len(ref)
+        got = buf[:cap].cpu().numpy()
+        assert len(set(map(tuple, got.tolist()))) == cap
+        assert set(map(tuple, got.tolist())) <= ref_set
+        assert (buf[cap:].cpu().numpy() == -7).all()
 
 
 def test_noalloc_export_rejects_contexts_above_its_limit(gpu):
