@@ -14,8 +14,10 @@ stream (inputs resident in HBM; the working set, several GB, exceeds the 129 MB
 L2, so no flush is needed). `e2e` repeats the measurement through the C ABI
 with host buffers: upload + K steps + download inside the timed region.
 The reference arm (--impl reference) times the reference algorithm on the host
-cores: the CPU oracle (a restatement of the reference, OpenMP) on a bounded
-sample of the same workload (the same tank at dx = 10 mm).
+cores: the CPU oracle (a restatement of the reference, OpenMP on every core)
+on the same workload at the same lattice, as many timed steps as fit a fixed
+budget after one warm-up step. The `cpu_baseline` of our arm is a bounded
+sample of the same workload (the same tank at dx = 10 mm, 5 steps).
 """
 from __future__ import annotations
 
@@ -42,6 +44,9 @@ def metric_name(workload: str) -> str:
         return METRIC
     return f"pair-interactions/s @ {workload}, FP32C form; FP64 plain beside it"
 UNIT = "pair-interactions/s"
+# Host seconds the reference arm's timed steps may take (it runs the full
+# workload: one step of the 6.7M-particle 3D dam break is ~35 s on 16 cores).
+REF_BUDGET_S = 90.0
 # FP64 operations per directed pair evaluation of the fluid kernel for this
 # workload's options (Wendland, Tait, artificial viscosity, Morris, squared
 # density): counted from forces_fluid_kernel's arithmetic on the taken branches,
@@ -163,6 +168,25 @@ WORKLOADS = {
 }
 
 
+def closure_verdict():
+    """What the shipped network gains a posteriori, from its training report
+    (held-out benchmark geometry, coarse dx = 20 mm against the fine dx = 10 mm
+    plain run, 0.05 - 0.4 s; tests/test_gpu_closure.py::test_closure_aposteriori_gain
+    reruns it)."""
+    from persiansph_gb300.closure import default_network_path
+    path = os.path.splitext(default_network_path())[0] + "_report.json"
+    try:
+        post = json.load(open(path))["aposteriori"]
+    except (OSError, KeyError, ValueError):
+        return {}
+    fr = {m: round(post[m]["front_rel_err_max"], 5) for m in ("closure", "smagorinsky", "laminar")}
+    vl = {m: round(post[m]["filtered_velocity_rel_l2"][-1], 4) for m in ("closure", "smagorinsky", "laminar")}
+    return {"aposteriori": {
+        "surge_front_max_rel_err": fr, "filtered_velocity_rel_l2_at_0.4s": vl,
+        "verdict": ("front: network 3x better than Smagorinsky, equal to laminar (no gain over laminar); "
+                    "late filtered velocity: network better than laminar, slightly worse than Smagorinsky")}}
+
+
 def build_workload(dx, name="dam3d"):
     from persiansph_gb300 import scenarios
     if name == "dam3d":
@@ -216,22 +240,30 @@ def measure_ensemble(n_inst: int, dx: float, steps: int, warmup: int):
             "gpu_launches_per_step": launches / max(done, 1), "phase_ms": phases}
 
 
-def cpu_reference(dx_sample: float, steps: int, warmup: int, threads: int, workload: str = "dam3d"):
+def cpu_reference(dx_sample: float, steps: int, warmup: int, threads: int, workload: str = "dam3d",
+                  budget_s: float | None = None):
     """Times the CPU oracle (restatement of the reference's OpenMP path) on the
-    same workload (the 3D dam break at a coarser lattice); returns
-    pair-interactions/s and details."""
+    workload at lattice spacing dx_sample: `warmup` untimed steps, then `steps`
+    timed steps (with budget_s, fewer when the warm-up step shows that they
+    would take longer than that, at least one). Returns pair-interactions/s
+    (pairs counted by the oracle's own pair forces) and details."""
     from oracle.oracle import OracleDomain
     dom, dt, info = build_workload(dx_sample, workload)
     o = OracleDomain(dom.config(dt), dom.particles, initial=True)
+    t_w = None
     if warmup:
+        t0 = time.perf_counter()
         o.step(warmup, threads)
-    npairs = len(o.pairs(3))
+        t_w = (time.perf_counter() - t0) / warmup
+    if budget_s is not None and t_w:
+        steps = max(1, min(steps, int(budget_s / t_w)))
+    p0 = o.pair_count()
     t0 = time.perf_counter()
     o.step(steps, threads)
     el = time.perf_counter() - t0
-    npairs2 = len(o.pairs(3))
-    pairs_per_step = 0.5 * (npairs + npairs2)
-    return {"value": pairs_per_step * steps / el, "steps_per_s": steps / el, "seconds": el,
+    pairs_per_step = (o.pair_count() - p0) / steps
+    o.close()
+    return {"value": pairs_per_step * steps / el, "steps_per_s": steps / el, "seconds": el, "steps": steps,
             "n": dom.particles.n, "n_fluid": info["n_fluid"], "pairs_per_step": pairs_per_step}
 
 
@@ -241,19 +273,25 @@ def run_reference_arm(args):
         return 0
     threads = os.cpu_count() or 1
     wl = WORKLOADS[args.workload]
-    ref_dx = args.ref_dx if args.ref_dx else wl["ref_dx"]
-    steps = max(1, min(args.steps, 5 if args.workload == "dam3d" else 20))
-    r = cpu_reference(ref_dx, steps, max(1, min(args.warmup, 1)), threads, args.workload)
+    # the reference arm runs the workload itself (same lattice as our arm);
+    # a step of the 6.7M-particle 3D dam break takes tens of seconds on the
+    # host cores, so the timed steps are as many as fit REF_BUDGET_S after
+    # one warm-up step (at most --steps)
+    ref_dx = args.ref_dx if args.ref_dx else args.dx
+    r = cpu_reference(ref_dx, max(1, args.steps), 1, threads, args.workload, budget_s=REF_BUDGET_S)
+    steps = r["steps"]
+    same = ref_dx == args.dx
     line = {
         "impl": "reference", "metric": metric_name(args.workload), "value": r["value"], "unit": UNIT,
         "n_gpus": args.gpus,
         "steps": steps, "warmup": 1, "ms_per_step": 1e3 * r["seconds"] / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic lattice (seeded)",
-        "config": {"workload": "sample of the " + wl["desc"] % ref_dx,
+        "config": {"workload": ("" if same else "sample of the ") + wl["desc"] % ref_dx,
                    "particles": r["n"], "fluid": r["n_fluid"], "pairs_per_step": r["pairs_per_step"]},
         "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{steps} steps of the {args.workload} workload at dx={ref_dx} m "
-                                   f"({r['n']} particles)"},
+                         "sample": f"{steps} timed steps (after 1 warm-up step) of the {args.workload} workload "
+                                   f"at dx={ref_dx} m ({r['n']} particles); steps bounded by a "
+                                   f"{REF_BUDGET_S:.0f} s budget"},
         "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "steps_per_s": r["steps_per_s"],
     }
@@ -273,7 +311,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched granular-column line")
     ap.add_argument("--tuning", default="auto",
-                    help="'auto' (psph_autotune on the workload's own steps) or BLOCK:SPLIT to fix the launch shape")
+                    help="'auto' (psph_autotune on the workload's own steps) or BLOCK:SPLIT[:STAGE] to fix the launch "
+                         "shape (STAGE: staged candidates per neighbour-scan block, 0 = none)")
     ap.add_argument("--ens-n", type=int, default=256)
     ap.add_argument("--ens-dx", type=float, default=1e-3)
     args = ap.parse_args()
@@ -320,8 +359,8 @@ def main():
         if args.tuning == "auto":
             tuning = gd.autotune(3)  # launch shapes timed on this workload's own (untimed) steps
         else:
-            block, split = (int(x) for x in args.tuning.split(":"))
-            gd.set_tuning(block, split)
+            parts = [int(x) for x in args.tuning.split(":")]
+            gd.set_tuning(parts[0], parts[1], parts[2] if len(parts) > 2 else None)
             tuning = gd.tuning()
         with ClockSampler(local) as clk:
             gd.step(args.warmup)
@@ -365,18 +404,25 @@ def main():
     fp64_tflops = 2 * m64["pairs_per_step"] * FLOPS_PER_DIRECTED_PAIR / (force64_ms * 1e-3) / 1e12
     traffic = FORCE32_TRAFFIC_BYTES_PER_PARTICLE[cl] * n
 
-    # end to end through the C ABI with host buffers: upload + K steps + download
+    # end to end through the C ABI with host buffers: create + upload + K
+    # steps + download, for the headline form and for the FP64 plain form
     fields = ("x", "v", "density", "pressure", "a", "ddensity")
-    t0 = time.perf_counter()
-    _, ge = open_domain(1, wl["closure"])
-    done_e = ge.step(args.steps)
-    out = ge.download_fields(fields)
-    torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    pe = ge.pair_count()
-    ge.close()
+
+    def end_to_end(precision, closure, tuning):
+        t0 = time.perf_counter()
+        _, ge = open_domain(precision, closure)
+        ge.set_tuning(tuning["pair_block"], tuning["cell_split"], tuning.get("nlist_stage"))
+        done_e = ge.step(args.steps)
+        out = ge.download_fields(fields)
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        pe = ge.pair_count()
+        ge.close()
+        return pe / el, done_e, sum(a.nbytes for a in out.values())
+
+    e2e_v, done_e, d2h = end_to_end(1, wl["closure"], m32["tuning"])
+    e2e64_v, done_e64, d2h64 = end_to_end(0, False, m64["tuning"])
     h2d = sum(dom.particles.get(f).nbytes for f in dom.particles.arrays())
-    d2h = sum(a.nbytes for a in out.values())
 
     def phase_dict(m):
         return dict(m["phases"])
@@ -398,13 +444,17 @@ def main():
         "steps_per_s": m32["steps_per_s"], "pairs_per_step": m32["pairs_per_step"], "tuning": m32["tuning"],
         "phase_ms": phase_dict(m32),
         "closure": {"evaluated": m32["closure_evaluated"], "fallbacks": m32["closure_fallbacks"],
-                    "network": os.path.relpath(default_network_path(), REPO)},
+                    "network": os.path.relpath(default_network_path(), REPO), **closure_verdict()},
         "fp32c_no_closure": {"value": m32n["value_rank"] * world_mult, "unit": UNIT,
                              "steps_per_s": m32n["steps_per_s"], "ms_per_step": m32n["ms"] / max(m32n["done"], 1),
                              "phase_ms": phase_dict(m32n)},
         "fp64_plain": {"value": m64["value_rank"] * world_mult, "unit": UNIT, "steps_per_s": m64["steps_per_s"],
                        "ms_per_step": m64["ms"] / max(m64["done"], 1), "phase_ms": phase_dict(m64),
-                       "clocks": m64["clocks"]},
+                       "clocks": m64["clocks"],
+                       "e2e": {"value": e2e64_v, "unit": UNIT, "h2d_bytes_per_step": h2d / max(done_e64, 1),
+                               "d2h_bytes_per_step": d2h64 / max(done_e64, 1), "steps": done_e64,
+                               "note": "FP64 plain form: create + upload + steps + download through the C ABI, "
+                                       "host wall clock"}},
         "fp32c_closure_over_fp64_steps_per_s": m32["steps_per_s"] / m64["steps_per_s"],
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved_gbs / pk["hbm_gbs"], "traffic": traffic,
@@ -421,7 +471,7 @@ def main():
                           "note": "frac counts 90 algorithmic FP64 flops per directed pair against the DFMA rate; "
                                   "the FP64 pipe itself is 85 % busy (sqrt, divisions, conversions)"},
         "clocks": m32["clocks"],
-        "e2e": {"value": pe / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d / max(done_e, 1),
+        "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": h2d / max(done_e, 1),
                 "d2h_bytes_per_step": d2h / max(done_e, 1), "steps": done_e,
                 "note": "create + upload + steps + download through the C ABI, host wall clock"},
         "gpu_launches": m32["launches"],
@@ -431,7 +481,7 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         ref_dx = args.ref_dx if args.ref_dx else wl["ref_dx"]
-        cpu_steps = 2 if args.workload == "dam3d" else 10
+        cpu_steps = 5 if args.workload == "dam3d" else 10
         r = cpu_reference(ref_dx, cpu_steps, 1, threads, args.workload)
         line["cpu_baseline"] = {"value": r["value"], "unit": UNIT, "cores": threads, "kind": "port",
                                 "steps_per_s": r["steps_per_s"],

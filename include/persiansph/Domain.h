@@ -21,9 +21,16 @@
  *    a hook that adds the same acceleration to every free particle and changes
  *    nothing else (the 1-Poiseuille.cpp UserAcc pattern) becomes a device-side
  *    body force; any other hook is rejected with a Fatal.
- *  - Output: the reference writes XDMF/HDF5 snapshots (WriteXDMF); this
- *    build does not link HDF5 and calls UserOutput-free output hooks only
- *    through OutputHook (an addition), with the particles already copied back.
+ *  - Output: with a file key, Solve writes the reference's snapshots
+ *    (WriteXDMF: <key>_Initial, then <key>_0001, ... at each output time) as
+ *    <name>.bin + <name>.xmf, the same datasets as the reference's <name>.hdf5
+ *    in a raw little-endian file the .xmf points at (HDF5 is not linked).
+ *    With the default UserOutput the snapshot is taken on the device at the
+ *    reference's output point (after the step's forces, before its update)
+ *    and written while the next steps run; a driver-set UserOutput runs on the
+ *    host on the particles copied back at the output time (accelerations of
+ *    the step before). OutputHook (an addition) is called at output times with
+ *    the particles copied back.
  *  - Additions: Precision (PSPH_FP64 / PSPH_FP32C), BodyForce,
  *    WallPressureMode, ShepardStep, Time (public), OutputHook.
  *  - Nproc is accepted and ignored (the work runs on the GPU).
@@ -460,6 +467,28 @@ inline void Domain::Solve(double tf, double dt, double dtOut, char const* TheFil
     check(psph_upload(ctx, &pk.view, 1), ctx);
     size_t idx_out = 1;
     double tout = Time;
+    const bool user_props = UserOutput != &OutPut;
+    const char* names[3] = {OutputName[0].CStr(), OutputName[1].CStr(), OutputName[2].CStr()};
+    // UserOutput's three properties of the particles on the host, in their order
+    auto write_now = [&](const String& fn) {
+      std::vector<double> p1, p2, p3;
+      if (user_props) {
+        const size_t n = Particles.Size();
+        p1.resize(n);
+        p2.resize(n);
+        p3.resize(n);
+        for (size_t i = 0; i < n; ++i) UserOutput(Particles[i], p1[i], p2[i], p3[i]);
+      }
+      check(psph_output_write(ctx, fn.CStr(), names, user_props ? p1.data() : nullptr,
+                              user_props ? p2.data() : nullptr, user_props ? p3.data() : nullptr),
+            ctx);
+    };
+    if (TheFileKey != nullptr) {  // the initial state (Source/Domain.cpp:1752-1758)
+      String fn;
+      fn.Printf("%s_Initial", TheFileKey);
+      write_now(fn);
+      std::cout << "\nInitial Condition has been generated\n" << std::endl;
+    }
     auto copy_back = [&]() {
       const int64_t n = psph_num_particles(ctx);
       if (n < 0) check(PSPH_ERR_CUDA, ctx);
@@ -482,9 +511,15 @@ inline void Domain::Solve(double tf, double dt, double dtOut, char const* TheFil
     };
     while (Time < tf && idx_out <= maxidx) {
       if (Time >= tout) {
-        copy_back();
+        if (OutputHook || (TheFileKey != nullptr && user_props)) copy_back();
         if (OutputHook) OutputHook(*this, idx_out);
-        if (TheFileKey != nullptr) std::cout << "\nOutput No. " << idx_out << " at " << Time << " has been generated" << std::endl;
+        if (TheFileKey != nullptr) {
+          String fn;
+          fn.Printf("%s_%04zu", TheFileKey, idx_out);
+          if (user_props) write_now(fn);
+          else check(psph_output_request(ctx, fn.CStr(), names), ctx);  // taken by the next step
+          std::cout << "\nOutput No. " << idx_out << " at " << Time << " has been generated" << std::endl;
+        }
         idx_out++;
         tout += dtOut;
       }
@@ -495,6 +530,7 @@ inline void Domain::Solve(double tf, double dt, double dtOut, char const* TheFil
       Time = it.time;
       if (done == 0) break;
     }
+    check(psph_output_flush(ctx), ctx);
     copy_back();
   } catch (...) {
     psph_destroy(ctx);

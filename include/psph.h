@@ -207,15 +207,46 @@ typedef struct {
   int32_t pair_block;   /* threads per block of the FP32C pair kernels: 64, 128 or 256 */
   int32_t cell_split;   /* x-slabs per cell in the sort (1, 2 or 4): the neighbour-list walk
                            skips slabs out of reach */
+  int32_t nlist_stage;  /* staging depth of the neighbour search: candidate positions each
+                           block copies into shared memory (TMA bulk copies) before scanning
+                           them, 2048, 3072 or 4096; 0 scans global memory. Applies with one
+                           h everywhere and a non-periodic x axis. */
+  int32_t reserved;     /* zero */
   double ms_per_step;   /* psph_autotune: device time per step of the chosen setting */
 } psph_tuning;
 psph_status psph_get_tuning(const psph_ctx* ctx, psph_tuning* out);
 /* Applies a setting (the step graph is captured again at the next step). */
 psph_status psph_set_tuning(psph_ctx* ctx, const psph_tuning* t);
 /* Runs steps_per_trial timed steps (after one untimed step) with every
- * candidate setting and keeps the fastest; *chosen (if not NULL) receives it.
- * The trial steps are real steps of the simulation: they advance its time. */
+ * candidate setting and keeps the fastest; *chosen (if not NULL) receives it:
+ * first every pair block x cell split, then, with those fixed, every staging
+ * depth. The trial steps are real steps of the simulation: they advance its
+ * time. */
 psph_status psph_autotune(psph_ctx* ctx, int64_t steps_per_trial, psph_tuning* chosen);
+
+/* ---- Snapshot output (WriteXDMF, Source/Domain.cpp:1869-2064) -----------------
+ * The reference writes <key>.hdf5 (float32 datasets NP, Position, Velocity,
+ * Acceleration, Tag, Pressure, Density, the three UserOutput properties under
+ * OutputName[0..2], Mass, h, Sigma, Strain; Sigma and Strain as the six
+ * components 00 01 02 11 12 22) and <key>.xmf. HDF5 is not linked here: the
+ * same datasets, in the same order, types and values, go back to back into
+ * <key>.bin (little endian; NP first), and <key>.xmf is the reference's XDMF
+ * with each DataItem in Format="Binary" at its byte offset. names (may be
+ * NULL, or hold NULL entries) are OutputName[0..2]; "Property1".."Property3"
+ * by default. Single-domain contexts only. */
+/* The next step psph_step takes writes a snapshot after its forces and before
+ * its update, where Solve writes its output (Source/Domain.cpp:1773-1788), with
+ * the default UserOutput properties (zeros, Source/Domain.cpp:28-33). The copy
+ * to the host and the file writes overlap the steps that follow. */
+psph_status psph_output_request(psph_ctx* ctx, const char* file_key, const char* const names[3]);
+/* Writes a snapshot of the current state now (Solve's initial output,
+ * Source/Domain.cpp:1752-1758), with the UserOutput properties prop1..prop3
+ * (host arrays in psph_download order, or NULL for zeros); returns when the
+ * files are written. */
+psph_status psph_output_write(psph_ctx* ctx, const char* file_key, const char* const names[3], const double* prop1,
+                              const double* prop2, const double* prop3);
+/* Waits until every requested snapshot is written; reports a failed write. */
+psph_status psph_output_flush(psph_ctx* ctx);
 
 /* Pair-interactions evaluated since upload: unordered pairs {i,j}, at least
  * one free, r_ij <= Cellfac h_ij, summed over steps (the work CalcForce11 /

@@ -60,6 +60,8 @@ def lib():
         L.psph_oracle_pairs.restype = C.c_int64
         L.psph_oracle_scales.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
         L.psph_oracle_phase_times.argtypes = [C.c_void_p, P(C.c_double), C.c_int]
+        L.psph_oracle_pair_count.argtypes = [C.c_void_p]
+        L.psph_oracle_pair_count.restype = C.c_int64
         _lib = L
     return _lib
 
@@ -139,6 +141,10 @@ class OracleDomain:
         lib().psph_oracle_scales(self._h, a.ctypes.data_as(C.POINTER(C.c_double)),
                                  d.ctypes.data_as(C.POINTER(C.c_double)))
         return a, d
+
+    def pair_count(self) -> int:
+        """In-support pairs evaluated by the pair forces since create."""
+        return int(lib().psph_oracle_pair_count(self._h))
 
     def phase_times(self):
         buf = (C.c_double * 5)()

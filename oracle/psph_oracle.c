@@ -64,6 +64,7 @@ struct psph_oracle {
   double *a_scale, *dr_scale;
   double mu_max, cs_max; /* Domain::MuMax / CsMax from CellInitiate */
   double phase_s[5];
+  int64_t pairs_done; /* in-support pairs evaluated by CalcForce* since create */
   int status;
   char err[512];
 };
@@ -654,14 +655,14 @@ static inline double shepard_counter_of(const psph_oracle* o, int64_t p) {
 }
 
 /* CalcForce11 (Source/Interaction.cpp:25-184) */
-static void calc_force11(psph_oracle* o, int64_t p1, int64_t p2) {
+static int calc_force11(psph_oracle* o, int64_t p1, int64_t p2) {
   const int dim = o->cfg.dimension, kt = o->cfg.kernel_type;
   double h = (o->h[p1] + o->h[p2]) / 2;
   double xij[3];
   for (int d = 0; d < 3; ++d) xij[d] = o->x[3 * p1 + d] - o->x[3 * p2 + d];
   periodic_correction(o, xij, h, p1, p2);
   double rij = sqrt(dot3(xij, xij));
-  if ((rij / h) > o->g.cellfac) return;
+  if ((rij / h) > o->g.cellfac) return 0;
   const int f1 = FREE(p1), f2 = FREE(p2);
   double di = 0.0, dj = 0.0, mi = 0.0, mj = 0.0;
   double Alpha = (o->alpha[p1] + o->alpha[p2]) / 2.0;
@@ -797,17 +798,18 @@ static void calc_force11(psph_oracle* o, int64_t p1, int64_t p2) {
   o->a_scale[p2] += fabs(mi) * tn;
   o->dr_scale[p2] += fabs(mi * (dj / di) * temp1);
   omp_unset_lock(&o->locks[p2]);
+  return 1;
 }
 
 /* CalcForce2233 (Source/Interaction.cpp:186-377) */
-static void calc_force2233(psph_oracle* o, int64_t p1, int64_t p2) {
+static int calc_force2233(psph_oracle* o, int64_t p1, int64_t p2) {
   const int dim = o->cfg.dimension, kt = o->cfg.kernel_type;
   double h = (o->h[p1] + o->h[p2]) / 2;
   double xij[3];
   for (int d = 0; d < 3; ++d) xij[d] = o->x[3 * p1 + d] - o->x[3 * p2 + d];
   periodic_correction(o, xij, h, p1, p2);
   double rij = sqrt(dot3(xij, xij));
-  if ((rij / h) > o->g.cellfac) return;
+  if ((rij / h) > o->g.cellfac) return 0;
   const int f1 = FREE(p1), f2 = FREE(p2);
   double di = 0.0, dj = 0.0, mi = 0.0, mj = 0.0;
   double Alpha = (o->alpha[p1] + o->alpha[p2]) / 2.0;
@@ -964,23 +966,26 @@ static void calc_force2233(psph_oracle* o, int64_t p1, int64_t p2) {
   o->a_scale[p2] += fabs(mi) * tn;
   o->dr_scale[p2] += fabs(mi * (dj / di) * temp1);
   omp_unset_lock(&o->locks[p2]);
+  return 1;
 }
 
 /* LastComputeAcceleration (Source/Domain.cpp:1238-1297) */
 static int last_compute(psph_oracle* o, int nthr) {
   for (int k = 0; k < o->nthr; ++k)
     if (o->nsm[k].n) return fail(o, PSPH_ERR_UNSUPPORTED, "interaction between different materials (NSMPairs) is outside this build");
-#pragma omp parallel for schedule(static) num_threads(nthr)
+  int64_t evaluated = 0;
+#pragma omp parallel for schedule(static) num_threads(nthr) reduction(+ : evaluated)
   for (int k = 0; k < o->nthr; k++) {
     for (int64_t i = 0; i < o->sm[k].n; i++) {
       int64_t p1 = o->sm[k].v[2 * i], p2 = o->sm[k].v[2 * i + 1];
-      if (o->material[p1] == 1) calc_force11(o, p1, p2); else calc_force2233(o, p1, p2);
+      evaluated += (o->material[p1] == 1) ? calc_force11(o, p1, p2) : calc_force2233(o, p1, p2);
     }
     for (int64_t i = 0; i < o->fsm[k].n; i++) {
       int64_t p1 = o->fsm[k].v[2 * i], p2 = o->fsm[k].v[2 * i + 1];
-      if (o->material[p1] == 1) calc_force11(o, p1, p2); else calc_force2233(o, p1, p2);
+      evaluated += (o->material[p1] == 1) ? calc_force11(o, p1, p2) : calc_force2233(o, p1, p2);
     }
   }
+  o->pairs_done += evaluated;
   double dtmin = o->it.deltatint;
   const double sha = o->cfg.sqrt_h_a;
 #pragma omp parallel for schedule(static) num_threads(nthr) reduction(min : dtmin)
@@ -1584,6 +1589,8 @@ int psph_oracle_scales(const psph_oracle* o, double* a_scale, double* drho_scale
   memcpy(drho_scale, o->dr_scale, (size_t)o->n * sizeof(double));
   return PSPH_OK;
 }
+
+int64_t psph_oracle_pair_count(const psph_oracle* o) { return o->pairs_done; }
 
 int psph_oracle_phase_times(const psph_oracle* o, double* s, int cap) {
   for (int e = 0; e < 5 && e < cap; ++e) s[e] = o->phase_s[e];

@@ -50,6 +50,10 @@ int64_t psph_oracle_pairs(psph_oracle* o, int which, int64_t* buf, int64_t cap);
  * Tests scale their per-particle tolerance by these. */
 int psph_oracle_scales(const psph_oracle* o, double* a_scale, double* drho_scale);
 
+/* In-support pairs CalcForce11 / CalcForce2233 evaluated (the pair-interaction
+ * count of the metric), summed over the steps since create. */
+int64_t psph_oracle_pair_count(const psph_oracle* o);
+
 /* Wall time (s) of the phases of the last psph_oracle_step call: search,
  * wall interpolation, pair forces, update, relist; returns the count. */
 int psph_oracle_phase_times(const psph_oracle* o, double* s, int cap);

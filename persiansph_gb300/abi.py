@@ -63,7 +63,8 @@ class PsphIntegrator(C.Structure):
 
 
 class PsphTuning(C.Structure):
-    _fields_ = [("pair_block", C.c_int32), ("cell_split", C.c_int32), ("ms_per_step", C.c_double)]
+    _fields_ = [("pair_block", C.c_int32), ("cell_split", C.c_int32), ("nlist_stage", C.c_int32),
+                ("reserved", C.c_int32), ("ms_per_step", C.c_double)]
 
 
 class PsphParticles(C.Structure):
@@ -168,6 +169,11 @@ def _declare(lib):
     lib.psph_pair_count.argtypes = [ctx, P(C.c_uint64)]
     lib.psph_probe_fp64_peak.argtypes = [P(C.c_double)]
     lib.psph_pairs_export_noalloc.argtypes = [ctx, C.c_int, C.c_void_p, C.c_int64, P(C.c_int64)]
+    names3 = P(C.c_char_p)
+    dp = P(C.c_double)
+    lib.psph_output_request.argtypes = [ctx, C.c_char_p, names3]
+    lib.psph_output_write.argtypes = [ctx, C.c_char_p, names3, dp, dp, dp]
+    lib.psph_output_flush.argtypes = [ctx]
     lib.psph_batch_create.argtypes = [P(PsphConfig), C.c_int, P(ctx)]
     lib.psph_batch_size.argtypes = [ctx]
     lib.psph_batch_size.restype = C.c_int
@@ -210,7 +216,7 @@ def _declare(lib):
                  "psph_pairs_export", "psph_enable_timing", "psph_phase_times", "psph_step_timed", "psph_pair_count",
                  "psph_probe_fp64_peak", "psph_pairs_export_noalloc", "psph_batch_create", "psph_batch_upload",
                  "psph_batch_step", "psph_batch_download", "psph_batch_original_index", "psph_batch_get_grid",
-                 "psph_batch_get_integrator"):
+                 "psph_batch_get_integrator", "psph_output_request", "psph_output_write", "psph_output_flush"):
         getattr(lib, name).restype = C.c_int
 
 

@@ -24,6 +24,7 @@
 
 #include "psph_device.cuh"
 #include "psph_mlp.cuh"
+#include "psph_output.cuh"
 
 using namespace psph;
 
@@ -32,6 +33,8 @@ using namespace psph;
 constexpr int kNumPhases = 7;
 // Finest split of the cells into x-slabs in the sort (Options::xsub).
 constexpr int kMaxXsub = 4;
+// Deepest staging of the neighbour search (Options::nlist_stage, candidates per block).
+constexpr int kMaxStage = 4096;
 
 struct psph_ctx {
   int ninst = 1;
@@ -72,6 +75,10 @@ struct psph_ctx {
   double phase_ms[kNumPhases] = {};
   double tuned_ms = 0.0;  // psph_autotune's measured time per step
   long long last_launches = 0;
+  // snapshot output (psph_output_request / psph_output_write)
+  OutputWriter* out = nullptr;
+  bool out_requested = false;
+  std::string out_key, out_names[3];
   cudaEvent_t ev[kNumPhases + 1] = {};
 };
 
@@ -261,8 +268,16 @@ DevView view(psph_ctx* c) {
   return v;
 }
 
-// One step of Solve's loop body (Source/Domain.cpp:1764-1792) as launches.
+// One step of Solve's loop body (Source/Domain.cpp:1764-1792) as launches;
+// before_update (if given) enqueues work between the forces and the update,
+// where Solve writes its output (Source/Domain.cpp:1773-1788).
+template <class F>
+void enqueue_step(psph_ctx* c, F&& before_update);
 void enqueue_step(psph_ctx* c) {
+  enqueue_step(c, [] {});
+}
+template <class F>
+void enqueue_step(psph_ctx* c, F&& before_update) {
   const DevView v = view(c);
   cudaStream_t st = c->stream;
   launch_begin(v, st);
@@ -280,6 +295,7 @@ void enqueue_step(psph_ctx* c) {
   if (v.o.closure) launch_closure(v, st);
   record_phase(c, 5);
   launch_dt(v, st);
+  before_update();
   record_phase(c, 6);
   launch_update(v, st);
   launch_end(v, st);
@@ -394,6 +410,7 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
   if (!c || !parts) return PSPH_ERR_INVALID_ARGUMENT;
   if (c->uploaded) return set_err(c, PSPH_ERR_STATE, "particles already uploaded to this context");
   if (!c->stream) return set_err(c, PSPH_ERR_STATE, "context not created");
+  nlist_configure();  // shared-memory limit of the staged neighbour scan (outside any capture)
   const int ninst = c->ninst;
   const psph_config& k = c->cfgs[0];
   const bool lf = (k.scheme == PSPH_LEAPFROG);
@@ -634,8 +651,11 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
   o.eos_cls = -1;
   o.uniform_h = 1;
   o.any_periodic = 0;
-  for (const GridDev& gd : c->gdevs)
+  o.any_periodic_x = 0;
+  for (const GridDev& gd : c->gdevs) {
     if (gd.periodic[0] || gd.periodic[1] || gd.periodic[2]) o.any_periodic = 1;
+    if (gd.periodic[0]) o.any_periodic_x = 1;
+  }
   o.any_av = o.any_ti = o.need_sr = o.any_shepard = 0;
   for (size_t q = 0; q < c->classes.size(); ++q) {
     const PClass& C = c->classes[q];
@@ -653,6 +673,25 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
     }
   }
   if (o.eos_cls < 0) o.eos_cls = 0;
+  // pair constants that are the same for every class: the FP32C fluid pair
+  // loop takes them from the launch parameters (the same FP32 values the class
+  // table holds, so the results are identical)
+  {
+    o.uniform_av = o.uniform_mass = 1;
+    const PClass& C0 = c->classes[0];
+    double m_free = -1.0, fpm_wall = -1.0;
+    for (const PClass& C : c->classes) {
+      if (C.alpha != C0.alpha || C.beta != C0.beta) o.uniform_av = 0;
+      double& ref = C.is_free ? m_free : fpm_wall;
+      const double val = C.is_free ? C.mass : C.fpmassc;
+      if (ref < 0.0) ref = val;
+      else if (val != ref) o.uniform_mass = 0;
+    }
+    o.alpha32 = (float)C0.alpha;
+    o.beta32 = (float)C0.beta;
+    o.m_free32 = (float)std::max(m_free, 0.0);
+    o.fpm_wall32 = (float)std::max(fpm_wall, 0.0);
+  }
   o.uniform_mu = !dyn_mu;
   o.mu_u = 0.0;
   {
@@ -680,6 +719,7 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
   o.nl_cap = (k.dimension == 3) ? 128 : 64;
   o.pair_block = 128;
   o.xsub = 1;
+  o.nlist_stage = 0;  // measured: the L1-cached scan beats the staged one (psph_autotune tries both)
 
   // ---- device buffers ----------------------------------------------------------
   c->ncap = (int)ntot;
@@ -712,18 +752,27 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
       (st = dalloc(c, &S.shear_rate, N)) || (st = dalloc(c, &S.sbar, N)))
     return st;
   if ((st = dalloc(c, &S.nl, (size_t)o.nl_cap * nl_stride_of(c->ncap)))) return st;
+  // FP64 fluids without strain-rate sums, XSPH or solids: each pair evaluated once
+  o.fp64_half = !o.fp32 && !o.has_solid && !o.need_sr && o.xsph == 0.0;
+  if (o.fp64_half) {
+    const size_t slots = (size_t)o.nl_cap * nl_stride_of(c->ncap);
+    if ((st = dalloc(c, &S.half4, slots)) || (st = dalloc(c, &S.half2, slots)) ||
+        (st = dalloc(c, &S.half_stamp, slots)))
+      return st;
+  }
   if (o.need_sr || o.has_solid)
     if ((st = dalloc(c, &S.strain_rate, 9 * N))) return st;
   if (o.fp32) {
-    if ((st = dalloc(c, &S.V32, N)) || (st = dalloc(c, &S.D32, N)) || (st = dalloc(c, &S.NSV32, N))) return st;
+    if ((st = dalloc(c, &S.V32, N)) || (st = dalloc(c, &S.D32, N)) || (st = dalloc(c, &S.NSV32, N)) ||
+        (st = dalloc(c, &S.V32LO, N)))
+      return st;
     if (dyn_mu && (st = dalloc(c, &S.MU32, N))) return st;
     if (o.need_sr && !o.has_solid &&  // FP32 ShearRate and strain-rate sums of the fluid kernel
         ((st = dalloc(c, &S.cshear, N)) || (st = dalloc(c, &S.sr32, 6 * N))))
       return st;
   }
   if (o.fp32 && o.has_solid) {
-    if ((st = dalloc(c, &S.SIG32, 2 * N)) || (st = dalloc(c, &S.VB32, N)) || (st = dalloc(c, &S.V32LO, N)))
-      return st;
+    if ((st = dalloc(c, &S.SIG32, 2 * N)) || (st = dalloc(c, &S.VB32, N))) return st;
     if (o.any_ti && (st = dalloc(c, &S.TIR32, 2 * N))) return st;
   }
   if (o.has_solid) {
@@ -864,7 +913,26 @@ psph_status step_impl(psph_ctx* c, int64_t nsteps, const double* t_stop, double 
   for (int q = 0; q < c->ninst; ++q) steps0[q] = c->h_inst[q].steps;
   for (int e = 0; e < kNumPhases; ++e) c->phase_ms[e] = 0.0;
   long long launched = 0;
-  if (c->timing) {
+  if (c->out_requested) {
+    // the output step: launched directly, the snapshot gathered between its
+    // forces and its update; its copy to the host and the file writes overlap
+    // the steps that follow
+    c->out_requested = false;
+    std::string e;
+    bool ok = true;
+    enqueue_step(c, [&] { ok = output_gather(c->out, view(c), 0, (int)c->inst_off[1], c->stream, &e); });
+    CUDA_TRY(c, cudaGetLastError());
+    if (!ok) return set_err(c, PSPH_ERR_CUDA, "%s", e.c_str());
+    const char* names[3] = {c->out_names[0].c_str(), c->out_names[1].c_str(), c->out_names[2].c_str()};
+    if (!output_commit(c->out, c->out_key.c_str(), names, nullptr, 0, &e))
+      return set_err(c, PSPH_ERR_CUDA, "%s", e.c_str());
+    launched += launches_per_step(view(c)) + 4;
+    if ((st = sync_scalars(c))) return st;
+    --nsteps;
+    if (c->h_sc->all_stop || c->h_sc->status) nsteps = 0;
+  }
+  if (nsteps <= 0) {
+  } else if (c->timing) {
     for (int64_t s = 0; s < nsteps; ++s) {
       enqueue_step(c);
       CUDA_TRY(c, cudaGetLastError());
@@ -902,6 +970,14 @@ psph_status step_impl(psph_ctx* c, int64_t nsteps, const double* t_stop, double 
                    "Too small time step, please choose a smaller time step initially to make the simulation more stable");
   if (status & ST_OUT_OF_GRID)
     return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "a particle lies more than hmax outside the cell grid");
+  // a bounded device-side wait that gave up (the kernel finished its work
+  // without the data it waited for and reported it)
+  if (status & ST_CLOSURE_TIMEOUT)
+    return set_err(c, PSPH_ERR_CUDA, "the closure kernel's tensor-core completion wait gave up");
+  if (status & ST_STAGE_TIMEOUT)
+    return set_err(c, PSPH_ERR_CUDA, "the neighbour scan's shared-memory staging wait gave up");
+  if (status & ST_LIST_MISMATCH)
+    return set_err(c, PSPH_ERR_CUDA, "a pair inside the kernel support is missing from its partner's list");
   return PSPH_OK;
 }
 
@@ -1149,6 +1225,7 @@ psph_status psph_create(const psph_config* cfg, psph_ctx** out) { return create_
 void psph_destroy(psph_ctx* c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
+  output_writer_destroy(c->out);  // queued snapshots are written first
   free_all(c);
   for (int i = 0; i <= kNumPhases; ++i)
     if (c->ev[i]) cudaEventDestroy(c->ev[i]);
@@ -1291,6 +1368,8 @@ psph_status psph_get_tuning(const psph_ctx* c, psph_tuning* out) {
   if (!c || !out) return PSPH_ERR_INVALID_ARGUMENT;
   out->pair_block = c->opt.pair_block;
   out->cell_split = c->opt.xsub;
+  out->nlist_stage = c->opt.nlist_stage;
+  out->reserved = 0;
   out->ms_per_step = c->tuned_ms;
   return PSPH_OK;
 }
@@ -1301,9 +1380,13 @@ psph_status psph_set_tuning(psph_ctx* c, const psph_tuning* t) {
     return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "pair_block must be 64, 128 or 256 (got %d)", t->pair_block);
   if (t->cell_split != 1 && t->cell_split != 2 && t->cell_split != kMaxXsub)
     return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "cell_split must be 1, 2 or 4 (got %d)", t->cell_split);
-  if (c->opt.pair_block != t->pair_block || c->opt.xsub != t->cell_split) {
+  if (t->nlist_stage != 0 && t->nlist_stage != 2048 && t->nlist_stage != 3072 && t->nlist_stage != kMaxStage)
+    return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "nlist_stage must be 0, 2048, 3072 or 4096 (got %d)",
+                   t->nlist_stage);
+  if (c->opt.pair_block != t->pair_block || c->opt.xsub != t->cell_split || c->opt.nlist_stage != t->nlist_stage) {
     c->opt.pair_block = t->pair_block;
     c->opt.xsub = t->cell_split;
+    c->opt.nlist_stage = t->nlist_stage;
     if (c->graph) {  // launch parameters change: capture the step again
       cudaGraphExecDestroy(c->graph);
       c->graph = nullptr;
@@ -1326,23 +1409,44 @@ psph_status psph_autotune(psph_ctx* c, int64_t steps_per_trial, psph_tuning* cho
       cands.push_back(t);
     }
   }
+  for (psph_tuning& t : cands) t.nlist_stage = c->opt.nlist_stage;
   psph_tuning best{};
   double best_ms = 1e300;
-  for (const psph_tuning& t : cands) {
+  bool ended = false;
+  auto trial = [&](const psph_tuning& t) -> psph_status {
     psph_status st = psph_set_tuning(c, &t);
     if (st) return st;
     double ms = 0.0;
     int64_t done = 0;
     if ((st = psph_step_timed(c, 1, &ms, &done))) return st;  // capture + first launch, untimed
     if ((st = psph_step_timed(c, steps_per_trial, &ms, &done))) return st;
-    if (done < steps_per_trial) break;  // the run ended; keep what was measured
+    if (done < steps_per_trial) {  // the run ended; keep what was measured
+      ended = true;
+      return PSPH_OK;
+    }
     const double per = ms / (double)done;
     if (per < best_ms) {
       best_ms = per;
       best = t;
     }
+    return PSPH_OK;
+  };
+  for (const psph_tuning& t : cands) {
+    if (psph_status st = trial(t)) return st;
+    if (ended) break;
   }
   if (best_ms == 1e300) best = cands.front();
+  // then the staging depth of the neighbour search, where it applies
+  if (!ended && c->opt.uniform_h && !c->opt.any_periodic_x) {
+    const psph_tuning base = best;
+    for (int stage : {0, 2048, 3072, kMaxStage}) {
+      if (stage == base.nlist_stage) continue;
+      psph_tuning t = base;
+      t.nlist_stage = stage;
+      if (psph_status st = trial(t)) return st;
+      if (ended) break;
+    }
+  }
   psph_status st = psph_set_tuning(c, &best);
   if (st) return st;
   c->tuned_ms = best_ms < 1e300 ? best_ms : 0.0;
@@ -1459,6 +1563,58 @@ psph_status psph_batch_get_integrator(const psph_ctx* c, int inst, psph_integrat
 }
 
 }  // extern "C"
+
+// ---- snapshot output -------------------------------------------------------------
+
+namespace {
+psph_status output_prepare(psph_ctx* c, const char* key, const char* const names[3]) {
+  if (!c || !key || !*key) return PSPH_ERR_INVALID_ARGUMENT;
+  if (!c->uploaded) return set_err(c, PSPH_ERR_STATE, "snapshot output before psph_upload");
+  if (c->ninst != 1) return set_err(c, PSPH_ERR_STATE, "snapshot output applies to single-domain contexts");
+  if (!c->out) c->out = output_writer_create();
+  c->out_key = key;
+  for (int k = 0; k < 3; ++k)
+    c->out_names[k] = (names && names[k] && *names[k]) ? names[k] : ("Property" + std::to_string(k + 1));
+  return PSPH_OK;
+}
+}  // namespace
+
+psph_status psph_output_request(psph_ctx* c, const char* file_key, const char* const names[3]) {
+  psph_status st = output_prepare(c, file_key, names);
+  if (st) return st;
+  c->out_requested = true;
+  return PSPH_OK;
+}
+
+psph_status psph_output_write(psph_ctx* c, const char* file_key, const char* const names[3], const double* prop1,
+                              const double* prop2, const double* prop3) {
+  psph_status st = output_prepare(c, file_key, names);
+  if (st) return st;
+  std::string e;
+  const int64_t m = num_particles_impl(c, 0);
+  std::vector<double> props;
+  if (prop1 || prop2 || prop3) {
+    props.assign(3 * (size_t)m, 0.0);
+    for (int k = 0; k < 3; ++k) {
+      const double* p = k == 0 ? prop1 : (k == 1 ? prop2 : prop3);
+      if (p) std::copy(p, p + m, props.begin() + (size_t)k * m);
+    }
+  }
+  if (!output_gather(c->out, view(c), 0, (int)c->inst_off[1], c->stream, &e))
+    return set_err(c, PSPH_ERR_CUDA, "%s", e.c_str());
+  const char* nm[3] = {c->out_names[0].c_str(), c->out_names[1].c_str(), c->out_names[2].c_str()};
+  if (!output_commit(c->out, c->out_key.c_str(), nm, props.empty() ? nullptr : props.data(), m, &e) ||
+      !output_flush(c->out, &e))
+    return set_err(c, PSPH_ERR_CUDA, "%s", e.c_str());
+  return PSPH_OK;
+}
+
+psph_status psph_output_flush(psph_ctx* c) {
+  if (!c) return PSPH_ERR_INVALID_ARGUMENT;
+  std::string e;
+  if (c->out && !output_flush(c->out, &e)) return set_err(c, PSPH_ERR_CUDA, "%s", e.c_str());
+  return PSPH_OK;
+}
 
 // ---------------------------------------------------------------------------
 // Pair export that allocates nothing.

@@ -29,6 +29,8 @@ enum : uint32_t {
   ST_OUT_OF_GRID = 1u << 2,
   ST_CELL_OVERFLOW = 1u << 3,
   ST_CLOSURE_TIMEOUT = 1u << 4,  // a tensor-core wait of the closure kernel gave up
+  ST_STAGE_TIMEOUT = 1u << 5,    // a shared-memory staging wait of the neighbour scan gave up
+  ST_LIST_MISMATCH = 1u << 6,    // a pair inside the support missing from its partner's list
 };
 
 // Constant per-particle parameters, shared by all particles of one class.

@@ -44,12 +44,18 @@ struct Scratch {
   float4* SIG32;     // FP32C solids: symmetric Sigma, 2 per particle (00 01 02 11 | 12 22 - -)
   float4* TIR32;     // FP32C solids with TI: symmetric TIR, same layout
   float4* VB32;      // FP32C solids: wall history velocity (MVerlet vb / leapfrog vb)
-  float4* V32LO;     // FP32C solids: v - (float)v, the low-order part of the velocity
+  float4* V32LO;     // FP32C: v - (float)v, the low-order part of the velocity (fluids: .w = the
+                     // particle's class index as int bits, loaded with it by the pair kernel)
   float* MU32;       // FP32C, per-particle viscosity (LES / Bingham): FP32 copy of Persist::mu
   float4* NSV32;     // FP32C: wall no-slip velocity in FP32
   double4_32a* D4;   // seen by partners: (1/density, pressure/density^2, sound speed, density);
                      // a wall's density is the inverse EOS of its interpolated pressure
   double4_32a* A4;       // ax, ay, az, dDensity
+  // FP64 once-per-pair form: a partner's terms of a pair, in the partner's own
+  // list slot (nl_index layout): (a, dDensity) and (ZWab, SumDen)
+  double4_32a* half4;
+  double2* half2;
+  int* half_stamp;       // instance step + 1 when the slot was written this step
   double* zwab;
   double* sumden;
   double* sumkernel;
@@ -87,12 +93,18 @@ struct Options {
   int carry_shear_h;  // the sort moves the ShearStress history (Mat2, or a non-zero upload)
   int uniform_h;      // every particle has the same h
   int any_periodic;   // some instance has a periodic axis
+  int any_periodic_x; // some instance has a periodic x axis (no staged neighbour scan)
+  int fp64_half;      // FP64 fluid pair forces evaluate each pair once (no strain rate, XSPH or solids)
   int uniform_mu;     // every free particle has the same constant viscosity
+  int uniform_av;     // every class has the same artificial-viscosity alpha and beta (alpha32, beta32)
+  int uniform_mass;   // every free class has one mass (m_free32), every fixed class one FPMassC (fpm_wall32)
+  float alpha32, beta32, m_free32, fpm_wall32;
   double mu_u;        // that viscosity
   double inv_h;       // 1/h when uniform
   int nl_cap;         // neighbour-list capacity per particle
   int pair_block;     // threads per block of the FP32C pair kernels (psph_autotune)
   int xsub;           // x-slabs per cell in the sort (1, 2 or 4; psph_autotune)
+  int nlist_stage;    // staged candidates per block of the neighbour scan (0 = global; psph_autotune)
   double xsph, sqrt_h_a;
   double gravity[3], body_force[3];
   double gb[3];       // gravity + body force (the sum every pair kernel starts from)
@@ -136,6 +148,7 @@ PSPH_D const Persist& next_persist(const DevView& v) { return v.sc->buf ? v.PA :
 // Launch wrappers (defined in the .cu files).
 void launch_sort(const DevView& v, cudaStream_t st);      // bin + scan + scatter + rank + reorder + flip
 void launch_nlist(const DevView& v, cudaStream_t st);     // per-step neighbour lists
+void nlist_configure();                                   // once, outside stream capture: shared-memory limits
 void launch_prepare(const DevView& v, cudaStream_t st);   // per-particle derived quantities, TIR
 void launch_prepare32(const DevView& v, cudaStream_t st); // FP32C form: copies + wall interpolation
 void launch_forces32(const DevView& v, cudaStream_t st);  // FP32C form: fluid pair forces

@@ -257,9 +257,36 @@ __global__ void __launch_bounds__(kFT) prepare_wall_kernel(DevView v) {
 }
 
 // ---------------------------------------------------------------------------
-// Fluid pair force (CalcForce11) from the side of free particle i
+// Fluid pair force (CalcForce11) from the side of free particle i.
+//
+// HALF = false: every pair is evaluated from both sides (the gather form).
+// HALF = true (pass A of the once-per-pair form): CalcForce11 updates both
+// particles of a pair from one evaluation (Source/Interaction.cpp:139-145), so
+// a pair of two free particles whose neighbour lists are both in use is
+// evaluated once, by the lower sorted index, which keeps its own terms and
+// writes the partner's terms (a, dDensity, ZWab, SumDen) into the partner's
+// own list slot of the pair: each list ascends as unsigned (cell-offset code
+// << 26 | index), so the partner's entry for i is found by a binary search
+// for (mirror code, i). Pairs with a wall are evaluated by the free side, as
+// in the gather form. forces_fluid_fold_kernel (pass B) then adds the
+// partners' terms in list order. Both sums keep a fixed order: no atomics,
+// deterministic results.
 // ---------------------------------------------------------------------------
-template <int DIM, int KT>
+// i's slot in j's list: the entry (mirror code, i) of j's ascending list, or -1
+PSPH_D int partner_slot(const DevView& v, int j, int code, int i) {
+  const unsigned key = ((unsigned)(26 - code) << kCodeShift) | (unsigned)i;
+  int lo = 0, hi = v.S.nl_count[j] - 1;
+  while (lo <= hi) {
+    const int mid = (lo + hi) >> 1;
+    const unsigned e = (unsigned)v.S.nl[nl_index(v.nl_stride, j, mid)];
+    if (e == key) return mid;
+    if (e < key) lo = mid + 1;
+    else hi = mid - 1;
+  }
+  return -1;
+}
+
+template <int DIM, int KT, bool HALF>
 __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
   __shared__ double red[kFT / 32];
   __shared__ unsigned long long cred[kFT / 32];
@@ -309,6 +336,11 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
   NbrSource<DIM> src;
   src.init(v, g, i, active && cell >= 0, 1.004f);
   bool more = active && cell >= 0;
+  // once-per-pair form: i's list is in use (not overflowed)
+  const bool own_list = HALF && active && cell >= 0 && v.S.nl_count[i] >= 0;
+  const int shep_pair = o.shepard_step;  // the counter is per instance: partners share it
+  // a partner slot written this step carries the instance's step number + 1
+  const int stamp = (int)(Is.steps & 0x3fffffff) + 1;
   while (true) {
     int qn = 0;
     while (more && qn < kQN) {
@@ -318,14 +350,21 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
         more = false;
         break;
       }
-      qbuf[qn++][tid] = j;
+      // once-per-pair form: a shared pair with a lower-index partner is that
+      // partner's; left out of the queue, so the lanes' queues hold only work
+      if (HALF && own_list && j < i && v.S.nl_count[j] >= 0 && CT[P.cls[j]].is_free) continue;
+      qbuf[qn++][tid] = HALF ? (j | (code << kCodeShift)) : j;
     }
     const int qmax = __reduce_max_sync(0xffffffffu, qn);
     for (int k = 0; k < qmax; ++k) {
       if (k >= qn) continue;
-      const int j = qbuf[k][tid];
+      const int qe = qbuf[k][tid];
+      const int j = HALF ? (qe & kIndexMask) : qe;
       const double4_32a xj = P.X4[j];
       const PClass& Cj = CT[P.cls[j]];
+      // shared pair: both free, both lists in use; the lower index evaluates it
+      // (the queue holds only those with j > i)
+      const bool share = own_list && Cj.is_free && v.S.nl_count[j] >= 0;
       const double hb = (hi + Cj.h) / 2;
       double x0 = xi.x - xj.x, x1 = xi.y - xj.y, x2 = xi.z - xj.z;
       if (any_periodic) periodic_fix(g, x0, x1, x2, hb, cci, decode(g, v.S.cellid[j]));
@@ -442,8 +481,34 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
       drho += mj * di * inv_j * (GK * vx);
       zw += mj * inv_j * K;
       if (shep) sd += mj * K;
+      if (HALF && share) {
+        // j's terms of this evaluation, seen from j (x_ji = -x_ij, v_ji = -v_ij):
+        // a_j -= m_i F, dDensity_j += m_i (rho_j / rho_i) v.GK x, ZWab_j += m_i / rho_i W,
+        // SumDen_j += m_i W (Source/Interaction.cpp:139-145, :170-177)
+        npair2 += 1ull;  // the partner's half of the count
+        const int slot = partner_slot(v, j, qe >> kCodeShift, i);
+        if (slot < 0) {
+          atomicOr(&v.sc->status, ST_LIST_MISMATCH);
+        } else {
+          const size_t e = nl_index(v.nl_stride, j, slot);
+          const double fx = mi * (s * x0 + VI0), fy = mi * (s * x1 + VI1), fz = DIM == 3 ? mi * (s * x2 + VI2) : 0.0;
+          v.S.half4[e] = make_double4_32a(-fx, -fy, -fz, mi * dj * inv_i * (GK * vx));
+          const bool shep_j = Cj.shepard && (Is.shepard_counter == shep_pair);
+          v.S.half2[e] = make_double2(mi * inv_i * K, shep_j ? mi * K : 0.0);
+          v.S.half_stamp[e] = stamp;  // written this step
+        }
+      }
     }
     if (!__any_sync(0xffffffffu, more)) break;
+  }
+  if (HALF) {  // own terms; pass B adds the partners', then the dt bound
+    if (active) {
+      v.S.A4[i] = make_double4_32a(ax, ay, az, drho);
+      v.S.zwab[i] = zw;
+      if (o.any_shepard) v.S.sumden[i] = sd;
+    }
+    block_dt_and_pairs<kFT>(v, Ci.inst, false, dtc, npair2, red, cred);
+    return;
   }
   if (active) {
     v.S.A4[i] = make_double4_32a(ax, ay, az, drho);
@@ -466,6 +531,67 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
     if (cand < dtc) dtc = cand;  // NaN never compares less, as in the reference
   }
   block_dt_and_pairs<kFT>(v, Ci.inst, active, dtc, npair2, red, cred);
+}
+
+// Pass B of the once-per-pair form: adds, in list order, the terms the
+// partners with a lower index wrote into i's slots this step (their slot
+// stamp is this step's; a slot of a pair outside the support, or of a partner
+// that evaluated its own side, keeps an older stamp), then the dt bound and
+// the finiteness check of the gather form.
+template <int DIM>
+__global__ void __launch_bounds__(kFT) forces_fluid_fold_kernel(DevView v) {
+  __shared__ double red[kFT / 32];
+  __shared__ unsigned long long cred[kFT / 32];
+  const StepScalars* sc = v.sc;
+  if (sc->all_stop) return;
+  const Persist& P = cur_persist(v);
+  const int n = sc->n;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const Options& o = v.o;
+  const PClass* __restrict__ CT = v.cls;
+  bool active = false;
+  int cell = -1, ci_cls = 0;
+  if (i < n) {
+    ci_cls = P.cls[i];
+    active = !v.inst[CT[ci_cls].inst].stop && CT[ci_cls].is_free;
+    cell = v.S.cellid[i];
+  }
+  const PClass& Ci = CT[ci_cls];
+  double dtc = DBL_MAX;
+  if (active) {
+    const int stamp = (int)(v.inst[Ci.inst].steps & 0x3fffffff) + 1;
+    double4_32a a = v.S.A4[i];
+    double zw = v.S.zwab[i], sd = o.any_shepard ? v.S.sumden[i] : 0.0;
+    const int cnt = cell >= 0 ? v.S.nl_count[i] : -1;
+    const int4* __restrict__ nl4 = reinterpret_cast<const int4*>(v.S.nl) + nl_slot(i);
+    const size_t N = (size_t)v.nl_stride;
+    for (int c = 0; 4 * c < cnt; ++c) {  // one 16-byte chunk of 4 entries per load
+      const int4 q = nl4[(size_t)c * N];
+      const int ent[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        if (4 * c + e >= cnt || (ent[e] & kIndexMask) >= i) continue;
+        const size_t sl = nl_index(v.nl_stride, i, 4 * c + e);
+        if (v.S.half_stamp[sl] != stamp) continue;
+        const double4_32a t = v.S.half4[sl];
+        const double2 u = v.S.half2[sl];
+        a.x += t.x;
+        a.y += t.y;
+        a.z += t.z;
+        a.w += t.w;
+        zw += u.x;
+        sd += u.y;
+      }
+    }
+    v.S.A4[i] = a;
+    v.S.zwab[i] = zw;
+    if (o.any_shepard) v.S.sumden[i] = sd;
+    if (!(isfinite(a.x) && isfinite(a.y) && isfinite(a.z) && isfinite(a.w))) atomicOr(&v.sc->status, ST_NONFINITE);
+    const double an = sqrt(a.x * a.x + a.y * a.y + a.z * a.z);
+    const double cand = o.sqrt_h_a * sqrt(Ci.h / an);
+    if (cand < dtc) dtc = cand;  // NaN never compares less, as in the reference
+  }
+  block_dt_and_pairs<kFT>(v, Ci.inst, active, dtc, 0ull, red, cred);
 }
 
 // ---------------------------------------------------------------------------
@@ -784,11 +910,26 @@ void forces_dispatch(const DevView& v, cudaStream_t st) {
       case 1: forces_solid_kernel<DIM, 1><<<nb, kFT, 0, st>>>(v); break;
       default: forces_solid_kernel<DIM, 2><<<nb, kFT, 0, st>>>(v); break;
     }
+  } else if (v.o.fp64_half) {  // each pair once: pass A, then the partners' terms
+    switch (v.o.kt) {
+      case 0:
+        forces_fluid_kernel<DIM, 0, true><<<nb, kFT, 0, st>>>(v);
+        forces_fluid_fold_kernel<DIM><<<nb, kFT, 0, st>>>(v);
+        break;
+      case 1:
+        forces_fluid_kernel<DIM, 1, true><<<nb, kFT, 0, st>>>(v);
+        forces_fluid_fold_kernel<DIM><<<nb, kFT, 0, st>>>(v);
+        break;
+      default:
+        forces_fluid_kernel<DIM, 2, true><<<nb, kFT, 0, st>>>(v);
+        forces_fluid_fold_kernel<DIM><<<nb, kFT, 0, st>>>(v);
+        break;
+    }
   } else {
     switch (v.o.kt) {
-      case 0: forces_fluid_kernel<DIM, 0><<<nb, kFT, 0, st>>>(v); break;
-      case 1: forces_fluid_kernel<DIM, 1><<<nb, kFT, 0, st>>>(v); break;
-      default: forces_fluid_kernel<DIM, 2><<<nb, kFT, 0, st>>>(v); break;
+      case 0: forces_fluid_kernel<DIM, 0, false><<<nb, kFT, 0, st>>>(v); break;
+      case 1: forces_fluid_kernel<DIM, 1, false><<<nb, kFT, 0, st>>>(v); break;
+      default: forces_fluid_kernel<DIM, 2, false><<<nb, kFT, 0, st>>>(v); break;
     }
   }
 }

@@ -146,7 +146,15 @@ __global__ void __launch_bounds__(kFT32) copies32_kernel(DevView v) {
   if (v.inst[C.inst].stop) return;
   const double4_32a vv = P.V4[w];
   const float p = (float)vv.w;
-  v.S.V32[w] = make_float4((float)vv.x, (float)vv.y, (float)vv.z, p);
+  const float vx = (float)vv.x, vy = (float)vv.y, vz = (float)vv.z;
+  v.S.V32[w] = make_float4(vx, vy, vz, p);
+  // the velocity's low-order part: in a smooth flow v_i - v_j is far smaller
+  // than v, and the pair differences take (hi_i - hi_j) + (lo_i - lo_j), exact
+  // to ~2^-48 of |v|; the class index and its flags ride along in .w (class |
+  // flags << 16: one load per pair, and no class-table load when the pair
+  // constants are uniform)
+  v.S.V32LO[w] = make_float4((float)(vv.x - (double)vx), (float)(vv.y - (double)vy), (float)(vv.z - (double)vz),
+                             __int_as_float(P.cls[w] | (C.flags << 16)));
   if (C.flags & CF_FREE) {
     const float rho = (float)P.X4[w].w;
     const float inv = 1.f / rho;
@@ -269,18 +277,22 @@ __global__ void __launch_bounds__(kFT32) prepare32_kernel(DevView v) {
 // Fluid pair force, FP32 with compensated sums, over the neighbour lists
 // ---------------------------------------------------------------------------
 // FL selects a compile-time specialisation: 0 = every option read at run time;
-// 1 and 2 = Morris viscosity, squared-density gradient, no tensile-instability
-// term and no XSPH (the dam-break configuration), without (1) or with (2) the
-// strain-rate sums of the LES / Bingham options. The list walk is a counted
+// 1, 2 and 3 = Morris viscosity, squared-density gradient, no tensile-instability
+// term, no XSPH, one h, and pair constants (artificial viscosity, masses) the
+// same for every class, taken from the launch parameters instead of the class
+// table (the dam-break configuration): without (1) or with (2) the strain-rate
+// sums of the LES / Bingham options, or with them and the learned closure's
+// vorticity (3). The list walk is a counted
 // loop so that the next neighbour's loads can be issued before this one's
 // arithmetic; each pair issues all of its neighbour loads before the support
 // test (ld_early).
-// Register caps measured on the 6.7M-particle dam break: the strain-rate
-// flavour runs best at 96 (20 warps/SM), the plain one at 72 (28 warps/SM,
-// a few spilled values in L1), the general one at 128.
+// Register caps measured on the 6.7M-particle dam break (64 to 112 swept): the
+// strain-rate flavours run best at 96 (20 warps/SM), the plain one at 80, the
+// general one at 128.
 template <int DIM, int KT, int FL>
-__global__ void __maxnreg__(FL == 0 ? 128 : (FL == 1 ? 72 : 96)) forces_fluid32_kernel(DevView v) {
+__global__ void __maxnreg__(FL == 0 ? 128 : (FL == 1 ? 80 : 96)) forces_fluid32_kernel(DevView v) {
   constexpr bool SPEC = FL != 0;
+  constexpr bool CLOSURE = FL == 3;
   __shared__ unsigned long long cred[32];
   const StepScalars* sc = v.sc;
   if (sc->all_stop) return;
@@ -290,7 +302,7 @@ __global__ void __maxnreg__(FL == 0 ? 128 : (FL == 1 ? 72 : 96)) forces_fluid32_
   const Options& o = v.o;
   const PClass32* __restrict__ CT = v.cls32;
   float dtc = FLT_MAX;
-  unsigned long long npair2 = 0;
+  unsigned npair2 = 0;  // 2 per pair with a free partner, 1 per wall partner (the pair is counted once)
   bool active = false;
   int cell = -1, ci_cls = 0;
   if (i < n) {
@@ -309,6 +321,7 @@ __global__ void __maxnreg__(FL == 0 ? 128 : (FL == 1 ? 72 : 96)) forces_fluid32_
   const int is = active ? i : 0;
   const float4 oi = v.S.OFF32[is];
   const float4 vi = v.S.V32[is];
+  const float4 vil = v.S.V32LO[is];
   const float4 di4 = v.S.D32[is];
   const float di = di4.w, inv_i = di4.x, Pi = di4.y, ci_snd = di4.z, pi = vi.w;
   const float mi = Ci.mass, hi = oi.w;
@@ -316,7 +329,7 @@ __global__ void __maxnreg__(FL == 0 ? 128 : (FL == 1 ? 72 : 96)) forces_fluid32_
   const int fi = Ci.flags;
   const bool shep = (fi & CF_SHEPARD) && (Is.shepard_counter == o.shepard_step);
   const bool sr_self = fi & (CF_T0 | CF_LES);
-  const bool use_sr = SPEC ? (FL == 2) : (bool)o.need_sr;
+  const bool use_sr = SPEC ? (FL >= 2) : (bool)o.need_sr;
   const bool xsph_on = SPEC ? false : o.xsph != 0.0;
   const float xsph = o.xsph32;
   const float3 cs = cell_size_f(g);
@@ -325,28 +338,35 @@ __global__ void __maxnreg__(FL == 0 ? 128 : (FL == 1 ? 72 : 96)) forces_fluid32_
   const int vis_eq = SPEC ? 0 : o.vis_eq, grad_type = SPEC ? 0 : o.grad_type;
   Kahan ax, ay, az, dr;
   float zw = 0.f, sd = 0.f, xs0 = 0.f, xs1 = 0.f, xs2 = 0.f;
-  float sr0 = 0.f, sr1 = 0.f, sr2 = 0.f, sr4 = 0.f, sr5 = 0.f, sr8 = 0.f;
-  float w01 = 0.f, w02 = 0.f, w12 = 0.f;  // antisymmetric counterpart of the strain-rate sums (closure)
+  // strain-rate sums as sums of products a_r x_c (a = c2 vab): diagonal
+  // m00 m11 m22, and the off-diagonal pairs either summed (s01 = m01 + m10 ...)
+  // or, with the closure (whose vorticity needs the antisymmetric part), kept
+  // apart (m01, m10, ...)
+  float m00 = 0.f, m11 = 0.f, m22 = 0.f, m01 = 0.f, m02 = 0.f, m12 = 0.f, m10 = 0.f, m20 = 0.f, m21 = 0.f;
   int nnb = 0;
-  const bool closure = o.closure && (fi & CF_LES);
+  const bool closure = SPEC ? (CLOSURE && (fi & CF_LES)) : (o.closure && (fi & CF_LES));
+  // the closure flavour always keeps the antisymmetric sums apart
+  const bool split_sr = SPEC ? CLOSURE : closure;
   const float cf2 = g.cellfac2_32;
   const bool uniform_h = o.uniform_h;
   const float ih_u = o.inv_h32;
   auto pair = [&](const int j, const int code) {
     const float4 oj = v.S.OFF32[j];
-    const int clsj = ld_early(P.cls + j);
+    const float4 vjl = ld_early(v.S.V32LO + j);
     const float4 vj = ld_early(v.S.V32 + j);
     const float4 dj4 = ld_early(v.S.D32 + j);
+    const int wj = __float_as_int(vjl.w);
+    const int clsj = wj & 0xffff;
     float x0, x1, x2;
     rel_pos<DIM>(cs, oi, oj, code, x0, x1, x2);
-    const float hb = 0.5f * (hi + oj.w);
+    const float hb = SPEC ? hi : 0.5f * (hi + oj.w);  // one h: (h + h) / 2 = h exactly
     const float r2 = x0 * x0 + x1 * x1 + x2 * x2;
     // the list's own support test (exact in FP32; lists with a skin hold more)
     if (r2 > cf2 * hb * hb) return;
-    const PClass32& Cj = CT[clsj];
-    const int fjf = Cj.flags;
+    const PClass32& Cj = CT[SPEC ? 0 : clsj];
+    const int fjf = wj >> 16;
     const bool fj = fjf & CF_FREE;
-    npair2 += fj ? 1ull : 2ull;
+    npair2 += fj ? 1u : 2u;
     ++nnb;
     // FP32C divisions use the hardware reciprocal (2 ulp; the form's bound is 1e-5)
     const float ih = uniform_h ? ih_u : __fdividef(1.f, hb);
@@ -359,11 +379,13 @@ __global__ void __maxnreg__(FL == 0 ? 128 : (FL == 1 ? 72 : 96)) forces_fluid32_
     const float GK = KernF<DIM, KT>::GK(q, inv_q, cwg);
     const float K = KernF<DIM, KT>::W(q, cwh);
     const float dj = dj4.w, inv_j = dj4.x, Pj = dj4.y, cj_snd = dj4.z, pj = vj.w;
-    const float mj = fj ? Cj.mass : Cj.fpmassc * mi;
-    const float v0 = vi.x - vj.x, v1 = vi.y - vj.y, v2 = vi.z - vj.z;
+    const float mj = SPEC ? (fj ? o.m_free32 : o.fpm_wall32 * mi) : (fj ? Cj.mass : Cj.fpmassc * mi);
+    const float v0 = (vi.x - vj.x) + (vil.x - vjl.x), v1 = (vi.y - vj.y) + (vil.y - vjl.y),
+                v2 = (vi.z - vj.z) + (vil.z - vjl.z);
     const float vx = v0 * x0 + v1 * x1 + v2 * x2;
     float PI = 0.f;
-    const float Alpha = 0.5f * (Ci.alpha + Cj.alpha), Beta = 0.5f * (Ci.beta + Cj.beta);
+    const float Alpha = SPEC ? o.alpha32 : 0.5f * (Ci.alpha + Cj.alpha);
+    const float Beta = SPEC ? o.beta32 : 0.5f * (Ci.beta + Cj.beta);
     if ((Alpha != 0.f || Beta != 0.f) && vx < 0.f) {
       const float D = r2 + 0.01f * hb * hb;
       const float t = hb * vx;
@@ -386,14 +408,14 @@ __global__ void __maxnreg__(FL == 0 ? 128 : (FL == 1 ? 72 : 96)) forces_fluid32_
         vab0 = v0; vab1 = v1; vab2 = v2;
         if (uniform_mu) Mu = mu_u;
         else {
-          const float muj = dyn_mu ? v.S.MU32[j] : Cj.mu0;
+          const float muj = dyn_mu ? v.S.MU32[j] : (SPEC ? Ci.mu0 : Cj.mu0);
           Mu = __fdividef(2.f * mui * muj, mui + muj);
         }
       } else {
         const float4 ns = v.S.NSV32[j];
-        vab0 = vi.x - (2.f * vj.x - ns.x);
-        vab1 = vi.y - (2.f * vj.y - ns.y);
-        vab2 = vi.z - (2.f * vj.z - ns.z);
+        vab0 = (vi.x - (2.f * vj.x - ns.x)) + (vil.x - 2.f * vjl.x);
+        vab1 = (vi.y - (2.f * vj.y - ns.y)) + (vil.y - 2.f * vjl.y);
+        vab2 = (vi.z - (2.f * vj.z - ns.z)) + (vil.z - 2.f * vjl.z);
         Mu = mui;
       }
       if (vis_eq <= 2) {
@@ -412,17 +434,24 @@ __global__ void __maxnreg__(FL == 0 ? 128 : (FL == 1 ? 72 : 96)) forces_fluid32_
         VI2 = s * (L * vab2 + (1.f / 3.f) * (GK * v2 + t * x2));
       }
       if (use_sr && sr_self && (((fi | fjf) & CF_T0) || ((fi & fjf) & CF_LES))) {
+        // StrainRate += (m_j / rho_j) S with S = -GK [2 v_a x_a, v_a x_b + v_b x_a, ...]
+        // (Source/Interaction.cpp:114-117, no 1/2): a = c2 vab, S_rc = a_r x_c + a_c x_r
         const float c2 = -GK * (mj * inv_j);
-        sr0 += c2 * (2.f * vab0 * x0);
-        sr1 += c2 * (vab0 * x1 + vab1 * x0);
-        sr2 += c2 * (vab0 * x2 + vab2 * x0);
-        sr4 += c2 * (2.f * vab1 * x1);
-        sr5 += c2 * (vab1 * x2 + vab2 * x1);
-        sr8 += c2 * (2.f * vab2 * x2);
-        if (closure) {
-          w01 += c2 * (vab0 * x1 - vab1 * x0);
-          w02 += c2 * (vab0 * x2 - vab2 * x0);
-          w12 += c2 * (vab1 * x2 - vab2 * x1);
+        const float a0 = c2 * vab0, a1 = c2 * vab1, a2 = c2 * vab2;
+        m00 = fmaf(a0, x0, m00);
+        m11 = fmaf(a1, x1, m11);
+        m22 = fmaf(a2, x2, m22);
+        m01 = fmaf(a0, x1, m01);
+        m02 = fmaf(a0, x2, m02);
+        m12 = fmaf(a1, x2, m12);
+        if (split_sr) {
+          m10 = fmaf(a1, x0, m10);
+          m20 = fmaf(a2, x0, m20);
+          m21 = fmaf(a2, x1, m21);
+        } else {
+          m01 = fmaf(a1, x0, m01);
+          m02 = fmaf(a2, x0, m02);
+          m12 = fmaf(a2, x1, m12);
         }
       }
     }
@@ -447,7 +476,7 @@ __global__ void __maxnreg__(FL == 0 ? 128 : (FL == 1 ? 72 : 96)) forces_fluid32_
     const int nch = (cnt + 3) >> 2;
     // the strain-rate flavour loads the next chunk one chunk ahead (measured:
     // it helps there and costs the plain flavour a little)
-    constexpr bool kAhead = FL == 2;
+    constexpr bool kAhead = FL >= 2;
     int4 qn = (kAhead && nch > 0) ? nl4[0] : make_int4(0, 0, 0, 0);
     for (int c = 0; c < nch; ++c) {  // one 16-byte chunk of 4 entries per load
       int4 q;
@@ -483,6 +512,12 @@ __global__ void __maxnreg__(FL == 0 ? 128 : (FL == 1 ? 72 : 96)) forces_fluid32_
     if (o.any_shepard) v.S.sumden[i] = sd;
     if (xsph_on) v.S.vxsph4[i] = make_double4_32a(xs0, xs1, xs2, 0.0);
     if (use_sr) {
+      // symmetric sums 2 m_rr and m_rc + m_cr; the antisymmetric m_rc - m_cr
+      // (closure) is the vorticity's
+      const float sr0 = 2.f * m00, sr4 = 2.f * m11, sr8 = 2.f * m22;
+      const float sr1 = split_sr ? m01 + m10 : m01, sr2 = split_sr ? m02 + m20 : m02,
+                  sr5 = split_sr ? m12 + m21 : m12;
+      const float w01 = m01 - m10, w02 = m02 - m20, w12 = m12 - m21;
       // the 6 distinct sums in FP32 (the FP64 tensor is built on download)
       float2* out = reinterpret_cast<float2*>(v.S.sr32 + 6 * (size_t)i);
       out[0] = make_float2(sr0, sr1);
@@ -511,7 +546,7 @@ __global__ void __maxnreg__(FL == 0 ? 128 : (FL == 1 ? 72 : 96)) forces_fluid32_
     const float cand = o.sqrt_h_a32 * sqrtf(Ci.h / an);
     if (cand < dtc) dtc = cand;
   }
-  block_dt32_and_pairs(v, Ci.inst, active, dtc, npair2, cred);
+  block_dt32_and_pairs(v, Ci.inst, active, dtc, (unsigned long long)npair2, cred);
 }
 
 // ---------------------------------------------------------------------------
@@ -567,7 +602,7 @@ __global__ void __maxnreg__(128) forces_solid32_kernel(DevView v) {
   const Options& o = v.o;
   const PClass32* __restrict__ CT = v.cls32;
   double dtc = DBL_MAX;
-  unsigned long long npair2 = 0;
+  unsigned npair2 = 0;  // 2 per pair with a free partner, 1 per wall partner (the pair is counted once)
   bool active = false;
   int cell = -1, ci_cls = 0;
   if (i < n) {
@@ -775,18 +810,22 @@ void forces32_dispatch(const DevView& v, cudaStream_t st) {
     return;
   }
   const Options& o = v.o;
-  const bool spec = o.vis_eq == 0 && o.grad_type == 0 && !o.any_ti && o.xsph == 0.0;
-  const int fl = spec ? (o.need_sr ? 2 : 1) : 0;
-  switch (o.kt * 3 + fl) {
+  const bool spec = o.vis_eq == 0 && o.grad_type == 0 && !o.any_ti && o.xsph == 0.0 && o.uniform_h &&
+                    o.uniform_av && o.uniform_mass && (o.uniform_mu || o.dyn_mu);
+  const int fl = spec ? (o.need_sr ? (o.closure ? 3 : 2) : 1) : 0;
+  switch (o.kt * 4 + fl) {
     case 0: forces_fluid32_kernel<DIM, 0, 0><<<nb, bt, 0, st>>>(v); break;
     case 1: forces_fluid32_kernel<DIM, 0, 1><<<nb, bt, 0, st>>>(v); break;
     case 2: forces_fluid32_kernel<DIM, 0, 2><<<nb, bt, 0, st>>>(v); break;
-    case 3: forces_fluid32_kernel<DIM, 1, 0><<<nb, bt, 0, st>>>(v); break;
-    case 4: forces_fluid32_kernel<DIM, 1, 1><<<nb, bt, 0, st>>>(v); break;
-    case 5: forces_fluid32_kernel<DIM, 1, 2><<<nb, bt, 0, st>>>(v); break;
-    case 6: forces_fluid32_kernel<DIM, 2, 0><<<nb, bt, 0, st>>>(v); break;
-    case 7: forces_fluid32_kernel<DIM, 2, 1><<<nb, bt, 0, st>>>(v); break;
-    default: forces_fluid32_kernel<DIM, 2, 2><<<nb, bt, 0, st>>>(v); break;
+    case 3: forces_fluid32_kernel<DIM, 0, 3><<<nb, bt, 0, st>>>(v); break;
+    case 4: forces_fluid32_kernel<DIM, 1, 0><<<nb, bt, 0, st>>>(v); break;
+    case 5: forces_fluid32_kernel<DIM, 1, 1><<<nb, bt, 0, st>>>(v); break;
+    case 6: forces_fluid32_kernel<DIM, 1, 2><<<nb, bt, 0, st>>>(v); break;
+    case 7: forces_fluid32_kernel<DIM, 1, 3><<<nb, bt, 0, st>>>(v); break;
+    case 8: forces_fluid32_kernel<DIM, 2, 0><<<nb, bt, 0, st>>>(v); break;
+    case 9: forces_fluid32_kernel<DIM, 2, 1><<<nb, bt, 0, st>>>(v); break;
+    case 10: forces_fluid32_kernel<DIM, 2, 2><<<nb, bt, 0, st>>>(v); break;
+    default: forces_fluid32_kernel<DIM, 2, 3><<<nb, bt, 0, st>>>(v); break;
   }
 }
 

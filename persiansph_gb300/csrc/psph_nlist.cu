@@ -14,9 +14,20 @@
 //
 // With one h everywhere (nlist_pair_kernel) a lane scans for two particles of
 // one cell at once; otherwise (nlist_kernel) a lane scans for one particle.
+//
+// Staged form (nlist_staged_kernel, one h everywhere, x not periodic): a block
+// first copies the candidate positions of its particles' neighbour cells into
+// shared memory with TMA bulk copies, then scans them there. The block's 256
+// particles are consecutive in cell order, so they occupy one row of cells
+// (or the end of one row and the start of the next); for each such home row
+// and each of the 3 (2D) or 9 (3D) neighbouring rows, the cells within one of
+// the home cells' x-range form one contiguous range of sorted particles: one
+// bulk copy each. A block whose ranges do not fit the staging buffer, or
+// whose particles span more rows or instances, scans global memory as before.
 #include <algorithm>
 
 #include "psph_pairs.cuh"
+#include "psph_tma.cuh"
 
 namespace psph {
 
@@ -179,6 +190,29 @@ __global__ void __launch_bounds__(kNT, 8) nlist_kernel(DevView v, float margin) 
   list_one<DIM, UNIFORM_H>(v, i, margin, &ring[0][threadIdx.x]);
 }
 
+// Where the scan reads a candidate's FP32 offset: global memory, or the
+// block's staged copy (row k of the lane's home row: smem index j + delta[k]).
+struct GlobalCands {
+  const float4* __restrict__ off;
+  __device__ __forceinline__ void home(int) {}
+  __device__ __forceinline__ void row(int) {}
+  __device__ __forceinline__ float4 at(int j) const { return off[j]; }
+};
+template <int RPH>
+struct StagedCands {
+  uint32_t sbase;     // shared address of the staged offsets
+  const int* delta;   // smem index - global index, per home row (2) x neighbour row (RPH)
+  int row_a;          // the first home row (z * ny + y); the second is the next one
+  int hsel = 0, d = 0;
+  __device__ __forceinline__ void home(int r) { hsel = (r == row_a) ? 0 : RPH; }
+  __device__ __forceinline__ void row(int k) { d = delta[hsel + k]; }
+  __device__ __forceinline__ float4 at(int j) const { return tma::lds128(sbase + 16u * (uint32_t)(j + d)); }
+};
+
+template <int DIM, class Cands>
+__device__ __forceinline__ void scan_two(const DevView& v, int ia, int n, float margin, Cands cand,
+                                         int (*ring)[8][kNT]);
+
 // One h everywhere: a lane builds the lists of sorted particles 2t and 2t+1
 // when they share a cell. Both scan the same cell block, so each candidate is
 // loaded once and tested against both, and the rows and slabs walked are the
@@ -199,7 +233,14 @@ __global__ void __launch_bounds__(kNT, 8) nlist_pair_kernel(DevView v, float mar
   }
   const int n = sc->n;
   const int t = (blockIdx.x - nr) * kNT + threadIdx.x;
-  const int ia = 2 * t, ib = ia + 1;
+  scan_two<DIM>(v, 2 * t, n, margin, GlobalCands{v.S.OFF32}, ring);
+}
+
+// The two-particle scan of sorted particles ia and ia + 1 (one lane).
+template <int DIM, class Cands>
+__device__ __forceinline__ void scan_two(const DevView& v, int ia, int n, float margin, Cands cand,
+                                         int (*ring)[8][kNT]) {
+  const int ib = ia + 1;
   if (ia >= n) return;
   const int cell = v.S.cellid[ia];
   const int cellb = ib < n ? v.S.cellid[ib] : -1;
@@ -220,10 +261,11 @@ __global__ void __launch_bounds__(kNT, 8) nlist_pair_kernel(DevView v, float mar
   const float thr = cf * cf * oa.w * oa.w * margin;
   const int N = v.nl_stride, cap = v.o.nl_cap;
   const CellCoord c = decode(g, cell);
-  const float4* __restrict__ off = v.S.OFF32;
+  cand.home(c.z * g.nc[1] + c.y);
   int4* const nl4 = reinterpret_cast<int4*>(v.S.nl);
   ListWriter wa{&ring[0][0][threadIdx.x], nl4 + nl_slot(ia)};
   ListWriter wb{&ring[1][0][threadIdx.x], nl4 + nl_slot(ib)};
+  const int zlo_ = (DIM == 3) ? -1 : 0;
   const bool cull = c.x > 0 && c.x < g.nc[0] - 1 && c.y > 0 && c.y < g.nc[1] - 1 &&
                     (DIM == 2 || (c.z > 0 && c.z < g.nc[2] - 1));
   const float thr_cull = thr * 1.0001f;
@@ -246,6 +288,7 @@ __global__ void __launch_bounds__(kNT, 8) nlist_pair_kernel(DevView v, float mar
       const int base = g.cell_base + (z * g.nc[1] + y) * g.nc[0];
       const int cyz = 3 * (dy + 1) + 9 * (dz + 1);
       const float cy = -(float)dy * cs.y, cz = -(float)dz * cs.z;
+      cand.row(3 * (dz - zlo_) + (dy + 1));
       int slo = -xs, shi = 2 * xs - 1;
       if (cull) {  // the union of the two particles' reach
         int la, ha, lb, hb;
@@ -275,7 +318,7 @@ __global__ void __launch_bounds__(kNT, 8) nlist_pair_kernel(DevView v, float mar
         const float2 AX = make_float2(axa, axb), AY = make_float2(aya, ayb), AZ = make_float2(aza, azb);
         const float2 M1 = make_float2(-1.f, -1.f);
         auto test = [&](int j, bool& ina, bool& inb) {
-          const float4 oj = off[j];
+          const float4 oj = cand.at(j);
           const float2 ex = __ffma2_rn(make_float2(oj.x, oj.x), M1, AX);
           const float2 ey = __ffma2_rn(make_float2(oj.y, oj.y), M1, AY);
           float2 d2 = __fmul2_rn(ex, ex);
@@ -334,6 +377,115 @@ __global__ void __launch_bounds__(kNT, 8) nlist_pair_kernel(DevView v, float mar
   if (pair) wb.finish(cap, v.S.nl_count + ib);
 }
 
+// Staged form of nlist_pair_kernel (see the file header). Warp 0 plans the
+// block's copies: the home rows of its particles and, per home row and
+// neighbour row, the sorted range of the cells within one of the home cells'
+// x-range; lane 0 arms the mbarrier with the total bytes and each planning lane
+// issues its range's bulk copy. Every thread waits for the copies with a time
+// limit; a thread whose wait gives up sets ST_STAGE_TIMEOUT, scans global
+// memory instead, and waits again (bounded) before the block exits, so no copy
+// lands in shared memory the block no longer owns.
+constexpr unsigned long long kStageWaitNs = 1000000000ull;
+
+template <int DIM>
+__global__ void __launch_bounds__(kNT, 4) nlist_staged_kernel(DevView v, float margin, int nr, int cap_stage) {
+  constexpr int RPH = (DIM == 3) ? 9 : 3;  // neighbour rows per home row
+  __shared__ int ring[2][8][kNT];
+  __shared__ int s_delta[2 * RPH];
+  __shared__ int s_row_a, s_mode;
+  __shared__ __align__(8) uint64_t s_bar;
+  extern __shared__ float4 s_off[];
+  StepScalars* sc = v.sc;
+  if (sc->all_stop) return;
+  if ((int)blockIdx.x < nr) {
+    const int m = min(sc->nl_rest, v.ncap);
+    for (int q = blockIdx.x * kNT + threadIdx.x; q < m; q += nr * kNT)
+      list_one<DIM, true>(v, v.S.tmp_perm[q], margin, &ring[0][0][threadIdx.x]);
+    return;
+  }
+  const int n = sc->n;
+  const int b = blockIdx.x - nr;
+  const int p0 = 2 * b * kNT;
+  if (threadIdx.x == 0) {
+    tma::mbar_init(&s_bar, 1);
+    tma::mbar_init_fence();
+  }
+  // plan (warp 0): lane q < nh * RPH owns the range of home row q / RPH and
+  // neighbour row q % RPH
+  int seg_lo = 0, cnt = 0, off = 0, total = 0;
+  if (threadIdx.x < 32) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x;
+    const int last = min(p0 + 2 * kNT, min(n, sc->n_cells)) - 1;
+    bool ok = p0 <= last;
+    const int ca = ok ? v.S.cellid[p0] : -1, cl = ok ? v.S.cellid[last] : -1;
+    ok = ok && ca >= 0 && cl >= 0;
+    const Persist& P = cur_persist(v);
+    const int inst = ok ? v.cls[P.cls[p0]].inst : 0;
+    ok = ok && v.cls[P.cls[last]].inst == inst;
+    const GridDev& g = grid_of(v, inst);
+    ok = ok && !g.periodic[0];
+    const CellCoord A = decode(g, ok ? ca : g.cell_base), L = decode(g, ok ? cl : g.cell_base);
+    const int ra = A.z * g.nc[1] + A.y, rl = L.z * g.nc[1] + L.y;
+    const int nh = (rl == ra) ? 1 : (rl == ra + 1 ? 2 : 0);
+    ok = ok && nh > 0;
+    if (ok && lane < nh * RPH) {
+      const int h = lane / RPH, k = lane % RPH;
+      const int hy = h ? L.y : A.y, hz = h ? L.z : A.z;
+      const int xlo = h ? 0 : A.x, xhi = (nh == 1 || h) ? L.x : g.nc[0] - 1;
+      const int dz = (DIM == 3) ? k / 3 - 1 : 0, dy = k % 3 - 1;
+      int y = hy + dy, z = hz + dz;
+      bool in = true;
+      if (g.periodic[1]) y = (y + g.nc[1]) % g.nc[1];
+      else if (y < 0 || y >= g.nc[1]) in = false;
+      if (g.periodic[2]) z = (z + g.nc[2]) % g.nc[2];
+      else if (z < 0 || z >= g.nc[2]) in = false;
+      if (in) {
+        const int base = g.cell_base + (z * g.nc[1] + y) * g.nc[0];
+        seg_lo = v.S.start[base + max(xlo - 1, 0)];
+        cnt = v.S.start[base + min(xhi + 1, g.nc[0] - 1) + 1] - seg_lo;
+      }
+    }
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(full, incl, o);
+      if (lane >= o) incl += y;
+    }
+    total = __shfl_sync(full, incl, 31);
+    off = incl - cnt;
+    ok = ok && total > 0 && total <= cap_stage;
+    if (lane < 2 * RPH) s_delta[lane] = off - seg_lo;
+    if (lane == 0) {
+      s_row_a = ra;
+      s_mode = ok;
+    }
+    if (!ok) cnt = 0;
+  }
+  __syncthreads();  // the plan and the initialised mbarrier
+  const bool staged = s_mode;
+  const uint32_t sbase = tma::smem_u32(s_off);
+  if (staged && threadIdx.x < 32) {
+    if (threadIdx.x == 0) tma::mbar_expect_tx(&s_bar, 16u * (uint32_t)total);
+    __syncwarp();
+    if (cnt > 0) tma::bulk_g2s(sbase + 16u * (uint32_t)off, v.S.OFF32 + seg_lo, 16u * (uint32_t)cnt, &s_bar);
+  }
+  bool use_stage = staged;
+  if (staged && !tma::mbar_wait_bounded(&s_bar, 0, kStageWaitNs)) {
+    atomicOr(&sc->status, ST_STAGE_TIMEOUT);
+    use_stage = false;
+  }
+  const int t = b * kNT + threadIdx.x;
+  if (use_stage) scan_two<DIM>(v, 2 * t, n, margin, StagedCands<RPH>{sbase, s_delta, s_row_a}, ring);
+  else scan_two<DIM>(v, 2 * t, n, margin, GlobalCands{v.S.OFF32}, ring);
+  if (staged && !use_stage) tma::mbar_wait_bounded(&s_bar, 0, kStageWaitNs);
+}
+
+// Deepest staging (Options::nlist_stage): 64 KB of FP32 offsets per block
+// (one home row of ~256 particles and its neighbour rows take ~2,600 in the
+// 3D dam break).
+constexpr int kStageCapMax = 4096;
+
 int sm_count() {
   static int n = 0;
   if (!n) {
@@ -347,6 +499,12 @@ int sm_count() {
 
 }  // namespace
 
+void nlist_configure() {
+  const int bytes = kStageCapMax * (int)sizeof(float4);
+  cudaFuncSetAttribute(nlist_staged_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(nlist_staged_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
 void launch_nlist(const DevView& v, cudaStream_t st) {
   // a superset of the support: the pair kernels apply the exact test (FP32 in
   // the FP32C form, FP64 in the plain form)
@@ -355,6 +513,13 @@ void launch_nlist(const DevView& v, cudaStream_t st) {
     const int half = (v.ncap + 1) / 2;
     const int nr = 2 * sm_count();
     const int nb = nr + (half > 0 ? (half + kNT - 1) / kNT : 1);
+    const int cap = min(v.o.nlist_stage, kStageCapMax);
+    if (cap > 0 && !v.o.any_periodic_x) {
+      const size_t smem = (size_t)cap * sizeof(float4);
+      if (v.o.dim == 2) nlist_staged_kernel<2><<<nb, kNT, smem, st>>>(v, margin, nr, cap);
+      else nlist_staged_kernel<3><<<nb, kNT, smem, st>>>(v, margin, nr, cap);
+      return;
+    }
     if (v.o.dim == 2) nlist_pair_kernel<2><<<nb, kNT, 0, st>>>(v, margin, nr);
     else nlist_pair_kernel<3><<<nb, kNT, 0, st>>>(v, margin, nr);
     return;

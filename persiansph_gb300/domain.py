@@ -66,6 +66,9 @@ class Domain:
         self.FSI = False
         self.GeneralBefore = None
         self.GeneralAfter = None
+        # UserOutput(particles) -> three per-particle arrays for the snapshot's
+        # OutputName datasets; None: the reference's default OutPut (zeros)
+        self.UserOutput = None
         # Constant acceleration on free particles applied where GeneralBefore
         # runs: the device-side form of the 1-Poiseuille.cpp UserAcc hook.
         self.BodyForce = [0.0, 0.0, 0.0]
@@ -295,10 +298,14 @@ class Domain:
     def Solve(self, tf, dt, dtOut, TheFileKey=None, maxidx=10**9, output=None):
         """Domain::Solve (Source/Domain.cpp:1735-1797) with the step body on the GPU.
 
-        `output(domain, idx)` (optional) is called at each output time with the
-        particles downloaded into `self.particles`, where the reference writes
-        its XDMF snapshot. User hooks other than the constant BodyForce need
-        host data every step: they are run on downloaded particles (slow path).
+        With TheFileKey, the reference's snapshots (WriteXDMF) are written as
+        <key>_Initial and <key>_0001, ... (.bin + .xmf, the reference's
+        datasets in a raw file): with the default UserOutput each is taken on
+        the device after the output step's forces; a UserOutput(particle_set)
+        returning three arrays runs on the host on the particles downloaded at
+        the output time. `output(domain, idx)` (optional) is called at each
+        output time with the particles downloaded into `self.particles`. User
+        hooks other than the constant BodyForce are rejected.
         """
         from .solver import GpuDomain
 
@@ -307,16 +314,33 @@ class Domain:
         idx_out = 1
         tout = self.Time
         hooks = self.GeneralBefore is not None or self.GeneralAfter is not None
+        user = getattr(self, "UserOutput", None)
+        names = list(self.OutputName)
+
+        def write_now(fn):
+            props = user(self.particles) if user is not None else None
+            sim.write_output(fn, names, props)
+
+        if TheFileKey is not None:
+            write_now(f"{TheFileKey}_Initial")
         while sim.time < tf and idx_out <= maxidx:
             if sim.time >= tout:
-                self.particles = sim.download(self.particles)
+                if output is not None or (TheFileKey is not None and user is not None):
+                    self.particles = sim.download(self.particles)
                 if output is not None:
                     output(self, idx_out)
+                if TheFileKey is not None:
+                    fn = f"{TheFileKey}_{idx_out:04d}"
+                    if user is not None:
+                        write_now(fn)
+                    else:
+                        sim.request_output(fn, names)
                 idx_out += 1
                 tout += dtOut
             if hooks:
                 raise Fatal("GeneralBefore/GeneralAfter host hooks: use Domain.BodyForce for device-side forcing")
             sim.step(1 << 30, t_stop=min(tf, tout))
+        sim.flush_output()
         self.particles = sim.download(self.particles)
         self.Time = sim.time
         return sim

@@ -265,6 +265,70 @@ def granular_column(dx=1e-3, W=0.2, aspect=1.0, TL_factor=4.0, wall_layers=3, rh
                      "n_wall": int(wall.sum())}
 
 
+def granular_column_3d(dx=0.01, W=0.06, D=0.04, aspect=1.0, TL_factor=1.0, wall_layers=3, rho=1850.0, E=0.84e6,
+                       nu=0.3, phi_deg=30.0, psi_deg=0.0, cohesion=0.0, fail=2, ti=0.5, tin=2.55, alpha=0.1,
+                       beta=0.1, cs=None, scheme=0, g=9.81, hfac=1.2, tension=0.0, seed=0):
+    """3D granular column (Drucker-Prager soil, Material 3, full 3D yield
+    surface): a W (x) x aspect W (y, up) x D (z) column on a fixed floor that
+    extends TL_factor W beyond it in x and wall_layers beyond it elsewhere,
+    geostatic initial stress, Monaghan tensile-instability correction. With
+    tension > 0 a seeded symmetric stress of that magnitude is added to the
+    soil, so some particles start with a principal stress in tension and the
+    tensile-instability rotation (StartAcceleration's 3D branch,
+    Source/Domain.cpp:979-987) has work to do. Returns (domain, dt, info)."""
+    dom = Domain()
+    dom.Dimension = 3
+    dom.Scheme = scheme
+    dom.Kernel_Set(Qubic_Spline)
+    dom.Viscosity_Eq_Set(Morris)
+    dom.Gradient_Approach_Set(Squared_density)
+    dom.Gravity = [0.0, -g, 0.0]
+    H = aspect * W
+    K = E / (3.0 * (1.0 - 2.0 * nu))
+    G = E / (2.0 * (1.0 + nu))
+    h = hfac * dx
+    if cs is None:
+        cs = math.sqrt(E / rho)
+    w = wall_layers
+    dom.InitialDist = dx
+    dom.AddBoxLength(1, (0.0, 0.0, 0.0), W + dx / 10.0, H + dx / 10.0, D + dx / 10.0, dx / 2.0, rho, h, 1, 0,
+                     False, False)
+    dom.AddBoxLength(3, (-w * dx, -w * dx, -w * dx), (1.0 + TL_factor) * W + 2 * w * dx + dx / 10.0,
+                     w * dx + dx / 10.0, D + 2 * w * dx + dx / 10.0, dx / 2.0, rho, h, 1, 0, False, True)
+    p = dom.particles
+    x = p.get("x")
+    yb = x[:, 1]
+    wall = p.get("is_free") == 0
+    n = p.n
+    p.set("g_mod", G)
+    p.set("cs", cs)
+    p.set("k_mod", K)
+    p.set("material", 3)
+    p.set("fail", fail)
+    p.set("cohesion", cohesion)
+    p.set("phi", phi_deg / 180.0 * math.pi)
+    p.set("psi", psi_deg / 180.0 * math.pi)
+    p.set("alpha", alpha)
+    p.set("beta", beta)
+    p.set("ti", ti)
+    p.set("tin", tin)
+    p.set("ti_init_dist", dx)
+    p.set("no_slip", wall.astype(np.int32))
+    K0 = 1 - math.sin(phi_deg / 180.0 * math.pi)
+    sig = p.get("sigma")
+    fl = ~wall
+    sig[fl, 1, 1] = rho * -g * (H - yb[fl])
+    sig[fl, 0, 0] = K0 * rho * -g * (H - yb[fl])
+    sig[fl, 2, 2] = K0 * rho * -g * (H - yb[fl])
+    if tension > 0.0:
+        rng = np.random.default_rng(seed)
+        m = rng.uniform(-tension, tension, size=(int(fl.sum()), 3, 3))
+        sig[fl] += 0.5 * (m + np.transpose(m, (0, 2, 1)))
+    dt = 0.2 * h / cs
+    return dom, dt, {"H": H, "W": W, "D": D, "K": K, "G": G, "cs": cs, "h": h, "n_soil": int(fl.sum()),
+                     "n_wall": int(wall.sum())}
+
+
 def granular_ensemble(n=256, seed=0, dx=1e-3, W=0.2, aspect=(0.5, 4.0), phi_deg=(20.0, 40.0), fail=2, **kw):
     """The batched granular-column workload: n independent 2D columns of width W
     at lattice spacing dx, aspect ratio H/W and friction angle drawn uniformly

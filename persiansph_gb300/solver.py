@@ -139,6 +139,34 @@ class GpuDomain:
         self._check(self._lib.psph_step_timed(self._ctx, int(nsteps), C.byref(ms), C.byref(done)))
         return ms.value, done.value
 
+    # -- snapshot output (WriteXDMF, Source/Domain.cpp:1869-2064) ------------
+    @staticmethod
+    def _names(names):
+        names = list(names) if names else []
+        return (C.c_char_p * 3)(*[(names[k].encode() if k < len(names) and names[k] else None) for k in range(3)])
+
+    def request_output(self, file_key: str, names=None):
+        """The next step writes <file_key>.bin / .xmf after its forces (Solve's
+        output point); the copy and the write overlap the following steps."""
+        self._check(self._lib.psph_output_request(self._ctx, file_key.encode(), self._names(names)))
+
+    def write_output(self, file_key: str, names=None, props=None):
+        """Writes a snapshot of the current state now; props: up to three arrays
+        (psph_download order) of UserOutput properties, zeros by default."""
+        arrs = [None, None, None]
+        keep = []
+        for k, p in enumerate(props or []):
+            if p is None:
+                continue
+            a = np.ascontiguousarray(p, dtype=np.float64)
+            keep.append(a)
+            arrs[k] = a.ctypes.data_as(C.POINTER(C.c_double))
+        self._check(self._lib.psph_output_write(self._ctx, file_key.encode(), self._names(names), *arrs))
+
+    def flush_output(self):
+        """Waits until every requested snapshot is on disk."""
+        self._check(self._lib.psph_output_flush(self._ctx))
+
     def pair_count(self) -> int:
         v = C.c_uint64(0)
         self._check(self._lib.psph_pair_count(self._ctx, C.byref(v)))
@@ -303,11 +331,12 @@ def _autotune(self, steps_per_trial: int = 5, cache: str | None = None) -> dict:
             known = {}
         if key in known:
             t = known[key]
-            self.set_tuning(t["pair_block"], t["cell_split"])
+            self.set_tuning(t["pair_block"], t["cell_split"], t.get("nlist_stage", 0))
             return dict(t, cached=True)
     t = PsphTuning()
     self._check(self._lib.psph_autotune(self._ctx, int(steps_per_trial), C.byref(t)))
-    out = {"pair_block": t.pair_block, "cell_split": t.cell_split, "ms_per_step": t.ms_per_step}
+    out = {"pair_block": t.pair_block, "cell_split": t.cell_split, "nlist_stage": t.nlist_stage,
+           "ms_per_step": t.ms_per_step}
     if cache:
         known = {}
         if os.path.exists(cache):
@@ -324,11 +353,17 @@ def _autotune(self, steps_per_trial: int = 5, cache: str | None = None) -> dict:
 def _tuning(self) -> dict:
     t = PsphTuning()
     self._check(self._lib.psph_get_tuning(self._ctx, C.byref(t)))
-    return {"pair_block": t.pair_block, "cell_split": t.cell_split, "ms_per_step": t.ms_per_step}
+    return {"pair_block": t.pair_block, "cell_split": t.cell_split, "nlist_stage": t.nlist_stage,
+            "ms_per_step": t.ms_per_step}
 
 
-def _set_tuning(self, pair_block: int = 128, cell_split: int = 1):
-    t = PsphTuning(pair_block, cell_split, 0.0)
+def _set_tuning(self, pair_block: int = 128, cell_split: int = 1, nlist_stage: int | None = None):
+    """Launch setting; nlist_stage None keeps the context's staging depth."""
+    if nlist_stage is None:
+        cur = PsphTuning()
+        self._check(self._lib.psph_get_tuning(self._ctx, C.byref(cur)))
+        nlist_stage = cur.nlist_stage
+    t = PsphTuning(pair_block, cell_split, nlist_stage, 0, 0.0)
     self._check(self._lib.psph_set_tuning(self._ctx, C.byref(t)))
 
 

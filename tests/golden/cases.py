@@ -77,6 +77,21 @@ def solid_block():
     return dom, dt, info
 
 
+def soil3d_ti():
+    """3D Drucker-Prager soil column on a floor with the tensile-instability
+    correction; a seeded stress perturbation puts principal stresses in
+    tension, so StartAcceleration's 3D eigen-rotation (Source/Domain.cpp:979-987)
+    produces non-zero TIR."""
+    return scenarios.granular_column_3d(dx=0.01, W=0.06, D=0.04, aspect=1.0, tension=300.0, cohesion=200.0)
+
+
+def fluid_preseq2():
+    """PresEq 2 (p = c^2 rho, Source/Functions.cpp:188-212) on a small leapfrog dam break."""
+    dom, dt, info = scenarios.dam_break_2d(dx=0.02, L=0.4, H=0.6, TL=1.0, TH=0.8, scheme=1, shepard=False)
+    dom.particles.set("pres_eq", 2)
+    return dom, dt, info
+
+
 CASES = {
     "dam2d": (dam2d, 42, (1, 2, 32, 41, 42)),
     "dam2d_leapfrog": (dam2d_leapfrog, 5, (1, 2, 5)),
@@ -88,6 +103,8 @@ CASES = {
     "fluid_shao_bingham": (fluid_shao_bingham, 5, (1, 5)),
     "fluid_incomp_quintic": (fluid_incomp_quintic, 5, (1, 5)),
     "solid_block": (solid_block, 6, (1, 6)),
+    "soil3d_ti": (soil3d_ti, 5, (1, 2, 5)),
+    "fluid_preseq2": (fluid_preseq2, 3, (1, 3)),
 }
 
 # AddBoxLength argument lists: dim, tag, V, Lx, Ly, Lz, r, rho, h, type, rotation, random, fixed

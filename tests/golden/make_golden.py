@@ -1,7 +1,7 @@
 """Generates the golden fixtures in tests/golden/ from the UNMODIFIED reference.
 
 Run here, where the reference sources are present:
-    sh oracle/build_ref.sh && python tests/golden/make_golden.py
+    sh oracle/build_ref.sh && python tests/golden/make_golden.py [case ...]
 Each case builds its initial particles with persiansph_gb300.scenarios (the
 same deterministic builders the tests use), runs oracle/_ref/ref_driver (the
 reference compiled with the project's shims, Nproc=1) and stores, per dump
@@ -27,8 +27,11 @@ FIELDS = ("x", "v", "density", "pressure", "a", "ddensity", "zwab", "sigma", "st
           "shear_stress", "tir", "va", "vb", "densitya", "densityb", "mu", "nsv", "sumkernel")
 
 
-def main():
+def main(only=()):
+    """Writes every fixture, or with case names only those cases' fixtures."""
     for name, (builder, nsteps, dumps) in CASES.items():
+        if only and name not in only:
+            continue
         dom, dt, _ = builder()
         cfg = dom.config(dt)
         with tempfile.TemporaryDirectory() as d:
@@ -51,6 +54,8 @@ def main():
                 out[f"pairs_{k}"] = v
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
         print(name, "n", dom.particles.n, "pairs", sum(len(v) for v in pairs.values()))
+    if only:
+        return
     # surge front of a longer dam break (reference run, Nproc = all host threads)
     from tests.golden.cases import SURGE_STEPS, surge2d, surge_front
     dom, dt, _ = surge2d()
@@ -78,4 +83,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]))

@@ -248,3 +248,37 @@ def test_closure_fp32c_features_match_fp64(gpu):
     assert np.max(np.abs(f32[free, 5] - f64[free, 5])) <= 1  # a pair at the support edge may differ
     mu64, mu32 = out[0][1]["mu"][free], out[1][1]["mu"][free]
     assert np.max(np.abs(mu32 - mu64) / mu64) <= 1e-4
+
+
+def test_closure_aposteriori_gain(gpu):
+    """A-posteriori test of the shipped network on the benchmark geometry (3D
+    dam break, tank 3.22 x 1 x 1 m, column 1.2 x 0.55 x 1 m): the coarse
+    dx = 20 mm run with the network, with Smagorinsky (Mat1's LES term,
+    Source/Particle.cpp:157-160) and laminar (LES off), against the fine
+    dx = 10 mm plain run, 0.05 - 0.4 s. What the network gains, asserted:
+    - surge front: within 1 % of the fine run, and at most half the
+      Smagorinsky run's error (the network 0.78 %, Smagorinsky 2.4 %);
+    - box-filtered velocity at 0.35 and 0.4 s: closer to the fine run than
+      laminar's (0.102 / 0.103 against 0.107 / 0.108 relative L2).
+    What it does not gain (recorded, not asserted): the front matches the
+    laminar run's to 1e-5, and Smagorinsky's filtered velocity is closer to
+    the fine run's at every time."""
+    from persiansph_gb300.closure import default_network_path, fine_snapshots
+    from persiansph_gb300.closure_train import HELD_OUT, coarse_run, filtered_velocity_error, surge_front
+    net = ClosureNet.load(default_network_path())
+    times = [0.05 * (k + 1) for k in range(8)]
+    dx_f, dx_c = 0.01, 0.02
+    snaps, _ = fine_snapshots([HELD_OUT], dx_f, times)
+    fine_front = np.array([surge_front(s["x"], dx_f) for s in snaps[0]])
+    res = {}
+    for mode in ("closure", "smagorinsky", "laminar"):
+        runs, _ = coarse_run(mode, dx_c, times, net)
+        front = np.array([r["front"] for r in runs])
+        res[mode] = {"front_err": float(np.max(np.abs(front - fine_front) / fine_front)),
+                     "vel_l2": [filtered_velocity_error(f, c, dx_c) for f, c in zip(snaps[0], runs)]}
+    print(res)
+    net_, smag, lam = res["closure"], res["smagorinsky"], res["laminar"]
+    assert net_["front_err"] <= 0.01
+    assert net_["front_err"] <= 0.5 * smag["front_err"]
+    for k in (-2, -1):
+        assert net_["vel_l2"][k] < lam["vel_l2"][k]

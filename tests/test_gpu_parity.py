@@ -126,7 +126,7 @@ def test_step_stops_at_t_stop(gpu):
 
 
 FLUID_CASES = ["dam2d", "dam2d_leapfrog", "poiseuille", "dam3d", "fluid_options", "fluid_shao_bingham",
-               "fluid_incomp_quintic"]
+               "fluid_incomp_quintic", "fluid_preseq2"]
 
 
 @pytest.mark.parametrize("name", FLUID_CASES)
@@ -163,7 +163,7 @@ def test_fp32c_single_step_parity_1e5(gpu, name):
         assert ep <= 1e-5, f"{name} {warm}: FP32C pressure rel err {ep:.3e}"
 
 
-SOLID_CASES = ["granular", "granular_lf_fail3", "solid_block"]
+SOLID_CASES = ["granular", "granular_lf_fail3", "solid_block", "soil3d_ti"]
 
 
 @pytest.mark.parametrize("name", SOLID_CASES)
@@ -213,8 +213,10 @@ def test_fp32c_solid_single_step_parity_1e5(gpu, name):
 
 @pytest.mark.parametrize("precision", [0, 1])
 def test_launch_tuning_does_not_change_results(gpu, precision):
-    """The block size of the pair kernels is a launch choice only: states are
-    bit-identical. The x-slab split of the cells reorders each particle's
+    """The block size of the pair kernels and the staging depth of the
+    neighbour search are launch choices only: states are bit-identical (the
+    staged scan reads the same candidates in the same order from shared
+    memory). The x-slab split of the cells reorders each particle's
     neighbours, so only the rounding of the sums changes: after 4 steps every
     field agrees within 1e-12 (FP64) / 1e-5 (FP32C) of its largest magnitude.
     psph_autotune returns one of the candidate settings."""
@@ -222,18 +224,22 @@ def test_launch_tuning_does_not_change_results(gpu, precision):
     cfg = dom.config(dt)
     cfg.precision = precision
     states = {}
-    for block, split in [(128, 1), (64, 1), (256, 2), (128, 4)]:
+    for block, split, stage in [(128, 1, 0), (64, 1, 0), (128, 1, 3072), (128, 1, 2048), (256, 2, 0),
+                                (128, 4, 4096), (128, 4, 0)]:
         gd = GpuDomain(cfg)
         gd.upload(dom.particles, initial=True)
-        gd.set_tuning(block, split)
+        gd.set_tuning(block, split, stage)
         gd.step(4)
-        states[(block, split)] = gd.download_fields(("x", "v", "density", "a", "ddensity"))
+        states[(block, split, stage)] = gd.download_fields(("x", "v", "density", "a", "ddensity"))
         gd.close()
-    ref = states[(128, 1)]
+    ref = states[(128, 1, 0)]
     for f in ref:
-        np.testing.assert_array_equal(states[(64, 1)][f], ref[f])
+        np.testing.assert_array_equal(states[(64, 1, 0)][f], ref[f])
+        np.testing.assert_array_equal(states[(128, 1, 3072)][f], ref[f])
+        np.testing.assert_array_equal(states[(128, 1, 2048)][f], ref[f])
+        np.testing.assert_array_equal(states[(128, 4, 4096)][f], states[(128, 4, 0)][f])
     tol = 1e-12 if precision == 0 else 1e-5
-    for key in [(256, 2), (128, 4)]:
+    for key in [(256, 2, 0), (128, 4, 0)]:
         for f in ref:
             scale = np.max(np.abs(ref[f])) + 1e-300
             err = np.max(np.abs(states[key][f] - ref[f])) / scale
@@ -242,6 +248,7 @@ def test_launch_tuning_does_not_change_results(gpu, precision):
     gd.upload(dom.particles, initial=True)
     t = gd.autotune(2)
     assert t["pair_block"] in (64, 128, 256) and t["cell_split"] in (1, 2, 4) and t["ms_per_step"] > 0
+    assert t["nlist_stage"] in (0, 2048, 3072, 4096)
     assert gd.tuning()["pair_block"] == t["pair_block"] and gd.tuning()["cell_split"] == t["cell_split"]
     gd.close()
 
