@@ -47,11 +47,13 @@ UNIT = "pair-interactions/s"
 # Host seconds the reference arm's timed steps may take (it runs the full
 # workload: one step of the 6.7M-particle 3D dam break is ~35 s on 16 cores).
 REF_BUDGET_S = 90.0
-# FP64 operations per directed pair evaluation of the fluid kernel for this
+# FP64 operations per pair-interaction of the fluid pair force for this
 # workload's options (Wendland, Tait, artificial viscosity, Morris, squared
-# density): counted from forces_fluid_kernel's arithmetic on the taken branches,
-# with an FMA counted as 2 and a division or square root as 1.
-FLOPS_PER_DIRECTED_PAIR = 90
+# density), counted from forces_fluid_kernel's arithmetic on the taken branches
+# with an FMA counted as 2 and a division or square root as 1: 90 for one
+# evaluation and 16 for the partner's terms (a, dDensity, ZWab, SumDen), as
+# CalcForce11 does once per unordered pair (Source/Interaction.cpp:139-145).
+FLOPS_PER_PAIR = 106
 # Algorithmic HBM bytes per particle of one FP32C fluid pair-kernel launch:
 # read each particle's inputs once (offset+h 16, v+p 16, 1/rho, p/rho^2, c, rho
 # 16, class 4, cell 4) and write its outputs once (a + drho 32, zwab 8, sumden
@@ -401,7 +403,7 @@ def main():
     force64_ms = m64["phases"]["forces"]
     cl = bool(wl["closure"])
     achieved_gbs = FORCE32_BYTES_PER_PARTICLE[cl] * n / (force32_ms * 1e-3) / 1e9
-    fp64_tflops = 2 * m64["pairs_per_step"] * FLOPS_PER_DIRECTED_PAIR / (force64_ms * 1e-3) / 1e12
+    fp64_tflops = m64["pairs_per_step"] * FLOPS_PER_PAIR / (force64_ms * 1e-3) / 1e12
     traffic = FORCE32_TRAFFIC_BYTES_PER_PARTICLE[cl] * n
 
     # end to end through the C ABI with host buffers: create + upload + K
@@ -468,8 +470,9 @@ def main():
                           "frac": fp64_tflops / fp64.value if fp64.value else None,
                           "peak_source": "measured here by psph_probe_fp64_peak (DFMA chains)",
                           "fp64_pipe_active_ncu_small_case": FORCE64_NCU_FP64_PIPE,
-                          "note": "frac counts 90 algorithmic FP64 flops per directed pair against the DFMA rate; "
-                                  "the FP64 pipe itself is 85 % busy (sqrt, divisions, conversions)"},
+                          "note": "frac counts 106 algorithmic FP64 flops per pair-interaction (one evaluation "
+                                  "and the partner's terms, each pair once) against the DFMA rate; the FP64 pipe "
+                                  "itself is ~84 % busy (square roots, divisions, conversions, idle lanes)"},
         "clocks": m32["clocks"],
         "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": h2d / max(done_e, 1),
                 "d2h_bytes_per_step": d2h / max(done_e, 1), "steps": done_e,

@@ -6,7 +6,10 @@ FP64 numpy restatement of the network in include/psph.h: 6 -> 64 -> 64 -> 64
 GPU path (weights W1..W3, the standardised inputs and the first two hidden
 activations; round to nearest even), and the training loss
 mean((softplus(z) - y)^2) with straight-through gradients through the
-roundings. The features follow the same definitions as the closure kernel.
+roundings. The GPU's backward pass runs on the tensor cores, whose operands
+are BF16: the deltas of layers 3 and 2 are rounded where they enter a
+product (the deltas of the layer below, and the W3 / W2 gradients), as here.
+The features follow the same definitions as the closure kernel.
 """
 from __future__ import annotations
 
@@ -91,14 +94,14 @@ def loss_grad(params, norm, x, y, quantize=True):
     loss = float(np.mean(e * e))
     g4 = 2.0 * e * sigmoid(f["z4"]) / B
     d3 = g4[:, None] * w["w4"][None, :] * dsilu(f["z3"])
-    d2 = (d3 @ q(w["W3"])) * dsilu(f["z2"])
-    d1 = (d2 @ q(w["W2"])) * dsilu(f["z1"])
+    d2 = (q(d3) @ q(w["W3"])) * dsilu(f["z2"])
+    d1 = (q(d2) @ q(w["W2"])) * dsilu(f["z1"])
     grad = np.zeros(NPARAMS)
     grad[OW1:OB1] = (d1.T @ f["u"]).ravel()
     grad[OB1:OW2] = d1.sum(0)
-    grad[OW2:OB2] = (d2.T @ f["a1"]).ravel()
+    grad[OW2:OB2] = (q(d2).T @ f["a1"]).ravel()
     grad[OB2:OW3] = d2.sum(0)
-    grad[OW3:OB3] = (d3.T @ f["a2"]).ravel()
+    grad[OW3:OB3] = (q(d3).T @ f["a2"]).ravel()
     grad[OB3:OW4] = d3.sum(0)
     grad[OW4:OB4] = g4 @ f["a3"]
     grad[OB4] = g4.sum()

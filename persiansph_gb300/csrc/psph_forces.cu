@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(kFT) prepare_wall_kernel(DevView v) {
 // HALF = true (pass A of the once-per-pair form): CalcForce11 updates both
 // particles of a pair from one evaluation (Source/Interaction.cpp:139-145), so
 // a pair of two free particles whose neighbour lists are both in use is
-// evaluated once, by the lower sorted index, which keeps its own terms and
+// evaluated once, by one side (evaluates_pair), which keeps its own terms and
 // writes the partner's terms (a, dDensity, ZWab, SumDen) into the partner's
 // own list slot of the pair: each list ascends as unsigned (cell-offset code
 // << 26 | index), so the partner's entry for i is found by a binary search
@@ -272,6 +272,12 @@ __global__ void __launch_bounds__(kFT) prepare_wall_kernel(DevView v) {
 // partners' terms in list order. Both sums keep a fixed order: no atomics,
 // deterministic results.
 // ---------------------------------------------------------------------------
+// Which side of a shared pair evaluates it: by the parity of i + j the lower or
+// the higher index, so each particle evaluates about half of its shared pairs
+// whatever its place in its cell (the lanes of a warp then carry nearly equal
+// queues); own(i, j) == !own(j, i) for i != j.
+PSPH_D bool evaluates_pair(int i, int j) { return ((i ^ j) & 1) ? (i < j) : (i > j); }
+
 // i's slot in j's list: the entry (mirror code, i) of j's ascending list, or -1
 PSPH_D int partner_slot(const DevView& v, int j, int code, int i) {
   const unsigned key = ((unsigned)(26 - code) << kCodeShift) | (unsigned)i;
@@ -350,9 +356,9 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
         more = false;
         break;
       }
-      // once-per-pair form: a shared pair with a lower-index partner is that
-      // partner's; left out of the queue, so the lanes' queues hold only work
-      if (HALF && own_list && j < i && v.S.nl_count[j] >= 0 && CT[P.cls[j]].is_free) continue;
+      // once-per-pair form: a shared pair the partner evaluates is left out of
+      // the queue, so the lanes' queues hold only work
+      if (HALF && own_list && !evaluates_pair(i, j) && v.S.nl_count[j] >= 0 && CT[P.cls[j]].is_free) continue;
       qbuf[qn++][tid] = HALF ? (j | (code << kCodeShift)) : j;
     }
     const int qmax = __reduce_max_sync(0xffffffffu, qn);
@@ -362,8 +368,8 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
       const int j = HALF ? (qe & kIndexMask) : qe;
       const double4_32a xj = P.X4[j];
       const PClass& Cj = CT[P.cls[j]];
-      // shared pair: both free, both lists in use; the lower index evaluates it
-      // (the queue holds only those with j > i)
+      // shared pair: both free, both lists in use; evaluates_pair picks the
+      // side (the queue holds only those this side evaluates)
       const bool share = own_list && Cj.is_free && v.S.nl_count[j] >= 0;
       const double hb = (hi + Cj.h) / 2;
       double x0 = xi.x - xj.x, x1 = xi.y - xj.y, x2 = xi.z - xj.z;
@@ -534,7 +540,7 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
 }
 
 // Pass B of the once-per-pair form: adds, in list order, the terms the
-// partners with a lower index wrote into i's slots this step (their slot
+// partners that evaluated their pair wrote into i's slots this step (their slot
 // stamp is this step's; a slot of a pair outside the support, or of a partner
 // that evaluated its own side, keeps an older stamp), then the dt bound and
 // the finiteness check of the gather form.
@@ -570,7 +576,7 @@ __global__ void __launch_bounds__(kFT) forces_fluid_fold_kernel(DevView v) {
       const int ent[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
-        if (4 * c + e >= cnt || (ent[e] & kIndexMask) >= i) continue;
+        if (4 * c + e >= cnt || evaluates_pair(i, ent[e] & kIndexMask)) continue;
         const size_t sl = nl_index(v.nl_stride, i, 4 * c + e);
         if (v.S.half_stamp[sl] != stamp) continue;
         const double4_32a t = v.S.half4[sl];

@@ -7,10 +7,16 @@
 //    by a TMA bulk copy, tcgen05.mma issued by one thread with the FP32
 //    accumulator in tensor memory, tcgen05.ld back to registers (thread t owns
 //    row t) for bias + SiLU; the 64 -> 1 output layer runs on the CUDA cores.
-//  * Training runs on the CUDA cores in FP32 with the same BF16 rounding of the
-//    weights and hidden activations (straight-through gradients): forward,
-//    loss, backward, per-chunk weight gradients, a fixed-order reduction and
-//    Adam, so a training run is deterministic.
+//  * Training runs on the tensor cores too (train_tc_kernel): per 128-sample
+//    tile the forward pass (three MMAs, pre-activations kept for the backward
+//    pass), the loss gradient, the backward deltas of the hidden layers as MMAs
+//    against transposed weight images (BF16 deltas, FP32 accumulation), and the
+//    gradients of W2 and W3 as MMAs with the samples along K (deltas^T times
+//    activations), accumulated in tensor memory over the CTA's tiles. The small
+//    parameters (W1, biases, output layer) are summed on the CUDA cores; every
+//    sum has a fixed order (per-CTA partials, then one reduction) and Adam
+//    follows, so a training run is deterministic. Straight-through gradients
+//    through the BF16 roundings of weights, activations and deltas.
 // Every wait on a tensor-core or copy completion is bounded (1 s); a wait that
 // gives up sets ST_CLOSURE_TIMEOUT (or an error status) and the kernel returns
 // after freeing its tensor memory.
@@ -486,92 +492,14 @@ __global__ void infer_cc_kernel(const float* __restrict__ params, const float* _
 }
 
 // ---------------------------------------------------------------------------
-// training (CUDA cores, FP32, deterministic)
+// training: the parameters the tensor cores do not take (CUDA cores, FP32)
 // ---------------------------------------------------------------------------
 constexpr int kTrainThreads = 128;
 
-// Forward of minibatch sample b (data row idx[b]); activations stored
-// sample-major [b][64] for the backward pass.
-__global__ void train_fwd_kernel(const float* __restrict__ params, const float* __restrict__ norm,
-                                 const float* __restrict__ X, const int* __restrict__ idx, int B, float* U, float* Z1,
-                                 float* Z2, float* Z3, float* Z4) {
-  __shared__ float p[kNParams];
-  for (int k = threadIdx.x; k < kNParams; k += blockDim.x) p[k] = params[k];
-  __syncthreads();
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= B) return;
-  const int row = idx ? idx[b] : b;
-  float u[kMlpIn];
-  for (int k = 0; k < kMlpIn; ++k) u[k] = (X[(size_t)kMlpIn * row + k] - norm[k]) * norm[kMlpIn + k];
-  float uo[kMlpIn];
-  Z4[b] = cc_forward(p, u, uo, Z1 + (size_t)kMlpH * b, Z2 + (size_t)kMlpH * b, Z3 + (size_t)kMlpH * b);
-  for (int k = 0; k < kMlpIn; ++k) U[(size_t)8 * b + k] = uo[k];
-}
-
-// dL/dz4 and the per-block loss partial sums (fixed-order reduction on the host).
-__global__ void train_loss_kernel(const float* __restrict__ Z4, const float* __restrict__ Y,
-                                  const float* __restrict__ W, const int* __restrict__ idx, int B, float* G4,
-                                  double* loss_part) {
-  __shared__ double red[kTrainThreads];
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  double l = 0.0;
-  if (b < B) {
-    const int row = idx ? idx[b] : b;
-    const float z = Z4[b];
-    const float y = Y[row];
-    const float w = W ? W[row] : 1.f;
-    const float e = softplus(z) - y;
-    G4[b] = 2.f * w * e * sigm(z) / (float)B;
-    l = (double)w * (double)e * (double)e;
-  }
-  red[threadIdx.x] = l;
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) loss_part[blockIdx.x] = red[0];
-}
-
-// Deltas of the three hidden layers (pre-activation gradients), [b][64].
-__global__ void train_bwd_kernel(const float* __restrict__ params, const float* __restrict__ Z1,
-                                 const float* __restrict__ Z2, const float* __restrict__ Z3,
-                                 const float* __restrict__ G4, int B, float* D1, float* D2, float* D3) {
-  __shared__ float p[kNParams];
-  for (int k = threadIdx.x; k < kNParams; k += blockDim.x) p[k] = params[k];
-  __syncthreads();
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= B) return;
-  const float g = G4[b];
-  const float* z1 = Z1 + (size_t)kMlpH * b;
-  const float* z2 = Z2 + (size_t)kMlpH * b;
-  const float* z3 = Z3 + (size_t)kMlpH * b;
-  float d3[kMlpH], d2[kMlpH];
-#pragma unroll
-  for (int k = 0; k < kMlpH; ++k) {
-    d3[k] = g * p[kOW4 + k] * dsilu(z3[k]);
-    D3[(size_t)kMlpH * b + k] = d3[k];
-  }
-#pragma unroll 4
-  for (int m = 0; m < kMlpH; ++m) {
-    float s = 0.f;
-#pragma unroll
-    for (int k = 0; k < kMlpH; ++k) s += bf16r(p[kOW3 + k * kMlpH + m]) * d3[k];
-    d2[m] = s * dsilu(z2[m]);
-    D2[(size_t)kMlpH * b + m] = d2[m];
-  }
-#pragma unroll 4
-  for (int m = 0; m < kMlpH; ++m) {
-    float s = 0.f;
-#pragma unroll
-    for (int k = 0; k < kMlpH; ++k) s += bf16r(p[kOW2 + k * kMlpH + m]) * d2[k];
-    D1[(size_t)kMlpH * b + m] = s * dsilu(z1[m]);
-  }
-}
-
-// Gradient of every parameter summed over one chunk of samples:
-// part[chunk][param]. Threads of a warp take consecutive parameters, so the
-// activation reads of a weight row are contiguous.
+// Gradient of W1, the biases and the output layer summed over one chunk of
+// samples: part[chunk][param] (W2 and W3 come from the tensor cores). Threads
+// of a warp take consecutive parameters, so the activation reads of a weight
+// row are contiguous.
 __global__ void train_wgrad_kernel(const float* __restrict__ U, const float* __restrict__ Z1,
                                    const float* __restrict__ Z2, const float* __restrict__ Z3,
                                    const float* __restrict__ G4, const float* __restrict__ D1,
@@ -587,15 +515,11 @@ __global__ void train_wgrad_kernel(const float* __restrict__ U, const float* __r
   } else if (pidx < kOW2) {
     const int nn = pidx - kOB1;
     for (int b = b0; b < b1; ++b) acc += D1[(size_t)kMlpH * b + nn];
-  } else if (pidx < kOB2) {
-    const int q = pidx - kOW2, nn = q / kMlpH, k = q % kMlpH;
-    for (int b = b0; b < b1; ++b) acc += D2[(size_t)kMlpH * b + nn] * bf16r(silu(Z1[(size_t)kMlpH * b + k]));
+  } else if (pidx < kOB2) {  // W2: the tensor-core partials
   } else if (pidx < kOW3) {
     const int nn = pidx - kOB2;
     for (int b = b0; b < b1; ++b) acc += D2[(size_t)kMlpH * b + nn];
-  } else if (pidx < kOB3) {
-    const int q = pidx - kOW3, nn = q / kMlpH, k = q % kMlpH;
-    for (int b = b0; b < b1; ++b) acc += D3[(size_t)kMlpH * b + nn] * bf16r(silu(Z2[(size_t)kMlpH * b + k]));
+  } else if (pidx < kOB3) {  // W3: the tensor-core partials
   } else if (pidx < kOW4) {
     const int nn = pidx - kOB3;
     for (int b = b0; b < b1; ++b) acc += D3[(size_t)kMlpH * b + nn];
@@ -608,12 +532,286 @@ __global__ void train_wgrad_kernel(const float* __restrict__ U, const float* __r
   part[(size_t)blockIdx.y * kNParams + pidx] = acc;
 }
 
-__global__ void train_reduce_kernel(const float* __restrict__ part, int nchunks, float* grad) {
+// Sums the per-chunk partials of the CUDA-core parameters and, for W2 and W3,
+// the per-CTA tensor-core partials (mma[cta][0] = dW3, mma[cta][1] = dW2, row =
+// output unit, column = input unit), each in a fixed order.
+__global__ void train_reduce_kernel(const float* __restrict__ part, int nchunks, const float* __restrict__ mma,
+                                    int nctas, float* grad) {
   const int pidx = blockIdx.x * blockDim.x + threadIdx.x;
   if (pidx >= kNParams) return;
   float s = 0.f;
-  for (int c = 0; c < nchunks; ++c) s += part[(size_t)c * kNParams + pidx];
+  const bool w2 = pidx >= kOW2 && pidx < kOB2, w3 = pidx >= kOW3 && pidx < kOB3;
+  if (w2 || w3) {
+    const int q = w2 ? pidx - kOW2 : pidx - kOW3;
+    for (int c = 0; c < nctas; ++c) s += mma[((size_t)c * 2 + (w2 ? 1 : 0)) * kMlpH * kMlpH + q];
+  } else {
+    for (int c = 0; c < nchunks; ++c) s += part[(size_t)c * kNParams + pidx];
+  }
   grad[pidx] = s;
+}
+
+// ---------------------------------------------------------------------------
+// training on the tensor cores
+// ---------------------------------------------------------------------------
+// The operand images of one optimizer step, built on the device from the FP32
+// master parameters: W1 (K padded to 16), W2 and W3 (row = output unit, K =
+// input unit) for the forward pass; W2^T and W3^T (row = input unit, K =
+// output unit) for the backward pass.
+struct TrainImages {
+  uint8_t w[5][kImgBytes];  // W1, W2, W3, W2^T, W3^T
+};
+
+__global__ void train_images_kernel(const float* __restrict__ p, TrainImages* img) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= 5 * kMlpH * kMlpH) return;
+  const int im = idx / (kMlpH * kMlpH), r = (idx / kMlpH) % kMlpH, k = idx % kMlpH;
+  float w;
+  switch (im) {
+    case 0: w = k < kMlpIn ? p[kOW1 + r * kMlpIn + k] : 0.f; break;
+    case 1: w = p[kOW2 + r * kMlpH + k]; break;
+    case 2: w = p[kOW3 + r * kMlpH + k]; break;
+    case 3: w = p[kOW2 + k * kMlpH + r]; break;
+    default: w = p[kOW3 + k * kMlpH + r]; break;
+  }
+  *reinterpret_cast<__nv_bfloat16*>(img->w[im] + sw128_offset(r, k)) = __float2bfloat16_rn(w);
+}
+
+// shared memory of train_tc_kernel (offsets from a 1024-byte aligned base)
+constexpr int kTrA = 0;                            // A tile: 128 rows x 64 BF16 (16 KB)
+constexpr int kTrW = kTrA + kMlpTile * 128;        // the five operand images (40 KB)
+constexpr int kTrDT = kTrW + 5 * kImgBytes;        // deltas^T of layers 3 and 2: 2 x (2 x [128 x 64]) (64 KB)
+constexpr int kTrAT = kTrDT + 4 * kMlpTile * 128;  // activations^T a2, a1: 2 x (2 x [64 x 64]) (32 KB)
+constexpr int kTrF = kTrAT + 4 * kImgBytes;        // b1 b2 b3 w4 b4 (+3) and the normalisation
+constexpr int kTrSmemBytes = kTrF + kSmFloats * 4 + 1024;
+constexpr int kTrCols = 256;                       // TMEM: layer accumulator 0-63, dW3 64-127, dW2 128-191
+
+// D[128 x 64] (+)= A[128 x 16 ksteps] B[64 x 16 ksteps]^T, A and B K-major in
+// 64-column sub-tiles of a_stride / b_stride bytes (the caller commits).
+__device__ __forceinline__ void tc_mma_chain(uint32_t tmem_d, const uint8_t* a, int a_stride, const uint8_t* b,
+                                             int b_stride, int ksteps, bool accumulate) {
+  for (int k = 0; k < ksteps; ++k) {
+    const uint64_t ad = sw128_desc(smem_u32(a + (k >> 2) * a_stride)) + 2 * (k & 3);
+    const uint64_t bd = sw128_desc(smem_u32(b + (k >> 2) * b_stride)) + 2 * (k & 3);
+    mma_bf16(tmem_d, ad, bd, (accumulate || k > 0) ? 1u : 0u);
+  }
+}
+
+// Every thread: its writes to the operand tiles become visible to the tensor
+// core, then thread 0 runs the MMAs and waits; afterwards the accumulator is
+// readable. Returns false when the wait gave up.
+template <class F>
+__device__ bool tc_sync_mma(uint64_t* bar, uint32_t& phase, int* err, F&& issue) {
+  proxy_fence_smem();
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    tc_fence_after();
+    issue();
+    mma_commit(bar);  // one arrival for everything issued
+    if (!mbar_wait_bounded(bar, phase, 1000000000ull)) *err = 1;
+  }
+  phase ^= 1u;
+  __syncthreads();
+  tc_fence_after();
+  return *err == 0;
+}
+
+__device__ __forceinline__ void tmem_row64(uint32_t taddr, int col, float* z) {
+  const uint32_t a = taddr + ((uint32_t)(threadIdx.x & ~31) << 16) + (uint32_t)col;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) tmem_ld16(a + 16 * j, z + 16 * j);
+  tmem_wait_ld();
+}
+
+// column c of a transposed operand ([rows] x 128 samples, two 64-wide
+// sub-tiles of sub_bytes): 64 values of this thread's sample
+__device__ __forceinline__ void store_col64(uint8_t* t, int sub_bytes, int c, const float* x) {
+  uint8_t* base = t + (c >> 6) * sub_bytes;
+  const int k = c & 63;
+#pragma unroll
+  for (int r = 0; r < kMlpH; ++r)
+    *reinterpret_cast<__nv_bfloat16*>(base + sw128_offset(r, k)) = __float2bfloat16_rn(x[r]);
+}
+
+// One CTA of 128 threads per tile of 128 samples (thread t = sample t of the
+// tile), looping over tiles; writes the activations and deltas the CUDA-core
+// gradients need (U, Z1..Z4, G4, D1..D3), the loss partial of each tile, and
+// its tensor-core partials of dW3 and dW2 (mma[cta][2][64][64]).
+__global__ void __launch_bounds__(kTcThreads) train_tc_kernel(
+    const TrainImages* __restrict__ img, const float* __restrict__ params, const float* __restrict__ norm,
+    const float* __restrict__ X, const float* __restrict__ Y, const float* __restrict__ W, const int* __restrict__ idx,
+    int B, float* U, float* Z1, float* Z2, float* Z3, float* Z4, float* G4, float* D1, float* D2, float* D3,
+    double* loss_part, float* mma, int* status) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ uint64_t bars[2];
+  __shared__ uint32_t slot;
+  __shared__ int err;
+  __shared__ double lred[kTcThreads / 32];
+  const int tid = threadIdx.x;
+  const uint32_t sbase = smem_u32(smem_raw);
+  uint8_t* sm = smem_raw + ((1024 - (sbase & 1023)) & 1023);
+  uint8_t* A = sm + kTrA;
+  uint8_t* Wi = sm + kTrW;
+  uint8_t* DT = sm + kTrDT;  // [2 layers][2 sub-tiles][128 rows x 128 B]
+  uint8_t* AT = sm + kTrAT;  // [2 layers][2 sub-tiles][64 rows x 128 B]
+  float* f = reinterpret_cast<float*>(sm + kTrF);
+  constexpr int kDsub = kMlpTile * 128, kAsub = kImgBytes;
+  uint8_t* dt3 = DT;
+  uint8_t* dt2 = DT + 2 * kDsub;
+  uint8_t* at2 = AT;
+  uint8_t* at1 = AT + 2 * kAsub;
+  if (tid == 0) {
+    err = 0;
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    mbar_init_fence();
+  }
+  // biases, output layer and normalisation; the delta tiles' rows 64-127 stay
+  // zero (M is 128, the layers have 64 units)
+  for (int k = tid; k < 4 * kMlpH; k += blockDim.x) {
+    const int seg = k / kMlpH, e = k % kMlpH;
+    f[k] = params[(seg == 0 ? kOB1 : seg == 1 ? kOB2 : seg == 2 ? kOB3 : kOW4) + e];
+  }
+  if (tid == 0) f[4 * kMlpH] = params[kOB4];
+  for (int k = tid; k < 2 * kMlpIn; k += blockDim.x) f[4 * kMlpH + 4 + k] = norm[k];
+  for (int k = tid; k < 4 * kDsub / 16; k += blockDim.x) reinterpret_cast<uint4*>(DT)[k] = make_uint4(0, 0, 0, 0);
+  if (tid < 32) tmem_alloc(&slot, kTrCols);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t taddr = slot;
+  if (tid == 0) {
+    mbar_expect_tx(&bars[0], 5 * kImgBytes);
+    bulk_g2s(Wi, img->w[0], 5 * kImgBytes, &bars[0]);
+    if (!mbar_wait_bounded(&bars[0], 0, 1000000000ull)) err = 1;
+  }
+  __syncthreads();
+  uint32_t phase = 0;
+  const float* b1 = f;
+  const float* b2 = f + kMlpH;
+  const float* b3 = f + 2 * kMlpH;
+  const float* w4 = f + 3 * kMlpH;
+  const float* mean = f + 4 * kMlpH + 4;
+  const float* inv_std = mean + kMlpIn;
+  const int ntiles = (B + kMlpTile - 1) / kMlpTile;
+  bool first = true;
+  float z[kMlpH], d[kMlpH];
+  for (int tile = blockIdx.x; tile < ntiles && !err; tile += gridDim.x) {
+    const int b = tile * kMlpTile + tid;
+    const bool valid = b < B;
+    const int row = valid ? (idx ? idx[b] : b) : 0;
+    // layer 1: standardised features, BF16, K padded to 16
+    float u[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) u[k] = (valid && k < kMlpIn) ? bf16r((X[(size_t)kMlpIn * row + k] - mean[k]) * inv_std[k]) : 0.f;
+    {
+      uint4 q0, q1;
+      q0.x = pack_bf16(u[0], u[1]); q0.y = pack_bf16(u[2], u[3]); q0.z = pack_bf16(u[4], u[5]); q0.w = pack_bf16(u[6], u[7]);
+      q1.x = pack_bf16(u[8], u[9]); q1.y = pack_bf16(u[10], u[11]); q1.z = pack_bf16(u[12], u[13]); q1.w = pack_bf16(u[14], u[15]);
+      *reinterpret_cast<uint4*>(A + sw128_offset(tid, 0)) = q0;
+      *reinterpret_cast<uint4*>(A + sw128_offset(tid, 8)) = q1;
+    }
+    if (!tc_sync_mma(&bars[1], phase, &err, [&] { tc_mma_chain(taddr, A, 0, Wi, 0, 1, false); })) break;
+    tmem_row64(taddr, 0, z);
+#pragma unroll
+    for (int k = 0; k < kMlpH; ++k) z[k] += b1[k];
+    if (valid) {
+      for (int k = 0; k < kMlpH; ++k) Z1[(size_t)kMlpH * b + k] = z[k];
+      for (int k = 0; k < 8; ++k) U[(size_t)8 * b + k] = k < kMlpIn ? u[k] : 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < kMlpH; ++k) z[k] = bf16r(silu(z[k]));
+    store_row64(A, tid, z);
+    store_col64(at1, kAsub, tid, z);
+    // layer 2
+    if (!tc_sync_mma(&bars[1], phase, &err, [&] { tc_mma_chain(taddr, A, 0, Wi + kImgBytes, 0, 4, false); }))
+      break;
+    tmem_row64(taddr, 0, z);
+#pragma unroll
+    for (int k = 0; k < kMlpH; ++k) z[k] += b2[k];
+    if (valid)
+      for (int k = 0; k < kMlpH; ++k) Z2[(size_t)kMlpH * b + k] = z[k];
+#pragma unroll
+    for (int k = 0; k < kMlpH; ++k) z[k] = bf16r(silu(z[k]));
+    store_row64(A, tid, z);
+    store_col64(at2, kAsub, tid, z);
+    // layer 3 and the output
+    if (!tc_sync_mma(&bars[1], phase, &err, [&] { tc_mma_chain(taddr, A, 0, Wi + 2 * kImgBytes, 0, 4, false); }))
+      break;
+    tmem_row64(taddr, 0, z);
+    float o = f[4 * kMlpH];
+#pragma unroll
+    for (int k = 0; k < kMlpH; ++k) {
+      z[k] += b3[k];
+      o += w4[k] * silu(z[k]);
+    }
+    // loss and its gradient (mean over the minibatch)
+    double lp = 0.0;
+    float g = 0.f;
+    if (valid) {
+      const float y = Y[row], w = W ? W[row] : 1.f;
+      const float e = softplus(o) - y;
+      g = 2.f * w * e * sigm(o) / (float)B;
+      lp = (double)w * (double)e * (double)e;
+      Z4[b] = o;
+      G4[b] = g;
+      for (int k = 0; k < kMlpH; ++k) Z3[(size_t)kMlpH * b + k] = z[k];
+    }
+    for (int off = 16; off > 0; off >>= 1) lp += __shfl_down_sync(0xffffffffu, lp, off);
+    if ((tid & 31) == 0) lred[tid >> 5] = lp;
+    // delta of layer 3
+#pragma unroll
+    for (int k = 0; k < kMlpH; ++k) d[k] = g * w4[k] * dsilu(z[k]);
+    if (valid)
+      for (int k = 0; k < kMlpH; ++k) D3[(size_t)kMlpH * b + k] = d[k];
+    store_row64(A, tid, d);
+    store_col64(dt3, kDsub, tid, d);
+    // delta of layer 2: (d3 W3) o silu'(z2)
+    if (!tc_sync_mma(&bars[1], phase, &err, [&] { tc_mma_chain(taddr, A, 0, Wi + 4 * kImgBytes, 0, 4, false); }))
+      break;
+    if (tid == 0) {
+      double t = 0.0;
+      for (int w = 0; w < kTcThreads / 32; ++w) t += lred[w];
+      loss_part[tile] = t;
+    }
+    tmem_row64(taddr, 0, d);
+#pragma unroll
+    for (int k = 0; k < kMlpH; ++k) d[k] *= dsilu(valid ? Z2[(size_t)kMlpH * b + k] : 0.f);
+    if (valid)
+      for (int k = 0; k < kMlpH; ++k) D2[(size_t)kMlpH * b + k] = d[k];
+    store_row64(A, tid, d);
+    store_col64(dt2, kDsub, tid, d);
+    // delta of layer 1: (d2 W2) o silu'(z1)
+    if (!tc_sync_mma(&bars[1], phase, &err, [&] { tc_mma_chain(taddr, A, 0, Wi + 3 * kImgBytes, 0, 4, false); }))
+      break;
+    tmem_row64(taddr, 0, d);
+    if (valid)
+      for (int k = 0; k < kMlpH; ++k) D1[(size_t)kMlpH * b + k] = d[k] * dsilu(Z1[(size_t)kMlpH * b + k]);
+    // dW3 += d3^T a2 and dW2 += d2^T a1 over this tile's samples (K = 128)
+    const bool acc = !first;
+    if (!tc_sync_mma(&bars[1], phase, &err, [&] {
+          tc_mma_chain(taddr + 64, dt3, kDsub, at2, kAsub, 8, acc);
+          tc_mma_chain(taddr + 128, dt2, kDsub, at1, kAsub, 8, acc);
+        }))
+      break;
+    first = false;
+  }
+  // this CTA's dW3 / dW2 rows (TMEM lanes 0-63 = output units)
+  if (!err && !first && tid < kMlpH) {
+    float* out = mma + (size_t)blockIdx.x * 2 * kMlpH * kMlpH;
+    tmem_row64(taddr, 64, z);
+    for (int k = 0; k < kMlpH; ++k) out[(size_t)tid * kMlpH + k] = z[k];
+    tmem_row64(taddr, 128, z);
+    for (int k = 0; k < kMlpH; ++k) out[(size_t)(kMlpH + tid) * kMlpH + k] = z[k];
+  } else if (!err && first && tid < kMlpH) {  // no tile: zero partials
+    float* out = mma + (size_t)blockIdx.x * 2 * kMlpH * kMlpH;
+    for (int k = 0; k < 2 * kMlpH; ++k) out[(size_t)(k / kMlpH * kMlpH + tid) * kMlpH + k % kMlpH] = 0.f;
+  }
+  if (err && tid == 0) atomicExch(status, 1);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (tid < 32) tmem_dealloc(taddr, kTrCols);
 }
 
 __global__ void adam_kernel(float* params, const float* grad, float* m, float* v, float lr, float b1, float b2,
@@ -665,6 +863,15 @@ int num_sms() {
     if (n <= 0) n = 148;
   }
   return n;
+}
+
+bool tr_attr_set = false;
+cudaError_t ensure_train_attrs() {
+  if (tr_attr_set) return cudaSuccess;
+  const cudaError_t e =
+      cudaFuncSetAttribute(train_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrSmemBytes);
+  if (e == cudaSuccess) tr_attr_set = true;
+  return e;
 }
 
 bool tc_attr_set = false;
@@ -726,6 +933,9 @@ struct psph_mlp {
   int* d_idx = nullptr;
   float *d_U = nullptr, *d_Z1 = nullptr, *d_Z2 = nullptr, *d_Z3 = nullptr, *d_Z4 = nullptr, *d_G4 = nullptr;
   float *d_D1 = nullptr, *d_D2 = nullptr, *d_D3 = nullptr, *d_part = nullptr;
+  float* d_mma = nullptr;            // per-CTA tensor-core partials of dW3, dW2
+  TrainImages* d_timg = nullptr;     // operand images of the current parameters
+  int mma_cap = 0;
   double* d_loss = nullptr;
   int* d_status = nullptr;
 };
@@ -756,8 +966,18 @@ void dfree(T*& p) {
   p = nullptr;
 }
 
+// CTAs of train_tc_kernel for a minibatch of B samples
+int train_ctas(int B) { return std::max(1, std::min((B + kMlpTile - 1) / kMlpTile, num_sms())); }
+
 psph_status ensure_batch(psph_mlp* m, int B) {
   const int nchunk = (B + 127) / 128;
+  const int nctas = train_ctas(B);
+  if (!m->d_timg) MLP_TRY(m, cudaMalloc(&m->d_timg, sizeof(TrainImages)));
+  if (nctas > m->mma_cap) {
+    dfree(m->d_mma);
+    MLP_TRY(m, cudaMalloc(&m->d_mma, (size_t)nctas * 2 * kMlpH * kMlpH * sizeof(float)));
+    m->mma_cap = nctas;
+  }
   if (B <= m->cap && nchunk <= m->nchunk_cap) return PSPH_OK;
   for (float** p : {&m->d_U, &m->d_Z1, &m->d_Z2, &m->d_Z3, &m->d_Z4, &m->d_G4, &m->d_D1, &m->d_D2, &m->d_D3,
                     &m->d_part})
@@ -785,17 +1005,24 @@ psph_status batch_grad(psph_mlp* m, const float* dX, const float* dY, const floa
   psph_status st = ensure_batch(m, B);
   if (st) return st;
   const int nb = (B + kTrainThreads - 1) / kTrainThreads;
-  train_fwd_kernel<<<nb, kTrainThreads>>>(m->d_params, m->d_norm, dX, d_idx, B, m->d_U, m->d_Z1, m->d_Z2, m->d_Z3,
-                                          m->d_Z4);
-  train_loss_kernel<<<nb, kTrainThreads>>>(m->d_Z4, dY, dW, d_idx, B, m->d_G4, m->d_loss);
-  train_bwd_kernel<<<nb, kTrainThreads>>>(m->d_params, m->d_Z1, m->d_Z2, m->d_Z3, m->d_G4, B, m->d_D1, m->d_D2,
-                                          m->d_D3);
+  MLP_TRY(m, ensure_train_attrs());
+  // tensor cores: forward, loss gradient, deltas, dW2 / dW3
+  train_images_kernel<<<(5 * kMlpH * kMlpH + 255) / 256, 256>>>(m->d_params, m->d_timg);
+  MLP_TRY(m, cudaMemset(m->d_status, 0, sizeof(int)));
+  const int nctas = train_ctas(B);
+  train_tc_kernel<<<nctas, kTcThreads, kTrSmemBytes>>>(m->d_timg, m->d_params, m->d_norm, dX, dY, dW, d_idx, B,
+                                                       m->d_U, m->d_Z1, m->d_Z2, m->d_Z3, m->d_Z4, m->d_G4, m->d_D1,
+                                                       m->d_D2, m->d_D3, m->d_loss, m->d_mma, m->d_status);
+  // CUDA cores: W1, the biases and the output layer, per chunk of samples
   const int chunk = 128, nchunk = (B + chunk - 1) / chunk;
   dim3 grid((kNParams + 127) / 128, nchunk);
   train_wgrad_kernel<<<grid, 128>>>(m->d_U, m->d_Z1, m->d_Z2, m->d_Z3, m->d_G4, m->d_D1, m->d_D2, m->d_D3, B, chunk,
                                     m->d_part);
-  train_reduce_kernel<<<(kNParams + 127) / 128, 128>>>(m->d_part, nchunk, m->d_grad);
+  train_reduce_kernel<<<(kNParams + 127) / 128, 128>>>(m->d_part, nchunk, m->d_mma, nctas, m->d_grad);
   MLP_TRY(m, cudaGetLastError());
+  int tstatus = 0;
+  MLP_TRY(m, cudaMemcpy(&tstatus, m->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (tstatus) return mlp_err(m, PSPH_ERR_CUDA, "training: a tensor-core completion wait gave up");
   if (loss) {
     std::vector<double> parts(nb);
     MLP_TRY(m, cudaMemcpy(parts.data(), m->d_loss, nb * sizeof(double), cudaMemcpyDeviceToHost));
@@ -891,6 +1118,8 @@ void psph_mlp_destroy(psph_mlp* m) {
                     &m->d_Z2, &m->d_Z3, &m->d_Z4, &m->d_G4, &m->d_D1, &m->d_D2, &m->d_D3, &m->d_part})
     dfree(*p);
   dfree(m->d_img);
+  dfree(m->d_timg);
+  dfree(m->d_mma);
   dfree(m->d_idx);
   dfree(m->d_loss);
   dfree(m->d_status);
