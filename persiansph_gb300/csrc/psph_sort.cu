@@ -26,6 +26,21 @@ namespace {
 
 constexpr int kBT = 256;
 
+// A double's value in FP32 (truncated, not rounded) from its bits on the
+// integer pipe: the estimates below need ~1e-6 relative accuracy, and a
+// double-to-float conversion instruction runs on the FP64 pipe. Finite
+// inputs; magnitudes outside FP32's normal range give 0 or infinity.
+__device__ __forceinline__ float d2f_bits(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+  const unsigned sign = hi & 0x80000000u;
+  if (e <= 0) return __int_as_float((int)sign);
+  if (e >= 255) return __int_as_float((int)(sign | 0x7f800000u));
+  const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+  return __int_as_float((int)(sign | ((unsigned)e << 23) | m));
+}
+
 __global__ void bin_kernel(DevView v, const uint8_t* __restrict__ alive, int* __restrict__ key,
                            int* __restrict__ count, StepScalars* sc, int dim, int xsub) {
   if (sc->all_stop) return;
@@ -42,14 +57,17 @@ __global__ void bin_kernel(DevView v, const uint8_t* __restrict__ alive, int* __
       const double4_32a x = P.X4[i];
       const double xs[3] = {x.x, x.y, x.z};
       int c[3] = {0, 0, 0};
+      double a0 = 0.0;  // x - BLPF_x
       bool orphan = false, out = false;
       for (int d = 0; d < dim; ++d) {
         // ListGenerate's floor((x - BLPF) / CellSize) (Source/Domain.cpp:669-691).
-        // An FP32 estimate decides it unless the quotient lies within the
-        // estimate's error of an integer; only then the FP64 division runs
-        // (a division costs tens of operations on the FP64 pipe).
+        // An FP32 estimate (the difference converted on the integer pipe)
+        // decides it unless the quotient lies within the estimate's error of
+        // an integer; only then the FP64 division runs (a division costs tens
+        // of operations on the FP64 pipe).
         const double a = xs[d] - g.blpf[d];
-        const float t = (float)a * g.inv_cell_size32[d];
+        if (d == 0) a0 = a;
+        const float t = d2f_bits(a) * g.inv_cell_size32[d];
         const float ft = floorf(t), fr = t - ft, tol = 1e-3f + 4e-7f * fabsf(t);
         int cd = (int)ft;
         if (!(fr >= tol && fr <= 1.f - tol)) cd = (int)floor(a / g.cell_size[d]);
@@ -72,7 +90,7 @@ __global__ void bin_kernel(DevView v, const uint8_t* __restrict__ alive, int* __
       } else {
         int slab = 0;
         if (xsub > 1) {  // x-slab inside the cell (clamped for particles outside it), in FP32
-          const float ox = (float)((xs[0] - g.blpf[0]) - c[0] * g.cell_size[0]);
+          const float ox = d2f_bits(a0) - (float)c[0] * g.cell_size32[0];
           slab = min(max((int)floorf(ox * (float)xsub * g.inv_cell_size32[0]), 0), xsub - 1);
         }
         k = (g.cell_base + (c[2] * g.nc[1] + c[1]) * g.nc[0] + c[0]) * xsub + slab;
