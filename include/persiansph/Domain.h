@@ -153,9 +153,11 @@ class Domain {
   // host SoA image of the particles for the C ABI
   struct Pack {
     std::vector<int32_t> id, material, is_free, no_slip, pres_eq, shepard, les, vis_m, fail;
+    std::vector<int32_t> seepage_type, var_porosity, is_sat;
     std::vector<double> vec[7];     // x v va vb a nsv vxsph
-    std::vector<double> sca[32];
+    std::vector<double> sca[38];
     std::vector<double> ten[12];
+    std::vector<double> s;          // Particle::S
     psph_particles view;
   };
   void pack(Pack& pk) const;
@@ -182,7 +184,7 @@ inline const VecF* vec_fields() {
   return f;
 }
 inline const ScaF* sca_fields() {
-  static const ScaF f[32] = {
+  static const ScaF f[38] = {
       {&Particle::Density, &psph_particles::density},       {&Particle::Densitya, &psph_particles::densitya},
       {&Particle::Densityb, &psph_particles::densityb},     {&Particle::dDensity, &psph_particles::ddensity},
       {&Particle::Pressure, &psph_particles::pressure},     {&Particle::Mass, &psph_particles::mass},
@@ -198,7 +200,11 @@ inline const ScaF* sca_fields() {
       {&Particle::c, &psph_particles::cohesion},            {&Particle::phi, &psph_particles::phi},
       {&Particle::psi, &psph_particles::psi},               {&Particle::ZWab, &psph_particles::zwab},
       {&Particle::SumDen, &psph_particles::sumden},         {&Particle::SumKernel, &psph_particles::sumkernel},
-      {&Particle::ShearRate, &psph_particles::shear_rate},  {&Particle::SBar, &psph_particles::sbar}};
+      {&Particle::ShearRate, &psph_particles::shear_rate},  {&Particle::SBar, &psph_particles::sbar},
+      // soil-water interaction; k and k2 last: an upload reads them, a download leaves them
+      {&Particle::n0, &psph_particles::n0},                 {&Particle::d, &psph_particles::d},
+      {&Particle::RhoF, &psph_particles::rho_f},            {&Particle::V, &psph_particles::volume},
+      {&Particle::k, &psph_particles::k},                   {&Particle::k2, &psph_particles::k2}};
   return f;
 }
 inline const TenF* ten_fields() {
@@ -242,6 +248,9 @@ inline void Domain::pack(Pack& pk) const {
   ints(pk.les, &psph_particles::les, [](const Particle& q) { return q.LES ? 1 : 0; });
   ints(pk.vis_m, &psph_particles::vis_m, [](const Particle& q) { return (int)q.VisM; });
   ints(pk.fail, &psph_particles::fail, [](const Particle& q) { return (int)q.Fail; });
+  ints(pk.seepage_type, &psph_particles::seepage_type, [](const Particle& q) { return (int)q.SeepageType; });
+  ints(pk.var_porosity, &psph_particles::var_porosity, [](const Particle& q) { return q.VarPorosity ? 1 : 0; });
+  ints(pk.is_sat, &psph_particles::is_sat, [](const Particle& q) { return q.IsSat ? 1 : 0; });
   for (int f = 0; f < 7; ++f) {
     const detail::VecF& F = detail::vec_fields()[f];
     pk.vec[f].resize(3 * n);
@@ -249,12 +258,15 @@ inline void Domain::pack(Pack& pk) const {
       for (int d = 0; d < 3; ++d) pk.vec[f][3 * i + d] = ((*Particles[i]).*F.m)(d);
     pk.view.*F.p = pk.vec[f].data();
   }
-  for (int f = 0; f < 32; ++f) {
+  for (int f = 0; f < 38; ++f) {
     const detail::ScaF& F = detail::sca_fields()[f];
     pk.sca[f].resize(n);
     for (size_t i = 0; i < n; ++i) pk.sca[f][i] = (*Particles[i]).*F.m;
     pk.view.*F.p = pk.sca[f].data();
   }
+  pk.s.resize(n);
+  for (size_t i = 0; i < n; ++i) pk.s[i] = Particles[i]->S;
+  pk.view.s = pk.s.data();
   for (int f = 0; f < 12; ++f) {
     const detail::TenF& F = detail::ten_fields()[f];
     pk.ten[f].resize(9 * n);
@@ -274,7 +286,9 @@ inline void Domain::unpack(const Pack& pk) {
       const detail::VecF& F = detail::vec_fields()[f];
       for (int d = 0; d < 3; ++d) (q.*F.m)(d) = pk.vec[f][3 * i + d];
     }
-    for (int f = 0; f < 32; ++f) q.*(detail::sca_fields()[f].m) = pk.sca[f][i];
+    for (int f = 0; f < 36; ++f) q.*(detail::sca_fields()[f].m) = pk.sca[f][i];  // not k, k2
+    q.IsSat = pk.is_sat[i] != 0;
+    q.S = pk.s[i];
     for (int f = 0; f < 12; ++f) std::memcpy((q.*(detail::ten_fields()[f].m)).data(), &pk.ten[f][9 * i], 9 * sizeof(double));
   }
 }
@@ -431,7 +445,7 @@ inline void Domain::DelParticles(int const& Tags) {
 
 inline void Domain::Solve(double tf, double dt, double dtOut, char const* TheFileKey, size_t maxidx) {
   std::cout << "\n--------------Solving---------------------------------------------------------------" << std::endl;
-  if (SWIType != 0 || FSI) throw new Fatal("soil-water interaction and FSI are outside this build");
+  if (FSI) throw new Fatal("fluid-solid interaction (FSI) is outside this build");
   if (BC.InOutFlow != 0) throw new Fatal("in/out-flow boundaries are outside this build");
   const Vec3_t body = BodyForce + hook_acceleration(GeneralBefore, "GeneralBefore") +
                       hook_acceleration(GeneralAfter, "GeneralAfter");
@@ -457,6 +471,7 @@ inline void Domain::Solve(double tf, double dt, double dtOut, char const* TheFil
   cfg.R = R;
   cfg.dt = dt;
   cfg.time = Time;
+  cfg.swi_type = (int)SWIType;
 
   psph_ctx* ctx = nullptr;
   Pack pk;

@@ -15,7 +15,8 @@ namespace SPH {
 class Particle {
  public:
   Particle(int Tag, Vec3_t const& x0, Vec3_t const& v0, double Mass0, double Density0, double h0, bool Fixed)
-      : IsFree(!Fixed), ID(Tag), x(x0), v(v0), Density(Density0), RefDensity(Density0), Mass(Mass0), h(h0) {}
+      : IsFree(!Fixed), ID(Tag), x(x0), v(v0), Density(Density0), RefDensity(Density0), Mass(Mass0), h(h0),
+        V(Mass0 / Density0) {}
 
   // flags and identifiers
   bool IsFree;
@@ -57,6 +58,13 @@ class Particle {
   double G = 0.0, K = 0.0, c = 0.0, phi = 0.0, psi = 0.0, Sigmay = 0.0;
   Mat3_t Sigma, Sigmaa, Sigmab, ShearStress, ShearStressa, ShearStressb, Strain, Straina, Strainb;
   Mat3_t StrainRate, RotationRate, TIR;
+
+  // soil-water interaction (fluid and soil in one domain)
+  size_t SeepageType = 0;
+  bool VarPorosity = false, IsSat = false;
+  double n0 = 0.0, k = 0.0, k2 = 0.0, d = 0.0, RhoF = 0.0;
+  double V;         // volume: Mass / RefDensity at construction
+  double S = 0.0;   // SWIType 1: surface-erosion velocity derivative of the last step
 };
 
 }  // namespace SPH

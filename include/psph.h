@@ -30,12 +30,12 @@
 extern "C" {
 #endif
 
-#define PSPH_ABI_VERSION 1
+#define PSPH_ABI_VERSION 2
 
 typedef enum psph_status {
   PSPH_OK = 0,
   PSPH_ERR_INVALID_ARGUMENT = 1, /* bad enum/size/pointer; reference aborts or throws Fatal */
-  PSPH_ERR_UNSUPPORTED = 2,      /* valid reference option outside this build (FSI, seepage, in/out-flow) */
+  PSPH_ERR_UNSUPPORTED = 2,      /* valid reference option outside this build (FSI, in/out-flow) */
   PSPH_ERR_CUDA = 3,             /* a CUDA runtime call failed */
   PSPH_ERR_OUT_OF_MEMORY = 4,
   PSPH_ERR_NONFINITE = 5,        /* NaN/Inf found in an acceleration or density rate */
@@ -68,7 +68,10 @@ typedef struct psph_config {
   int32_t gradient_type;      /* PSPH_SQUARED_DENSITY ... */
   int32_t scheme;             /* PSPH_MVERLET or PSPH_LEAPFROG */
   int32_t periodic[3];        /* Domain::BC.Periodic */
-  int32_t swi_type;           /* Domain::SWIType; only 0 (no seepage) is in this build */
+  int32_t swi_type;           /* Domain::SWIType: fluid-soil interaction (CalcForce13) when fluid
+                                 (Material 1) and soil (Material 3) share a domain: 0 seepage force,
+                                 1 seepage + surface erosion, 2 seepage + pore pressure, 3 none
+                                 (0, 1 and 3 also switch soil between saturated and dry weight) */
   int32_t shepard_step;       /* Particle::ShepardStep, uniform over particles (default 40) */
   int32_t precision;          /* PSPH_FP64 or PSPH_FP32C */
   int32_t wall_pressure_mode; /* PSPH_WALLP_REFERENCE or PSPH_WALLP_PHYSICAL */
@@ -129,6 +132,17 @@ typedef struct psph_particles {
   /* 3x3 tensors */
   double *sigma, *sigmaa, *sigmab, *shear_stress, *shear_stressa, *shear_stressb, *strain, *straina,
       *strainb, *strain_rate, *rotation_rate, *tir;
+  /* Soil-water interaction of soil particles (Source/Particle.h:41-42, :110-121).
+   * seepage_type: SeepageType (0 Darcy, 1 Kozeny-Carman, 2 Ergun, 3 Den Adel);
+   * var_porosity: VarPorosity (porosity, k and k2 follow the volumetric strain);
+   * is_sat: IsSat (on download, the saturation state after the last step);
+   * n0, d, rho_f: initial porosity, grain size, fluid density RhoF;
+   * k, k2: permeabilities, read on upload (an initial upload derives them from
+   * n0 and d for SeepageType 1-3, as InitialChecks does), not written on download;
+   * volume: V (default Mass/RefDensity, the Particle constructor's value);
+   * s: S, the surface-erosion velocity derivative of the last step (download only). */
+  int32_t *seepage_type, *var_porosity, *is_sat;
+  double *n0, *k, *k2, *d, *rho_f, *volume, *s;
 } psph_particles;
 
 typedef struct psph_ctx psph_ctx;

@@ -166,7 +166,7 @@ def write_state_dir(path: str, cfg: PsphConfig, pset: ParticleSet, extra: dict |
         "gradient_type": [cfg.gradient_type], "scheme": [cfg.scheme], "periodic": list(cfg.periodic),
         "gravity": list(cfg.gravity), "body_force": list(cfg.body_force), "xsph": [cfg.xsph],
         "sqrt_h_a": [cfg.sqrt_h_a], "R": [cfg.R], "dom_max": list(cfg.dom_max), "dom_min": list(cfg.dom_min),
-        "dt": [cfg.dt], "time": [cfg.time], "shepard_step": [cfg.shepard_step],
+        "dt": [cfg.dt], "time": [cfg.time], "shepard_step": [cfg.shepard_step], "swi_type": [cfg.swi_type],
     }
     if extra:
         lines.update(extra)

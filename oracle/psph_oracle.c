@@ -14,8 +14,10 @@
  *    can keep a larger value; with Nproc=1 both are the plain minimum.
  *  - A particle more than hmax outside the grid makes ListGenerate index out of
  *    bounds in the reference (Source/Domain.cpp:669-691); here it is an error.
- *  - Interactions outside this build (NSMPairs: fluid-soil seepage, FSI) are
- *    reported as PSPH_ERR_UNSUPPORTED instead of being computed.
+ *  - Fluid-solid pairs (CalcForce12, FSI) are reported as PSPH_ERR_UNSUPPORTED
+ *    instead of being computed; solid-soil pairs, which the reference aborts
+ *    on, as PSPH_ERR_INVALID_ARGUMENT.
+ *  - Particle::n (porosity) is not kept: only the permeabilities it feeds are.
  */
 #include "psph_oracle.h"
 
@@ -55,6 +57,7 @@ struct psph_oracle {
   int32_t* LL; /* Particle::LL */
   int32_t* CC; /* Particle::CC[3] */
   int32_t* HOC;
+  int32_t* satcheck; /* Particle::SatCheck of the current step */
   int64_t ncells;
   int nthr;
   pairvec *sm, *fsm, *nsm;
@@ -595,6 +598,8 @@ static void start_acceleration(psph_oracle* o, int nthr) {
     o->zwab[i] = 0.0;
     o->sumden[i] = 0.0;
     o->sumkernel[i] = 0.0;
+    o->satcheck[i] = 0;
+    o->s[i] = 0.0;
     if (dim == 2) o->v[3 * i + 2] = 0.0;
     memset(o->strain_rate + 9 * i, 0, 9 * sizeof(double));
     memset(o->rotation_rate + 9 * i, 0, 9 * sizeof(double));
@@ -633,6 +638,30 @@ static void primary_compute(psph_oracle* o, int nthr) {
         for (int d = 0; d < 3; ++d) o->nsv[3 * W + d] += o->v[3 * F + d] * K;
       omp_unset_lock(&o->locks[W]);
     }
+    /* saturation check from the fluid-soil candidate pairs (Source/Domain.cpp:1060-1089):
+     * a soil particle with a fluid particle in a neighbouring cell at or
+     * above its own cell row and position is saturated this step */
+    if (o->cfg.swi_type != 2)
+      for (int64_t a = 0; a < o->nsm[k].n; a++) {
+        int64_t P1 = o->nsm[k].v[2 * a], P2 = o->nsm[k].v[2 * a + 1];
+        const int prod = o->material[P1] * o->material[P2];
+        if (o->material[P1] == 3 && prod == 3)
+          if (!o->satcheck[P1])
+            if (o->CC[3 * P2 + 1] >= o->CC[3 * P1 + 1])
+              if (o->x[3 * P2 + 1] >= o->x[3 * P1 + 1]) {
+                omp_set_lock(&o->locks[P1]);
+                o->satcheck[P1] = 1;
+                omp_unset_lock(&o->locks[P1]);
+              }
+        if (o->material[P2] == 3 && prod == 3)
+          if (!o->satcheck[P2])
+            if (o->CC[3 * P1 + 1] >= o->CC[3 * P2 + 1])
+              if (o->x[3 * P1 + 1] >= o->x[3 * P2 + 1]) {
+                omp_set_lock(&o->locks[P2]);
+                o->satcheck[P2] = 1;
+                omp_unset_lock(&o->locks[P2]);
+              }
+      }
   }
 #pragma omp parallel for schedule(static) num_threads(nthr)
   for (int64_t i = 0; i < o->nfixed; i++) {
@@ -647,6 +676,27 @@ static void primary_compute(psph_oracle* o, int nthr) {
         for (int d = 0; d < 3; ++d) o->nsv[3 * a + d] = o->nsv[3 * a + d] / o->sumkernel[a];
       if (o->material[a] > 1 && o->ti[a] > 0.0) tensile_tir(dim, o->sigma + 9 * a, o->ti[a], o->density[a], o->tir + 9 * a);
     }
+  }
+  /* saturated soil weighs its buoyant weight (Source/Domain.cpp:1209-1234) */
+  if (o->cfg.swi_type != 2) {
+#pragma omp parallel for schedule(static) num_threads(nthr)
+    for (int64_t i = 0; i < o->n; i++)
+      if (o->material[i] == 3) {
+        if (o->satcheck[i] && !o->is_sat[i]) {
+          o->mass[i] = o->volume[i] * (o->ref_density[i] - o->rho_f[i]);
+          o->density[i] = o->density[i] - o->rho_f[i];
+          o->densityb[i] = o->densityb[i] - o->rho_f[i];
+          o->ref_density[i] = o->ref_density[i] - o->rho_f[i];
+          o->is_sat[i] = 1;
+        }
+        if (!o->satcheck[i] && o->is_sat[i]) {
+          o->mass[i] = o->volume[i] * (o->ref_density[i] + o->rho_f[i]);
+          o->density[i] = o->density[i] + o->rho_f[i];
+          o->densityb[i] = o->densityb[i] + o->rho_f[i];
+          o->ref_density[i] = o->ref_density[i] + o->rho_f[i];
+          o->is_sat[i] = 0;
+        }
+      }
   }
 }
 
@@ -771,6 +821,7 @@ static int calc_force11(psph_oracle* o, int64_t p1, int64_t p2) {
       double c = mj / dj;
       for (int e = 0; e < 9; ++e) o->strain_rate[9 * p1 + e] = o->strain_rate[9 * p1 + e] + SR[e] * c;
     }
+    if (o->cfg.swi_type == 1) o->s[p1] = o->s[p1] + mj / dj * vab[0] * xij[1] * -GK;
     o->zwab[p1] += mj / dj * K;
   } else
     o->zwab[p1] = 1.0;
@@ -790,6 +841,7 @@ static int calc_force11(psph_oracle* o, int64_t p1, int64_t p2) {
       double c = mi / di;
       for (int e = 0; e < 9; ++e) o->strain_rate[9 * p2 + e] = o->strain_rate[9 * p2 + e] + SR[e] * c;
     }
+    if (o->cfg.swi_type == 1) o->s[p2] = o->s[p2] + mi / di * vab[0] * xij[1] * -GK;
     o->zwab[p2] += mi / di * K;
   } else
     o->zwab[p2] = 1.0;
@@ -939,6 +991,7 @@ static int calc_force2233(psph_oracle* o, int64_t p1, int64_t p2) {
       o->strain_rate[9 * p1 + e] = o->strain_rate[9 * p1 + e] + SR[e] * c;
       o->rotation_rate[9 * p1 + e] = o->rotation_rate[9 * p1 + e] + RR[e] * c;
     }
+    if (o->cfg.swi_type == 1) o->s[p1] = o->s[p1] + mj / dj * vab[0] * xij[1] * -GK;
   } else
     o->zwab[p1] = 1.0;
   if (o->shepard[p1])
@@ -959,6 +1012,7 @@ static int calc_force2233(psph_oracle* o, int64_t p1, int64_t p2) {
       o->strain_rate[9 * p2 + e] = o->strain_rate[9 * p2 + e] + SR[e] * c;
       o->rotation_rate[9 * p2 + e] = o->rotation_rate[9 * p2 + e] + RR[e] * c;
     }
+    if (o->cfg.swi_type == 1) o->s[p2] = o->s[p2] + mi / di * vab[0] * xij[1] * -GK;
   } else
     o->zwab[p2] = 1.0;
   if (o->shepard[p2])
@@ -969,10 +1023,71 @@ static int calc_force2233(psph_oracle* o, int64_t p1, int64_t p2) {
   return 1;
 }
 
+/* Seepage (Source/Functions.cpp:266-298): Darcy (0, 1) or Forchheimer (2, 3)
+ * coefficients of the drag between pore fluid and soil skeleton */
+static void Seepage(int ST, double k, double k2, double mu, double rho, double* SF1, double* SF2) {
+  *SF1 = mu / k;
+  *SF2 = (ST >= 2) ? k2 * rho : 0.0;
+}
+
+/* CalcForce13 (Source/Interaction.cpp:508-653): fluid-soil pair. Both of the
+ * reference's orientations give the same terms (v = v_fluid - v_soil; the
+ * pore-pressure term's sign follows x_ij), written here from the soil side. */
+static int calc_force13(psph_oracle* o, int64_t p1, int64_t p2) {
+  const int dim = o->cfg.dimension, kt = o->cfg.kernel_type;
+  double h = o->h[p1] < o->h[p2] ? o->h[p1] : o->h[p2];
+  double xij[3];
+  for (int d = 0; d < 3; ++d) xij[d] = o->x[3 * p1 + d] - o->x[3 * p2 + d];
+  periodic_correction(o, xij, h, p1, p2);
+  double rij = sqrt(dot3(xij, xij));
+  if ((rij / h) > o->g.cellfac) return 0;
+  const int swi = o->cfg.swi_type;
+  if (swi == 3) return 1;
+  double K = Kernel(dim, kt, rij / h, h) / (o->density[p1] * o->density[p2]);
+  const int64_t S = (o->material[p1] == 3) ? p1 : p2, F = (S == p1) ? p2 : p1;
+  double v[3], SF1 = 0.0, SF2 = 0.0, SFt[3];
+  for (int d = 0; d < 3; ++d) v[d] = o->v[3 * F + d] - o->v[3 * S + d];
+  const double nv = sqrt(dot3(v, v));
+  if (swi == 1 && o->zwab[S] < 0.25) {
+    /* surface erosion: drag of a grain at the soil surface plus lift from the
+     * fluid's velocity derivative (Source/Interaction.cpp:561-566) */
+    double Cd = 24.0 * (o->mu_ref[F] / o->ref_density[F]) / (o->d[S] * nv + 0.01 * h * h) + 2.0;
+    double c = 3.0 / (4.0 * o->d[S]) * o->ref_density[F] * (1.0 - o->n0[S]) * Cd * nv;
+    for (int d = 0; d < 3; ++d) SFt[d] = c * v[d] * K;
+    SFt[1] += (o->ref_density[F] * (1.0 - o->n0[S]) * nv * fabs(o->s[F] - o->s[S])) * K;
+  } else {
+    Seepage(o->seepage_type[S], o->k[S], o->k2[S], o->mu_ref[F], o->ref_density[F], &SF1, &SF2);
+    for (int d = 0; d < 3; ++d) SFt[d] = (SF1 * v[d] + SF2 * nv * v[d]) * K;
+  }
+  if (dim == 2) SFt[2] = 0.0;
+  double as[3];
+  for (int d = 0; d < 3; ++d) as[d] = o->mass[F] * SFt[d];
+  if (swi == 2) {
+    /* pore pressure of the fluid on the soil (Source/Interaction.cpp:608-637) */
+    double GK = GradKernel(dim, kt, rij / h, h) / (o->density[p1] * o->density[p2]);
+    double c = o->mass[F] * o->pressure[F] * GK;
+    for (int d = 0; d < 3; ++d) as[d] = (S == p1) ? as[d] - c * xij[d] : as[d] + c * xij[d];
+  }
+  const double tf = o->mass[S] * sqrt(dot3(SFt, SFt)), ts = sqrt(dot3(as, as));
+  omp_set_lock(&o->locks[S]);
+  for (int d = 0; d < 3; ++d) o->a[3 * S + d] += as[d];
+  o->a_scale[S] += ts;
+  omp_unset_lock(&o->locks[S]);
+  omp_set_lock(&o->locks[F]);
+  for (int d = 0; d < 3; ++d) o->a[3 * F + d] -= o->mass[S] * SFt[d];
+  o->a_scale[F] += tf;
+  omp_unset_lock(&o->locks[F]);
+  return 1;
+}
+
 /* LastComputeAcceleration (Source/Domain.cpp:1238-1297) */
 static int last_compute(psph_oracle* o, int nthr) {
   for (int k = 0; k < o->nthr; ++k)
-    if (o->nsm[k].n) return fail(o, PSPH_ERR_UNSUPPORTED, "interaction between different materials (NSMPairs) is outside this build");
+    for (int64_t i = 0; i < o->nsm[k].n; i++) {
+      const int prod = o->material[o->nsm[k].v[2 * i]] * o->material[o->nsm[k].v[2 * i + 1]];
+      if (prod == 2) return fail(o, PSPH_ERR_UNSUPPORTED, "fluid-solid interaction (CalcForce12, FSI) is outside this build");
+      if (prod != 3) return fail(o, PSPH_ERR_INVALID_ARGUMENT, "Out of Interaction types");
+    }
   int64_t evaluated = 0;
 #pragma omp parallel for schedule(static) num_threads(nthr) reduction(+ : evaluated)
   for (int k = 0; k < o->nthr; k++) {
@@ -985,6 +1100,9 @@ static int last_compute(psph_oracle* o, int nthr) {
       evaluated += (o->material[p1] == 1) ? calc_force11(o, p1, p2) : calc_force2233(o, p1, p2);
     }
   }
+#pragma omp parallel for schedule(static) num_threads(nthr) reduction(+ : evaluated)
+  for (int k = 0; k < o->nthr; k++)
+    for (int64_t i = 0; i < o->nsm[k].n; i++) evaluated += calc_force13(o, o->nsm[k].v[2 * i], o->nsm[k].v[2 * i + 1]);
   o->pairs_done += evaluated;
   double dtmin = o->it.deltatint;
   const double sha = o->cfg.sqrt_h_a;
@@ -1192,6 +1310,37 @@ static int dp_return(psph_oracle* o, int64_t i, double* Sig, const double* Sn, c
 }
 
 /* Mat3Leapfrog (Particle.cpp:641-795; porosity update out of scope) */
+/* Kozeny-Carman (1), Ergun (2) and Den Adel (3) permeabilities at porosity n
+ * (InitialChecks, Source/Domain.cpp:1687-1713; VarPorosity, Particle.cpp:450-474);
+ * SeepageType 0 keeps the given k */
+static void permeability(psph_oracle* o, int64_t i, double n) {
+  const double d = o->d[i];
+  switch (o->seepage_type[i]) {
+    case 1:
+      o->k[i] = n * n * n * d * d / (180.0 * (1.0 - n) * (1.0 - n));
+      break;
+    case 2:
+      o->k[i] = n * n * n * d * d / (150.0 * (1.0 - n) * (1.0 - n));
+      o->k2[i] = 1.75 * (1.0 - n) / (n * n * n * d);
+      break;
+    case 3:
+      o->k[i] = n * n * n * d * d / (150.0 * (1.0 - n) * (1.0 - n));
+      o->k2[i] = 0.4 / (n * n * d);
+      break;
+    default:
+      break;
+  }
+}
+
+/* VarPorosity (Source/Particle.cpp:444-479, :757-792): the porosity follows the
+ * volumetric strain, n = (n0 + ev) / (1 + ev), and the permeabilities follow n */
+static void var_porosity(psph_oracle* o, int64_t i) {
+  if (!o->var_porosity[i]) return;
+  const double* E = o->strain + 9 * i;
+  double ev = (E[0] + E[4] + E[8]);
+  permeability(o, i, (o->n0[i] + ev) / (1.0 + ev));
+}
+
 static int mat3_leapfrog(psph_oracle* o, int64_t i, double dt) {
   double *Sig = o->sigma + 9 * i, *Sa = o->sigmaa + 9 * i, *Sb = o->sigmab + 9 * i;
   const double *SR = o->strain_rate + 9 * i, *RR = o->rotation_rate + 9 * i;
@@ -1213,10 +1362,11 @@ static int mat3_leapfrog(psph_oracle* o, int64_t i, double dt) {
   for (int e = 0; e < 9; ++e) Eb[e] = Ea[e];
   for (int e = 0; e < 9; ++e) Ea[e] = SR[e] * dt + Ea[e];
   for (int e = 0; e < 9; ++e) E[e] = (Ea[e] + Eb[e]) * (1.0 / 2.0);
+  var_porosity(o, i);
   return PSPH_OK;
 }
 
-/* Mat3MVerlet (Particle.cpp:320-482; porosity update out of scope) */
+/* Mat3MVerlet (Particle.cpp:320-482) */
 static int mat3_mverlet(psph_oracle* o, int64_t i, double dt, int ct) {
   double *Sig = o->sigma + 9 * i, *Sb = o->sigmab + 9 * i;
   const double *SR = o->strain_rate + 9 * i, *RR = o->rotation_rate + 9 * i;
@@ -1240,6 +1390,7 @@ static int mat3_mverlet(psph_oracle* o, int64_t i, double dt, int ct) {
   else
     for (int e = 0; e < 9; ++e) E[e] = SR[e] * (2.0 * dt) + Eb[e];
   memcpy(Eb, Stress, sizeof Stress);
+  var_porosity(o, i);
   return PSPH_OK;
 }
 
@@ -1401,10 +1552,12 @@ static int validate(psph_oracle* o) {
   if (c->dimension != 2 && c->dimension != 3) return fail(o, PSPH_ERR_INVALID_ARGUMENT, "Please correct the dimension (2=>2D or 3=>3D)");
   if (c->kernel_type < 0 || c->kernel_type > 2) return fail(o, PSPH_ERR_INVALID_ARGUMENT, "Kernel Type No is out of range");
   if (c->vis_eq < 0 || c->vis_eq > 3) return fail(o, PSPH_ERR_INVALID_ARGUMENT, "Viscosity Equation No is out of range");
-  if (c->swi_type != 0) return fail(o, PSPH_ERR_UNSUPPORTED, "soil-water interaction is outside this build");
+  if (c->swi_type < 0 || c->swi_type > 3) return fail(o, PSPH_ERR_INVALID_ARGUMENT, "Soil-Water Interaction Type No is out of range");
   for (int64_t i = 0; i < o->n; ++i) {
     if (o->material[i] < 1 || o->material[i] > 3) return fail(o, PSPH_ERR_INVALID_ARGUMENT, "Material Type No is out of range");
     if (o->pres_eq[i] < 0 || o->pres_eq[i] > 2) return fail(o, PSPH_ERR_INVALID_ARGUMENT, "Please correct Pressure Equation No");
+    if (o->material[i] == 3 && (o->seepage_type[i] < 0 || o->seepage_type[i] > 3))
+      return fail(o, PSPH_ERR_INVALID_ARGUMENT, "Seepage Type No is out of range");
   }
   return PSPH_OK;
 }
@@ -1440,6 +1593,10 @@ psph_oracle* psph_oracle_create(const psph_config* cfg, const psph_particles* p,
   PSPH_VEC_FIELDS(COPY_V)
   PSPH_TEN_FIELDS(COPY_T)
   if (!p->ref_density && p->density) memcpy(o->ref_density, p->density, (size_t)n * sizeof(double));
+  /* Particle::V = Mass / RefDensity (the constructor's value, Source/Particle.cpp:88) */
+  if (!p->volume)
+    for (int64_t i = 0; i < n; ++i) o->volume[i] = o->mass[i] / o->ref_density[i];
+  o->satcheck = (int32_t*)calloc((size_t)(n ? n : 1), sizeof(int32_t));
   o->orig = (int64_t*)malloc((size_t)(n ? n : 1) * sizeof(int64_t));
   for (int64_t i = 0; i < n; ++i) o->orig[i] = i;
   o->LL = (int32_t*)malloc((size_t)(n ? n : 1) * sizeof(int32_t));
@@ -1466,6 +1623,9 @@ psph_oracle* psph_oracle_create(const psph_config* cfg, const psph_particles* p,
     /* InitialChecks (Source/Domain.cpp:1662-1678): initial EOS pressure */
     for (int64_t i = 0; i < n; i++)
       if (o->material[i] < 3) o->pressure[i] = EOS(o->pres_eq[i], o->cs[i], o->p0[i], o->density[i], o->ref_density[i]);
+    /* permeabilities of the soil from its porosity (Source/Domain.cpp:1680-1716) */
+    for (int64_t i = 0; i < n; i++)
+      if (o->material[i] == 3) permeability(o, i, o->n0[i]);
   }
   if (grid) {
     o->g = *grid;
@@ -1503,6 +1663,7 @@ void psph_oracle_destroy(psph_oracle* o) {
   free(o->LL);
   free(o->CC);
   free(o->HOC);
+  free(o->satcheck);
   free(o->fixed);
   free(o->a_scale);
   free(o->dr_scale);

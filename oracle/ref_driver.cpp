@@ -99,6 +99,7 @@ static int load_state(SPH::Domain& dom, const char* dir) {
     for (int d = 0; d < 3; ++d) g_body_force[d] = v[d];
     if (v[0] != 0.0 || v[1] != 0.0 || v[2] != 0.0) dom.GeneralBefore = &BodyForceHook;
   }
+  dom.SWIType = (size_t)psph_io_cfg1(dir, "swi_type", 0);
   dom.MuMax = 0.0;  // left uninitialised by the Domain constructor
   dom.CsMax = 0.0;
 
@@ -125,6 +126,9 @@ static int load_state(SPH::Domain& dom, const char* dir) {
   SET_INT(les, P->LES = val != 0)
   SET_INT(vis_m, P->VisM = (size_t)val)
   SET_INT(fail, P->Fail = (size_t)val)
+  SET_INT(seepage_type, P->SeepageType = (size_t)val)
+  SET_INT(var_porosity, P->VarPorosity = val != 0)
+  SET_INT(is_sat, P->IsSat = val != 0)
 #define SET_F64(NAME, MEMBER)                                           \
   if (RD(#NAME, dbuf.data(), 8 * (size_t)n) == 0)                       \
     for (int i = 0; i < n; ++i) dom.Particles[i]->MEMBER = dbuf[i];
@@ -136,7 +140,8 @@ static int load_state(SPH::Domain& dom, const char* dir) {
   SET_F64(ti_init_dist, TIInitDist) SET_F64(g_mod, G) SET_F64(k_mod, K) SET_F64(sigmay, Sigmay)
   SET_F64(cohesion, c) SET_F64(phi, phi) SET_F64(psi, psi) SET_F64(zwab, ZWab)
   SET_F64(sumden, SumDen) SET_F64(sumkernel, SumKernel) SET_F64(shear_rate, ShearRate)
-  SET_F64(sbar, SBar)
+  SET_F64(sbar, SBar) SET_F64(n0, n0) SET_F64(k, k) SET_F64(k2, k2) SET_F64(d, d) SET_F64(rho_f, RhoF)
+  SET_F64(s, S)
 #define SET_VEC(NAME, MEMBER)                                                         \
   if (RD(#NAME, vbuf.data(), 24 * (size_t)n) == 0)                                    \
     for (int i = 0; i < n; ++i)                                                       \
@@ -152,8 +157,9 @@ static int load_state(SPH::Domain& dom, const char* dir) {
   SET_TEN(shear_stressb, ShearStressb) SET_TEN(strain, Strain) SET_TEN(straina, Straina)
   SET_TEN(strainb, Strainb) SET_TEN(strain_rate, StrainRate) SET_TEN(rotation_rate, RotationRate)
   SET_TEN(tir, TIR)
-  // mass-derived volume, as the Particle constructor computes it
+  // mass-derived volume, as the Particle constructor computes it, unless given
   for (int i = 0; i < n; ++i) dom.Particles[i]->V = dom.Particles[i]->Mass / dom.Particles[i]->RefDensity;
+  SET_F64(volume, V)
   double ss = psph_io_cfg1(dir, "shepard_step", 40);
   for (int i = 0; i < n; ++i) dom.Particles[i]->ShepardStep = (size_t)ss;
   return n;
@@ -170,7 +176,8 @@ static void dump_state(SPH::Domain& dom, const std::string& dir, long step) {
   psph_io_write(d, #NAME, ib.data(), 4 * n);
   W_INT(id, P->ID) W_INT(material, P->Material) W_INT(is_free, P->IsFree) W_INT(no_slip, P->NoSlip)
   W_INT(pres_eq, P->PresEq) W_INT(shepard, P->Shepard) W_INT(les, P->LES) W_INT(vis_m, P->VisM)
-  W_INT(fail, P->Fail)
+  W_INT(fail, P->Fail) W_INT(seepage_type, P->SeepageType) W_INT(var_porosity, P->VarPorosity)
+  W_INT(is_sat, P->IsSat)
 #define W_F64(NAME, MEMBER)                                           \
   for (size_t i = 0; i < n; ++i) db[i] = dom.Particles[i]->MEMBER;    \
   psph_io_write(d, #NAME, db.data(), 8 * n);
@@ -181,7 +188,8 @@ static void dump_state(SPH::Domain& dom, const std::string& dir, long step) {
   W_F64(csmag, CSmag) W_F64(ti, TI) W_F64(tin, TIn) W_F64(ti_init_dist, TIInitDist) W_F64(g_mod, G)
   W_F64(k_mod, K) W_F64(sigmay, Sigmay) W_F64(cohesion, c) W_F64(phi, phi) W_F64(psi, psi)
   W_F64(zwab, ZWab) W_F64(sumden, SumDen) W_F64(sumkernel, SumKernel) W_F64(shear_rate, ShearRate)
-  W_F64(sbar, SBar)
+  W_F64(sbar, SBar) W_F64(n0, n0) W_F64(k, k) W_F64(k2, k2) W_F64(d, d) W_F64(rho_f, RhoF)
+  W_F64(volume, V) W_F64(s, S)
 #define W_VEC(NAME, MEMBER)                                                       \
   for (size_t i = 0; i < n; ++i)                                                  \
     for (int k = 0; k < 3; ++k) vb[3 * i + k] = dom.Particles[i]->MEMBER(k);      \

@@ -21,14 +21,15 @@ extern "C" {
 
 /* Per-particle int32 fields, in file order. */
 #define PSPH_INT_FIELDS(X) \
-  X(id) X(material) X(is_free) X(no_slip) X(pres_eq) X(shepard) X(les) X(vis_m) X(fail)
+  X(id) X(material) X(is_free) X(no_slip) X(pres_eq) X(shepard) X(les) X(vis_m) X(fail) \
+  X(seepage_type) X(var_porosity) X(is_sat)
 
 /* Per-particle float64 scalar fields. */
 #define PSPH_F64_FIELDS(X)                                                                      \
   X(density) X(densitya) X(densityb) X(ddensity) X(pressure) X(mass) X(h) X(cs) X(p0)            \
   X(ref_density) X(fpmassc) X(alpha) X(beta) X(mu) X(mu_ref) X(t0) X(bingham_m) X(csmag) X(ti)   \
   X(tin) X(ti_init_dist) X(g_mod) X(k_mod) X(sigmay) X(cohesion) X(phi) X(psi) X(zwab) X(sumden) \
-  X(sumkernel) X(shear_rate) X(sbar)
+  X(sumkernel) X(shear_rate) X(sbar) X(n0) X(k) X(k2) X(d) X(rho_f) X(volume) X(s)
 
 /* Per-particle 3-vectors. */
 #define PSPH_VEC_FIELDS(X) X(x) X(v) X(va) X(vb) X(a) X(nsv) X(vxsph)

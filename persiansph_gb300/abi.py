@@ -13,9 +13,9 @@ import os
 import numpy as np
 
 # Field lists in include/psph.h order.
-INT_FIELDS = ("id", "material", "is_free", "no_slip", "pres_eq", "shepard", "les", "vis_m", "fail")
+BASE_INT_FIELDS = ("id", "material", "is_free", "no_slip", "pres_eq", "shepard", "les", "vis_m", "fail")
 VEC_FIELDS = ("x", "v", "va", "vb", "a", "nsv", "vxsph")
-F64_FIELDS = (
+BASE_F64_FIELDS = (
     "density", "densitya", "densityb", "ddensity", "pressure", "mass", "h", "cs", "p0", "ref_density",
     "fpmassc", "alpha", "beta", "mu", "mu_ref", "t0", "bingham_m", "csmag", "ti", "tin", "ti_init_dist",
     "g_mod", "k_mod", "sigmay", "cohesion", "phi", "psi", "zwab", "sumden", "sumkernel", "shear_rate", "sbar",
@@ -24,6 +24,11 @@ TEN_FIELDS = (
     "sigma", "sigmaa", "sigmab", "shear_stress", "shear_stressa", "shear_stressb", "strain", "straina",
     "strainb", "strain_rate", "rotation_rate", "tir",
 )
+# soil-water interaction fields, after the tensors in the struct
+SEEP_INT_FIELDS = ("seepage_type", "var_porosity", "is_sat")
+SEEP_F64_FIELDS = ("n0", "k", "k2", "d", "rho_f", "volume", "s")
+INT_FIELDS = BASE_INT_FIELDS + SEEP_INT_FIELDS
+F64_FIELDS = BASE_F64_FIELDS + SEEP_F64_FIELDS
 ALL_FIELDS = INT_FIELDS + VEC_FIELDS + F64_FIELDS + TEN_FIELDS
 
 # status codes (psph_status)
@@ -70,10 +75,12 @@ class PsphTuning(C.Structure):
 class PsphParticles(C.Structure):
     _fields_ = (
         [("n", C.c_int64)]
-        + [(f, C.POINTER(C.c_int32)) for f in INT_FIELDS]
+        + [(f, C.POINTER(C.c_int32)) for f in BASE_INT_FIELDS]
         + [(f, C.POINTER(C.c_double)) for f in VEC_FIELDS]
-        + [(f, C.POINTER(C.c_double)) for f in F64_FIELDS]
+        + [(f, C.POINTER(C.c_double)) for f in BASE_F64_FIELDS]
         + [(f, C.POINTER(C.c_double)) for f in TEN_FIELDS]
+        + [(f, C.POINTER(C.c_int32)) for f in SEEP_INT_FIELDS]
+        + [(f, C.POINTER(C.c_double)) for f in SEEP_F64_FIELDS]
     )
 
 

@@ -288,9 +288,11 @@ void enqueue_step(psph_ctx* c, F&& before_update) {
   record_phase(c, 2);
   if (v.o.fp32) launch_prepare32(v, st);
   else launch_prepare(v, st);
+  if (v.o.mixed && v.o.swi != 2) launch_saturation(v, st);
   record_phase(c, 3);
   if (v.o.fp32) launch_forces32(v, st);
   else launch_forces(v, st);
+  if (v.o.mixed) launch_seepage(v, st);
   record_phase(c, 4);
   if (v.o.closure) launch_closure(v, st);
   record_phase(c, 5);
@@ -368,7 +370,8 @@ psph_status create_impl(const psph_config* cfgs, int ninst, psph_ctx** out) {
     if (k.gradient_type < 0 || k.gradient_type > 1) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Gradient type out of range");
     if (k.scheme != PSPH_MVERLET && k.scheme != PSPH_LEAPFROG)
       return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Scheme must be 0 (Modified Verlet) or 1 (Leapfrog)");
-    if (k.swi_type != 0) return set_err(c, PSPH_ERR_UNSUPPORTED, "soil-water interaction (SWIType) is outside this build");
+    if (k.swi_type < 0 || k.swi_type > 3)
+      return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Soil-Water Interaction Type No is out of range");
     if (k.precision != PSPH_FP64 && k.precision != PSPH_FP32C)
       return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "precision must be PSPH_FP64 or PSPH_FP32C");
     if (k.dimension == 2 && k.periodic[2]) return set_err(c, PSPH_ERR_UNSUPPORTED, "periodic z in 2D");
@@ -379,12 +382,13 @@ psph_status create_impl(const psph_config* cfgs, int ninst, psph_ctx** out) {
     bool same = k.dimension == a.dimension && k.kernel_type == a.kernel_type && k.vis_eq == a.vis_eq &&
                 k.gradient_type == a.gradient_type && k.scheme == a.scheme && k.precision == a.precision &&
                 k.wall_pressure_mode == a.wall_pressure_mode && k.shepard_step == a.shepard_step &&
-                k.xsph == a.xsph && k.sqrt_h_a == a.sqrt_h_a;
+                k.xsph == a.xsph && k.sqrt_h_a == a.sqrt_h_a && k.swi_type == a.swi_type;
     for (int d = 0; d < 3; ++d) same = same && k.gravity[d] == a.gravity[d] && k.body_force[d] == a.body_force[d];
     if (!same)
       return set_err(c, PSPH_ERR_INVALID_ARGUMENT,
                      "instance %d: an ensemble shares dimension, kernel, viscosity, gradient, scheme, precision, "
-                     "wall pressure, gravity, body force, XSPH, sqrt_h_a and Shepard step with instance 0", q);
+                     "wall pressure, gravity, body force, XSPH, sqrt_h_a, Shepard step and SWIType with instance 0",
+                     q);
   }
   int dev = 0;
   if (psph_device_check(&dev) != PSPH_OK) return set_err(c, PSPH_ERR_NO_DEVICE, "no sm_103 CUDA device available");
@@ -451,8 +455,7 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
   struct Worker {
     std::vector<PClass> classes;
     std::unordered_map<std::string, int, ClassKeyHash> index;
-    int material = -1;
-    bool mixed = false;
+    int materials = 0;  // bit m: Material m present
     int64_t err_at = -1;
     psph_status err = PSPH_OK;
     char msg[160] = {0};
@@ -512,6 +515,22 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
       C.fail = iflt(p->fail, i, 0);
       C.id = iflt(p->id, i, 0);
       C.inst = q;
+      if (C.material == 3) {
+        C.seep_type = iflt(p->seepage_type, i, 0);
+        C.var_por = iflt(p->var_porosity, i, 0) != 0;
+        C.is_sat = iflt(p->is_sat, i, 0) != 0;
+        C.n0 = dflt(p->n0, i, 0.0);
+        C.kp = dflt(p->k, i, 0.0);
+        C.kp2 = dflt(p->k2, i, 0.0);
+        C.dgrain = dflt(p->d, i, 0.0);
+        C.rho_f = dflt(p->rho_f, i, 0.0);
+        // Particle::V: the constructor's Mass / RefDensity unless given
+        C.vol = p->volume ? p->volume[i] : C.mass / C.rho0;
+        if (C.seep_type < 0 || C.seep_type > 3)
+          FAIL(PSPH_ERR_INVALID_ARGUMENT, "Seepage Type No is out of range (particle %lld)", (long long)i);
+        // InitialChecks: permeabilities from the porosity (Source/Domain.cpp:1680-1716)
+        if (initial) permeability(C.seep_type, C.n0, C.dgrain, &C.kp, &C.kp2);
+      }
       if (C.material < 1 || C.material > 3)
         FAIL(PSPH_ERR_INVALID_ARGUMENT, "Material Type No is out of range (particle %lld)", (long long)i);
       if (C.pres_eq < 0 || C.pres_eq > 2)
@@ -520,8 +539,7 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
       if (C.material == 3 && C.fail > 3) FAIL(PSPH_ERR_INVALID_ARGUMENT, "Failure Type No is out of range");
       if (C.material == 1 && C.t0 > 0.0 && C.vis_m > 1)
         FAIL(PSPH_ERR_INVALID_ARGUMENT, "Non-Newtonian Viscosity Type No is out of range");
-      if (W.material < 0) W.material = C.material;
-      if (C.material != W.material) W.mixed = true;
+      W.materials |= 1 << C.material;
 #undef FAIL
       int id;
       // consecutive particles mostly share their parameters: compare with the
@@ -548,19 +566,13 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
     }
   };
   run_threads(nthreads, work);
-  int material0 = -1;
+  int materials = 0;
+  std::unordered_map<std::string, int, ClassKeyHash> index;
   {
-    std::unordered_map<std::string, int, ClassKeyHash> index;
     for (int t = 0; t < nthreads; ++t) {
       const Worker& W = workers[t];
       if (W.err) return set_err(c, W.err, "%s", W.msg);
-      if (W.material >= 0) {
-        if (material0 < 0) material0 = W.material;
-        if (W.mixed || W.material != material0)
-          return set_err(c, PSPH_ERR_UNSUPPORTED,
-                         "particles of different materials interact through CalcForce12/13 (FSI, seepage), outside "
-                         "this build");
-      }
+      materials |= W.materials;
       std::vector<int> remap(W.classes.size());
       for (size_t k = 0; k < W.classes.size(); ++k) {
         std::string key((const char*)&W.classes[k], sizeof(PClass));
@@ -577,6 +589,56 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
       }
       const int64_t g0 = ntot * t / nthreads, g1 = ntot * (t + 1) / nthreads;
       for (int64_t g = g0; g < g1; ++g) cls[g] = remap[cls[g]];
+    }
+  }
+  // Materials that share a domain: fluid with soil couples through CalcForce13;
+  // a solid (Material 2) with anything else needs CalcForce12 (FSI)
+  const bool mixed = materials == ((1 << 1) | (1 << 3));
+  if (!mixed && (materials & (materials - 1)))
+    return set_err(c, PSPH_ERR_UNSUPPORTED,
+                   "solid particles (Material 2) share the domain with another material: fluid-solid interaction "
+                   "(CalcForce12, FSI) is outside this build");
+  if (mixed) {
+    if (k.precision != PSPH_FP64)
+      return set_err(c, PSPH_ERR_UNSUPPORTED, "fluid-soil domains run in the FP64 form (PSPH_FP64)");
+    for (int q = 0; q < ninst; ++q)
+      if (c->cfgs[q].periodic[1])
+        return set_err(c, PSPH_ERR_UNSUPPORTED, "fluid-soil domains with a periodic y axis");
+    // Saturation switch (Source/Domain.cpp:1209-1234): a soil particle moves to
+    // the class with Mass = V (RefDensity -+ RhoF) and RefDensity -+ RhoF. Each
+    // soil class gets that twin; a chain of twins is closed after a few links
+    // (later flips return to the previous class, which differs from the
+    // reference's repeated -+ RhoF by rounding of RefDensity only).
+    if (k.swi_type != 2) {
+      std::vector<int> depth(c->classes.size(), 0);
+      for (size_t q = 0; q < c->classes.size(); ++q) {
+        if (c->classes[q].material != 3) continue;
+        const PClass C = c->classes[q];
+        PClass T = C;
+        T.twin = 0;
+        T.mass = C.vol * (C.is_sat ? C.rho0 + C.rho_f : C.rho0 - C.rho_f);
+        T.rho0 = C.is_sat ? C.rho0 + C.rho_f : C.rho0 - C.rho_f;
+        T.is_sat = !C.is_sat;
+        std::string key((const char*)&T, sizeof(PClass));
+        auto it = index.find(key);
+        int id;
+        if (it != index.end()) {
+          id = it->second;
+        } else if (depth[q] >= 3) {
+          id = -1;  // closed below
+        } else {
+          id = (int)c->classes.size();
+          if (id >= 65535) return set_err(c, PSPH_ERR_UNSUPPORTED, "more than 65535 distinct particle parameter sets");
+          index.emplace(key, id);
+          c->classes.push_back(T);
+          depth.push_back(depth[q] + 1);
+        }
+        c->classes[q].twin = id;
+      }
+      for (size_t q = 0; q < c->classes.size(); ++q)
+        if (c->classes[q].material == 3 && c->classes[q].twin < 0)
+          for (size_t r = 0; r < c->classes.size(); ++r)
+            if (c->classes[r].twin == (int)q) c->classes[q].twin = (int)r;  // back to the class it came from
     }
   }
 
@@ -635,10 +697,12 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
   o.grad_type = k.gradient_type;
   o.scheme = k.scheme;
   o.wallp_physical = (k.wall_pressure_mode == PSPH_WALLP_PHYSICAL);
-  o.has_solid = (material0 > 1);
+  o.has_solid = (materials & ((1 << 2) | (1 << 3))) != 0;
+  o.mixed = mixed;
+  o.swi = k.swi_type;
   o.fp32 = (k.precision == PSPH_FP32C);
   if (ntot >= (1LL << 26)) return set_err(c, PSPH_ERR_UNSUPPORTED, "this build handles fewer than 2^26 particles");
-  o.soil_pairs = (material0 == 3);
+  o.soil_pairs = (materials & (1 << 3)) != 0;
   o.dyn_mu = dyn_mu;
   o.xsph = k.xsph;
   o.sqrt_h_a = k.sqrt_h_a;
@@ -664,7 +728,7 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
     if (C.ti > 0.0) o.any_ti = 1;
     if (C.material == 1 && (C.t0 > 0.0 || C.les)) o.need_sr = 1;
     if (C.shepard) o.any_shepard = 1;
-    if (C.is_free) {
+    if (C.is_free && (!mixed || C.material == 1)) {  // the fluid's EOS (walls take it from the fluid)
       if (o.eos_cls < 0) o.eos_cls = (int)q;
       else {
         const PClass& E = c->classes[o.eos_cls];
@@ -751,6 +815,8 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
       (st = dalloc(c, &S.sumkernel, N)) || (st = dalloc(c, &S.nsv4, N)) || (st = dalloc(c, &S.vxsph4, N)) ||
       (st = dalloc(c, &S.shear_rate, N)) || (st = dalloc(c, &S.sbar, N)))
     return st;
+  if (o.mixed && o.swi == 1 && (st = dalloc(c, &S.s_acc, N))) return st;
+  if (o.mixed && o.swi != 2 && (st = dalloc(c, &S.satcheck, N))) return st;
   if ((st = dalloc(c, &S.nl, (size_t)o.nl_cap * nl_stride_of(c->ncap)))) return st;
   // FP64 fluids without strain-rate sums, XSPH or solids: each pair evaluated once
   o.fp64_half = !o.fp32 && !o.has_solid && !o.need_sr && o.xsph == 0.0;
@@ -885,6 +951,7 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
       I.deltatmin = it.deltatmin;
       I.steps = it.steps;
       I.first_step = it.first_step;
+      I.k_initial = initial ? 1 : 0;
       I.ct = it.ct;
       I.shepard_counter = it.shepard_counter;
       I.t_stop = 1e300;
@@ -1092,7 +1159,7 @@ psph_status download_impl(psph_ctx* c, int q, psph_particles* out) {
       {out->mu, o.dyn_mu ? P.mu : nullptr, 1, 0, 1},
       {out->strain_rate, c->S.strain_rate, 9, 0, 9}, {out->rotation_rate, c->S.rotation_rate, 9, 0, 9},
       {out->sigma, P.sigma, 9, 0, 9}, {out->strain, P.strain, 9, 0, 9}, {out->shear_stress, P.shear, 9, 0, 9},
-      {out->tir, P.tir, 9, 0, 9},
+      {out->tir, P.tir, 9, 0, 9}, {out->s, c->S.s_acc, 1, 0, 1},
       {lf ? out->sigmaa : out->sigmab, P.sigma_h, 9, 0, 9}, {lf ? out->sigmab : nullptr, c->S.sigma_o, 9, 0, 9},
       {lf ? out->straina : out->strainb, P.strain_h, 9, 0, 9}, {lf ? out->strainb : nullptr, c->S.strain_o, 9, 0, 9},
       {lf ? out->shear_stressa : out->shear_stressb, P.shear_h, 9, 0, 9},
@@ -1150,6 +1217,10 @@ psph_status download_impl(psph_ctx* c, int q, psph_particles* out) {
       {out->k_mod, offsetof(PClass, k_mod), 0}, {out->sigmay, offsetof(PClass, sigmay), 0},
       {out->cohesion, offsetof(PClass, coh), 0}, {out->phi, offsetof(PClass, phi), 0},
       {out->psi, offsetof(PClass, psi), 0},
+      {out->seepage_type, offsetof(PClass, seep_type), 1}, {out->var_porosity, offsetof(PClass, var_por), 1},
+      {out->is_sat, offsetof(PClass, is_sat), 1}, {out->n0, offsetof(PClass, n0), 0},
+      {out->d, offsetof(PClass, dgrain), 0}, {out->rho_f, offsetof(PClass, rho_f), 0},
+      {out->volume, offsetof(PClass, vol), 0},
   };
   for (const K& k : consts) {
     if (!k.out) continue;

@@ -37,6 +37,10 @@ enum : uint32_t {
 struct PClass {
   double cs, p0, rho0, fpmassc, alpha, beta, mu0, mu_ref, t0, bm, csmag, ti, tin, tid;
   double g_mod, k_mod, sigmay, coh, phi, psi, h, mass;
+  // soil-water interaction of soil classes (Source/Particle.h:110-121): initial
+  // porosity, permeabilities k and k2 (InitialChecks' values), grain size d,
+  // fluid density RhoF, particle volume V
+  double n0, kp, kp2, dgrain, rho_f, vol;
   // Drucker-Prager constants of the class (alpha, k_f, sin psi), derived on the
   // device once after upload with the same expressions the return mapping
   // used per particle (zero while the table is built on the host)
@@ -46,6 +50,10 @@ struct PClass {
   double eos_b, eos_inv_rho0;
   float eos_b32;
   int material, is_free, no_slip, pres_eq, shepard, les, vis_m, fail, id, inst;
+  int seep_type, var_por, is_sat;
+  // the class a particle of this class moves to when its saturation changes
+  // (saturated soil weighs its buoyant weight); set after the table is built
+  int twin;
 };
 
 // FP32 copy of the class constants used inside the FP32C pair loops (so those
@@ -58,6 +66,22 @@ struct PClass32 {
 };
 enum : int { CF_FREE = 1, CF_NOSLIP = 2, CF_LES = 4, CF_SHEPARD = 8, CF_T0 = 16, CF_TI = 32 };
 
+// Kozeny-Carman (1), Ergun (2) and Den Adel (3) permeabilities of soil at
+// porosity n and grain size d, in the reference's expression order
+// (InitialChecks, Source/Domain.cpp:1687-1713; VarPorosity, Source/Particle.cpp:450-474);
+// SeepageType 0 keeps the given k and k2.
+PSPH_HD void permeability(int type, double n, double d, double* k, double* k2) {
+  if (type == 1) {
+    *k = n * n * n * d * d / (180.0 * (1.0 - n) * (1.0 - n));
+  } else if (type == 2) {
+    *k = n * n * n * d * d / (150.0 * (1.0 - n) * (1.0 - n));
+    *k2 = 1.75 * (1.0 - n) / (n * n * n * d);
+  } else if (type == 3) {
+    *k = n * n * n * d * d / (150.0 * (1.0 - n) * (1.0 - n));
+    *k2 = 0.4 / (n * n * d);
+  }
+}
+
 // Per-instance (per-domain) scalars advanced on the device. A context holds one
 // instance for a single Domain, or many independent instances for an ensemble.
 struct InstState {
@@ -65,6 +89,8 @@ struct InstState {
   long long steps;
   unsigned long long dtmin_bits;  // running minimum of the acceleration time-step bound (ordered bits)
   int first_step, ct, shepard_counter, stop;
+  int k_initial;  // the first step after an initial upload: permeabilities are InitialChecks' values
+  int pad;
 };
 
 // Context-wide scalars.

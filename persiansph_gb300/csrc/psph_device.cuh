@@ -57,6 +57,8 @@ struct Scratch {
   double2* half2;
   int* half_stamp;       // instance step + 1 when the slot was written this step
   double* zwab;
+  double* s_acc;         // SWIType 1: Particle::S, the surface-erosion velocity derivative
+  uint8_t* satcheck;     // fluid-soil: Particle::SatCheck of this step
   double* sumden;
   double* sumkernel;
   double4_32a* nsv4;     // wall no-slip velocity
@@ -90,6 +92,9 @@ struct Options {
   int eos_cls;        // that class
   int dyn_mu;
   int soil_pairs;     // Material 3 (soil-soil walls take the partner's density)
+  int mixed;          // fluid (Material 1) and soil (Material 3) share the domain: each pair
+                      // kernel keeps to its material, CalcForce13 couples them (FP64 form)
+  int swi;            // Domain::SWIType
   int carry_shear_h;  // the sort moves the ShearStress history (Mat2, or a non-zero upload)
   int uniform_h;      // every particle has the same h
   int any_periodic;   // some instance has a periodic axis
@@ -155,6 +160,8 @@ void launch_forces32(const DevView& v, cudaStream_t st);  // FP32C form: fluid p
 void launch_expand_sr32(const DevView& v, int n, cudaStream_t st);  // sr32 -> the FP64 strain_rate tensors
 void launch_wall(const DevView& v, cudaStream_t st);      // wall interpolation
 void launch_forces(const DevView& v, cudaStream_t st);    // pair forces + per-block dt minimum
+void launch_saturation(const DevView& v, cudaStream_t st); // fluid-soil: saturation check and weight switch
+void launch_seepage(const DevView& v, cudaStream_t st);   // fluid-soil pair forces (CalcForce13) + dt minimum
 void launch_dt(const DevView& v, cudaStream_t st);        // dt reduction + AdaptiveTimeStep
 void launch_update(const DevView& v, cudaStream_t st);    // Move + material update + periodic wrap + leave
 void launch_begin(const DevView& v, cudaStream_t st);     // stop test, first-step counters

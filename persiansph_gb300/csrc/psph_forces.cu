@@ -311,12 +311,14 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
   int cell = -1, ci_cls = 0;
   if (i < n) {
     ci_cls = P.cls[i];
-    const bool run = !v.inst[CT[ci_cls].inst].stop;
+    // a fluid-soil domain runs this kernel for its fluid particles only
+    const bool run = !v.inst[CT[ci_cls].inst].stop && (!o.mixed || CT[ci_cls].material == 1);
     active = run && CT[ci_cls].is_free;
     cell = v.S.cellid[i];
     if (run && !active) {
       v.S.A4[i] = make_double4_32a(o.gravity[0], o.gravity[1], o.gravity[2], 0.0);
       v.S.zwab[i] = 1.0;
+      if (v.S.s_acc) v.S.s_acc[i] = 0.0;
     }
   }
   const PClass& Ci = CT[ci_cls];
@@ -335,6 +337,8 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
   double drho = 0.0, zw = 0.0, sd = 0.0, xs0 = 0.0, xs1 = 0.0, xs2 = 0.0;
   double sr0 = 0.0, sr1 = 0.0, sr2 = 0.0, sr4 = 0.0, sr5 = 0.0, sr8 = 0.0;
   double w01 = 0.0, w02 = 0.0, w12 = 0.0;  // antisymmetric counterpart of the strain-rate sums (closure)
+  double ss = 0.0;  // SWIType 1: the surface-erosion velocity derivative S
+  const bool want_s = v.S.s_acc != nullptr;
   int nnb = 0;
   const bool closure = o.closure && Ci.les;
   const bool any_periodic = g.periodic[0] | g.periodic[1] | g.periodic[2];
@@ -368,6 +372,7 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
       const int j = HALF ? (qe & kIndexMask) : qe;
       const double4_32a xj = P.X4[j];
       const PClass& Cj = CT[P.cls[j]];
+      if (!HALF && o.mixed && Cj.material != 1) continue;  // soil partners: CalcForce13
       // shared pair: both free, both lists in use; evaluates_pair picks the
       // side (the queue holds only those this side evaluates)
       const bool share = own_list && Cj.is_free && v.S.nl_count[j] >= 0;
@@ -428,8 +433,9 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
         TI = (Ci.ti * Ri + Cj.ti * Rj) * pow(K / Wd, (Ci.tin + Cj.tin) / 2.0);
       }
       double VI0 = 0.0, VI1 = 0.0, VI2 = 0.0;
+      double vab0 = 0.0;
       if ((Ci.no_slip || Cj.no_slip) || fj) {
-        double Mu, vab0, vab1, vab2;
+        double Mu, vab1, vab2;
         if (fj) {
           vab0 = v0; vab1 = v1; vab2 = v2;
           if (o.uniform_mu) Mu = o.mu_u;
@@ -487,6 +493,7 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
       drho += mj * di * inv_j * (GK * vx);
       zw += mj * inv_j * K;
       if (shep) sd += mj * K;
+      if (!HALF && want_s) ss = ss + mj / dj * vab0 * x1 * -GK;  // Source/Interaction.cpp:154
       if (HALF && share) {
         // j's terms of this evaluation, seen from j (x_ji = -x_ij, v_ji = -v_ij):
         // a_j -= m_i F, dDensity_j += m_i (rho_j / rho_i) v.GK x, ZWab_j += m_i / rho_i W,
@@ -520,6 +527,7 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
     v.S.A4[i] = make_double4_32a(ax, ay, az, drho);
     v.S.zwab[i] = zw;
     if (o.any_shepard) v.S.sumden[i] = sd;
+    if (want_s) v.S.s_acc[i] = ss;
     if (o.xsph != 0.0) v.S.vxsph4[i] = make_double4_32a(xs0, xs1, xs2, 0.0);
     if (o.need_sr) {
       double* out = v.S.strain_rate + 9 * (size_t)i;
@@ -536,7 +544,8 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
     const double cand = o.sqrt_h_a * sqrt(hi / an);
     if (cand < dtc) dtc = cand;  // NaN never compares less, as in the reference
   }
-  block_dt_and_pairs<kFT>(v, Ci.inst, active, dtc, npair2, red, cred);
+  // fluid-soil: the dt bound waits for the CalcForce13 terms (seepage kernel)
+  block_dt_and_pairs<kFT>(v, Ci.inst, active && !o.mixed, dtc, npair2, red, cred);
 }
 
 // Pass B of the once-per-pair form: adds, in list order, the terms the
@@ -622,17 +631,21 @@ __global__ void __launch_bounds__(kFT) forces_solid_kernel(DevView v) {
   int cell = -1, ci_cls = 0;
   if (i < n) {
     ci_cls = P.cls[i];
-    const bool run = !v.inst[CT[ci_cls].inst].stop;
+    // a fluid-soil domain runs this kernel for its soil particles only
+    const bool run = !v.inst[CT[ci_cls].inst].stop && (!o.mixed || CT[ci_cls].material == 3);
     active = run && CT[ci_cls].is_free;
     cell = v.S.cellid[i];
     if (run && !active) {
       v.S.A4[i] = make_double4_32a(o.gravity[0], o.gravity[1], o.gravity[2], 0.0);
       v.S.zwab[i] = 1.0;
+      if (v.S.s_acc) v.S.s_acc[i] = 0.0;
     }
   }
   const PClass& Ci = CT[ci_cls];
   const GridDev& g = grid_of(v, Ci.inst);
   const InstState& Is = v.inst[Ci.inst];
+  const bool want_s = v.S.s_acc != nullptr;
+  double ss = 0.0;  // SWIType 1: the surface-erosion velocity derivative S
   const int is = active ? i : 0;
   const double4_32a xi = P.X4[is];
   const double4_32a vi = P.V4[is];
@@ -668,6 +681,7 @@ __global__ void __launch_bounds__(kFT) forces_solid_kernel(DevView v) {
       const int j = qbuf[k][tid];
       const double4_32a xj = P.X4[j];
       const PClass& Cj = CT[P.cls[j]];
+      if (o.mixed && Cj.material != 3) continue;  // fluid partners: CalcForce13
       const double hb = (hi + Cj.h) / 2;
       double x0 = xi.x - xj.x, x1 = xi.y - xj.y, x2 = xi.z - xj.z;
       if (any_periodic) periodic_fix(g, x0, x1, x2, hb, cci, decode(g, v.S.cellid[j]));
@@ -769,6 +783,7 @@ __global__ void __launch_bounds__(kFT) forces_solid_kernel(DevView v) {
         xs0 -= s * v0; xs1 -= s * v1; xs2 -= s * v2;
       }
       if (shep) sd += mj * K;
+      if (want_s) ss = ss + mj / dj * vab0 * x1 * -GK;  // Source/Interaction.cpp:347
     }
     if (!__any_sync(0xffffffffu, more)) break;
   }
@@ -776,6 +791,7 @@ __global__ void __launch_bounds__(kFT) forces_solid_kernel(DevView v) {
     v.S.A4[i] = make_double4_32a(ax, ay, az, drho);
     v.S.zwab[i] = zw;
     if (o.any_shepard) v.S.sumden[i] = sd;
+    if (want_s) v.S.s_acc[i] = ss;
     if (o.xsph != 0.0) v.S.vxsph4[i] = make_double4_32a(xs0, xs1, xs2, 0.0);
     double* out = v.S.strain_rate + 9 * (size_t)i;
     out[0] = sr[0]; out[1] = sr[1]; out[2] = sr[2];
@@ -790,7 +806,7 @@ __global__ void __launch_bounds__(kFT) forces_solid_kernel(DevView v) {
     const double cand = o.sqrt_h_a * sqrt(hi / an);
     if (cand < dtc) dtc = cand;
   }
-  block_dt_and_pairs<kFT>(v, Ci.inst, active, dtc, npair2, red, cred);
+  block_dt_and_pairs<kFT>(v, Ci.inst, active && !o.mixed, dtc, npair2, red, cred);
 }
 
 // Per-instance step control, one block looping over the instances.
@@ -848,6 +864,7 @@ __global__ void end_kernel(DevView v) {
       I.shepard_counter = (I.shepard_counter == v.o.shepard_step) ? 0 : I.shepard_counter + 1;
     }
     I.first_step = 0;
+    I.k_initial = 0;
   }
 }
 
@@ -895,6 +912,203 @@ __global__ void pairs_export_kernel(DevView v, int which, long long* out, long l
   });
 }
 
+// ---------------------------------------------------------------------------
+// Fluid-soil coupling (a fluid and a soil in one domain, FP64 form)
+// ---------------------------------------------------------------------------
+// Saturation check (Source/Domain.cpp:1060-1089): a soil particle is saturated
+// this step when a fluid particle in a neighbouring cell (a candidate pair of
+// MainNeighbourSearch with one side free) lies in a cell row at or above its
+// own and at or above its own height.
+template <int DIM>
+__global__ void __launch_bounds__(kFT) saturation_check_kernel(DevView v) {
+  if (v.sc->all_stop) return;
+  const Persist& P = cur_persist(v);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= v.sc->n) return;
+  const PClass* __restrict__ CT = v.cls;
+  const PClass& Ci = CT[P.cls[i]];
+  const int cell = v.S.cellid[i];
+  if (Ci.material != 3 || cell < 0 || v.inst[Ci.inst].stop) return;
+  const GridDev& g = grid_of(v, Ci.inst);
+  const CellCoord ci = decode(g, cell);
+  const double yi = P.X4[i].y;
+  bool sat = false;
+  for_neighbor_ranges<DIM>(g, ci, v.S.start, [&](int lo, int hi) {
+    for (int j = lo; j < hi && !sat; ++j) {
+      const PClass& Cj = CT[P.cls[j]];
+      if (Cj.material != 1 || !(Ci.is_free || Cj.is_free)) continue;
+      if (decode(g, v.S.cellid[j]).y >= ci.y && P.X4[j].y >= yi) sat = true;
+    }
+  });
+  v.S.satcheck[i] = sat ? 1 : 0;
+}
+
+// The weight switch that follows (Source/Domain.cpp:1209-1234): a soil particle
+// whose saturation changed takes its class's twin (Mass = V (RefDensity -+ RhoF),
+// RefDensity -+ RhoF) and Density, Densityb -+ RhoF; the density its partners
+// see is updated with it.
+__global__ void __launch_bounds__(kFT) saturation_apply_kernel(DevView v) {
+  if (v.sc->all_stop) return;
+  const Persist& P = cur_persist(v);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= v.sc->n) return;
+  const PClass* __restrict__ CT = v.cls;
+  const int q = P.cls[i];
+  const PClass& C = CT[q];
+  if (C.material != 3 || v.S.cellid[i] < 0 || v.inst[C.inst].stop || C.twin < 0) return;
+  const bool sat = v.S.satcheck[i] != 0;
+  if (sat == (C.is_sat != 0)) return;
+  const double rf = C.rho_f;
+  double4_32a x = P.X4[i];
+  x.w = sat ? x.w - rf : x.w + rf;
+  P.X4[i] = x;
+  double4_32a& hb = (v.o.scheme == PSPH_MVERLET) ? P.H4[i] : P.H4b[i];  // Densityb
+  double4_32a h = hb;
+  h.w = sat ? h.w - rf : h.w + rf;
+  hb = h;
+  P.cls[i] = C.twin;
+  const PClass& T = CT[C.twin];
+  const double rho = x.w, inv = 1.0 / rho, pr = P.V4[i].w;
+  const double snd = T.is_free ? sound_speed(T.pres_eq, T.cs, rho, T.rho0) : v.S.D4[i].z;
+  v.S.D4[i] = make_double4_32a(inv, pr * inv * inv, snd, rho);
+}
+
+// Seepage (Source/Functions.cpp:266-298): Darcy (0, 1) or Forchheimer (2, 3)
+PSPH_D void seepage_coeffs(int type, double k, double k2, double mu, double rho, double& sf1, double& sf2) {
+  sf1 = mu / k;
+  sf2 = (type >= 2) ? k2 * rho : 0.0;
+}
+
+// CalcForce13 (Source/Interaction.cpp:508-653) from the side of free particle
+// i, for its partners of the other material, added to the acceleration its own
+// material's pair kernel wrote; then the dt bound and the finiteness check of
+// the gather form. Both orientations of the reference give the same terms:
+// v = v_fluid - v_soil, SFt = (SF1 v + SF2 |v| v) K with K = W(r/h, h) /
+// (Density_1 Density_2) and h the smaller smoothing length; the soil gains
+// m_fluid SFt (SWIType 2: minus m_fluid p_fluid GK x_soil,fluid), the fluid
+// loses m_soil SFt.
+template <int DIM, int KT>
+__global__ void __launch_bounds__(kFT) seepage_kernel(DevView v) {
+  __shared__ double red[kFT / 32];
+  __shared__ unsigned long long cred[kFT / 32];
+  const StepScalars* sc = v.sc;
+  if (sc->all_stop) return;
+  const Persist& P = cur_persist(v);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const Options& o = v.o;
+  const PClass* __restrict__ CT = v.cls;
+  double dtc = DBL_MAX;
+  unsigned long long npair2 = 0;
+  bool active = false;
+  int cell = -1, ci_cls = 0;
+  if (i < sc->n) {
+    ci_cls = P.cls[i];
+    active = !v.inst[CT[ci_cls].inst].stop && CT[ci_cls].is_free;
+    cell = v.S.cellid[i];
+  }
+  const PClass& Ci = CT[ci_cls];
+  const GridDev& g = grid_of(v, Ci.inst);
+  const InstState& Is = v.inst[Ci.inst];
+  const bool soil_i = (Ci.material == 3);
+  const int swi = o.swi;
+  double4_32a a4 = active ? v.S.A4[i] : make_double4_32a(0, 0, 0, 0);
+  double ax = a4.x, ay = a4.y, az = a4.z;
+  if (active && cell >= 0) {
+    const double4_32a xi = P.X4[i], vi = P.V4[i];
+    const CellCoord cci = decode(g, cell);
+    const bool any_periodic = g.periodic[0] | g.periodic[1] | g.periodic[2];
+    NbrSource<DIM> src;
+    src.init(v, g, i, true, 1.004f);
+    while (true) {
+      int code;
+      const int j = src.next(v, &code);
+      if (j < 0) break;
+      const int cj_cls = P.cls[j];
+      const PClass& Cj = CT[cj_cls];
+      if (Cj.material == Ci.material) continue;
+      const double h = Ci.h < Cj.h ? Ci.h : Cj.h;
+      const double4_32a xj = P.X4[j];
+      double x0 = xi.x - xj.x, x1 = xi.y - xj.y, x2 = xi.z - xj.z;
+      if (any_periodic) periodic_fix(g, x0, x1, x2, h, cci, decode(g, v.S.cellid[j]));
+      const double r = sqrt(x0 * x0 + x1 * x1 + x2 * x2);
+      const double q = r / h;
+      if (!(q <= g.cellfac)) continue;
+      npair2 += Cj.is_free ? 1ull : 2ull;
+      if (swi == 3) continue;
+      const double inv_h = 1.0 / h, ih2 = inv_h * inv_h;
+      const double cwh = Kern<DIM, KT>::cw() * (DIM == 2 ? ih2 : ih2 * inv_h);
+      const double rr = xi.w * xj.w;
+      const double K = Kern<DIM, KT>::W(q, cwh) / rr;
+      // soil side S, fluid side F
+      const int s = soil_i ? i : j, f = soil_i ? j : i;
+      const PClass& Cs = soil_i ? Ci : Cj;
+      const PClass& Cf = soil_i ? Cj : Ci;
+      const double4_32a vs = soil_i ? vi : P.V4[j];
+      const double4_32a vf = soil_i ? P.V4[j] : vi;
+      const double w0 = vf.x - vs.x, w1 = vf.y - vs.y, w2 = vf.z - vs.z;
+      const double nv = sqrt(w0 * w0 + w1 * w1 + w2 * w2);
+      double S0, S1, S2;
+      bool erosion = false;
+      if (swi == 1) {
+        // a fixed soil particle's ZWab is 1 once CalcForce2233 saw it, else 0
+        const double zw = Cs.is_free ? v.S.zwab[s] : (v.S.sumkernel[s] != 0.0 ? 1.0 : 0.0);
+        erosion = zw < 0.25;
+      }
+      if (erosion) {  // Source/Interaction.cpp:561-566
+        const double Cd = 24.0 * (Cf.mu_ref / Cf.rho0) / (Cs.dgrain * nv + 0.01 * h * h) + 2.0;
+        const double c = 3.0 / (4.0 * Cs.dgrain) * Cf.rho0 * (1.0 - Cs.n0) * Cd * nv;
+        S0 = c * w0 * K;
+        S1 = c * w1 * K;
+        S2 = c * w2 * K;
+        S1 += (Cf.rho0 * (1.0 - Cs.n0) * nv * fabs(v.S.s_acc[f] - v.S.s_acc[s])) * K;
+      } else {
+        double kp = Cs.kp, kp2 = Cs.kp2;
+        if (Cs.var_por && Cs.is_free && !Is.k_initial) {
+          // VarPorosity: the permeabilities of the strain the last update left
+          const double* E = P.strain + 9 * (size_t)s;
+          const double ev = (E[0] + E[4] + E[8]);
+          permeability(Cs.seep_type, (Cs.n0 + ev) / (1.0 + ev), Cs.dgrain, &kp, &kp2);
+        }
+        double sf1, sf2;
+        seepage_coeffs(Cs.seep_type, kp, kp2, Cf.mu_ref, Cf.rho0, sf1, sf2);
+        S0 = (sf1 * w0 + sf2 * nv * w0) * K;
+        S1 = (sf1 * w1 + sf2 * nv * w1) * K;
+        S2 = (sf1 * w2 + sf2 * nv * w2) * K;
+      }
+      if (DIM == 2) S2 = 0.0;
+      if (soil_i) {
+        const double mf = Cf.mass;
+        double a0 = mf * S0, a1 = mf * S1, a2 = mf * S2;
+        if (swi == 2) {  // pore pressure (Source/Interaction.cpp:608-637), x = x_soil - x_fluid
+          const double GK = Kern<DIM, KT>::GK(q, h / r, cwh * ih2) / rr;
+          const double c = mf * P.V4[j].w * GK;
+          a0 = a0 - c * x0;
+          a1 = a1 - c * x1;
+          a2 = a2 - c * x2;
+        }
+        ax += a0;
+        ay += a1;
+        az += a2;
+      } else {
+        const double ms = Cs.mass;
+        ax -= ms * S0;
+        ay -= ms * S1;
+        az -= ms * S2;
+      }
+    }
+    v.S.A4[i] = make_double4_32a(ax, ay, az, a4.w);
+    if (!(isfinite(ax) && isfinite(ay) && isfinite(az) && isfinite(a4.w))) atomicOr(&v.sc->status, ST_NONFINITE);
+    const double an = sqrt(ax * ax + ay * ay + az * az);
+    const double cand = o.sqrt_h_a * sqrt(Ci.h / an);
+    if (cand < dtc) dtc = cand;
+  } else if (active) {
+    const double an = sqrt(ax * ax + ay * ay + az * az);
+    const double cand = o.sqrt_h_a * sqrt(Ci.h / an);
+    if (cand < dtc) dtc = cand;
+  }
+  block_dt_and_pairs<kFT>(v, Ci.inst, active, dtc, npair2, red, cred);
+}
+
 inline int nblk(int n, int bt) { return n <= 0 ? 1 : (n + bt - 1) / bt; }
 
 template <int DIM>
@@ -911,6 +1125,13 @@ template <int DIM>
 void forces_dispatch(const DevView& v, cudaStream_t st) {
   const int nb = nblk(v.ncap, kFT);
   if (v.o.has_solid) {
+    if (v.o.mixed) {  // fluid-soil: the fluid's pairs, then the soil's (each kernel keeps to its material)
+      switch (v.o.kt) {
+        case 0: forces_fluid_kernel<DIM, 0, false><<<nb, kFT, 0, st>>>(v); break;
+        case 1: forces_fluid_kernel<DIM, 1, false><<<nb, kFT, 0, st>>>(v); break;
+        default: forces_fluid_kernel<DIM, 2, false><<<nb, kFT, 0, st>>>(v); break;
+      }
+    }
     switch (v.o.kt) {
       case 0: forces_solid_kernel<DIM, 0><<<nb, kFT, 0, st>>>(v); break;
       case 1: forces_solid_kernel<DIM, 1><<<nb, kFT, 0, st>>>(v); break;
@@ -954,6 +1175,30 @@ void launch_wall(const DevView&, cudaStream_t) {}  // fused into launch_prepare
 void launch_forces(const DevView& v, cudaStream_t st) {
   if (v.o.dim == 2) forces_dispatch<2>(v, st);
   else forces_dispatch<3>(v, st);
+}
+
+void launch_saturation(const DevView& v, cudaStream_t st) {
+  const int nb = nblk(v.ncap, kFT);
+  if (v.o.dim == 2) saturation_check_kernel<2><<<nb, kFT, 0, st>>>(v);
+  else saturation_check_kernel<3><<<nb, kFT, 0, st>>>(v);
+  saturation_apply_kernel<<<nb, kFT, 0, st>>>(v);
+}
+
+void launch_seepage(const DevView& v, cudaStream_t st) {
+  const int nb = nblk(v.ncap, kFT);
+  if (v.o.dim == 2) {
+    switch (v.o.kt) {
+      case 0: seepage_kernel<2, 0><<<nb, kFT, 0, st>>>(v); break;
+      case 1: seepage_kernel<2, 1><<<nb, kFT, 0, st>>>(v); break;
+      default: seepage_kernel<2, 2><<<nb, kFT, 0, st>>>(v); break;
+    }
+  } else {
+    switch (v.o.kt) {
+      case 0: seepage_kernel<3, 0><<<nb, kFT, 0, st>>>(v); break;
+      case 1: seepage_kernel<3, 1><<<nb, kFT, 0, st>>>(v); break;
+      default: seepage_kernel<3, 2><<<nb, kFT, 0, st>>>(v); break;
+    }
+  }
 }
 
 void launch_dt(const DevView& v, cudaStream_t st) { dt_finalize_kernel<<<1, 256, 0, st>>>(v); }

@@ -424,7 +424,8 @@ void launch_upload_pack(const double* sx, const double* sd, const double* sp, co
 }
 
 int launches_per_step(const DevView& v) {
-  return (v.o.fp32 ? 17 : 16) + (v.o.closure ? 1 : 0) + (v.o.has_solid ? 1 : 0) + (v.o.fp64_half ? 1 : 0);
+  return (v.o.fp32 ? 17 : 16) + (v.o.closure ? 1 : 0) + (v.o.has_solid ? 1 : 0) + (v.o.fp64_half ? 1 : 0) +
+         (v.o.mixed ? (v.o.swi != 2 ? 4 : 2) : 0);
 }
 
 }  // namespace psph

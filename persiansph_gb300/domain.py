@@ -267,8 +267,8 @@ class Domain:
 
     # -- boundary to the C ABI ----------------------------------------------
     def config(self, dt: float) -> PsphConfig:
-        if self.SWIType != 0 or self.FSI:
-            raise Fatal("soil-water interaction and FSI are outside this build")
+        if self.FSI:
+            raise Fatal("fluid-solid interaction (FSI) is outside this build")
         if self.BC.InOutFlow:
             raise Fatal("in/out-flow boundaries are outside this build")
         c = PsphConfig()
@@ -283,7 +283,7 @@ class Domain:
             c.body_force[d] = float(self.BodyForce[d])
             c.dom_max[d] = float(self.DomMax[d])
             c.dom_min[d] = float(self.DomMin[d])
-        c.swi_type = 0
+        c.swi_type = int(self.SWIType)
         c.shepard_step = int(self.ShepardStep)
         c.precision = int(self.Precision)
         c.wall_pressure_mode = int(self.WallPressureMode)

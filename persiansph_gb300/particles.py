@@ -29,6 +29,8 @@ REF_NAMES = {
     "Sigmaa": "sigmaa", "Sigmab": "sigmab", "ShearStress": "shear_stress", "ShearStressa": "shear_stressa",
     "ShearStressb": "shear_stressb", "Strain": "strain", "Straina": "straina", "Strainb": "strainb",
     "StrainRate": "strain_rate", "RotationRate": "rotation_rate", "TIR": "tir",
+    "SeepageType": "seepage_type", "VarPorosity": "var_porosity", "IsSat": "is_sat", "n0": "n0", "k": "k",
+    "k2": "k2", "d": "d", "RhoF": "rho_f", "V": "volume", "S": "s",
 }
 
 
@@ -119,7 +121,7 @@ class Particle:
             raise AttributeError(ref_name)
         v = self._set.get(f)[self._i]
         if f in INT_FIELDS:
-            return bool(v) if f in ("is_free", "no_slip", "shepard", "les") else int(v)
+            return bool(v) if f in ("is_free", "no_slip", "shepard", "les", "var_porosity", "is_sat") else int(v)
         return v if (f in VEC_FIELDS or f in TEN_FIELDS) else float(v)
 
     def __setattr__(self, ref_name, value):

@@ -8,6 +8,7 @@ example drivers do, with sizes parameterised so tests can run them small:
   dam_break_2d    2D water column in a tank (3-DamBreak.cpp shape)
   dam_break_3d    3D water column in a tank (4-DamBreak3D.cpp shape)
   granular_column 2D Drucker-Prager soil column (Old_Tests/ReposeAngle2.cpp shape)
+  seepage_bed_2d  2D dam break over an erodible soil bed (Old_Tests/Dam_Scouring2.cpp shape)
 
 All inputs are synthetic and seeded; the reference ships no datasets.
 """
@@ -327,6 +328,106 @@ def granular_column_3d(dx=0.01, W=0.06, D=0.04, aspect=1.0, TL_factor=1.0, wall_
     dt = 0.2 * h / cs
     return dom, dt, {"H": H, "W": W, "D": D, "K": K, "G": G, "cs": cs, "h": h, "n_soil": int(fl.sum()),
                      "n_wall": int(wall.sum())}
+
+
+def seepage_bed_2d(dx=0.01, L=0.3, H=0.2, Hs=0.1, TL=0.6, wall_layers=3, rho_f=1000.0, rho_grain=1580.0,
+                   n0=0.42, grain=0.00392, E=5.0e6, nu=0.3, phi_deg=38.0, swi=0, seepage_type=1,
+                   var_porosity=False, k=1.0e-9, k2=0.0, grains=0, scheme=0, g=9.81, hfac=1.2, mu=1.0e-3,
+                   alpha=0.1, seed=0, sat_from_x=None):
+    """2D dam break over an erodible soil bed, the shape of Old_Tests/Dam_Scouring2.cpp:
+    a TL-wide tank whose lower Hs is a saturated-density soil bed (Material 3,
+    Drucker-Prager, non-associated Fail 3, density (1 - n0) rho_grain + n0 rho_f)
+    and an L x H water column (Material 1) on the bed at the left. Walls are soil
+    below the bed surface and fluid above it, so every pair type meets: fluid and
+    soil with their own kind and walls, fluid with soil, and each with the other's
+    walls. `grains` water particles (chosen with numpy default_rng(seed)) become
+    soil grains suspended in the water (the surface-erosion branch of SWIType 1
+    acts on soil with few soil neighbours). SWIType `swi`, SeepageType
+    `seepage_type` (k and k2 are used as given for type 0, derived from n0 and
+    the grain size otherwise). Bed particles right of `sat_from_x` start marked
+    saturated (IsSat), as after a drained flood. Returns (domain, dt, info).
+    """
+    dom = Domain()
+    dom.Dimension = 2
+    dom.Scheme = scheme
+    dom.Kernel_Set(Qubic_Spline)
+    dom.Viscosity_Eq_Set(Morris)
+    dom.Gradient_Approach_Set(Squared_density)
+    dom.Gravity = [0.0, -g, 0.0]
+    dom.SWIType = swi
+    dom.InitialDist = dx
+    h = hfac * dx
+    rho_s = rho_grain * (1.0 - n0) + n0 * rho_f
+    K = E / (3.0 * (1.0 - 2.0 * nu))
+    G = E / (2.0 * (1.0 + nu))
+    cs_s = math.sqrt(K / (rho_s - rho_f))
+    cs_f = 10.0 * math.sqrt(2.0 * g * H)
+    TH = Hs + H + 2 * dx
+    _tank(dom, dx, TL, TH, 0.0, wall_layers)
+    p = dom.particles
+    x = p.get("x")
+    xb, yb = x[:, 0], x[:, 1]
+    wall = (xb < 0.0) | (yb < 0.0) | (xb > TL)
+    bed = (~wall) & (yb < Hs)
+    water = (~wall) & (yb >= Hs) & (yb < Hs + H) & (xb < L)
+    p.keep(wall | bed | water)
+    x = p.get("x")
+    xb, yb = x[:, 0], x[:, 1]
+    wall = (xb < 0.0) | (yb < 0.0) | (xb > TL)
+    soil = yb < Hs
+    water = (~wall) & (~soil)
+    if grains:
+        rng = np.random.default_rng(seed)
+        pick = rng.choice(np.flatnonzero(water), size=grains, replace=False)
+        soil = soil.copy()
+        soil[pick] = True
+    fluid = ~soil
+    n = p.n
+    p.set("h", h)
+    p.set("material", np.where(soil, 3, 1).astype(np.int32))
+    p.set("is_free", (~wall).astype(np.int32))
+    p.set("no_slip", wall.astype(np.int32))
+    ids = np.where(wall, np.where(soil, 4, 2), np.where(soil, 3, 1)).astype(np.int32)
+    p.set("id", ids)
+    p.set("alpha", alpha)
+    # fluid: Tait EOS, hydrostatic density above the bed
+    dens = np.full(n, rho_s)
+    fl_free = fluid & ~wall
+    dens[fluid] = rho_f
+    dens[fl_free] = rho_f * np.power(1 + 7.0 * g * (Hs + H - yb[fl_free]) / (cs_f * cs_f), 1.0 / 7.0)
+    p.set("density", dens)
+    p.set("densityb", dens)
+    p.set("ref_density", np.where(soil, rho_s, rho_f))
+    p.set("cs", np.where(soil, cs_s, cs_f))
+    p.set("pres_eq", np.where(soil, 0, 1).astype(np.int32))
+    p.set("mu", np.where(soil, 0.0, mu))
+    p.set("mu_ref", np.where(soil, 0.0, mu))
+    p.set("mass", np.where(soil, rho_s, rho_f) * dx * dx)
+    # soil: Drucker-Prager, geostatic stress of the bed
+    p.set("beta", np.where(soil, 0.1, 0.0))
+    p.set("g_mod", np.where(soil, G, 0.0))
+    p.set("k_mod", np.where(soil, K, 0.0))
+    p.set("fail", np.where(soil, 3, 0).astype(np.int32))
+    p.set("phi", np.where(soil, phi_deg / 180.0 * math.pi, 0.0))
+    p.set("seepage_type", np.where(soil, seepage_type, 0).astype(np.int32))
+    p.set("var_porosity", (soil & bool(var_porosity)).astype(np.int32))
+    p.set("n0", np.where(soil, n0, 0.0))
+    p.set("d", np.where(soil, grain, 0.0))
+    p.set("rho_f", np.where(soil, rho_f, 0.0))
+    p.set("k", np.where(soil, k, 0.0))
+    p.set("k2", np.where(soil, k2, 0.0))
+    if sat_from_x is not None:
+        p.set("is_sat", (soil & ~wall & (xb > sat_from_x)).astype(np.int32))
+    sig = p.get("sigma")
+    bed_free = soil & ~wall & (yb < Hs)
+    K0 = 1 - math.sin(phi_deg / 180.0 * math.pi)
+    depth = Hs - yb[bed_free]
+    sig[bed_free, 1, 1] = -(rho_s - rho_f) * g * depth
+    sig[bed_free, 0, 0] = K0 * sig[bed_free, 1, 1]
+    sig[bed_free, 2, 2] = K0 * sig[bed_free, 1, 1]
+    dt = min(0.25 * h / cs_f, 0.2 * h / cs_s)
+    return dom, dt, {"h": h, "cs_f": cs_f, "cs_s": cs_s, "n_fluid": int((fluid & ~wall).sum()),
+                     "n_soil": int((soil & ~wall).sum()), "n_wall": int(wall.sum())}
 
 
 def granular_ensemble(n=256, seed=0, dx=1e-3, W=0.2, aspect=(0.5, 4.0), phi_deg=(20.0, 40.0), fail=2, **kw):

@@ -24,7 +24,8 @@ from oracle.oracle import read_pairs_dir, read_state_dir, reference_box, run_ref
 from tests.golden.cases import CASES, BOXES  # noqa: E402
 
 FIELDS = ("x", "v", "density", "pressure", "a", "ddensity", "zwab", "sigma", "strain_rate", "rotation_rate",
-          "shear_stress", "tir", "va", "vb", "densitya", "densityb", "mu", "nsv", "sumkernel")
+          "shear_stress", "tir", "va", "vb", "densitya", "densityb", "mu", "nsv", "sumkernel", "mass",
+          "ref_density", "is_sat", "s", "strain")
 
 
 def main(only=()):

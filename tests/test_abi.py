@@ -37,9 +37,10 @@ def test_struct_layouts_match_header():
 #include <stddef.h>
 #include "psph.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(psph_config), sizeof(psph_grid), sizeof(psph_integrator),
-         sizeof(psph_particles), offsetof(psph_config, gravity), offsetof(psph_particles, sigma),
-         sizeof(psph_tuning));
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(psph_config), sizeof(psph_grid),
+         sizeof(psph_integrator), sizeof(psph_particles), offsetof(psph_config, gravity),
+         offsetof(psph_particles, sigma), sizeof(psph_tuning), offsetof(psph_particles, seepage_type),
+         offsetof(psph_particles, s));
   return 0;
 }
 '''
@@ -56,10 +57,12 @@ int main(void) {
     assert out[4] == abi.PsphConfig.gravity.offset
     assert out[5] == abi.PsphParticles.sigma.offset
     assert out[6] == ctypes.sizeof(abi.PsphTuning)
+    assert out[7] == abi.PsphParticles.seepage_type.offset
+    assert out[8] == abi.PsphParticles.s.offset
 
 
 def test_abi_version():
-    assert abi.load_library().psph_abi_version() == 1
+    assert abi.load_library().psph_abi_version() == 2
 
 
 def test_create_reports_no_device_or_validates():
