@@ -530,6 +530,13 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
           FAIL(PSPH_ERR_INVALID_ARGUMENT, "Seepage Type No is out of range (particle %lld)", (long long)i);
         // InitialChecks: permeabilities from the porosity (Source/Domain.cpp:1680-1716)
         if (initial) permeability(C.seep_type, C.n0, C.dgrain, &C.kp, &C.kp2);
+        // after the first step a free VarPorosity particle's permeabilities follow
+        // its strain (the pair kernel derives them): the uploaded values would only
+        // split the class table
+        if (!initial && C.var_por && C.is_free && C.seep_type >= 1) {
+          C.kp = 0.0;
+          if (C.seep_type >= 2) C.kp2 = 0.0;
+        }
       }
       if (C.material < 1 || C.material > 3)
         FAIL(PSPH_ERR_INVALID_ARGUMENT, "Material Type No is out of range (particle %lld)", (long long)i);

@@ -333,7 +333,7 @@ def granular_column_3d(dx=0.01, W=0.06, D=0.04, aspect=1.0, TL_factor=1.0, wall_
 def seepage_bed_2d(dx=0.01, L=0.3, H=0.2, Hs=0.1, TL=0.6, wall_layers=3, rho_f=1000.0, rho_grain=1580.0,
                    n0=0.42, grain=0.00392, E=5.0e6, nu=0.3, phi_deg=38.0, swi=0, seepage_type=1,
                    var_porosity=False, k=1.0e-9, k2=0.0, grains=0, scheme=0, g=9.81, hfac=1.2, mu=1.0e-3,
-                   alpha=0.1, seed=0, sat_from_x=None):
+                   alpha=0.1, seed=0, sat_from_x=None, cohesion=0.0):
     """2D dam break over an erodible soil bed, the shape of Old_Tests/Dam_Scouring2.cpp:
     a TL-wide tank whose lower Hs is a saturated-density soil bed (Material 3,
     Drucker-Prager, non-associated Fail 3, density (1 - n0) rho_grain + n0 rho_f)
@@ -409,6 +409,7 @@ def seepage_bed_2d(dx=0.01, L=0.3, H=0.2, Hs=0.1, TL=0.6, wall_layers=3, rho_f=1
     p.set("k_mod", np.where(soil, K, 0.0))
     p.set("fail", np.where(soil, 3, 0).astype(np.int32))
     p.set("phi", np.where(soil, phi_deg / 180.0 * math.pi, 0.0))
+    p.set("cohesion", np.where(soil, cohesion, 0.0))
     p.set("seepage_type", np.where(soil, seepage_type, 0).astype(np.int32))
     p.set("var_porosity", (soil & bool(var_porosity)).astype(np.int32))
     p.set("n0", np.where(soil, n0, 0.0))

@@ -95,6 +95,8 @@ class GpuDomain:
         return out
 
     def _untracked(self, f: str) -> bool:
+        if f in ("k", "k2"):  # permeabilities are read on upload only
+            return True
         lf = self.cfg.scheme == 1
         if lf:
             return False

@@ -92,26 +92,33 @@ def fluid_preseq2():
     return dom, dt, info
 
 
+# The seepage cases' soil has 1 kPa cohesion: a cohesionless bed surface sits
+# on the Drucker-Prager apex, where rounding-level differences (a different
+# summation order) switch the return mapping's branch within tens of steps and
+# no two correct implementations agree to 1e-9 (measured on the oracle with
+# 1e-14 position noise: 4e-4 after 25 steps, 4e-13 with the cohesion).
+
+
 def seep_darcy():
     """Fluid over a soil bed, SWIType 0 (seepage force + buoyant weight), Kozeny-Carman permeability;
     the dry right part of the bed starts marked saturated, so it switches back at the first step."""
-    return scenarios.seepage_bed_2d(swi=0, seepage_type=1, sat_from_x=0.45)
+    return scenarios.seepage_bed_2d(swi=0, seepage_type=1, sat_from_x=0.45, cohesion=1000.0)
 
 
 def seep_erosion_ergun():
     """SWIType 1 (seepage + surface erosion of suspended grains), Ergun permeability following the
     volumetric strain (VarPorosity), leapfrog."""
-    return scenarios.seepage_bed_2d(swi=1, seepage_type=2, var_porosity=True, grains=6, scheme=1)
+    return scenarios.seepage_bed_2d(swi=1, seepage_type=2, var_porosity=True, grains=6, scheme=1, cohesion=1000.0)
 
 
 def seep_pore_pressure():
     """SWIType 2 (seepage + pore pressure of the fluid), Den Adel permeability."""
-    return scenarios.seepage_bed_2d(swi=2, seepage_type=3)
+    return scenarios.seepage_bed_2d(swi=2, seepage_type=3, cohesion=1000.0)
 
 
 def seep_buoyancy_only():
     """SWIType 3 (no drag; saturated soil still weighs its buoyant weight), Darcy with a given k."""
-    return scenarios.seepage_bed_2d(swi=3, seepage_type=0, k=2.0e-9)
+    return scenarios.seepage_bed_2d(swi=3, seepage_type=0, k=2.0e-9, cohesion=1000.0)
 
 
 CASES = {
@@ -128,7 +135,7 @@ CASES = {
     "soil3d_ti": (soil3d_ti, 5, (1, 2, 5)),
     "fluid_preseq2": (fluid_preseq2, 3, (1, 3)),
     "seep_darcy": (seep_darcy, 32, (1, 2, 32)),
-    "seep_erosion_ergun": (seep_erosion_ergun, 10, (1, 2, 10)),
+    "seep_erosion_ergun": (seep_erosion_ergun, 20, (1, 2, 20)),
     "seep_pore_pressure": (seep_pore_pressure, 10, (1, 10)),
     "seep_buoyancy_only": (seep_buoyancy_only, 10, (1, 10)),
 }

@@ -46,4 +46,12 @@ def assert_step_parity(gpu: dict, ora: dict, a_scale, dr_scale, dt, tol=1e-12, l
             continue
         e = np.max(np.abs(got - ref)) / scale
         assert e <= 1e3 * tol, f"{label}: {f} rel err {e:.3e}"
+    # fluid-soil coupling: saturation state and the weights it sets, the erosion derivative S
+    assert np.array_equal(gpu["is_sat"], ora["is_sat"]), f"{label}: saturation state differs"
+    em = np.max(np.abs(gpu["mass"] - ora["mass"]) / np.abs(ora["mass"]))
+    assert em <= tol, f"{label}: mass rel err {em:.3e}"
+    s_scale = np.max(np.abs(ora["s"]))
+    if s_scale > 0.0:
+        es = np.max(np.abs(gpu["s"] - ora["s"])[free]) / s_scale
+        assert es <= 1e3 * tol, f"{label}: S rel err {es:.3e}"
     return ea, ed
