@@ -445,7 +445,6 @@ inline void Domain::DelParticles(int const& Tags) {
 
 inline void Domain::Solve(double tf, double dt, double dtOut, char const* TheFileKey, size_t maxidx) {
   std::cout << "\n--------------Solving---------------------------------------------------------------" << std::endl;
-  if (FSI) throw new Fatal("fluid-solid interaction (FSI) is outside this build");
   if (BC.InOutFlow != 0) throw new Fatal("in/out-flow boundaries are outside this build");
   const Vec3_t body = BodyForce + hook_acceleration(GeneralBefore, "GeneralBefore") +
                       hook_acceleration(GeneralAfter, "GeneralAfter");
@@ -472,6 +471,7 @@ inline void Domain::Solve(double tf, double dt, double dtOut, char const* TheFil
   cfg.dt = dt;
   cfg.time = Time;
   cfg.swi_type = (int)SWIType;
+  cfg.fsi = FSI ? 1 : 0;
 
   psph_ctx* ctx = nullptr;
   Pack pk;

@@ -85,7 +85,10 @@ typedef struct psph_config {
   double dom_min[3];          /* Domain::DomMin (default +1e11: no override) */
   double dt;                  /* Solve's dt argument: initial and maximum time step */
   double time;                /* Domain::Time at upload */
-  int32_t reserved[8];        /* must be zero */
+  int32_t fsi;                /* Domain::FSI: free solid particles take the pressure and velocity
+                                 their free fluid neighbours interpolate (Source/Domain.cpp:1090-1160);
+                                 fluid-solid pairs use CalcForce12 either way */
+  int32_t reserved[7];        /* must be zero */
 } psph_config;
 
 /* Cell grid made by CellInitiate (Source/Domain.cpp:549-660). */

@@ -167,6 +167,7 @@ def write_state_dir(path: str, cfg: PsphConfig, pset: ParticleSet, extra: dict |
         "gravity": list(cfg.gravity), "body_force": list(cfg.body_force), "xsph": [cfg.xsph],
         "sqrt_h_a": [cfg.sqrt_h_a], "R": [cfg.R], "dom_max": list(cfg.dom_max), "dom_min": list(cfg.dom_min),
         "dt": [cfg.dt], "time": [cfg.time], "shepard_step": [cfg.shepard_step], "swi_type": [cfg.swi_type],
+        "fsi": [cfg.fsi],
     }
     if extra:
         lines.update(extra)

@@ -14,9 +14,13 @@
  *    can keep a larger value; with Nproc=1 both are the plain minimum.
  *  - A particle more than hmax outside the grid makes ListGenerate index out of
  *    bounds in the reference (Source/Domain.cpp:669-691); here it is an error.
- *  - Fluid-solid pairs (CalcForce12, FSI) are reported as PSPH_ERR_UNSUPPORTED
- *    instead of being computed; solid-soil pairs, which the reference aborts
- *    on, as PSPH_ERR_INVALID_ARGUMENT.
+ *  - Solid-soil pairs, which the reference aborts on, are reported as
+ *    PSPH_ERR_INVALID_ARGUMENT.
+ *  - The FSI interpolation's normalisation runs once per list entry of
+ *    FreeFSIParticles, which holds a solid particle once per fluid pair
+ *    (Source/Domain.cpp:1109, :1126, :1151-1157): the sums are divided by the
+ *    kernel sum as many times, in sequence, as the reference does with
+ *    Nproc = 1 (with more threads the duplicate entries race there).
  *  - Particle::n (porosity) is not kept: only the permeabilities it feeds are.
  */
 #include "psph_oracle.h"
@@ -58,6 +62,10 @@ struct psph_oracle {
   int32_t* CC; /* Particle::CC[3] */
   int32_t* HOC;
   int32_t* satcheck; /* Particle::SatCheck of the current step */
+  /* FSI interpolation of the current step (Particle::FSIPressure, FSINSv,
+   * FSISumKernel) and the particle's entries in FreeFSIParticles */
+  double *fsi_p, *fsi_nsv, *fsi_sk;
+  int32_t* fsi_cnt;
   int64_t ncells;
   int nthr;
   pairvec *sm, *fsm, *nsm;
@@ -600,6 +608,10 @@ static void start_acceleration(psph_oracle* o, int nthr) {
     o->sumkernel[i] = 0.0;
     o->satcheck[i] = 0;
     o->s[i] = 0.0;
+    o->fsi_p[i] = 0.0;
+    o->fsi_sk[i] = 0.0;
+    o->fsi_cnt[i] = 0;
+    for (int d = 0; d < 3; ++d) o->fsi_nsv[3 * i + d] = 0.0;
     if (dim == 2) o->v[3 * i + 2] = 0.0;
     memset(o->strain_rate + 9 * i, 0, 9 * sizeof(double));
     memset(o->rotation_rate + 9 * i, 0, 9 * sizeof(double));
@@ -661,6 +673,39 @@ static void primary_compute(psph_oracle* o, int nthr) {
                 o->satcheck[P2] = 1;
                 omp_unset_lock(&o->locks[P2]);
               }
+      }
+    /* FSI: a free solid particle interpolates pressure and velocity from its
+     * free fluid candidates (Source/Domain.cpp:1090-1145); which sum the
+     * velocity goes to, and the gravity term's sign, follow the pair's
+     * orientation as in the reference */
+    if (o->cfg.fsi)
+      for (int64_t a = 0; a < o->nsm[k].n; a++) {
+        int64_t P1 = o->nsm[k].v[2 * a], P2 = o->nsm[k].v[2 * a + 1];
+        if (o->material[P1] * o->material[P2] != 2 || !(FREE(P1) * FREE(P2))) continue;
+        double xij[3];
+        for (int d = 0; d < 3; ++d) xij[d] = o->x[3 * P1 + d] - o->x[3 * P2 + d];
+        double h = (o->h[P1] + o->h[P2]) / 2.0;
+        periodic_correction(o, xij, h, P1, P2);
+        double K = Kernel(dim, kt, sqrt(dot3(xij, xij)) / h, h);
+        const int64_t S = (o->material[P1] == 1) ? P2 : P1, F = (S == P1) ? P2 : P1;
+        omp_set_lock(&o->locks[S]);
+        o->fsi_cnt[S] += 1;
+        o->fsi_sk[S] += K;
+        if (S == P2)
+          for (int d = 0; d < 3; ++d) o->nsv[3 * S + d] += o->v[3 * F + d] * K;
+        else
+          for (int d = 0; d < 3; ++d) o->fsi_nsv[3 * S + d] += o->v[3 * F + d] * K;
+        o->fsi_p[S] += o->pressure[F] * K + dot3(G, xij) * o->density[F] * K;
+        omp_unset_lock(&o->locks[S]);
+      }
+  }
+  if (o->cfg.fsi) {
+    /* Source/Domain.cpp:1147-1160, once per FreeFSIParticles entry */
+#pragma omp parallel for schedule(static) num_threads(nthr)
+    for (int64_t i = 0; i < o->n; i++)
+      for (int32_t c = 0; c < o->fsi_cnt[i]; ++c) {
+        o->fsi_p[i] = o->fsi_p[i] / o->fsi_sk[i];
+        for (int d = 0; d < 3; ++d) o->fsi_nsv[3 * i + d] = o->fsi_nsv[3 * i + d] / o->fsi_sk[i];
       }
   }
 #pragma omp parallel for schedule(static) num_threads(nthr)
@@ -1023,6 +1068,95 @@ static int calc_force2233(psph_oracle* o, int64_t p1, int64_t p2) {
   return 1;
 }
 
+/* CalcForce12 (Source/Interaction.cpp:379-507): fluid-solid pair. The solid
+ * side enters with the density its interpolated FSIPressure gives under the
+ * fluid's EOS, the fluid's mass on both sides and the no-slip velocity from
+ * FSINSv; the reference's artificial-viscosity branch is dead (Alpha and Beta
+ * are set to zero just before their test), and the solid gets no density rate
+ * or strain rate. */
+static int calc_force12(psph_oracle* o, int64_t p1, int64_t p2) {
+  const int dim = o->cfg.dimension, kt = o->cfg.kernel_type;
+  double h = (o->h[p1] + o->h[p2]) / 2;
+  double xij[3];
+  for (int d = 0; d < 3; ++d) xij[d] = o->x[3 * p1 + d] - o->x[3 * p2 + d];
+  periodic_correction(o, xij, h, p1, p2);
+  double rij = sqrt(dot3(xij, xij));
+  if ((rij / h) > o->g.cellfac) return 0;
+  double di, dj, mi, mj, vij[3];
+  for (int d = 0; d < 3; ++d) vij[d] = o->v[3 * p1 + d] - o->v[3 * p2 + d];
+  double GK = GradKernel(dim, kt, rij / h, h);
+  const int fluid1 = (o->material[p1] == 1);
+  if (fluid1) {
+    di = o->density[p1];
+    mi = o->mass[p1];
+    dj = DensitySolid(o->pres_eq[p1], o->cs[p1], o->p0[p1], o->fsi_p[p2], o->ref_density[p1]);
+    mj = o->mass[p1];
+  } else {
+    di = DensitySolid(o->pres_eq[p2], o->cs[p2], o->p0[p2], o->fsi_p[p1], o->ref_density[p2]);
+    mi = o->mass[p2];
+    dj = o->density[p2];
+    mj = o->mass[p2];
+  }
+  const double PIij = 0.0;
+  double SR[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, VI[3] = {0, 0, 0}, vab[3], Mu;
+  if (fluid1) {
+    for (int d = 0; d < 3; ++d) vab[d] = o->v[3 * p1 + d] - (2.0 * o->v[3 * p2 + d] - o->fsi_nsv[3 * p2 + d]);
+    Mu = o->mu[p1];
+  } else {
+    for (int d = 0; d < 3; ++d) vab[d] = (2.0 * o->v[3 * p1 + d] - o->fsi_nsv[3 * p1 + d]) - o->v[3 * p2 + d];
+    Mu = o->mu[p2];
+  }
+  if ((o->t0[p1] > 0.0 || o->t0[p2] > 0.0) || (o->les[p1] || o->les[p2])) {
+    SR[0] = 2.0 * vab[0] * xij[0];
+    SR[1] = vab[0] * xij[1] + vab[1] * xij[0];
+    SR[2] = vab[0] * xij[2] + vab[2] * xij[0];
+    SR[3] = vab[0] * xij[1] + vab[1] * xij[0];
+    SR[4] = 2.0 * vab[1] * xij[1];
+    SR[5] = vab[1] * xij[2] + vab[2] * xij[1];
+    SR[6] = vab[0] * xij[2] + vab[2] * xij[0];
+    SR[7] = vab[1] * xij[2] + vab[2] * xij[1];
+    SR[8] = 2.0 * vab[2] * xij[2];
+    for (int e = 0; e < 9; ++e) SR[e] = SR[e] * -GK;
+  }
+  Viscous_Force(o->cfg.vis_eq, VI, Mu, di, dj, GK, vab, dim, kt, rij, h, xij, vij);
+  const double p1v = fluid1 ? o->pressure[p1] : o->fsi_p[p1];
+  const double p2v = fluid1 ? o->fsi_p[p2] : o->pressure[p2];
+  double s;
+  if (o->cfg.gradient_type == 0) s = -1.0 * (p1v / (di * di) + p2v / (dj * dj) + PIij) * GK;
+  else s = -1.0 * ((p1v + p2v) / (di * dj) + PIij) * GK;
+  double temp[3];
+  for (int d = 0; d < 3; ++d) temp[d] = s * xij[d] + VI[d];
+  if (dim == 2) temp[2] = 0.0;
+  double gx[3] = {GK * xij[0], GK * xij[1], GK * xij[2]};
+  double temp1 = dot3(vij, gx);
+  const double tn = sqrt(dot3(temp, temp));
+  omp_set_lock(&o->locks[p1]);
+  for (int d = 0; d < 3; ++d) o->a[3 * p1 + d] += mj * temp[d];
+  if (fluid1) {
+    o->ddensity[p1] += mj * (di / dj) * temp1;
+    if (o->t0[p1] > 0.0 || o->les[p1]) {
+      double c = mj / dj;
+      for (int e = 0; e < 9; ++e) o->strain_rate[9 * p1 + e] = o->strain_rate[9 * p1 + e] + SR[e] * c;
+    }
+    o->dr_scale[p1] += fabs(mj * (di / dj) * temp1);
+  }
+  o->a_scale[p1] += fabs(mj) * tn;
+  omp_unset_lock(&o->locks[p1]);
+  omp_set_lock(&o->locks[p2]);
+  for (int d = 0; d < 3; ++d) o->a[3 * p2 + d] -= mi * temp[d];
+  if (!fluid1) {
+    o->ddensity[p2] += mi * (dj / di) * temp1;
+    if (o->t0[p2] > 0.0 || o->les[p2]) {
+      double c = mi / di;
+      for (int e = 0; e < 9; ++e) o->strain_rate[9 * p2 + e] = o->strain_rate[9 * p2 + e] + SR[e] * c;
+    }
+    o->dr_scale[p2] += fabs(mi * (dj / di) * temp1);
+  }
+  o->a_scale[p2] += fabs(mi) * tn;
+  omp_unset_lock(&o->locks[p2]);
+  return 1;
+}
+
 /* Seepage (Source/Functions.cpp:266-298): Darcy (0, 1) or Forchheimer (2, 3)
  * coefficients of the drag between pore fluid and soil skeleton */
 static void Seepage(int ST, double k, double k2, double mu, double rho, double* SF1, double* SF2) {
@@ -1085,8 +1219,7 @@ static int last_compute(psph_oracle* o, int nthr) {
   for (int k = 0; k < o->nthr; ++k)
     for (int64_t i = 0; i < o->nsm[k].n; i++) {
       const int prod = o->material[o->nsm[k].v[2 * i]] * o->material[o->nsm[k].v[2 * i + 1]];
-      if (prod == 2) return fail(o, PSPH_ERR_UNSUPPORTED, "fluid-solid interaction (CalcForce12, FSI) is outside this build");
-      if (prod != 3) return fail(o, PSPH_ERR_INVALID_ARGUMENT, "Out of Interaction types");
+      if (prod != 2 && prod != 3) return fail(o, PSPH_ERR_INVALID_ARGUMENT, "Out of Interaction types");
     }
   int64_t evaluated = 0;
 #pragma omp parallel for schedule(static) num_threads(nthr) reduction(+ : evaluated)
@@ -1102,7 +1235,10 @@ static int last_compute(psph_oracle* o, int nthr) {
   }
 #pragma omp parallel for schedule(static) num_threads(nthr) reduction(+ : evaluated)
   for (int k = 0; k < o->nthr; k++)
-    for (int64_t i = 0; i < o->nsm[k].n; i++) evaluated += calc_force13(o, o->nsm[k].v[2 * i], o->nsm[k].v[2 * i + 1]);
+    for (int64_t i = 0; i < o->nsm[k].n; i++) {
+      int64_t p1 = o->nsm[k].v[2 * i], p2 = o->nsm[k].v[2 * i + 1];
+      evaluated += (o->material[p1] * o->material[p2] == 3) ? calc_force13(o, p1, p2) : calc_force12(o, p1, p2);
+    }
   o->pairs_done += evaluated;
   double dtmin = o->it.deltatint;
   const double sha = o->cfg.sqrt_h_a;
@@ -1597,6 +1733,10 @@ psph_oracle* psph_oracle_create(const psph_config* cfg, const psph_particles* p,
   if (!p->volume)
     for (int64_t i = 0; i < n; ++i) o->volume[i] = o->mass[i] / o->ref_density[i];
   o->satcheck = (int32_t*)calloc((size_t)(n ? n : 1), sizeof(int32_t));
+  o->fsi_p = (double*)calloc((size_t)(n ? n : 1), sizeof(double));
+  o->fsi_sk = (double*)calloc((size_t)(n ? n : 1), sizeof(double));
+  o->fsi_nsv = (double*)calloc((size_t)(n ? n : 1) * 3, sizeof(double));
+  o->fsi_cnt = (int32_t*)calloc((size_t)(n ? n : 1), sizeof(int32_t));
   o->orig = (int64_t*)malloc((size_t)(n ? n : 1) * sizeof(int64_t));
   for (int64_t i = 0; i < n; ++i) o->orig[i] = i;
   o->LL = (int32_t*)malloc((size_t)(n ? n : 1) * sizeof(int32_t));
@@ -1664,6 +1804,10 @@ void psph_oracle_destroy(psph_oracle* o) {
   free(o->CC);
   free(o->HOC);
   free(o->satcheck);
+  free(o->fsi_p);
+  free(o->fsi_sk);
+  free(o->fsi_nsv);
+  free(o->fsi_cnt);
   free(o->fixed);
   free(o->a_scale);
   free(o->dr_scale);

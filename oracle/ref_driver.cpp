@@ -100,6 +100,7 @@ static int load_state(SPH::Domain& dom, const char* dir) {
     if (v[0] != 0.0 || v[1] != 0.0 || v[2] != 0.0) dom.GeneralBefore = &BodyForceHook;
   }
   dom.SWIType = (size_t)psph_io_cfg1(dir, "swi_type", 0);
+  dom.FSI = psph_io_cfg1(dir, "fsi", 0) != 0.0;
   dom.MuMax = 0.0;  // left uninitialised by the Domain constructor
   dom.CsMax = 0.0;
 

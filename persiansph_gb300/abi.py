@@ -47,7 +47,8 @@ class PsphConfig(C.Structure):
         ("swi_type", C.c_int32), ("shepard_step", C.c_int32), ("precision", C.c_int32),
         ("wall_pressure_mode", C.c_int32), ("gravity", C.c_double * 3), ("body_force", C.c_double * 3),
         ("xsph", C.c_double), ("sqrt_h_a", C.c_double), ("R", C.c_double), ("dom_max", C.c_double * 3),
-        ("dom_min", C.c_double * 3), ("dt", C.c_double), ("time", C.c_double), ("reserved", C.c_int32 * 8),
+        ("dom_min", C.c_double * 3), ("dt", C.c_double), ("time", C.c_double), ("fsi", C.c_int32),
+        ("reserved", C.c_int32 * 7),
     ]
 
 

@@ -288,11 +288,12 @@ void enqueue_step(psph_ctx* c, F&& before_update) {
   record_phase(c, 2);
   if (v.o.fp32) launch_prepare32(v, st);
   else launch_prepare(v, st);
-  if (v.o.mixed && v.o.swi != 2) launch_saturation(v, st);
+  if (v.o.couple_soil && v.o.swi != 2) launch_saturation(v, st);
+  if (v.o.fsi) launch_fsi(v, st);
   record_phase(c, 3);
   if (v.o.fp32) launch_forces32(v, st);
   else launch_forces(v, st);
-  if (v.o.mixed) launch_seepage(v, st);
+  if (v.o.mixed) launch_coupling(v, st);
   record_phase(c, 4);
   if (v.o.closure) launch_closure(v, st);
   record_phase(c, 5);
@@ -375,7 +376,7 @@ psph_status create_impl(const psph_config* cfgs, int ninst, psph_ctx** out) {
     if (k.precision != PSPH_FP64 && k.precision != PSPH_FP32C)
       return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "precision must be PSPH_FP64 or PSPH_FP32C");
     if (k.dimension == 2 && k.periodic[2]) return set_err(c, PSPH_ERR_UNSUPPORTED, "periodic z in 2D");
-    for (int e = 0; e < 8; ++e)
+    for (int e = 0; e < 7; ++e)
       if (k.reserved[e]) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "reserved fields must be zero");
     // one set of kernels serves all instances: the physics switches must agree
     const psph_config& a = cfgs[0];
@@ -598,16 +599,19 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
       for (int64_t g = g0; g < g1; ++g) cls[g] = remap[cls[g]];
     }
   }
-  // Materials that share a domain: fluid with soil couples through CalcForce13;
-  // a solid (Material 2) with anything else needs CalcForce12 (FSI)
-  const bool mixed = materials == ((1 << 1) | (1 << 3));
+  // Materials that share a domain: fluid with soil couples through
+  // CalcForce13, fluid with a solid through CalcForce12; a solid with a soil
+  // has no pair force in the reference (LastComputeAcceleration aborts on it)
+  const bool fluid_soil = materials == ((1 << 1) | (1 << 3));
+  const bool fluid_solid = materials == ((1 << 1) | (1 << 2));
+  const bool mixed = fluid_soil || fluid_solid;
   if (!mixed && (materials & (materials - 1)))
     return set_err(c, PSPH_ERR_UNSUPPORTED,
-                   "solid particles (Material 2) share the domain with another material: fluid-solid interaction "
-                   "(CalcForce12, FSI) is outside this build");
-  if (mixed) {
-    if (k.precision != PSPH_FP64)
-      return set_err(c, PSPH_ERR_UNSUPPORTED, "fluid-soil domains run in the FP64 form (PSPH_FP64)");
+                   "solid (Material 2) and soil (Material 3) particles share the domain: the reference has no pair "
+                   "force for them");
+  if (mixed && k.precision != PSPH_FP64)
+    return set_err(c, PSPH_ERR_UNSUPPORTED, "domains of two materials run in the FP64 form (PSPH_FP64)");
+  if (fluid_soil) {
     for (int q = 0; q < ninst; ++q)
       if (c->cfgs[q].periodic[1])
         return set_err(c, PSPH_ERR_UNSUPPORTED, "fluid-soil domains with a periodic y axis");
@@ -706,6 +710,9 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
   o.wallp_physical = (k.wall_pressure_mode == PSPH_WALLP_PHYSICAL);
   o.has_solid = (materials & ((1 << 2) | (1 << 3))) != 0;
   o.mixed = mixed;
+  o.couple_soil = fluid_soil;
+  o.couple_solid = fluid_solid;
+  o.fsi = fluid_solid && k.fsi != 0;
   o.swi = k.swi_type;
   o.fp32 = (k.precision == PSPH_FP32C);
   if (ntot >= (1LL << 26)) return set_err(c, PSPH_ERR_UNSUPPORTED, "this build handles fewer than 2^26 particles");
@@ -744,6 +751,8 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
     }
   }
   if (o.eos_cls < 0) o.eos_cls = 0;
+  // two materials: a wall takes its density from its partner's EOS pair by pair
+  if (mixed) o.uniform_eos = 0;
   // pair constants that are the same for every class: the FP32C fluid pair
   // loop takes them from the launch parameters (the same FP32 values the class
   // table holds, so the results are identical)
@@ -822,8 +831,9 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
       (st = dalloc(c, &S.sumkernel, N)) || (st = dalloc(c, &S.nsv4, N)) || (st = dalloc(c, &S.vxsph4, N)) ||
       (st = dalloc(c, &S.shear_rate, N)) || (st = dalloc(c, &S.sbar, N)))
     return st;
-  if (o.mixed && o.swi == 1 && (st = dalloc(c, &S.s_acc, N))) return st;
-  if (o.mixed && o.swi != 2 && (st = dalloc(c, &S.satcheck, N))) return st;
+  if (o.couple_soil && o.swi == 1 && (st = dalloc(c, &S.s_acc, N))) return st;
+  if (o.couple_soil && o.swi != 2 && (st = dalloc(c, &S.satcheck, N))) return st;
+  if (o.couple_solid && ((st = dalloc(c, &S.fsi_p, N)) || (st = dalloc(c, &S.fsi_nsv, N)))) return st;
   if ((st = dalloc(c, &S.nl, (size_t)o.nl_cap * nl_stride_of(c->ncap)))) return st;
   // FP64 fluids without strain-rate sums, XSPH or solids: each pair evaluated once
   o.fp64_half = !o.fp32 && !o.has_solid && !o.need_sr && o.xsph == 0.0;

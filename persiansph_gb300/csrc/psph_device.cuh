@@ -59,6 +59,8 @@ struct Scratch {
   double* zwab;
   double* s_acc;         // SWIType 1: Particle::S, the surface-erosion velocity derivative
   uint8_t* satcheck;     // fluid-soil: Particle::SatCheck of this step
+  double* fsi_p;         // fluid-solid: Particle::FSIPressure of this step (0 without FSI)
+  double4_32a* fsi_nsv;  // fluid-solid: Particle::FSINSv of this step
   double* sumden;
   double* sumkernel;
   double4_32a* nsv4;     // wall no-slip velocity
@@ -92,8 +94,12 @@ struct Options {
   int eos_cls;        // that class
   int dyn_mu;
   int soil_pairs;     // Material 3 (soil-soil walls take the partner's density)
-  int mixed;          // fluid (Material 1) and soil (Material 3) share the domain: each pair
-                      // kernel keeps to its material, CalcForce13 couples them (FP64 form)
+  int mixed;          // fluid (Material 1) and a soil or a solid share the domain: each pair
+                      // kernel keeps to its material, a coupling kernel adds the pairs of
+                      // different materials (FP64 form)
+  int couple_soil;    // fluid + soil: CalcForce13, the saturation switch
+  int couple_solid;   // fluid + solid: CalcForce12
+  int fsi;            // Domain::FSI: the solid's interpolated pressure and velocity
   int swi;            // Domain::SWIType
   int carry_shear_h;  // the sort moves the ShearStress history (Mat2, or a non-zero upload)
   int uniform_h;      // every particle has the same h
@@ -161,7 +167,8 @@ void launch_expand_sr32(const DevView& v, int n, cudaStream_t st);  // sr32 -> t
 void launch_wall(const DevView& v, cudaStream_t st);      // wall interpolation
 void launch_forces(const DevView& v, cudaStream_t st);    // pair forces + per-block dt minimum
 void launch_saturation(const DevView& v, cudaStream_t st); // fluid-soil: saturation check and weight switch
-void launch_seepage(const DevView& v, cudaStream_t st);   // fluid-soil pair forces (CalcForce13) + dt minimum
+void launch_fsi(const DevView& v, cudaStream_t st);       // fluid-solid: FSI interpolation of the solid
+void launch_coupling(const DevView& v, cudaStream_t st);  // pairs of different materials (CalcForce12/13) + dt
 void launch_dt(const DevView& v, cudaStream_t st);        // dt reduction + AdaptiveTimeStep
 void launch_update(const DevView& v, cudaStream_t st);    // Move + material update + periodic wrap + leave
 void launch_begin(const DevView& v, cudaStream_t st);     // stop test, first-step counters

@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
   int cell = -1, ci_cls = 0;
   if (i < n) {
     ci_cls = P.cls[i];
-    // a fluid-soil domain runs this kernel for its fluid particles only
+    // a domain of two materials runs this kernel for its fluid particles only
     const bool run = !v.inst[CT[ci_cls].inst].stop && (!o.mixed || CT[ci_cls].material == 1);
     active = run && CT[ci_cls].is_free;
     cell = v.S.cellid[i];
@@ -372,7 +372,7 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
       const int j = HALF ? (qe & kIndexMask) : qe;
       const double4_32a xj = P.X4[j];
       const PClass& Cj = CT[P.cls[j]];
-      if (!HALF && o.mixed && Cj.material != 1) continue;  // soil partners: CalcForce13
+      if (!HALF && o.mixed && Cj.material != 1) continue;  // soil or solid partners: the coupling kernel
       // shared pair: both free, both lists in use; evaluates_pair picks the
       // side (the queue holds only those this side evaluates)
       const bool share = own_list && Cj.is_free && v.S.nl_count[j] >= 0;
@@ -544,7 +544,7 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
     const double cand = o.sqrt_h_a * sqrt(hi / an);
     if (cand < dtc) dtc = cand;  // NaN never compares less, as in the reference
   }
-  // fluid-soil: the dt bound waits for the CalcForce13 terms (seepage kernel)
+  // two materials: the dt bound waits for the coupling kernel's terms
   block_dt_and_pairs<kFT>(v, Ci.inst, active && !o.mixed, dtc, npair2, red, cred);
 }
 
@@ -631,8 +631,8 @@ __global__ void __launch_bounds__(kFT) forces_solid_kernel(DevView v) {
   int cell = -1, ci_cls = 0;
   if (i < n) {
     ci_cls = P.cls[i];
-    // a fluid-soil domain runs this kernel for its soil particles only
-    const bool run = !v.inst[CT[ci_cls].inst].stop && (!o.mixed || CT[ci_cls].material == 3);
+    // a domain of two materials runs this kernel for its soil or solid particles only
+    const bool run = !v.inst[CT[ci_cls].inst].stop && (!o.mixed || CT[ci_cls].material != 1);
     active = run && CT[ci_cls].is_free;
     cell = v.S.cellid[i];
     if (run && !active) {
@@ -681,7 +681,7 @@ __global__ void __launch_bounds__(kFT) forces_solid_kernel(DevView v) {
       const int j = qbuf[k][tid];
       const double4_32a xj = P.X4[j];
       const PClass& Cj = CT[P.cls[j]];
-      if (o.mixed && Cj.material != 3) continue;  // fluid partners: CalcForce13
+      if (o.mixed && Cj.material != Ci.material) continue;  // fluid partners: the coupling kernel
       const double hb = (hi + Cj.h) / 2;
       double x0 = xi.x - xj.x, x1 = xi.y - xj.y, x2 = xi.z - xj.z;
       if (any_periodic) periodic_fix(g, x0, x1, x2, hb, cci, decode(g, v.S.cellid[j]));
@@ -979,16 +979,164 @@ PSPH_D void seepage_coeffs(int type, double k, double k2, double mu, double rho,
   sf2 = (type >= 2) ? k2 * rho : 0.0;
 }
 
-// CalcForce13 (Source/Interaction.cpp:508-653) from the side of free particle
-// i, for its partners of the other material, added to the acceleration its own
-// material's pair kernel wrote; then the dt bound and the finiteness check of
-// the gather form. Both orientations of the reference give the same terms:
-// v = v_fluid - v_soil, SFt = (SF1 v + SF2 |v| v) K with K = W(r/h, h) /
-// (Density_1 Density_2) and h the smaller smoothing length; the soil gains
-// m_fluid SFt (SWIType 2: minus m_fluid p_fluid GK x_soil,fluid), the fluid
-// loses m_soil SFt.
+// CalcForce13 (Source/Interaction.cpp:508-653) seen from particle i, whose
+// partner j is of the other material; returns the acceleration term. Both of
+// the reference's orientations give the same terms: v = v_fluid - v_soil,
+// SFt = (SF1 v + SF2 |v| v) K with K = W(r/h, h) / (Density_1 Density_2) and h
+// the smaller smoothing length; the soil gains m_fluid SFt (SWIType 2: minus
+// m_fluid p_fluid GK x_soil,fluid), the fluid loses m_soil SFt.
 template <int DIM, int KT>
-__global__ void __launch_bounds__(kFT) seepage_kernel(DevView v) {
+PSPH_D void seepage_pair(const DevView& v, const Persist& P, const InstState& Is, int i, int j, const PClass& Ci,
+                         const PClass& Cj, const double4_32a& xi, const double4_32a& xj, const double4_32a& vi,
+                         double h, double x0, double x1, double x2, double r, double q, double* da) {
+  const int swi = v.o.swi;
+  da[0] = da[1] = da[2] = 0.0;
+  if (swi == 3) return;
+  const bool soil_i = (Ci.material == 3);
+  const double inv_h = 1.0 / h, ih2 = inv_h * inv_h;
+  const double cwh = Kern<DIM, KT>::cw() * (DIM == 2 ? ih2 : ih2 * inv_h);
+  const double rr = xi.w * xj.w;
+  const double K = Kern<DIM, KT>::W(q, cwh) / rr;
+  // soil side s, fluid side f
+  const int s = soil_i ? i : j, f = soil_i ? j : i;
+  const PClass& Cs = soil_i ? Ci : Cj;
+  const PClass& Cf = soil_i ? Cj : Ci;
+  const double4_32a vs = soil_i ? vi : P.V4[j];
+  const double4_32a vf = soil_i ? P.V4[j] : vi;
+  const double w0 = vf.x - vs.x, w1 = vf.y - vs.y, w2 = vf.z - vs.z;
+  const double nv = sqrt(w0 * w0 + w1 * w1 + w2 * w2);
+  double S0, S1, S2;
+  bool erosion = false;
+  if (swi == 1) {
+    // a fixed soil particle's ZWab is 1 once CalcForce2233 saw it, else 0
+    const double zw = Cs.is_free ? v.S.zwab[s] : (v.S.sumkernel[s] != 0.0 ? 1.0 : 0.0);
+    erosion = zw < 0.25;
+  }
+  if (erosion) {  // Source/Interaction.cpp:561-566
+    const double Cd = 24.0 * (Cf.mu_ref / Cf.rho0) / (Cs.dgrain * nv + 0.01 * h * h) + 2.0;
+    const double c = 3.0 / (4.0 * Cs.dgrain) * Cf.rho0 * (1.0 - Cs.n0) * Cd * nv;
+    S0 = c * w0 * K;
+    S1 = c * w1 * K;
+    S2 = c * w2 * K;
+    S1 += (Cf.rho0 * (1.0 - Cs.n0) * nv * fabs(v.S.s_acc[f] - v.S.s_acc[s])) * K;
+  } else {
+    double kp = Cs.kp, kp2 = Cs.kp2;
+    if (Cs.var_por && Cs.is_free && !Is.k_initial) {
+      // VarPorosity: the permeabilities of the strain the last update left
+      const double* E = P.strain + 9 * (size_t)s;
+      const double ev = (E[0] + E[4] + E[8]);
+      permeability(Cs.seep_type, (Cs.n0 + ev) / (1.0 + ev), Cs.dgrain, &kp, &kp2);
+    }
+    double sf1, sf2;
+    seepage_coeffs(Cs.seep_type, kp, kp2, Cf.mu_ref, Cf.rho0, sf1, sf2);
+    S0 = (sf1 * w0 + sf2 * nv * w0) * K;
+    S1 = (sf1 * w1 + sf2 * nv * w1) * K;
+    S2 = (sf1 * w2 + sf2 * nv * w2) * K;
+  }
+  if (DIM == 2) S2 = 0.0;
+  if (soil_i) {
+    const double mf = Cf.mass;
+    da[0] = mf * S0;
+    da[1] = mf * S1;
+    da[2] = mf * S2;
+    if (swi == 2) {  // pore pressure (Source/Interaction.cpp:608-637), x = x_soil - x_fluid
+      const double GK = Kern<DIM, KT>::GK(q, h / r, cwh * ih2) / rr;
+      const double c = mf * P.V4[j].w * GK;
+      da[0] = da[0] - c * x0;
+      da[1] = da[1] - c * x1;
+      da[2] = da[2] - c * x2;
+    }
+  } else {
+    const double ms = Cs.mass;
+    da[0] = -(ms * S0);
+    da[1] = -(ms * S1);
+    da[2] = -(ms * S2);
+  }
+}
+
+// CalcForce12 (Source/Interaction.cpp:379-507) seen from particle i, whose
+// partner j is of the other material (fluid f, solid s; h the mean smoothing
+// length). The solid enters with the density its FSIPressure gives under the
+// fluid's EOS and the no-slip velocity 2 v_s - FSINSv; both sides take the
+// fluid's mass; the reference's artificial-viscosity branch is dead (Alpha and
+// Beta are zeroed before their test). The solid gains m_f temp, the fluid too
+// (temp from each side's own orientation), and only the fluid gets the density
+// rate and, with T0 or LES, the strain rate (added into sr).
+template <int DIM, int KT>
+PSPH_D void solid_pair(const DevView& v, const Persist& P, int i, int j, const PClass& Ci, const PClass& Cj,
+                       const double4_32a& xi, const double4_32a& xj, const double4_32a& vi, double hb, double x0,
+                       double x1, double x2, double r2, double q, double* da, double* drho, double* sr) {
+  const Options& o = v.o;
+  const bool fluid_i = (Ci.material == 1);
+  const PClass& Cf = fluid_i ? Ci : Cj;
+  const PClass& Cs = fluid_i ? Cj : Ci;
+  const int s = fluid_i ? j : i, f = fluid_i ? i : j;
+  const double4_32a vj = P.V4[j];
+  const double rho_f = fluid_i ? xi.w : xj.w;
+  const double p_f = fluid_i ? vi.w : vj.w;
+  const double fp = v.S.fsi_p[s];
+  const double rho_s = density_solid(Cf.pres_eq, Cf.cs, Cf.p0, fp, Cf.rho0);
+  const double mf = Cf.mass;
+  const double mu = o.dyn_mu ? P.mu[f] : Cf.mu0;
+  const double4_32a ns = v.S.fsi_nsv[s];
+  const double4_32a vs = fluid_i ? vj : vi, vf = fluid_i ? vi : vj;
+  // vab from i's orientation
+  const double sg = fluid_i ? 1.0 : -1.0;
+  const double vab0 = sg * (vf.x - (2.0 * vs.x - ns.x)), vab1 = sg * (vf.y - (2.0 * vs.y - ns.y)),
+               vab2 = sg * (vf.z - (2.0 * vs.z - ns.z));
+  const double v0 = vi.x - vj.x, v1 = vi.y - vj.y, v2 = vi.z - vj.z;
+  const double inv_hb = 1.0 / hb, ih2 = inv_hb * inv_hb;
+  const double cwh = Kern<DIM, KT>::cw() * (DIM == 2 ? ih2 : ih2 * inv_hb);
+  const double cwg = cwh * ih2;
+  const double inv_r = (r2 > 0.0) ? rsqrt(r2) : 0.0;
+  const double inv_q = hb * inv_r;
+  const double GK = Kern<DIM, KT>::GK(q, inv_q, cwg);
+  const double di = fluid_i ? rho_f : rho_s, dj = fluid_i ? rho_s : rho_f;
+  double VI0, VI1, VI2;
+  if (o.vis_eq <= 2) {
+    double c;
+    if (o.vis_eq == 0) c = 2.0 * mu / (di * dj) * GK;
+    else if (o.vis_eq == 1) c = 8.0 * mu / ((di + dj) * (di + dj)) * GK;
+    else c = -mu / (di * dj) * Kern<DIM, KT>::Lap(q, inv_q, cwg);
+    VI0 = c * vab0; VI1 = c * vab1; VI2 = c * vab2;
+  } else {
+    const double L = Kern<DIM, KT>::Lap(q, inv_q, cwg);
+    const double S2 = Kern<DIM, KT>::D2(q, cwg);
+    const double sv = -mu / (di * dj);
+    const double vx = v0 * x0 + v1 * x1 + v2 * x2;
+    const double t = vx / r2 * (-GK + S2);
+    VI0 = sv * (L * vab0 + (1.0 / 3.0) * (GK * v0 + t * x0));
+    VI1 = sv * (L * vab1 + (1.0 / 3.0) * (GK * v1 + t * x1));
+    VI2 = sv * (L * vab2 + (1.0 / 3.0) * (GK * v2 + t * x2));
+  }
+  double sp;
+  if (o.grad_type == 0) sp = -(p_f / (rho_f * rho_f) + fp / (rho_s * rho_s)) * GK;
+  else sp = -((p_f + fp) / (rho_f * rho_s)) * GK;
+  da[0] = mf * (sp * x0 + VI0);
+  da[1] = mf * (sp * x1 + VI1);
+  da[2] = DIM == 3 ? mf * (sp * x2 + VI2) : 0.0;
+  *drho = 0.0;
+  if (fluid_i) {
+    *drho = mf * (rho_f / rho_s) * (GK * (v0 * x0 + v1 * x1 + v2 * x2));
+    if (sr && (Cf.t0 > 0.0 || Cf.les) &&
+        ((Ci.t0 > 0.0 || Cj.t0 > 0.0) || (Ci.les || Cj.les))) {
+      const double c2 = -GK * (mf / rho_s);
+      sr[0] += c2 * (2.0 * vab0 * x0);
+      sr[1] += c2 * (vab0 * x1 + vab1 * x0);
+      sr[2] += c2 * (vab0 * x2 + vab2 * x0);
+      sr[3] += c2 * (2.0 * vab1 * x1);
+      sr[4] += c2 * (vab1 * x2 + vab2 * x1);
+      sr[5] += c2 * (2.0 * vab2 * x2);
+    }
+  }
+}
+
+// The pairs of different materials from the side of free particle i, added in
+// list order to what its own material's pair kernel wrote (CalcForce13 for
+// fluid and soil, CalcForce12 for fluid and solid); then the dt bound and the
+// finiteness check of the gather form.
+template <int DIM, int KT>
+__global__ void __launch_bounds__(kFT) coupling_kernel(DevView v) {
   __shared__ double red[kFT / 32];
   __shared__ unsigned long long cred[kFT / 32];
   const StepScalars* sc = v.sc;
@@ -1009,95 +1157,52 @@ __global__ void __launch_bounds__(kFT) seepage_kernel(DevView v) {
   const PClass& Ci = CT[ci_cls];
   const GridDev& g = grid_of(v, Ci.inst);
   const InstState& Is = v.inst[Ci.inst];
-  const bool soil_i = (Ci.material == 3);
-  const int swi = o.swi;
   double4_32a a4 = active ? v.S.A4[i] : make_double4_32a(0, 0, 0, 0);
-  double ax = a4.x, ay = a4.y, az = a4.z;
+  double ax = a4.x, ay = a4.y, az = a4.z, drho = a4.w;
   if (active && cell >= 0) {
     const double4_32a xi = P.X4[i], vi = P.V4[i];
     const CellCoord cci = decode(g, cell);
     const bool any_periodic = g.periodic[0] | g.periodic[1] | g.periodic[2];
+    // the fluid's strain-rate sums gain CalcForce12's terms
+    const bool want_sr = o.couple_solid && o.need_sr && Ci.material == 1 && (Ci.t0 > 0.0 || Ci.les);
+    double sr[6] = {0, 0, 0, 0, 0, 0};
     NbrSource<DIM> src;
     src.init(v, g, i, true, 1.004f);
     while (true) {
       int code;
       const int j = src.next(v, &code);
       if (j < 0) break;
-      const int cj_cls = P.cls[j];
-      const PClass& Cj = CT[cj_cls];
+      const PClass& Cj = CT[P.cls[j]];
       if (Cj.material == Ci.material) continue;
-      const double h = Ci.h < Cj.h ? Ci.h : Cj.h;
+      // CalcForce13 takes the smaller smoothing length, CalcForce12 the mean
+      const double h = o.couple_soil ? (Ci.h < Cj.h ? Ci.h : Cj.h) : (Ci.h + Cj.h) / 2;
       const double4_32a xj = P.X4[j];
       double x0 = xi.x - xj.x, x1 = xi.y - xj.y, x2 = xi.z - xj.z;
       if (any_periodic) periodic_fix(g, x0, x1, x2, h, cci, decode(g, v.S.cellid[j]));
-      const double r = sqrt(x0 * x0 + x1 * x1 + x2 * x2);
+      const double r2 = x0 * x0 + x1 * x1 + x2 * x2;
+      const double r = sqrt(r2);
       const double q = r / h;
       if (!(q <= g.cellfac)) continue;
       npair2 += Cj.is_free ? 1ull : 2ull;
-      if (swi == 3) continue;
-      const double inv_h = 1.0 / h, ih2 = inv_h * inv_h;
-      const double cwh = Kern<DIM, KT>::cw() * (DIM == 2 ? ih2 : ih2 * inv_h);
-      const double rr = xi.w * xj.w;
-      const double K = Kern<DIM, KT>::W(q, cwh) / rr;
-      // soil side S, fluid side F
-      const int s = soil_i ? i : j, f = soil_i ? j : i;
-      const PClass& Cs = soil_i ? Ci : Cj;
-      const PClass& Cf = soil_i ? Cj : Ci;
-      const double4_32a vs = soil_i ? vi : P.V4[j];
-      const double4_32a vf = soil_i ? P.V4[j] : vi;
-      const double w0 = vf.x - vs.x, w1 = vf.y - vs.y, w2 = vf.z - vs.z;
-      const double nv = sqrt(w0 * w0 + w1 * w1 + w2 * w2);
-      double S0, S1, S2;
-      bool erosion = false;
-      if (swi == 1) {
-        // a fixed soil particle's ZWab is 1 once CalcForce2233 saw it, else 0
-        const double zw = Cs.is_free ? v.S.zwab[s] : (v.S.sumkernel[s] != 0.0 ? 1.0 : 0.0);
-        erosion = zw < 0.25;
-      }
-      if (erosion) {  // Source/Interaction.cpp:561-566
-        const double Cd = 24.0 * (Cf.mu_ref / Cf.rho0) / (Cs.dgrain * nv + 0.01 * h * h) + 2.0;
-        const double c = 3.0 / (4.0 * Cs.dgrain) * Cf.rho0 * (1.0 - Cs.n0) * Cd * nv;
-        S0 = c * w0 * K;
-        S1 = c * w1 * K;
-        S2 = c * w2 * K;
-        S1 += (Cf.rho0 * (1.0 - Cs.n0) * nv * fabs(v.S.s_acc[f] - v.S.s_acc[s])) * K;
+      double da[3], dr = 0.0;
+      if (o.couple_soil) {
+        seepage_pair<DIM, KT>(v, P, Is, i, j, Ci, Cj, xi, xj, vi, h, x0, x1, x2, r, q, da);
       } else {
-        double kp = Cs.kp, kp2 = Cs.kp2;
-        if (Cs.var_por && Cs.is_free && !Is.k_initial) {
-          // VarPorosity: the permeabilities of the strain the last update left
-          const double* E = P.strain + 9 * (size_t)s;
-          const double ev = (E[0] + E[4] + E[8]);
-          permeability(Cs.seep_type, (Cs.n0 + ev) / (1.0 + ev), Cs.dgrain, &kp, &kp2);
-        }
-        double sf1, sf2;
-        seepage_coeffs(Cs.seep_type, kp, kp2, Cf.mu_ref, Cf.rho0, sf1, sf2);
-        S0 = (sf1 * w0 + sf2 * nv * w0) * K;
-        S1 = (sf1 * w1 + sf2 * nv * w1) * K;
-        S2 = (sf1 * w2 + sf2 * nv * w2) * K;
+        solid_pair<DIM, KT>(v, P, i, j, Ci, Cj, xi, xj, vi, h, x0, x1, x2, r2, q, da, &dr, want_sr ? sr : nullptr);
       }
-      if (DIM == 2) S2 = 0.0;
-      if (soil_i) {
-        const double mf = Cf.mass;
-        double a0 = mf * S0, a1 = mf * S1, a2 = mf * S2;
-        if (swi == 2) {  // pore pressure (Source/Interaction.cpp:608-637), x = x_soil - x_fluid
-          const double GK = Kern<DIM, KT>::GK(q, h / r, cwh * ih2) / rr;
-          const double c = mf * P.V4[j].w * GK;
-          a0 = a0 - c * x0;
-          a1 = a1 - c * x1;
-          a2 = a2 - c * x2;
-        }
-        ax += a0;
-        ay += a1;
-        az += a2;
-      } else {
-        const double ms = Cs.mass;
-        ax -= ms * S0;
-        ay -= ms * S1;
-        az -= ms * S2;
-      }
+      ax += da[0];
+      ay += da[1];
+      az += da[2];
+      drho += dr;
     }
-    v.S.A4[i] = make_double4_32a(ax, ay, az, a4.w);
-    if (!(isfinite(ax) && isfinite(ay) && isfinite(az) && isfinite(a4.w))) atomicOr(&v.sc->status, ST_NONFINITE);
+    v.S.A4[i] = make_double4_32a(ax, ay, az, drho);
+    if (want_sr) {
+      double* out = v.S.strain_rate + 9 * (size_t)i;
+      out[0] += sr[0]; out[1] += sr[1]; out[2] += sr[2];
+      out[3] += sr[1]; out[4] += sr[3]; out[5] += sr[4];
+      out[6] += sr[2]; out[7] += sr[4]; out[8] += sr[5];
+    }
+    if (!(isfinite(ax) && isfinite(ay) && isfinite(az) && isfinite(drho))) atomicOr(&v.sc->status, ST_NONFINITE);
     const double an = sqrt(ax * ax + ay * ay + az * az);
     const double cand = o.sqrt_h_a * sqrt(Ci.h / an);
     if (cand < dtc) dtc = cand;
@@ -1107,6 +1212,67 @@ __global__ void __launch_bounds__(kFT) seepage_kernel(DevView v) {
     if (cand < dtc) dtc = cand;
   }
   block_dt_and_pairs<kFT>(v, Ci.inst, active, dtc, npair2, red, cred);
+}
+
+// FSI interpolation (Source/Domain.cpp:1090-1160): a free solid particle takes
+// FSIPressure = sum(p_f K + (g.x) rho_f K) and FSINSv = sum(v_f K) over its free
+// fluid candidates (K = 0 outside the support), divided by the kernel sum once
+// per candidate, as the reference's normalisation loop runs once per entry of
+// FreeFSIParticles (one entry per pair; with Nproc = 1). As in the reference,
+// the gravity term's x is x_first - x_second of MainNeighbourSearch's pair, and
+// only pairs that list the solid first add to FSINSv (the others add to the
+// solid's NSv, which nothing reads for a free particle). Fixed solids get 0.
+template <int DIM, int KT>
+__global__ void __launch_bounds__(kFT) fsi_kernel(DevView v) {
+  if (v.sc->all_stop) return;
+  const Persist& P = cur_persist(v);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= v.sc->n) return;
+  const PClass* __restrict__ CT = v.cls;
+  const PClass& Ci = CT[P.cls[i]];
+  const int cell = v.S.cellid[i];
+  if (Ci.material != 2 || v.inst[Ci.inst].stop) return;
+  double sk = 0.0, sp = 0.0, n0 = 0.0, n1 = 0.0, n2 = 0.0;
+  int cnt = 0;
+  if (Ci.is_free && cell >= 0) {
+    const GridDev& g = grid_of(v, Ci.inst);
+    const CellCoord ci = decode(g, cell);
+    const double4_32a xi = P.X4[i];
+    const int oi = P.orig[i];
+    const double gx = v.o.gravity[0], gy = v.o.gravity[1], gz = v.o.gravity[2];
+    const bool any_periodic = g.periodic[0] | g.periodic[1] | g.periodic[2];
+    for_neighbor_ranges<DIM>(g, ci, v.S.start, [&](int lo, int hi) {
+      for (int j = lo; j < hi; ++j) {
+        const PClass& Cj = CT[P.cls[j]];
+        if (Cj.material != 1 || !Cj.is_free) continue;
+        const CellCoord cj = decode(g, v.S.cellid[j]);
+        const bool solid_first = first_of_pair(g, ci, cj, oi, P.orig[j]);
+        const double4_32a xj = P.X4[j], vj = P.V4[j];
+        const double hb = (Ci.h + Cj.h) / 2.0;
+        double x0, x1, x2;
+        if (solid_first) {
+          x0 = xi.x - xj.x; x1 = xi.y - xj.y; x2 = xi.z - xj.z;
+          if (any_periodic) periodic_fix(g, x0, x1, x2, hb, ci, cj);
+        } else {
+          x0 = xj.x - xi.x; x1 = xj.y - xi.y; x2 = xj.z - xi.z;
+          if (any_periodic) periodic_fix(g, x0, x1, x2, hb, cj, ci);
+        }
+        const double inv_hb = 1.0 / hb, ih2 = inv_hb * inv_hb;
+        const double K = Kern<DIM, KT>::W(sqrt(x0 * x0 + x1 * x1 + x2 * x2) * inv_hb,
+                                          Kern<DIM, KT>::cw() * (DIM == 2 ? ih2 : ih2 * inv_hb));
+        ++cnt;
+        sk += K;
+        if (solid_first) { n0 += vj.x * K; n1 += vj.y * K; n2 += vj.z * K; }
+        sp += vj.w * K + (gx * x0 + gy * x1 + gz * x2) * xj.w * K;
+      }
+    });
+    for (int c = 0; c < cnt; ++c) {
+      sp = sp / sk;
+      n0 = n0 / sk; n1 = n1 / sk; n2 = n2 / sk;
+    }
+  }
+  v.S.fsi_p[i] = sp;
+  v.S.fsi_nsv[i] = make_double4_32a(n0, n1, n2, 0.0);
 }
 
 inline int nblk(int n, int bt) { return n <= 0 ? 1 : (n + bt - 1) / bt; }
@@ -1184,22 +1350,35 @@ void launch_saturation(const DevView& v, cudaStream_t st) {
   saturation_apply_kernel<<<nb, kFT, 0, st>>>(v);
 }
 
-void launch_seepage(const DevView& v, cudaStream_t st) {
+template <template <int, int> class Launch>
+void by_dim_kernel(const DevView& v, cudaStream_t st) {
   const int nb = nblk(v.ncap, kFT);
   if (v.o.dim == 2) {
     switch (v.o.kt) {
-      case 0: seepage_kernel<2, 0><<<nb, kFT, 0, st>>>(v); break;
-      case 1: seepage_kernel<2, 1><<<nb, kFT, 0, st>>>(v); break;
-      default: seepage_kernel<2, 2><<<nb, kFT, 0, st>>>(v); break;
+      case 0: Launch<2, 0>::run(v, nb, st); break;
+      case 1: Launch<2, 1>::run(v, nb, st); break;
+      default: Launch<2, 2>::run(v, nb, st); break;
     }
   } else {
     switch (v.o.kt) {
-      case 0: seepage_kernel<3, 0><<<nb, kFT, 0, st>>>(v); break;
-      case 1: seepage_kernel<3, 1><<<nb, kFT, 0, st>>>(v); break;
-      default: seepage_kernel<3, 2><<<nb, kFT, 0, st>>>(v); break;
+      case 0: Launch<3, 0>::run(v, nb, st); break;
+      case 1: Launch<3, 1>::run(v, nb, st); break;
+      default: Launch<3, 2>::run(v, nb, st); break;
     }
   }
 }
+template <int DIM, int KT>
+struct CouplingLaunch {
+  static void run(const DevView& v, int nb, cudaStream_t st) { coupling_kernel<DIM, KT><<<nb, kFT, 0, st>>>(v); }
+};
+template <int DIM, int KT>
+struct FsiLaunch {
+  static void run(const DevView& v, int nb, cudaStream_t st) { fsi_kernel<DIM, KT><<<nb, kFT, 0, st>>>(v); }
+};
+
+void launch_coupling(const DevView& v, cudaStream_t st) { by_dim_kernel<CouplingLaunch>(v, st); }
+
+void launch_fsi(const DevView& v, cudaStream_t st) { by_dim_kernel<FsiLaunch>(v, st); }
 
 void launch_dt(const DevView& v, cudaStream_t st) { dt_finalize_kernel<<<1, 256, 0, st>>>(v); }
 

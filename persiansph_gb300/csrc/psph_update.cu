@@ -425,7 +425,7 @@ void launch_upload_pack(const double* sx, const double* sd, const double* sp, co
 
 int launches_per_step(const DevView& v) {
   return (v.o.fp32 ? 17 : 16) + (v.o.closure ? 1 : 0) + (v.o.has_solid ? 1 : 0) + (v.o.fp64_half ? 1 : 0) +
-         (v.o.mixed ? (v.o.swi != 2 ? 4 : 2) : 0);
+         (v.o.mixed ? 2 : 0) + (v.o.couple_soil && v.o.swi != 2 ? 2 : 0) + (v.o.fsi ? 1 : 0);
 }
 
 }  // namespace psph

@@ -267,8 +267,6 @@ class Domain:
 
     # -- boundary to the C ABI ----------------------------------------------
     def config(self, dt: float) -> PsphConfig:
-        if self.FSI:
-            raise Fatal("fluid-solid interaction (FSI) is outside this build")
         if self.BC.InOutFlow:
             raise Fatal("in/out-flow boundaries are outside this build")
         c = PsphConfig()
@@ -284,6 +282,7 @@ class Domain:
             c.dom_max[d] = float(self.DomMax[d])
             c.dom_min[d] = float(self.DomMin[d])
         c.swi_type = int(self.SWIType)
+        c.fsi = int(bool(self.FSI))
         c.shepard_step = int(self.ShepardStep)
         c.precision = int(self.Precision)
         c.wall_pressure_mode = int(self.WallPressureMode)

@@ -9,6 +9,7 @@ example drivers do, with sizes parameterised so tests can run them small:
   dam_break_3d    3D water column in a tank (4-DamBreak3D.cpp shape)
   granular_column 2D Drucker-Prager soil column (Old_Tests/ReposeAngle2.cpp shape)
   seepage_bed_2d  2D dam break over an erodible soil bed (Old_Tests/Dam_Scouring2.cpp shape)
+  elastic_gate_2d 2D water column behind an elastic gate (Old_Tests/FSI_ElasticGate.cpp shape)
 
 All inputs are synthetic and seeded; the reference ships no datasets.
 """
@@ -429,6 +430,79 @@ def seepage_bed_2d(dx=0.01, L=0.3, H=0.2, Hs=0.1, TL=0.6, wall_layers=3, rho_f=1
     dt = min(0.25 * h / cs_f, 0.2 * h / cs_s)
     return dom, dt, {"h": h, "cs_f": cs_f, "cs_s": cs_s, "n_fluid": int((fluid & ~wall).sum()),
                      "n_soil": int((soil & ~wall).sum()), "n_wall": int(wall.sum())}
+
+
+def elastic_gate_2d(dx=0.01, L1=0.2, H=0.15, Tr=0.03, H1=0.15, TL_extra=0.1, wall_layers=3, rho_f=1000.0,
+                    rho_r=1100.0, K=2.0e7, G=4.27e6, mu=1.0e-3, fsi=False, scheme=0, g=9.81, hfac=1.2, ti=0.3):
+    """2D water column held by an elastic gate, the shape of
+    Old_Tests/FSI_ElasticGate.cpp: water (Material 1) fills x < L1 up to H in a
+    tank; a gate of thickness Tr (Material 2, hypoelastic, PresEq 0, sound
+    speed sqrt(K / rho_r), artificial viscosity alpha 1, tensile-instability
+    correction `ti`) stands at x = L1 from two layers above the floor to H1,
+    clamped by three fixed layers above H1. Fluid and gate meet through
+    CalcForce12; `fsi` turns on the reference's FSI interpolation of the
+    gate's pressure and velocity. Returns (domain, dt, info).
+    """
+    dom = Domain()
+    dom.Dimension = 2
+    dom.Scheme = scheme
+    dom.Kernel_Set(Qubic_Spline)
+    dom.Viscosity_Eq_Set(Morris)
+    dom.Gradient_Approach_Set(Squared_density)
+    dom.Gravity = [0.0, -g, 0.0]
+    dom.FSI = bool(fsi)
+    dom.InitialDist = dx
+    h = hfac * dx
+    cs_w = 10.0 * math.sqrt(2.0 * g * H) * 2.0
+    cs_r = math.sqrt(K / rho_r)
+    TL = L1 + Tr + TL_extra
+    TH = H1 + 4 * dx
+    _tank(dom, dx, TL, TH, 0.0, wall_layers)
+    p = dom.particles
+    x = p.get("x")
+    xb, yb = x[:, 0], x[:, 1]
+    wall = (xb < 0.0) | (yb < 0.0) | (xb > TL)
+    p.keep(wall | ((xb < L1) & (yb < H)))
+    n_tank = p.n
+    dom.AddBoxLength(3, (L1, 0.0, 0.0), Tr + dx / 10.0, H1 + 3.0 * dx + dx / 10.0, 0, dx / 2.0, rho_r, h, 1, 0,
+                     False, False)
+    p = dom.particles
+    x = p.get("x")
+    xb, yb = x[:, 0], x[:, 1]
+    gate = np.zeros(p.n, bool)
+    gate[n_tank:] = True
+    keep = ~gate | (yb >= 2.0 * dx)
+    p.keep(keep)
+    gate = gate[keep]
+    x = p.get("x")
+    xb, yb = x[:, 0], x[:, 1]
+    wall = (~gate) & ((xb < 0.0) | (yb < 0.0) | (xb > TL))
+    clamp = gate & (yb > H1)
+    fixed = wall | clamp
+    water = ~gate & ~wall
+    p.set("h", h)
+    p.set("material", np.where(gate, 2, 1).astype(np.int32))
+    p.set("is_free", (~fixed).astype(np.int32))
+    p.set("no_slip", fixed.astype(np.int32))
+    p.set("id", np.where(gate, np.where(clamp, 4, 3), np.where(wall, 2, 1)).astype(np.int32))
+    rho = np.where(gate, rho_r, rho_f).astype(float)
+    dens = rho.copy()
+    dens[water] = rho_f * np.power(1 + 7.0 * g * (H - yb[water]) / (cs_w * cs_w), 1.0 / 7.0)
+    p.set("density", dens)
+    p.set("densityb", dens)
+    p.set("ref_density", rho)
+    p.set("mass", rho * dx * dx)
+    p.set("cs", np.where(gate, cs_r, cs_w))
+    p.set("pres_eq", np.where(gate, 0, 1).astype(np.int32))
+    p.set("mu", np.where(gate, 0.0, mu))
+    p.set("mu_ref", np.where(gate, 0.0, mu))
+    p.set("alpha", np.where(gate, 1.0, 0.1))
+    p.set("g_mod", np.where(gate, G, 0.0))
+    p.set("ti", np.where(gate, ti, 0.0))
+    p.set("ti_init_dist", np.where(gate, dx, 0.0))
+    dt = min(0.2 * h / cs_w, 0.2 * h / cs_r)
+    return dom, dt, {"h": h, "cs_w": cs_w, "cs_r": cs_r, "n_water": int(water.sum()),
+                     "n_gate": int((gate & ~clamp).sum()), "n_fixed": int(fixed.sum())}
 
 
 def granular_ensemble(n=256, seed=0, dx=1e-3, W=0.2, aspect=(0.5, 4.0), phi_deg=(20.0, 40.0), fail=2, **kw):

@@ -121,6 +121,16 @@ def seep_buoyancy_only():
     return scenarios.seepage_bed_2d(swi=3, seepage_type=0, k=2.0e-9, cohesion=1000.0)
 
 
+def gate_fsi_off():
+    """Water behind an elastic gate (Material 2), coupled by CalcForce12 with the FSI interpolation off."""
+    return scenarios.elastic_gate_2d(fsi=False)
+
+
+def gate_fsi_on():
+    """The same with the FSI interpolation of the gate's pressure and velocity, leapfrog."""
+    return scenarios.elastic_gate_2d(fsi=True, scheme=1)
+
+
 CASES = {
     "dam2d": (dam2d, 42, (1, 2, 32, 41, 42)),
     "dam2d_leapfrog": (dam2d_leapfrog, 5, (1, 2, 5)),
@@ -138,6 +148,8 @@ CASES = {
     "seep_erosion_ergun": (seep_erosion_ergun, 20, (1, 2, 20)),
     "seep_pore_pressure": (seep_pore_pressure, 10, (1, 10)),
     "seep_buoyancy_only": (seep_buoyancy_only, 10, (1, 10)),
+    "gate_fsi_off": (gate_fsi_off, 32, (1, 2, 32)),
+    "gate_fsi_on": (gate_fsi_on, 20, (1, 2, 20)),
 }
 
 # AddBoxLength argument lists: dim, tag, V, Lx, Ly, Lz, r, rho, h, type, rotation, random, fixed

@@ -1,7 +1,10 @@
-"""Fluid-soil domains on the GPU (CalcForce13, the saturation switch, VarPorosity):
-trajectories against the reference's golden outputs, and the combinations this
-build rejects. Per-step parity against the oracle runs with every other case
-in test_gpu_parity.py (the seepage cases are part of its case table)."""
+"""Domains of two materials on the GPU: fluid with soil (CalcForce13, the
+saturation switch, VarPorosity) and fluid with an elastic solid (CalcForce12,
+the FSI interpolation). The seepage state against the reference's golden
+trajectories, and the combinations this build rejects. Per-step parity against
+the oracle and the trajectories of x, v, density and pressure run with every
+other case in test_gpu_parity.py (the seep_* and gate_* cases are part of its
+case table)."""
 import os
 
 import numpy as np
@@ -54,20 +57,20 @@ def _rejected(dom, dt, **cfg_changes):
     return e.value
 
 
-def test_fluid_soil_needs_fp64(gpu):
-    dom, dt, _ = scenarios.seepage_bed_2d()
-    err = _rejected(dom, dt, precision=1)
-    assert err.code == 2 and "FP64" in str(err)
+def test_two_materials_need_fp64(gpu):
+    for dom, dt, _ in (scenarios.seepage_bed_2d(), scenarios.elastic_gate_2d()):
+        err = _rejected(dom, dt, precision=1)
+        assert err.code == 2 and "FP64" in str(err)
 
 
-def test_fluid_solid_is_rejected(gpu):
-    """A solid (Material 2) beside a fluid would need CalcForce12 (FSI)."""
+def test_solid_with_soil_is_rejected(gpu):
+    """The reference has no pair force between a solid (Material 2) and a soil
+    (LastComputeAcceleration aborts on such a pair)."""
     dom, dt, _ = scenarios.seepage_bed_2d()
     p = dom.particles
-    p.get("material")[p.get("material") == 3] = 2
-    p.get("fail")[:] = 0
+    p.get("material")[p.get("material") == 1] = 2
     err = _rejected(dom, dt)
-    assert err.code == 2 and "CalcForce12" in str(err)
+    assert err.code == 2 and "no pair force" in str(err)
 
 
 def test_seepage_type_out_of_range(gpu):
