@@ -63,13 +63,15 @@ FORCE32_BYTES_PER_PARTICLE = {False: 104, True: 148}
 # DRAM bytes per particle one launch actually moved: ncu captures of the same
 # kernels on the same tank at dx = 10 mm (1,021,104 particles),
 # dram__bytes_read.sum + dram__bytes_write.sum per particle (LES + closure
-# flavour: 271.24 + 56.53 MB); the traffic grows with the particle count, so
-# a full-size launch moves this x n.
-FORCE32_TRAFFIC_BYTES_PER_PARTICLE = {False: 304.6, True: 321.0}
+# flavour: 283.39 + 56.51 MB; without LES: an earlier capture of that
+# flavour); the traffic grows with the
+# particle count, so a full-size launch moves this x n. Most of the excess over
+# the algorithmic bytes is the neighbour list (~80 entries x 4 B a particle).
+FORCE32_TRAFFIC_BYTES_PER_PARTICLE = {False: 304.6, True: 332.9}
 # Pipe activity of that launch (LES + closure flavour) and of the FP64 pair
-# kernel in the same capture series (sm__pipe_*_cycles_active, % of peak).
-FORCE32_NCU = {"issue_active": 0.640, "fma_pipe": 0.346, "fp64_pipe": 0.040, "warps_active": 0.297}
-FORCE64_NCU_FP64_PIPE = 0.854
+# kernel (pass A) in the same capture series (sm__pipe_*_cycles_active, % of peak).
+FORCE32_NCU = {"issue_active": 0.573, "fma_pipe": 0.294, "fp64_pipe": 0.040, "warps_active": 0.298}
+FORCE64_NCU_FP64_PIPE = 0.834
 
 
 def peaks():
@@ -472,7 +474,7 @@ def main():
                           "fp64_pipe_active_ncu_small_case": FORCE64_NCU_FP64_PIPE,
                           "note": "frac counts 106 algorithmic FP64 flops per pair-interaction (one evaluation "
                                   "and the partner's terms, each pair once) against the DFMA rate; the FP64 pipe "
-                                  "itself is ~84 % busy (square roots, divisions, conversions, idle lanes)"},
+                                  "itself is ~83 % busy (square roots, divisions, conversions, idle lanes)"},
         "clocks": m32["clocks"],
         "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": h2d / max(done_e, 1),
                 "d2h_bytes_per_step": d2h / max(done_e, 1), "steps": done_e,
