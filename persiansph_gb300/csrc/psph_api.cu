@@ -128,13 +128,6 @@ void free_all(psph_ctx* c) {
 double dflt(const double* a, int64_t i, double d) { return a ? a[i] : d; }
 int32_t iflt(const int32_t* a, int64_t i, int32_t d) { return a ? a[i] : d; }
 
-double eos_host(int eq, double cs, double p0, double rho, double rho0) {
-  switch (eq) {  // Source/Functions.cpp:188-212, same expression order
-    case 0: return p0 + (cs * cs) * (rho - rho0);
-    case 1: return p0 + (rho0 * cs * cs / 7.0) * (std::pow(rho / rho0, 7.0) - 1);
-    default: return (cs * cs) * rho;
-  }
-}
 
 // Threads for the per-particle host loops of an upload (one per ~200k
 // particles, at most the hardware's).
@@ -570,18 +563,21 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
       cls[g] = id;  // local to the chunk until the merge below
       // InitialChecks: initial pressure from the EOS for fluids and solids (Source/Domain.cpp:1675-1677)
       const double p_in = dflt(p->pressure, i, 0.0);
-      pressure[g] = (initial && C.material < 3) ? eos_host(C.pres_eq, C.cs, C.p0, p->density[i], C.rho0) : p_in;
+      // (the EOS the update applies every step: the Tait power as products, no pow call)
+      pressure[g] = (initial && C.material < 3) ? eos(C.pres_eq, C.cs, C.p0, p->density[i], C.rho0) : p_in;
     }
   };
   run_threads(nthreads, work);
   int materials = 0;
   std::unordered_map<std::string, int, ClassKeyHash> index;
   {
+    std::vector<std::vector<int>> remaps(nthreads);
     for (int t = 0; t < nthreads; ++t) {
       const Worker& W = workers[t];
       if (W.err) return set_err(c, W.err, "%s", W.msg);
       materials |= W.materials;
-      std::vector<int> remap(W.classes.size());
+      std::vector<int>& remap = remaps[t];
+      remap.resize(W.classes.size());
       for (size_t k = 0; k < W.classes.size(); ++k) {
         std::string key((const char*)&W.classes[k], sizeof(PClass));
         auto it = index.find(key);
@@ -595,9 +591,13 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
           remap[k] = it->second;
         }
       }
+    }
+    // each chunk's local class ids to the merged table's, chunks in parallel
+    run_threads(nthreads, [&](int t) {
+      const std::vector<int>& remap = remaps[t];
       const int64_t g0 = ntot * t / nthreads, g1 = ntot * (t + 1) / nthreads;
       for (int64_t g = g0; g < g1; ++g) cls[g] = remap[cls[g]];
-    }
+    });
   }
   // Materials that share a domain: fluid with soil couples through
   // CalcForce13, fluid with a solid through CalcForce12; a solid with a soil
@@ -1117,6 +1117,14 @@ __global__ void dl_gather_kernel(const double* __restrict__ src, int stride, int
   if (r < 0) return;
   for (int e = 0; e < width; ++e) dst[(size_t)r * width + e] = src[(size_t)s * stride + off + e];
 }
+// original index (relative to the instance) per row
+__global__ void dl_orig_kernel(const int* __restrict__ orig, long long base, long long* __restrict__ dst,
+                               const int* __restrict__ row, int n) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const int r = row[s];
+  if (r >= 0) dst[r] = orig[s] - base;
+}
 // a class constant (int or double at byte offset off of PClass) per row
 __global__ void dl_class_kernel(const PClass* __restrict__ tab, const int* __restrict__ cls, size_t off, int is_int,
                                 void* __restrict__ dst, const int* __restrict__ row, int n) {
@@ -1129,16 +1137,13 @@ __global__ void dl_class_kernel(const PClass* __restrict__ tab, const int* __res
   else static_cast<double*>(dst)[r] = *reinterpret_cast<const double*>(rec);
 }
 
-psph_status download_impl(psph_ctx* c, int q, psph_particles* out) {
-  if (!c || !out) return PSPH_ERR_INVALID_ARGUMENT;
-  if (!c->uploaded) return set_err(c, PSPH_ERR_STATE, "psph_download before psph_upload");
-  if (q < 0 || q >= c->ninst) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "instance %d out of range", q);
+// Output rows of instance q on the device: c->dl_row[s] is slot s's row in
+// original order (leavers and other instances: -1); *m receives the row count.
+psph_status download_rows(psph_ctx* c, int q, int64_t* m) {
   psph_status st;
   if ((st = sync_scalars(c))) return st;
   const int n = c->h_sc->n;
   const Persist& P = c->h_sc->buf ? c->PB : c->PA;
-  const Options& o = c->opt;
-  const bool lf = (o.scheme == PSPH_LEAPFROG);
   cudaStream_t s = c->stream;
   const size_t N = (size_t)c->ncap;
   if (!c->dl_row) {
@@ -1155,7 +1160,24 @@ psph_status download_impl(psph_ctx* c, int q, psph_particles* out) {
   int m32 = 0;
   CUDA_TRY(c, cudaMemcpyAsync(&m32, c->dl_rank + len, sizeof(int), cudaMemcpyDeviceToHost, s));
   CUDA_TRY(c, cudaStreamSynchronize(s));
-  const int64_t m = m32;
+  *m = m32;
+  return PSPH_OK;
+}
+
+psph_status download_impl(psph_ctx* c, int q, psph_particles* out) {
+  if (!c || !out) return PSPH_ERR_INVALID_ARGUMENT;
+  if (!c->uploaded) return set_err(c, PSPH_ERR_STATE, "psph_download before psph_upload");
+  if (q < 0 || q >= c->ninst) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "instance %d out of range", q);
+  psph_status st;
+  int64_t m = 0;
+  if ((st = download_rows(c, q, &m))) return st;
+  const int n = c->h_sc->n;
+  const Persist& P = c->h_sc->buf ? c->PB : c->PA;
+  const Options& o = c->opt;
+  const bool lf = (o.scheme == PSPH_LEAPFROG);
+  cudaStream_t s = c->stream;
+  const size_t N = (size_t)c->ncap;
+  const int nb = n > 0 ? (n + 255) / 256 : 1;
   if (out->n < m)
     return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "output holds %lld particles, need %lld", (long long)out->n, (long long)m);
   out->n = m;
@@ -1182,16 +1204,51 @@ psph_status download_impl(psph_ctx* c, int q, psph_particles* out) {
       {lf ? out->shear_stressa : out->shear_stressb, P.shear_h, 9, 0, 9},
       {lf ? out->shear_stressb : nullptr, c->S.shear_o, 9, 0, 9},
   };
+  // The requested fields are gathered into the device staging buffer in
+  // batches of at most kStageWidth values per row (a wider field alone); the
+  // first batch's gathers run while host threads populate the output pages.
+  constexpr int kStageWidth = 16;
+  std::vector<const F*> act;
   int width = 1;
   for (const F& f : fields)
-    if (f.out && f.dev && f.width > width) width = f.width;
+    if (f.out && f.dev) {
+      act.push_back(&f);
+      width = std::max(width, f.width);
+    }
+  std::vector<int> batch_of(act.size()), seg(act.size());
+  int stage = width, nbatch = 0;
+  for (size_t a = 0, used = 0; a < act.size(); ++a) {
+    if (used > 0 && used + act[a]->width > (size_t)std::max(kStageWidth, width)) {
+      ++nbatch;
+      used = 0;
+    }
+    batch_of[a] = nbatch;
+    seg[a] = (int)used;
+    used += act[a]->width;
+    stage = std::max(stage, (int)used);
+  }
+  if (!act.empty()) ++nbatch;
+  if (stage > c->dl_width) {
+    if ((st = dalloc(c, &c->dl_buf, N * (size_t)stage))) return st;
+    c->dl_width = stage;
+  }
+  auto gather_batch = [&](int b) {
+    for (size_t a = 0; a < act.size(); ++a) {
+      if (batch_of[a] != b) continue;
+      const F& f = *act[a];
+      // the FP32C fluid kernel keeps its strain-rate sums in FP32: expand them first
+      if (f.dev == c->S.strain_rate && c->S.sr32) launch_expand_sr32(view(c), n, s);
+      dl_gather_kernel<<<nb, 256, 0, s>>>(f.dev, f.stride, f.off, f.width, c->dl_buf + (size_t)seg[a] * m,
+                                          c->dl_row, n);
+    }
+  };
+  if (nbatch > 0) gather_batch(0);
   {
     // Fresh output pages are populated here by host threads in parallel (one
     // write per page; the copies overwrite them): a device copy into
     // untouched pageable memory would take each page fault in turn.
     std::vector<std::pair<char*, size_t>> ranges;
-    for (const F& f : fields)
-      if (f.out && f.dev) ranges.emplace_back(reinterpret_cast<char*>(f.out), (size_t)m * f.width * sizeof(double));
+    for (const F* f : act) ranges.emplace_back(reinterpret_cast<char*>(f->out), (size_t)m * f->width * sizeof(double));
     size_t total = 0;
     for (const auto& r : ranges) total += r.second;
     const size_t page = (size_t)std::max(4096L, sysconf(_SC_PAGESIZE));
@@ -1204,16 +1261,13 @@ psph_status download_impl(psph_ctx* c, int q, psph_particles* out) {
         }
       });
   }
-  if (width > c->dl_width) {
-    if ((st = dalloc(c, &c->dl_buf, N * (size_t)width))) return st;
-    c->dl_width = width;
-  }
-  for (const F& f : fields) {
-    if (!f.out || !f.dev) continue;
-    // the FP32C fluid kernel keeps its strain-rate sums in FP32: expand them first
-    if (f.dev == c->S.strain_rate && c->S.sr32) launch_expand_sr32(view(c), n, s);
-    dl_gather_kernel<<<nb, 256, 0, s>>>(f.dev, f.stride, f.off, f.width, c->dl_buf, c->dl_row, n);
-    CUDA_TRY(c, cudaMemcpyAsync(f.out, c->dl_buf, (size_t)m * f.width * sizeof(double), cudaMemcpyDeviceToHost, s));
+  for (int b = 0; b < nbatch; ++b) {
+    if (b > 0) gather_batch(b);  // after the previous batch's copies (same stream)
+    for (size_t a = 0; a < act.size(); ++a) {
+      if (batch_of[a] != b) continue;
+      CUDA_TRY(c, cudaMemcpyAsync(act[a]->out, c->dl_buf + (size_t)seg[a] * m,
+                                  (size_t)m * act[a]->width * sizeof(double), cudaMemcpyDeviceToHost, s));
+    }
   }
   // class constants, gathered from the device class table
   struct K { void* out; size_t off; int is_int; };
@@ -1272,22 +1326,34 @@ psph_status integrator_impl(psph_ctx* c, int q, psph_integrator* it) {
   return PSPH_OK;
 }
 
+// (the rows are counted on the device: the alive flags and original indices
+// of millions of particles stay there)
 int64_t num_particles_impl(psph_ctx* c, int q) {
   if (!c || !c->uploaded || q < 0 || q >= c->ninst) return 0;
-  std::vector<std::pair<int, int>> order;
-  if (alive_of(c, q, order, nullptr)) return -1;
-  return (int64_t)order.size();
+  int64_t m = 0;
+  if (download_rows(c, q, &m)) return -1;
+  return m;
 }
 
 psph_status original_index_impl(psph_ctx* c, int q, int64_t* out) {
   if (!c || !out) return PSPH_ERR_INVALID_ARGUMENT;
   if (!c->uploaded) return set_err(c, PSPH_ERR_STATE, "psph_original_index before psph_upload");
   if (q < 0 || q >= c->ninst) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "instance %d out of range", q);
-  std::vector<std::pair<int, int>> order;
-  psph_status st = alive_of(c, q, order, nullptr);
+  int64_t m = 0;
+  psph_status st = download_rows(c, q, &m);
   if (st) return st;
-  const int64_t base = c->inst_off[q];
-  for (size_t r = 0; r < order.size(); ++r) out[r] = order[r].first - base;
+  if (m == 0) return PSPH_OK;
+  const int n = c->h_sc->n;
+  const Persist& P = c->h_sc->buf ? c->PB : c->PA;
+  if (c->dl_width < 1) {
+    if ((st = dalloc(c, &c->dl_buf, (size_t)c->ncap))) return st;
+    c->dl_width = 1;
+  }
+  long long* dst = reinterpret_cast<long long*>(c->dl_buf);
+  dl_orig_kernel<<<(n + 255) / 256, 256, 0, c->stream>>>(P.orig, c->inst_off[q], dst, c->dl_row, n);
+  CUDA_TRY(c, cudaMemcpyAsync(out, dst, (size_t)m * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  CUDA_TRY(c, cudaGetLastError());
   return PSPH_OK;
 }
 
