@@ -15,6 +15,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <thread>
 #include <unistd.h>
@@ -444,8 +445,12 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
     });
     for (char f : found) dyn_mu = dyn_mu || f;
   }
-  std::vector<int> cls(ntot);
-  std::vector<double> pressure(ntot);
+  // per-particle class and initial pressure, written by the workers below
+  // (left uninitialised here: their pages are first touched in parallel)
+  std::unique_ptr<int[]> cls_buf(new int[ntot > 0 ? ntot : 1]);
+  std::unique_ptr<double[]> pressure_buf(new double[ntot > 0 ? ntot : 1]);
+  int* const cls = cls_buf.get();
+  double* const pressure = pressure_buf.get();
   struct Worker {
     std::vector<PClass> classes;
     std::unordered_map<std::string, int, ClassKeyHash> index;
@@ -918,10 +923,10 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
       if (lf && ((st = put(sh2 + 3 * off, p->vb, 3 * m)) || (st = put(sh2s + off, p->densityb, m)))) return st;
       if (dyn_mu && (st = put(smu + off, p->mu, m))) return st;
     }
-    if ((st = put(sp, pressure.data(), NN))) return st;
+    if ((st = put(sp, pressure, NN))) return st;
     launch_upload_pack(sx, sd, sp, sv, sh1, sh1s, sh2, sh2s, smu, c->PA, (int)N, k.dimension == 2, lf, dyn_mu,
                        c->stream);
-    CUDA_TRY(c, cudaMemcpyAsync(c->PA.cls, cls.data(), N * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(c->PA.cls, cls, N * sizeof(int), cudaMemcpyHostToDevice, c->stream));
     CUDA_TRY(c, cudaMemsetAsync(c->d_alive, 1, N, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     if (o.has_solid) {
