@@ -331,11 +331,17 @@ def granular_column_3d(dx=0.01, W=0.06, D=0.04, aspect=1.0, TL_factor=1.0, wall_
                      "n_wall": int(wall.sum())}
 
 
-def seepage_bed_2d(dx=0.01, L=0.3, H=0.2, Hs=0.1, TL=0.6, wall_layers=3, rho_f=1000.0, rho_grain=1580.0,
+def seepage_bed_2d(**kw):
+    """seepage_bed in 2D."""
+    return seepage_bed(dim=2, **kw)
+
+
+def seepage_bed(dim=2, dx=0.01, L=0.3, H=0.2, Hs=0.1, TL=0.6, TW=0.1, wall_layers=3, rho_f=1000.0, rho_grain=1580.0,
                    n0=0.42, grain=0.00392, E=5.0e6, nu=0.3, phi_deg=38.0, swi=0, seepage_type=1,
                    var_porosity=False, k=1.0e-9, k2=0.0, grains=0, scheme=0, g=9.81, hfac=1.2, mu=1.0e-3,
                    alpha=0.1, seed=0, sat_from_x=None, cohesion=0.0):
-    """2D dam break over an erodible soil bed, the shape of Old_Tests/Dam_Scouring2.cpp:
+    """Dam break over an erodible soil bed, the shape of Old_Tests/Dam_Scouring2.cpp
+    (in 2D, or in 3D with a tank TW deep in z):
     a TL-wide tank whose lower Hs is a saturated-density soil bed (Material 3,
     Drucker-Prager, non-associated Fail 3, density (1 - n0) rho_grain + n0 rho_f)
     and an L x H water column (Material 1) on the bed at the left. Walls are soil
@@ -349,7 +355,7 @@ def seepage_bed_2d(dx=0.01, L=0.3, H=0.2, Hs=0.1, TL=0.6, wall_layers=3, rho_f=1
     saturated (IsSat), as after a drained flood. Returns (domain, dt, info).
     """
     dom = Domain()
-    dom.Dimension = 2
+    dom.Dimension = dim
     dom.Scheme = scheme
     dom.Kernel_Set(Qubic_Spline)
     dom.Viscosity_Eq_Set(Morris)
@@ -364,17 +370,24 @@ def seepage_bed_2d(dx=0.01, L=0.3, H=0.2, Hs=0.1, TL=0.6, wall_layers=3, rho_f=1
     cs_s = math.sqrt(K / (rho_s - rho_f))
     cs_f = 10.0 * math.sqrt(2.0 * g * H)
     TH = Hs + H + 2 * dx
-    _tank(dom, dx, TL, TH, 0.0, wall_layers)
+    _tank(dom, dx, TL, TH, TW if dim == 3 else 0.0, wall_layers)
     p = dom.particles
+
+    def walls(x):
+        w = (x[:, 0] < 0.0) | (x[:, 1] < 0.0) | (x[:, 0] > TL)
+        if dim == 3:
+            w |= (x[:, 2] < 0.0) | (x[:, 2] > TW)
+        return w
+
     x = p.get("x")
     xb, yb = x[:, 0], x[:, 1]
-    wall = (xb < 0.0) | (yb < 0.0) | (xb > TL)
+    wall = walls(x)
     bed = (~wall) & (yb < Hs)
     water = (~wall) & (yb >= Hs) & (yb < Hs + H) & (xb < L)
     p.keep(wall | bed | water)
     x = p.get("x")
     xb, yb = x[:, 0], x[:, 1]
-    wall = (xb < 0.0) | (yb < 0.0) | (xb > TL)
+    wall = walls(x)
     soil = yb < Hs
     water = (~wall) & (~soil)
     if grains:
@@ -403,7 +416,7 @@ def seepage_bed_2d(dx=0.01, L=0.3, H=0.2, Hs=0.1, TL=0.6, wall_layers=3, rho_f=1
     p.set("pres_eq", np.where(soil, 0, 1).astype(np.int32))
     p.set("mu", np.where(soil, 0.0, mu))
     p.set("mu_ref", np.where(soil, 0.0, mu))
-    p.set("mass", np.where(soil, rho_s, rho_f) * dx * dx)
+    p.set("mass", np.where(soil, rho_s, rho_f) * dx ** dim)
     # soil: Drucker-Prager, geostatic stress of the bed
     p.set("beta", np.where(soil, 0.1, 0.0))
     p.set("g_mod", np.where(soil, G, 0.0))

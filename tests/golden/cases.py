@@ -121,6 +121,12 @@ def seep_buoyancy_only():
     return scenarios.seepage_bed_2d(swi=3, seepage_type=0, k=2.0e-9, cohesion=1000.0)
 
 
+def seep3d_erosion():
+    """3D fluid over a soil bed: SWIType 1, Ergun permeability with VarPorosity, suspended grains."""
+    return scenarios.seepage_bed(dim=3, dx=0.02, L=0.16, H=0.1, Hs=0.06, TL=0.3, TW=0.1, swi=1, seepage_type=2,
+                                 var_porosity=True, grains=4, cohesion=1000.0)
+
+
 def gate_fsi_off():
     """Water behind an elastic gate (Material 2), coupled by CalcForce12 with the FSI interpolation off."""
     return scenarios.elastic_gate_2d(fsi=False)
@@ -148,6 +154,7 @@ CASES = {
     "seep_erosion_ergun": (seep_erosion_ergun, 20, (1, 2, 20)),
     "seep_pore_pressure": (seep_pore_pressure, 10, (1, 10)),
     "seep_buoyancy_only": (seep_buoyancy_only, 10, (1, 10)),
+    "seep3d_erosion": (seep3d_erosion, 10, (1, 2, 10)),
     "gate_fsi_off": (gate_fsi_off, 32, (1, 2, 32)),
     "gate_fsi_on": (gate_fsi_on, 20, (1, 2, 20)),
 }
