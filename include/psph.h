@@ -88,7 +88,15 @@ typedef struct psph_config {
   int32_t fsi;                /* Domain::FSI: free solid particles take the pressure and velocity
                                  their free fluid neighbours interpolate (Source/Domain.cpp:1090-1160);
                                  fluid-solid pairs use CalcForce12 either way */
-  int32_t reserved[7];        /* must be zero */
+  int32_t in_out_flow;        /* Domain::BC.InOutFlow (Source/Domain.cpp:1327-1635): particles are
+                                 given the in-flow state near -x (1), the out-flow state near +x (2),
+                                 or both (3), and leaving particles are recycled to the in-flow; 0 none */
+  int32_t mass_conservation;  /* BC.MassConservation: out-flow velocity scaled by |in| / |out| */
+  int32_t reserved[5];        /* must be zero */
+  double initial_dist;        /* Domain::InitialDist (spacing of the recycled in-flow lattice) */
+  double bc_cellfac;          /* BC.cellfac: width of the in/out-flow zones in hmax (0: the reference's 3.9) */
+  double in_v[3], in_density;   /* BC.inv, BC.inDensity: what the default InCon (InFlowCon) sets */
+  double out_v[3], out_density; /* BC.outv, BC.outDensity: what the default OutCon (OutFlowCon) sets */
 } psph_config;
 
 /* Cell grid made by CellInitiate (Source/Domain.cpp:549-660). */
@@ -146,6 +154,9 @@ typedef struct psph_particles {
    * s: S, the surface-erosion velocity derivative of the last step (download only). */
   int32_t *seepage_type, *var_porosity, *is_sat;
   double *n0, *k, *k2, *d, *rho_f, *volume, *s;
+  /* Particle::InOut: 0, or 1 / 2 while the particle is in the in-flow / out-flow
+   * state (config in_out_flow) */
+  int32_t* in_out;
 } psph_particles;
 
 typedef struct psph_ctx psph_ctx;

@@ -167,7 +167,9 @@ def write_state_dir(path: str, cfg: PsphConfig, pset: ParticleSet, extra: dict |
         "gravity": list(cfg.gravity), "body_force": list(cfg.body_force), "xsph": [cfg.xsph],
         "sqrt_h_a": [cfg.sqrt_h_a], "R": [cfg.R], "dom_max": list(cfg.dom_max), "dom_min": list(cfg.dom_min),
         "dt": [cfg.dt], "time": [cfg.time], "shepard_step": [cfg.shepard_step], "swi_type": [cfg.swi_type],
-        "fsi": [cfg.fsi],
+        "fsi": [cfg.fsi], "in_out_flow": [cfg.in_out_flow], "mass_conservation": [cfg.mass_conservation],
+        "bc_cellfac": [cfg.bc_cellfac], "in_v": list(cfg.in_v), "in_density": [cfg.in_density],
+        "out_v": list(cfg.out_v), "out_density": [cfg.out_density], "initial_dist": [cfg.initial_dist],
     }
     if extra:
         lines.update(extra)

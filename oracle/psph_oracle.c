@@ -66,6 +66,12 @@ struct psph_oracle {
    * FSISumKernel) and the particle's entries in FreeFSIParticles */
   double *fsi_p, *fsi_nsv, *fsi_sk;
   int32_t* fsi_cnt;
+  /* in/out-flow state (Domain::BC, Source/Boundary_Condition.h:38-60) */
+  int inoutcounter;
+  double in_loc1, in_loc2, in_loc3, out_loc;
+  int64_t *in_part, n_in_part, cap_in_part; /* BC.InPart, in list order */
+  int64_t n_out_part;                       /* BC.OutPart.Size() */
+  int64_t next_orig;                        /* original index of the next appended particle */
   int64_t ncells;
   int nthr;
   pairvec *sm, *fsm, *nsm;
@@ -1541,6 +1547,13 @@ static int move(psph_oracle* o, int nthr) {
 #pragma omp parallel for schedule(static) num_threads(nthr)
   for (int64_t i = 0; i < o->n; i++) {
     if (!FREE(i)) continue;
+    if (o->in_out[i] > 0) {  /* in/out-flow particles keep their prescribed state (Source/Domain.cpp:1305-1320) */
+      for (int d = 0; d < 3; ++d) o->a[3 * i + d] = 0.0;
+      if (o->in_out[i] == 1 || o->cfg.out_density > 0.0) {
+        o->ddensity[i] = 0.0;
+        o->zwab[i] = 0.0;
+      }
+    }
     double* x = o->x + 3 * i;
     double* v = o->v + 3 * i;
     const double* a = o->a + 3 * i;
@@ -1648,9 +1661,248 @@ static void check_particle_leave(psph_oracle* o) {
   o->n = k;
 }
 
+/* Grows every per-particle array to hold n_new particles (appended ones start
+ * zeroed; the caller fills them as the Particle constructor would). */
+static void grow(psph_oracle* o, int64_t n_new) {
+  const int64_t n = o->n;
+#define GROW_I(NAME) o->NAME = (int32_t*)realloc(o->NAME, (size_t)n_new * sizeof(int32_t)); memset(o->NAME + n, 0, (size_t)(n_new - n) * sizeof(int32_t));
+#define GROW_D(NAME) o->NAME = (double*)realloc(o->NAME, (size_t)n_new * sizeof(double)); memset(o->NAME + n, 0, (size_t)(n_new - n) * sizeof(double));
+#define GROW_V(NAME) o->NAME = (double*)realloc(o->NAME, (size_t)n_new * 3 * sizeof(double)); memset(o->NAME + 3 * n, 0, (size_t)(n_new - n) * 3 * sizeof(double));
+#define GROW_T(NAME) o->NAME = (double*)realloc(o->NAME, (size_t)n_new * 9 * sizeof(double)); memset(o->NAME + 9 * n, 0, (size_t)(n_new - n) * 9 * sizeof(double));
+  PSPH_INT_FIELDS(GROW_I)
+  PSPH_F64_FIELDS(GROW_D)
+  PSPH_VEC_FIELDS(GROW_V)
+  PSPH_TEN_FIELDS(GROW_T)
+  o->orig = (int64_t*)realloc(o->orig, (size_t)n_new * sizeof(int64_t));
+  o->LL = (int32_t*)realloc(o->LL, (size_t)n_new * sizeof(int32_t));
+  o->CC = (int32_t*)realloc(o->CC, (size_t)n_new * 3 * sizeof(int32_t));
+  o->fixed = (int64_t*)realloc(o->fixed, (size_t)n_new * sizeof(int64_t));
+  o->a_scale = (double*)realloc(o->a_scale, (size_t)n_new * sizeof(double));
+  o->dr_scale = (double*)realloc(o->dr_scale, (size_t)n_new * sizeof(double));
+  o->satcheck = (int32_t*)realloc(o->satcheck, (size_t)n_new * sizeof(int32_t));
+  o->fsi_p = (double*)realloc(o->fsi_p, (size_t)n_new * sizeof(double));
+  o->fsi_sk = (double*)realloc(o->fsi_sk, (size_t)n_new * sizeof(double));
+  o->fsi_cnt = (int32_t*)realloc(o->fsi_cnt, (size_t)n_new * sizeof(int32_t));
+  o->fsi_nsv = (double*)realloc(o->fsi_nsv, (size_t)n_new * 3 * sizeof(double));
+  o->locks = (omp_lock_t*)realloc(o->locks, (size_t)n_new * sizeof(omp_lock_t));
+  for (int64_t i = n; i < n_new; ++i) {
+    omp_init_lock(&o->locks[i]);
+    o->orig[i] = o->next_orig++;
+    o->LL[i] = -1;
+  }
+  o->n = n_new;
+}
+
+static void in_part_push(psph_oracle* o, int64_t a) {
+  if (o->n_in_part == o->cap_in_part) {
+    o->cap_in_part = o->cap_in_part ? 2 * o->cap_in_part : 256;
+    o->in_part = (int64_t*)realloc(o->in_part, (size_t)o->cap_in_part * sizeof(int64_t));
+  }
+  o->in_part[o->n_in_part++] = a;
+}
+
+/* The particles of the cells with x index in [qa, qb) in InFlowBCFresh's
+ * traversal order (q2, q3, q1, then each cell's chain), for which keep()
+ * holds (Source/Domain.cpp:1508-1530). */
+#define FLOW_TRAVERSE(o, qa, qb, BODY)                                                        \
+  for (int q2 = 0; o->cfg.periodic[1] ? (q2 < (o->g.cell_no[1] - 2)) : (q2 < o->g.cell_no[1]); q2++) \
+    for (int q3 = 0; o->cfg.periodic[2] ? (q3 < (o->g.cell_no[2] - 2)) : (q3 < o->g.cell_no[2]); q3++) \
+      for (int q1 = (qa); q1 < (qb); q1++) {                                                   \
+        int32_t temp = HOCI(o, q1, q2, q3);                                                    \
+        while (temp != -1) {                                                                   \
+          BODY;                                                                                \
+          temp = o->LL[temp];                                                                  \
+        }                                                                                      \
+      }
+
+/* InCon / OutCon: the reference's default hooks, InFlowCon and OutFlowCon
+ * (Source/Domain.cpp:35-45), give BC.inv / inDensity and BC.outv / outDensity */
+static void set_flow_state(psph_oracle* o, int64_t a, const double* vel, double den, int set_v, int set_d) {
+  if (set_v)
+    for (int d = 0; d < 3; ++d) o->v[3 * a + d] = o->vb[3 * a + d] = o->va[3 * a + d] = vel[d];
+  if (set_d) {
+    o->density[a] = o->densityb[a] = o->densitya[a] = den;
+    o->pressure[a] = EOS(o->pres_eq[a], o->cs[a], o->p0[a], o->density[a], o->ref_density[a]);
+  }
+}
+
+/* InFlowBCFresh (Source/Domain.cpp:1490-1636) */
+static int in_flow_fresh(psph_oracle* o) {
+  const psph_config* c = &o->cfg;
+  const double cellfac = c->bc_cellfac > 0.0 ? c->bc_cellfac : 3.9;
+  const int iof = c->in_out_flow;
+  if (o->inoutcounter == 0) {
+    if (iof == 1 || iof == 3) {
+      const double* inv = c->in_v;
+      if (!(sqrt(dot3(inv, inv)) > 0.0) || !(c->in_density > 0.0))
+        return fail(o, PSPH_ERR_INVALID_ARGUMENT, "BC.inv or BC.inDensity are not defined");
+      o->n_in_part = 0;
+      o->in_loc1 = o->g.blpf[0] + cellfac * o->g.hmax;
+      const int temp1 = (int)(floor((o->in_loc1 - o->g.blpf[0]) / o->g.cell_size[0]));
+      FLOW_TRAVERSE(o, 0, temp1 + 1, if (FREE(temp) && (o->x[3 * temp] <= o->in_loc1)) {
+        in_part_push(o, temp);
+        o->in_out[temp] = 1;
+      })
+      if (o->n_in_part == 0) return fail(o, PSPH_ERR_INVALID_ARGUMENT, "no free particle in the in-flow zone");
+      o->in_loc2 = o->in_loc3 = o->x[3 * o->in_part[0]];
+      for (int64_t i = 0; i < o->n_in_part; i++) {
+        const double x0 = o->x[3 * o->in_part[i]];
+        if (x0 < o->in_loc2) o->in_loc2 = x0;
+        if (x0 > o->in_loc3) o->in_loc3 = x0;
+      }
+    }
+    if (iof == 2 || iof == 3) o->out_loc = o->g.trpr[0] - cellfac * o->g.hmax;
+    o->inoutcounter = 2;
+  }
+  if (o->inoutcounter == 1) {
+    o->n_in_part = 0;
+    const int temp1 = (int)(floor((o->in_loc1 - o->g.blpf[0]) / o->g.cell_size[0]));
+    FLOW_TRAVERSE(o, 0, temp1 + 1, if (FREE(temp) && (o->x[3 * temp] <= o->in_loc1) && o->in_out[temp] == 1)
+                                       in_part_push(o, temp))
+    o->inoutcounter = 2;
+  }
+  o->n_out_part = 0;
+  if (iof == 2 || iof == 3) {
+    const int temp1 = (int)(floor((o->out_loc - o->g.blpf[0]) / o->g.cell_size[0]));
+    FLOW_TRAVERSE(o, temp1, o->g.cell_no[0], if (FREE(temp) && (o->x[3 * temp] >= o->out_loc)) {
+      o->in_out[temp] = 2;
+      o->n_out_part++;
+    })
+  }
+  for (int64_t i = 0; i < o->n_in_part; i++) set_flow_state(o, o->in_part[i], c->in_v, c->in_density, 1, 1);
+  const double temp11 = c->mass_conservation ? o->n_in_part * 1.0 / (o->n_out_part * 1.0) : 1.0;
+  if (o->n_out_part > 0) {
+    double vel[3];
+    for (int d = 0; d < 3; ++d) vel[d] = temp11 * c->out_v[d];
+    const int set_v = sqrt(dot3(c->out_v, c->out_v)) > 0.0 || temp11 != 1.0;
+    for (int64_t a = 0; a < o->n; a++)
+      if (o->in_out[a] == 2 && FREE(a) && o->x[3 * a] >= o->out_loc)
+        set_flow_state(o, a, vel, c->out_density, set_v, c->out_density > 0.0);
+  }
+  return PSPH_OK;
+}
+
+/* The fields InFlowBCLeave copies from in-flow particle b into the recycled
+ * particle a (Source/Domain.cpp:1363-1395). */
+static void recycle_from(psph_oracle* o, int64_t a, int64_t b, const double* pos) {
+  for (int d = 0; d < 3; ++d) o->x[3 * a + d] = pos[d];
+  o->material[a] = 1;
+  o->in_out[a] = 1;
+  o->p0[a] = o->p0[b];
+  o->pres_eq[a] = o->pres_eq[b];
+  o->cs[a] = o->cs[b];
+  o->alpha[a] = o->alpha[b];
+  o->beta[a] = o->beta[b];
+  o->mu[a] = o->mu[b];
+  o->mu_ref[a] = o->mu_ref[b];
+  o->t0[a] = 0.0;
+  o->mass[a] = o->mass[b];
+  o->h[a] = o->h[b];
+  o->id[a] = o->id[b];
+  o->ti[a] = 0.0;
+  o->ref_density[a] = o->ref_density[b];
+  o->shepard[a] = o->shepard[b];
+  o->les[a] = o->les[b];
+  o->csmag[a] = o->csmag[b];
+}
+
+/* InFlowBCLeave (Source/Domain.cpp:1327-1488), replacing CheckParticleLeave:
+ * particles outside the grid box free their slots (DelPart, index order);
+ * in-flow particles that crossed InFlowLoc1 leave the in-flow state and a
+ * copy of each, shifted back by the in-flow zone's width, takes a freed slot
+ * or is appended (AddPart, InPart order); unused slots are deleted. */
+static void in_flow_leave(psph_oracle* o) {
+  const psph_config* c = &o->cfg;
+  int64_t *del = (int64_t*)malloc((size_t)(o->n ? o->n : 1) * sizeof(int64_t)), ndel = 0;
+  for (int64_t i = 0; i < o->n; i++) {
+    const double* x = o->x + 3 * i;
+    if ((x[0] > o->g.trpr[0]) || (x[1] > o->g.trpr[1]) || (x[2] > o->g.trpr[2]) || (x[0] < o->g.blpf[0]) ||
+        (x[1] < o->g.blpf[1]) || (x[2] < o->g.blpf[2])) {
+      o->in_out[i] = 0;
+      del[ndel++] = i;
+    }
+  }
+  int64_t nadd = 0;
+  int64_t* add_b = (int64_t*)malloc((size_t)(o->n_in_part ? o->n_in_part : 1) * sizeof(int64_t));
+  double* add_x = (double*)malloc((size_t)(o->n_in_part ? o->n_in_part : 1) * 3 * sizeof(double));
+  if (c->in_out_flow == 1 || c->in_out_flow == 3) {
+    int64_t keep = 0;
+    for (int64_t i = 0; i < o->n_in_part; i++) {
+      const int64_t b = o->in_part[i];
+      if (o->x[3 * b] > o->in_loc1) {
+        for (int d = 0; d < 3; ++d) add_x[3 * nadd + d] = o->x[3 * b + d];
+        add_x[3 * nadd] -= (o->in_loc3 - o->in_loc2 + c->initial_dist);
+        o->in_out[b] = 0;
+        add_b[nadd++] = b;
+      } else {
+        o->in_part[keep++] = b;
+      }
+    }
+    o->n_in_part = keep;
+  }
+  if (nadd >= ndel) {
+    for (int64_t i = 0; i < ndel; i++) {
+      recycle_from(o, del[i], add_b[i], add_x + 3 * i);
+      in_part_push(o, del[i]);
+    }
+    if (nadd != ndel) {
+      const int64_t n0 = o->n;
+      grow(o, n0 + (nadd - ndel));
+      for (int64_t i = ndel; i < nadd; i++) {
+        const int64_t a = n0 + (i - ndel), b = add_b[i];
+        /* new Particle(ID_b, x, v_b, Mass_b, RefDensity_b, h_b, false): constructor defaults */
+        o->is_free[a] = 1;
+        o->fpmassc[a] = 1.0;
+        o->bingham_m[a] = 300.0;
+        o->csmag[a] = 0.17;
+        o->tin[a] = 4.0;
+        for (int d = 0; d < 3; ++d) o->v[3 * a + d] = o->v[3 * b + d];
+        o->density[a] = o->ref_density[b];
+        o->volume[a] = o->mass[b] / o->ref_density[b];
+        recycle_from(o, a, b, add_x + 3 * i);
+        in_part_push(o, a);
+      }
+    }
+  } else {
+    for (int64_t i = 0; i < nadd; i++) {
+      recycle_from(o, del[i], add_b[i], add_x + 3 * i);
+      in_part_push(o, del[i]);
+    }
+    /* DelItems of the unused slots; InPart holds indices and is rebuilt next step */
+    int64_t k = 0, next = nadd;
+    for (int64_t i = 0; i < o->n; ++i) {
+      if (next < ndel && del[next] == i) {
+        next++;
+        continue;
+      }
+      if (k != i) {
+#define MOVE_I2(NAME) o->NAME[k] = o->NAME[i];
+#define MOVE_D2(NAME) o->NAME[k] = o->NAME[i];
+#define MOVE_V2(NAME) memmove(o->NAME + 3 * k, o->NAME + 3 * i, 3 * sizeof(double));
+#define MOVE_T2(NAME) memmove(o->NAME + 9 * k, o->NAME + 9 * i, 9 * sizeof(double));
+        PSPH_INT_FIELDS(MOVE_I2)
+        PSPH_F64_FIELDS(MOVE_D2)
+        PSPH_VEC_FIELDS(MOVE_V2)
+        PSPH_TEN_FIELDS(MOVE_T2)
+        o->orig[k] = o->orig[i];
+      }
+      k++;
+    }
+    o->n = k;
+    o->inoutcounter = 1;
+  }
+  free(del);
+  free(add_b);
+  free(add_x);
+}
+
 static int one_step(psph_oracle* o, int nthr) {
   double t0 = now_s();
   start_acceleration(o, nthr);
+  if (o->cfg.in_out_flow > 0) {
+    int st = in_flow_fresh(o);
+    if (st) return st;
+  }
   /* FirstStep of Move_MVerlet forces ct=30 (Particle.cpp:191-195) */
   if (o->cfg.scheme == PSPH_MVERLET && o->it.first_step) o->it.ct = 30;
   main_search(o, nthr);
@@ -1667,7 +1919,8 @@ static int one_step(psph_oracle* o, int nthr) {
   o->it.time += o->it.deltat;
   o->it.steps += 1;
   double t4 = now_s();
-  check_particle_leave(o);
+  if (o->cfg.in_out_flow > 0) in_flow_leave(o);
+  else check_particle_leave(o);
   cell_reset(o);
   st = list_generate(o);
   double t5 = now_s();
@@ -1689,6 +1942,12 @@ static int validate(psph_oracle* o) {
   if (c->kernel_type < 0 || c->kernel_type > 2) return fail(o, PSPH_ERR_INVALID_ARGUMENT, "Kernel Type No is out of range");
   if (c->vis_eq < 0 || c->vis_eq > 3) return fail(o, PSPH_ERR_INVALID_ARGUMENT, "Viscosity Equation No is out of range");
   if (c->swi_type < 0 || c->swi_type > 3) return fail(o, PSPH_ERR_INVALID_ARGUMENT, "Soil-Water Interaction Type No is out of range");
+  if (c->in_out_flow < 0 || c->in_out_flow > 3) return fail(o, PSPH_ERR_INVALID_ARGUMENT, "InOutFlow is out of range");
+  if (c->in_out_flow > 0 && c->periodic[0])
+    return fail(o, PSPH_ERR_INVALID_ARGUMENT, "Periodic BC in the X direction cannot be used with In/Out-Flow BC simultaneously");
+  for (int64_t i = 0; i < o->n && c->in_out_flow > 0; ++i)
+    if (o->shepard[i])
+      return fail(o, PSPH_ERR_UNSUPPORTED, "Shepard filtering with in/out-flow (the released particles' own Shepard counters)");
   for (int64_t i = 0; i < o->n; ++i) {
     if (o->material[i] < 1 || o->material[i] > 3) return fail(o, PSPH_ERR_INVALID_ARGUMENT, "Material Type No is out of range");
     if (o->pres_eq[i] < 0 || o->pres_eq[i] > 2) return fail(o, PSPH_ERR_INVALID_ARGUMENT, "Please correct Pressure Equation No");
@@ -1739,6 +1998,7 @@ psph_oracle* psph_oracle_create(const psph_config* cfg, const psph_particles* p,
   o->fsi_cnt = (int32_t*)calloc((size_t)(n ? n : 1), sizeof(int32_t));
   o->orig = (int64_t*)malloc((size_t)(n ? n : 1) * sizeof(int64_t));
   for (int64_t i = 0; i < n; ++i) o->orig[i] = i;
+  o->next_orig = n;
   o->LL = (int32_t*)malloc((size_t)(n ? n : 1) * sizeof(int32_t));
   o->CC = (int32_t*)calloc((size_t)(n ? n : 1) * 3, sizeof(int32_t));
   o->fixed = (int64_t*)malloc((size_t)(n ? n : 1) * sizeof(int64_t));
@@ -1808,6 +2068,7 @@ void psph_oracle_destroy(psph_oracle* o) {
   free(o->fsi_sk);
   free(o->fsi_nsv);
   free(o->fsi_cnt);
+  free(o->in_part);
   free(o->fixed);
   free(o->a_scale);
   free(o->dr_scale);

@@ -101,6 +101,13 @@ static int load_state(SPH::Domain& dom, const char* dir) {
   }
   dom.SWIType = (size_t)psph_io_cfg1(dir, "swi_type", 0);
   dom.FSI = psph_io_cfg1(dir, "fsi", 0) != 0.0;
+  dom.BC.InOutFlow = (int)psph_io_cfg1(dir, "in_out_flow", 0);
+  dom.BC.MassConservation = psph_io_cfg1(dir, "mass_conservation", 0) != 0.0;
+  if (psph_io_cfg1(dir, "bc_cellfac", 0.0) > 0.0) dom.BC.cellfac = psph_io_cfg1(dir, "bc_cellfac", 0.0);
+  if (psph_io_cfg(dir, "in_v", v, 3) == 3) dom.BC.inv = v[0], v[1], v[2];
+  if (psph_io_cfg(dir, "out_v", v, 3) == 3) dom.BC.outv = v[0], v[1], v[2];
+  dom.BC.inDensity = psph_io_cfg1(dir, "in_density", 0.0);
+  dom.BC.outDensity = psph_io_cfg1(dir, "out_density", 0.0);
   dom.MuMax = 0.0;  // left uninitialised by the Domain constructor
   dom.CsMax = 0.0;
 
@@ -130,6 +137,7 @@ static int load_state(SPH::Domain& dom, const char* dir) {
   SET_INT(seepage_type, P->SeepageType = (size_t)val)
   SET_INT(var_porosity, P->VarPorosity = val != 0)
   SET_INT(is_sat, P->IsSat = val != 0)
+  SET_INT(in_out, P->InOut = (size_t)val)
 #define SET_F64(NAME, MEMBER)                                           \
   if (RD(#NAME, dbuf.data(), 8 * (size_t)n) == 0)                       \
     for (int i = 0; i < n; ++i) dom.Particles[i]->MEMBER = dbuf[i];
@@ -178,7 +186,7 @@ static void dump_state(SPH::Domain& dom, const std::string& dir, long step) {
   W_INT(id, P->ID) W_INT(material, P->Material) W_INT(is_free, P->IsFree) W_INT(no_slip, P->NoSlip)
   W_INT(pres_eq, P->PresEq) W_INT(shepard, P->Shepard) W_INT(les, P->LES) W_INT(vis_m, P->VisM)
   W_INT(fail, P->Fail) W_INT(seepage_type, P->SeepageType) W_INT(var_porosity, P->VarPorosity)
-  W_INT(is_sat, P->IsSat)
+  W_INT(is_sat, P->IsSat) W_INT(in_out, P->InOut)
 #define W_F64(NAME, MEMBER)                                           \
   for (size_t i = 0; i < n; ++i) db[i] = dom.Particles[i]->MEMBER;    \
   psph_io_write(d, #NAME, db.data(), 8 * n);
@@ -284,6 +292,7 @@ static int run(const char* in, const char* out, long nsteps, int nproc, const st
     // Solve's per-step body (Source/Domain.cpp:1764-1792), output disabled
     clk::time_point t0 = clk::now();
     dom.StartAcceleration(dom.Gravity);
+    if (dom.BC.InOutFlow > 0) dom.InFlowBCFresh();
     clk::time_point t1 = clk::now();
     dom.MainNeighbourSearch();
     clk::time_point t2 = clk::now();

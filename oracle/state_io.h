@@ -22,7 +22,7 @@ extern "C" {
 /* Per-particle int32 fields, in file order. */
 #define PSPH_INT_FIELDS(X) \
   X(id) X(material) X(is_free) X(no_slip) X(pres_eq) X(shepard) X(les) X(vis_m) X(fail) \
-  X(seepage_type) X(var_porosity) X(is_sat)
+  X(seepage_type) X(var_porosity) X(is_sat) X(in_out)
 
 /* Per-particle float64 scalar fields. */
 #define PSPH_F64_FIELDS(X)                                                                      \

@@ -27,7 +27,8 @@ TEN_FIELDS = (
 # soil-water interaction fields, after the tensors in the struct
 SEEP_INT_FIELDS = ("seepage_type", "var_porosity", "is_sat")
 SEEP_F64_FIELDS = ("n0", "k", "k2", "d", "rho_f", "volume", "s")
-INT_FIELDS = BASE_INT_FIELDS + SEEP_INT_FIELDS
+FLOW_INT_FIELDS = ("in_out",)
+INT_FIELDS = BASE_INT_FIELDS + SEEP_INT_FIELDS + FLOW_INT_FIELDS
 F64_FIELDS = BASE_F64_FIELDS + SEEP_F64_FIELDS
 ALL_FIELDS = INT_FIELDS + VEC_FIELDS + F64_FIELDS + TEN_FIELDS
 
@@ -48,7 +49,9 @@ class PsphConfig(C.Structure):
         ("wall_pressure_mode", C.c_int32), ("gravity", C.c_double * 3), ("body_force", C.c_double * 3),
         ("xsph", C.c_double), ("sqrt_h_a", C.c_double), ("R", C.c_double), ("dom_max", C.c_double * 3),
         ("dom_min", C.c_double * 3), ("dt", C.c_double), ("time", C.c_double), ("fsi", C.c_int32),
-        ("reserved", C.c_int32 * 7),
+        ("in_out_flow", C.c_int32), ("mass_conservation", C.c_int32), ("reserved", C.c_int32 * 5),
+        ("initial_dist", C.c_double), ("bc_cellfac", C.c_double), ("in_v", C.c_double * 3),
+        ("in_density", C.c_double), ("out_v", C.c_double * 3), ("out_density", C.c_double),
     ]
 
 
@@ -82,6 +85,7 @@ class PsphParticles(C.Structure):
         + [(f, C.POINTER(C.c_double)) for f in TEN_FIELDS]
         + [(f, C.POINTER(C.c_int32)) for f in SEEP_INT_FIELDS]
         + [(f, C.POINTER(C.c_double)) for f in SEEP_F64_FIELDS]
+        + [(f, C.POINTER(C.c_int32)) for f in FLOW_INT_FIELDS]
     )
 
 

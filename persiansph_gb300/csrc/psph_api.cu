@@ -370,7 +370,7 @@ psph_status create_impl(const psph_config* cfgs, int ninst, psph_ctx** out) {
     if (k.precision != PSPH_FP64 && k.precision != PSPH_FP32C)
       return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "precision must be PSPH_FP64 or PSPH_FP32C");
     if (k.dimension == 2 && k.periodic[2]) return set_err(c, PSPH_ERR_UNSUPPORTED, "periodic z in 2D");
-    for (int e = 0; e < 7; ++e)
+    for (int e = 0; e < 5; ++e)
       if (k.reserved[e]) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "reserved fields must be zero");
     // one set of kernels serves all instances: the physics switches must agree
     const psph_config& a = cfgs[0];

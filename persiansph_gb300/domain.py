@@ -28,13 +28,20 @@ class Fatal(RuntimeError):
 
 
 class Boundary:
-    """SPH::Boundary (Source/Boundary_Condition.h:26-53); only the periodic flags are on the GPU path."""
+    """SPH::Boundary (Source/Boundary_Condition.h:26-53, defaults of
+    Source/Boundary_Condition.cpp:24-41)."""
 
     def __init__(self):
         self.Periodic = [False, False, False]
         self.InOutFlow = 0
         self.allv = [0.0, 0.0, 0.0]
         self.allDensity = 0.0
+        self.inv = [0.0, 0.0, 0.0]
+        self.outv = [0.0, 0.0, 0.0]
+        self.inDensity = 0.0
+        self.outDensity = 0.0
+        self.cellfac = 3.9
+        self.MassConservation = False
 
 
 def _libc_rand():
@@ -267,8 +274,6 @@ class Domain:
 
     # -- boundary to the C ABI ----------------------------------------------
     def config(self, dt: float) -> PsphConfig:
-        if self.BC.InOutFlow:
-            raise Fatal("in/out-flow boundaries are outside this build")
         c = PsphConfig()
         c.dimension = int(self.Dimension)
         c.kernel_type = self._kernel_type
@@ -283,6 +288,15 @@ class Domain:
             c.dom_min[d] = float(self.DomMin[d])
         c.swi_type = int(self.SWIType)
         c.fsi = int(bool(self.FSI))
+        c.in_out_flow = int(self.BC.InOutFlow)
+        c.mass_conservation = int(bool(self.BC.MassConservation))
+        c.bc_cellfac = float(self.BC.cellfac)
+        c.initial_dist = float(self.InitialDist)
+        c.in_density = float(self.BC.inDensity)
+        c.out_density = float(self.BC.outDensity)
+        for d in range(3):
+            c.in_v[d] = float(self.BC.inv[d])
+            c.out_v[d] = float(self.BC.outv[d])
         c.shepard_step = int(self.ShepardStep)
         c.precision = int(self.Precision)
         c.wall_pressure_mode = int(self.WallPressureMode)

@@ -30,7 +30,7 @@ REF_NAMES = {
     "ShearStressb": "shear_stressb", "Strain": "strain", "Straina": "straina", "Strainb": "strainb",
     "StrainRate": "strain_rate", "RotationRate": "rotation_rate", "TIR": "tir",
     "SeepageType": "seepage_type", "VarPorosity": "var_porosity", "IsSat": "is_sat", "n0": "n0", "k": "k",
-    "k2": "k2", "d": "d", "RhoF": "rho_f", "V": "volume", "S": "s",
+    "k2": "k2", "d": "d", "RhoF": "rho_f", "V": "volume", "S": "s", "InOut": "in_out",
 }
 
 

@@ -518,6 +518,57 @@ def elastic_gate_2d(dx=0.01, L1=0.2, H=0.15, Tr=0.03, H1=0.15, TL_extra=0.1, wal
                      "n_gate": int((gate & ~clamp).sum()), "n_fixed": int(fixed.sum())}
 
 
+def channel_flow_2d(dx=0.01, L=0.5, H=0.1, U=2.0, cs=20.0, flow=3, mass_conservation=False, out_v=None,
+                    out_density=None, wall_layers=3, rho=1000.0, mu=1.0e-3, alpha=0.1, scheme=0, hfac=1.2):
+    """2D channel with in/out-flow boundaries, the shape of Old_Tests/Current-flow.cpp:
+    water between two no-slip walls, L long and H high, particles entering at
+    -x with velocity (U, 0, 0) and density rho (BC.inv, BC.inDensity; the
+    default InCon), leaving at +x (BC.InOutFlow = `flow`; BC.outv and
+    BC.outDensity as given, with BC.MassConservation), no gravity. Particles
+    that cross the in-flow zone are recycled upstream. Returns (domain, dt, info)."""
+    dom = Domain()
+    dom.Dimension = 2
+    dom.Scheme = scheme
+    dom.Kernel_Set(Qubic_Spline)
+    dom.Viscosity_Eq_Set(Morris)
+    dom.Gradient_Approach_Set(Squared_density)
+    dom.Gravity = [0.0, 0.0, 0.0]
+    dom.InitialDist = dx
+    h = hfac * dx
+    w = wall_layers
+    dom.AddBoxLength(1, (0.0, -w * dx, 0.0), L + dx / 10.0, H + 2 * w * dx + dx / 10.0, 0, dx / 2.0, rho, h, 1, 0,
+                     False, False)
+    p = dom.particles
+    x = p.get("x")
+    yb = x[:, 1]
+    wall = (yb < 0.0) | (yb > H)
+    p.set("h", h)
+    p.set("density", rho)
+    p.set("ref_density", rho)
+    p.set("cs", cs)
+    p.set("pres_eq", 1)
+    p.set("mu", mu)
+    p.set("mu_ref", mu)
+    p.set("material", 1)
+    p.set("alpha", alpha)
+    p.set("id", np.where(wall, 2, 1).astype(np.int32))
+    p.set("is_free", (~wall).astype(np.int32))
+    p.set("no_slip", wall.astype(np.int32))
+    v = p.get("v")
+    v[~wall, 0] = U
+    p.set("mass", rho * dx * dx)
+    dom.BC.InOutFlow = flow
+    dom.BC.inv = [U, 0.0, 0.0]
+    dom.BC.inDensity = rho
+    dom.BC.MassConservation = bool(mass_conservation)
+    if out_v is not None:
+        dom.BC.outv = list(out_v)
+    if out_density is not None:
+        dom.BC.outDensity = out_density
+    dt = 0.25 * h / cs
+    return dom, dt, {"h": h, "cs": cs, "U": U, "n_fluid": int((~wall).sum()), "n_wall": int(wall.sum())}
+
+
 def granular_ensemble(n=256, seed=0, dx=1e-3, W=0.2, aspect=(0.5, 4.0), phi_deg=(20.0, 40.0), fail=2, **kw):
     """The batched granular-column workload: n independent 2D columns of width W
     at lattice spacing dx, aspect ratio H/W and friction angle drawn uniformly

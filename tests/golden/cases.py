@@ -127,6 +127,19 @@ def seep3d_erosion():
                                  var_porosity=True, grains=4, cohesion=1000.0)
 
 
+def channel_inout():
+    """In/out-flow channel (InOutFlow 3), out-flow density prescribed, Modified Verlet over the
+    ct==30 restart: at step 9 an in-flow column is released and its copies are appended upstream
+    (beyond the grid box, as the reference places them), at step 10 they leave and the surplus
+    slots are deleted."""
+    return scenarios.channel_flow_2d(flow=3, out_density=1000.0)
+
+
+def channel_inflow_mc():
+    """InOutFlow 3 with mass conservation and an out-flow velocity, leapfrog."""
+    return scenarios.channel_flow_2d(flow=3, mass_conservation=True, out_v=(2.0, 0.0, 0.0), scheme=1)
+
+
 def gate_fsi_off():
     """Water behind an elastic gate (Material 2), coupled by CalcForce12 with the FSI interpolation off."""
     return scenarios.elastic_gate_2d(fsi=False)
@@ -155,6 +168,8 @@ CASES = {
     "seep_pore_pressure": (seep_pore_pressure, 10, (1, 10)),
     "seep_buoyancy_only": (seep_buoyancy_only, 10, (1, 10)),
     "seep3d_erosion": (seep3d_erosion, 10, (1, 2, 10)),
+    "channel_inout": (channel_inout, 40, (1, 2, 9, 10, 20, 32, 40)),
+    "channel_inflow_mc": (channel_inflow_mc, 40, (1, 20, 40)),
     "gate_fsi_off": (gate_fsi_off, 32, (1, 2, 32)),
     "gate_fsi_on": (gate_fsi_on, 20, (1, 2, 20)),
 }

@@ -25,7 +25,7 @@ from tests.golden.cases import CASES, BOXES  # noqa: E402
 
 FIELDS = ("x", "v", "density", "pressure", "a", "ddensity", "zwab", "sigma", "strain_rate", "rotation_rate",
           "shear_stress", "tir", "va", "vb", "densitya", "densityb", "mu", "nsv", "sumkernel", "mass",
-          "ref_density", "is_sat", "s", "strain")
+          "ref_density", "is_sat", "s", "strain", "in_out")
 
 
 def main(only=()):
