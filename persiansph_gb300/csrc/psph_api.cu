@@ -15,6 +15,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <string>
 #include <thread>
@@ -24,6 +25,7 @@
 #include <vector>
 
 #include "psph_device.cuh"
+#include "psph_inout.cuh"
 #include "psph_mlp.cuh"
 #include "psph_output.cuh"
 
@@ -52,6 +54,7 @@ struct psph_ctx {
   // download scratch (allocated at the first download): output row of each
   // sorted particle, its scan, and a staging buffer in the caller's layout
   int *dl_flag = nullptr, *dl_rank = nullptr, *dl_row = nullptr, *dl_bs = nullptr;
+  size_t dl_cap = 0;  // entries of dl_flag / dl_rank
   double* dl_buf = nullptr;
   int dl_width = 0;
   std::vector<PClass> classes;
@@ -81,6 +84,20 @@ struct psph_ctx {
   bool out_requested = false;
   std::string out_key, out_names[3];
   cudaEvent_t ev[kNumPhases + 1] = {};
+  // in/out-flow boundary (one FP64 fluid domain): BC state and the
+  // reference's ordered lists, kept on the host (psph_inout.cu holds the kernels)
+  bool inout = false;
+  int inoutcounter = 0;                 // BC.inoutcounter
+  double in_loc1 = 0.0, in_loc2 = 0.0, in_loc3 = 0.0, out_loc = 0.0;
+  std::vector<long long> in_part;       // BC.InPart (original indices), in list order
+  long long next_orig = 0;              // original index of the next appended particle
+  int* d_slot_of = nullptr;             // slot of each original index
+  long long slot_cap = 0;
+  int* d_flow_count = nullptr;
+  void* d_flow_buf = nullptr;           // candidates / slots / recycle commands
+  size_t flow_buf_bytes = 0;
+  int cls_cap = 0;                      // device class-table capacity
+  std::map<std::string, int> class_index;  // class record -> index (classes added as particles are recycled)
 };
 
 namespace {
@@ -367,6 +384,10 @@ psph_status create_impl(const psph_config* cfgs, int ninst, psph_ctx** out) {
       return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Scheme must be 0 (Modified Verlet) or 1 (Leapfrog)");
     if (k.swi_type < 0 || k.swi_type > 3)
       return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "Soil-Water Interaction Type No is out of range");
+    if (k.in_out_flow < 0 || k.in_out_flow > 3) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "InOutFlow is out of range");
+    if (k.in_out_flow > 0 && k.periodic[0])
+      return set_err(c, PSPH_ERR_INVALID_ARGUMENT,
+                     "Periodic BC in the X direction cannot be used with In/Out-Flow BC simultaneously");
     if (k.precision != PSPH_FP64 && k.precision != PSPH_FP32C)
       return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "precision must be PSPH_FP64 or PSPH_FP32C");
     if (k.dimension == 2 && k.periodic[2]) return set_err(c, PSPH_ERR_UNSUPPORTED, "periodic z in 2D");
@@ -377,7 +398,8 @@ psph_status create_impl(const psph_config* cfgs, int ninst, psph_ctx** out) {
     bool same = k.dimension == a.dimension && k.kernel_type == a.kernel_type && k.vis_eq == a.vis_eq &&
                 k.gradient_type == a.gradient_type && k.scheme == a.scheme && k.precision == a.precision &&
                 k.wall_pressure_mode == a.wall_pressure_mode && k.shepard_step == a.shepard_step &&
-                k.xsph == a.xsph && k.sqrt_h_a == a.sqrt_h_a && k.swi_type == a.swi_type;
+                k.xsph == a.xsph && k.sqrt_h_a == a.sqrt_h_a && k.swi_type == a.swi_type &&
+                k.in_out_flow == a.in_out_flow;
     for (int d = 0; d < 3; ++d) same = same && k.gravity[d] == a.gravity[d] && k.body_force[d] == a.body_force[d];
     if (!same)
       return set_err(c, PSPH_ERR_INVALID_ARGUMENT,
@@ -616,6 +638,21 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
                    "force for them");
   if (mixed && k.precision != PSPH_FP64)
     return set_err(c, PSPH_ERR_UNSUPPORTED, "domains of two materials run in the FP64 form (PSPH_FP64)");
+  const bool inout = k.in_out_flow > 0;
+  if (inout) {
+    if (ninst != 1) return set_err(c, PSPH_ERR_UNSUPPORTED, "in/out-flow boundaries in an ensemble");
+    if (k.precision != PSPH_FP64)
+      return set_err(c, PSPH_ERR_UNSUPPORTED, "in/out-flow boundaries run in the FP64 form (PSPH_FP64)");
+    if (materials != (1 << 1))
+      return set_err(c, PSPH_ERR_UNSUPPORTED, "in/out-flow boundaries with soil or solid particles");
+    if (k.periodic[1] || k.periodic[2])
+      return set_err(c, PSPH_ERR_UNSUPPORTED, "in/out-flow boundaries with a periodic y or z axis");
+    for (const PClass& C : c->classes)
+      if (C.shepard)
+        return set_err(c, PSPH_ERR_UNSUPPORTED,
+                       "Shepard filtering with in/out-flow boundaries (the reference restarts a released "
+                       "particle's own Shepard counter)");
+  }
   if (fluid_soil) {
     for (int q = 0; q < ninst; ++q)
       if (c->cfgs[q].periodic[1])
@@ -715,6 +752,8 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
   o.wallp_physical = (k.wall_pressure_mode == PSPH_WALLP_PHYSICAL);
   o.has_solid = (materials & ((1 << 2) | (1 << 3))) != 0;
   o.mixed = mixed;
+  o.in_out_flow = k.in_out_flow;
+  o.out_density = k.out_density;
   o.couple_soil = fluid_soil;
   o.couple_solid = fluid_solid;
   o.fsi = fluid_solid && k.fsi != 0;
@@ -807,7 +846,10 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
   o.nlist_stage = 0;  // measured: the L1-cached scan beats the staged one (psph_autotune tries both)
 
   // ---- device buffers ----------------------------------------------------------
-  c->ncap = (int)ntot;
+  // in/out-flow domains gain particles as the in-flow is recycled: headroom
+  const int64_t ncap = ntot + (inout ? std::max<int64_t>(1024, ntot / 4) : 0);
+  if (ncap >= (1LL << 26)) return set_err(c, PSPH_ERR_UNSUPPORTED, "this build handles fewer than 2^26 particles");
+  c->ncap = (int)ncap;
   const size_t N = (size_t)ntot;
   psph_status st = PSPH_OK;
   for (Persist* P : {&c->PA, &c->PB}) {
@@ -816,6 +858,7 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
       return st;
     if (lf && (st = dalloc(c, &P->H4b, N))) return st;
     if (dyn_mu && (st = dalloc(c, &P->mu, N))) return st;
+    if (inout && (st = dalloc(c, &P->io, N))) return st;
     if (o.has_solid) {
       if ((st = dalloc(c, &P->sigma, 9 * N)) || (st = dalloc(c, &P->sigma_h, 9 * N)) ||
           (st = dalloc(c, &P->strain, 9 * N)) || (st = dalloc(c, &P->strain_h, 9 * N)) ||
@@ -868,7 +911,8 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
         (st = dalloc(c, &S.strain_o, 9 * N)) || (st = dalloc(c, &S.shear_o, 9 * N)))
       return st;
   }
-  if ((st = dalloc(c, &c->d_cls, c->classes.size())) || (st = dalloc(c, &c->d_sc, 1)) ||
+  c->cls_cap = (int)c->classes.size() + (inout ? 256 : 0);  // recycled in-flow particles may need new classes
+  if ((st = dalloc(c, &c->d_cls, (size_t)c->cls_cap)) || (st = dalloc(c, &c->d_sc, 1)) ||
       (st = dalloc(c, &c->d_alive, N)) || (st = dalloc(c, &c->d_grids, (size_t)ninst)) ||
       (st = dalloc(c, &c->d_inst, (size_t)ninst)))
     return st;
@@ -923,11 +967,14 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
       if (lf && ((st = put(sh2 + 3 * off, p->vb, 3 * m)) || (st = put(sh2s + off, p->densityb, m)))) return st;
       if (dyn_mu && (st = put(smu + off, p->mu, m))) return st;
     }
-    if ((st = put(sp, pressure, NN))) return st;
-    launch_upload_pack(sx, sd, sp, sv, sh1, sh1s, sh2, sh2s, smu, c->PA, (int)N, k.dimension == 2, lf, dyn_mu,
+    const size_t NP = (size_t)ntot;  // the particles (N holds the in-flow headroom too)
+    if ((st = put(sp, pressure, NP))) return st;
+    launch_upload_pack(sx, sd, sp, sv, sh1, sh1s, sh2, sh2s, smu, c->PA, (int)NP, k.dimension == 2, lf, dyn_mu,
                        c->stream);
-    CUDA_TRY(c, cudaMemcpyAsync(c->PA.cls, cls, N * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    CUDA_TRY(c, cudaMemsetAsync(c->d_alive, 1, N, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(c->PA.cls, cls, NP * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaMemsetAsync(c->d_alive, 1, NP, c->stream));
+    if (inout && parts[0].in_out)
+      CUDA_TRY(c, cudaMemcpyAsync(c->PA.io, parts[0].in_out, NP * sizeof(int), cudaMemcpyHostToDevice, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     if (o.has_solid) {
       // Mat3 neither reads nor writes the ShearStress history: a soil domain
@@ -986,8 +1033,308 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
     sc.buf = 0;
     CUDA_TRY(c, cudaMemcpy(c->d_sc, &sc, sizeof sc, cudaMemcpyHostToDevice));
   }
+  c->inout = inout;
+  c->inoutcounter = 0;
+  c->in_part.clear();
+  c->next_orig = ntot;
+  if (inout) {
+    c->class_index.clear();
+    for (size_t q = 0; q < c->classes.size(); ++q)
+      c->class_index.emplace(std::string((const char*)&c->classes[q], sizeof(PClass)), (int)q);
+  }
   c->uploaded = true;
   return PSPH_OK;
+}
+
+// ---- in/out-flow boundary (Source/Domain.cpp:1327-1635) ------------------------
+// The per-particle work runs in psph_inout.cu; here the reference's ordered
+// lists: BC.InPart in its list order, DelPart in index order, AddPart in
+// InPart order. A particle's original index orders it as the reference's
+// particle array does.
+
+psph_status flow_buffer(psph_ctx* c, size_t bytes) {
+  psph_status st;
+  if (!c->d_flow_count && (st = dalloc(c, &c->d_flow_count, 4))) return st;
+  if (bytes > c->flow_buf_bytes) {
+    const size_t cap = std::max(bytes, 2 * c->flow_buf_bytes);
+    char* p = nullptr;
+    if ((st = dalloc(c, &p, cap))) return st;
+    c->d_flow_buf = p;
+    c->flow_buf_bytes = cap;
+  }
+  return PSPH_OK;
+}
+
+// slot of every original index of the current order
+psph_status flow_slot_map(psph_ctx* c) {
+  psph_status st;
+  if (c->next_orig > c->slot_cap) {
+    const long long cap = std::max(c->next_orig, 2 * c->slot_cap);
+    if ((st = dalloc(c, &c->d_slot_of, (size_t)cap))) return st;
+    c->slot_cap = cap;
+  }
+  CUDA_TRY(c, cudaMemsetAsync(c->d_slot_of, 0xff, (size_t)c->next_orig * sizeof(int), c->stream));
+  flow_slot_of(view(c), c->h_sc->n, c->d_slot_of, c->stream);
+  return PSPH_OK;
+}
+
+// the class of a recycled particle, added to the table when new
+int flow_class(psph_ctx* c, const PClass& C, bool* added) {
+  const std::string key((const char*)&C, sizeof(PClass));
+  auto it = c->class_index.find(key);
+  if (it != c->class_index.end()) return it->second;
+  if ((int)c->classes.size() >= c->cls_cap) return -1;
+  const int id = (int)c->classes.size();
+  c->classes.push_back(C);
+  c->class_index.emplace(key, id);
+  *added = true;
+  return id;
+}
+
+// The fields InFlowBCLeave copies from in-flow particle B into a recycled
+// particle (Source/Domain.cpp:1363-1395; T0 and TI are zeroed there).
+void flow_copy_fields(PClass& R, const PClass& B) {
+  R.material = 1;
+  R.p0 = B.p0;
+  R.pres_eq = B.pres_eq;
+  R.cs = B.cs;
+  R.alpha = B.alpha;
+  R.beta = B.beta;
+  R.mu0 = B.mu0;
+  R.mu_ref = B.mu_ref;
+  R.t0 = 0.0;
+  R.mass = B.mass;
+  R.h = B.h;
+  R.id = B.id;
+  R.ti = 0.0;
+  R.rho0 = B.rho0;
+  R.shepard = B.shepard;
+  R.les = B.les;
+  R.csmag = B.csmag;
+}
+
+psph_status flow_upload_list(psph_ctx* c, const std::vector<long long>& v) {
+  psph_status st;
+  if ((st = flow_buffer(c, std::max<size_t>(v.size(), 1) * sizeof(long long)))) return st;
+  if (!v.empty())
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_flow_buf, v.data(), v.size() * sizeof(long long), cudaMemcpyHostToDevice,
+                                c->stream));
+  return PSPH_OK;
+}
+
+// InFlowBCFresh (Source/Domain.cpp:1490-1636), after the step's cell sort
+psph_status inout_fresh(psph_ctx* c) {
+  const psph_config& k = c->cfgs[0];
+  const psph_grid& g = c->grids[0];
+  const double cellfac = k.bc_cellfac > 0.0 ? k.bc_cellfac : 3.9;
+  const int iof = k.in_out_flow;
+  const int n = c->h_sc->n;
+  cudaStream_t s = c->stream;
+  psph_status st;
+  if ((st = flow_slot_map(c))) return st;
+  // BC.InPart by the reference's traversal: cells (q2, q3, q1) in loop order,
+  // each cell's chain in descending index order
+  std::vector<FlowCand> cand;
+  auto traverse = [&](int need_io) -> psph_status {
+    const int temp1 = (int)std::floor((c->in_loc1 - g.blpf[0]) / g.cell_size[0]);
+    psph_status e;
+    if ((e = flow_buffer(c, std::max(n, 1) * sizeof(FlowCand)))) return e;
+    CUDA_TRY(c, cudaMemsetAsync(c->d_flow_count, 0, sizeof(int), s));
+    flow_inflow_candidates(view(c), n, temp1, c->in_loc1, need_io, c->d_flow_count,
+                           static_cast<FlowCand*>(c->d_flow_buf), n, s);
+    int m = 0;
+    CUDA_TRY(c, cudaMemcpyAsync(&m, c->d_flow_count, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(c, cudaStreamSynchronize(s));
+    cand.resize((size_t)m);
+    if (m > 0)
+      CUDA_TRY(c, cudaMemcpy(cand.data(), c->d_flow_buf, (size_t)m * sizeof(FlowCand), cudaMemcpyDeviceToHost));
+    std::sort(cand.begin(), cand.end(), [](const FlowCand& a, const FlowCand& b) {
+      if (a.cy != b.cy) return a.cy < b.cy;
+      if (a.cz != b.cz) return a.cz < b.cz;
+      if (a.cx != b.cx) return a.cx < b.cx;
+      return a.orig > b.orig;
+    });
+    c->in_part.clear();
+    for (const FlowCand& f : cand) c->in_part.push_back(f.orig);
+    return PSPH_OK;
+  };
+  if (c->inoutcounter == 0) {
+    if (iof == 1 || iof == 3) {
+      const double* inv = k.in_v;
+      if (!(std::sqrt(inv[0] * inv[0] + inv[1] * inv[1] + inv[2] * inv[2]) > 0.0) || !(k.in_density > 0.0))
+        return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "BC.inv or BC.inDensity are not defined");
+      c->in_loc1 = g.blpf[0] + cellfac * g.hmax;
+      if ((st = traverse(0))) return st;
+      if (cand.empty()) return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "no free particle in the in-flow zone");
+      c->in_loc2 = c->in_loc3 = cand[0].x0;
+      for (const FlowCand& f : cand) {
+        if (f.x0 < c->in_loc2) c->in_loc2 = f.x0;
+        if (f.x0 > c->in_loc3) c->in_loc3 = f.x0;
+      }
+      if ((st = flow_upload_list(c, c->in_part))) return st;
+      flow_set_io(view(c), static_cast<const long long*>(c->d_flow_buf), (int)c->in_part.size(), c->d_slot_of, 1, s);
+    }
+    if (iof == 2 || iof == 3) c->out_loc = g.trpr[0] - cellfac * g.hmax;
+    c->inoutcounter = 2;
+  }
+  if (c->inoutcounter == 1) {
+    if ((st = traverse(1))) return st;
+    c->inoutcounter = 2;
+  }
+  int n_out = 0;
+  if (iof == 2 || iof == 3) {
+    CUDA_TRY(c, cudaMemsetAsync(c->d_flow_count, 0, sizeof(int), s));
+    flow_outflow_mark(view(c), n, c->out_loc, c->d_flow_count, s);
+    CUDA_TRY(c, cudaMemcpyAsync(&n_out, c->d_flow_count, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(c, cudaStreamSynchronize(s));
+  }
+  if (!c->in_part.empty()) {  // InCon on BC.InPart
+    if ((st = flow_upload_list(c, c->in_part))) return st;
+    flow_inflow_state(view(c), static_cast<const long long*>(c->d_flow_buf), (int)c->in_part.size(), c->d_slot_of,
+                      k.in_v, k.in_density, s);
+  }
+  if (n_out > 0) {  // OutCon on BC.OutPart
+    const double temp11 = k.mass_conservation ? c->in_part.size() * 1.0 / (n_out * 1.0) : 1.0;
+    const double* ov = k.out_v;
+    const double vel[3] = {temp11 * ov[0], temp11 * ov[1], temp11 * ov[2]};
+    const int set_v = (std::sqrt(ov[0] * ov[0] + ov[1] * ov[1] + ov[2] * ov[2]) > 0.0 || temp11 != 1.0) ? 1 : 0;
+    flow_outflow_state(view(c), n, c->out_loc, vel, k.out_density, set_v, k.out_density > 0.0 ? 1 : 0, s);
+  }
+  CUDA_TRY(c, cudaGetLastError());
+  return PSPH_OK;
+}
+
+// InFlowBCLeave (Source/Domain.cpp:1327-1488), after the step's update
+psph_status inout_leave(psph_ctx* c) {
+  const psph_config& k = c->cfgs[0];
+  const int iof = k.in_out_flow;
+  const int n = c->h_sc->n;
+  cudaStream_t s = c->stream;
+  psph_status st;
+  // DelPart: the particles outside the grid box, in index order
+  if ((st = flow_buffer(c, std::max(n, 1) * sizeof(FlowSlot)))) return st;
+  CUDA_TRY(c, cudaMemsetAsync(c->d_flow_count, 0, sizeof(int), s));
+  flow_leaving(view(c), n, c->d_flow_count, static_cast<FlowSlot*>(c->d_flow_buf), n, s);
+  int ndel = 0;
+  CUDA_TRY(c, cudaMemcpyAsync(&ndel, c->d_flow_count, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(c, cudaStreamSynchronize(s));
+  std::vector<FlowSlot> del((size_t)ndel);
+  if (ndel > 0) CUDA_TRY(c, cudaMemcpy(del.data(), c->d_flow_buf, (size_t)ndel * sizeof(FlowSlot), cudaMemcpyDeviceToHost));
+  std::sort(del.begin(), del.end(), [](const FlowSlot& a, const FlowSlot& b) { return a.orig < b.orig; });
+  // AddPart: in-flow particles past InFlowLoc1, in BC.InPart order
+  std::vector<FlowSlot> add;
+  std::vector<long long> released;
+  if ((iof == 1 || iof == 3) && !c->in_part.empty()) {
+    const size_t m = c->in_part.size();
+    if ((st = flow_buffer(c, m * (sizeof(long long) + sizeof(FlowSlot)) + 64))) return st;
+    long long* d_list = static_cast<long long*>(c->d_flow_buf);
+    FlowSlot* d_slots = reinterpret_cast<FlowSlot*>(static_cast<char*>(c->d_flow_buf) + ((m * sizeof(long long) + 63) & ~size_t(63)));
+    CUDA_TRY(c, cudaMemcpyAsync(d_list, c->in_part.data(), m * sizeof(long long), cudaMemcpyHostToDevice, s));
+    flow_gather_slots(view(c), d_list, (int)m, c->d_slot_of, d_slots, s);
+    std::vector<FlowSlot> cur(m);
+    CUDA_TRY(c, cudaMemcpyAsync(cur.data(), d_slots, m * sizeof(FlowSlot), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(c, cudaStreamSynchronize(s));
+    std::vector<long long> keep;
+    for (const FlowSlot& f : cur) {
+      if (f.slot >= 0 && f.x > c->in_loc1) {
+        FlowSlot a = f;
+        a.x -= (c->in_loc3 - c->in_loc2 + k.initial_dist);
+        add.push_back(a);
+        released.push_back(f.orig);
+      } else {
+        keep.push_back(f.orig);
+      }
+    }
+    c->in_part.swap(keep);
+    if (!released.empty()) {
+      if ((st = flow_upload_list(c, released))) return st;
+      flow_set_io(view(c), static_cast<const long long*>(c->d_flow_buf), (int)released.size(), c->d_slot_of, 0, s);
+    }
+  }
+  const size_t nadd = add.size(), nd = del.size();
+  std::vector<FlowRecycle> cmds;
+  bool added = false;
+  const size_t nreuse = std::min(nadd, nd);
+  for (size_t i = 0; i < nreuse; ++i) {  // a freed slot takes the new in-flow particle
+    PClass R = c->classes[(size_t)del[i].cls];
+    flow_copy_fields(R, c->classes[(size_t)add[i].cls]);
+    const int cls = flow_class(c, R, &added);
+    if (cls < 0) return set_err(c, PSPH_ERR_UNSUPPORTED, "in/out-flow: too many distinct particle parameter sets");
+    FlowRecycle r{del[i].slot, add[i].slot, cls, 0, del[i].orig, add[i].x, add[i].y, add[i].z, 0.0};
+    cmds.push_back(r);
+    c->in_part.push_back(del[i].orig);
+  }
+  int appended = 0;
+  for (size_t i = nd; i < nadd; ++i) {  // surplus: new particles (the Particle constructor's defaults)
+    const PClass& B = c->classes[(size_t)add[i].cls];
+    PClass R;
+    std::memset(&R, 0, sizeof R);
+    R.fpmassc = 1.0;
+    R.bm = 300.0;
+    R.tin = 4.0;
+    R.is_free = 1;
+    flow_copy_fields(R, B);
+    R.vol = B.mass / B.rho0;
+    const int cls = flow_class(c, R, &added);
+    if (cls < 0) return set_err(c, PSPH_ERR_UNSUPPORTED, "in/out-flow: too many distinct particle parameter sets");
+    const int slot = n + appended;
+    if (slot >= c->ncap)
+      return set_err(c, PSPH_ERR_UNSUPPORTED, "in/out-flow: the recycled in-flow exceeds the particle headroom (%d)",
+                     c->ncap);
+    const long long orig = c->next_orig++;
+    FlowRecycle r{slot, add[i].slot, cls, 1, orig, add[i].x, add[i].y, add[i].z, B.rho0};
+    cmds.push_back(r);
+    c->in_part.push_back(orig);
+    ++appended;
+  }
+  if (nadd < nd) c->inoutcounter = 1;  // the surplus slots are deleted (the next sort drops them)
+  if (added) {
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_cls, c->classes.data(), c->classes.size() * sizeof(PClass), cudaMemcpyHostToDevice, s));
+    launch_class_constants(c->d_cls, (int)c->classes.size(), c->opt.dim, s);
+  }
+  if (!cmds.empty()) {
+    if ((st = flow_buffer(c, cmds.size() * sizeof(FlowRecycle)))) return st;
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_flow_buf, cmds.data(), cmds.size() * sizeof(FlowRecycle), cudaMemcpyHostToDevice, s));
+    flow_recycle(view(c), static_cast<const FlowRecycle*>(c->d_flow_buf), (int)cmds.size(), s);
+  }
+  if (appended > 0) {
+    const int nn = n + appended, nt = c->h_sc->n_total + appended;
+    CUDA_TRY(c, cudaMemcpyAsync(&c->d_sc->n, &nn, sizeof(int), cudaMemcpyHostToDevice, s));
+    CUDA_TRY(c, cudaMemcpyAsync(&c->d_sc->n_total, &nt, sizeof(int), cudaMemcpyHostToDevice, s));
+  }
+  CUDA_TRY(c, cudaStreamSynchronize(s));
+  CUDA_TRY(c, cudaGetLastError());
+  return PSPH_OK;
+}
+
+// Steps of an in/out-flow domain: each step's launches in two parts, the
+// host's list work between them and after (no graph: the lists decide the
+// next launches).
+psph_status inout_steps(psph_ctx* c, int64_t nsteps, long long* launched) {
+  psph_status st;
+  for (int64_t k = 0; k < nsteps; ++k) {
+    cudaStream_t s = c->stream;
+    launch_begin(view(c), s);
+    launch_sort(view(c), s);
+    CUDA_TRY(c, cudaGetLastError());
+    if ((st = sync_scalars(c))) return st;
+    if (c->h_sc->all_stop) break;
+    if ((st = inout_fresh(c))) return st;
+    const DevView v = view(c);
+    launch_nlist(v, s);
+    launch_prepare(v, s);
+    launch_forces(v, s);
+    if (v.o.closure) launch_closure(v, s);
+    launch_dt(v, s);
+    launch_update(v, s);
+    launch_end(v, s);
+    CUDA_TRY(c, cudaGetLastError());
+    *launched += launches_per_step(v);
+    if ((st = sync_scalars(c))) return st;
+    if (c->h_sc->status) break;
+    if ((st = inout_leave(c))) return st;
+  }
+  return sync_scalars(c);
 }
 
 psph_status step_impl(psph_ctx* c, int64_t nsteps, const double* t_stop, double t_all, int64_t* steps_done) {
@@ -1021,6 +1368,8 @@ psph_status step_impl(psph_ctx* c, int64_t nsteps, const double* t_stop, double 
     if (c->h_sc->all_stop || c->h_sc->status) nsteps = 0;
   }
   if (nsteps <= 0) {
+  } else if (c->inout) {
+    if ((st = inout_steps(c, nsteps, &launched))) return st;
   } else if (c->timing) {
     for (int64_t s = 0; s < nsteps; ++s) {
       enqueue_step(c);
@@ -1122,6 +1471,14 @@ __global__ void dl_gather_kernel(const double* __restrict__ src, int stride, int
   if (r < 0) return;
   for (int e = 0; e < width; ++e) dst[(size_t)r * width + e] = src[(size_t)s * stride + off + e];
 }
+// a per-particle int per row
+__global__ void dl_gather_int_kernel(const int* __restrict__ src, int* __restrict__ dst, const int* __restrict__ row,
+                                     int n) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const int r = row[s];
+  if (r >= 0) dst[r] = src[s];
+}
 // original index (relative to the instance) per row
 __global__ void dl_orig_kernel(const int* __restrict__ orig, long long base, long long* __restrict__ dst,
                                const int* __restrict__ row, int n) {
@@ -1151,12 +1508,16 @@ psph_status download_rows(psph_ctx* c, int q, int64_t* m) {
   const Persist& P = c->h_sc->buf ? c->PB : c->PA;
   cudaStream_t s = c->stream;
   const size_t N = (size_t)c->ncap;
-  if (!c->dl_row) {
-    if ((st = dalloc(c, &c->dl_flag, N + 1)) || (st = dalloc(c, &c->dl_rank, N + 1)) ||
-        (st = dalloc(c, &c->dl_row, N)) || (st = dalloc(c, &c->dl_bs, N / 1024 + 2)))
+  // (an in/out-flow domain's appended particles take original indices past the upload's)
+  const int lo = (int)c->inst_off[q], hi = c->inout ? (int)c->next_orig : (int)c->inst_off[q + 1], len = hi - lo;
+  if (!c->dl_row && (st = dalloc(c, &c->dl_row, N))) return st;
+  if ((size_t)len + 1 > c->dl_cap) {  // the per-original-index scan (grows with an in/out-flow domain)
+    const size_t cap = std::max((size_t)len + 1, std::max(N + 1, 2 * c->dl_cap));
+    if ((st = dalloc(c, &c->dl_flag, cap)) || (st = dalloc(c, &c->dl_rank, cap)) ||
+        (st = dalloc(c, &c->dl_bs, cap / 1024 + 2)))
       return st;
+    c->dl_cap = cap;
   }
-  const int lo = (int)c->inst_off[q], hi = (int)c->inst_off[q + 1], len = hi - lo;
   const int nb = n > 0 ? (n + 255) / 256 : 1;
   CUDA_TRY(c, cudaMemsetAsync(c->dl_flag, 0, sizeof(int) * (size_t)(len + 1), s));
   if (n > 0) dl_flag_kernel<<<nb, 256, 0, s>>>(c->d_alive, P.orig, n, lo, hi, c->dl_flag);
@@ -1273,6 +1634,11 @@ psph_status download_impl(psph_ctx* c, int q, psph_particles* out) {
       CUDA_TRY(c, cudaMemcpyAsync(act[a]->out, c->dl_buf + (size_t)seg[a] * m,
                                   (size_t)m * act[a]->width * sizeof(double), cudaMemcpyDeviceToHost, s));
     }
+  }
+  if (out->in_out && P.io) {  // Particle::InOut (in/out-flow domains)
+    int* dst = reinterpret_cast<int*>(c->dl_buf);
+    dl_gather_int_kernel<<<nb, 256, 0, s>>>(P.io, dst, c->dl_row, n);
+    CUDA_TRY(c, cudaMemcpyAsync(out->in_out, dst, (size_t)m * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
   }
   // class constants, gathered from the device class table
   struct K { void* out; size_t off; int is_int; };

@@ -13,6 +13,7 @@ struct Persist {
   double4_32a* H4b;  // leapfrog: vb, Densityb (wall vb is read by the soil pair force) | MVerlet: null
   int* cls;      // class index
   int* orig;     // original particle index
+  int* io;       // in/out-flow state (Particle::InOut: 0, 1 in-flow, 2 out-flow); null without the boundary
   double* mu;    // dynamic viscosity (LES / Bingham); null when constant per class
   // soil / solid tensors (9 doubles per particle, row-major); null without solids
   double* sigma;
@@ -93,6 +94,8 @@ struct Options {
   int uniform_eos;    // all free particles of the material share one EOS class
   int eos_cls;        // that class
   int dyn_mu;
+  int in_out_flow;    // Domain::BC.InOutFlow (single FP64 fluid domain)
+  double out_density; // BC.outDensity (whether out-flow particles keep their density)
   int soil_pairs;     // Material 3 (soil-soil walls take the partner's density)
   int mixed;          // fluid (Material 1) and a soil or a solid share the domain: each pair
                       // kernel keeps to its material, a coupling kernel adds the pairs of

@@ -245,6 +245,7 @@ __global__ void reorder_kernel(DevView v, const int* __restrict__ perm, const in
       }
     }
     dst.orig[s] = src.orig[i];
+    if (src.io) dst.io[s] = src.io[i];
     const int k = key[i];
     cellid[s] = (k < nbins) ? k / xsub : -1;
     alive[s] = 1;

@@ -143,7 +143,16 @@ __global__ void __launch_bounds__(kUT) update_kernel(DevView v) {
   double4_32a X = P.X4[s];
   double4_32a V = P.V4[s];
   double4_32a H = P.H4[s];
-  const double4_32a A = v.S.A4[s];
+  double4_32a A = v.S.A4[s];
+  if (P.io && P.io[s] > 0) {
+    // in/out-flow particles keep their prescribed state (Source/Domain.cpp:1305-1320)
+    A.x = A.y = A.z = 0.0;
+    if (P.io[s] == 1 || o.out_density > 0.0) {
+      A.w = 0.0;
+      v.S.zwab[s] = 0.0;
+    }
+    v.S.A4[s] = A;
+  }
   double x[3] = {X.x, X.y, X.z}, vel[3] = {V.x, V.y, V.z};
   const double a[3] = {A.x, A.y, A.z};
   const double drho = A.w;

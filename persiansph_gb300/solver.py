@@ -87,10 +87,13 @@ class GpuDomain:
         out = ParticleSet(len(keep))
         for f in ALL_FIELDS:
             arr = fields[f]
-            if base is not None and base.has(f):
-                prev = base.get(f)[keep]
-                untouched = self._untracked(f)
-                arr = prev.copy() if untouched else arr
+            if base is not None and base.has(f) and self._untracked(f):
+                # fields the device does not keep come from the uploaded set
+                # (particles an in/out-flow boundary appended have none: zero)
+                src = base.get(f)
+                arr = np.zeros_like(arr)
+                old = keep < src.shape[0]
+                arr[old] = src[keep[old]]
             out._arr[f] = np.ascontiguousarray(arr)
         return out
 

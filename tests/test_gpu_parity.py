@@ -45,6 +45,8 @@ def test_candidate_pairs_bit_exact(gpu, name):
 def test_support_pairs_bit_exact(gpu, name):
     builder, _, _ = CASES[name]
     dom, dt, _ = builder()
+    if dom.config(dt).in_out_flow:
+        pytest.skip("an in/out-flow boundary's lists are not part of an upload (its trajectory test covers it)")
     o = OracleDomain(dom.config(dt), dom.particles, initial=True)
     o.step(2)
     gd = continue_on_gpu(dom.config(dt), o)
@@ -56,8 +58,9 @@ def test_single_step_parity_1e12(gpu, name):
     builder, _, dumps = CASES[name]
     dom, dt, _ = builder()
     cfg = dom.config(dt)
-    # from the initial state (Solve's set-up) and from a developed state
-    for warm in (0, 3):
+    # from the initial state (Solve's set-up) and from a developed state (an
+    # in/out-flow boundary's lists are not part of an upload: initial state only)
+    for warm in ((0,) if cfg.in_out_flow else (0, 3)):
         o = OracleDomain(cfg, dom.particles, initial=True)
         if warm:
             o.step(warm)
