@@ -850,7 +850,7 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
   const int64_t ncap = ntot + (inout ? std::max<int64_t>(1024, ntot / 4) : 0);
   if (ncap >= (1LL << 26)) return set_err(c, PSPH_ERR_UNSUPPORTED, "this build handles fewer than 2^26 particles");
   c->ncap = (int)ncap;
-  const size_t N = (size_t)ntot;
+  const size_t N = (size_t)ncap;  // every per-particle array holds the headroom
   psph_status st = PSPH_OK;
   for (Persist* P : {&c->PA, &c->PB}) {
     if ((st = dalloc(c, &P->X4, N)) || (st = dalloc(c, &P->V4, N)) || (st = dalloc(c, &P->H4, N)) ||
