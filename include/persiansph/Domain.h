@@ -10,7 +10,11 @@
  * Gradient_Approach_Set), AddSingleParticle / AddBoxLength / AddBoxNo /
  * DelParticles, the public data drivers set (Particles, Dimension, Gravity,
  * Scheme, BC.Periodic, XSPH, InitialDist, DomMax/DomMin, sqrt_h_a, Nproc,
- * SWIType, FSI) and the hooks (GeneralBefore, GeneralAfter, UserOutput).
+ * SWIType, FSI, the in/out-flow settings of BC) and the hooks (GeneralBefore,
+ * GeneralAfter, UserOutput, InCon / OutCon / AllCon). A user InCon / OutCon
+ * runs on the host once per in/out-flow particle per step, as in the
+ * reference; particles an in/out-flow boundary appends become new Particle
+ * objects at the end of Particles when they are copied back.
  * Solve (Source/Domain.cpp:1735-1797) keeps its outer loop over output times;
  * each stretch between outputs is one psph_step call, and the particles are
  * copied back into dom.Particles at every output time and at the end.
@@ -61,8 +65,9 @@ enum Gradient_Type { Squared_density = 0, Multiplied_density = 1 };
 
 namespace SPH {
 
-// Boundary (Source/Boundary_Condition.h:25-55); only Periodic is used by the
-// hot path, InOutFlow != 0 is rejected.
+// Boundary (Source/Boundary_Condition.h:25-55): Periodic, and the in/out-flow
+// settings (InOutFlow, inv/inDensity, outv/outDensity, allv/allDensity,
+// cellfac, MassConservation) Solve hands to the device.
 class Boundary {
  public:
   double inDensity = 0.0, outDensity = 0.0, allDensity = 0.0;
@@ -78,7 +83,19 @@ class Boundary {
 class Domain;
 inline void General(Domain&) {}
 inline void OutPut(Particle*, double& a, double& b, double& c) { a = b = c = 0.0; }
-inline void InFlowCon(Vec3_t&, Vec3_t&, double&, Boundary&) {}
+// the default in/out-flow hooks (Source/Domain.cpp:35-51)
+inline void InFlowCon(Vec3_t&, Vec3_t& Vel, double& Den, Boundary& bdry) {
+  Vel = bdry.inv;
+  Den = bdry.inDensity;
+}
+inline void OutFlowCon(Vec3_t&, Vec3_t& Vel, double& Den, Boundary& bdry) {
+  Vel = bdry.outv;
+  Den = bdry.outDensity;
+}
+inline void AllFlowCon(Vec3_t&, Vec3_t& Vel, double& Den, Boundary& bdry) {
+  Vel = bdry.allv;
+  Den = bdry.allDensity;
+}
 
 class Domain {
  public:
@@ -131,8 +148,8 @@ class Domain {
   Boundary BC;
   PtOut UserOutput = &OutPut;
   PtVel InCon = &InFlowCon;
-  PtVel OutCon = &InFlowCon;
-  PtVel AllCon = &InFlowCon;
+  PtVel OutCon = &OutFlowCon;
+  PtVel AllCon = &AllFlowCon;
   Vec3_t DomMax, DomMin;
   PtDom GeneralBefore = &General;
   PtDom GeneralAfter = &General;
@@ -153,7 +170,7 @@ class Domain {
   // host SoA image of the particles for the C ABI
   struct Pack {
     std::vector<int32_t> id, material, is_free, no_slip, pres_eq, shepard, les, vis_m, fail;
-    std::vector<int32_t> seepage_type, var_porosity, is_sat;
+    std::vector<int32_t> seepage_type, var_porosity, is_sat, in_out;
     std::vector<double> vec[7];     // x v va vb a nsv vxsph
     std::vector<double> sca[38];
     std::vector<double> ten[12];
@@ -163,6 +180,23 @@ class Domain {
   void pack(Pack& pk) const;
   void unpack(const Pack& pk);
   Vec3_t hook_acceleration(PtDom hook, const char* name);
+  void WholeVelocity();
+  // a user InCon / OutCon called by the library (psph_flow_fn) for one particle
+  static void flow_hook(PtVel hook, Domain* d, const double* x, double* v, double* den) {
+    Vec3_t X(x[0], x[1], x[2]), V(0, 0, 0);
+    double D = 0.0;
+    hook(X, V, D, d->BC);
+    for (int k = 0; k < 3; ++k) v[k] = V(k);
+    *den = D;
+  }
+  static void in_flow_hook(const double* x, double* v, double* den, void* u) {
+    Domain* d = static_cast<Domain*>(u);
+    flow_hook(d->InCon, d, x, v, den);
+  }
+  static void out_flow_hook(const double* x, double* v, double* den, void* u) {
+    Domain* d = static_cast<Domain*>(u);
+    flow_hook(d->OutCon, d, x, v, den);
+  }
   static void check(psph_status st, psph_ctx* ctx) {
     if (st != PSPH_OK) {
       const std::string msg = psph_last_error(ctx);
@@ -251,6 +285,7 @@ inline void Domain::pack(Pack& pk) const {
   ints(pk.seepage_type, &psph_particles::seepage_type, [](const Particle& q) { return (int)q.SeepageType; });
   ints(pk.var_porosity, &psph_particles::var_porosity, [](const Particle& q) { return q.VarPorosity ? 1 : 0; });
   ints(pk.is_sat, &psph_particles::is_sat, [](const Particle& q) { return q.IsSat ? 1 : 0; });
+  ints(pk.in_out, &psph_particles::in_out, [](const Particle& q) { return (int)q.InOut; });
   for (int f = 0; f < 7; ++f) {
     const detail::VecF& F = detail::vec_fields()[f];
     pk.vec[f].resize(3 * n);
@@ -277,11 +312,25 @@ inline void Domain::pack(Pack& pk) const {
 
 // Copies a downloaded image (original order, leavers removed) back into the
 // particle objects; particles that left the domain are deleted as
-// CheckParticleLeave does (Source/Domain.cpp:517-547).
+// CheckParticleLeave does (Source/Domain.cpp:517-547). The per-particle
+// constants come back too: an in/out-flow boundary recycles a particle with
+// the in-flow's ID, material and parameters (Source/Domain.cpp:1363-1395).
 inline void Domain::unpack(const Pack& pk) {
   const size_t n = (size_t)pk.view.n;
   for (size_t i = 0; i < n; ++i) {
     Particle& q = *Particles[i];
+    q.ID = pk.id[i];
+    q.Material = pk.material[i];
+    q.IsFree = pk.is_free[i] != 0;
+    q.NoSlip = pk.no_slip[i] != 0;
+    q.PresEq = pk.pres_eq[i];
+    q.Shepard = pk.shepard[i] != 0;
+    q.LES = pk.les[i] != 0;
+    q.VisM = (size_t)pk.vis_m[i];
+    q.Fail = (size_t)pk.fail[i];
+    q.SeepageType = (size_t)pk.seepage_type[i];
+    q.VarPorosity = pk.var_porosity[i] != 0;
+    q.InOut = (size_t)pk.in_out[i];
     for (int f = 0; f < 7; ++f) {
       const detail::VecF& F = detail::vec_fields()[f];
       for (int d = 0; d < 3; ++d) (q.*F.m)(d) = pk.vec[f][3 * i + d];
@@ -443,9 +492,23 @@ inline void Domain::DelParticles(int const& Tags) {
   Particles.swap(kept);
 }
 
+// WholeVelocity (Source/Domain.cpp:1636-1659): with BC.allv or BC.allDensity
+// set, the free particles take what AllCon gives for their position; runs on
+// the host before the upload, whose InitialChecks derives the pressure from the
+// new density.
+inline void Domain::WholeVelocity() {
+  if (!(norm(BC.allv) > 0.0 || BC.allDensity > 0.0)) return;
+  for (size_t i = 0; i < Particles.Size(); i++) {
+    Vec3_t vel(0, 0, 0);
+    double den = 0.0;
+    AllCon(Particles[i]->x, vel, den, BC);
+    if (Particles[i]->IsFree && norm(BC.allv) > 0.0) Particles[i]->v = vel;
+    if (Particles[i]->IsFree && BC.allDensity > 0.0) Particles[i]->Density = den;
+  }
+}
+
 inline void Domain::Solve(double tf, double dt, double dtOut, char const* TheFileKey, size_t maxidx) {
   std::cout << "\n--------------Solving---------------------------------------------------------------" << std::endl;
-  if (BC.InOutFlow != 0) throw new Fatal("in/out-flow boundaries are outside this build");
   const Vec3_t body = BodyForce + hook_acceleration(GeneralBefore, "GeneralBefore") +
                       hook_acceleration(GeneralAfter, "GeneralAfter");
   psph_config cfg;
@@ -472,12 +535,27 @@ inline void Domain::Solve(double tf, double dt, double dtOut, char const* TheFil
   cfg.time = Time;
   cfg.swi_type = (int)SWIType;
   cfg.fsi = FSI ? 1 : 0;
+  cfg.in_out_flow = BC.InOutFlow;
+  cfg.mass_conservation = BC.MassConservation ? 1 : 0;
+  cfg.bc_cellfac = BC.cellfac;
+  cfg.initial_dist = InitialDist;
+  cfg.in_density = BC.inDensity;
+  cfg.out_density = BC.outDensity;
+  for (int d = 0; d < 3; ++d) {
+    cfg.in_v[d] = BC.inv(d);
+    cfg.out_v[d] = BC.outv(d);
+  }
+  WholeVelocity();
 
   psph_ctx* ctx = nullptr;
   Pack pk;
   try {
     const psph_status cst = psph_create(&cfg, &ctx);
     check(cst, ctx);
+    if (BC.InOutFlow > 0) {  // user InCon / OutCon run on the host, per in/out-flow particle
+      if (InCon != &InFlowCon) check(psph_set_flow_profile(ctx, PSPH_FLOW_IN, &Domain::in_flow_hook, this), ctx);
+      if (OutCon != &OutFlowCon) check(psph_set_flow_profile(ctx, PSPH_FLOW_OUT, &Domain::out_flow_hook, this), ctx);
+    }
     pack(pk);
     check(psph_upload(ctx, &pk.view, 1), ctx);
     size_t idx_out = 1;
@@ -504,20 +582,38 @@ inline void Domain::Solve(double tf, double dt, double dtOut, char const* TheFil
       write_now(fn);
       std::cout << "\nInitial Condition has been generated\n" << std::endl;
     }
+    // the particle objects by original index (the upload's order; an in/out-flow
+    // boundary appends particles with the next indices)
+    std::vector<Particle*> by_orig;
+    for (size_t i = 0; i < Particles.Size(); ++i) by_orig.push_back(Particles[i]);
     auto copy_back = [&]() {
       const int64_t n = psph_num_particles(ctx);
       if (n < 0) check(PSPH_ERR_CUDA, ctx);
       std::vector<int64_t> orig((size_t)std::max<int64_t>(n, 1));
       check(psph_original_index(ctx, orig.data()), ctx);
-      if ((size_t)n != Particles.Size()) {  // CheckParticleLeave removed some: keep the survivors in order
-        Array<Particle*> kept;
-        std::vector<char> alive(Particles.Size(), 0);
-        for (int64_t r = 0; r < n; ++r) alive[(size_t)orig[(size_t)r]] = 1;
-        for (size_t i = 0; i < Particles.Size(); ++i) {
-          if (alive[i]) kept.Push(Particles[i]);
-          else delete Particles[i];
+      // the survivors in order (CheckParticleLeave / InFlowBCLeave removed the
+      // rest), and new objects for appended in-flow particles
+      Array<Particle*> now;
+      std::vector<char> alive(by_orig.size(), 0);
+      bool same = (size_t)n == Particles.Size();
+      for (int64_t r = 0; r < n; ++r) {
+        const size_t o = (size_t)orig[(size_t)r];
+        if (o >= by_orig.size()) {
+          by_orig.resize(o + 1, nullptr);
+          alive.resize(o + 1, 0);
         }
-        Particles.swap(kept);
+        if (!by_orig[o]) by_orig[o] = new Particle(0, Vec3_t(0, 0, 0), Vec3_t(0, 0, 0), 0.0, 1.0, 0.0, false);
+        alive[o] = 1;
+        now.Push(by_orig[o]);
+        if (same && Particles[(size_t)r] != by_orig[o]) same = false;
+      }
+      if (!same) {
+        for (size_t o = 0; o < by_orig.size(); ++o)
+          if (by_orig[o] && !alive[o]) {
+            delete by_orig[o];
+            by_orig[o] = nullptr;
+          }
+        Particles.swap(now);
         pack(pk);
       }
       pk.view.n = n;

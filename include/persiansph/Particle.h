@@ -65,6 +65,7 @@ class Particle {
   double n0 = 0.0, k = 0.0, k2 = 0.0, d = 0.0, RhoF = 0.0;
   double V;         // volume: Mass / RefDensity at construction
   double S = 0.0;   // SWIType 1: surface-erosion velocity derivative of the last step
+  size_t InOut = 0; // in/out-flow boundary: 1 in the in-flow zone, 2 in the out-flow zone
 };
 
 }  // namespace SPH

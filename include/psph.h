@@ -30,12 +30,13 @@
 extern "C" {
 #endif
 
-#define PSPH_ABI_VERSION 2
+/* 3: psph_config gained the in/out-flow settings, psph_particles in_out */
+#define PSPH_ABI_VERSION 3
 
 typedef enum psph_status {
   PSPH_OK = 0,
   PSPH_ERR_INVALID_ARGUMENT = 1, /* bad enum/size/pointer; reference aborts or throws Fatal */
-  PSPH_ERR_UNSUPPORTED = 2,      /* valid reference option outside this build (FSI, in/out-flow) */
+  PSPH_ERR_UNSUPPORTED = 2,      /* valid reference option outside this build (e.g. in/out-flow in FP32C) */
   PSPH_ERR_CUDA = 3,             /* a CUDA runtime call failed */
   PSPH_ERR_OUT_OF_MEMORY = 4,
   PSPH_ERR_NONFINITE = 5,        /* NaN/Inf found in an acceleration or density rate */
@@ -202,6 +203,24 @@ psph_status psph_original_index(psph_ctx* ctx, int64_t* out);
 
 psph_status psph_get_grid(const psph_ctx* ctx, psph_grid* grid);
 psph_status psph_get_integrator(const psph_ctx* ctx, psph_integrator* integ);
+
+/* ---- In/out-flow profiles (Domain::InCon / OutCon, Source/Domain.h:128-129) ----
+ * With in_out_flow set, InFlowBCFresh (Source/Domain.cpp:1594-1633) gives each
+ * in-flow particle the velocity and density InCon returns for its position,
+ * and each out-flow particle what OutCon returns (the velocity scaled by
+ * MassConservation's InPart/OutPart ratio and taken only when out_v or that
+ * ratio asks for it; the density only with out_density > 0). By default they
+ * are the reference's InFlowCon / OutFlowCon, the constants in_v / in_density
+ * and out_v / out_density of psph_config. A profile set here replaces one of
+ * them: fn(x, v, density, user) gets the particle's position x[3] and writes
+ * v[3] and *density (zero on entry). It runs on the calling thread inside
+ * psph_step, once per in-flow (out-flow) particle per step, in BC.InPart order
+ * (out-flow particles in original-index order). fn = NULL restores the
+ * default. Contexts with in_out_flow != 0 only (PSPH_ERR_STATE otherwise). */
+typedef void (*psph_flow_fn)(const double* x, double* v, double* density, void* user);
+#define PSPH_FLOW_IN 1
+#define PSPH_FLOW_OUT 2
+psph_status psph_set_flow_profile(psph_ctx* ctx, int which, psph_flow_fn fn, void* user);
 
 /* Neighbour pairs of the current positions, as original indices, written as
  * (first, second) int64 couples in the orientation MainNeighbourSearch would

@@ -12,8 +12,9 @@ import subprocess
 
 import numpy as np
 
-from persiansph_gb300.abi import (ALL_FIELDS, INT_FIELDS, PsphConfig, PsphGrid, PsphIntegrator, PsphParticles,
-                                  field_dtype, field_shape, particles_struct)
+from persiansph_gb300.abi import (ALL_FIELDS, INT_FIELDS, NO_FLOW_FN, PSPH_FLOW_IN, PSPH_FLOW_OUT, FlowFn, PsphConfig,
+                                  PsphGrid, PsphIntegrator, PsphParticles, field_dtype, field_shape, flow_callback,
+                                  particles_struct)
 from persiansph_gb300.particles import ParticleSet
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -62,6 +63,7 @@ def lib():
         L.psph_oracle_phase_times.argtypes = [C.c_void_p, P(C.c_double), C.c_int]
         L.psph_oracle_pair_count.argtypes = [C.c_void_p]
         L.psph_oracle_pair_count.restype = C.c_int64
+        L.psph_oracle_set_flow_profile.argtypes = [C.c_void_p, C.c_int, FlowFn, C.c_void_p]
         _lib = L
     return _lib
 
@@ -79,6 +81,7 @@ class OracleDomain:
         arrs = {f: np.ascontiguousarray(pset.get(f)) for f in ALL_FIELDS if pset.has(f)}
         s = particles_struct(arrs, pset.n)
         self._cfg = cfg
+        self._flow_cbs, self._flow_errors = {}, []
         self._h = L.psph_oracle_create(C.byref(cfg), C.byref(s), int(initial),
                                        C.byref(grid) if grid is not None else None,
                                        C.byref(integ) if integ is not None else None)
@@ -93,11 +96,28 @@ class OracleDomain:
             lib().psph_oracle_destroy(self._h)
             self._h = None
 
+    def set_flow_profile(self, which: int, fn=None):
+        """A user InCon (PSPH_FLOW_IN) or OutCon (PSPH_FLOW_OUT): fn(position)
+        -> (velocity, density); None restores the BC constants."""
+        cb = flow_callback(fn, self._flow_errors) if fn is not None else NO_FLOW_FN
+        lib().psph_oracle_set_flow_profile(self._h, int(which), cb, None)
+        self._flow_cbs[which] = cb
+
+    def use_flow_hooks(self, dom):
+        """Registers a Domain's user InCon / OutCon (None: the defaults)."""
+        for which, hook in ((PSPH_FLOW_IN, getattr(dom, "InCon", None)), (PSPH_FLOW_OUT, getattr(dom, "OutCon", None))):
+            if hook is not None:
+                self.set_flow_profile(which, lambda x, h=hook, bc=dom.BC: h(x, bc))
+
     def __del__(self):
         self.close()
 
     def step(self, nsteps: int, nthreads: int = 1):
         st = lib().psph_oracle_step(self._h, nsteps, nthreads)
+        if self._flow_errors:
+            err = self._flow_errors[0]
+            self._flow_errors.clear()
+            raise err
         if st:
             raise OracleError(f"status {st}: {lib().psph_oracle_error(self._h).decode()}")
 

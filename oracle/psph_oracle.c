@@ -72,6 +72,8 @@ struct psph_oracle {
   int64_t *in_part, n_in_part, cap_in_part; /* BC.InPart, in list order */
   int64_t n_out_part;                       /* BC.OutPart.Size() */
   int64_t next_orig;                        /* original index of the next appended particle */
+  psph_flow_fn flow_fn[3];                  /* Domain::InCon / OutCon (NULL: InFlowCon / OutFlowCon) */
+  void* flow_user[3];
   int64_t ncells;
   int nthr;
   pairvec *sm, *fsm, *nsm;
@@ -1769,15 +1771,34 @@ static int in_flow_fresh(psph_oracle* o) {
       o->n_out_part++;
     })
   }
-  for (int64_t i = 0; i < o->n_in_part; i++) set_flow_state(o, o->in_part[i], c->in_v, c->in_density, 1, 1);
+  /* InCon on BC.InPart, in list order (Source/Domain.cpp:1594-1608) */
+  for (int64_t i = 0; i < o->n_in_part; i++) {
+    const int64_t a = o->in_part[i];
+    if (o->flow_fn[PSPH_FLOW_IN]) {
+      double vel[3] = {0.0, 0.0, 0.0}, den = 0.0;
+      o->flow_fn[PSPH_FLOW_IN](&o->x[3 * a], vel, &den, o->flow_user[PSPH_FLOW_IN]);
+      set_flow_state(o, a, vel, den, 1, 1);
+    } else {
+      set_flow_state(o, a, c->in_v, c->in_density, 1, 1);
+    }
+  }
+  /* OutCon on BC.OutPart (Source/Domain.cpp:1610-1633) */
   const double temp11 = c->mass_conservation ? o->n_in_part * 1.0 / (o->n_out_part * 1.0) : 1.0;
   if (o->n_out_part > 0) {
-    double vel[3];
-    for (int d = 0; d < 3; ++d) vel[d] = temp11 * c->out_v[d];
     const int set_v = sqrt(dot3(c->out_v, c->out_v)) > 0.0 || temp11 != 1.0;
     for (int64_t a = 0; a < o->n; a++)
-      if (o->in_out[a] == 2 && FREE(a) && o->x[3 * a] >= o->out_loc)
-        set_flow_state(o, a, vel, c->out_density, set_v, c->out_density > 0.0);
+      if (o->in_out[a] == 2 && FREE(a) && o->x[3 * a] >= o->out_loc) {
+        double vel[3], den = c->out_density;
+        if (o->flow_fn[PSPH_FLOW_OUT]) {
+          double hv[3] = {0.0, 0.0, 0.0};
+          den = 0.0;
+          o->flow_fn[PSPH_FLOW_OUT](&o->x[3 * a], hv, &den, o->flow_user[PSPH_FLOW_OUT]);
+          for (int d = 0; d < 3; ++d) vel[d] = temp11 * hv[d];
+        } else {
+          for (int d = 0; d < 3; ++d) vel[d] = temp11 * c->out_v[d];
+        }
+        set_flow_state(o, a, vel, den, set_v, c->out_density > 0.0);
+      }
   }
   return PSPH_OK;
 }
@@ -2161,4 +2182,11 @@ int64_t psph_oracle_pair_count(const psph_oracle* o) { return o->pairs_done; }
 int psph_oracle_phase_times(const psph_oracle* o, double* s, int cap) {
   for (int e = 0; e < 5 && e < cap; ++e) s[e] = o->phase_s[e];
   return 5;
+}
+
+int psph_oracle_set_flow_profile(psph_oracle* o, int which, psph_flow_fn fn, void* user) {
+  if (!o || (which != PSPH_FLOW_IN && which != PSPH_FLOW_OUT)) return PSPH_ERR_INVALID_ARGUMENT;
+  o->flow_fn[which] = fn;
+  o->flow_user[which] = fn ? user : NULL;
+  return PSPH_OK;
 }

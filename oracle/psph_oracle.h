@@ -50,6 +50,11 @@ int64_t psph_oracle_pairs(psph_oracle* o, int which, int64_t* buf, int64_t cap);
  * Tests scale their per-particle tolerance by these. */
 int psph_oracle_scales(const psph_oracle* o, double* a_scale, double* drho_scale);
 
+/* A user InCon (which = PSPH_FLOW_IN) or OutCon (PSPH_FLOW_OUT) for an
+ * in/out-flow domain, with psph_set_flow_profile's meaning; fn = NULL restores
+ * the reference's default (the BC constants). */
+int psph_oracle_set_flow_profile(psph_oracle* o, int which, psph_flow_fn fn, void* user);
+
 /* In-support pairs CalcForce11 / CalcForce2233 evaluated (the pair-interaction
  * count of the metric), summed over the steps since create. */
 int64_t psph_oracle_pair_count(const psph_oracle* o);

@@ -69,6 +69,27 @@ static void BodyForceHook(SPH::Domain& dom) {
     if (dom.Particles[i]->IsFree) dom.Particles[i]->a += bf;
 }
 
+/* In/out-flow profiles written the way the reference's drivers write their
+ * InCon / OutCon hooks (Old_Tests/HydraulicJump.cpp:29-53): a hydrostatic
+ * density under a level and a velocity that varies across the channel.
+ * Config key flow_profile = H cs g (channel height, sound speed, gravity). */
+static double g_prof[3] = {0.0, 0.0, 0.0};
+
+static void ProfileInCon(Vec3_t& position, Vec3_t& Vel, double& Den, SPH::Boundary& bdry) {
+  const double H = g_prof[0], Cs = g_prof[1], G = g_prof[2];
+  const double y = position(1);
+  Vel = bdry.inv(0) * 4.0 * y * (H - y) / (H * H), 0.0, 0.0;
+  Den = bdry.inDensity * pow((1.0 + 7.0 * G * (H - y) / (Cs * Cs)), 1.0 / 7.0);
+}
+
+static void ProfileOutCon(Vec3_t& position, Vec3_t& Vel, double& Den, SPH::Boundary& bdry) {
+  const double H = g_prof[0], Cs = g_prof[1], G = g_prof[2];
+  const double y = position(1);
+  Vel = bdry.outv(0) * (0.5 + y / H), 0.0, 0.0;
+  Den = bdry.outDensity * pow((1.0 + 7.0 * G * (0.5 * H - y) / (Cs * Cs)), 1.0 / 7.0);
+  if (y > 0.5 * H) Den = bdry.outDensity;
+}
+
 static void mkdir_p(const std::string& d) { mkdir(d.c_str(), 0755); }
 
 static void cfg_line(FILE* f, const char* k, const double* v, int n) {
@@ -108,6 +129,10 @@ static int load_state(SPH::Domain& dom, const char* dir) {
   if (psph_io_cfg(dir, "out_v", v, 3) == 3) dom.BC.outv = v[0], v[1], v[2];
   dom.BC.inDensity = psph_io_cfg1(dir, "in_density", 0.0);
   dom.BC.outDensity = psph_io_cfg1(dir, "out_density", 0.0);
+  if (psph_io_cfg(dir, "flow_profile", g_prof, 3) == 3) {
+    dom.InCon = &ProfileInCon;
+    dom.OutCon = &ProfileOutCon;
+  }
   dom.MuMax = 0.0;  // left uninitialised by the Domain constructor
   dom.CsMax = 0.0;
 

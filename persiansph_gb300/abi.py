@@ -34,6 +34,9 @@ ALL_FIELDS = INT_FIELDS + VEC_FIELDS + F64_FIELDS + TEN_FIELDS
 
 # status codes (psph_status)
 PSPH_OK = 0
+# psph_set_flow_profile: which hook (Domain::InCon / OutCon) and the C callback type
+PSPH_FLOW_IN, PSPH_FLOW_OUT = 1, 2
+FlowFn = C.CFUNCTYPE(None, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p)
 STATUS_NAMES = {
     0: "PSPH_OK", 1: "PSPH_ERR_INVALID_ARGUMENT", 2: "PSPH_ERR_UNSUPPORTED", 3: "PSPH_ERR_CUDA",
     4: "PSPH_ERR_OUT_OF_MEMORY", 5: "PSPH_ERR_NONFINITE", 6: "PSPH_ERR_DT_COLLAPSE", 7: "PSPH_ERR_CFL",
@@ -172,6 +175,7 @@ def _declare(lib):
     lib.psph_original_index.argtypes = [ctx, P(C.c_int64)]
     lib.psph_get_grid.argtypes = [ctx, P(PsphGrid)]
     lib.psph_get_integrator.argtypes = [ctx, P(PsphIntegrator)]
+    lib.psph_set_flow_profile.argtypes = [ctx, C.c_int, FlowFn, C.c_void_p]
     lib.psph_pairs_export.argtypes = [ctx, C.c_int, P(C.c_int64), C.c_int64, P(C.c_int64)]
     lib.psph_enable_timing.argtypes = [ctx, C.c_int]
     lib.psph_phase_times.argtypes = [ctx, P(C.c_double), C.c_int, P(C.c_int)]
@@ -225,11 +229,29 @@ def _declare(lib):
         getattr(lib, name).restype = C.c_int
     for name in ("psph_device_check", "psph_create", "psph_set_stream", "psph_set_grid", "psph_set_integrator",
                  "psph_upload", "psph_step", "psph_download", "psph_original_index", "psph_get_grid", "psph_get_integrator",
+                 "psph_set_flow_profile",
                  "psph_pairs_export", "psph_enable_timing", "psph_phase_times", "psph_step_timed", "psph_pair_count",
                  "psph_probe_fp64_peak", "psph_pairs_export_noalloc", "psph_batch_create", "psph_batch_upload",
                  "psph_batch_step", "psph_batch_download", "psph_batch_original_index", "psph_batch_get_grid",
                  "psph_batch_get_integrator", "psph_output_request", "psph_output_write", "psph_output_flush"):
         getattr(lib, name).restype = C.c_int
+
+
+def flow_callback(fn, errors: list):
+    """A psph_flow_fn calling fn(position) -> (velocity, density), the Python
+    form of a Domain::InCon / OutCon hook; exceptions are collected in errors
+    (a C callback cannot raise) for the caller to re-raise."""
+    def cb(x, v, den, _user):
+        try:
+            vel, d = fn(np.array([x[0], x[1], x[2]]))
+            v[0], v[1], v[2] = float(vel[0]), float(vel[1]), float(vel[2])
+            den[0] = float(d)
+        except BaseException as e:  # noqa: BLE001 - re-raised by the caller
+            errors.append(e)
+    return FlowFn(cb)
+
+
+NO_FLOW_FN = C.cast(None, FlowFn)
 
 
 class PsphError(RuntimeError):

@@ -97,6 +97,8 @@ struct psph_ctx {
   void* d_flow_buf = nullptr;           // candidates / slots / recycle commands
   size_t flow_buf_bytes = 0;
   int cls_cap = 0;                      // device class-table capacity
+  psph_flow_fn flow_fn[3] = {};         // user InCon / OutCon (PSPH_FLOW_IN / PSPH_FLOW_OUT); null: the constants
+  void* flow_user[3] = {};
   std::map<std::string, int> class_index;  // class record -> index (classes added as particles are recycled)
 };
 
@@ -1122,6 +1124,47 @@ psph_status flow_upload_list(psph_ctx* c, const std::vector<long long>& v) {
   return PSPH_OK;
 }
 
+// A user InCon / OutCon on the listed particles (slot and position each):
+// called here on the host in list order, the states applied by one launch.
+psph_status flow_profile_apply(psph_ctx* c, int which, const std::vector<FlowSlot>& parts, double scale, int set_v,
+                               int set_d) {
+  std::vector<FlowState> states;
+  states.reserve(parts.size());
+  for (const FlowSlot& f : parts) {
+    if (f.slot < 0) continue;
+    const double x[3] = {f.x, f.y, f.z};
+    double vel[3] = {0.0, 0.0, 0.0}, den = 0.0;
+    c->flow_fn[which](x, vel, &den, c->flow_user[which]);
+    states.push_back(FlowState{f.slot, set_v, set_d, 0, scale * vel[0], scale * vel[1], scale * vel[2], den});
+  }
+  if (states.empty()) return PSPH_OK;
+  psph_status st;
+  if ((st = flow_buffer(c, states.size() * sizeof(FlowState)))) return st;
+  CUDA_TRY(c, cudaMemcpyAsync(c->d_flow_buf, states.data(), states.size() * sizeof(FlowState), cudaMemcpyHostToDevice,
+                              c->stream));
+  flow_apply(view(c), static_cast<const FlowState*>(c->d_flow_buf), (int)states.size(), c->stream);
+  // the host vector must outlive the copy; the buffer is reused by the next list
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return PSPH_OK;
+}
+
+// slot and position of the listed original indices (slot -1: not alive)
+psph_status flow_gather(psph_ctx* c, const std::vector<long long>& origs, std::vector<FlowSlot>& out) {
+  const size_t m = origs.size();
+  out.resize(m);
+  if (m == 0) return PSPH_OK;
+  psph_status st;
+  if ((st = flow_buffer(c, m * (sizeof(long long) + sizeof(FlowSlot)) + 64))) return st;
+  long long* d_list = static_cast<long long*>(c->d_flow_buf);
+  FlowSlot* d_slots =
+      reinterpret_cast<FlowSlot*>(static_cast<char*>(c->d_flow_buf) + ((m * sizeof(long long) + 63) & ~size_t(63)));
+  CUDA_TRY(c, cudaMemcpyAsync(d_list, origs.data(), m * sizeof(long long), cudaMemcpyHostToDevice, c->stream));
+  flow_gather_slots(view(c), d_list, (int)m, c->d_slot_of, d_slots, c->stream);
+  CUDA_TRY(c, cudaMemcpyAsync(out.data(), d_slots, m * sizeof(FlowSlot), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return PSPH_OK;
+}
+
 // InFlowBCFresh (Source/Domain.cpp:1490-1636), after the step's cell sort
 psph_status inout_fresh(psph_ctx* c) {
   const psph_config& k = c->cfgs[0];
@@ -1189,16 +1232,38 @@ psph_status inout_fresh(psph_ctx* c) {
     CUDA_TRY(c, cudaStreamSynchronize(s));
   }
   if (!c->in_part.empty()) {  // InCon on BC.InPart
-    if ((st = flow_upload_list(c, c->in_part))) return st;
-    flow_inflow_state(view(c), static_cast<const long long*>(c->d_flow_buf), (int)c->in_part.size(), c->d_slot_of,
-                      k.in_v, k.in_density, s);
+    if (c->flow_fn[PSPH_FLOW_IN]) {
+      std::vector<FlowSlot> parts;
+      if ((st = flow_gather(c, c->in_part, parts))) return st;
+      if ((st = flow_profile_apply(c, PSPH_FLOW_IN, parts, 1.0, 1, 1))) return st;
+    } else {
+      if ((st = flow_upload_list(c, c->in_part))) return st;
+      flow_inflow_state(view(c), static_cast<const long long*>(c->d_flow_buf), (int)c->in_part.size(),
+                        c->d_slot_of, k.in_v, k.in_density, s);
+    }
   }
   if (n_out > 0) {  // OutCon on BC.OutPart
     const double temp11 = k.mass_conservation ? c->in_part.size() * 1.0 / (n_out * 1.0) : 1.0;
     const double* ov = k.out_v;
-    const double vel[3] = {temp11 * ov[0], temp11 * ov[1], temp11 * ov[2]};
     const int set_v = (std::sqrt(ov[0] * ov[0] + ov[1] * ov[1] + ov[2] * ov[2]) > 0.0 || temp11 != 1.0) ? 1 : 0;
-    flow_outflow_state(view(c), n, c->out_loc, vel, k.out_density, set_v, k.out_density > 0.0 ? 1 : 0, s);
+    const int set_d = k.out_density > 0.0 ? 1 : 0;
+    if (c->flow_fn[PSPH_FLOW_OUT]) {
+      std::vector<FlowSlot> parts((size_t)n_out);
+      if ((st = flow_buffer(c, (size_t)n_out * sizeof(FlowSlot)))) return st;
+      CUDA_TRY(c, cudaMemsetAsync(c->d_flow_count, 0, sizeof(int), s));
+      flow_outflow_list(view(c), n, c->out_loc, c->d_flow_count, static_cast<FlowSlot*>(c->d_flow_buf), n_out, s);
+      int m = 0;
+      CUDA_TRY(c, cudaMemcpyAsync(&m, c->d_flow_count, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CUDA_TRY(c, cudaStreamSynchronize(s));
+      parts.resize((size_t)std::min(m, n_out));
+      if (!parts.empty())
+        CUDA_TRY(c, cudaMemcpy(parts.data(), c->d_flow_buf, parts.size() * sizeof(FlowSlot), cudaMemcpyDeviceToHost));
+      std::sort(parts.begin(), parts.end(), [](const FlowSlot& a, const FlowSlot& b) { return a.orig < b.orig; });
+      if ((st = flow_profile_apply(c, PSPH_FLOW_OUT, parts, temp11, set_v, set_d))) return st;
+    } else {
+      const double vel[3] = {temp11 * ov[0], temp11 * ov[1], temp11 * ov[2]};
+      flow_outflow_state(view(c), n, c->out_loc, vel, k.out_density, set_v, set_d, s);
+    }
   }
   CUDA_TRY(c, cudaGetLastError());
   return PSPH_OK;
@@ -1225,15 +1290,8 @@ psph_status inout_leave(psph_ctx* c) {
   std::vector<FlowSlot> add;
   std::vector<long long> released;
   if ((iof == 1 || iof == 3) && !c->in_part.empty()) {
-    const size_t m = c->in_part.size();
-    if ((st = flow_buffer(c, m * (sizeof(long long) + sizeof(FlowSlot)) + 64))) return st;
-    long long* d_list = static_cast<long long*>(c->d_flow_buf);
-    FlowSlot* d_slots = reinterpret_cast<FlowSlot*>(static_cast<char*>(c->d_flow_buf) + ((m * sizeof(long long) + 63) & ~size_t(63)));
-    CUDA_TRY(c, cudaMemcpyAsync(d_list, c->in_part.data(), m * sizeof(long long), cudaMemcpyHostToDevice, s));
-    flow_gather_slots(view(c), d_list, (int)m, c->d_slot_of, d_slots, s);
-    std::vector<FlowSlot> cur(m);
-    CUDA_TRY(c, cudaMemcpyAsync(cur.data(), d_slots, m * sizeof(FlowSlot), cudaMemcpyDeviceToHost, s));
-    CUDA_TRY(c, cudaStreamSynchronize(s));
+    std::vector<FlowSlot> cur;
+    if ((st = flow_gather(c, c->in_part, cur))) return st;
     std::vector<long long> keep;
     for (const FlowSlot& f : cur) {
       if (f.slot >= 0 && f.x > c->in_loc1) {
@@ -1816,6 +1874,15 @@ psph_status psph_get_grid(const psph_ctx* c, psph_grid* g) {
 
 psph_status psph_get_integrator(const psph_ctx* c, psph_integrator* it) {
   return integrator_impl(const_cast<psph_ctx*>(c), 0, it);
+}
+
+psph_status psph_set_flow_profile(psph_ctx* c, int which, psph_flow_fn fn, void* user) {
+  if (!c || (which != PSPH_FLOW_IN && which != PSPH_FLOW_OUT)) return PSPH_ERR_INVALID_ARGUMENT;
+  if (c->ninst != 1 || c->cfgs[0].in_out_flow <= 0)
+    return set_err(c, PSPH_ERR_STATE, "psph_set_flow_profile needs a single domain with in_out_flow set");
+  c->flow_fn[which] = fn;
+  c->flow_user[which] = fn ? user : nullptr;
+  return PSPH_OK;
 }
 
 psph_status psph_pairs_export(psph_ctx* c, int which, int64_t* pairs, int64_t cap, int64_t* n_total) {

@@ -113,6 +113,34 @@ __global__ void outflow_state_kernel(DevView v, double out_loc, double vx, doubl
   set_flow_state(v, s, vx, vy, vz, den, set_v != 0, set_d != 0);
 }
 
+// the out-flow particles (those outflow_state_kernel sets), with their
+// positions, for a user OutCon on the host
+__global__ void outflow_list_kernel(DevView v, double out_loc, int* __restrict__ count, FlowSlot* __restrict__ out,
+                                    int cap) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= v.sc->n) return;
+  const Persist& P = cur_persist(v);
+  if (v.S.cellid[s] < 0 || P.io[s] != 2 || !v.cls[P.cls[s]].is_free || !(P.X4[s].x >= out_loc)) return;
+  const int k = atomicAdd(count, 1);
+  if (k < cap) {
+    FlowSlot f;
+    f.orig = P.orig[s];
+    f.slot = s;
+    f.cls = P.cls[s];
+    const double4_32a x = P.X4[s];
+    f.x = x.x; f.y = x.y; f.z = x.z;
+    out[k] = f;
+  }
+}
+
+// the states a user InCon / OutCon returned, one per listed particle
+__global__ void apply_states_kernel(DevView v, const FlowState* __restrict__ states, int m) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= m) return;
+  const FlowState f = states[k];
+  if (f.slot >= 0 && f.slot < v.sc->n) set_flow_state(v, f.slot, f.vx, f.vy, f.vz, f.den, f.set_v != 0, f.set_d != 0);
+}
+
 // DelPart: the particles the update found outside the grid box, which leave
 // the in/out-flow state
 __global__ void leaving_kernel(DevView v, int* __restrict__ count, FlowSlot* __restrict__ out, int cap) {
@@ -208,6 +236,13 @@ void flow_gather_slots(const DevView& v, const long long* origs, int m, const in
 }
 void flow_recycle(const DevView& v, const FlowRecycle* cmds, int m, cudaStream_t st) {
   if (m > 0) recycle_kernel<<<blocks(m), kIT, 0, st>>>(v, cmds, m);
+}
+void flow_outflow_list(const DevView& v, int n, double out_loc, int* count, FlowSlot* out, int cap,
+                       cudaStream_t st) {
+  outflow_list_kernel<<<blocks(n), kIT, 0, st>>>(v, out_loc, count, out, cap);
+}
+void flow_apply(const DevView& v, const FlowState* states, int m, cudaStream_t st) {
+  if (m > 0) apply_states_kernel<<<blocks(m), kIT, 0, st>>>(v, states, m);
 }
 
 }  // namespace psph

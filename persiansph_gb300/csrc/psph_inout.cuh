@@ -29,6 +29,13 @@ struct FlowRecycle {
   double x, y, z, density;
 };
 
+// the state a user InCon / OutCon gave one particle (set_v / set_d: which
+// parts to take)
+struct FlowState {
+  int slot, set_v, set_d, pad;
+  double vx, vy, vz, den;
+};
+
 void flow_slot_of(const DevView& v, int n, int* slot_of, cudaStream_t st);
 void flow_inflow_candidates(const DevView& v, int n, int qmax, double loc1, int need_io, int* count, FlowCand* out,
                             int cap, cudaStream_t st);
@@ -42,5 +49,8 @@ void flow_leaving(const DevView& v, int n, int* count, FlowSlot* out, int cap, c
 void flow_gather_slots(const DevView& v, const long long* origs, int m, const int* slot_of, FlowSlot* out,
                        cudaStream_t st);
 void flow_recycle(const DevView& v, const FlowRecycle* cmds, int m, cudaStream_t st);
+void flow_outflow_list(const DevView& v, int n, double out_loc, int* count, FlowSlot* out, int cap,
+                       cudaStream_t st);
+void flow_apply(const DevView& v, const FlowState* states, int m, cudaStream_t st);
 
 }  // namespace psph

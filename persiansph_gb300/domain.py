@@ -76,6 +76,15 @@ class Domain:
         # UserOutput(particles) -> three per-particle arrays for the snapshot's
         # OutputName datasets; None: the reference's default OutPut (zeros)
         self.UserOutput = None
+        # In/out-flow hooks (Source/Domain.h:128-130): InCon(position, BC) and
+        # OutCon(position, BC) -> (velocity, density) for the in-flow and
+        # out-flow particles of every step, AllCon for WholeVelocity's initial
+        # state; None: the reference's InFlowCon / OutFlowCon / AllFlowCon,
+        # which return BC.inv / inDensity, BC.outv / outDensity, BC.allv /
+        # allDensity.
+        self.InCon = None
+        self.OutCon = None
+        self.AllCon = None
         # Constant acceleration on free particles applied where GeneralBefore
         # runs: the device-side form of the 1-Poiseuille.cpp UserAcc hook.
         self.BodyForce = [0.0, 0.0, 0.0]
@@ -308,6 +317,31 @@ class Domain:
         return c
 
     # -- solve ---------------------------------------------------------------
+    def WholeVelocity(self):
+        """Domain::WholeVelocity (Source/Domain.cpp:1636-1659): with BC.allv or
+        BC.allDensity set, every free particle takes the velocity and / or the
+        density AllCon gives for its position (the pressure follows from the
+        density at upload, InitialChecks' EOS)."""
+        bc = self.BC
+        set_v = math.sqrt(sum(float(a) * float(a) for a in bc.allv)) > 0.0
+        set_d = bc.allDensity > 0.0
+        if not (set_v or set_d):
+            return
+        p = self.particles
+        x, v, den = p.get("x"), p.get("v"), p.get("density")
+        free = p.get("is_free") != 0
+        for i in range(p.n):
+            if self.AllCon is not None:
+                vel, d = self.AllCon(x[i].copy(), bc)
+            else:
+                vel, d = bc.allv, bc.allDensity
+            if free[i] and set_v:
+                v[i] = [float(c) for c in vel]
+            if free[i] and set_d:
+                den[i] = float(d)
+        p.set("v", v)
+        p.set("density", den)
+
     def Solve(self, tf, dt, dtOut, TheFileKey=None, maxidx=10**9, output=None):
         """Domain::Solve (Source/Domain.cpp:1735-1797) with the step body on the GPU.
 
@@ -322,7 +356,10 @@ class Domain:
         """
         from .solver import GpuDomain
 
+        self.WholeVelocity()
         sim = GpuDomain(self.config(dt))
+        if self.BC.InOutFlow:
+            sim.use_flow_hooks(self)
         sim.upload(self.particles, initial=True)
         idx_out = 1
         tout = self.Time

@@ -518,8 +518,34 @@ def elastic_gate_2d(dx=0.01, L1=0.2, H=0.15, Tr=0.03, H1=0.15, TL_extra=0.1, wal
                      "n_gate": int((gate & ~clamp).sum()), "n_fixed": int(fixed.sum())}
 
 
+def channel_profiles(H, cs, g=9.81):
+    """User InCon / OutCon hooks written the way the reference's drivers write
+    theirs (Old_Tests/HydraulicJump.cpp:29-53): the in-flow gets a parabolic
+    velocity across a channel of height H (BC.inv[0] at its centre) and the
+    hydrostatic Tait density under the level H; the out-flow gets BC.outv[0]
+    scaled by 0.5 + y/H and the hydrostatic density under the level H/2
+    (BC.outDensity above it). Each hook maps (position, BC) to (velocity,
+    density)."""
+    def in_con(x, bc):
+        y = float(x[1])
+        vel = (bc.inv[0] * 4.0 * y * (H - y) / (H * H), 0.0, 0.0)
+        den = bc.inDensity * math.pow((1.0 + 7.0 * g * (H - y) / (cs * cs)), 1.0 / 7.0)
+        return vel, den
+
+    def out_con(x, bc):
+        y = float(x[1])
+        vel = (bc.outv[0] * (0.5 + y / H), 0.0, 0.0)
+        den = bc.outDensity * math.pow((1.0 + 7.0 * g * (0.5 * H - y) / (cs * cs)), 1.0 / 7.0)
+        if y > 0.5 * H:
+            den = bc.outDensity
+        return vel, den
+
+    return in_con, out_con
+
+
 def channel_flow_2d(dx=0.01, L=0.5, H=0.1, U=2.0, cs=20.0, flow=3, mass_conservation=False, out_v=None,
-                    out_density=None, wall_layers=3, rho=1000.0, mu=1.0e-3, alpha=0.1, scheme=0, hfac=1.2):
+                    out_density=None, wall_layers=3, rho=1000.0, mu=1.0e-3, alpha=0.1, scheme=0, hfac=1.2,
+                    profile=False):
     """2D channel with in/out-flow boundaries, the shape of Old_Tests/Current-flow.cpp:
     water between two no-slip walls, L long and H high, particles entering at
     -x with velocity (U, 0, 0) and density rho (BC.inv, BC.inDensity; the
@@ -565,8 +591,12 @@ def channel_flow_2d(dx=0.01, L=0.5, H=0.1, U=2.0, cs=20.0, flow=3, mass_conserva
         dom.BC.outv = list(out_v)
     if out_density is not None:
         dom.BC.outDensity = out_density
+    info = {"h": h, "cs": cs, "U": U, "n_fluid": int((~wall).sum()), "n_wall": int(wall.sum())}
+    if profile:  # user hooks instead of the BC constants
+        dom.InCon, dom.OutCon = channel_profiles(H, cs)
+        info["flow_profile"] = (H, cs, 9.81)
     dt = 0.25 * h / cs
-    return dom, dt, {"h": h, "cs": cs, "U": U, "n_fluid": int((~wall).sum()), "n_wall": int(wall.sum())}
+    return dom, dt, info
 
 
 def granular_ensemble(n=256, seed=0, dx=1e-3, W=0.2, aspect=(0.5, 4.0), phi_deg=(20.0, 40.0), fail=2, **kw):

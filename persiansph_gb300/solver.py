@@ -10,8 +10,8 @@ import ctypes as C
 
 import numpy as np
 
-from .abi import (ALL_FIELDS, PsphConfig, PsphError, PsphGrid, PsphIntegrator, PsphTuning, field_dtype, field_shape,
-                  load_library, particles_struct)
+from .abi import (ALL_FIELDS, NO_FLOW_FN, PSPH_FLOW_IN, PSPH_FLOW_OUT, PsphConfig, PsphError, PsphGrid, PsphIntegrator,
+                  PsphTuning, field_dtype, field_shape, flow_callback, load_library, particles_struct)
 from .particles import ParticleSet
 
 
@@ -30,11 +30,31 @@ class GpuDomain:
         if integ is not None:
             self._check(self._lib.psph_set_integrator(self._ctx, C.byref(integ)))
         self._uploaded = None
+        self._flow_cbs = {}
+        self._flow_errors = []
 
     def _check(self, st: int):
+        if self._flow_errors:
+            err = self._flow_errors[0]
+            self._flow_errors.clear()
+            raise err
         if st != 0:
             msg = self._lib.psph_last_error(self._ctx).decode() if self._ctx else ""
             raise PsphError(st, msg)
+
+    def set_flow_profile(self, which: int, fn=None):
+        """psph_set_flow_profile: fn(position) -> (velocity, density) replaces
+        the in-flow (PSPH_FLOW_IN) or out-flow (PSPH_FLOW_OUT) constants of an
+        in/out-flow domain, like a user InCon / OutCon; None restores them."""
+        cb = flow_callback(fn, self._flow_errors) if fn is not None else NO_FLOW_FN
+        self._check(self._lib.psph_set_flow_profile(self._ctx, int(which), cb, None))
+        self._flow_cbs[which] = cb  # kept alive while the context may call it
+
+    def use_flow_hooks(self, dom):
+        """Registers a Domain's user InCon / OutCon (None: the defaults)."""
+        for which, hook in ((PSPH_FLOW_IN, getattr(dom, "InCon", None)), (PSPH_FLOW_OUT, getattr(dom, "OutCon", None))):
+            if hook is not None:
+                self.set_flow_profile(which, lambda x, h=hook, bc=dom.BC: h(x, bc))
 
     def close(self):
         if self._ctx:

@@ -140,6 +140,13 @@ def channel_inflow_mc():
     return scenarios.channel_flow_2d(flow=3, mass_conservation=True, out_v=(2.0, 0.0, 0.0), scheme=1)
 
 
+def channel_profile():
+    """InOutFlow 3 with user InCon / OutCon hooks (parabolic in-flow velocity, hydrostatic densities,
+    a scaled out-flow velocity) and mass conservation, Modified Verlet."""
+    return scenarios.channel_flow_2d(flow=3, mass_conservation=True, out_v=(2.0, 0.0, 0.0), out_density=1000.0,
+                                     profile=True)
+
+
 def gate_fsi_off():
     """Water behind an elastic gate (Material 2), coupled by CalcForce12 with the FSI interpolation off."""
     return scenarios.elastic_gate_2d(fsi=False)
@@ -170,6 +177,7 @@ CASES = {
     "seep3d_erosion": (seep3d_erosion, 10, (1, 2, 10)),
     "channel_inout": (channel_inout, 40, (1, 2, 9, 10, 20, 32, 40)),
     "channel_inflow_mc": (channel_inflow_mc, 40, (1, 20, 40)),
+    "channel_profile": (channel_profile, 40, (1, 9, 10, 20, 40)),
     "gate_fsi_off": (gate_fsi_off, 32, (1, 2, 32)),
     "gate_fsi_on": (gate_fsi_on, 20, (1, 2, 20)),
 }

@@ -33,10 +33,12 @@ def main(only=()):
     for name, (builder, nsteps, dumps) in CASES.items():
         if only and name not in only:
             continue
-        dom, dt, _ = builder()
+        dom, dt, info = builder()
         cfg = dom.config(dt)
+        # user InCon / OutCon: the reference driver's profile hooks with the same parameters
+        extra = {"flow_profile": list(info["flow_profile"])} if "flow_profile" in info else None
         with tempfile.TemporaryDirectory() as d:
-            write_state_dir(os.path.join(d, "in"), cfg, dom.particles)
+            write_state_dir(os.path.join(d, "in"), cfg, dom.particles, extra)
             run_reference(os.path.join(d, "in"), os.path.join(d, "out"), nsteps, 1, [0] + list(dumps))
             out = {}
             for k in dumps:

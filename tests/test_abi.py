@@ -62,7 +62,7 @@ int main(void) {
 
 
 def test_abi_version():
-    assert abi.load_library().psph_abi_version() == 2
+    assert abi.load_library().psph_abi_version() == 3
 
 
 def test_create_reports_no_device_or_validates():

@@ -43,3 +43,41 @@ def test_cxx_solve_matches_python_path(gpu, tmp_path, precision):
     np.testing.assert_array_equal(v, ref["v"])
     np.testing.assert_array_equal(rho, ref["density"])
     np.testing.assert_array_equal(p, ref["pressure"])
+
+
+def test_cxx_inout_solve_matches_python_path(gpu, tmp_path):
+    """An in/out-flow channel with user InCon / OutCon / AllCon hooks (the
+    HydraulicJump.cpp pattern) solved through the C++ Domain::Solve and
+    through the Python Domain.Solve with the same hooks: identical states,
+    including the particles the boundary recycled and appended."""
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    exe = build(os.path.join(CXX, "channel_driver.cpp"), str(tmp_path / "channel"))
+    tf = 0.015
+    out = str(tmp_path / "state.bin")
+    subprocess.run([exe, out, repr(tf)], check=True, capture_output=True, text=True)
+    raw = np.fromfile(out, np.uint8)
+    n = int(raw[:8].view(np.int64)[0])
+    a = raw[8:8 + 8 * (8 * n + 1)].view(np.float64)
+    x, v = a[:3 * n].reshape(n, 3), a[3 * n:6 * n].reshape(n, 3)
+    rho, p, t = a[6 * n:7 * n], a[7 * n:8 * n], a[8 * n]
+    ints = raw[8 + 8 * (8 * n + 1):].view(np.int32)
+    in_out, ids = ints[:n], ints[n:2 * n]
+
+    from tests.golden.cases import channel_profile
+    dom, dt, info = channel_profile()
+    dom.AllCon = dom.InCon
+    dom.BC.allv = [info["U"], 0.0, 0.0]
+    dom.BC.allDensity = 1000.0
+    dom.particles.set("v", np.zeros((dom.particles.n, 3)))
+    dom.Solve(tf, dt, tf)
+    ps = dom.particles
+    assert n == ps.n
+    assert t == dom.Time
+    np.testing.assert_array_equal(x, ps.get("x"))
+    np.testing.assert_array_equal(v, ps.get("v"))
+    np.testing.assert_array_equal(rho, ps.get("density"))
+    np.testing.assert_array_equal(p, ps.get("pressure"))
+    np.testing.assert_array_equal(in_out, ps.get("in_out"))
+    np.testing.assert_array_equal(ids, ps.get("id"))
+    assert (in_out == 1).any() and (in_out == 2).any()

@@ -27,6 +27,7 @@ def test_inout_state_matches_reference(gpu, name):
     dom, dt, _ = builder()
     g = dict(np.load(os.path.join(GOLD, name + ".npz")))
     gd = GpuDomain(dom.config(dt))
+    gd.use_flow_hooks(dom)
     gd.upload(dom.particles, initial=True)
     prev = 0
     for k in dumps:
@@ -73,3 +74,39 @@ def test_inout_rejects_periodic_x(gpu):
     with pytest.raises(PsphError) as e:
         GpuDomain(cfg)
     assert e.value.code == 1 and "Periodic" in str(e.value)
+
+
+def test_flow_profile_errors(gpu):
+    """A user InCon that raises stops the step with its exception; a profile
+    on a domain without in/out-flow boundaries is refused."""
+    dom, dt, _ = scenarios.channel_flow_2d()
+    gd = GpuDomain(dom.config(dt))
+
+    def bad(x):
+        raise ValueError("profile failed")
+
+    gd.set_flow_profile(1, bad)
+    gd.upload(dom.particles, initial=True)
+    with pytest.raises(ValueError, match="profile failed"):
+        gd.step(1)
+    plain, dt2, _ = scenarios.dam_break_2d(dx=0.02)
+    gp = GpuDomain(plain.config(dt2))
+    with pytest.raises(PsphError) as e:
+        gp.set_flow_profile(1, lambda x: ((0.0, 0.0, 0.0), 1000.0))
+    assert e.value.code == 10
+
+
+def test_flow_profile_default_restored(gpu):
+    """Setting a profile and then None gives the default constants' trajectory."""
+    dom, dt, _ = scenarios.channel_flow_2d(flow=3, out_density=1000.0)
+    ref = GpuDomain(dom.config(dt))
+    ref.upload(dom.particles, initial=True)
+    ref.step(12)
+    gd = GpuDomain(dom.config(dt))
+    gd.set_flow_profile(1, lambda x: ((9.0, 0.0, 0.0), 1010.0))
+    gd.set_flow_profile(1, None)
+    gd.upload(dom.particles, initial=True)
+    gd.step(12)
+    a, b = ref.download_fields(("x", "density")), gd.download_fields(("x", "density"))
+    np.testing.assert_array_equal(a["x"], b["x"])
+    np.testing.assert_array_equal(a["density"], b["density"])

@@ -62,11 +62,13 @@ def test_single_step_parity_1e12(gpu, name):
     # in/out-flow boundary's lists are not part of an upload: initial state only)
     for warm in ((0,) if cfg.in_out_flow else (0, 3)):
         o = OracleDomain(cfg, dom.particles, initial=True)
+        o.use_flow_hooks(dom)
         if warm:
             o.step(warm)
         gd = continue_on_gpu(cfg, o) if warm else None
         if gd is None:
             gd = GpuDomain(cfg)
+            gd.use_flow_hooks(dom)
             gd.upload(dom.particles, initial=True)
         o.step(1)
         gd.step(1)
@@ -82,6 +84,7 @@ def test_trajectory_matches_reference(gpu, name):
     dom, dt, _ = builder()
     g = golden(name)
     gd = GpuDomain(dom.config(dt))
+    gd.use_flow_hooks(dom)
     gd.upload(dom.particles, initial=True)
     prev = 0
     for k in dumps:
