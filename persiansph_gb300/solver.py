@@ -23,6 +23,8 @@ class GpuDomain:
         self._lib = load_library()
         self._ctx = C.c_void_p()
         self.cfg = cfg
+        self._flow_cbs = {}
+        self._flow_errors = []
         st = self._lib.psph_create(C.byref(cfg), C.byref(self._ctx))
         self._check(st)
         if grid is not None:
@@ -30,8 +32,6 @@ class GpuDomain:
         if integ is not None:
             self._check(self._lib.psph_set_integrator(self._ctx, C.byref(integ)))
         self._uploaded = None
-        self._flow_cbs = {}
-        self._flow_errors = []
 
     def _check(self, st: int):
         if self._flow_errors:
