@@ -20,11 +20,14 @@
  * copied back into dom.Particles at every output time and at the end.
  *
  * Differences a driver can see:
- *  - GeneralBefore / GeneralAfter run on the host in the reference, every
- *    step. Here Solve calls each hook once on a probe copy of the particles:
- *    a hook that adds the same acceleration to every free particle and changes
- *    nothing else (the 1-Poiseuille.cpp UserAcc pattern) becomes a device-side
- *    body force; any other hook is rejected with a Fatal.
+ *  - GeneralBefore / GeneralAfter run on the host every step, where the
+ *    reference calls them (after the neighbour search; after the forces):
+ *    the particles are copied back into dom.Particles (with Time), the hook
+ *    runs, and what it changed goes back to the device (psph_patch). That
+ *    costs two copies of the particles per step; a constant acceleration is
+ *    cheaper as Domain::BodyForce, which the pair kernels add on the device.
+ *    A hook may change particle parameters (cohesion, friction angle, ...)
+ *    but not switch on a pair term no particle had (psph_patch says which).
  *  - Output: with a file key, Solve writes the reference's snapshots
  *    (WriteXDMF: <key>_Initial, then <key>_0001, ... at each output time) as
  *    <name>.bin + <name>.xmf, the same datasets as the reference's <name>.hdf5
@@ -51,6 +54,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
 #include <functional>
 #include <iostream>
 #include <utility>
@@ -179,7 +183,20 @@ class Domain {
   };
   void pack(Pack& pk) const;
   void unpack(const Pack& pk);
-  Vec3_t hook_acceleration(PtDom hook, const char* name);
+  // GeneralBefore / GeneralAfter inside a step (psph_set_step_hooks): Solve
+  // sets hook_run_ to copy the particles back, call the hook and patch them
+  std::function<void(int)> hook_run_;
+  std::exception_ptr hook_error_;
+  static int step_hook(psph_ctx*, int where, void* u) {
+    Domain* d = static_cast<Domain*>(u);
+    try {
+      d->hook_run_(where);
+      return 0;
+    } catch (...) {
+      d->hook_error_ = std::current_exception();
+      return 1;
+    }
+  }
   void WholeVelocity();
   // a user InCon / OutCon called by the library (psph_flow_fn) for one particle
   static void flow_hook(PtVel hook, Domain* d, const double* x, double* v, double* den) {
@@ -342,50 +359,6 @@ inline void Domain::unpack(const Pack& pk) {
   }
 }
 
-// The acceleration a host hook adds to every free particle, found by running
-// it once on the particles with a = 0; throws if the hook does anything else.
-inline Vec3_t Domain::hook_acceleration(PtDom hook, const char* name) {
-  if (hook == &General) return Vec3_t(0, 0, 0);
-  const size_t n = Particles.Size();
-  std::vector<Vec3_t> a0(n), x0(n), v0(n);
-  std::vector<double> rho0(n), mu0(n);
-  for (size_t i = 0; i < n; ++i) {
-    a0[i] = Particles[i]->a;
-    x0[i] = Particles[i]->x;
-    v0[i] = Particles[i]->v;
-    rho0[i] = Particles[i]->Density;
-    mu0[i] = Particles[i]->Mu;
-    Particles[i]->a = 0.0;
-  }
-  hook(*this);
-  bool ok = true, have = false;
-  Vec3_t acc(0, 0, 0);
-  for (size_t i = 0; i < n && ok; ++i) {
-    const Particle& q = *Particles[i];
-    ok = (q.x(0) == x0[i](0) && q.x(1) == x0[i](1) && q.x(2) == x0[i](2) && q.v(0) == v0[i](0) &&
-          q.v(1) == v0[i](1) && q.v(2) == v0[i](2) && q.Density == rho0[i] && q.Mu == mu0[i]);
-    if (!ok) break;
-    if (q.IsFree) {
-      if (!have) {
-        acc = q.a;
-        have = true;
-      } else {
-        ok = (q.a(0) == acc(0) && q.a(1) == acc(1) && q.a(2) == acc(2));
-      }
-    } else {
-      ok = (q.a(0) == 0.0 && q.a(1) == 0.0 && q.a(2) == 0.0);
-    }
-  }
-  if (Particles.Size() != n) ok = false;
-  for (size_t i = 0; i < std::min(n, Particles.Size()); ++i) Particles[i]->a = a0[i];
-  if (!ok)
-    throw new Fatal(
-        "%s: a host hook runs every step in the reference; on the GPU only a hook that adds one constant "
-        "acceleration to the free particles is supported (set Domain::BodyForce for that)",
-        name);
-  return acc;
-}
-
 inline void Domain::AddBoxLength(int tag, Vec3_t const& V, double Lx, double Ly, double Lz, double r, double Density,
                                  double h, int type, int rotation, bool random, bool Fixed) {
   // Source/Domain.cpp:294-495: hexagonal (type 0) or cubic (type 1) lattice
@@ -509,8 +482,7 @@ inline void Domain::WholeVelocity() {
 
 inline void Domain::Solve(double tf, double dt, double dtOut, char const* TheFileKey, size_t maxidx) {
   std::cout << "\n--------------Solving---------------------------------------------------------------" << std::endl;
-  const Vec3_t body = BodyForce + hook_acceleration(GeneralBefore, "GeneralBefore") +
-                      hook_acceleration(GeneralAfter, "GeneralAfter");
+  const Vec3_t body = BodyForce;
   psph_config cfg;
   std::memset(&cfg, 0, sizeof cfg);
   cfg.dimension = Dimension;
@@ -552,6 +524,11 @@ inline void Domain::Solve(double tf, double dt, double dtOut, char const* TheFil
   try {
     const psph_status cst = psph_create(&cfg, &ctx);
     check(cst, ctx);
+    const bool before = GeneralBefore != &General, after = GeneralAfter != &General;
+    if (before || after)  // host hooks inside every step, where the reference calls them
+      check(psph_set_step_hooks(ctx, &Domain::step_hook, this,
+                                (before ? PSPH_HOOK_BEFORE : 0) | (after ? PSPH_HOOK_AFTER : 0)),
+            ctx);
     if (BC.InOutFlow > 0) {  // user InCon / OutCon run on the host, per in/out-flow particle
       if (InCon != &InFlowCon) check(psph_set_flow_profile(ctx, PSPH_FLOW_IN, &Domain::in_flow_hook, this), ctx);
       if (OutCon != &OutFlowCon) check(psph_set_flow_profile(ctx, PSPH_FLOW_OUT, &Domain::out_flow_hook, this), ctx);
@@ -620,6 +597,25 @@ inline void Domain::Solve(double tf, double dt, double dtOut, char const* TheFil
       check(psph_download(ctx, &pk.view), ctx);
       unpack(pk);
     };
+    // a hook sees the particles and Time of that point of the step; its
+    // changes go back with psph_patch
+    hook_run_ = [&](int where) {
+      copy_back();
+      psph_integrator it;
+      check(psph_get_integrator(ctx, &it), ctx);
+      Time = it.time;
+      (where == PSPH_HOOK_BEFORE ? GeneralBefore : GeneralAfter)(*this);
+      pack(pk);
+      check(psph_patch(ctx, &pk.view), ctx);
+    };
+    auto step_check = [&](psph_status st) {
+      if (st != PSPH_OK && hook_error_) {
+        std::exception_ptr e = hook_error_;
+        hook_error_ = nullptr;
+        std::rethrow_exception(e);
+      }
+      check(st, ctx);
+    };
     while (Time < tf && idx_out <= maxidx) {
       if (Time >= tout) {
         if (OutputHook || (TheFileKey != nullptr && user_props)) copy_back();
@@ -635,7 +631,7 @@ inline void Domain::Solve(double tf, double dt, double dtOut, char const* TheFil
         tout += dtOut;
       }
       int64_t done = 0;
-      check(psph_step(ctx, (int64_t)1 << 40, std::min(tf, tout), &done), ctx);
+      step_check(psph_step(ctx, (int64_t)1 << 40, std::min(tf, tout), &done));
       psph_integrator it;
       check(psph_get_integrator(ctx, &it), ctx);
       Time = it.time;
@@ -645,9 +641,11 @@ inline void Domain::Solve(double tf, double dt, double dtOut, char const* TheFil
     copy_back();
   } catch (...) {
     psph_destroy(ctx);
+    hook_run_ = nullptr;
     throw;
   }
   psph_destroy(ctx);
+  hook_run_ = nullptr;
   std::cout << "\n--------------Solving is finished---------------------------------------------------" << std::endl;
 }
 

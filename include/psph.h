@@ -222,6 +222,42 @@ typedef void (*psph_flow_fn)(const double* x, double* v, double* density, void* 
 #define PSPH_FLOW_OUT 2
 psph_status psph_set_flow_profile(psph_ctx* ctx, int which, psph_flow_fn fn, void* user);
 
+/* ---- Host hooks inside a step (Domain::GeneralBefore / GeneralAfter) ----------
+ * The reference calls GeneralBefore after the neighbour search and
+ * GeneralAfter after the forces and the time-step bound, both on the host with
+ * the whole Domain in reach (Source/Domain.cpp:1767-1770). With a hook set,
+ * psph_step launches each step in parts and calls fn(ctx, where, user) at
+ * those points (where = PSPH_HOOK_BEFORE / PSPH_HOOK_AFTER, as selected by
+ * where_mask). Inside fn the caller reads the particles with psph_download
+ * (at PSPH_HOOK_BEFORE the accelerations are Gravity and the density rates
+ * zero, as StartAcceleration left them; at PSPH_HOOK_AFTER this step's) and
+ * writes changes back with psph_patch; psph_get_integrator gives Time. A
+ * non-zero return from fn ends psph_step with PSPH_ERR_STATE. Each hook costs a
+ * download and, when the hook patches, an upload of the particles: the slow
+ * path for hooks that touch particles every step (a constant acceleration
+ * belongs in psph_config.body_force instead). fn = NULL removes the hooks.
+ * Single-domain contexts only. */
+typedef int (*psph_hook_fn)(psph_ctx* ctx, int where, void* user);
+#define PSPH_HOOK_BEFORE 1
+#define PSPH_HOOK_AFTER 2
+psph_status psph_set_step_hooks(psph_ctx* ctx, psph_hook_fn fn, void* user, int where_mask);
+
+/* Writes particles back into a context: p holds psph_num_particles particles in
+ * psph_download's order. The non-NULL arrays among the state fields (x, v, va,
+ * vb, a, density, densitya, densityb, ddensity, pressure, mu when it varies
+ * per particle, sigma, strain, shear_stress and their histories) replace the
+ * device's values; the non-NULL per-particle parameters (mass, h, material
+ * constants, flags, as psph_upload reads them) move a particle whose
+ * parameters changed to the matching parameter set. Parameters that would
+ * change what the step computes for the whole domain (a new material, a
+ * different h where h is uniform, tensile instability, artificial viscosity,
+ * strain rates or Shepard filtering where no particle had them, another EOS
+ * where the fluid's is uniform) are refused with PSPH_ERR_UNSUPPORTED, as are
+ * parameter changes in the FP32C form or in a fluid-soil / fluid-solid domain.
+ * At PSPH_HOOK_BEFORE changed accelerations or density rates enter the step
+ * as its starting values (FP64 form; the FP32C form refuses them). */
+psph_status psph_patch(psph_ctx* ctx, const psph_particles* p);
+
 /* Neighbour pairs of the current positions, as original indices, written as
  * (first, second) int64 couples in the orientation MainNeighbourSearch would
  * list them (Source/Domain.cpp:808-945). which = 0: every candidate pair

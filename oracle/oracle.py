@@ -5,6 +5,7 @@ CPU-baseline / reference legs of bench.py, never by the product package.
 """
 from __future__ import annotations
 
+import copy
 import ctypes as C
 import json
 import os
@@ -12,9 +13,10 @@ import subprocess
 
 import numpy as np
 
-from persiansph_gb300.abi import (ALL_FIELDS, INT_FIELDS, NO_FLOW_FN, PSPH_FLOW_IN, PSPH_FLOW_OUT, FlowFn, PsphConfig,
-                                  PsphGrid, PsphIntegrator, PsphParticles, field_dtype, field_shape, flow_callback,
-                                  particles_struct)
+from persiansph_gb300.abi import (ALL_FIELDS, INT_FIELDS, NO_FLOW_FN, NO_HOOK_FN, PSPH_FLOW_IN, PSPH_FLOW_OUT,
+                                  PSPH_HOOK_AFTER, PSPH_HOOK_BEFORE, FlowFn, HookFn, PsphConfig, PsphGrid,
+                                  PsphIntegrator, PsphParticles, field_dtype, field_shape, flow_callback,
+                                  particles_struct, step_hook_callback)
 from persiansph_gb300.particles import ParticleSet
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -64,6 +66,8 @@ def lib():
         L.psph_oracle_pair_count.argtypes = [C.c_void_p]
         L.psph_oracle_pair_count.restype = C.c_int64
         L.psph_oracle_set_flow_profile.argtypes = [C.c_void_p, C.c_int, FlowFn, C.c_void_p]
+        L.psph_oracle_set_step_hooks.argtypes = [C.c_void_p, HookFn, C.c_void_p, C.c_int]
+        L.psph_oracle_patch.argtypes = [C.c_void_p, P(PsphParticles)]
         _lib = L
     return _lib
 
@@ -102,6 +106,52 @@ class OracleDomain:
         cb = flow_callback(fn, self._flow_errors) if fn is not None else NO_FLOW_FN
         lib().psph_oracle_set_flow_profile(self._h, int(which), cb, None)
         self._flow_cbs[which] = cb
+
+    def set_step_hooks(self, before=None, after=None):
+        """Domain::GeneralBefore / GeneralAfter: hook(time, particles) with the
+        particles as a ParticleSet, changed in place (or returned), written back."""
+        hooks = {}
+        if before is not None:
+            hooks[PSPH_HOOK_BEFORE] = before
+        if after is not None:
+            hooks[PSPH_HOOK_AFTER] = after
+        if not hooks:
+            lib().psph_oracle_set_step_hooks(self._h, NO_HOOK_FN, None, 0)
+            self._hook_cb = None
+            return
+
+        def run(fn):
+            pset = ParticleSet(self.n)
+            pset._arr.update(self.download())
+            out = fn(self.integrator().time, pset)
+            self.patch(out if out is not None else pset)
+
+        cb = step_hook_callback(hooks, run, self._flow_errors)
+        lib().psph_oracle_set_step_hooks(self._h, cb, None, sum(hooks))
+        self._hook_cb = cb
+
+    def use_step_hooks(self, dom):
+        """A Domain's GeneralBefore / GeneralAfter (hook(domain)), each called on a
+        shallow copy of dom holding the oracle's particles and Time."""
+        def adapt(h):
+            if h is None:
+                return None
+
+            def run(t, pset):
+                view = copy.copy(dom)
+                view.Time = t
+                view.particles = pset
+                h(view)
+                return view.particles
+            return run
+        self.set_step_hooks(adapt(getattr(dom, "GeneralBefore", None)), adapt(getattr(dom, "GeneralAfter", None)))
+
+    def patch(self, pset):
+        arrs = {f: np.ascontiguousarray(pset.get(f)) for f in ALL_FIELDS if pset.has(f)}
+        s = particles_struct(arrs, pset.n)
+        st = lib().psph_oracle_patch(self._h, C.byref(s))
+        if st:
+            raise OracleError(f"patch: status {st}")
 
     def use_flow_hooks(self, dom):
         """Registers a Domain's user InCon / OutCon (None: the defaults)."""

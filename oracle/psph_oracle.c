@@ -74,6 +74,9 @@ struct psph_oracle {
   int64_t next_orig;                        /* original index of the next appended particle */
   psph_flow_fn flow_fn[3];                  /* Domain::InCon / OutCon (NULL: InFlowCon / OutFlowCon) */
   void* flow_user[3];
+  psph_oracle_hook_fn hook_fn;              /* Domain::GeneralBefore / GeneralAfter */
+  void* hook_user;
+  int hook_mask;
   int64_t ncells;
   int nthr;
   pairvec *sm, *fsm, *nsm;
@@ -1927,11 +1930,17 @@ static int one_step(psph_oracle* o, int nthr) {
   /* FirstStep of Move_MVerlet forces ct=30 (Particle.cpp:191-195) */
   if (o->cfg.scheme == PSPH_MVERLET && o->it.first_step) o->it.ct = 30;
   main_search(o, nthr);
+  /* GeneralBefore (Source/Domain.cpp:1767) */
+  if (o->hook_fn && (o->hook_mask & PSPH_HOOK_BEFORE) && o->hook_fn(o, PSPH_HOOK_BEFORE, o->hook_user))
+    return fail(o, PSPH_ERR_STATE, "the GeneralBefore hook asked to stop the run");
   double t1 = now_s();
   primary_compute(o, nthr);
   double t2 = now_s();
   int st = last_compute(o, nthr);
   if (st) return st;
+  /* GeneralAfter (Source/Domain.cpp:1770) */
+  if (o->hook_fn && (o->hook_mask & PSPH_HOOK_AFTER) && o->hook_fn(o, PSPH_HOOK_AFTER, o->hook_user))
+    return fail(o, PSPH_ERR_STATE, "the GeneralAfter hook asked to stop the run");
   double t3 = now_s();
   st = adaptive_time_step(o);
   if (st) return st;
@@ -2188,5 +2197,30 @@ int psph_oracle_set_flow_profile(psph_oracle* o, int which, psph_flow_fn fn, voi
   if (!o || (which != PSPH_FLOW_IN && which != PSPH_FLOW_OUT)) return PSPH_ERR_INVALID_ARGUMENT;
   o->flow_fn[which] = fn;
   o->flow_user[which] = fn ? user : NULL;
+  return PSPH_OK;
+}
+
+int psph_oracle_set_step_hooks(psph_oracle* o, psph_oracle_hook_fn fn, void* user, int where_mask) {
+  if (!o) return PSPH_ERR_INVALID_ARGUMENT;
+  o->hook_fn = fn;
+  o->hook_user = fn ? user : NULL;
+  o->hook_mask = fn ? where_mask : 0;
+  return PSPH_OK;
+}
+
+/* The non-NULL arrays of p (psph_oracle_download's order and count) replace
+ * the particles' fields; k, k2 and the in/out-flow flags are left, as
+ * psph_patch leaves them. */
+int psph_oracle_patch(psph_oracle* o, const psph_particles* p) {
+  if (!o || !p || p->n != o->n) return PSPH_ERR_INVALID_ARGUMENT;
+  const int64_t n = o->n;
+#define IN_I(NAME) if (p->NAME && strcmp(#NAME, "in_out") != 0) memcpy(o->NAME, p->NAME, (size_t)n * sizeof(int32_t));
+#define IN_D(NAME) if (p->NAME && strcmp(#NAME, "k") != 0 && strcmp(#NAME, "k2") != 0) memcpy(o->NAME, p->NAME, (size_t)n * sizeof(double));
+#define IN_V(NAME) if (p->NAME) memcpy(o->NAME, p->NAME, (size_t)n * 3 * sizeof(double));
+#define IN_T(NAME) if (p->NAME) memcpy(o->NAME, p->NAME, (size_t)n * 9 * sizeof(double));
+  PSPH_INT_FIELDS(IN_I)
+  PSPH_F64_FIELDS(IN_D)
+  PSPH_VEC_FIELDS(IN_V)
+  PSPH_TEN_FIELDS(IN_T)
   return PSPH_OK;
 }

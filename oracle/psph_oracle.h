@@ -55,6 +55,15 @@ int psph_oracle_scales(const psph_oracle* o, double* a_scale, double* drho_scale
  * the reference's default (the BC constants). */
 int psph_oracle_set_flow_profile(psph_oracle* o, int which, psph_flow_fn fn, void* user);
 
+/* Domain::GeneralBefore / GeneralAfter (psph_set_step_hooks' meaning): fn runs
+ * after the neighbour search (PSPH_HOOK_BEFORE) and after the forces
+ * (PSPH_HOOK_AFTER) of every step; inside it psph_oracle_download and
+ * psph_oracle_patch read and write the particles. A non-zero return stops the
+ * step with PSPH_ERR_STATE. */
+typedef int (*psph_oracle_hook_fn)(psph_oracle* o, int where, void* user);
+int psph_oracle_set_step_hooks(psph_oracle* o, psph_oracle_hook_fn fn, void* user, int where_mask);
+int psph_oracle_patch(psph_oracle* o, const psph_particles* p);
+
 /* In-support pairs CalcForce11 / CalcForce2233 evaluated (the pair-interaction
  * count of the metric), summed over the steps since create. */
 int64_t psph_oracle_pair_count(const psph_oracle* o);

@@ -90,6 +90,42 @@ static void ProfileOutCon(Vec3_t& position, Vec3_t& Vel, double& Den, SPH::Bound
   if (y > 0.5 * H) Den = bdry.outDensity;
 }
 
+/* A GeneralAfter hook written the way the reference's soil drivers write their
+ * UserDamping (Old_Tests/Embankment.cpp:31-58): while Time < t_end the free
+ * particles of one material are damped (a -= DampS v), and once Time reaches
+ * t_change the particles with one tag get a new cohesion and friction angle.
+ * Config key damping = DampS t_end material t_change tag cohesion phi. */
+static double g_damp[7] = {0, 0, 0, 0, 0, 0, 0};
+static int g_damp_check = 0;
+
+static void DampingHook(SPH::Domain& dom) {
+  const double t = DOM_TIME(dom);
+  if (t < g_damp[1])
+    for (size_t i = 0; i < dom.Particles.Size(); i++)
+      if (dom.Particles[i]->IsFree && dom.Particles[i]->Material == (int)g_damp[2])
+        dom.Particles[i]->a -= g_damp[0] * dom.Particles[i]->v;
+  if (t >= g_damp[3] && g_damp_check == 0) {
+    for (size_t i = 0; i < dom.Particles.Size(); i++)
+      if (dom.Particles[i]->ID == (int)g_damp[4] && dom.Particles[i]->Material == (int)g_damp[2]) {
+        dom.Particles[i]->c = g_damp[5];
+        dom.Particles[i]->phi = g_damp[6];
+      }
+    g_damp_check = 1;
+  }
+}
+
+/* A GeneralBefore hook that adds a position-dependent acceleration to the
+ * free particles (a spring towards a point). Config key spring = k xc yc. */
+static double g_spring[3] = {0, 0, 0};
+
+static void SpringHook(SPH::Domain& dom) {
+  for (size_t i = 0; i < dom.Particles.Size(); i++)
+    if (dom.Particles[i]->IsFree) {
+      dom.Particles[i]->a(0) += g_spring[0] * (g_spring[1] - dom.Particles[i]->x(0));
+      dom.Particles[i]->a(1) += g_spring[0] * (g_spring[2] - dom.Particles[i]->x(1));
+    }
+}
+
 static void mkdir_p(const std::string& d) { mkdir(d.c_str(), 0755); }
 
 static void cfg_line(FILE* f, const char* k, const double* v, int n) {
@@ -129,6 +165,8 @@ static int load_state(SPH::Domain& dom, const char* dir) {
   if (psph_io_cfg(dir, "out_v", v, 3) == 3) dom.BC.outv = v[0], v[1], v[2];
   dom.BC.inDensity = psph_io_cfg1(dir, "in_density", 0.0);
   dom.BC.outDensity = psph_io_cfg1(dir, "out_density", 0.0);
+  if (psph_io_cfg(dir, "damping", g_damp, 7) == 7) dom.GeneralAfter = &DampingHook;
+  if (psph_io_cfg(dir, "spring", g_spring, 3) == 3) dom.GeneralBefore = &SpringHook;
   if (psph_io_cfg(dir, "flow_profile", g_prof, 3) == 3) {
     dom.InCon = &ProfileInCon;
     dom.OutCon = &ProfileOutCon;

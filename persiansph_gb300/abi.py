@@ -37,6 +37,9 @@ PSPH_OK = 0
 # psph_set_flow_profile: which hook (Domain::InCon / OutCon) and the C callback type
 PSPH_FLOW_IN, PSPH_FLOW_OUT = 1, 2
 FlowFn = C.CFUNCTYPE(None, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p)
+# psph_set_step_hooks: where a hook runs (Domain::GeneralBefore / GeneralAfter) and the C callback type
+PSPH_HOOK_BEFORE, PSPH_HOOK_AFTER = 1, 2
+HookFn = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, C.c_void_p)
 STATUS_NAMES = {
     0: "PSPH_OK", 1: "PSPH_ERR_INVALID_ARGUMENT", 2: "PSPH_ERR_UNSUPPORTED", 3: "PSPH_ERR_CUDA",
     4: "PSPH_ERR_OUT_OF_MEMORY", 5: "PSPH_ERR_NONFINITE", 6: "PSPH_ERR_DT_COLLAPSE", 7: "PSPH_ERR_CFL",
@@ -176,6 +179,8 @@ def _declare(lib):
     lib.psph_get_grid.argtypes = [ctx, P(PsphGrid)]
     lib.psph_get_integrator.argtypes = [ctx, P(PsphIntegrator)]
     lib.psph_set_flow_profile.argtypes = [ctx, C.c_int, FlowFn, C.c_void_p]
+    lib.psph_set_step_hooks.argtypes = [ctx, HookFn, C.c_void_p, C.c_int]
+    lib.psph_patch.argtypes = [ctx, P(PsphParticles)]
     lib.psph_pairs_export.argtypes = [ctx, C.c_int, P(C.c_int64), C.c_int64, P(C.c_int64)]
     lib.psph_enable_timing.argtypes = [ctx, C.c_int]
     lib.psph_phase_times.argtypes = [ctx, P(C.c_double), C.c_int, P(C.c_int)]
@@ -229,7 +234,7 @@ def _declare(lib):
         getattr(lib, name).restype = C.c_int
     for name in ("psph_device_check", "psph_create", "psph_set_stream", "psph_set_grid", "psph_set_integrator",
                  "psph_upload", "psph_step", "psph_download", "psph_original_index", "psph_get_grid", "psph_get_integrator",
-                 "psph_set_flow_profile",
+                 "psph_set_flow_profile", "psph_set_step_hooks", "psph_patch",
                  "psph_pairs_export", "psph_enable_timing", "psph_phase_times", "psph_step_timed", "psph_pair_count",
                  "psph_probe_fp64_peak", "psph_pairs_export_noalloc", "psph_batch_create", "psph_batch_upload",
                  "psph_batch_step", "psph_batch_download", "psph_batch_original_index", "psph_batch_get_grid",
@@ -252,6 +257,23 @@ def flow_callback(fn, errors: list):
 
 
 NO_FLOW_FN = C.cast(None, FlowFn)
+NO_HOOK_FN = C.cast(None, HookFn)
+
+
+def step_hook_callback(hooks: dict, run, errors: list):
+    """A psph_hook_fn / oracle hook calling run(hooks[where]) for the points
+    present in hooks; exceptions are collected in errors and stop the step."""
+    def cb(_ctx, where, _user):
+        fn = hooks.get(where)
+        if fn is None:
+            return 0
+        try:
+            run(fn)
+            return 0
+        except BaseException as e:  # noqa: BLE001 - re-raised by the caller
+            errors.append(e)
+            return 1
+    return HookFn(cb)
 
 
 class PsphError(RuntimeError):

@@ -99,6 +99,13 @@ struct psph_ctx {
   int cls_cap = 0;                      // device class-table capacity
   psph_flow_fn flow_fn[3] = {};         // user InCon / OutCon (PSPH_FLOW_IN / PSPH_FLOW_OUT); null: the constants
   void* flow_user[3] = {};
+  // host hooks inside a step (GeneralBefore / GeneralAfter, psph_set_step_hooks)
+  psph_hook_fn hook_fn = nullptr;
+  void* hook_user = nullptr;
+  int hook_mask = 0;
+  int in_hook = 0;                      // PSPH_HOOK_* while a hook runs
+  bool hook_set_a = false;              // the GeneralBefore hook patched accelerations or density rates
+  bool hook_set_x = false;              // ... or positions (the FP32 cell offsets follow)
   std::map<std::string, int> class_index;  // class record -> index (classes added as particles are recycled)
 };
 
@@ -428,6 +435,66 @@ psph_status create_impl(const psph_config* cfgs, int ninst, psph_ctx** out) {
   return PSPH_OK;
 }
 
+
+// The options that follow from the parameter sets: which pair terms any
+// particle needs and which constants every particle shares (the kernels take
+// those from the launch parameters).
+void derive_class_options(const std::vector<PClass>& classes, bool mixed, bool dyn_mu, Options& o) {
+  o.uniform_eos = 1;
+  o.eos_cls = -1;
+  o.uniform_h = 1;
+  o.any_av = o.any_ti = o.need_sr = o.any_shepard = 0;
+  for (size_t q = 0; q < classes.size(); ++q) {
+    const PClass& C = classes[q];
+    if (C.h != classes[0].h) o.uniform_h = 0;
+    if (C.alpha != 0.0 || C.beta != 0.0) o.any_av = 1;
+    if (C.ti > 0.0) o.any_ti = 1;
+    if (C.material == 1 && (C.t0 > 0.0 || C.les)) o.need_sr = 1;
+    if (C.shepard) o.any_shepard = 1;
+    if (C.is_free && (!mixed || C.material == 1)) {  // the fluid's EOS (walls take it from the fluid)
+      if (o.eos_cls < 0) o.eos_cls = (int)q;
+      else {
+        const PClass& E = classes[o.eos_cls];
+        if (E.pres_eq != C.pres_eq || E.cs != C.cs || E.p0 != C.p0 || E.rho0 != C.rho0) o.uniform_eos = 0;
+      }
+    }
+  }
+  if (o.eos_cls < 0) o.eos_cls = 0;
+  // two materials: a wall takes its density from its partner's EOS pair by pair
+  if (mixed) o.uniform_eos = 0;
+  // pair constants that are the same for every class: the FP32C fluid pair
+  // loop takes them from the launch parameters (the same FP32 values the class
+  // table holds, so the results are identical)
+  {
+    o.uniform_av = o.uniform_mass = 1;
+    const PClass& C0 = classes[0];
+    double m_free = -1.0, fpm_wall = -1.0;
+    for (const PClass& C : classes) {
+      if (C.alpha != C0.alpha || C.beta != C0.beta) o.uniform_av = 0;
+      double& ref = C.is_free ? m_free : fpm_wall;
+      const double val = C.is_free ? C.mass : C.fpmassc;
+      if (ref < 0.0) ref = val;
+      else if (val != ref) o.uniform_mass = 0;
+    }
+    o.alpha32 = (float)C0.alpha;
+    o.beta32 = (float)C0.beta;
+    o.m_free32 = (float)std::max(m_free, 0.0);
+    o.fpm_wall32 = (float)std::max(fpm_wall, 0.0);
+  }
+  o.uniform_mu = !dyn_mu;
+  o.mu_u = 0.0;
+  {
+    bool first = true;
+    for (const PClass& C : classes)
+      if (C.is_free) {
+        if (first) { o.mu_u = C.mu0; first = false; }
+        else if (C.mu0 != o.mu_u) o.uniform_mu = 0;
+      }
+    // zero viscosity keeps the reference's 0/0 harmonic mean (Source/Interaction.cpp:103)
+    if (!(o.mu_u > 0.0)) o.uniform_mu = 0;
+  }
+  o.inv_h = 1.0 / classes[0].h;
+}
 
 psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
   if (!c || !parts) return PSPH_ERR_INVALID_ARGUMENT;
@@ -780,57 +847,7 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
     if (gd.periodic[0] || gd.periodic[1] || gd.periodic[2]) o.any_periodic = 1;
     if (gd.periodic[0]) o.any_periodic_x = 1;
   }
-  o.any_av = o.any_ti = o.need_sr = o.any_shepard = 0;
-  for (size_t q = 0; q < c->classes.size(); ++q) {
-    const PClass& C = c->classes[q];
-    if (C.h != c->classes[0].h) o.uniform_h = 0;
-    if (C.alpha != 0.0 || C.beta != 0.0) o.any_av = 1;
-    if (C.ti > 0.0) o.any_ti = 1;
-    if (C.material == 1 && (C.t0 > 0.0 || C.les)) o.need_sr = 1;
-    if (C.shepard) o.any_shepard = 1;
-    if (C.is_free && (!mixed || C.material == 1)) {  // the fluid's EOS (walls take it from the fluid)
-      if (o.eos_cls < 0) o.eos_cls = (int)q;
-      else {
-        const PClass& E = c->classes[o.eos_cls];
-        if (E.pres_eq != C.pres_eq || E.cs != C.cs || E.p0 != C.p0 || E.rho0 != C.rho0) o.uniform_eos = 0;
-      }
-    }
-  }
-  if (o.eos_cls < 0) o.eos_cls = 0;
-  // two materials: a wall takes its density from its partner's EOS pair by pair
-  if (mixed) o.uniform_eos = 0;
-  // pair constants that are the same for every class: the FP32C fluid pair
-  // loop takes them from the launch parameters (the same FP32 values the class
-  // table holds, so the results are identical)
-  {
-    o.uniform_av = o.uniform_mass = 1;
-    const PClass& C0 = c->classes[0];
-    double m_free = -1.0, fpm_wall = -1.0;
-    for (const PClass& C : c->classes) {
-      if (C.alpha != C0.alpha || C.beta != C0.beta) o.uniform_av = 0;
-      double& ref = C.is_free ? m_free : fpm_wall;
-      const double val = C.is_free ? C.mass : C.fpmassc;
-      if (ref < 0.0) ref = val;
-      else if (val != ref) o.uniform_mass = 0;
-    }
-    o.alpha32 = (float)C0.alpha;
-    o.beta32 = (float)C0.beta;
-    o.m_free32 = (float)std::max(m_free, 0.0);
-    o.fpm_wall32 = (float)std::max(fpm_wall, 0.0);
-  }
-  o.uniform_mu = !dyn_mu;
-  o.mu_u = 0.0;
-  {
-    bool first = true;
-    for (const PClass& C : c->classes)
-      if (C.is_free) {
-        if (first) { o.mu_u = C.mu0; first = false; }
-        else if (C.mu0 != o.mu_u) o.uniform_mu = 0;
-      }
-    // zero viscosity keeps the reference's 0/0 harmonic mean (Source/Interaction.cpp:103)
-    if (!(o.mu_u > 0.0)) o.uniform_mu = 0;
-  }
-  o.inv_h = 1.0 / c->classes[0].h;
+  derive_class_options(c->classes, mixed, dyn_mu, o);
   for (int d = 0; d < 3; ++d) {
     o.gb[d] = o.gravity[d] + o.body_force[d];
     o.gravity32[d] = (float)o.gravity[d];
@@ -1365,11 +1382,58 @@ psph_status inout_leave(psph_ctx* c) {
   return PSPH_OK;
 }
 
-// Steps of an in/out-flow domain: each step's launches in two parts, the
-// host's list work between them and after (no graph: the lists decide the
-// next launches).
-psph_status inout_steps(psph_ctx* c, int64_t nsteps, long long* launched) {
+// StartAcceleration's a = Gravity and dDensity = 0 (Source/Domain.cpp:1005-1007),
+// what a GeneralBefore hook finds
+__global__ void start_accel_kernel(double4_32a* __restrict__ A4, const StepScalars* sc, double gx, double gy,
+                                   double gz) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < sc->n) A4[s] = make_double4_32a(gx, gy, gz, 0.0);
+}
+
+// The FP32 offsets from the cell origins after a GeneralBefore hook moved
+// particles (the cell sort's rule; the cells stay those of the sort)
+__global__ void offsets32_kernel(DevView v) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= v.sc->n) return;
+  const Persist& P = cur_persist(v);
+  const double4_32a xs = P.X4[s];
+  const PClass& C = v.cls[P.cls[s]];
+  const float h = (float)C.h;
+  const int cell = v.S.cellid[s];
+  if (cell >= 0) {
+    const GridDev& g = grid_of(v, C.inst);
+    const int lk = cell - g.cell_base;
+    const int cx = lk % g.nc[0], t = lk / g.nc[0], cy = t % g.nc[1], cz = t / g.nc[1];
+    v.S.OFF32[s] = make_float4((float)(xs.x - (g.blpf[0] + cx * g.cell_size[0])),
+                               (float)(xs.y - (g.blpf[1] + cy * g.cell_size[1])),
+                               (float)(v.o.dim == 3 ? xs.z - (g.blpf[2] + cz * g.cell_size[2]) : 0.0), h);
+  } else {
+    v.S.OFF32[s] = make_float4((float)xs.x, (float)xs.y, (float)xs.z, h);
+  }
+}
+
+psph_status run_hook(psph_ctx* c, int where) {
   psph_status st;
+  if ((st = sync_scalars(c))) return st;
+  c->in_hook = where;
+  const int rc = c->hook_fn(c, where, c->hook_user);
+  c->in_hook = 0;
+  if (rc != 0)
+    return set_err(c, PSPH_ERR_STATE, "the %s hook asked to stop the run (returned %d)",
+                   where == PSPH_HOOK_BEFORE ? "GeneralBefore" : "GeneralAfter", rc);
+  return PSPH_OK;
+}
+
+// Steps launched in parts, with host work between them (no graph: the host
+// decides between the parts): the in/out-flow lists (InFlowBCFresh after the
+// cell sort, InFlowBCLeave after the update) and the host hooks (GeneralBefore
+// after the neighbour search, GeneralAfter after the forces and the time-step
+// bound), in Solve's order (Source/Domain.cpp:1764-1792). With output set, the
+// first step writes the snapshot where Solve does, after GeneralAfter.
+psph_status split_steps(psph_ctx* c, int64_t nsteps, long long* launched, bool output) {
+  psph_status st;
+  const bool before = c->hook_fn && (c->hook_mask & PSPH_HOOK_BEFORE);
+  const bool after = c->hook_fn && (c->hook_mask & PSPH_HOOK_AFTER);
   for (int64_t k = 0; k < nsteps; ++k) {
     cudaStream_t s = c->stream;
     launch_begin(view(c), s);
@@ -1377,20 +1441,53 @@ psph_status inout_steps(psph_ctx* c, int64_t nsteps, long long* launched) {
     CUDA_TRY(c, cudaGetLastError());
     if ((st = sync_scalars(c))) return st;
     if (c->h_sc->all_stop) break;
-    if ((st = inout_fresh(c))) return st;
-    const DevView v = view(c);
-    launch_nlist(v, s);
-    launch_prepare(v, s);
-    launch_forces(v, s);
-    if (v.o.closure) launch_closure(v, s);
-    launch_dt(v, s);
-    launch_update(v, s);
-    launch_end(v, s);
-    CUDA_TRY(c, cudaGetLastError());
-    *launched += launches_per_step(v);
+    if (c->inout && (st = inout_fresh(c))) return st;
+    launch_nlist(view(c), s);
+    if (before) {
+      const int n = c->h_sc->n;
+      const double* gv = c->opt.gravity;
+      start_accel_kernel<<<n > 0 ? (n + 255) / 256 : 1, 256, 0, s>>>(c->S.A4, c->d_sc, gv[0], gv[1], gv[2]);
+      c->hook_set_a = c->hook_set_x = false;
+      if ((st = run_hook(c, PSPH_HOOK_BEFORE))) return st;
+      c->opt.a_from_hook = c->hook_set_a ? 1 : 0;
+      if (c->hook_set_x) offsets32_kernel<<<n > 0 ? (n + 255) / 256 : 1, 256, 0, s>>>(view(c));
+    }
+    {
+      const DevView v = view(c);
+      if (v.o.fp32) launch_prepare32(v, s);
+      else launch_prepare(v, s);
+      if (v.o.couple_soil && v.o.swi != 2) launch_saturation(v, s);
+      if (v.o.fsi) launch_fsi(v, s);
+      if (v.o.fp32) launch_forces32(v, s);
+      else launch_forces(v, s);
+      if (v.o.mixed) launch_coupling(v, s);
+      if (v.o.closure) launch_closure(v, s);
+      launch_dt(v, s);
+    }
+    c->opt.a_from_hook = 0;
+    if (after && (st = run_hook(c, PSPH_HOOK_AFTER))) return st;
+    if (output && k == 0) {  // Solve's output point (Source/Domain.cpp:1773-1788)
+      std::string e;
+      const int hi = c->inout ? (int)c->next_orig : (int)c->inst_off[1];
+      if (!output_gather(c->out, view(c), 0, hi, s, &e)) return set_err(c, PSPH_ERR_CUDA, "%s", e.c_str());
+    }
+    {
+      const DevView v = view(c);
+      launch_update(v, s);
+      launch_end(v, s);
+      CUDA_TRY(c, cudaGetLastError());
+      *launched += launches_per_step(v);
+    }
+    if (output && k == 0) {
+      std::string e;
+      const char* names[3] = {c->out_names[0].c_str(), c->out_names[1].c_str(), c->out_names[2].c_str()};
+      if (!output_commit(c->out, c->out_key.c_str(), names, nullptr, 0, &e))
+        return set_err(c, PSPH_ERR_CUDA, "%s", e.c_str());
+      *launched += 4;
+    }
     if ((st = sync_scalars(c))) return st;
     if (c->h_sc->status) break;
-    if ((st = inout_leave(c))) return st;
+    if (c->inout && (st = inout_leave(c))) return st;
   }
   return sync_scalars(c);
 }
@@ -1407,7 +1504,11 @@ psph_status step_impl(psph_ctx* c, int64_t nsteps, const double* t_stop, double 
   for (int q = 0; q < c->ninst; ++q) steps0[q] = c->h_inst[q].steps;
   for (int e = 0; e < kNumPhases; ++e) c->phase_ms[e] = 0.0;
   long long launched = 0;
-  if (c->out_requested) {
+  if (c->out_requested && (c->inout || c->hook_fn)) {
+    c->out_requested = false;
+    if ((st = split_steps(c, nsteps, &launched, true))) return st;
+    nsteps = 0;
+  } else if (c->out_requested) {
     // the output step: launched directly, the snapshot gathered between its
     // forces and its update; its copy to the host and the file writes overlap
     // the steps that follow
@@ -1426,8 +1527,8 @@ psph_status step_impl(psph_ctx* c, int64_t nsteps, const double* t_stop, double 
     if (c->h_sc->all_stop || c->h_sc->status) nsteps = 0;
   }
   if (nsteps <= 0) {
-  } else if (c->inout) {
-    if ((st = inout_steps(c, nsteps, &launched))) return st;
+  } else if (c->inout || c->hook_fn) {
+    if ((st = split_steps(c, nsteps, &launched, false))) return st;
   } else if (c->timing) {
     for (int64_t s = 0; s < nsteps; ++s) {
       enqueue_step(c);
@@ -1528,6 +1629,22 @@ __global__ void dl_gather_kernel(const double* __restrict__ src, int stride, int
   const int r = row[s];
   if (r < 0) return;
   for (int e = 0; e < width; ++e) dst[(size_t)r * width + e] = src[(size_t)s * stride + off + e];
+}
+// psph_patch: the caller's row r = row[s] back into slot s (dl_gather_kernel's reverse)
+__global__ void patch_scatter_kernel(double* __restrict__ dst, int stride, int off, int width,
+                                     const double* __restrict__ src, const int* __restrict__ row, int n) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const int r = row[s];
+  if (r < 0) return;
+  for (int e = 0; e < width; ++e) dst[(size_t)s * stride + off + e] = src[(size_t)r * width + e];
+}
+__global__ void patch_scatter_int_kernel(int* __restrict__ dst, const int* __restrict__ src,
+                                         const int* __restrict__ row, int n) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const int r = row[s];
+  if (r >= 0) dst[s] = src[r];
 }
 // a per-particle int per row
 __global__ void dl_gather_int_kernel(const int* __restrict__ src, int* __restrict__ dst, const int* __restrict__ row,
@@ -1757,6 +1874,197 @@ psph_status integrator_impl(psph_ctx* c, int q, psph_integrator* it) {
 
 // (the rows are counted on the device: the alive flags and original indices
 // of millions of particles stay there)
+// The per-particle parameters psph_patch reads, over a particle's current
+// parameter set (the conversions of psph_upload; k and k2 are read on upload
+// only, as psph_download leaves them).
+void class_overlay(PClass& C, const psph_particles* p, int64_t i, bool dyn_mu) {
+  auto d = [&](const double* a, double& f) {
+    if (a) f = a[i];
+  };
+  auto n = [&](const int32_t* a, int& f) {
+    if (a) f = a[i];
+  };
+  d(p->cs, C.cs); d(p->p0, C.p0); d(p->ref_density, C.rho0); d(p->fpmassc, C.fpmassc);
+  d(p->alpha, C.alpha); d(p->beta, C.beta);
+  if (!dyn_mu) d(p->mu, C.mu0);
+  d(p->mu_ref, C.mu_ref); d(p->t0, C.t0); d(p->bingham_m, C.bm); d(p->csmag, C.csmag); d(p->ti, C.ti);
+  d(p->tin, C.tin); d(p->ti_init_dist, C.tid); d(p->g_mod, C.g_mod); d(p->k_mod, C.k_mod); d(p->sigmay, C.sigmay);
+  d(p->cohesion, C.coh); d(p->phi, C.phi); d(p->psi, C.psi); d(p->h, C.h); d(p->mass, C.mass);
+  n(p->material, C.material); n(p->pres_eq, C.pres_eq); n(p->vis_m, C.vis_m); n(p->fail, C.fail); n(p->id, C.id);
+  auto b = [&](const int32_t* a, int& f) {
+    if (a) f = a[i] != 0;
+  };
+  b(p->is_free, C.is_free); b(p->no_slip, C.no_slip); b(p->shepard, C.shepard); b(p->les, C.les);
+  if (C.material == 3) {
+    n(p->seepage_type, C.seep_type);
+    b(p->var_porosity, C.var_por);
+    b(p->is_sat, C.is_sat);
+    d(p->n0, C.n0); d(p->d, C.dgrain); d(p->rho_f, C.rho_f); d(p->volume, C.vol);
+  }
+}
+
+psph_status patch_impl(psph_ctx* c, const psph_particles* p) {
+  if (!c || !p) return PSPH_ERR_INVALID_ARGUMENT;
+  if (!c->uploaded) return set_err(c, PSPH_ERR_STATE, "psph_patch before psph_upload");
+  if (c->ninst != 1) return set_err(c, PSPH_ERR_STATE, "psph_patch applies to single-domain contexts");
+  psph_status st;
+  int64_t m = 0;
+  if ((st = download_rows(c, 0, &m))) return st;
+  if (p->n != m)
+    return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "psph_patch got %lld particles, the context holds %lld",
+                   (long long)p->n, (long long)m);
+  if (m == 0) return PSPH_OK;
+  const int n = c->h_sc->n;
+  const Persist& P = c->h_sc->buf ? c->PB : c->PA;
+  const Options& o = c->opt;
+  const bool lf = (o.scheme == PSPH_LEAPFROG);
+  cudaStream_t s = c->stream;
+  const size_t N = (size_t)c->ncap;
+  const int nb = n > 0 ? (n + 255) / 256 : 1;
+  // accelerations and density rates at GeneralBefore are the step's starting
+  // values: unchanged ones (Gravity, 0) need nothing
+  bool set_a = p->a || p->ddensity;
+  if (set_a && c->in_hook == PSPH_HOOK_BEFORE) {
+    bool same = true;
+    for (int64_t r = 0; r < m && same; ++r) {
+      if (p->a)
+        for (int k = 0; k < 3; ++k) same = same && p->a[3 * r + k] == o.gravity[k];
+      if (p->ddensity) same = same && p->ddensity[r] == 0.0;
+    }
+    if (same) {
+      set_a = false;
+    } else if (o.fp32) {
+      return set_err(c, PSPH_ERR_UNSUPPORTED,
+                     "a GeneralBefore hook changed accelerations or density rates: the FP32C pair kernels start "
+                     "them from Gravity (use the FP64 form, or psph_config.body_force for a constant acceleration)");
+    } else {
+      c->hook_set_a = true;
+    }
+  }
+  if (p->x && c->in_hook == PSPH_HOOK_BEFORE) c->hook_set_x = true;
+  struct F { const double* in; double* dev; int stride, off, width; };
+  auto d4 = [](double4_32a* q) { return reinterpret_cast<double*>(q); };
+  const F fields[] = {
+      {p->x, d4(P.X4), 4, 0, 3}, {p->density, d4(P.X4), 4, 3, 1},
+      {p->v, d4(P.V4), 4, 0, 3}, {p->pressure, d4(P.V4), 4, 3, 1},
+      {lf ? p->va : p->vb, d4(P.H4), 4, 0, 3}, {lf ? p->densitya : p->densityb, d4(P.H4), 4, 3, 1},
+      {lf ? p->vb : nullptr, d4(P.H4b), 4, 0, 3}, {lf ? p->densityb : nullptr, d4(P.H4b), 4, 3, 1},
+      {set_a ? p->a : nullptr, d4(c->S.A4), 4, 0, 3}, {set_a ? p->ddensity : nullptr, d4(c->S.A4), 4, 3, 1},
+      {o.dyn_mu ? p->mu : nullptr, P.mu, 1, 0, 1},
+      {p->sigma, P.sigma, 9, 0, 9}, {p->strain, P.strain, 9, 0, 9}, {p->shear_stress, P.shear, 9, 0, 9},
+      {lf ? p->sigmaa : p->sigmab, P.sigma_h, 9, 0, 9}, {lf ? p->straina : p->strainb, P.strain_h, 9, 0, 9},
+      {lf ? p->shear_stressa : p->shear_stressb, P.shear_h, 9, 0, 9},
+  };
+  if (c->dl_width < 9) {
+    if ((st = dalloc(c, &c->dl_buf, N * 9))) return st;
+    c->dl_width = 9;
+  }
+  for (const F& f : fields) {
+    if (!f.in || !f.dev) continue;
+    CUDA_TRY(c, cudaMemcpyAsync(c->dl_buf, f.in, (size_t)m * f.width * sizeof(double), cudaMemcpyHostToDevice, s));
+    patch_scatter_kernel<<<nb, 256, 0, s>>>(f.dev, f.stride, f.off, f.width, c->dl_buf, c->dl_row, n);
+  }
+  CUDA_TRY(c, cudaGetLastError());
+
+  // per-particle parameters: each particle's set, found or added
+  std::vector<int> cur((size_t)m), next((size_t)m);
+  {
+    int* dcls = reinterpret_cast<int*>(c->dl_buf);
+    dl_gather_int_kernel<<<nb, 256, 0, s>>>(P.cls, dcls, c->dl_row, n);
+    CUDA_TRY(c, cudaMemcpyAsync(cur.data(), dcls, (size_t)m * sizeof(int), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(c, cudaStreamSynchronize(s));
+  }
+  if (c->class_index.empty())
+    for (size_t q = 0; q < c->classes.size(); ++q)
+      c->class_index.emplace(std::string((const char*)&c->classes[q], sizeof(PClass)), (int)q);
+  const size_t ncls0 = c->classes.size();
+  bool changed = false;
+  int last_in = -1, last_out = -1;
+  PClass last_rec;
+  std::memset(&last_rec, 0, sizeof last_rec);
+  const bool has_params =
+      p->cs || p->p0 || p->ref_density || p->fpmassc || p->alpha || p->beta || (!o.dyn_mu && p->mu) || p->mu_ref ||
+      p->t0 || p->bingham_m || p->csmag || p->ti || p->tin || p->ti_init_dist || p->g_mod || p->k_mod ||
+      p->sigmay || p->cohesion || p->phi || p->psi || p->h || p->mass || p->material || p->pres_eq || p->vis_m ||
+      p->fail || p->id || p->is_free || p->no_slip || p->shepard || p->les || p->seepage_type ||
+      p->var_porosity || p->is_sat || p->n0 || p->d || p->rho_f || p->volume;
+  for (int64_t r = 0; has_params && r < m; ++r) {
+    PClass C = c->classes[(size_t)cur[(size_t)r]];
+    class_overlay(C, p, r, o.dyn_mu != 0);
+    int id;
+    if (last_out >= 0 && cur[(size_t)r] == last_in && std::memcmp(&C, &last_rec, sizeof C) == 0) {
+      id = last_out;
+    } else {
+      const std::string key((const char*)&C, sizeof(PClass));
+      auto it = c->class_index.find(key);
+      if (it != c->class_index.end()) {
+        id = it->second;
+      } else {
+        id = (int)c->classes.size();
+        if (id >= 65535) return set_err(c, PSPH_ERR_UNSUPPORTED, "more than 65535 distinct particle parameter sets");
+        c->classes.push_back(C);
+        c->class_index.emplace(key, id);
+      }
+      last_in = cur[(size_t)r];
+      last_out = id;
+      last_rec = C;
+    }
+    next[(size_t)r] = id;
+    changed = changed || id != cur[(size_t)r];
+  }
+  if (changed) {
+    // the step's kernels and buffers were chosen for the parameter sets of the
+    // upload: a change that alters any of those choices is refused
+    auto refuse = [&](const char* why) {
+      c->classes.resize(ncls0);
+      c->class_index.clear();
+      return set_err(c, PSPH_ERR_UNSUPPORTED, "psph_patch: changed particle parameters %s", why);
+    };
+    if (o.fp32) return refuse("in the FP32C form");
+    if (o.mixed) return refuse("in a domain of two materials");
+    int mats0 = 0, mats1 = 0;
+    for (size_t q = 0; q < c->classes.size(); ++q) (q < ncls0 ? mats0 : mats1) |= 1 << c->classes[q].material;
+    if (mats1 & ~mats0) return refuse("introduce a material the domain did not have");
+    for (size_t q = ncls0; q < c->classes.size(); ++q) c->classes[q].inst = 0;
+    Options o1 = o;
+    derive_class_options(c->classes, false, o.dyn_mu != 0, o1);
+    if (o1.uniform_h != o.uniform_h || o1.inv_h != o.inv_h) return refuse("make h differ where it was uniform");
+    if (o1.any_av != o.any_av) return refuse("switch on artificial viscosity where no particle had it");
+    if (o1.any_ti != o.any_ti) return refuse("switch on tensile instability where no particle had it");
+    if (o1.need_sr != o.need_sr) return refuse("ask for strain rates (T0 or LES) where no particle did");
+    if (o1.any_shepard != o.any_shepard) return refuse("switch on Shepard filtering where no particle had it");
+    if (o1.uniform_eos != o.uniform_eos || o1.eos_cls != o.eos_cls)
+      return refuse("give the fluid a second equation of state");
+    if (o1.uniform_mu != o.uniform_mu || o1.mu_u != o.mu_u)
+      return refuse("change a viscosity every free particle shared");
+    // the grown table (each set's derived constants recomputed on the device)
+    if ((int)c->classes.size() > c->cls_cap) {
+      PClass* grown = nullptr;
+      const int cap = std::max((int)c->classes.size(), 2 * c->cls_cap);
+      if ((st = dalloc(c, &grown, (size_t)cap))) return st;
+      c->d_cls = grown;
+      c->cls_cap = cap;
+    }
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_cls, c->classes.data(), c->classes.size() * sizeof(PClass),
+                                cudaMemcpyHostToDevice, s));
+    launch_class_constants(c->d_cls, (int)c->classes.size(), o.dim, s);
+    c->opt.nclasses = (int)c->classes.size();
+    int* dnext = reinterpret_cast<int*>(c->dl_buf);
+    CUDA_TRY(c, cudaMemcpyAsync(dnext, next.data(), (size_t)m * sizeof(int), cudaMemcpyHostToDevice, s));
+    patch_scatter_int_kernel<<<nb, 256, 0, s>>>(P.cls, dnext, c->dl_row, n);
+    if (c->graph) {  // the launches hold the class table: capture the step again
+      cudaGraphExecDestroy(c->graph);
+      c->graph = nullptr;
+    }
+  } else if (c->classes.size() > ncls0) {
+    c->classes.resize(ncls0);  // sets looked up but unused
+    c->class_index.clear();
+  }
+  CUDA_TRY(c, cudaStreamSynchronize(s));
+  CUDA_TRY(c, cudaGetLastError());
+  return PSPH_OK;
+}
+
 int64_t num_particles_impl(psph_ctx* c, int q) {
   if (!c || !c->uploaded || q < 0 || q >= c->ninst) return 0;
   int64_t m = 0;
@@ -1875,6 +2183,20 @@ psph_status psph_get_grid(const psph_ctx* c, psph_grid* g) {
 psph_status psph_get_integrator(const psph_ctx* c, psph_integrator* it) {
   return integrator_impl(const_cast<psph_ctx*>(c), 0, it);
 }
+
+psph_status psph_set_step_hooks(psph_ctx* c, psph_hook_fn fn, void* user, int where_mask) {
+  if (!c) return PSPH_ERR_INVALID_ARGUMENT;
+  if (fn && (where_mask & ~(PSPH_HOOK_BEFORE | PSPH_HOOK_AFTER)))
+    return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "where_mask takes PSPH_HOOK_BEFORE and PSPH_HOOK_AFTER");
+  if (c->ninst != 1) return set_err(c, PSPH_ERR_STATE, "step hooks need a single-domain context");
+  if (c->in_hook) return set_err(c, PSPH_ERR_STATE, "psph_set_step_hooks inside a hook");
+  c->hook_fn = fn;
+  c->hook_user = fn ? user : nullptr;
+  c->hook_mask = fn ? where_mask : 0;
+  return PSPH_OK;
+}
+
+psph_status psph_patch(psph_ctx* c, const psph_particles* p) { return patch_impl(c, p); }
 
 psph_status psph_set_flow_profile(psph_ctx* c, int which, psph_flow_fn fn, void* user) {
   if (!c || (which != PSPH_FLOW_IN && which != PSPH_FLOW_OUT)) return PSPH_ERR_INVALID_ARGUMENT;
@@ -2192,8 +2514,9 @@ psph_status psph_output_write(psph_ctx* c, const char* file_key, const char* con
       if (p) std::copy(p, p + m, props.begin() + (size_t)k * m);
     }
   }
-  if (!output_gather(c->out, view(c), 0, (int)c->inst_off[1], c->stream, &e))
-    return set_err(c, PSPH_ERR_CUDA, "%s", e.c_str());
+  // (an in/out-flow domain's appended particles take original indices past the upload's)
+  const int hi = c->inout ? (int)c->next_orig : (int)c->inst_off[1];
+  if (!output_gather(c->out, view(c), 0, hi, c->stream, &e)) return set_err(c, PSPH_ERR_CUDA, "%s", e.c_str());
   const char* nm[3] = {c->out_names[0].c_str(), c->out_names[1].c_str(), c->out_names[2].c_str()};
   if (!output_commit(c->out, c->out_key.c_str(), nm, props.empty() ? nullptr : props.data(), m, &e) ||
       !output_flush(c->out, &e))

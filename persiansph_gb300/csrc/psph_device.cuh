@@ -122,6 +122,8 @@ struct Options {
   double xsph, sqrt_h_a;
   double gravity[3], body_force[3];
   double gb[3];       // gravity + body force (the sum every pair kernel starts from)
+  int a_from_hook;    // FP64 pair kernels start from this step's A4 (set by a GeneralBefore
+                      // hook, Source/Domain.cpp:1767) instead of Gravity
   // FP32 copies for the FP32C kernels, converted once on the host (a
   // double-to-float conversion on the device runs on the FP64 pipe)
   float inv_h32, mu_u32, xsph32, sqrt_h_a32, gravity32[3];

@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
     active = run && CT[ci_cls].is_free;
     cell = v.S.cellid[i];
     if (run && !active) {
-      v.S.A4[i] = make_double4_32a(o.gravity[0], o.gravity[1], o.gravity[2], 0.0);
+      if (!o.a_from_hook) v.S.A4[i] = make_double4_32a(o.gravity[0], o.gravity[1], o.gravity[2], 0.0);
       v.S.zwab[i] = 1.0;
       if (v.S.s_acc) v.S.s_acc[i] = 0.0;
     }
@@ -335,6 +335,13 @@ __global__ void __launch_bounds__(kFT) forces_fluid_kernel(DevView v) {
   double ax = o.gravity[0] + o.body_force[0], ay = o.gravity[1] + o.body_force[1],
          az = o.gravity[2] + o.body_force[2];
   double drho = 0.0, zw = 0.0, sd = 0.0, xs0 = 0.0, xs1 = 0.0, xs2 = 0.0;
+  if (o.a_from_hook && active) {  // StartAcceleration's values as a GeneralBefore hook left them
+    const double4_32a a0 = v.S.A4[i];
+    ax = a0.x + o.body_force[0];
+    ay = a0.y + o.body_force[1];
+    az = a0.z + o.body_force[2];
+    drho = a0.w;
+  }
   double sr0 = 0.0, sr1 = 0.0, sr2 = 0.0, sr4 = 0.0, sr5 = 0.0, sr8 = 0.0;
   double w01 = 0.0, w02 = 0.0, w12 = 0.0;  // antisymmetric counterpart of the strain-rate sums (closure)
   double ss = 0.0;  // SWIType 1: the surface-erosion velocity derivative S
@@ -636,7 +643,7 @@ __global__ void __launch_bounds__(kFT) forces_solid_kernel(DevView v) {
     active = run && CT[ci_cls].is_free;
     cell = v.S.cellid[i];
     if (run && !active) {
-      v.S.A4[i] = make_double4_32a(o.gravity[0], o.gravity[1], o.gravity[2], 0.0);
+      if (!o.a_from_hook) v.S.A4[i] = make_double4_32a(o.gravity[0], o.gravity[1], o.gravity[2], 0.0);
       v.S.zwab[i] = 1.0;
       if (v.S.s_acc) v.S.s_acc[i] = 0.0;
     }
@@ -657,6 +664,13 @@ __global__ void __launch_bounds__(kFT) forces_solid_kernel(DevView v) {
   double ax = o.gravity[0] + o.body_force[0], ay = o.gravity[1] + o.body_force[1],
          az = o.gravity[2] + o.body_force[2];
   double drho = 0.0, zw = 0.0, sd = 0.0, xs0 = 0.0, xs1 = 0.0, xs2 = 0.0;
+  if (o.a_from_hook && active) {  // StartAcceleration's values as a GeneralBefore hook left them
+    const double4_32a a0 = v.S.A4[i];
+    ax = a0.x + o.body_force[0];
+    ay = a0.y + o.body_force[1];
+    az = a0.z + o.body_force[2];
+    drho = a0.w;
+  }
   double sr[6] = {0, 0, 0, 0, 0, 0}, rr[3] = {0, 0, 0};  // sr: 00 01 02 11 12 22; rr: 01 02 12
   const bool any_periodic = g.periodic[0] | g.periodic[1] | g.periodic[2];
   const double I22 = (DIM == 2) ? 0.0 : 1.0;  // Domain::I (Source/Domain.cpp:1665)

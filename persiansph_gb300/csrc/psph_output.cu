@@ -28,6 +28,8 @@
 #include <thread>
 #include <vector>
 
+#include <algorithm>
+
 #include "psph_output.cuh"
 
 namespace psph {
@@ -202,6 +204,7 @@ struct OutputWriter {
   char* h_stage = nullptr;   // pinned host copy
   size_t bytes = 0;
   int ncap = 0;
+  int idx_cap = 0;  // entries of the per-original-index flag / rank arrays
   int* d_flag = nullptr;     // ncap + 1
   int* d_rank = nullptr;     // ncap + 1
   int* d_bs = nullptr;       // scan block sums
@@ -236,7 +239,9 @@ void writer_loop(OutputWriter* w) {
   }
 }
 
-bool ensure(OutputWriter* w, int ncap, std::string* err) {
+// Buffers for ncap particles whose original indices span len values (more
+// than ncap once an in/out-flow boundary has appended particles).
+bool ensure(OutputWriter* w, int ncap, int len, std::string* err) {
   auto fail = [&](const char* what, cudaError_t ce) {
     *err = std::string(what) + ": " + cudaGetErrorString(ce);
     return false;
@@ -249,23 +254,28 @@ bool ensure(OutputWriter* w, int ncap, std::string* err) {
       return fail("event", ce);
     w->th = std::thread(writer_loop, w);
   }
-  if (w->ncap >= ncap && w->d_stage) return true;
-  const size_t bytes = kHeader + (size_t)unit(kNumSets) * 4 * (size_t)ncap;
-  cudaFree(w->d_stage);
-  cudaFreeHost(w->h_stage);
-  cudaFree(w->d_flag);
-  cudaFree(w->d_rank);
-  cudaFree(w->d_bs);
-  w->d_stage = w->h_stage = nullptr;
-  w->d_flag = w->d_rank = w->d_bs = nullptr;
-  if ((ce = cudaMalloc(&w->d_stage, bytes)) != cudaSuccess) return fail("snapshot staging buffer", ce);
-  if ((ce = cudaMallocHost(&w->h_stage, bytes)) != cudaSuccess) return fail("snapshot host buffer", ce);
-  if ((ce = cudaMalloc(&w->d_flag, sizeof(int) * ((size_t)ncap + 1))) != cudaSuccess ||
-      (ce = cudaMalloc(&w->d_rank, sizeof(int) * ((size_t)ncap + 1))) != cudaSuccess ||
-      (ce = cudaMalloc(&w->d_bs, sizeof(int) * ((size_t)ncap / 1024 + 2))) != cudaSuccess)
-    return fail("snapshot row buffers", ce);
-  w->bytes = bytes;
-  w->ncap = ncap;
+  if (!(w->ncap >= ncap && w->d_stage)) {
+    const size_t bytes = kHeader + (size_t)unit(kNumSets) * 4 * (size_t)ncap;
+    cudaFree(w->d_stage);
+    cudaFreeHost(w->h_stage);
+    w->d_stage = w->h_stage = nullptr;
+    if ((ce = cudaMalloc(&w->d_stage, bytes)) != cudaSuccess) return fail("snapshot staging buffer", ce);
+    if ((ce = cudaMallocHost(&w->h_stage, bytes)) != cudaSuccess) return fail("snapshot host buffer", ce);
+    w->bytes = bytes;
+    w->ncap = ncap;
+  }
+  const int idx = std::max(ncap, len);
+  if (!(w->idx_cap >= idx && w->d_flag)) {
+    cudaFree(w->d_flag);
+    cudaFree(w->d_rank);
+    cudaFree(w->d_bs);
+    w->d_flag = w->d_rank = w->d_bs = nullptr;
+    if ((ce = cudaMalloc(&w->d_flag, sizeof(int) * ((size_t)idx + 1))) != cudaSuccess ||
+        (ce = cudaMalloc(&w->d_rank, sizeof(int) * ((size_t)idx + 1))) != cudaSuccess ||
+        (ce = cudaMalloc(&w->d_bs, sizeof(int) * ((size_t)idx / 1024 + 2))) != cudaSuccess)
+      return fail("snapshot row buffers", ce);
+    w->idx_cap = idx;
+  }
   return true;
 }
 }  // namespace
@@ -307,7 +317,7 @@ void output_writer_destroy(OutputWriter* w) {
 }
 
 bool output_gather(OutputWriter* w, const DevView& v, int lo, int hi, cudaStream_t st, std::string* err) {
-  if (!ensure(w, v.ncap, err)) return false;
+  if (!ensure(w, v.ncap, hi - lo, err)) return false;
   // the staging buffer of the previous output must have left for the host
   if (w->copy_pending) cudaStreamWaitEvent(st, w->copied, 0);
   const int len = hi - lo, nb = (v.ncap + 255) / 256;

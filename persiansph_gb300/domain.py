@@ -351,8 +351,12 @@ class Domain:
         the device after the output step's forces; a UserOutput(particle_set)
         returning three arrays runs on the host on the particles downloaded at
         the output time. `output(domain, idx)` (optional) is called at each
-        output time with the particles downloaded into `self.particles`. User
-        hooks other than the constant BodyForce are rejected.
+        output time with the particles downloaded into `self.particles`.
+        GeneralBefore(domain) / GeneralAfter(domain) run on the host inside
+        every step, where the reference calls them, with `self.particles` and
+        `self.Time` the context's at that point; what they change is written
+        back (the per-step slow path; BodyForce is the device-side constant
+        acceleration).
         """
         from .solver import GpuDomain
 
@@ -360,10 +364,11 @@ class Domain:
         sim = GpuDomain(self.config(dt))
         if self.BC.InOutFlow:
             sim.use_flow_hooks(self)
+        if self.GeneralBefore is not None or self.GeneralAfter is not None:
+            sim.use_step_hooks(self, live=True)
         sim.upload(self.particles, initial=True)
         idx_out = 1
         tout = self.Time
-        hooks = self.GeneralBefore is not None or self.GeneralAfter is not None
         user = getattr(self, "UserOutput", None)
         names = list(self.OutputName)
 
@@ -387,8 +392,6 @@ class Domain:
                         sim.request_output(fn, names)
                 idx_out += 1
                 tout += dtOut
-            if hooks:
-                raise Fatal("GeneralBefore/GeneralAfter host hooks: use Domain.BodyForce for device-side forcing")
             sim.step(1 << 30, t_stop=min(tf, tout))
         sim.flush_output()
         self.particles = sim.download(self.particles)

@@ -518,6 +518,43 @@ def elastic_gate_2d(dx=0.01, L1=0.2, H=0.15, Tr=0.03, H1=0.15, TL_extra=0.1, wal
                      "n_gate": int((gate & ~clamp).sum()), "n_fixed": int(fixed.sum())}
 
 
+def soil_damping_hook(damp, t_end, material, t_change, tag, cohesion, phi):
+    """A GeneralAfter hook in the style of the reference's soil drivers
+    (Old_Tests/Embankment.cpp:31-58, UserDamping): while Time < t_end the free
+    particles of `material` are damped (a -= damp v); from t_change on, the
+    particles with ID `tag` of that material take the given cohesion and
+    friction angle (radians). Takes the Domain, as the reference's hooks do."""
+    def hook(dom):
+        p = dom.particles
+        mat = p.get("material")
+        if dom.Time < t_end:
+            sel = (p.get("is_free") != 0) & (mat == material)
+            a, v = p.get("a"), p.get("v")
+            a[sel] -= damp * v[sel]
+            p.set("a", a)
+        if dom.Time >= t_change:
+            sel = (p.get("id") == tag) & (mat == material)
+            c, ph = p.get("cohesion"), p.get("phi")
+            c[sel] = cohesion
+            ph[sel] = phi
+            p.set("cohesion", c)
+            p.set("phi", ph)
+    return hook
+
+
+def spring_hook(k, xc, yc):
+    """A GeneralBefore hook adding a position-dependent acceleration to the free
+    particles: a += k (centre - x) in x and y."""
+    def hook(dom):
+        p = dom.particles
+        free = p.get("is_free") != 0
+        a, x = p.get("a"), p.get("x")
+        a[free, 0] += k * (xc - x[free, 0])
+        a[free, 1] += k * (yc - x[free, 1])
+        p.set("a", a)
+    return hook
+
+
 def channel_profiles(H, cs, g=9.81):
     """User InCon / OutCon hooks written the way the reference's drivers write
     theirs (Old_Tests/HydraulicJump.cpp:29-53): the in-flow gets a parabolic

@@ -6,12 +6,14 @@ non-zero status raises `PsphError` (the reference throws `Fatal` there).
 """
 from __future__ import annotations
 
+import copy
 import ctypes as C
 
 import numpy as np
 
-from .abi import (ALL_FIELDS, NO_FLOW_FN, PSPH_FLOW_IN, PSPH_FLOW_OUT, PsphConfig, PsphError, PsphGrid, PsphIntegrator,
-                  PsphTuning, field_dtype, field_shape, flow_callback, load_library, particles_struct)
+from .abi import (ALL_FIELDS, NO_FLOW_FN, NO_HOOK_FN, PSPH_FLOW_IN, PSPH_FLOW_OUT, PSPH_HOOK_AFTER, PSPH_HOOK_BEFORE,
+                  PsphConfig, PsphError, PsphGrid, PsphIntegrator, PsphTuning, field_dtype, field_shape, flow_callback,
+                  load_library, particles_struct, step_hook_callback)
 from .particles import ParticleSet
 
 
@@ -49,6 +51,55 @@ class GpuDomain:
         cb = flow_callback(fn, self._flow_errors) if fn is not None else NO_FLOW_FN
         self._check(self._lib.psph_set_flow_profile(self._ctx, int(which), cb, None))
         self._flow_cbs[which] = cb  # kept alive while the context may call it
+
+    def set_step_hooks(self, before=None, after=None):
+        """psph_set_step_hooks: host hooks inside every step, where the reference
+        calls GeneralBefore (after the neighbour search) and GeneralAfter (after
+        the forces). Each is hook(time, particles) with the particles downloaded
+        into a ParticleSet; it changes them in place (or returns a replacement)
+        and the result is written back with psph_patch. None removes a hook."""
+        hooks = {}
+        if before is not None:
+            hooks[PSPH_HOOK_BEFORE] = before
+        if after is not None:
+            hooks[PSPH_HOOK_AFTER] = after
+        if not hooks:
+            self._check(self._lib.psph_set_step_hooks(self._ctx, NO_HOOK_FN, None, 0))
+            self._hook_cb = None
+            return
+
+        def run(fn):
+            pset = self.download()
+            out = fn(self.time, pset)
+            self.patch(out if out is not None else pset)
+
+        cb = step_hook_callback(hooks, run, self._flow_errors)
+        self._check(self._lib.psph_set_step_hooks(self._ctx, cb, None, sum(hooks)))
+        self._hook_cb = cb  # kept alive while the context may call it
+
+    def use_step_hooks(self, dom, live: bool = False):
+        """Registers a Domain's GeneralBefore / GeneralAfter (hook(domain), the
+        reference's form). The hook sees a Domain whose `particles` and `Time`
+        are the context's at that point: `dom` itself when live (Solve), else a
+        shallow copy, so the caller's Domain keeps its particles."""
+        def adapt(h):
+            if h is None:
+                return None
+
+            def run(t, pset):
+                view = dom if live else copy.copy(dom)
+                view.Time = t
+                view.particles = pset
+                h(view)
+                return view.particles
+            return run
+        self.set_step_hooks(adapt(getattr(dom, "GeneralBefore", None)), adapt(getattr(dom, "GeneralAfter", None)))
+
+    def patch(self, pset: ParticleSet):
+        """psph_patch: writes the particles (psph_download's order) back."""
+        arrs = {f: np.ascontiguousarray(pset.get(f)) for f in ALL_FIELDS if pset.has(f)}
+        s = particles_struct(arrs, pset.n)
+        self._check(self._lib.psph_patch(self._ctx, C.byref(s)))
 
     def use_flow_hooks(self, dom):
         """Registers a Domain's user InCon / OutCon (None: the defaults)."""

@@ -2,10 +2,31 @@
 // against include/persiansph/Domain.h: the dam2d parity case of
 // tests/golden/cases.py, solved to tf, final state written as raw binary:
 // int64 n, x[3n], v[3n], density[n], pressure[n], double time.
+// With a fourth argument "hooks" it also sets a GeneralBefore hook (a spring
+// towards a point) and a GeneralAfter hook (damping of the fluid's
+// accelerations for a while, then a new artificial viscosity for part of it).
 #include <cstdio>
 #include <cstdlib>
+#include <string>
 
 #include "Domain.h"
+
+void UserSpring(SPH::Domain& dom) {
+  for (size_t i = 0; i < dom.Particles.Size(); i++)
+    if (dom.Particles[i]->IsFree) {
+      dom.Particles[i]->a(0) += 20.0 * (0.5 - dom.Particles[i]->x(0));
+      dom.Particles[i]->a(1) += 20.0 * (0.3 - dom.Particles[i]->x(1));
+    }
+}
+
+void UserDamping(SPH::Domain& dom) {
+  if (dom.Time < 0.02)
+    for (size_t i = 0; i < dom.Particles.Size(); i++)
+      if (dom.Particles[i]->IsFree) dom.Particles[i]->a -= 2.0 * dom.Particles[i]->v;
+  if (dom.Time >= 0.01)
+    for (size_t i = 0; i < dom.Particles.Size(); i++)
+      if (dom.Particles[i]->IsFree && dom.Particles[i]->x(0) < 0.2) dom.Particles[i]->Alpha = 0.05;
+}
 
 int main(int argc, char** argv) try {
   if (argc < 3) {
@@ -57,6 +78,10 @@ int main(int argc, char** argv) try {
       p->Density = rho * std::pow((1 + 7.0 * g * (H - yb) / (cs * cs)), (1.0 / 7.0));
       p->Densityb = p->Density;
     }
+  }
+  if (argc > 4 && std::string(argv[4]) == "hooks") {
+    dom.GeneralBefore = &UserSpring;
+    dom.GeneralAfter = &UserDamping;
   }
   const double dt = 0.25 * h / cs;
   dom.Solve(/*tf*/ tf, /*dt*/ dt, /*dtOut*/ tf, nullptr, 999);

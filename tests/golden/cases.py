@@ -5,6 +5,8 @@ steps after which the reference state is stored. The steps are chosen to cover
 the Modified Verlet restart (ct==30: steps 1 and 32), the Shepard
 re-initialisation (ShepardCounter==40: step 41) and the Leapfrog first step.
 """
+import math
+
 from persiansph_gb300 import scenarios
 from persiansph_gb300.domain import Multiplied_density, Takeda, Shao, Incompressible_Full
 
@@ -140,6 +142,31 @@ def channel_inflow_mc():
     return scenarios.channel_flow_2d(flow=3, mass_conservation=True, out_v=(2.0, 0.0, 0.0), scheme=1)
 
 
+def granular_damped():
+    """A cohesive granular column with a GeneralAfter hook in the style of the reference's soil
+    drivers: damping of the soil's accelerations for the first 20 steps, and a new cohesion and
+    friction angle for the upper half of the column (ID 6) from step 10 on."""
+    dom, dt, info = scenarios.granular_column(dx=0.01, W=0.2, aspect=1.0, cohesion=1000.0)
+    p = dom.particles
+    ids = p.get("id")
+    upper = (p.get("material") == 3) & (p.get("is_free") != 0) & (p.get("x")[:, 1] > 0.1)
+    ids[upper] = 6
+    p.set("id", ids)
+    damping = [50.0, 20.5 * dt, 3, 10.5 * dt, 6, 500.0, 25.0 / 180.0 * math.pi]
+    dom.GeneralAfter = scenarios.soil_damping_hook(*damping)
+    info["damping"] = damping
+    return dom, dt, info
+
+
+def dam_spring():
+    """A small dam break with a GeneralBefore hook that adds a position-dependent acceleration."""
+    dom, dt, info = scenarios.dam_break_2d(dx=0.02, L=0.4, H=0.6, TL=1.0, TH=0.8)
+    spring = [20.0, 0.5, 0.3]
+    dom.GeneralBefore = scenarios.spring_hook(*spring)
+    info["spring"] = spring
+    return dom, dt, info
+
+
 def channel_profile():
     """InOutFlow 3 with user InCon / OutCon hooks (parabolic in-flow velocity, hydrostatic densities,
     a scaled out-flow velocity) and mass conservation, Modified Verlet."""
@@ -178,6 +205,8 @@ CASES = {
     "channel_inout": (channel_inout, 40, (1, 2, 9, 10, 20, 32, 40)),
     "channel_inflow_mc": (channel_inflow_mc, 40, (1, 20, 40)),
     "channel_profile": (channel_profile, 40, (1, 9, 10, 20, 40)),
+    "granular_damped": (granular_damped, 40, (1, 10, 11, 20, 21, 40)),
+    "dam_spring": (dam_spring, 20, (1, 10, 20)),
     "gate_fsi_off": (gate_fsi_off, 32, (1, 2, 32)),
     "gate_fsi_on": (gate_fsi_on, 20, (1, 2, 20)),
 }

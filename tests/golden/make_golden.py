@@ -36,7 +36,8 @@ def main(only=()):
         dom, dt, info = builder()
         cfg = dom.config(dt)
         # user InCon / OutCon: the reference driver's profile hooks with the same parameters
-        extra = {"flow_profile": list(info["flow_profile"])} if "flow_profile" in info else None
+        # user hooks: the reference driver's hooks with the same parameters
+        extra = {k: list(info[k]) for k in ("flow_profile", "damping", "spring") if k in info} or None
         with tempfile.TemporaryDirectory() as d:
             write_state_dir(os.path.join(d, "in"), cfg, dom.particles, extra)
             run_reference(os.path.join(d, "in"), os.path.join(d, "out"), nsteps, 1, [0] + list(dumps))

@@ -63,6 +63,7 @@ def test_single_step_parity_1e12(gpu, name):
     for warm in ((0,) if cfg.in_out_flow else (0, 3)):
         o = OracleDomain(cfg, dom.particles, initial=True)
         o.use_flow_hooks(dom)
+        o.use_step_hooks(dom)  # GeneralBefore / GeneralAfter of the case, if any
         if warm:
             o.step(warm)
         gd = continue_on_gpu(cfg, o) if warm else None
@@ -70,6 +71,7 @@ def test_single_step_parity_1e12(gpu, name):
             gd = GpuDomain(cfg)
             gd.use_flow_hooks(dom)
             gd.upload(dom.particles, initial=True)
+        gd.use_step_hooks(dom)
         o.step(1)
         gd.step(1)
         a_scale, dr_scale = o.scales()
@@ -85,6 +87,7 @@ def test_trajectory_matches_reference(gpu, name):
     g = golden(name)
     gd = GpuDomain(dom.config(dt))
     gd.use_flow_hooks(dom)
+    gd.use_step_hooks(dom)
     gd.upload(dom.particles, initial=True)
     prev = 0
     for k in dumps:

@@ -24,6 +24,7 @@ def test_oracle_matches_reference(name):
     g = load(name)
     o = OracleDomain(dom.config(dt), dom.particles, initial=True)
     o.use_flow_hooks(dom)
+    o.use_step_hooks(dom)
     grid = o.grid()
     np.testing.assert_array_equal(np.array(grid.blpf), g["grid_blpf"])
     np.testing.assert_array_equal(np.array(grid.trpr), g["grid_trpr"])
