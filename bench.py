@@ -39,6 +39,17 @@ METRIC = ("pair-interactions/s @ 3D dam break (5.28M fluid particles), FP32C for
           "FP64 plain beside it")
 
 
+def max_over_ranks(value: float, dist, device) -> float:
+    """The largest of the ranks' values (the job's timed region ends with its
+    slowest replica); the value itself on one rank (dist None)."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def metric_name(workload: str) -> str:
     if workload == "dam3d":
         return METRIC
@@ -377,10 +388,7 @@ def main():
             torch.cuda.synchronize()
             clk.stop()
         pc1 = gd.pair_count()
-        if dist:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(ms, dist, "cuda")
         launches = gd.last_launch_count()
         # per-phase device times (separate short run, events between phases)
         gd.enable_timing(True)
