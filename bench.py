@@ -326,8 +326,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched granular-column line")
     ap.add_argument("--tuning", default="auto",
-                    help="'auto' (psph_autotune on the workload's own steps) or BLOCK:SPLIT[:STAGE] to fix the launch "
-                         "shape (STAGE: staged candidates per neighbour-scan block, 0 = none)")
+                    help="'auto' (psph_autotune on the workload's own steps) or BLOCK:SPLIT[:STAGE[:SKIN]] to fix the "
+                         "launch shape (STAGE: staged candidates per neighbour-scan block, 0 = none; SKIN: FP32C "
+                         "neighbour-list skin in thousandths of the support, 0 = lists every step)")
     ap.add_argument("--ens-n", type=int, default=256)
     ap.add_argument("--ens-dx", type=float, default=1e-3)
     args = ap.parse_args()
@@ -375,11 +376,13 @@ def main():
             tuning = gd.autotune(3)  # launch shapes timed on this workload's own (untimed) steps
         else:
             parts = [int(x) for x in args.tuning.split(":")]
-            gd.set_tuning(parts[0], parts[1], parts[2] if len(parts) > 2 else None)
+            gd.set_tuning(parts[0], parts[1], parts[2] if len(parts) > 2 else None,
+                          parts[3] if len(parts) > 3 and precision == 1 else None)
             tuning = gd.tuning()
         with ClockSampler(local) as clk:
             gd.step(args.warmup)
             pc0 = gd.pair_count()
+            rb0 = gd.list_rebuilds()
             if dist:
                 dist.barrier()
             torch.cuda.synchronize()
@@ -388,6 +391,7 @@ def main():
             torch.cuda.synchronize()
             clk.stop()
         pc1 = gd.pair_count()
+        rebuilds = gd.list_rebuilds() - rb0
         ms = max_over_ranks(ms, dist, "cuda")
         launches = gd.last_launch_count()
         # per-phase device times (separate short run, events between phases)
@@ -400,6 +404,7 @@ def main():
         gd.close()
         return {"cfg": cfg, "tuning": tuning, "closure_evaluated": cstats[0], "closure_fallbacks": cstats[1], "ms": ms, "done": done, "pairs": pairs, "launches": launches, "phases": phases,
                 "clocks": clk.summary(), "value_rank": pairs / (ms * 1e-3), "steps_per_s": done / (ms * 1e-3),
+                "list_rebuilds": rebuilds,
                 "pairs_per_step": pairs / max(done, 1)}
 
     m32 = measure(1, closure=wl["closure"])  # PSPH_FP32C + learned closure: the headline form
@@ -454,6 +459,10 @@ def main():
                    "parallelism": "replicas only" if world > 1 else "single GPU",
                    "l2": "working set > L2" if n * 300 > 129e6 else "working set fits in L2"},
         "steps_per_s": m32["steps_per_s"], "pairs_per_step": m32["pairs_per_step"], "tuning": m32["tuning"],
+        "list_rebuilds": {"timed_steps": m32["done"], "rebuilds": m32["list_rebuilds"],
+                          "note": "steps of the timed region that ran the cell sort and the neighbour lists "
+                                  "(every step without a list skin; with one, when a particle had moved half of "
+                                  "it since the last rebuild); every step evaluates exactly the in-support pairs"},
         "phase_ms": phase_dict(m32),
         "closure": {"evaluated": m32["closure_evaluated"], "fallbacks": m32["closure_fallbacks"],
                     "network": os.path.relpath(default_network_path(), REPO), **closure_verdict()},

@@ -274,6 +274,9 @@ psph_status psph_enable_timing(psph_ctx* ctx, int enable);
 psph_status psph_phase_times(const psph_ctx* ctx, double* ms, int cap, int* n_phases);
 /* Number of kernel launches the last psph_step issued. */
 int64_t psph_last_launch_count(const psph_ctx* ctx);
+/* Steps since upload that ran the cell sort and the neighbour lists (every
+ * step, unless the lists have a skin: psph_tuning.skin_permille). */
+int64_t psph_list_rebuilds(psph_ctx* ctx);
 
 /* psph_step(ctx, nsteps, +inf, steps_done) bracketed by CUDA events on the
  * context's stream; *device_ms receives the device time of the steps. */
@@ -294,7 +297,14 @@ typedef struct {
                            block copies into shared memory (TMA bulk copies) before scanning
                            them, 2048, 3072 or 4096; 0 scans global memory. Applies with one
                            h everywhere and a non-periodic x axis. */
-  int32_t reserved;     /* zero */
+  int32_t skin_permille; /* FP32C form: neighbour lists with a skin of this many thousandths of the
+                            support (0 to 150; 0, the default, lists every step). The lists then
+                            hold every pair within (1 + skin) of the support, on cells at least
+                            that wide, and the cell sort and the lists run again only when a
+                            particle has moved half the skin (or left, or was patched); each step
+                            still evaluates exactly the pairs inside the support. Domains without
+                            a periodic axis and without Material 2; pair exports keep the
+                            reference's cells. */
   double ms_per_step;   /* psph_autotune: device time per step of the chosen setting */
 } psph_tuning;
 psph_status psph_get_tuning(const psph_ctx* ctx, psph_tuning* out);
@@ -303,8 +313,9 @@ psph_status psph_set_tuning(psph_ctx* ctx, const psph_tuning* t);
 /* Runs steps_per_trial timed steps (after one untimed step) with every
  * candidate setting and keeps the fastest; *chosen (if not NULL) receives it:
  * first every pair block x cell split, then, with those fixed, every staging
- * depth. The trial steps are real steps of the simulation: they advance its
- * time. */
+ * depth, then (FP32C) list skins of 50, 100 and 150 thousandths over at least
+ * 24 steps each. The trial steps are real steps of the simulation: they
+ * advance its time. */
 psph_status psph_autotune(psph_ctx* ctx, int64_t steps_per_trial, psph_tuning* chosen);
 
 /* ---- Snapshot output (WriteXDMF, Source/Domain.cpp:1869-2064) -----------------

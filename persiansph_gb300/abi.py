@@ -79,7 +79,7 @@ class PsphIntegrator(C.Structure):
 
 class PsphTuning(C.Structure):
     _fields_ = [("pair_block", C.c_int32), ("cell_split", C.c_int32), ("nlist_stage", C.c_int32),
-                ("reserved", C.c_int32), ("ms_per_step", C.c_double)]
+                ("skin_permille", C.c_int32), ("ms_per_step", C.c_double)]
 
 
 class PsphParticles(C.Structure):
@@ -186,6 +186,8 @@ def _declare(lib):
     lib.psph_phase_times.argtypes = [ctx, P(C.c_double), C.c_int, P(C.c_int)]
     lib.psph_last_launch_count.argtypes = [ctx]
     lib.psph_last_launch_count.restype = C.c_int64
+    lib.psph_list_rebuilds.argtypes = [ctx]
+    lib.psph_list_rebuilds.restype = C.c_int64
     lib.psph_step_timed.argtypes = [ctx, C.c_int64, P(C.c_double), P(C.c_int64)]
     lib.psph_pair_count.argtypes = [ctx, P(C.c_uint64)]
     lib.psph_probe_fp64_peak.argtypes = [P(C.c_double)]

@@ -38,6 +38,7 @@ constexpr int kNumPhases = 7;
 constexpr int kMaxXsub = 4;
 // Deepest staging of the neighbour search (Options::nlist_stage, candidates per block).
 constexpr int kMaxStage = 4096;
+constexpr int kMaxSkinPermille = 150;  // list skins up to 15 % of the support (the lists' capacity)
 
 struct psph_ctx {
   int ninst = 1;
@@ -65,7 +66,9 @@ struct psph_ctx {
   Scratch S{};
   PClass* d_cls = nullptr;
   PClass32* d_cls32 = nullptr;
-  GridDev* d_grids = nullptr;
+  GridDev* d_grids = nullptr;           // the lists' and the sort's grids (the reference's without a skin)
+  GridDev* d_grids_ref = nullptr;       // the reference's grids (CellInitiate)
+  int total_cells_ref = 0;
   InstState* d_inst = nullptr;
   InstState* h_inst = nullptr;  // pinned mirror
   StepScalars* d_sc = nullptr;
@@ -270,6 +273,7 @@ void record_phase(psph_ctx* c, int k) {
 DevView view(psph_ctx* c) {
   DevView v{};
   v.grids = c->d_grids;
+  v.grids_ref = c->d_grids_ref;
   v.inst = c->d_inst;
   v.ninst = c->ninst;
   v.total_cells = c->total_cells;
@@ -285,6 +289,15 @@ DevView view(psph_ctx* c) {
   v.ncap = c->ncap;
   v.nl_stride = nl_stride_of(c->ncap);
   v.nclasses = (int)c->classes.size();
+  return v;
+}
+
+// The view on the reference's cell grid (the same as view() without a skin):
+// the pair exports list the reference's candidate pairs in its orientation.
+DevView view_ref(psph_ctx* c) {
+  DevView v = view(c);
+  v.grids = c->d_grids_ref;
+  v.total_cells = c->total_cells_ref;
   return v;
 }
 
@@ -305,6 +318,7 @@ void enqueue_step(psph_ctx* c, F&& before_update) {
   launch_sort(v, st);
   record_phase(c, 1);
   launch_nlist(v, st);
+  if (v.o.skin > 0.f) launch_skin_offsets(v, st);
   record_phase(c, 2);
   if (v.o.fp32) launch_prepare32(v, st);
   else launch_prepare(v, st);
@@ -810,6 +824,7 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
       return set_err(c, PSPH_ERR_UNSUPPORTED, "the instances' grids hold more than 2^28 cells");
   }
   c->total_cells = (int)cell_base;
+  c->total_cells_ref = c->total_cells;
 
   // ---- options ---------------------------------------------------------------
   Options& o = c->opt;
@@ -860,6 +875,9 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
   // neighbour lists: 3D supports hold ~80 (h = 1.3 dx) particles, 2D ~20-44;
   // a particle with more falls back to scanning its cells
   o.nl_cap = (k.dimension == 3) ? 128 : 64;
+  // the FP32C form may run its lists with a skin (psph_set_tuning): room for
+  // (1 + skin)^3 more entries
+  if (k.precision == PSPH_FP32C) o.nl_cap = (k.dimension == 3) ? 160 : 96;
   o.pair_block = 128;
   o.xsub = 1;
   o.nlist_stage = 0;  // measured: the L1-cached scan beats the staged one (psph_autotune tries both)
@@ -912,6 +930,7 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
   }
   if (o.need_sr || o.has_solid)
     if ((st = dalloc(c, &S.strain_rate, 9 * N))) return st;
+  if (o.fp32 && ((st = dalloc(c, &S.OFFREF, N)) || (st = dalloc(c, &S.refcell, N)))) return st;
   if (o.fp32) {
     if ((st = dalloc(c, &S.V32, N)) || (st = dalloc(c, &S.D32, N)) || (st = dalloc(c, &S.NSV32, N)) ||
         (st = dalloc(c, &S.V32LO, N)))
@@ -933,6 +952,7 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
   c->cls_cap = (int)c->classes.size() + (inout ? 256 : 0);  // recycled in-flow particles may need new classes
   if ((st = dalloc(c, &c->d_cls, (size_t)c->cls_cap)) || (st = dalloc(c, &c->d_sc, 1)) ||
       (st = dalloc(c, &c->d_alive, N)) || (st = dalloc(c, &c->d_grids, (size_t)ninst)) ||
+      (st = dalloc(c, &c->d_grids_ref, (size_t)ninst)) ||
       (st = dalloc(c, &c->d_inst, (size_t)ninst)))
     return st;
   CUDA_TRY(c, cudaMallocHost(&c->h_sc, sizeof(StepScalars)));
@@ -1028,6 +1048,7 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
     CUDA_TRY(c, cudaGetLastError());
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     CUDA_TRY(c, cudaMemcpy(c->d_grids, c->gdevs.data(), ninst * sizeof(GridDev), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(c->d_grids_ref, c->gdevs.data(), ninst * sizeof(GridDev), cudaMemcpyHostToDevice));
     std::vector<InstState> is(ninst);
     for (int q = 0; q < ninst; ++q) {
       InstState& I = is[q];
@@ -1050,6 +1071,8 @@ psph_status upload_impl(psph_ctx* c, const psph_particles* parts, int initial) {
     sc.n = (int)ntot;
     sc.n_total = (int)ntot;
     sc.buf = 0;
+    sc.rebuild = 1;
+    sc.force_rebuild = 1;
     CUDA_TRY(c, cudaMemcpy(c->d_sc, &sc, sizeof sc, cudaMemcpyHostToDevice));
   }
   c->inout = inout;
@@ -1443,6 +1466,7 @@ psph_status split_steps(psph_ctx* c, int64_t nsteps, long long* launched, bool o
     if (c->h_sc->all_stop) break;
     if (c->inout && (st = inout_fresh(c))) return st;
     launch_nlist(view(c), s);
+    if (c->opt.skin > 0.f) launch_skin_offsets(view(c), s);
     if (before) {
       const int n = c->h_sc->n;
       const double* gv = c->opt.gravity;
@@ -1942,6 +1966,9 @@ psph_status patch_impl(psph_ctx* c, const psph_particles* p) {
     }
   }
   if (p->x && c->in_hook == PSPH_HOOK_BEFORE) c->hook_set_x = true;
+  // with a skin the next step lists again (patched positions may have moved
+  // particles past the skin)
+  if (c->opt.skin > 0.f) launch_mark_rebuild(view(c), false, true, c->stream);
   struct F { const double* in; double* dev; int stride, off, width; };
   auto d4 = [](double4_32a* q) { return reinterpret_cast<double*>(q); };
   const F fields[] = {
@@ -2213,7 +2240,10 @@ psph_status psph_pairs_export(psph_ctx* c, int which, int64_t* pairs, int64_t ca
   if (c->ninst != 1) return set_err(c, PSPH_ERR_STATE, "psph_pairs_export applies to single-domain contexts");
   // cell-sort the current positions (does not change the physical state)
   rearm_kernel<<<1, 256, 0, c->stream>>>(c->d_inst, c->ninst, c->d_sc);
-  const DevView v = view(c);
+  const DevView v = view_ref(c);
+  // this sort runs whatever the step decided, and with a skin the next step
+  // sorts and lists again on its own grid
+  launch_mark_rebuild(v, true, c->opt.skin > 0.f, c->stream);
   launch_sort(v, c->stream);
   unsigned long long* d_counter = nullptr;
   long long* d_out = nullptr;
@@ -2252,6 +2282,11 @@ psph_status psph_phase_times(const psph_ctx* c, double* ms, int cap, int* n_phas
 
 int64_t psph_last_launch_count(const psph_ctx* c) { return c ? c->last_launches : 0; }
 
+int64_t psph_list_rebuilds(psph_ctx* c) {
+  if (!c || !c->uploaded || sync_scalars(c)) return -1;
+  return (int64_t)c->h_sc->rebuilds;
+}
+
 psph_status psph_step_timed(psph_ctx* c, int64_t nsteps, double* device_ms, int64_t* steps_done) {
   if (!c || !device_ms) return PSPH_ERR_INVALID_ARGUMENT;
   if (!c->uploaded) return set_err(c, PSPH_ERR_STATE, "psph_step_timed before psph_upload");
@@ -2278,12 +2313,63 @@ psph_status psph_step_timed(psph_ctx* c, int64_t nsteps, double* device_ms, int6
   return st;
 }
 
+// Neighbour lists with a skin (the FP32C form): the lists hold every pair
+// within (1 + skin) of the support and are kept until a particle has moved
+// half the skin; the cell sort and the list scan then use cells of at least
+// (1 + skin) Cellfac hmax with the reference's bounds (BLPF, TRPR), so that
+// the 3x3(x3) block covers the wider reach. The pair set each step evaluates
+// is the same; the summation order follows the kept lists.
+psph_status apply_skin(psph_ctx* c, float skin) {
+  if (skin > 0.f) {
+    if (!c->uploaded) return set_err(c, PSPH_ERR_STATE, "a list skin is set after psph_upload");
+    if (!c->opt.fp32) return set_err(c, PSPH_ERR_UNSUPPORTED, "list skins apply to the FP32C form (PSPH_FP32C)");
+    if (c->opt.any_periodic) return set_err(c, PSPH_ERR_UNSUPPORTED, "list skins apply to domains without a periodic axis");
+    for (const PClass& C : c->classes)
+      if (C.material == 2)
+        return set_err(c, PSPH_ERR_UNSUPPORTED, "list skins apply to fluid and soil domains (Material 2 present)");
+    for (const GridDev& g : c->gdevs)
+      for (int d = 0; d < 3; ++d)
+        if (g.nc[d] > 1023)
+          return set_err(c, PSPH_ERR_UNSUPPORTED, "list skins need at most 1023 reference cells per axis (%d)", g.nc[d]);
+  }
+  std::vector<GridDev> gd(c->gdevs);
+  long long base = 0;
+  float disp2 = 0.f;
+  for (size_t q = 0; q < gd.size(); ++q) {
+    GridDev& g = gd[q];
+    if (skin > 0.f) {
+      const double reach = g.cellfac * g.hmax * (1.0 + (double)skin);
+      for (int d = 0; d < 3; ++d) {
+        if (g.cell_size[d] <= 0.0) continue;  // an axis beyond the dimension: one cell
+        const double L = g.trpr[d] - g.blpf[d];
+        const int cn = std::max(1, (int)std::floor(L / reach));
+        g.nc[d] = g.cn_ref[d] = cn;
+        g.cell_size[d] = L / cn;
+        g.inv_cell_size32[d] = (float)(1.0 / g.cell_size[d]);
+        g.cell_size32[d] = (float)g.cell_size[d];
+      }
+      const double half = 0.5 * (double)skin * g.cellfac * g.hmax;
+      g.skin_disp2 = (float)(half * half);
+      disp2 = (q == 0) ? g.skin_disp2 : std::min(disp2, g.skin_disp2);
+    }
+    g.ncells = g.nc[0] * g.nc[1] * g.nc[2];
+    g.cell_base = (int)base;
+    base += g.ncells;
+  }
+  if (c->uploaded)
+    CUDA_TRY(c, cudaMemcpy(c->d_grids, gd.data(), gd.size() * sizeof(GridDev), cudaMemcpyHostToDevice));
+  c->total_cells = (int)base;
+  c->opt.skin = skin;
+  c->opt.skin_disp2 = disp2;
+  return PSPH_OK;
+}
+
 psph_status psph_get_tuning(const psph_ctx* c, psph_tuning* out) {
   if (!c || !out) return PSPH_ERR_INVALID_ARGUMENT;
   out->pair_block = c->opt.pair_block;
   out->cell_split = c->opt.xsub;
   out->nlist_stage = c->opt.nlist_stage;
-  out->reserved = 0;
+  out->skin_permille = (int32_t)std::lround(c->opt.skin * 1000.0);
   out->ms_per_step = c->tuned_ms;
   return PSPH_OK;
 }
@@ -2297,10 +2383,21 @@ psph_status psph_set_tuning(psph_ctx* c, const psph_tuning* t) {
   if (t->nlist_stage != 0 && t->nlist_stage != 2048 && t->nlist_stage != 3072 && t->nlist_stage != kMaxStage)
     return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "nlist_stage must be 0, 2048, 3072 or 4096 (got %d)",
                    t->nlist_stage);
-  if (c->opt.pair_block != t->pair_block || c->opt.xsub != t->cell_split || c->opt.nlist_stage != t->nlist_stage) {
+  if (t->skin_permille < 0 || t->skin_permille > kMaxSkinPermille)
+    return set_err(c, PSPH_ERR_INVALID_ARGUMENT, "skin_permille must lie in [0, %d] (got %d)", kMaxSkinPermille,
+                   t->skin_permille);
+  const float skin = (float)(t->skin_permille / 1000.0);
+  if (c->opt.pair_block != t->pair_block || c->opt.xsub != t->cell_split || c->opt.nlist_stage != t->nlist_stage ||
+      c->opt.skin != skin) {
+    if (c->opt.skin != skin) {
+      psph_status st = apply_skin(c, skin);
+      if (st) return st;
+    }
     c->opt.pair_block = t->pair_block;
     c->opt.xsub = t->cell_split;
     c->opt.nlist_stage = t->nlist_stage;
+    // lists kept with a skin follow the sort's layout: the next step lists again
+    if (c->uploaded && c->opt.skin > 0.f) launch_mark_rebuild(view(c), false, true, c->stream);
     if (c->graph) {  // launch parameters change: capture the step again
       cudaGraphExecDestroy(c->graph);
       c->graph = nullptr;
@@ -2327,14 +2424,14 @@ psph_status psph_autotune(psph_ctx* c, int64_t steps_per_trial, psph_tuning* cho
   psph_tuning best{};
   double best_ms = 1e300;
   bool ended = false;
-  auto trial = [&](const psph_tuning& t) -> psph_status {
+  auto trial = [&](const psph_tuning& t, int64_t steps) -> psph_status {
     psph_status st = psph_set_tuning(c, &t);
     if (st) return st;
     double ms = 0.0;
     int64_t done = 0;
     if ((st = psph_step_timed(c, 1, &ms, &done))) return st;  // capture + first launch, untimed
-    if ((st = psph_step_timed(c, steps_per_trial, &ms, &done))) return st;
-    if (done < steps_per_trial) {  // the run ended; keep what was measured
+    if ((st = psph_step_timed(c, steps, &ms, &done))) return st;
+    if (done < steps) {  // the run ended; keep what was measured
       ended = true;
       return PSPH_OK;
     }
@@ -2346,7 +2443,7 @@ psph_status psph_autotune(psph_ctx* c, int64_t steps_per_trial, psph_tuning* cho
     return PSPH_OK;
   };
   for (const psph_tuning& t : cands) {
-    if (psph_status st = trial(t)) return st;
+    if (psph_status st = trial(t, steps_per_trial)) return st;
     if (ended) break;
   }
   if (best_ms == 1e300) best = cands.front();
@@ -2357,7 +2454,21 @@ psph_status psph_autotune(psph_ctx* c, int64_t steps_per_trial, psph_tuning* cho
       if (stage == base.nlist_stage) continue;
       psph_tuning t = base;
       t.nlist_stage = stage;
-      if (psph_status st = trial(t)) return st;
+      if (psph_status st = trial(t, steps_per_trial)) return st;
+      if (ended) break;
+    }
+  }
+  // then list skins (FP32C): each trial runs long enough for several rebuilds
+  // to be in its average
+  bool skins = !ended && c->opt.fp32 && !c->opt.any_periodic;
+  for (const PClass& C : c->classes) skins = skins && C.material != 2;
+  for (const GridDev& g : c->gdevs) skins = skins && g.nc[0] <= 1023 && g.nc[1] <= 1023 && g.nc[2] <= 1023;
+  if (skins) {
+    const psph_tuning base = best;
+    for (int permille : {50, 100, kMaxSkinPermille}) {
+      psph_tuning t = base;
+      t.skin_permille = permille;
+      if (psph_status st = trial(t, std::max<int64_t>(8 * steps_per_trial, 24))) return st;
       if (ended) break;
     }
   }
@@ -2625,7 +2736,8 @@ extern "C" psph_status psph_pairs_export_noalloc(psph_ctx* c, int which, int64_t
   int* block_sums = offsets + PSPH_NOALLOC_MAX_PARTICLES + 1;
   cudaStream_t s = c->stream;
   rearm_kernel<<<1, 256, 0, s>>>(c->d_inst, c->ninst, c->d_sc);
-  const DevView v = view(c);
+  const DevView v = view_ref(c);                       // the reference's cells, also with a skin
+  launch_mark_rebuild(v, true, c->opt.skin > 0.f, s);  // this sort runs; a skin's lists follow next step
   launch_sort(v, s);                                   // cell list of the current positions
   launch_pairs_count(v, which, counts, s);             // pairs each sorted particle lists first
   noalloc_total_kernel<<<1, 1024, 0, s>>>(counts, c->ncap, d_total);

@@ -106,6 +106,12 @@ struct StepScalars {
   int launches;
   unsigned long long closure_eval, closure_fallback;  // closure evaluations / Smagorinsky fallbacks
   int nl_rest;    // particles the neighbour-list scan handles one per lane (set by the sort)
+  // neighbour lists with a skin (FP32C form, Options::skin > 0): the cell sort
+  // and the lists are rebuilt only when a particle has moved half the skin
+  int rebuild;             // this step sorts and lists (always, without a skin)
+  int force_rebuild;       // the next step must (upload, a particle left, a patch, an export's sort)
+  unsigned int disp2_bits; // largest squared displacement since the last rebuild (FP32 bits)
+  unsigned int rebuilds;   // steps that sorted and listed since upload
 };
 
 struct GridDev {
@@ -119,6 +125,7 @@ struct GridDev {
   float inv_cell_size32[3];  // 1 / cell_size in FP32 (cell-index estimate of the sort)
   float cell_size32[3];      // cell_size rounded to FP32 (on the host)
   float cellfac2_32;         // Cellfac^2 in FP32
+  float skin_disp2;          // with a skin: (half the skin)^2, the displacement that forces a rebuild
 };
 
 // ---------------------------------------------------------------------------

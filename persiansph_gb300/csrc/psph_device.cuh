@@ -37,6 +37,9 @@ struct Scratch {
   int* block_sums;
   // per-step derived / outputs
   float4* OFF32;     // (position - cell origin, h) in FP32, written by the reorder
+  float4* OFFREF;    // with a skin: OFF32 at the last rebuild (displacements are measured from it)
+  int* refcell;      // with a skin: each particle's cell in the reference's grid (x | y << 10 | z << 20),
+                     // for the wall pressure's pair orientation
   int* nl;           // per-step neighbour lists, entry k of particle i at nl[k*ncap + i]:
                      // index | cell-offset code << 26
   int* nl_count;     // list length, or -1 when it exceeded the capacity (scan instead)
@@ -122,6 +125,8 @@ struct Options {
   double xsph, sqrt_h_a;
   double gravity[3], body_force[3];
   double gb[3];       // gravity + body force (the sum every pair kernel starts from)
+  float skin;         // FP32C neighbour lists with a skin (fraction of the support); 0: rebuilt every step
+  float skin_disp2;   // the smallest of the instances' GridDev::skin_disp2
   int a_from_hook;    // FP64 pair kernels start from this step's A4 (set by a GeneralBefore
                       // hook, Source/Domain.cpp:1767) instead of Gravity
   // FP32 copies for the FP32C kernels, converted once on the host (a
@@ -139,7 +144,8 @@ inline int nl_stride_of(int ncap) { return (ncap + 63) & ~63; }
 
 // Everything a launch needs, passed by value to the launch wrappers.
 struct DevView {
-  const GridDev* grids;   // per instance (device array)
+  const GridDev* grids;   // per instance (device array): the cells of the sort and the lists
+  const GridDev* grids_ref;  // the reference's grids (CellInitiate); the same as grids without a skin
   InstState* inst;        // per instance
   int ninst;
   int total_cells;        // sum of the instances' cells
@@ -164,6 +170,9 @@ PSPH_D const Persist& next_persist(const DevView& v) { return v.sc->buf ? v.PA :
 // Launch wrappers (defined in the .cu files).
 void launch_sort(const DevView& v, cudaStream_t st);      // bin + scan + scatter + rank + reorder + flip
 void launch_nlist(const DevView& v, cudaStream_t st);     // per-step neighbour lists
+void launch_skin_offsets(const DevView& v, cudaStream_t st);  // lists with a skin: FP32 offsets, reference cells
+// the next cell sort runs (now, a sort outside a step) / the next step rebuilds its lists
+void launch_mark_rebuild(const DevView& v, bool now, bool next_step, cudaStream_t st);
 void nlist_configure();                                   // once, outside stream capture: shared-memory limits
 void launch_prepare(const DevView& v, cudaStream_t st);   // per-particle derived quantities, TIR
 void launch_prepare32(const DevView& v, cudaStream_t st); // FP32C form: copies + wall interpolation

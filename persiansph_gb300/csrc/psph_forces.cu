@@ -862,7 +862,19 @@ __global__ void begin_kernel(DevView v) {
     I.dtmin_bits = (unsigned long long)__double_as_longlong(DBL_MAX);
   }
   live = __syncthreads_or(live);
-  if (threadIdx.x == 0) sc->all_stop = !live;
+  if (threadIdx.x == 0) {
+    sc->all_stop = !live;
+    // the cell sort and the neighbour lists run every step, or, with a skin,
+    // once a particle has moved half the skin since they last ran
+    bool rb = true;
+    if (v.o.skin > 0.f) rb = sc->force_rebuild || __uint_as_float(sc->disp2_bits) > v.o.skin_disp2;
+    sc->rebuild = rb ? 1 : 0;
+    if (rb && live) {
+      sc->force_rebuild = 0;
+      sc->disp2_bits = 0u;
+      sc->rebuilds += 1u;
+    }
+  }
 }
 
 // End of step: Time += deltat and the per-particle counters, once per instance.

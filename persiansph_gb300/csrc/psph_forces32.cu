@@ -195,6 +195,8 @@ __global__ void __launch_bounds__(kFT32) prepare32_kernel(DevView v) {
   const float3 cs = cell_size_f(g);
   const float gx = o.gravity32[0], gy = o.gravity32[1], gz = o.gravity32[2];
   const bool need_orient = !o.wallp_physical && (gx != 0.f || gy != 0.f || gz != 0.f);
+  const bool skin = o.skin > 0.f;
+  const int rc_w = (skin && need_orient && wall) ? v.S.refcell[w] : 0;
   float sk = 0.f, p = 0.f, n0 = 0.f, n1 = 0.f, n2 = 0.f;
   const float hw = oi.w;
   // one fluid neighbour of the same material: its position, velocity and
@@ -209,8 +211,13 @@ __global__ void __launch_bounds__(kFT32) prepare32_kernel(DevView v) {
     if (!(Cf.flags & CF_FREE) || Cf.material != mat) return;
     float x0, x1, x2;
     rel_pos<DIM>(cs, oi, of, code, x0, x1, x2);  // x_wall - x_fluid
-    if (need_orient && !first_of_pair_code(code, ow, P.orig[f])) {
-      x0 = -x0; x1 = -x1; x2 = -x2;
+    if (need_orient) {
+      // the pair's cell offset in the reference's grid (with a skin the lists'
+      // cells are coarser): it decides which particle the reference lists first
+      const int cd = skin ? ref_code(rc_w, v.S.refcell[f]) : code;
+      if (!first_of_pair_code(cd, ow, P.orig[f])) {
+        x0 = -x0; x1 = -x1; x2 = -x2;
+      }
     }
     const float hb = 0.5f * (hw + of.w);
     const float ih = 1.f / hb;

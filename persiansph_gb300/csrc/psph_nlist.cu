@@ -184,7 +184,7 @@ __device__ __forceinline__ void list_one(const DevView& v, int i, float margin, 
 template <int DIM, bool UNIFORM_H>
 __global__ void __launch_bounds__(kNT, 8) nlist_kernel(DevView v, float margin) {
   __shared__ int ring[8][kNT];
-  if (v.sc->all_stop) return;
+  if (v.sc->all_stop || !v.sc->rebuild) return;  // lists with a skin: kept from the last rebuild
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= v.sc->n) return;
   list_one<DIM, UNIFORM_H>(v, i, margin, &ring[0][threadIdx.x]);
@@ -224,7 +224,7 @@ template <int DIM>
 __global__ void __launch_bounds__(kNT, 8) nlist_pair_kernel(DevView v, float margin, int nr) {
   __shared__ int ring[2][8][kNT];
   const StepScalars* sc = v.sc;
-  if (sc->all_stop) return;
+  if (sc->all_stop || !sc->rebuild) return;
   if ((int)blockIdx.x < nr) {
     const int m = min(sc->nl_rest, v.ncap);
     for (int q = blockIdx.x * kNT + threadIdx.x; q < m; q += nr * kNT)
@@ -396,7 +396,7 @@ __global__ void __launch_bounds__(kNT, 4) nlist_staged_kernel(DevView v, float m
   __shared__ __align__(8) uint64_t s_bar;
   extern __shared__ float4 s_off[];
   StepScalars* sc = v.sc;
-  if (sc->all_stop) return;
+  if (sc->all_stop || !sc->rebuild) return;
   if ((int)blockIdx.x < nr) {
     const int m = min(sc->nl_rest, v.ncap);
     for (int q = blockIdx.x * kNT + threadIdx.x; q < m; q += nr * kNT)
@@ -508,7 +508,8 @@ void nlist_configure() {
 void launch_nlist(const DevView& v, cudaStream_t st) {
   // a superset of the support: the pair kernels apply the exact test (FP32 in
   // the FP32C form, FP64 in the plain form)
-  const float margin = v.o.fp32 ? 1.0002f : 1.004f;
+  // with a skin s the lists hold every pair within (1 + s) of the support
+  const float margin = v.o.fp32 ? 1.0002f * (1.f + v.o.skin) * (1.f + v.o.skin) : 1.004f;
   if (v.o.uniform_h) {  // two particles per lane; the leftovers' blocks first
     const int half = (v.ncap + 1) / 2;
     const int nr = 2 * sm_count();

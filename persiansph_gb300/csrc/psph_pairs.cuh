@@ -96,6 +96,16 @@ PSPH_D bool first_of_pair(const GridDev& g, const CellCoord& cw, const CellCoord
   return orig_w > orig_f;
 }
 
+// The cell-offset code of two cells of the reference's grid packed as
+// x | y << 10 | z << 20 (candidate minus home, each axis clamped to one cell:
+// an in-support pair is never farther apart there).
+PSPH_D int ref_code(int home, int cand) {
+  const int dx = min(max((cand & 1023) - (home & 1023), -1), 1);
+  const int dy = min(max(((cand >> 10) & 1023) - ((home >> 10) & 1023), -1), 1);
+  const int dz = min(max((cand >> 20) - (home >> 20), -1), 1);
+  return (dx + 1) + 3 * (dy + 1) + 9 * (dz + 1);
+}
+
 // Same rule from a cell-offset code (candidate cell minus home cell, wrapped).
 PSPH_D bool first_of_pair_code(int code, int orig_w, int orig_f) {
   const int dxc = code % 3 - 1, dyc = (code / 3) % 3 - 1, dzc = code / 9 - 1;

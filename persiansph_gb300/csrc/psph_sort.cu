@@ -43,7 +43,7 @@ __device__ __forceinline__ float d2f_bits(double x) {
 
 __global__ void bin_kernel(DevView v, const uint8_t* __restrict__ alive, int* __restrict__ key,
                            int* __restrict__ count, StepScalars* sc, int dim, int xsub) {
-  if (sc->all_stop) return;
+  if (sc->all_stop || !sc->rebuild) return;
   const Persist& P = cur_persist(v);
   const int n = sc->n;
   const int nbins = v.total_cells * xsub;
@@ -105,7 +105,9 @@ __global__ void bin_kernel(DevView v, const uint8_t* __restrict__ alive, int* __
 }
 
 // Phase 1: in-block exclusive scan of `in` (len entries), block totals to sums.
-__global__ void scan_blocks(const int* __restrict__ in, int* __restrict__ out, int* __restrict__ sums, int len) {
+__global__ void scan_blocks(const int* __restrict__ in, int* __restrict__ out, int* __restrict__ sums, int len,
+                            const StepScalars* sc) {
+  if (sc && (sc->all_stop || !sc->rebuild)) return;  // the cell sort's scan, on a step without a rebuild
   __shared__ int warp_tot[32];
   const int base = blockIdx.x * 1024;
   const int t = threadIdx.x;
@@ -136,7 +138,8 @@ __global__ void scan_blocks(const int* __restrict__ in, int* __restrict__ out, i
 }
 
 // Phase 2: one block scans the block totals (exclusive), writes the grand total.
-__global__ void scan_sums(int* __restrict__ sums, int nb, int* __restrict__ total_out) {
+__global__ void scan_sums(int* __restrict__ sums, int nb, int* __restrict__ total_out, const StepScalars* sc) {
+  if (sc && (sc->all_stop || !sc->rebuild)) return;
   __shared__ int carry;
   if (threadIdx.x == 0) carry = 0;
   __syncthreads();
@@ -172,14 +175,15 @@ __global__ void scan_sums(int* __restrict__ sums, int nb, int* __restrict__ tota
   if (threadIdx.x == 0) *total_out = carry;
 }
 
-__global__ void scan_add(int* __restrict__ out, const int* __restrict__ sums, int len) {
+__global__ void scan_add(int* __restrict__ out, const int* __restrict__ sums, int len, const StepScalars* sc) {
+  if (sc && (sc->all_stop || !sc->rebuild)) return;
   const int i = blockIdx.x * 1024 + threadIdx.x;
   if (i < len) out[i] += sums[blockIdx.x];
 }
 
 __global__ void scatter_kernel(const int* __restrict__ key, const int* __restrict__ start, int* __restrict__ fill,
                                int* __restrict__ tmp_perm, const StepScalars* sc) {
-  if (sc->all_stop) return;
+  if (sc->all_stop || !sc->rebuild) return;
   const int n = sc->n;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int k = key[i];
@@ -196,7 +200,7 @@ __global__ void scatter_kernel(const int* __restrict__ key, const int* __restric
 __global__ void rank_kernel(const int* __restrict__ key, const int* __restrict__ start,
                             const int* __restrict__ tmp_perm, DevView v, int* __restrict__ perm,
                             const StepScalars* sc, int ncells) {
-  if (sc->all_stop) return;
+  if (sc->all_stop || !sc->rebuild) return;
   const int* __restrict__ orig = cur_persist(v).orig;
   const int n = sc->n;
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
@@ -217,7 +221,7 @@ __global__ void rank_kernel(const int* __restrict__ key, const int* __restrict__
 __global__ void reorder_kernel(DevView v, const int* __restrict__ perm, const int* __restrict__ key,
                                const int* __restrict__ start, int* __restrict__ cellid, uint8_t* __restrict__ alive,
                                const StepScalars* sc, int nbins, int xsub, int has_solid, int dyn_mu) {
-  if (sc->all_stop) return;
+  if (sc->all_stop || !sc->rebuild) return;
   const Persist& src = cur_persist(v);
   const Persist& dst = next_persist(v);
   const int n_new = start[nbins + 1];
@@ -243,6 +247,7 @@ __global__ void reorder_kernel(DevView v, const int* __restrict__ perm, const in
       } else {
         v.S.OFF32[s] = make_float4((float)xs.x, (float)xs.y, (float)xs.z, h);
       }
+      if (v.o.skin > 0.f) v.S.OFFREF[s] = v.S.OFF32[s];  // displacements are measured from here
     }
     dst.orig[s] = src.orig[i];
     if (src.io) dst.io[s] = src.io[i];
@@ -259,7 +264,7 @@ __global__ void reorder_kernel(DevView v, const int* __restrict__ perm, const in
 // together (it mostly does: particles move little between steps).
 __global__ void reorder_tensors_kernel(DevView v, const int* __restrict__ perm, const int* __restrict__ start,
                                        const StepScalars* sc, int nbins) {
-  if (sc->all_stop) return;
+  if (sc->all_stop || !sc->rebuild) return;
   const Persist& src = cur_persist(v);
   const Persist& dst = next_persist(v);
   const int n_new = start[nbins + 1];
@@ -288,7 +293,7 @@ __global__ void reorder_tensors_kernel(DevView v, const int* __restrict__ perm, 
 }
 
 __global__ void finish_sort_kernel(const int* __restrict__ start, StepScalars* sc, int nbins) {
-  if (sc->all_stop) return;
+  if (sc->all_stop || !sc->rebuild) return;
   sc->n_cells = start[nbins];
   sc->n = start[nbins + 1];
   sc->buf ^= 1;
@@ -303,7 +308,7 @@ __global__ void finish_sort_kernel(const int* __restrict__ start, StepScalars* s
 // cells' first particles at odd indices (into rest, at most cap of them).
 __global__ void cell_starts_kernel(const int* __restrict__ sstart, int* __restrict__ start, int ncells, int xsub,
                                    StepScalars* sc, int* __restrict__ rest, int cap) {
-  if (sc->all_stop) return;
+  if (sc->all_stop || !sc->rebuild) return;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (xsub > 1) {
     if (c <= ncells) start[c] = sstart[(size_t)c * xsub];
@@ -326,12 +331,69 @@ __global__ void cell_starts_kernel(const int* __restrict__ sstart, int* __restri
   }
 }
 
+// Neighbour lists with a skin: on every step the FP32 offsets of the
+// particles from their cells' origins (the cells of the last rebuild), and
+// each particle's cell in the reference's grid (ListGenerate's floor and
+// clamp on the FP64 position, Source/Domain.cpp:669-691), which orients the
+// wall pressure's pairs as the reference's neighbour search does.
+__global__ void skin_offsets_kernel(DevView v) {
+  const StepScalars* sc = v.sc;
+  if (sc->all_stop) return;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= sc->n) return;
+  const Persist& P = cur_persist(v);
+  const PClass& C = v.cls[P.cls[s]];
+  const double4_32a xs = P.X4[s];
+  const float h = (float)C.h;
+  const int cell = v.S.cellid[s];
+  if (cell >= 0) {
+    const GridDev& g = grid_of(v, C.inst);
+    const int lk = cell - g.cell_base;
+    const int cx = lk % g.nc[0], t = lk / g.nc[0], cy = t % g.nc[1], cz = t / g.nc[1];
+    v.S.OFF32[s] = make_float4((float)(xs.x - (g.blpf[0] + cx * g.cell_size[0])),
+                               (float)(xs.y - (g.blpf[1] + cy * g.cell_size[1])),
+                               (float)(v.o.dim == 3 ? xs.z - (g.blpf[2] + cz * g.cell_size[2]) : 0.0), h);
+  } else {
+    v.S.OFF32[s] = make_float4((float)xs.x, (float)xs.y, (float)xs.z, h);
+  }
+  const GridDev& r = v.grids_ref[C.inst];
+  const double xd[3] = {xs.x, xs.y, xs.z};
+  int q[3] = {0, 0, 0};
+  for (int d = 0; d < v.o.dim; ++d) {
+    // floor((x - BLPF) / CellSize) from an FP32 estimate, with the FP64
+    // division only near a cell face (as the sort's bin_kernel)
+    const double a = xd[d] - r.blpf[d];
+    const float t = d2f_bits(a) * r.inv_cell_size32[d];
+    const float ft = floorf(t), fr = t - ft, tol = 1e-3f + 4e-7f * fabsf(t);
+    int k = (int)ft;
+    if (!(fr >= tol && fr <= 1.f - tol)) k = (int)floor(a / r.cell_size[d]);
+    q[d] = min(max(k, 0), r.cn_ref[d] - 1);  // clamped as ListGenerate clamps the particles just outside
+  }
+  v.S.refcell[s] = q[0] | (q[1] << 10) | (q[2] << 20);
+}
+
+// now: the next cell sort runs (a sort outside the step loop); next_step:
+// the next step sorts and lists again (with a skin, whose lists would
+// otherwise be kept)
+__global__ void mark_rebuild_kernel(StepScalars* sc, int now, int next_step) {
+  if (now) sc->rebuild = 1;
+  if (next_step) sc->force_rebuild = 1;
+}
+
 inline int grid_for(int n) {
   int b = (n + kBT - 1) / kBT;
   return b < 1 ? 1 : b;
 }
 
 }  // namespace
+
+void launch_skin_offsets(const DevView& v, cudaStream_t st) {
+  skin_offsets_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(v);
+}
+
+void launch_mark_rebuild(const DevView& v, bool now, bool next_step, cudaStream_t st) {
+  mark_rebuild_kernel<<<1, 1, 0, st>>>(v.sc, now ? 1 : 0, next_step ? 1 : 0);
+}
 
 void launch_sort(const DevView& v, cudaStream_t st) {
   const Scratch& S = v.S;
@@ -343,9 +405,9 @@ void launch_sort(const DevView& v, cudaStream_t st) {
   cudaMemsetAsync(S.count, 0, sizeof(int) * (size_t)len, st);
   bin_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(v, v.alive, S.key, S.count, v.sc, v.o.dim, xsub);
   const int nb = (len + 1023) / 1024;
-  scan_blocks<<<nb, 1024, 0, st>>>(S.count, sstart, S.block_sums, len);
-  scan_sums<<<1, 1024, 0, st>>>(S.block_sums, nb, sstart + len);
-  scan_add<<<nb, 1024, 0, st>>>(sstart, S.block_sums, len);
+  scan_blocks<<<nb, 1024, 0, st>>>(S.count, sstart, S.block_sums, len, v.sc);
+  scan_sums<<<1, 1024, 0, st>>>(S.block_sums, nb, sstart + len, v.sc);
+  scan_add<<<nb, 1024, 0, st>>>(sstart, S.block_sums, len, v.sc);
   cudaMemsetAsync(S.count, 0, sizeof(int) * (size_t)len, st);
   scatter_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(S.key, sstart, S.count, S.tmp_perm, v.sc);
   rank_kernel<<<grid_for(v.ncap), kBT, 0, st>>>(S.key, sstart, S.tmp_perm, v, S.perm, v.sc, nbins);
@@ -365,9 +427,9 @@ namespace psph {
 // that takes its scratch from caller-owned or static device memory.
 void launch_exclusive_scan(const int* in, int* out, int len, int* block_sums, cudaStream_t st) {
   const int nb = (len + 1023) / 1024 > 0 ? (len + 1023) / 1024 : 1;
-  scan_blocks<<<nb, 1024, 0, st>>>(in, out, block_sums, len);
-  scan_sums<<<1, 1024, 0, st>>>(block_sums, nb, out + len);
-  scan_add<<<nb, 1024, 0, st>>>(out, block_sums, len);
+  scan_blocks<<<nb, 1024, 0, st>>>(in, out, block_sums, len, nullptr);
+  scan_sums<<<1, 1024, 0, st>>>(block_sums, nb, out + len, nullptr);
+  scan_add<<<nb, 1024, 0, st>>>(out, block_sums, len, nullptr);
 }
 
 }  // namespace psph

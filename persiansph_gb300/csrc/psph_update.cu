@@ -374,6 +374,26 @@ __global__ void __launch_bounds__(kUT) update_kernel(DevView v) {
   P.V4[s] = make_double4_32a(vel[0], vel[1], vel[2], p);
   P.H4[s] = H;
   if (out) v.alive[s] = 0;
+  if (o.skin > 0.f) {
+    // neighbour lists with a skin: the largest displacement since the last
+    // rebuild (from the FP32 offset the sort recorded), and a particle that
+    // left forces the next step to sort again
+    const int cell = v.S.cellid[s];
+    float d2 = 0.f;
+    if (cell >= 0) {
+      const int lk = cell - g.cell_base;
+      const int cx = lk % g.nc[0], t = lk / g.nc[0], cy = t % g.nc[1], cz = t / g.nc[1];
+      const float4 r = v.S.OFFREF[s];
+      const float e0 = (float)(x[0] - (g.blpf[0] + cx * g.cell_size[0])) - r.x;
+      const float e1 = (float)(x[1] - (g.blpf[1] + cy * g.cell_size[1])) - r.y;
+      const float e2 = (DIM == 3) ? (float)(x[2] - (g.blpf[2] + cz * g.cell_size[2])) - r.z : 0.f;
+      d2 = e0 * e0 + e1 * e1 + e2 * e2;
+    }
+    if (out || !(d2 == d2)) atomicOr(&v.sc->force_rebuild, 1);
+    const unsigned am = __activemask();
+    const unsigned m = __reduce_max_sync(am, __float_as_uint(d2 == d2 ? d2 : 0.f));
+    if ((int)(threadIdx.x & 31) == __ffs(am) - 1) atomicMax(&v.sc->disp2_bits, m);
+  }
 }
 
 }  // namespace
@@ -434,7 +454,8 @@ void launch_upload_pack(const double* sx, const double* sd, const double* sp, co
 
 int launches_per_step(const DevView& v) {
   return (v.o.fp32 ? 17 : 16) + (v.o.closure ? 1 : 0) + (v.o.has_solid ? 1 : 0) + (v.o.fp64_half ? 1 : 0) +
-         (v.o.mixed ? 2 : 0) + (v.o.couple_soil && v.o.swi != 2 ? 2 : 0) + (v.o.fsi ? 1 : 0);
+         (v.o.mixed ? 2 : 0) + (v.o.couple_soil && v.o.swi != 2 ? 2 : 0) + (v.o.fsi ? 1 : 0) +
+         (v.o.skin > 0.f ? 1 : 0);
 }
 
 }  // namespace psph

@@ -407,12 +407,12 @@ def _autotune(self, steps_per_trial: int = 5, cache: str | None = None) -> dict:
             known = {}
         if key in known:
             t = known[key]
-            self.set_tuning(t["pair_block"], t["cell_split"], t.get("nlist_stage", 0))
+            self.set_tuning(t["pair_block"], t["cell_split"], t.get("nlist_stage", 0), t.get("skin_permille", 0))
             return dict(t, cached=True)
     t = PsphTuning()
     self._check(self._lib.psph_autotune(self._ctx, int(steps_per_trial), C.byref(t)))
     out = {"pair_block": t.pair_block, "cell_split": t.cell_split, "nlist_stage": t.nlist_stage,
-           "ms_per_step": t.ms_per_step}
+           "skin_permille": t.skin_permille, "ms_per_step": t.ms_per_step}
     if cache:
         known = {}
         if os.path.exists(cache):
@@ -430,23 +430,33 @@ def _tuning(self) -> dict:
     t = PsphTuning()
     self._check(self._lib.psph_get_tuning(self._ctx, C.byref(t)))
     return {"pair_block": t.pair_block, "cell_split": t.cell_split, "nlist_stage": t.nlist_stage,
-            "ms_per_step": t.ms_per_step}
+            "skin_permille": t.skin_permille, "ms_per_step": t.ms_per_step}
 
 
-def _set_tuning(self, pair_block: int = 128, cell_split: int = 1, nlist_stage: int | None = None):
-    """Launch setting; nlist_stage None keeps the context's staging depth."""
+def _set_tuning(self, pair_block: int = 128, cell_split: int = 1, nlist_stage: int | None = None,
+                skin_permille: int | None = None):
+    """Launch setting; nlist_stage / skin_permille None keep the context's
+    staging depth / list skin (thousandths of the support, FP32C form)."""
+    cur = PsphTuning()
+    self._check(self._lib.psph_get_tuning(self._ctx, C.byref(cur)))
     if nlist_stage is None:
-        cur = PsphTuning()
-        self._check(self._lib.psph_get_tuning(self._ctx, C.byref(cur)))
         nlist_stage = cur.nlist_stage
-    t = PsphTuning(pair_block, cell_split, nlist_stage, 0, 0.0)
+    if skin_permille is None:
+        skin_permille = cur.skin_permille
+    t = PsphTuning(pair_block, cell_split, nlist_stage, skin_permille, 0.0)
     self._check(self._lib.psph_set_tuning(self._ctx, C.byref(t)))
+
+
+def _list_rebuilds(self) -> int:
+    """Steps since upload that ran the cell sort and the neighbour lists."""
+    return int(self._lib.psph_list_rebuilds(self._ctx))
 
 
 for _cls in (GpuDomain, GpuEnsemble):
     _cls.autotune = _autotune
     _cls.tuning = _tuning
     _cls.set_tuning = _set_tuning
+    _cls.list_rebuilds = _list_rebuilds
     _cls.attach_closure = _attach_closure
     _cls.closure_stats = _closure_stats
     _cls.closure_features = _closure_features
