@@ -2356,8 +2356,11 @@ psph_status apply_skin(psph_ctx* c, float skin) {
     g.cell_base = (int)base;
     base += g.ncells;
   }
-  if (c->uploaded)
-    CUDA_TRY(c, cudaMemcpy(c->d_grids, gd.data(), gd.size() * sizeof(GridDev), cudaMemcpyHostToDevice));
+  if (c->uploaded) {  // after the context's own work (its stream), before its next launch
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_grids, gd.data(), gd.size() * sizeof(GridDev), cudaMemcpyHostToDevice,
+                                c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  }
   c->total_cells = (int)base;
   c->opt.skin = skin;
   c->opt.skin_disp2 = disp2;
