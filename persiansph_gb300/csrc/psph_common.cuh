@@ -114,6 +114,21 @@ struct StepScalars {
   unsigned int rebuilds;   // steps that sorted and listed since upload
 };
 
+// A double's value in FP32 (truncated, not rounded) from its bits on the
+// integer pipe: the estimates below need ~1e-6 relative accuracy, and a
+// double-to-float conversion instruction runs on the FP64 pipe. Finite
+// inputs; magnitudes outside FP32's normal range give 0 or infinity.
+PSPH_D float d2f_bits(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+  const unsigned sign = hi & 0x80000000u;
+  if (e <= 0) return __int_as_float((int)sign);
+  if (e >= 255) return __int_as_float((int)(sign | 0x7f800000u));
+  const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+  return __int_as_float((int)(sign | ((unsigned)e << 23) | m));
+}
+
 struct GridDev {
   double blpf[3], trpr[3], cell_size[3], dom_size[3];
   double hmax, cellfac;

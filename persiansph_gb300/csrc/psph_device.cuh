@@ -37,7 +37,7 @@ struct Scratch {
   int* block_sums;
   // per-step derived / outputs
   float4* OFF32;     // (position - cell origin, h) in FP32, written by the reorder
-  float4* OFFREF;    // with a skin: OFF32 at the last rebuild (displacements are measured from it)
+  float4* OFFREF;    // with a skin: the position at the last rebuild in FP32 (displacements are measured from it)
   int* refcell;      // with a skin: each particle's cell in the reference's grid (x | y << 10 | z << 20),
                      // for the wall pressure's pair orientation
   int* nl;           // per-step neighbour lists, entry k of particle i at nl[k*ncap + i]:

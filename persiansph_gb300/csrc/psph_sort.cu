@@ -26,21 +26,6 @@ namespace {
 
 constexpr int kBT = 256;
 
-// A double's value in FP32 (truncated, not rounded) from its bits on the
-// integer pipe: the estimates below need ~1e-6 relative accuracy, and a
-// double-to-float conversion instruction runs on the FP64 pipe. Finite
-// inputs; magnitudes outside FP32's normal range give 0 or infinity.
-__device__ __forceinline__ float d2f_bits(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
-  const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
-  const unsigned sign = hi & 0x80000000u;
-  if (e <= 0) return __int_as_float((int)sign);
-  if (e >= 255) return __int_as_float((int)(sign | 0x7f800000u));
-  const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
-  return __int_as_float((int)(sign | ((unsigned)e << 23) | m));
-}
-
 __global__ void bin_kernel(DevView v, const uint8_t* __restrict__ alive, int* __restrict__ key,
                            int* __restrict__ count, StepScalars* sc, int dim, int xsub) {
   if (sc->all_stop || !sc->rebuild) return;
@@ -247,7 +232,8 @@ __global__ void reorder_kernel(DevView v, const int* __restrict__ perm, const in
       } else {
         v.S.OFF32[s] = make_float4((float)xs.x, (float)xs.y, (float)xs.z, h);
       }
-      if (v.o.skin > 0.f) v.S.OFFREF[s] = v.S.OFF32[s];  // displacements are measured from here
+      if (v.o.skin > 0.f)  // displacements are measured from here (FP32, truncated)
+        v.S.OFFREF[s] = make_float4(d2f_bits(xs.x), d2f_bits(xs.y), d2f_bits(xs.z), 0.f);
     }
     dst.orig[s] = src.orig[i];
     if (src.io) dst.io[s] = src.io[i];

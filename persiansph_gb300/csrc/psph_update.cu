@@ -376,17 +376,14 @@ __global__ void __launch_bounds__(kUT) update_kernel(DevView v) {
   if (out) v.alive[s] = 0;
   if (o.skin > 0.f) {
     // neighbour lists with a skin: the largest displacement since the last
-    // rebuild (from the FP32 offset the sort recorded), and a particle that
-    // left forces the next step to sort again
-    const int cell = v.S.cellid[s];
+    // rebuild (from the FP32 position the sort recorded; both truncated on the
+    // integer pipe, this kernel's FP64 pipe being its limit), and a particle
+    // that left forces the next step to sort again
     float d2 = 0.f;
-    if (cell >= 0) {
-      const int lk = cell - g.cell_base;
-      const int cx = lk % g.nc[0], t = lk / g.nc[0], cy = t % g.nc[1], cz = t / g.nc[1];
+    if (v.S.cellid[s] >= 0) {
       const float4 r = v.S.OFFREF[s];
-      const float e0 = (float)(x[0] - (g.blpf[0] + cx * g.cell_size[0])) - r.x;
-      const float e1 = (float)(x[1] - (g.blpf[1] + cy * g.cell_size[1])) - r.y;
-      const float e2 = (DIM == 3) ? (float)(x[2] - (g.blpf[2] + cz * g.cell_size[2])) - r.z : 0.f;
+      const float e0 = d2f_bits(x[0]) - r.x, e1 = d2f_bits(x[1]) - r.y;
+      const float e2 = (DIM == 3) ? d2f_bits(x[2]) - r.z : 0.f;
       d2 = e0 * e0 + e1 * e1 + e2 * e2;
     }
     if (out || !(d2 == d2)) atomicOr(&v.sc->force_rebuild, 1);
