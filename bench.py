@@ -324,9 +324,10 @@ def main():
     ap.add_argument("--dx", type=float, default=None, help="lattice spacing (default: the workload's)")
     ap.add_argument("--ref-dx", type=float, default=None, help="lattice spacing of the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--develop", type=float, default=0.1,
+    ap.add_argument("--develop", type=float, default=0.25,
                     help="physical time (s) the workload is advanced with the headline form before any timing "
-                         "(0: time from rest)")
+                         "(0: time from rest); the default times the dam break's surge at speed, where lists "
+                         "with a skin are rebuilt most often")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched granular-column line")
     ap.add_argument("--tuning", default="auto",
                     help="'auto' (psph_autotune on the workload's own steps) or BLOCK:SPLIT[:STAGE[:SKIN]] to fix the "
