@@ -372,9 +372,13 @@ def main():
         if state is None:
             ps = dom.particles.copy()
         else:
+            # the workload's fields and the flow's state (the initial lattice
+            # sets no velocity: v and the integrator's histories come along)
             ps = ParticleSet(state[0].n)
-            for f in dom.particles.arrays():
-                ps.set(f, state[0].get(f).copy())
+            for f in set(dom.particles.arrays()) | {"x", "v", "va", "vb", "density", "densitya", "densityb",
+                                                    "pressure"}:
+                if state[0].has(f):
+                    ps.set(f, state[0].get(f).copy())
             if not closure:  # the constant viscosity, not the developed eddy viscosity
                 ps.set("mu", dom.particles.get("mu").copy())
         ps.set("les", np.full(ps.n, 1 if closure else 0, np.int32))
