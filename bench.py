@@ -434,10 +434,11 @@ def main():
         rebuilds = gd.list_rebuilds() - rb0
         ms = max_over_ranks(ms, dist, "cuda")
         launches = gd.last_launch_count()
-        # per-phase device times (separate short run, events between phases)
+        # per-phase device times (separate run, events between phases; long
+        # enough to hold the rebuilds of a list skin)
         gd.enable_timing(True)
-        gd.step(3)
-        phases = {k: x / 3.0 for k, x in gd.phase_times().items()}
+        gd.step(24)
+        phases = {k: x / 24.0 for k, x in gd.phase_times().items()}
         gd.enable_timing(False)
         pairs = pc1 - pc0
         cstats = gd.closure_stats() if closure else (0, 0)
