@@ -74,14 +74,16 @@ FORCE32_BYTES_PER_PARTICLE = {False: 104, True: 148}
 # DRAM bytes per particle one launch actually moved: ncu captures of the same
 # kernels on the same tank at dx = 10 mm (1,021,104 particles),
 # dram__bytes_read.sum + dram__bytes_write.sum per particle (LES + closure
-# flavour: 283.39 + 56.51 MB; without LES: an earlier capture of that
-# flavour); the traffic grows with the
-# particle count, so a full-size launch moves this x n. Most of the excess over
-# the algorithmic bytes is the neighbour list (~80 entries x 4 B a particle).
-FORCE32_TRAFFIC_BYTES_PER_PARTICLE = {False: 304.6, True: 332.9}
-# Pipe activity of that launch (LES + closure flavour) and of the FP64 pair
-# kernel (pass A) in the same capture series (sm__pipe_*_cycles_active, % of peak).
-FORCE32_NCU = {"issue_active": 0.573, "fma_pipe": 0.294, "fp64_pipe": 0.040, "warps_active": 0.298}
+# flavour with the 5 % list skin the autotuner picks: 276.56 + 54.12 MB; without
+# LES: an earlier capture of that flavour, lists every step); the traffic grows
+# with the particle count, so a full-size launch moves this x n. Most of the
+# excess over the algorithmic bytes is the neighbour list (~80 entries x 4 B a
+# particle).
+FORCE32_TRAFFIC_BYTES_PER_PARTICLE = {False: 304.6, True: 323.9}
+# Pipe activity of that launch (LES + closure flavour, list skin) and of the FP64
+# pair kernel (pass A) in the same capture series (sm__pipe_*_cycles_active, % of
+# peak).
+FORCE32_NCU = {"issue_active": 0.573, "fma_pipe": 0.297, "fp64_pipe": 0.040, "warps_active": 0.298}
 FORCE64_NCU_FP64_PIPE = 0.834
 
 
@@ -527,7 +529,8 @@ def main():
                      "kernel": "forces_fluid32_kernel", "peak_source": pk["src"],
                      "bytes_per_particle": FORCE32_BYTES_PER_PARTICLE[cl],
                      "note": "latency-bound gather kernel (neither HBM nor tensor bound); ncu pipe activity of "
-                             "the same kernel at dx=10 mm in ncu_small_case",
+                             "the same kernel at dx=10 mm in ncu_small_case "
+                             "(profiles/pair_kernel_skin_dam3d_10mm.md)",
                      "ncu_small_case": FORCE32_NCU},
         "roofline_fp64": {"bound": "fp64", "kernel": "forces_fluid_kernel", "achieved": fp64_tflops,
                           "peak": fp64.value, "unit": "TFLOP/s",
