@@ -33,14 +33,18 @@ def test_poiseuille_reaches_analytic_profile(gpu, precision):
     assert err <= 0.005, f"L2 error {err:.4f} against the analytic Poiseuille profile"
 
 
-@pytest.mark.parametrize("precision", [0, 1])
-def test_surge_front_follows_reference(gpu, precision):
+@pytest.mark.parametrize("precision,skin", [(0, 0), (1, 0), (1, 100)])
+def test_surge_front_follows_reference(gpu, precision, skin):
+    """The surge front of a 2D dam break within 1 % of the reference's; the
+    FP32C form also with neighbour lists kept under a 10 % skin."""
     g = dict(np.load(os.path.join(GOLD, "surge2d.npz")))
     dom, dt, _ = surge2d()
     cfg = dom.config(dt)
     cfg.precision = precision
     gd = GpuDomain(cfg)
     gd.upload(dom.particles, initial=True)
+    if skin:
+        gd.set_tuning(128, 1, 0, skin)
     times, fronts, prev = [], [], 0
     for k in SURGE_STEPS:
         gd.step(k - prev)
@@ -51,3 +55,5 @@ def test_surge_front_follows_reference(gpu, precision):
     ours = np.interp(g["time"], times, fronts)
     rel = np.abs(ours - g["front"]) / g["front"]
     assert rel.max() <= 0.01, f"surge front differs from the reference by {rel.max():.4f}"
+    if skin:  # the lists were kept on most steps
+        assert gd.list_rebuilds() < SURGE_STEPS[-1] // 2
