@@ -28,6 +28,39 @@ PSPH_D double J2of(const double* S) {
   return 0.5 * (S[0] * S[0] + 2.0 * S[1] * S[3] + 2.0 * S[2] * S[6] + S[4] * S[4] + 2.0 * S[5] * S[7] + S[8] * S[8]);
 }
 
+// Plane strain (2D): a tensor's xz, yz, zx and zy entries (2, 5, 6, 7) are
+// exact zeros in the strain rate, the stresses and the strains, and the
+// rotation rate holds only its xy / yx entries, when particles share one z and
+// v_z = 0 (the update zeroes it). Every product with those entries is then an
+// exact zero, so PL = true evaluates the same expressions on entries 0, 1, 3,
+// 4, 8 only and stores zeros in the rest (the FP64 pipe bounds this kernel).
+// live<PL>(e): entry e is evaluated.
+template <bool PL>
+PSPH_D constexpr bool live(int e) {
+  return !PL || (e != 2 && e != 5 && e != 6 && e != 7);
+}
+
+template <bool PL>
+PSPH_D double J2of_t(const double* S) {
+  if (!PL) return J2of(S);
+  return 0.5 * (S[0] * S[0] + 2.0 * S[1] * S[3] + S[4] * S[4] + S[8] * S[8]);
+}
+
+// True when the entries that PL = true leaves out are zeros (either sign) in
+// every tensor the Mat3 update and the strain integration read.
+PSPH_D bool plane_zeros(const double* SR, const double* RR, const double* Sig, const double* Sh, const double* E,
+                        const double* Eh) {
+  unsigned long long b = 0;
+  const double* T[6] = {SR, RR, Sig, Sh, E, Eh};
+#pragma unroll
+  for (int t = 0; t < 6; ++t)
+    b |= (unsigned long long)__double_as_longlong(T[t][2]) | (unsigned long long)__double_as_longlong(T[t][5]) |
+         (unsigned long long)__double_as_longlong(T[t][6]) | (unsigned long long)__double_as_longlong(T[t][7]);
+  b |= (unsigned long long)__double_as_longlong(RR[0]) | (unsigned long long)__double_as_longlong(RR[4]) |
+       (unsigned long long)__double_as_longlong(RR[8]);
+  return (b << 1) == 0ull;
+}
+
 PSPH_D double OIe(int e) { return (e == 0 || e == 4 || e == 8) ? 1.0 : 0.0; }
 
 // 2G(D - tr D/3 I) + S W^T + W S (solid, around ShearStress)
@@ -43,15 +76,28 @@ PSPH_D void mat2_rate(const double* SR, const double* RR, const double* SS, doub
 }
 
 // K tr(D) I + 2G(D - tr D/3 I) + Sigma W^T + W Sigma (soil, around Sigma)
+template <bool PL>
 PSPH_D void mat3_rate(const double* SR, const double* RR, const double* Sg, double K, double G, double* X) {
-  double RRT[9], SRT[9], RS[9];
-  for (int r = 0; r < 3; ++r)
-    for (int c = 0; c < 3; ++c) RRT[3 * r + c] = RR[3 * c + r];
-  mat_mult(Sg, RRT, SRT);
-  mat_mult(RR, Sg, RS);
+  double SRT[9], RS[9];
+  if (PL) {  // W = RR[1] (xy), RR[3] (yx): the nonzero terms of mat_mult's sums
+    SRT[0] = Sg[1] * RR[1]; SRT[1] = Sg[0] * RR[3]; SRT[3] = Sg[4] * RR[1]; SRT[4] = Sg[3] * RR[3];
+    RS[0] = RR[1] * Sg[3]; RS[1] = RR[1] * Sg[4]; RS[3] = RR[3] * Sg[0]; RS[4] = RR[3] * Sg[1];
+    SRT[8] = RS[8] = 0.0;
+  } else {
+    double RRT[9];
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) RRT[3 * r + c] = RR[3 * c + r];
+    mat_mult(Sg, RRT, SRT);
+    mat_mult(RR, Sg, RS);
+  }
   const double I1s = SR[0] + SR[4] + SR[8];
   const double sK = I1s * K, s3 = 1.0 / 3.0 * I1s, g2 = 2.0 * G;
-  for (int e = 0; e < 9; ++e) X[e] = ((OIe(e) * sK + ((SR[e] - OIe(e) * s3) * g2)) + SRT[e]) + RS[e];
+#pragma unroll
+  for (int e = 0; e < 9; ++e) {
+    if (!live<PL>(e)) { X[e] = 0.0; continue; }
+    if (PL && e == 8) X[e] = sK + ((SR[e] - s3) * g2);
+    else X[e] = ((OIe(e) * sK + ((SR[e] - OIe(e) * s3) * g2)) + SRT[e]) + RS[e];
+  }
 }
 
 PSPH_D double dp_apex(double* S, double alpha, double kf) {
@@ -66,9 +112,11 @@ PSPH_D double dp_apex(double* S, double alpha, double kf) {
   return I1;
 }
 
+template <bool PL = false>
 PSPH_D void deviator(const double* S, double I1, double* D) {
   const double s = 1.0 / 3.0 * I1;
-  for (int e = 0; e < 9; ++e) D[e] = S[e] - OIe(e) * s;
+#pragma unroll
+  for (int e = 0; e < 9; ++e) D[e] = live<PL>(e) ? S[e] - OIe(e) * s : 0.0;
 }
 
 // Drucker-Prager return (Source/Particle.cpp:357-425 / :677-746).
@@ -86,19 +134,22 @@ PSPH_D void dp_constants(double phi, double c, double I22, double* alpha, double
   }
 }
 
+template <bool PL>
 PSPH_D void dp_return(const PClass& C, double I22, double* Sig, const double* Sn, const double* SR, double I1strain,
                       double fac, double* SS) {
   const double alpha = C.dp_alpha, kf = C.dp_kf;  // dp_constants of the class (class_constants_kernel)
   const double K = C.k_mod, G = C.g_mod;
   double I1 = dp_apex(Sig, alpha, kf);
-  deviator(Sig, I1, SS);
-  double J2 = J2of(SS);
+  deviator<PL>(Sig, I1, SS);
+  double J2 = J2of_t<PL>(SS);
   if ((sqrt(J2) + alpha * I1 - kf) > 0.0) {
-    deviator(Sn, Sn[0] + Sn[4] + Sn[8], SS);
-    J2 = J2of(SS);
+    deviator<PL>(Sn, Sn[0] + Sn[4] + Sn[8], SS);
+    J2 = J2of_t<PL>(SS);
     if (sqrt(J2) > 0.0) {
       double sum = SS[0] * SR[0];
-      for (int e = 1; e < 9; ++e) sum = sum + SS[e] * SR[e];
+#pragma unroll
+      for (int e = 1; e < 9; ++e)
+        if (live<PL>(e)) sum = sum + SS[e] * SR[e];
       const double gj = G / sqrt(J2);
       double dL, s;
       if (C.fail == 2) {
@@ -108,17 +159,85 @@ PSPH_D void dp_return(const PClass& C, double I22, double* Sig, const double* Sn
         dL = 1.0 / (9.0 * alpha * K * 3.0 * C.dp_sin_psi + G) * ((3.0 * alpha * K * I1strain) + (G / sqrt(J2)) * sum);
         s = 3.0 * 3.0 * C.dp_sin_psi * K;
       }
+#pragma unroll
       for (int e = 0; e < 9; ++e) {
+        if (!live<PL>(e)) continue;  // stays zero
         const double Ie = (e == 8) ? I22 : OIe(e);
         Sig[e] = Sig[e] - ((Ie * s + SS[e] * gj) * dL) * fac;
       }
     }
     I1 = dp_apex(Sig, alpha, kf);
-    deviator(Sig, I1, SS);
-    J2 = J2of(SS);
+    deviator<PL>(Sig, I1, SS);
+    J2 = J2of_t<PL>(SS);
     if ((sqrt(J2) + alpha * I1 - kf) > 0.0 && sqrt(J2) > 0.0) {
       const double s1 = I1 / 3.0, s2 = (kf - alpha * I1) / sqrt(J2);
-      for (int e = 0; e < 9; ++e) Sig[e] = OIe(e) * s1 + SS[e] * s2;
+#pragma unroll
+      for (int e = 0; e < 9; ++e)
+        if (live<PL>(e)) Sig[e] = OIe(e) * s1 + SS[e] * s2;
+    }
+  }
+}
+
+// Mat3Leapfrog / Mat3MVerlet (Source/Particle.cpp:641-795 / :320-482) on one
+// particle's stress: Sig (in/out), Sh (the half-step or previous stress),
+// So (scratch), SS (the deviator out, when the state keeps one).
+template <bool PL>
+PSPH_D void mat3_update(const PClass& C, double I22, bool lf, int first, int ct, double dt, const double* SR,
+                        const double* RR, double* Sig, double* Sh, double* So, double* SS) {
+  double X9[9], Sn[9], SSd[9];
+  mat3_rate<PL>(SR, RR, Sig, C.k_mod, C.g_mod, X9);
+  const double I1strain = SR[0] + SR[4] + SR[8];
+#pragma unroll
+  for (int e = 0; e < 9; ++e) Sn[e] = live<PL>(e) ? Sig[e] : 0.0;
+  bool have_dev = false;
+  if (lf) {
+    if (first)
+#pragma unroll
+      for (int e = 0; e < 9; ++e) Sh[e] = live<PL>(e) ? X9[e] * (-dt / 2.0) + Sig[e] : 0.0;
+#pragma unroll
+    for (int e = 0; e < 9; ++e) {
+      if (!live<PL>(e)) { So[e] = Sh[e] = 0.0; continue; }
+      So[e] = Sh[e];
+      Sh[e] = X9[e] * dt + Sh[e];
+    }
+    if (C.fail > 1) { dp_return<PL>(C, I22, Sh, Sn, SR, I1strain, dt, SSd); have_dev = true; }
+#pragma unroll
+    for (int e = 0; e < 9; ++e) Sig[e] = live<PL>(e) ? (Sh[e] + So[e]) * (1.0 / 2.0) : 0.0;
+  } else {
+#pragma unroll
+    for (int e = 0; e < 9; ++e)
+      Sig[e] = !live<PL>(e) ? 0.0 : (ct == 30) ? X9[e] * dt + Sig[e] : X9[e] * (2.0 * dt) + Sh[e];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) Sh[e] = Sn[e];
+    if (C.fail > 1) { dp_return<PL>(C, I22, Sig, Sn, SR, I1strain, (ct == 30) ? dt : 2.0 * dt, SSd); have_dev = true; }
+  }
+  if (have_dev && SS)
+#pragma unroll
+    for (int e = 0; e < 9; ++e) SS[e] = SSd[e];
+}
+
+// Strain integration of Mat2 and Mat3 (the same Leapfrog / MVerlet steps as
+// the stress).
+template <bool PL>
+PSPH_D void strain_update(bool lf, int first, int ct, double dt, const double* SR, double* E, double* Eh, double* Eo) {
+  if (lf) {
+    if (first)
+#pragma unroll
+      for (int e = 0; e < 9; ++e) Eh[e] = live<PL>(e) ? SR[e] * (-dt / 2.0) + E[e] : 0.0;
+#pragma unroll
+    for (int e = 0; e < 9; ++e) {
+      if (!live<PL>(e)) { Eo[e] = Eh[e] = E[e] = 0.0; continue; }
+      Eo[e] = Eh[e];
+      Eh[e] = SR[e] * dt + Eh[e];
+      E[e] = (Eh[e] + Eo[e]) * (1.0 / 2.0);
+    }
+  } else {
+#pragma unroll
+    for (int e = 0; e < 9; ++e) {
+      if (!live<PL>(e)) { E[e] = Eh[e] = 0.0; continue; }
+      const double old = E[e];
+      E[e] = (ct == 30) ? SR[e] * dt + E[e] : SR[e] * (2.0 * dt) + Eh[e];
+      Eh[e] = old;
     }
   }
 }
@@ -284,6 +403,7 @@ __global__ void __launch_bounds__(kUT) update_kernel(DevView v) {
     double* Eo = v.S.strain_o + 9 * (size_t)s;
     const double I22 = (DIM == 2) ? 0.0 : 1.0;
     const bool lf = (o.scheme != PSPH_MVERLET);
+    bool plane = false;
     if (mat == 2) {
       // Mat2Leapfrog / Mat2MVerlet (Source/Particle.cpp:598-639 / :276-318)
       p = eos(C.pres_eq, C.cs, C.p0, rho, C.rho0);
@@ -318,47 +438,14 @@ __global__ void __launch_bounds__(kUT) update_kernel(DevView v) {
         for (int e = 0; e < 9; ++e) SS[e] = (SSh[e] + SSo[e]) * (1.0 / 2.0);
       for (int e = 0; e < 9; ++e) Sig[e] = OIe(e) * -p + SS[e];
     } else {
-      // Mat3Leapfrog / Mat3MVerlet (Source/Particle.cpp:641-795 / :320-482)
-      double X9[9], Sn[9], SSd[9];
-      mat3_rate(SR, RR, Sig, C.k_mod, C.g_mod, X9);
-      const double I1strain = SR[0] + SR[4] + SR[8];
-      for (int e = 0; e < 9; ++e) Sn[e] = Sig[e];
-      bool have_dev = false;
-      if (lf) {
-        if (first)
-          for (int e = 0; e < 9; ++e) Sh[e] = X9[e] * (-dt / 2.0) + Sig[e];
-        for (int e = 0; e < 9; ++e) {
-          So[e] = Sh[e];
-          Sh[e] = X9[e] * dt + Sh[e];
-        }
-        if (C.fail > 1) { dp_return(C, I22, Sh, Sn, SR, I1strain, dt, SSd); have_dev = true; }
-        for (int e = 0; e < 9; ++e) Sig[e] = (Sh[e] + So[e]) * (1.0 / 2.0);
-      } else {
-        for (int e = 0; e < 9; ++e) Sig[e] = (ct == 30) ? X9[e] * dt + Sig[e] : X9[e] * (2.0 * dt) + Sh[e];
-        for (int e = 0; e < 9; ++e) Sh[e] = Sn[e];
-        if (C.fail > 1) { dp_return(C, I22, Sig, Sn, SR, I1strain, (ct == 30) ? dt : 2.0 * dt, SSd); have_dev = true; }
-      }
-      if (have_dev && P.shear) {
-        double* SS = P.shear + 9 * (size_t)s;
-        for (int e = 0; e < 9; ++e) SS[e] = SSd[e];
-      }
+      double* SS = P.shear ? P.shear + 9 * (size_t)s : nullptr;
+      plane = (DIM == 2) && plane_zeros(SR, RR, Sig, Sh, E, Eh);
+      if (plane) mat3_update<true>(C, I22, lf, first, ct, dt, SR, RR, Sig, Sh, So, SS);
+      else mat3_update<false>(C, I22, lf, first, ct, dt, SR, RR, Sig, Sh, So, SS);
     }
     // strain integration (shared by Mat2 and Mat3)
-    if (lf) {
-      if (first)
-        for (int e = 0; e < 9; ++e) Eh[e] = SR[e] * (-dt / 2.0) + E[e];
-      for (int e = 0; e < 9; ++e) {
-        Eo[e] = Eh[e];
-        Eh[e] = SR[e] * dt + Eh[e];
-        E[e] = (Eh[e] + Eo[e]) * (1.0 / 2.0);
-      }
-    } else {
-      for (int e = 0; e < 9; ++e) {
-        const double old = E[e];
-        E[e] = (ct == 30) ? SR[e] * dt + E[e] : SR[e] * (2.0 * dt) + Eh[e];
-        Eh[e] = old;
-      }
-    }
+    if (plane) strain_update<true>(lf, first, ct, dt, SR, E, Eh, Eo);
+    else strain_update<false>(lf, first, ct, dt, SR, E, Eh, Eo);
   }
   // periodic wrap (Source/Particle.cpp:128-142) and CheckParticleLeave's test
   bool out = false;
