@@ -12,6 +12,7 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "psph.h"
 
@@ -128,6 +129,60 @@ PSPH_D float d2f_bits(double x) {
   const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
   return __int_as_float((int)(sign | ((unsigned)e << 23) | m));
 }
+
+// Double to float, rounded to nearest even (IEEE 754), on the integer pipe:
+// the same value as (float)x, without the FP64-pipe conversion instruction.
+// The 52-bit significand keeps its top 23 bits; the 29 dropped bits round up
+// past half, or at exactly half when the kept part is odd (a carry into the
+// exponent is the next binade). Magnitudes outside [2^-74, 2^127) (the top
+// binade may round to infinity, whose residual is infinite), infinities and
+// NaN take the conversion instruction.
+// d2f_split also returns lo = (float)(x - (double)hi), the rounding residual
+// x - hi (exact in FP64: the dropped bits, or minus their complement to the
+// next unit when hi rounded up) as float(+-bits) * 2^(E-1075), one rounding
+// of an integer below 2^29 and an exact power-of-two scaling in FP32's normal
+// range.
+__host__ __device__ inline unsigned long long psph_dbits(double x) {
+#ifdef __CUDA_ARCH__
+  return (unsigned long long)__double_as_longlong(x);
+#else
+  unsigned long long b;
+  memcpy(&b, &x, sizeof b);
+  return b;
+#endif
+}
+__host__ __device__ inline float psph_fbits(unsigned u) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(u);
+#else
+  float f;
+  memcpy(&f, &u, sizeof f);
+  return f;
+#endif
+}
+
+__host__ __device__ inline float d2f_split(double x, float* lo) {
+  const unsigned long long b = psph_dbits(x);
+  const unsigned E = (unsigned)(b >> 52) & 0x7ffu;
+  if (E < 949u || E > 1149u) {
+    const float h = (float)x;
+    if (lo) *lo = (float)(x - (double)h);
+    return h;
+  }
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  const unsigned long long m = b & 0xfffffffffffffull;
+  const unsigned keep = (unsigned)(m >> 29), rem = (unsigned)m & 0x1fffffffu;
+  const bool up = rem > 0x10000000u || (rem == 0x10000000u && (keep & 1u));
+  const unsigned hb = sign | (((E - 896u) << 23) + keep + (up ? 1u : 0u));
+  if (lo) {
+    const float scale = psph_fbits((E - 948u) << 23);  // 2^(E-1075)
+    int q = (int)(up ? rem - 0x20000000u : rem);
+    if (sign) q = -q;
+    *lo = (float)q * scale;  // +0 when exact, as x - (double)hi gives
+  }
+  return psph_fbits(hb);
+}
+__host__ __device__ inline float d2f_rn(double x) { return d2f_split(x, nullptr); }
 
 struct GridDev {
   double blpf[3], trpr[3], cell_size[3], dom_size[3];

@@ -34,6 +34,29 @@ PSPH_D void tensile_tir(const double* S, double TI, double rho, double* TIR) {
   // reference's R diag(0) R^T is zero. The bound is conservative by 1e-12 of
   // the stress scale, far above the rounding of either eigen-decomposition,
   // and skips the FP64 trigonometry or Jacobi sweeps for these particles.
+  // The same bound first in FP32 from truncated copies (integer pipe, no FP64
+  // square root): their errors stay below ~1e-6 of the scale, so an FP32
+  // bound under -1e-5 of the scale implies the exact test below.
+  {
+    float bound, scale;
+    const float s0 = d2f_bits(S[0]), s1 = d2f_bits(S[1]), s4 = d2f_bits(S[4]);
+    if (DIM == 2) {
+      const float m = 0.5f * (s0 + s4), d = 0.5f * (s0 - s4);
+      bound = m + sqrtf(d * d + s1 * s1);
+      scale = fabsf(s0) + fabsf(s4) + fabsf(s1);
+    } else {
+      const float s2 = d2f_bits(S[2]), s3 = d2f_bits(S[3]), s5 = d2f_bits(S[5]);
+      const float s6 = d2f_bits(S[6]), s7 = d2f_bits(S[7]), s8 = d2f_bits(S[8]);
+      bound = fmaxf(s0 + fabsf(s1) + fabsf(s2), fmaxf(s4 + fabsf(s3) + fabsf(s5), s8 + fabsf(s6) + fabsf(s7)));
+      scale = fabsf(s0) + fabsf(s4) + fabsf(s8) + fabsf(s1) + fabsf(s2) + fabsf(s5);
+    }
+    if (bound < -1e-5f * scale) {
+      if (DIM == 2) TIR[0] = TIR[1] = TIR[3] = TIR[4] = 0.0;
+      else
+        for (int e = 0; e < 9; ++e) TIR[e] = 0.0;
+      return;
+    }
+  }
   {
     double bound, scale;
     if (DIM == 2) {

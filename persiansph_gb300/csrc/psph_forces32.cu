@@ -145,18 +145,20 @@ __global__ void __launch_bounds__(kFT32) copies32_kernel(DevView v) {
   const PClass32& C = v.cls32[P.cls[w]];
   if (v.inst[C.inst].stop) return;
   const double4_32a vv = P.V4[w];
-  const float p = (float)vv.w;
-  const float vx = (float)vv.x, vy = (float)vv.y, vz = (float)vv.z;
+  // every conversion on the integer pipe (d2f_rn / d2f_split: the values of
+  // the conversion instruction, which runs on the FP64 pipe)
+  const float p = d2f_rn(vv.w);
+  float lx, ly, lz;
+  const float vx = d2f_split(vv.x, &lx), vy = d2f_split(vv.y, &ly), vz = d2f_split(vv.z, &lz);
   v.S.V32[w] = make_float4(vx, vy, vz, p);
   // the velocity's low-order part: in a smooth flow v_i - v_j is far smaller
   // than v, and the pair differences take (hi_i - hi_j) + (lo_i - lo_j), exact
   // to ~2^-48 of |v|; the class index and its flags ride along in .w (class |
   // flags << 16: one load per pair, and no class-table load when the pair
   // constants are uniform)
-  v.S.V32LO[w] = make_float4((float)(vv.x - (double)vx), (float)(vv.y - (double)vy), (float)(vv.z - (double)vz),
-                             __int_as_float(P.cls[w] | (C.flags << 16)));
+  v.S.V32LO[w] = make_float4(lx, ly, lz, __int_as_float(P.cls[w] | (C.flags << 16)));
   if (C.flags & CF_FREE) {
-    const float rho = (float)P.X4[w].w;
+    const float rho = d2f_rn(P.X4[w].w);
     const float inv = 1.f / rho;
     const float ratio = rho / C.rho0;
     const float c = (C.pres_eq == 1) ? C.cs * ratio * ratio * ratio : C.cs;
@@ -164,7 +166,7 @@ __global__ void __launch_bounds__(kFT32) copies32_kernel(DevView v) {
   }
   // FP32 copy of a per-particle viscosity: the pair loop then converts nothing
   // (a double-to-float conversion runs on the FP64 pipe, 1/64 of the FP32 rate)
-  if (v.o.dyn_mu) v.S.MU32[w] = (float)P.mu[w];
+  if (v.o.dyn_mu) v.S.MU32[w] = d2f_rn(P.mu[w]);
 }
 
 template <int DIM, int KT>
@@ -564,9 +566,12 @@ __global__ void __maxnreg__(FL == 0 ? 128 : (FL == 1 ? 80 : 96)) forces_fluid32_
 // ---------------------------------------------------------------------------
 // Symmetric 3x3 tensor (the stresses and TIR are symmetric: Jaumann rate of a
 // symmetric stress, R diag R^T) as 6 floats in two float4: 00 01 02 11 | 12 22.
+// An off-diagonal pair agrees to FP64 rounding (the two entries come from the
+// same terms summed in another order), far below FP32's: the upper entry is
+// taken. Conversions on the integer pipe (d2f_rn), no FP64 instruction.
 PSPH_D void sym_store(float4* dst, size_t w, const double* m) {
-  dst[2 * w] = make_float4((float)m[0], (float)(0.5 * (m[1] + m[3])), (float)(0.5 * (m[2] + m[6])), (float)m[4]);
-  dst[2 * w + 1] = make_float4((float)(0.5 * (m[5] + m[7])), (float)m[8], 0.f, 0.f);
+  dst[2 * w] = make_float4(d2f_rn(m[0]), d2f_rn(m[1]), d2f_rn(m[2]), d2f_rn(m[4]));
+  dst[2 * w + 1] = make_float4(d2f_rn(m[5]), d2f_rn(m[8]), 0.f, 0.f);
 }
 
 template <int DIM>
@@ -579,21 +584,22 @@ __global__ void __launch_bounds__(kFT32) solid_copies32_kernel(DevView v) {
   const PClass32& C = v.cls32[P.cls[w]];
   if (v.inst[C.inst].stop) return;
   const double4_32a vv = P.V4[w];
-  const float vx = (float)vv.x, vy = (float)vv.y, vz = (float)vv.z;
-  v.S.V32[w] = make_float4(vx, vy, vz, (float)vv.w);
+  float lx, ly, lz;
+  const float vx = d2f_split(vv.x, &lx), vy = d2f_split(vv.y, &ly), vz = d2f_split(vv.z, &lz);
+  v.S.V32[w] = make_float4(vx, vy, vz, d2f_rn(vv.w));
   // the velocity's low-order part: near-rigid motion (a column settling as one
   // body) makes v_i - v_j far smaller than v, and the pair differences take
   // (hi_i - hi_j) + (lo_i - lo_j), exact to ~2^-48 of |v|
-  v.S.V32LO[w] = make_float4((float)(vv.x - (double)vx), (float)(vv.y - (double)vy), (float)(vv.z - (double)vz), 0.f);
+  v.S.V32LO[w] = make_float4(lx, ly, lz, 0.f);
   const double4_32a d = v.S.D4[w];
-  v.S.D32[w] = make_float4((float)d.x, (float)d.y, (float)d.z, (float)d.w);
+  v.S.D32[w] = make_float4(d2f_rn(d.x), d2f_rn(d.y), d2f_rn(d.z), d2f_rn(d.w));
   sym_store(v.S.SIG32, (size_t)w, P.sigma + 9 * (size_t)w);
   if (v.o.any_ti) sym_store(v.S.TIR32, (size_t)w, P.tir + 9 * (size_t)w);
   if (!(C.flags & CF_FREE)) {
     const double4_32a vb = (v.o.scheme == PSPH_MVERLET) ? P.H4[w] : P.H4b[w];
-    v.S.VB32[w] = make_float4((float)vb.x, (float)vb.y, (float)vb.z, 0.f);
+    v.S.VB32[w] = make_float4(d2f_rn(vb.x), d2f_rn(vb.y), d2f_rn(vb.z), 0.f);
     const double4_32a ns = v.S.nsv4[w];
-    v.S.NSV32[w] = make_float4((float)ns.x, (float)ns.y, (float)ns.z, 0.f);
+    v.S.NSV32[w] = make_float4(d2f_rn(ns.x), d2f_rn(ns.y), d2f_rn(ns.z), 0.f);
   }
 }
 
